@@ -1,0 +1,974 @@
+/*
+ * bruno_oracle.cpp -- CPU restatement of ParBLiSS/bruno's de Bruijn graph-construction
+ * path.  TEST INFRASTRUCTURE ONLY: the parity checker for the CUDA library and the timed
+ * CPU baseline.  The product library never links, loads or calls this file.
+ *
+ * Every step follows the reference file:line cited beside it.  The reference's k-mer,
+ * alphabet, FASTQ-parser and distributed-hash-map layer lives in the un-vendored kmerind
+ * submodule, so the semantics taken from it are restated from their use inside bruno:
+ *   - 2-bit DNA codes A0 C1 G2 T3, first character in the most significant bits, last
+ *     character at the LSBs (debruijn_graph_loader.hpp:87-88, debruijn_chain_operations.hpp:380,
+ *     kmer_traits.hpp:79,86);
+ *   - nextFromChar appends at the 3' end, nextReverseFromChar prepends at the 5' end
+ *     (debruijn_graph_node.hpp:327,344);
+ *   - DNA16 codes A1 C2 G4 T8 N15, gap 0 (debruijn_graph_node.hpp:118-136);
+ *   - k-mer operator< is the lexicographic order of the strings, i.e. the unsigned order of
+ *     the packed words;
+ *   - reads containing N are dropped (compact_dbg_freq_construct_clean.cpp:210-213), and
+ *     reads shorter than the k+2 window give no k-mers (debruijn_biedge_loader.hpp:402,462-505).
+ * The distributed maps become per-shard open-addressing maps, one shard per host thread,
+ * standing in for the reference's MPI ranks: outputs must not depend on the shard count.
+ */
+#include "bruno_oracle.h"
+
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+
+typedef unsigned __int128 u128;
+
+/* ---------------------------------------------------------------- k-mer words */
+
+inline uint64_t rev_pairs(uint64_t x) {
+  x = ((x >> 2) & 0x3333333333333333ULL) | ((x & 0x3333333333333333ULL) << 2);
+  x = ((x >> 4) & 0x0F0F0F0F0F0F0F0FULL) | ((x & 0x0F0F0F0F0F0F0F0FULL) << 4);
+  return __builtin_bswap64(x);
+}
+inline u128 rev_pairs(u128 x) {
+  return ((u128)rev_pairs((uint64_t)x) << 64) | (u128)rev_pairs((uint64_t)(x >> 64));
+}
+inline uint64_t mix64(uint64_t x) {  /* splitmix64 finaliser */
+  x ^= x >> 30; x *= 0xbf58476d1ce4e5b9ULL;
+  x ^= x >> 27; x *= 0x94d049bb133111ebULL;
+  x ^= x >> 31; return x;
+}
+inline uint64_t hash_word(uint64_t x) { return mix64(x); }
+inline uint64_t hash_word(u128 x) { return mix64((uint64_t)x ^ mix64((uint64_t)(x >> 64))); }
+
+/* Operations of bliss::common::Kmer<k, DNA, W> for a runtime k. */
+template <typename W>
+struct KOps {
+  static constexpr int BITS = 8 * sizeof(W);
+  int k;
+  W mask;
+  explicit KOps(int k_) : k(k_) { mask = (2 * k >= BITS) ? ~W(0) : ((W(1) << (2 * k)) - 1); }
+  /* Kmer::reverse_complement: complement = 3 - c = c ^ 3, then reverse character order. */
+  W rc(W x) const { return rev_pairs(W(~x)) >> (BITS - 2 * k); }
+  /* reverse complement of the (k-1)-mer held in the low 2(k-1) bits */
+  W rc_km1(W x) const { return rev_pairs(W(~x)) >> (BITS - 2 * (k - 1)); }
+  unsigned first(W x) const { return (unsigned)(x >> (2 * (k - 1))) & 3u; }  /* getCharsAtPos(k-1) */
+  unsigned last(W x) const { return (unsigned)x & 3u; }                     /* getCharsAtPos(0) */
+  W next_from_char(W x, unsigned c) const { return ((x << 2) | W(c)) & mask; }
+  W next_reverse_from_char(W x, unsigned c) const { return (x >> 2) | (W(c) << (2 * (k - 1))); }
+  std::string ascii(W x) const {
+    static const char A[4] = {'A', 'C', 'G', 'T'};
+    std::string s(k, 'A');
+    for (int i = 0; i < k; ++i) s[k - 1 - i] = A[(unsigned)(x >> (2 * i)) & 3u];
+    return s;
+  }
+};
+
+inline void store_word(uint64_t *dst, uint64_t x, int) { dst[0] = x; }
+inline void store_word(uint64_t *dst, u128 x, int words) {
+  dst[0] = (uint64_t)x;
+  if (words > 1) dst[1] = (uint64_t)(x >> 64);
+}
+
+/* DNA16 nibble <-> DNA code (debruijn_graph_node.hpp:118-136 FROM_DNA16 table). */
+inline unsigned from_dna16(unsigned n) {
+  switch (n) { case 1: return 0; case 2: return 1; case 4: return 2; case 8: return 3; default: return 8; }
+}
+/* DNA16 complement = bit reversal of the nibble (A1<->T8, C2<->G4, N15, gap 0). */
+inline unsigned comp16(unsigned n) {
+  return ((n & 1u) << 3) | ((n & 2u) << 1) | ((n & 4u) >> 1) | ((n & 8u) >> 3);
+}
+/* transform::reverse_complement(compact_simple_biedge) (debruijn_biedge_loader.hpp:708-712):
+ * the 2-character DNA16 k-mer "in out" becomes "comp(out) comp(in)". */
+inline uint8_t rc_biedge(uint8_t e) { return (uint8_t)((comp16(e & 0xFu) << 4) | comp16(e >> 4)); }
+
+inline int char_code(unsigned char c) {
+  switch (c) {
+    case 'A': case 'a': return 0;
+    case 'C': case 'c': return 1;
+    case 'G': case 'g': return 2;
+    case 'T': case 't': return 3;
+    default: return -1;
+  }
+}
+
+/* ------------------------------------------------------- chain distance words */
+/* debruijn_chain_node.hpp:53-80 */
+constexpr uint32_t dist_mask = 0x7FFFFFFFu;
+constexpr uint32_t term_mask = 0x80000000u;
+inline uint32_t get_chain_dist(uint32_t x) { return x & dist_mask; }
+inline bool is_chain_terminal(uint32_t x) { return (x & dist_mask) == 0; }
+inline bool points_to_self(uint32_t x) { return x == term_mask; }
+inline bool points_to_chain_node(uint32_t x) { return (x ^ term_mask) > term_mask; }
+inline uint32_t mark_terminal(uint32_t x) { return x | term_mask; }
+
+/* ---------------------------------------------------------- saturating counts */
+/* debruijn_graph_node.hpp:81-91 */
+inline uint16_t sat_add(uint16_t a, uint16_t b) {
+  uint16_t c = (uint16_t)(a + b);
+  return (c < a) ? (uint16_t)0xFFFF : c;
+}
+inline void sat_incr(uint16_t &t) { t += (t < 0xFFFF); }
+
+/* ----------------------------------------------------- open-addressing map */
+template <typename K, typename V>
+struct OAMap {
+  std::vector<K> keys;
+  std::vector<V> vals;
+  std::vector<uint8_t> state;  /* 0 empty, 1 live, 2 erased */
+  size_t live = 0, used = 0, mask = 0;
+
+  void init(size_t expected) {
+    size_t cap = 16;
+    while (cap < 2 * expected + 16) cap <<= 1;
+    keys.assign(cap, K()); vals.assign(cap, V()); state.assign(cap, 0);
+    mask = cap - 1; live = used = 0;
+  }
+  static uint64_t h(const K &k) { return k.hash(); }
+  void grow() {
+    std::vector<K> ok; std::vector<V> ov; std::vector<uint8_t> os;
+    ok.swap(keys); ov.swap(vals); os.swap(state);
+    init(live * 2 + 16);
+    for (size_t i = 0; i < ok.size(); ++i)
+      if (os[i] == 1) { bool ins; get(ok[i], &ins) = ov[i]; }
+  }
+  V *find(const K &k) {
+    if (keys.empty()) return nullptr;
+    for (size_t i = h(k) & mask;; i = (i + 1) & mask) {
+      if (state[i] == 0) return nullptr;
+      if (state[i] == 1 && keys[i] == k) return &vals[i];
+    }
+  }
+  V &get(const K &k, bool *inserted) {
+    if (keys.empty()) init(16);
+    if (2 * (used + 1) > keys.size()) grow();
+    for (size_t i = h(k) & mask;; i = (i + 1) & mask) {
+      if (state[i] == 0) {
+        state[i] = 1; keys[i] = k; vals[i] = V(); ++live; ++used;
+        *inserted = true; return vals[i];
+      }
+      if (state[i] == 1 && keys[i] == k) { *inserted = false; return vals[i]; }
+    }
+  }
+  void erase_slot(size_t i) { state[i] = 2; --live; }
+};
+
+template <typename W>
+struct KmerKey {
+  W v;
+  bool operator==(const KmerKey &o) const { return v == o.v; }
+  uint64_t hash() const { return hash_word(v); }
+};
+template <typename W>
+struct K2Key {
+  W kmer;
+  uint8_t edge;
+  bool operator==(const K2Key &o) const { return kmer == o.kmer && edge == o.edge; }
+  uint64_t hash() const { return hash_word(kmer) ^ mix64(0x9e3779b97f4a7c15ULL * (edge + 1)); }
+};
+
+struct Node { uint16_t c[9]; };  /* compact_multi_biedge<DNA,uint16>: out ACGT, in ACGT, self */
+
+/* Oracle bookkeeping for one side of a chain node during one list-ranking round: the
+ * side's state at the start of the round, the number of updates it received, and the
+ * update with the largest (distance, terminal mark).  Used to prove that applying the
+ * round's updates in sequence (the reference) equals applying only that largest update
+ * (the CUDA kernels); a side where the two differ is an order-dependent collision. */
+template <typename W>
+struct SideLog {
+  uint32_t round = ~0u, n = 0;
+  W snapK = 0; uint32_t snapD = 0;
+  W bestK = 0; uint32_t bestD = 0;
+};
+
+template <typename W>
+struct ChainNode {               /* simple_biedge<K> (debruijn_chain_node.hpp:49-50) */
+  W inK, outK;
+  uint32_t inD, outD;
+  SideLog<W> log_in, log_out;
+};
+
+/* ------------------------------------------------------------- parallel helper */
+template <typename F>
+void parallel(int T, F f) {
+  if (T == 1) { f(0); return; }
+  std::vector<std::thread> th;
+  for (int t = 0; t < T; ++t) th.emplace_back(f, t);
+  for (auto &x : th) x.join();
+}
+
+double now() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct ReadSpan { size_t off; uint32_t len; };
+
+/* FASTQ record split (kmerind FASTQParser + NFilterSequencesIterator, selected at
+ * compact_dbg_freq_construct_clean.cpp:195-219): records are 4 lines, '@' header,
+ * sequence, '+' separator, quality; EOL characters are not part of the sequence
+ * (NonEOLIter, debruijn_biedge_loader.hpp:408-410); blank lines where a record header is
+ * expected are skipped.  Returns false on malformed input. */
+bool split_fastq(const char *buf, size_t n, std::vector<ReadSpan> &seqs, uint64_t &records) {
+  size_t pos = 0, line = 0;
+  records = 0;
+  while (pos < n) {
+    const char *nl = (const char *)memchr(buf + pos, '\n', n - pos);
+    size_t e = nl ? (size_t)(nl - buf) : n;
+    size_t le = e;
+    if (le > pos && buf[le - 1] == '\r') --le;
+    if ((line & 3) == 0 && le == pos) { pos = e + 1; continue; }  /* blank line between records */
+    switch (line & 3) {
+      case 0: if (buf[pos] != '@') return false; break;
+      case 1: seqs.push_back({pos, (uint32_t)(le - pos)}); break;
+      case 2: if (le == pos || buf[pos] != '+') return false; break;
+      default: ++records; break;
+    }
+    ++line;
+    pos = e + 1;
+  }
+  return (line & 3) == 0;
+}
+
+/* ====================================================================== run */
+template <typename W>
+struct Run {
+  const oracle_cfg cfg;
+  const int T;
+  const KOps<W> ko;
+  oracle_result *res;
+
+  std::vector<OAMap<K2Key<W>, uint32_t>> k2;          /* LocalK2CountMapType per shard */
+  std::vector<OAMap<KmerKey<W>, Node>> nodes;         /* debruijn_graph_map per shard */
+  std::vector<OAMap<KmerKey<W>, ChainNode<W>>> chain; /* debruijn_chain_graph map per shard */
+  std::vector<std::vector<std::pair<K2Key<W>, uint32_t>>> filtered;
+
+  Run(const oracle_cfg &c, oracle_result *r)
+      : cfg(c), T(c.threads > 0 ? c.threads : 1), ko(c.k), res(r) {}
+
+  /* owning shard: the high hash bits, independent of the low bits that pick map slots */
+  int shard(W kmer) const { return (int)((hash_word(kmer) >> 40) % (uint64_t)T); }
+
+  /* lex_less<KMER>::operator()(pair) (debruijn_common.hpp:53-57): keeps the pair when
+   * kmer < rc(kmer), otherwise flips the k-mer and reverse-complements the value. */
+  void canonical(W &kmer, uint8_t &edge) const {
+    W y = ko.rc(kmer);
+    if (!(kmer < y)) { kmer = y; edge = rc_biedge(edge); }
+  }
+
+  /* ---------------------------------------------------------------- palindromes
+   * kmer_traits.hpp:56-88 and debruijn_graph_filters.hpp:57-90.  DNA with odd k has no
+   * k-palindromes; DNA with even k has no (k-1)-palindromes. */
+  bool is_rc_palindrome(W x) const { return (ko.k & 1) ? false : (x == ko.rc(x)); }
+  bool km1_high(W x) const {  /* first k-1 characters form an rc-palindrome */
+    if ((ko.k & 1) == 0) return false;
+    W h = x >> 2;
+    return h == ko.rc_km1(h);
+  }
+  bool km1_low(W x) const {   /* last k-1 characters form an rc-palindrome */
+    if ((ko.k & 1) == 0) return false;
+    W l = x & (ko.mask >> 2);
+    return l == ko.rc_km1(l);
+  }
+  /* is_k1_rc_palindrome(l, k, high): the (k+1)-mer l.K is its own reverse complement */
+  bool k1pal_in(unsigned l, W x, bool high) const {
+    if ((ko.k & 1) == 0) return false;
+    if (ko.last(x) != 3u - l) return false;
+    return high;
+  }
+  /* is_k1_rc_palindrome(k, r, low): the (k+1)-mer K.r is its own reverse complement */
+  bool k1pal_out(W x, unsigned r, bool low) const {
+    if ((ko.k & 1) == 0) return false;
+    if (ko.first(x) != 3u - r) return false;
+    return low;
+  }
+  /* IsKplus1Palindrome (debruijn_graph_filters.hpp:57-90) via is_k1_k1pair_rc_palindrome
+   * (kmer_traits.hpp:108-125). */
+  bool is_kplus1_palindrome(W x, const Node &n) const {
+    if ((ko.k & 1) == 0) return false;
+    bool low = km1_low(x);
+    for (unsigned c = 0; c < 4; ++c)
+      if (n.c[c] > 0 && low && (ko.first(x) == 3u - c || ko.first(x) == c)) return true;
+    bool high = km1_high(x);
+    for (unsigned c = 0; c < 4; ++c)
+      if (n.c[4 + c] > 0 && high && (ko.last(x) == 3u - c || ko.last(x) == c)) return true;
+    return false;
+  }
+  static unsigned in_count(const Node &n) {
+    unsigned d = 0; for (int i = 4; i < 8; ++i) d += n.c[i] > 0; return d;
+  }
+  static unsigned out_count(const Node &n) {
+    unsigned d = 0; for (int i = 0; i < 4; ++i) d += n.c[i] > 0; return d;
+  }
+  /* IsBranchPoint (debruijn_graph_filters.hpp:142-160) */
+  bool is_branch(W x, const Node &n) const {
+    return in_count(n) >= 2 || out_count(n) >= 2 || is_rc_palindrome(x) || is_kplus1_palindrome(x, n);
+  }
+  /* IsChainNode (debruijn_graph_filters.hpp:206-220) */
+  bool is_chain(W x, const Node &n) const {
+    return in_count(n) < 2 && out_count(n) < 2 && !is_rc_palindrome(x) && !is_kplus1_palindrome(x, n);
+  }
+
+  /* compact_multi_biedge<DNA,COUNT>::update(edges, cnt) (debruijn_graph_node.hpp:200-211) */
+  static void node_update(Node &n, uint8_t edges, uint16_t cnt) {
+    unsigned out = from_dna16(edges & 0xFu), in = from_dna16(edges >> 4);
+    if (out < 4) n.c[out] = sat_add(n.c[out], cnt);
+    if (in < 4) n.c[4 + in] = sat_add(n.c[4 + in], cnt);
+    n.c[8] = sat_add(n.c[8], cnt);
+  }
+
+  /* ============================================================ parse + count */
+  /* debruijn_kmer_simple_biedge_parser (debruijn_biedge_loader.hpp:393-623) with
+   * biedge_generating_iterator::operator* (:356-372), then compute_biedge_freqencies
+   * (debruijn_graph_map.hpp:1085-1141): transform_input = lex_less, distribute to the
+   * owning shard, count into a uint32 (non-saturating) k2 counter. */
+  bool parse_and_count(const char *buf, size_t n) {
+    double t0 = now();
+    std::vector<ReadSpan> seqs;
+    uint64_t records = 0;
+    if (!split_fastq(buf, n, seqs, records)) return false;
+    res->n_reads = records;
+    const int k = ko.k;
+    std::vector<std::vector<std::vector<std::pair<W, uint8_t>>>> out(T, std::vector<std::vector<std::pair<W, uint8_t>>>(T));
+    std::vector<uint64_t> used(T, 0), inst(T, 0);
+    parallel(T, [&](int t) {
+      size_t b = seqs.size() * t / T, e = seqs.size() * (t + 1) / T;
+      std::vector<int> codes;
+      for (size_t r = b; r < e; ++r) {
+        const unsigned char *s = (const unsigned char *)buf + seqs[r].off;
+        uint32_t L = seqs[r].len;
+        codes.resize(L);
+        bool ok = true;
+        for (uint32_t i = 0; i < L; ++i) { codes[i] = char_code(s[i]); ok &= codes[i] >= 0; }
+        if (!ok) continue;                          /* NFilterSequencesIterator */
+        if (L < (uint32_t)k + 2) continue;           /* longer_than_window */
+        ++used[t];
+        W km = 0;
+        for (int i = 0; i < k - 1; ++i) km = (km << 2) | W(codes[i]);
+        for (uint32_t p = 0; p + k <= L; ++p) {
+          km = ((km << 2) | W(codes[p + k - 1])) & ko.mask;
+          unsigned in = p > 0 ? (1u << codes[p - 1]) : 0u;
+          unsigned o = (p + k < L) ? (1u << codes[p + k]) : 0u;
+          W ck = km; uint8_t e2 = (uint8_t)((in << 4) | o);
+          canonical(ck, e2);
+          out[t][shard(ck)].emplace_back(ck, e2);
+          ++inst[t];
+        }
+      }
+    });
+    for (int t = 0; t < T; ++t) { res->n_reads_used += used[t]; res->n_instances += inst[t]; }
+    double t1 = now();
+    res->seconds[ORACLE_T_PARSE] = t1 - t0;
+
+    k2.resize(T);
+    parallel(T, [&](int s) {
+      size_t total = 0;
+      for (int t = 0; t < T; ++t) total += out[t][s].size();
+      k2[s].init(total / 4 + 16);
+      for (int t = 0; t < T; ++t) {
+        for (auto &x : out[t][s]) {
+          bool ins;
+          uint32_t &c = k2[s].get(K2Key<W>{x.first, x.second}, &ins);
+          ++c;  /* insert with 1 or increment: no saturation, uint32 (:1120-1132) */
+        }
+        std::vector<std::pair<W, uint8_t>>().swap(out[t][s]);
+      }
+    });
+    res->seconds[ORACLE_T_COUNT_K2] = now() - t1;
+    return true;
+  }
+
+  /* ================================================== filter and insert nodes */
+  /* local_insert_by_freqencies (debruijn_graph_map.hpp:1258-1623) per shard. */
+  void filter_insert() {
+    double t0 = now();
+    nodes.resize(T);
+    filtered.resize(T);
+    std::vector<std::array<uint64_t, 16>> hist(T);
+    parallel(T, [&](int s) {
+      hist[s].fill(0);
+      /* step 2: to_vector (:1268-1270) */
+      std::vector<std::pair<K2Key<W>, uint32_t>> v;
+      v.reserve(k2[s].live);
+      for (size_t i = 0; i < k2[s].keys.size(); ++i)
+        if (k2[s].state[i] == 1) v.emplace_back(k2[s].keys[i], k2[s].vals[i]);
+      /* step 3: sort by k-mer (:1275-1279).  The edge is a secondary key only to make the
+       * oracle's own output order deterministic; every per-block quantity is a sum. */
+      std::sort(v.begin(), v.end(), [](const std::pair<K2Key<W>, uint32_t> &a, const std::pair<K2Key<W>, uint32_t> &b) {
+        return a.first.kmer < b.first.kmer || (a.first.kmer == b.first.kmer && a.first.edge < b.first.edge);
+      });
+      nodes[s].init(v.size() / 2 + 16);
+      std::vector<unsigned char> flag(v.size(), 0);
+      const uint64_t t0_lo = cfg.thresh[0], t0_hi = cfg.thresh[1], t1_lo = cfg.thresh[2],
+                     t1_hi = cfg.thresh[3], t2_lo = cfg.thresh[4], t2_hi = cfg.thresh[5];
+      const uint64_t cnt_max = 0xFFFF;  /* FreqType = uint16 */
+      if (cfg.thresholding) {
+        size_t b = 0;
+        while (b < v.size()) {
+          size_t e = b;
+          W km = v[b].first.kmer;
+          while (e < v.size() && v[e].first.kmer == km) ++e;
+          /* step 4: per-block sums (:1460-1507) */
+          const bool kpal = is_rc_palindrome(km), high = km1_high(km), low = km1_low(km);
+          uint64_t k_f = 0, k1in[4] = {0, 0, 0, 0}, k1out[4] = {0, 0, 0, 0};
+          for (size_t i = b; i < e; ++i) {
+            uint64_t c = v[i].second;
+            uint8_t ed = v[i].first.edge;
+            k_f += c;
+            unsigned ch = ed >> 4;
+            if (ch > 0) {
+              ch = from_dna16(ch);
+              bool split = k1pal_in(ch, km, high) && !kpal;
+              k1in[ch] += split ? ((c + 1) >> 1) : c;
+            }
+            ch = ed & 0xFu;
+            if (ch > 0) {
+              ch = from_dna16(ch);
+              bool split = k1pal_out(km, ch, low) && !kpal;
+              k1out[ch] += split ? ((c + 1) >> 1) : c;
+            }
+          }
+          /* caps (:1401-1407) */
+          k_f = std::min(cnt_max, k_f);
+          for (int c = 0; c < 4; ++c) { k1in[c] = std::min(cnt_max, k1in[c]); k1out[c] = std::min(cnt_max, k1out[c]); }
+          /* step 5: per-entry flags (:1410-1448) */
+          for (size_t i = b; i < e; ++i) {
+            uint64_t cnt = std::min(cnt_max, (uint64_t)v[i].second);
+            unsigned char f = 0;
+            if (cnt < t2_lo || cnt >= t2_hi) f |= 4;
+            if (k_f < t0_lo || k_f >= t0_hi) f |= 8;
+            uint8_t ed = v[i].first.edge;
+            uint64_t k1;
+            switch (ed & 0xF0) {
+              case 0x10: k1 = k1in[0]; break; case 0x20: k1 = k1in[1]; break;
+              case 0x40: k1 = k1in[2]; break; case 0x80: k1 = k1in[3]; break;
+              default: k1 = t1_hi; break;
+            }
+            if (k1 < t1_lo || k1 >= t1_hi) f |= 2;
+            switch (ed & 0x0F) {
+              case 0x01: k1 = k1out[0]; break; case 0x02: k1 = k1out[1]; break;
+              case 0x04: k1 = k1out[2]; break; case 0x08: k1 = k1out[3]; break;
+              default: k1 = t1_hi; break;
+            }
+            if (k1 < t1_lo || k1 >= t1_hi) f |= 1;
+            flag[i] = f;
+          }
+          b = e;
+        }
+      }
+      /* step 6: modify and compact (:1563-1594); flag 1 drops the out edge, 2 the in edge */
+      std::vector<std::pair<K2Key<W>, uint32_t>> kept;
+      kept.reserve(v.size());
+      for (size_t i = 0; i < v.size(); ++i) {
+        unsigned char f = flag[i];
+        ++hist[s][f];
+        if (f < 3) {
+          auto x = v[i];
+          if (f == 1) x.first.edge &= 0xF0;
+          if (f == 2) x.first.edge &= 0x0F;
+          kept.push_back(x);
+        }
+      }
+      /* step 7: local_insert, frequency overload (:256-285): cap at FreqType max */
+      for (auto &x : kept) {
+        if (x.second == 0) continue;
+        bool ins;
+        Node &nd = nodes[s].get(KmerKey<W>{x.first.kmer}, &ins);
+        node_update(nd, x.first.edge, (uint16_t)std::min<uint64_t>(cnt_max, x.second));
+      }
+      if (cfg.keep_filtered) filtered[s].swap(kept);
+      if (!cfg.keep_k2) { OAMap<K2Key<W>, uint32_t> e2; std::swap(e2, k2[s]); }
+    });
+    for (int s = 0; s < T; ++s)
+      for (int f = 0; f < 16; ++f) res->filter_flag_hist[f] += hist[s][f];
+    res->seconds[ORACLE_T_FILTER_INSERT] = now() - t0;
+  }
+
+  /* =========================================================== chain extraction */
+  /* debruijn_chain_graph::extract_chains (debruijn_chain_graph.hpp:604-667) with
+   * to_simple_biedge (debruijn_chain_node.hpp:83-111), then setup_chain_termini (:485-596)
+   * applying terminus_update (debruijn_chain_operations.hpp:57-93) through lex_less. */
+  void extract_chains() {
+    double t0 = now();
+    chain.resize(T);
+    std::vector<uint64_t> nb(T, 0), nc(T, 0);
+    parallel(T, [&](int s) {
+      chain[s].init(nodes[s].live / 2 + 16);
+      for (size_t i = 0; i < nodes[s].keys.size(); ++i) {
+        if (nodes[s].state[i] != 1) continue;
+        W x = nodes[s].keys[i].v;
+        const Node &n = nodes[s].vals[i];
+        if (is_branch(x, n)) ++nb[s];
+        if (!is_chain(x, n)) continue;
+        ChainNode<W> cn{W(0), W(0), term_mask, term_mask, SideLog<W>(), SideLog<W>()};
+        for (unsigned c = 0; c < 4; ++c)
+          if (n.c[4 + c] > 0) { cn.inK = ko.next_reverse_from_char(x, c); cn.inD = 1; }
+        for (unsigned c = 0; c < 4; ++c)
+          if (n.c[c] > 0) { cn.outK = ko.next_from_char(x, c); cn.outD = 1; }
+        bool ins;
+        chain[s].get(KmerKey<W>{x}, &ins) = cn;
+        ++nc[s];
+      }
+    });
+    for (int s = 0; s < T; ++s) { res->n_branch += nb[s]; res->n_chain_nodes += nc[s]; }
+    /* terminus updates: (neighbour, (branch, IN)) for out-neighbours, (neighbour, (branch,
+     * OUT)) for in-neighbours; lex_less flips k-mer and orientation for non-canonical keys
+     * (debruijn_chain_operations.hpp:494-497). */
+    std::vector<std::vector<std::vector<std::pair<W, int>>>> upd(T, std::vector<std::vector<std::pair<W, int>>>(T));
+    parallel(T, [&](int s) {
+      for (size_t i = 0; i < nodes[s].keys.size(); ++i) {
+        if (nodes[s].state[i] != 1) continue;
+        W x = nodes[s].keys[i].v;
+        const Node &n = nodes[s].vals[i];
+        if (!is_branch(x, n)) continue;
+        for (unsigned c = 0; c < 4; ++c) if (n.c[c] > 0) {
+          W nbk = ko.next_from_char(x, c); int o = -1;      /* OUT neighbour gets IN */
+          W y = ko.rc(nbk); if (!(nbk < y)) { nbk = y; o = -o; }
+          upd[s][shard(nbk)].emplace_back(nbk, o);
+        }
+        for (unsigned c = 0; c < 4; ++c) if (n.c[4 + c] > 0) {
+          W nbk = ko.next_reverse_from_char(x, c); int o = 1; /* IN neighbour gets OUT */
+          W y = ko.rc(nbk); if (!(nbk < y)) { nbk = y; o = -o; }
+          upd[s][shard(nbk)].emplace_back(nbk, o);
+        }
+      }
+    });
+    parallel(T, [&](int d) {
+      for (int s = 0; s < T; ++s)
+        for (auto &u : upd[s][d]) {
+          ChainNode<W> *cn = chain[d].find(KmerKey<W>{u.first});
+          if (!cn) continue;                 /* update only existing chain nodes */
+          if (u.second < 0) cn->inD = 0; else cn->outD = 0;   /* branch_neighbor */
+        }
+    });
+    res->seconds[ORACLE_T_CHAINMAP] = now() - t0;
+  }
+
+  /* ================================================================ list ranking */
+  struct Update { W key; W kmer; uint32_t dist; int orient; };
+
+  /* PointsToInternalNode (debruijn_chain_filters.hpp:169-186) */
+  static bool unfinished(const ChainNode<W> &c) {
+    return points_to_chain_node(c.inD) || points_to_chain_node(c.outD);
+  }
+  /* IsCycleNode (debruijn_chain_filters.hpp:189-213) */
+  static bool is_cycle(const ChainNode<W> &c, uint32_t maxd) {
+    return get_chain_dist(c.inD) == maxd && get_chain_dist(c.outD) == maxd;
+  }
+
+  /* order of updates in the max reduction: distance first, then the terminal mark */
+  static uint64_t update_rank(uint32_t dword) {
+    return ((uint64_t)get_chain_dist(dword) << 1) | (dword >> 31);
+  }
+
+  /* chain_update (debruijn_chain_operations.hpp:107-256), applied after lex_less has put
+   * the update on the key's canonical strand. */
+  static size_t chain_update(ChainNode<W> &x, const Update &y) {
+    uint32_t dist = get_chain_dist(y.dist);
+    if (y.orient < 0) {
+      if (points_to_chain_node(x.inD)) {
+        uint32_t dx = get_chain_dist(x.inD);
+        if (dist > dx) x.inK = y.kmer;
+        if (dist >= dx) { x.inD = y.dist; return 1; }
+      }
+    } else {
+      if (points_to_chain_node(x.outD)) {
+        uint32_t dx = get_chain_dist(x.outD);
+        if (dist > dx) x.outK = y.kmer;
+        if (dist >= dx) { x.outD = y.dist; return 1; }
+      }
+    }
+    return 0;
+  }
+
+  /* list_rank_min_update (debruijn_chain_graph.hpp:1040-1310) when cfg.min_update,
+   * list_rank (:793-994) otherwise.  Round-synchronous: every update of a round is made
+   * from the state at the start of the round, then all are applied. */
+  void list_rank() {
+    double t0 = now();
+    std::vector<std::vector<W>> unf(T);
+    parallel(T, [&](int s) {
+      for (size_t i = 0; i < chain[s].keys.size(); ++i)
+        if (chain[s].state[i] == 1 && unfinished(chain[s].vals[i])) unf[s].push_back(chain[s].keys[i].v);
+      std::sort(unf[s].begin(), unf[s].end());
+    });
+    size_t total_unf = 0;
+    for (int s = 0; s < T; ++s) total_unf += unf[s].size();
+    bool all_compacted = total_unf == 0;
+    uint64_t iterations = 0;
+    std::vector<std::vector<std::vector<Update>>> upd(T, std::vector<std::vector<Update>>(T));
+    std::vector<uint64_t> cnt(T), cyc(T), col(T), left(T);
+    while (!all_compacted) {
+      const uint32_t round = (uint32_t)iterations;
+      parallel(T, [&](int s) {
+        for (int d = 0; d < T; ++d) upd[s][d].clear();
+        for (W km : unf[s]) {
+          const ChainNode<W> md = *chain[s].find(KmerKey<W>{km});
+          uint32_t ldist = md.inD, rdist = md.outD;
+          uint32_t dist = get_chain_dist(ldist) + get_chain_dist(rdist);
+          bool send_l = cfg.min_update ? points_to_chain_node(ldist) : !is_chain_terminal(ldist);
+          bool send_r = cfg.min_update ? points_to_chain_node(rdist) : !is_chain_terminal(rdist);
+          if (send_l) {   /* send rr to ll, orientation OUT */
+            Update u{md.inK, is_chain_terminal(rdist) ? km : md.outK,
+                     points_to_chain_node(rdist) ? dist : mark_terminal(dist), 1};
+            W y = ko.rc(u.key);
+            if (!(u.key < y)) { u.key = y; u.kmer = ko.rc(u.kmer); u.orient = -u.orient; }
+            upd[s][shard(u.key)].push_back(u);
+          }
+          if (send_r) {   /* send ll to rr, orientation IN */
+            Update u{md.outK, is_chain_terminal(ldist) ? km : md.inK,
+                     points_to_chain_node(ldist) ? dist : mark_terminal(dist), -1};
+            W y = ko.rc(u.key);
+            if (!(u.key < y)) { u.key = y; u.kmer = ko.rc(u.kmer); u.orient = -u.orient; }
+            upd[s][shard(u.key)].push_back(u);
+          }
+        }
+      });
+      parallel(T, [&](int d) {
+        uint64_t c = 0, cl = 0;
+        std::vector<std::pair<ChainNode<W> *, int>> multi;
+        for (int s = 0; s < T; ++s)
+          for (const Update &u : upd[s][d]) {
+            ChainNode<W> *x = chain[d].find(KmerKey<W>{u.key});
+            if (!x) continue;                  /* updates to absent keys are dropped */
+            SideLog<W> &lg = u.orient < 0 ? x->log_in : x->log_out;
+            if (lg.round != round) {
+              lg.round = round; lg.n = 0;
+              lg.snapK = u.orient < 0 ? x->inK : x->outK;
+              lg.snapD = u.orient < 0 ? x->inD : x->outD;
+              lg.bestK = u.kmer; lg.bestD = u.dist;
+            } else if (update_rank(u.dist) > update_rank(lg.bestD)) {
+              lg.bestK = u.kmer; lg.bestD = u.dist;
+            }
+            if (++lg.n == 2) multi.emplace_back(x, u.orient);
+            c += chain_update(*x, u);
+          }
+        for (auto &m : multi) {
+          ChainNode<W> tmp = *m.first;
+          const SideLog<W> &lg = m.second < 0 ? tmp.log_in : tmp.log_out;
+          if (m.second < 0) { tmp.inK = lg.snapK; tmp.inD = lg.snapD; }
+          else { tmp.outK = lg.snapK; tmp.outD = lg.snapD; }
+          chain_update(tmp, Update{W(0), lg.bestK, lg.bestD, m.second});
+          bool same = m.second < 0 ? (tmp.inK == m.first->inK && tmp.inD == m.first->inD)
+                                   : (tmp.outK == m.first->outK && tmp.outD == m.first->outD);
+          if (!same) ++cl;
+        }
+        cnt[d] = c; col[d] = cl;
+      });
+      ++iterations;
+      const uint32_t maxd = 0x1u << iterations;
+      parallel(T, [&](int s) {
+        std::vector<W> keep;
+        uint64_t cy = 0;
+        for (W km : unf[s]) {
+          const ChainNode<W> &x = *chain[s].find(KmerKey<W>{km});
+          if (unfinished(x)) { keep.push_back(km); cy += is_cycle(x, maxd); }
+        }
+        unf[s].swap(keep);
+        cyc[s] = cy; left[s] = unf[s].size();
+      });
+      uint64_t count = 0, cycles = 0, remaining = 0;
+      for (int s = 0; s < T; ++s) { count += cnt[s]; cycles += cyc[s]; remaining += left[s]; res->collisions += col[s]; }
+      if (iterations >= 30) all_compacted = true;
+      else all_compacted = (count == 0) || (cycles == remaining);
+    }
+    res->iterations = iterations;
+
+    /* separate_cycles(iterations) when anything is still unfinished (:1283-1292, :670-705),
+     * then separate_isolated (:744-777). */
+    bool any_unfinished = false;
+    for (int s = 0; s < T; ++s)
+      for (size_t i = 0; i < chain[s].keys.size(); ++i)
+        if (chain[s].state[i] == 1 && unfinished(chain[s].vals[i])) any_unfinished = true;
+    std::vector<uint64_t> ncy(T, 0), niso(T, 0);
+    const uint32_t maxd = 0x1u << iterations;
+    parallel(T, [&](int s) {
+      for (size_t i = 0; i < chain[s].keys.size(); ++i) {
+        if (chain[s].state[i] != 1) continue;
+        if (any_unfinished && is_cycle(chain[s].vals[i], maxd)) { chain[s].erase_slot(i); ++ncy[s]; }
+      }
+      for (size_t i = 0; i < chain[s].keys.size(); ++i) {
+        if (chain[s].state[i] != 1) continue;
+        const ChainNode<W> &x = chain[s].vals[i];
+        if (points_to_self(x.inD) && points_to_self(x.outD)) { chain[s].erase_slot(i); ++niso[s]; }
+      }
+    });
+    for (int s = 0; s < T; ++s) { res->n_cycle_nodes += ncy[s]; res->n_isolated += niso[s]; }
+    res->seconds[ORACLE_T_LIST_RANK] = now() - t0;
+  }
+
+  /* ============================================================== emission */
+  struct Ranked { W K, rep; int32_t dist; };
+
+  /* to_ranked_chain_nodes (debruijn_chain_graph.hpp:1760-1773) with to_listranked_chain_node
+   * (debruijn_chain_operations.hpp:260-309); to_compressed_chains (:1778-1856) groups by
+   * rep after sorting with chain_rep_less (:332-340) and prints each group with
+   * print_chain_as_fasta(chain_only) (:359-384). */
+  void emit() {
+    double t0 = now();
+    std::vector<Ranked> rk;
+    for (int s = 0; s < T; ++s)
+      for (size_t i = 0; i < chain[s].keys.size(); ++i) {
+        if (chain[s].state[i] != 1) continue;
+        W key = chain[s].keys[i].v;
+        const ChainNode<W> &x = chain[s].vals[i];
+        W L = is_chain_terminal(x.inD) ? key : x.inK;
+        W R = is_chain_terminal(x.outD) ? ko.rc(key) : ko.rc(x.outK);
+        bool sense = L <= R;
+        rk.push_back({sense ? key : ko.rc(key), sense ? L : R,
+                      (int32_t)(sense ? get_chain_dist(x.inD) : get_chain_dist(x.outD))});
+      }
+    std::vector<Ranked> byrep(rk);
+    std::sort(byrep.begin(), byrep.end(), [](const Ranked &a, const Ranked &b) {
+      if (a.rep != b.rep) return a.rep < b.rep;
+      if (std::abs(a.dist) != std::abs(b.dist)) return std::abs(a.dist) < std::abs(b.dist);
+      return a.K < b.K;
+    });
+    std::string chars;
+    std::vector<W> reps;
+    std::vector<uint64_t> offs;
+    for (size_t i = 0; i < byrep.size(); ++i) {
+      if (i == 0 || byrep[i].rep != byrep[i - 1].rep) { reps.push_back(byrep[i].rep); offs.push_back(chars.size()); }
+      if (byrep[i].dist == 0) chars += ko.ascii(byrep[i].rep);
+      else chars += "ACGT"[ko.last(byrep[i].K)];
+    }
+    offs.push_back(chars.size());
+    std::sort(rk.begin(), rk.end(), [](const Ranked &a, const Ranked &b) { return a.K < b.K; });
+
+    const int w = res->words;
+    res->n_ranked = rk.size();
+    res->ranked_K = (uint64_t *)calloc(rk.size() * w + 1, 8);
+    res->ranked_rep = (uint64_t *)calloc(rk.size() * w + 1, 8);
+    res->ranked_dist = (int32_t *)calloc(rk.size() + 1, 4);
+    for (size_t i = 0; i < rk.size(); ++i) {
+      store_word(res->ranked_K + i * w, rk[i].K, w);
+      store_word(res->ranked_rep + i * w, rk[i].rep, w);
+      res->ranked_dist[i] = rk[i].dist;
+    }
+    res->n_chains = reps.size();
+    res->chain_rep = (uint64_t *)calloc(reps.size() * w + 1, 8);
+    res->chain_offsets = (uint64_t *)calloc(offs.size() + 1, 8);
+    res->chain_chars = (char *)malloc(chars.size() + 1);
+    for (size_t i = 0; i < reps.size(); ++i) store_word(res->chain_rep + i * w, reps[i], w);
+    for (size_t i = 0; i < offs.size(); ++i) res->chain_offsets[i] = offs[i];
+    memcpy(res->chain_chars, chars.data(), chars.size());
+    res->chain_chars[chars.size()] = 0;
+    res->seconds[ORACLE_T_COMPRESS] = now() - t0;
+  }
+
+  /* ====================================================== table outputs */
+  void export_tables() {
+    const int w = res->words;
+    if (cfg.keep_k2) {
+      std::vector<std::pair<K2Key<W>, uint32_t>> v;
+      for (int s = 0; s < T; ++s)
+        for (size_t i = 0; i < k2[s].keys.size(); ++i)
+          if (k2[s].state[i] == 1) v.emplace_back(k2[s].keys[i], k2[s].vals[i]);
+      export_k2(v, &res->n_k2, &res->k2_keys, &res->k2_edges, &res->k2_counts, w);
+    }
+    if (cfg.keep_filtered) {
+      std::vector<std::pair<K2Key<W>, uint32_t>> v;
+      for (int s = 0; s < T; ++s) v.insert(v.end(), filtered[s].begin(), filtered[s].end());
+      export_k2(v, &res->n_filtered, &res->filt_keys, &res->filt_edges, &res->filt_counts, w);
+    }
+    std::vector<std::pair<W, Node>> nv;
+    for (int s = 0; s < T; ++s)
+      for (size_t i = 0; i < nodes[s].keys.size(); ++i)
+        if (nodes[s].state[i] == 1) nv.emplace_back(nodes[s].keys[i].v, nodes[s].vals[i]);
+    std::sort(nv.begin(), nv.end(), [](const std::pair<W, Node> &a, const std::pair<W, Node> &b) { return a.first < b.first; });
+    res->n_nodes = nv.size();
+    res->node_keys = (uint64_t *)calloc(nv.size() * w + 1, 8);
+    res->node_counts = (uint16_t *)calloc(nv.size() * 9 + 1, 2);
+    res->node_flags = (uint8_t *)calloc(nv.size() + 1, 1);
+    for (size_t i = 0; i < nv.size(); ++i) {
+      store_word(res->node_keys + i * w, nv[i].first, w);
+      memcpy(res->node_counts + i * 9, nv[i].second.c, 18);
+      res->node_flags[i] = (uint8_t)((is_branch(nv[i].first, nv[i].second) ? 1 : 0) |
+                                     (is_chain(nv[i].first, nv[i].second) ? 2 : 0));
+    }
+  }
+  static void export_k2(std::vector<std::pair<K2Key<W>, uint32_t>> &v, uint64_t *n, uint64_t **keys,
+                        uint8_t **edges, uint32_t **counts, int w) {
+    std::sort(v.begin(), v.end(), [](const std::pair<K2Key<W>, uint32_t> &a, const std::pair<K2Key<W>, uint32_t> &b) {
+      return a.first.kmer < b.first.kmer || (a.first.kmer == b.first.kmer && a.first.edge < b.first.edge);
+    });
+    *n = v.size();
+    *keys = (uint64_t *)calloc(v.size() * w + 1, 8);
+    *edges = (uint8_t *)calloc(v.size() + 1, 1);
+    *counts = (uint32_t *)calloc(v.size() + 1, 4);
+    for (size_t i = 0; i < v.size(); ++i) {
+      store_word(*keys + i * w, v[i].first.kmer, w);
+      (*edges)[i] = v[i].first.edge;
+      (*counts)[i] = v[i].second;
+    }
+  }
+
+  int run(const char *buf, size_t n) {
+    if (!parse_and_count(buf, n)) { res->status = 2; return 2; }
+    /* Unthresholded build_index (compact_dbg_build.hpp:34-62) updates each node once per
+     * parsed pair with sat_incr (local_insert, debruijn_graph_map.hpp:175-197, update
+     * :187-198).  A sum of saturating increments equals the saturating add of the pair's
+     * count, so the same insert step serves both builds; it just sets no flags. */
+    filter_insert();
+    extract_chains();
+    list_rank();
+    emit();
+    export_tables();
+    return 0;
+  }
+};
+
+template <typename W>
+int run_typed(const char *buf, size_t n, const oracle_cfg &cfg, oracle_result *r) {
+  Run<W> run(cfg, r);
+  return run.run(buf, n);
+}
+
+/* ---------------------------------------------------------------- text output */
+std::string ascii_words(const uint64_t *p, int k, int words) {
+  static const char A[4] = {'A', 'C', 'G', 'T'};
+  std::string s(k, 'A');
+  for (int i = 0; i < k; ++i) {
+    int bit = 2 * i;
+    uint64_t w = (words == 1 || bit < 64) ? p[0] : p[1];
+    s[k - 1 - i] = A[(w >> (bit & 63)) & 3u];
+  }
+  return s;
+}
+
+}  // namespace
+
+extern "C" int oracle_run(const char *fastq, size_t nbytes, const oracle_cfg *cfg, oracle_result **out) {
+  if (!cfg || !out || cfg->k < 3 || cfg->k > 63) return 1;
+  oracle_result *r = (oracle_result *)calloc(1, sizeof(oracle_result));
+  r->words = cfg->k <= 32 ? 1 : 2;
+  oracle_cfg c = *cfg;
+  if (!c.thresholding) {
+    /* build_index: no flags (every entry kept with both edges) */
+    c.thresh[0] = c.thresh[2] = c.thresh[4] = 0;
+    c.thresh[1] = c.thresh[3] = c.thresh[5] = ~0ULL;
+  }
+  int rc = (cfg->k <= 32) ? run_typed<uint64_t>(fastq, nbytes, c, r) : run_typed<u128>(fastq, nbytes, c, r);
+  r->status = rc;
+  *out = r;
+  return rc;
+}
+
+extern "C" void oracle_free(oracle_result *r) {
+  if (!r) return;
+  free(r->k2_keys); free(r->k2_edges); free(r->k2_counts);
+  free(r->filt_keys); free(r->filt_edges); free(r->filt_counts);
+  free(r->node_keys); free(r->node_counts); free(r->node_flags);
+  free(r->ranked_K); free(r->ranked_rep); free(r->ranked_dist);
+  free(r->chain_rep); free(r->chain_offsets); free(r->chain_chars);
+  free(r);
+}
+
+extern "C" int oracle_write_outputs(const oracle_result *r, int32_t k, const char *prefix, int32_t benchmark) {
+  if (!r || r->status != 0) return 1;
+  const int w = r->words;
+  std::string p(prefix);
+  auto canon = [&](const uint64_t *x) {
+    /* lex_less on a k-mer word: min(x, rc(x)) */
+    if (w == 1) { KOps<uint64_t> ko(k); uint64_t v = x[0], y = ko.rc(v); return v < y ? v : y; }
+    return (uint64_t)0;
+  };
+  auto canon128 = [&](const uint64_t *x) {
+    KOps<u128> ko(k); u128 v = ((u128)(w > 1 ? x[1] : 0) << 64) | x[0], y = ko.rc(v); return v < y ? v : y;
+  };
+  auto canon_ascii = [&](const uint64_t *x) {
+    if (w == 1) { uint64_t c = canon(x); return ascii_words(&c, k, 1); }
+    u128 c = canon128(x); uint64_t q[2] = {(uint64_t)c, (uint64_t)(c >> 64)}; return ascii_words(q, k, 2);
+  };
+  auto is_canon = [&](const uint64_t *x) {
+    if (w == 1) return canon(x) == x[0];
+    u128 c = canon128(x); return (uint64_t)c == x[0] && (uint64_t)(c >> 64) == x[1];
+  };
+  auto less_words = [&](const uint64_t *a, const uint64_t *b) {
+    if (w == 2 && a[1] != b[1]) return a[1] < b[1];
+    return a[0] < b[0];
+  };
+  /* .chain.fasta: print_chain_string (compact_dbg_io.hpp:323-363), sorted by chain_rep_less;
+   * the leading newline of the first record is dropped. */
+  {
+    std::vector<size_t> idx(r->n_ranked);
+    for (size_t i = 0; i < idx.size(); ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](size_t a, size_t b) {
+      const uint64_t *ra = r->ranked_rep + a * w, *rb = r->ranked_rep + b * w;
+      if (less_words(ra, rb)) return true;
+      if (less_words(rb, ra)) return false;
+      int da = std::abs(r->ranked_dist[a]), db = std::abs(r->ranked_dist[b]);
+      if (da != db) return da < db;
+      return less_words(r->ranked_K + a * w, r->ranked_K + b * w);
+    });
+    std::string s;
+    for (size_t i : idx) {
+      if (r->ranked_dist[i] == 0) {
+        s += "\n>"; s += canon_ascii(r->ranked_K + i * w); s += "\n";
+        s += ascii_words(r->ranked_rep + i * w, k, w);
+      } else {
+        s += ascii_words(r->ranked_K + i * w, k, w).back();
+      }
+    }
+    FILE *f = fopen((p + ".chain.fasta").c_str(), "wb");
+    if (!f) return 1;
+    if (!s.empty()) fwrite(s.data() + 1, 1, s.size() - 1, f);
+    fclose(f);
+  }
+  /* .chain.components: print_chain_nodes (compact_dbg_io.hpp:463-498) sorted by K,
+   * print_chain_node (debruijn_chain_operations.hpp:434-441). */
+  if (!benchmark) {
+    std::string s;
+    for (size_t i = 0; i < r->n_ranked; ++i) {
+      const uint64_t *K = r->ranked_K + i * w;
+      s += canon_ascii(K); s += "\t"; s += ascii_words(r->ranked_rep + i * w, k, w); s += "\t";
+      s += std::to_string(r->ranked_dist[i]); s += "\t"; s += is_canon(K) ? "1" : "0"; s += "\n";
+    }
+    FILE *f = fopen((p + ".chain.components").c_str(), "wb");
+    if (!f) return 1;
+    fwrite(s.data(), 1, s.size(), f);
+    fclose(f);
+  }
+  /* .branch.fasta (compact_dbg_io.hpp:254-299), .branch.edges (compact_dbg_stats.hpp:219-262)
+   * and .graph.all, all sorted by k-mer; node lines follow print_graph_node
+   * (debruijn_graph_operations.hpp:57-78): k-mer, in A C G T, out A C G T, self. */
+  {
+    std::string fa, be, ga;
+    for (size_t i = 0; i < r->n_nodes; ++i) {
+      const uint64_t *x = r->node_keys + i * w;
+      const uint16_t *c = r->node_counts + i * 9;
+      std::string a = ascii_words(x, k, w);
+      bool br = (r->node_flags[i] & 1) != 0;
+      std::string line = a;
+      for (int j = 4; j < 8; ++j) line += "\t" + std::to_string(c[j]);
+      for (int j = 0; j < 4; ++j) line += "\t" + std::to_string(c[j]);
+      line += "\t" + std::to_string(c[8]) + "\n";
+      if (br) { fa += ">" + a + "\n" + a + "\n"; be += line; }
+      ga += line;
+    }
+    FILE *f = fopen((p + ".branch.fasta").c_str(), "wb");
+    if (!f) return 1;
+    fwrite(fa.data(), 1, fa.size(), f); fclose(f);
+    if (!benchmark) {
+      f = fopen((p + ".branch.edges").c_str(), "wb");
+      if (!f) return 1;
+      fwrite(be.data(), 1, be.size(), f); fclose(f);
+      f = fopen((p + ".graph.all").c_str(), "wb");
+      if (!f) return 1;
+      fwrite(ga.data(), 1, ga.size(), f); fclose(f);
+    }
+  }
+  return 0;
+}
