@@ -1,0 +1,287 @@
+#!/usr/bin/env python3
+"""Benchmark: k-mers/s of the plain build+compact path on the plain-scale workload.
+
+One step = one pass of the whole path -- FASTQ parse, (k+2)-mer counting, frequency filter
+and node insert, chain extraction, list ranking (list_rank_min_update) and compacted-chain
+emission -- over the 50 Mbp / 30x / 150 bp / k=31 / -L 3 synthetic workload.
+
+  value   k-mers/s with the FASTQ already resident in HBM (CUDA events on the library's
+          stream, which is torch's current stream).
+  e2e     the same through the C ABI with pinned host buffers: the FASTQ host->device copy
+          and the device->host read of the compacted chains are inside the timed region.
+  roofline  the dominant kernel (k_count) against the measured HBM copy bandwidth.
+  cpu_baseline  the CPU oracle (a restatement of the reference's CPU path) on a bounded
+          sample of the same workload, with every host thread.
+
+--impl reference runs the CPU path instead and prints the same line with "impl":
+"reference".  Multi-GPU runs are independent replicas (the path is one graph per GPU).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC, UNIT = "k-mers/s build+compact", "k-mers/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="plain-scale")
+    ap.add_argument("--cpu-sample", type=float, default=0.01, help="fraction of reads in the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, copy burst)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s"
+
+
+def workload_config(w, mu=True):
+    return {"workload": f"{w.name}: {w.genome_len / 1e6:g} Mbp genome"
+                        + (f" + {w.repeat_frac * 100:g}% repeats ({w.rep_len[0]}-{w.rep_len[1]} bp, "
+                           f"{w.rep_copies[0]}-{w.rep_copies[1]} copies, {w.rep_div[0] * 100:g}-{w.rep_div[1] * 100:g}% "
+                           f"divergence)" if w.repeat_frac else "")
+                        + f", {w.n_reads} x {w.read_len} bp reads ({w.coverage:.0f}x), {w.sub_rate * 100:g}% "
+                          f"substitutions, k={w.k}, -T -L {w.lower[0]}, "
+                        + ("list_rank_min_update" if mu else "list_rank"),
+            "genome_bp": w.genome_len, "reads": w.n_reads, "read_len": w.read_len, "k": w.k,
+            "threshold_k1_lower": w.lower[0], "seed": w.seed,
+            "l2": "inputs larger than L2 (FASTQ and k-mer table are GBs; no flush needed)"}
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region"""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(w, frac, threads):
+    """the oracle on the first `frac` of the workload's reads, all host threads"""
+    from bruno_gb300 import synth, thresholds
+    from oracle import oracle
+    ws = w.scaled(frac)
+    fq = synth.make_fastq(ws)
+    t0 = time.perf_counter()
+    r = oracle.run(fq, k=w.k, thresh=thresholds(w.lower), min_update=True, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": r["n_instances"] / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {ws.n_reads} of {w.n_reads} reads ({frac * 100:g}%), {r['n_instances']} k-mers, "
+                      f"{dt:.2f} s", "seconds": dt, "instances": r["n_instances"]}
+
+
+def run_reference(args, w):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sample = max(args.cpu_sample, 1e-4)
+    for _ in range(args.warmup):
+        cpu_baseline(w, sample, threads)
+    vals, secs = [], []
+    for _ in range(args.steps):
+        b = cpu_baseline(w, sample, threads)
+        vals.append(b["value"])
+        secs.append(b["seconds"])
+    value = statistics.mean(vals)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(secs), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded generator)",
+            "config": workload_config(w), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": b["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    from bruno_gb300 import synth
+    w = synth.WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, w)
+        return
+    import torch
+    import bruno_gb300 as bg
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream()
+
+    # workload in pinned host memory, and a device-resident copy
+    n = synth.fastq_size(w)
+    host = bg.PinnedBuffer(n)
+    synth.make_fastq(w, out=host.array)
+    dev = torch.empty(n, dtype=torch.uint8, device="cuda")
+    dev.copy_(torch.from_numpy(host.array[:n]), non_blocking=False)
+    torch.cuda.synchronize()
+
+    g = bg.Graph(k=w.k, thresh=bg.thresholds(w.lower), min_update=True, device=local)
+    g.set_stream(stream.cuda_stream)
+
+    def step_device():
+        g.build_and_compact(dev.data_ptr(), nbytes=n, is_device=True)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step_device()
+    sizes = g.sizes()
+    barrier()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kms, launches = [], 0
+    with ClockSampler(local) as clk:
+        start.record(stream)
+        for _ in range(args.steps):
+            step_device()
+            kms.append(g.phase_ms())
+            launches += g.sizes()["launches"]
+        end.record(stream)
+        barrier()
+    ms = start.elapsed_time(end)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    inst_step = sizes["n_instances"]
+    value = inst_step * args.steps * world / (ms / 1e3)
+
+    # end to end through the C ABI: host FASTQ in, compacted chains out
+    nc, nch = sizes["n_chains"], sizes["n_chain_chars"]
+    out_chars = bg.PinnedBuffer(max(1, nch))
+    out_offs = bg.PinnedBuffer(8 * (nc + 1))
+    out_reps = bg.PinnedBuffer(8 * g.words * max(1, nc))
+    import ctypes
+
+    def step_e2e():
+        g.build_and_compact(host.array[:n])
+        ncs, nchs = ctypes.c_size_t(), ctypes.c_size_t()
+        g._check(g.lib.bruno_copy_chains(g.ctx, ctypes.c_void_p(out_reps.ptr), ctypes.c_void_p(out_offs.ptr),
+                                         ctypes.c_void_p(out_chars.ptr), nc, max(1, nch), ctypes.byref(ncs),
+                                         ctypes.byref(nchs)), "copy_chains")
+    step_e2e()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step_e2e()
+    e1.record(stream)
+    barrier()
+    ems = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ems], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ems = float(t.item())
+    e2e_value = inst_step * args.steps * world / (ems / 1e3)
+    d2h = nch + 8 * (nc + 1) + 8 * g.words * nc
+
+    # roofline of the dominant kernel, k_count: algorithmic bytes per launch = the read
+    # sequence bytes + 16 B of read span per read + one 32 B sector read and one 32 B
+    # write-back per (k-mer, biedge) instance
+    k_count_ms = statistics.mean(p["k_count"] for p in kms)
+    alg_bytes = sizes["n_reads"] * w.read_len + 16 * sizes["n_reads"] + 64 * inst_step
+    peak, peak_src = measured_peak()
+    achieved = alg_bytes / (k_count_ms / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "k_count_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tj = json.load(f)
+        traffic = tj.get("bytes_per_instance", 0) * inst_step if tj.get("bytes_per_instance") else None
+    phases = {k: round(statistics.mean(p[k] for p in kms), 3) for k in kms[0]}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded generator, " + w.name + ")",
+                "config": workload_config(w),
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n, "d2h_bytes_per_step": d2h,
+                        "ms_per_step": ems / args.steps},
+                "roofline": {"bound": "hbm", "kernel": "k_count", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+                             "alg_bytes_per_launch": alg_bytes, "launch_ms": k_count_ms},
+                "gpu_launches": launches, "clocks": clk.summary(), "phase_ms": phases,
+                "sizes": {k: sizes[k] for k in ("n_reads", "n_instances", "n_k2", "n_nodes", "n_branch",
+                                                "n_chain_nodes", "iterations", "n_chains", "table_slots")}}
+        if not args.no_cpu_baseline:
+            b = cpu_baseline(w, args.cpu_sample, os.cpu_count() or 1)
+            line["cpu_baseline"] = {k: b[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        print(json.dumps(line), flush=True)
+    g.close()
+    host.free()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,365 @@
+"""GB300 de Bruijn graph construction and compaction: the Python host binding.
+
+A thin ctypes layer over the C ABI in ``include/bruno_gb300.h``; the work runs in the
+CUDA library ``_lib/libbruno_gb300.so``.  There is no CPU fallback: if the library is
+missing or no GPU is present, calls raise.
+
+The step names follow ParBLiSS/bruno's src/debruijn API (debruijn_graph_map::
+compute_biedge_freqencies / local_insert_by_freqencies, debruijn_chain_graph::
+extract_chains / list_rank_min_update / list_rank / to_ranked_chain_nodes /
+to_compressed_chains), so a driver written against the reference reads the same.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_lib", "libbruno_gb300.so")
+
+STATUS = {
+    0: "OK", 1: "ARG", 2: "BAD_INPUT", 3: "OOM", 4: "TABLE_FULL", 5: "RANK_NOT_CONVERGED",
+    6: "INVARIANT", 7: "CUDA", 8: "CAPACITY",
+}
+COUNT_MAX = 65535  # CountType = uint16 (compact_dbg_freq_construct_clean.cpp:187)
+
+
+class BrunoError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"bruno_gb300 {STATUS.get(status, status)}: {message}")
+        self.status = status
+        self.message = message
+
+
+class _Cfg(ctypes.Structure):
+    _fields_ = [
+        ("k", ctypes.c_int32), ("thresholding", ctypes.c_int32), ("thresh", ctypes.c_uint64 * 6),
+        ("min_update", ctypes.c_int32), ("device", ctypes.c_int32), ("table_slots", ctypes.c_uint64),
+        ("max_load", ctypes.c_double), ("keep_k2", ctypes.c_int32), ("keep_filtered", ctypes.c_int32),
+    ]
+
+
+class _Sizes(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "n_reads", "n_reads_used", "n_instances", "n_k2", "n_filtered", "n_nodes", "n_branch",
+        "n_chain_nodes", "iterations", "n_cycle_nodes", "n_isolated", "n_ranked", "n_chains",
+        "n_chain_chars", "table_slots", "collisions")] + [("filter_flag_hist", ctypes.c_uint64 * 16),
+                                                    ("launches", ctypes.c_uint64)]
+
+
+_lib: Optional[ctypes.CDLL] = None
+
+# every entry point of include/bruno_gb300.h
+EXPORTS = (
+    "bruno_ctx_create", "bruno_ctx_destroy", "bruno_set_stream", "bruno_last_error", "bruno_reset",
+    "bruno_load_fastq", "bruno_compute_biedge_freqencies", "bruno_local_insert_by_freqencies",
+    "bruno_extract_chains", "bruno_list_rank", "bruno_to_compressed_chains", "bruno_build_and_compact",
+    "bruno_get_sizes", "bruno_copy_k2", "bruno_copy_filtered", "bruno_copy_nodes", "bruno_copy_ranked",
+    "bruno_copy_chains", "bruno_host_alloc", "bruno_host_free", "bruno_phase_ms",
+)
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Loads the CUDA library (built by ``__graft_entry__.build()``); raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise BrunoError(1, f"CUDA library not built: {path} (run __graft_entry__.build())")
+    lib = ctypes.CDLL(path)
+    P, U64, I32, SZ = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, ctypes.c_size_t
+    PSZ = ctypes.POINTER(ctypes.c_size_t)
+    sig = {
+        "bruno_ctx_create": [ctypes.POINTER(_Cfg), ctypes.POINTER(P)],
+        "bruno_ctx_destroy": [P], "bruno_set_stream": [P, P], "bruno_reset": [P],
+        "bruno_load_fastq": [P, P, SZ, I32], "bruno_compute_biedge_freqencies": [P],
+        "bruno_local_insert_by_freqencies": [P, P], "bruno_extract_chains": [P],
+        "bruno_list_rank": [P, I32, ctypes.POINTER(U64)], "bruno_to_compressed_chains": [P],
+        "bruno_build_and_compact": [P, P, SZ, I32], "bruno_get_sizes": [P, ctypes.POINTER(_Sizes)],
+        "bruno_copy_k2": [P, P, P, P, SZ, PSZ], "bruno_copy_filtered": [P, P, P, P, SZ, PSZ],
+        "bruno_copy_nodes": [P, P, P, P, SZ, PSZ], "bruno_copy_ranked": [P, P, P, P, SZ, PSZ],
+        "bruno_copy_chains": [P, P, P, P, SZ, SZ, PSZ, PSZ],
+        "bruno_host_alloc": [SZ, ctypes.POINTER(P)], "bruno_host_free": [P],
+        "bruno_phase_ms": [P, ctypes.POINTER(ctypes.c_double), SZ],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    lib.bruno_last_error.argtypes = [P]
+    lib.bruno_last_error.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+def thresholds(lower: Sequence[int] = (), upper: Sequence[int] = (), count_max: int = COUNT_MAX) -> list[int]:
+    """The reference driver's -L/-U handling (compact_dbg_freq_construct_clean.cpp:874,937-961):
+    one value = the (k+1)-mer bound (and k / k+2 lower bounds drop to 0), three values =
+    k, k+1, k+2.  Order: k_lo, k_hi, k1_lo, k1_hi, k2_lo, k2_hi."""
+    t = [count_max + 1] * 6
+    lower, upper = list(lower), list(upper)
+    if len(lower) == 1:
+        t[2] = min(lower[0], t[2])
+        t[0] = t[4] = 0
+    elif len(lower) == 3:
+        t[0], t[2], t[4] = (min(v, c) for v, c in zip(lower, (t[0], t[2], t[4])))
+    elif lower:
+        raise ValueError("lower thresholds take 1 or 3 values")
+    if len(upper) == 1:
+        t[3] = min(upper[0], t[3])
+    elif len(upper) == 3:
+        t[1], t[3], t[5] = (min(v, c) for v, c in zip(upper, (t[1], t[3], t[5])))
+    elif upper:
+        raise ValueError("upper thresholds take 1 or 3 values")
+    return t
+
+
+def kmer_words(k: int) -> int:
+    return 1 if k <= 31 else 2
+
+
+def decode_kmers(words: np.ndarray, k: int) -> list[str]:
+    """2-bit packed k-mers (n x words uint64, low word first) -> strings."""
+    w = words.reshape(len(words), -1) if words.ndim == 1 else words
+    out = []
+    for row in w:
+        v = int(row[0]) | (int(row[1]) << 64 if len(row) > 1 else 0)
+        out.append("".join("ACGT"[(v >> (2 * (k - 1 - i))) & 3] for i in range(k)))
+    return out
+
+
+@dataclass
+class GraphConfig:
+    k: int = 31
+    thresholding: bool = True
+    thresh: list = field(default_factory=lambda: thresholds([2]))
+    min_update: bool = True
+    device: int = 0
+    table_slots: int = 0
+    max_load: float = 0.5
+    keep_k2: bool = False
+    keep_filtered: bool = False
+
+    def to_c(self) -> _Cfg:
+        c = _Cfg()
+        c.k, c.thresholding, c.min_update, c.device = self.k, int(self.thresholding), int(self.min_update), self.device
+        for i, v in enumerate(self.thresh):
+            c.thresh[i] = int(min(v, 2**64 - 1))
+        c.table_slots, c.max_load = self.table_slots, self.max_load
+        c.keep_k2, c.keep_filtered = int(self.keep_k2), int(self.keep_filtered)
+        return c
+
+
+class Graph:
+    """One de Bruijn graph build on one GPU (a bruno_ctx)."""
+
+    def __init__(self, config: Optional[GraphConfig] = None, **kw):
+        self.lib = load_library()
+        self.config = config or GraphConfig(**kw)
+        self.words = kmer_words(self.config.k)
+        self._cfg = self.config.to_c()
+        h = ctypes.c_void_p()
+        self._check(self.lib.bruno_ctx_create(ctypes.byref(self._cfg), ctypes.byref(h)), "ctx_create")
+        self.ctx = h
+        self._keep = []
+
+    # ------------------------------------------------------------------ plumbing
+    def _check(self, status: int, what: str) -> None:
+        if status != 0:
+            msg = what
+            if getattr(self, "ctx", None):
+                m = self.lib.bruno_last_error(self.ctx)
+                msg = f"{what}: {m.decode() if m else ''}"
+            raise BrunoError(status, msg)
+
+    def close(self) -> None:
+        if getattr(self, "ctx", None):
+            self.lib.bruno_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int) -> None:
+        """Runs later calls on an existing cudaStream_t (e.g. torch's current stream)."""
+        self._check(self.lib.bruno_set_stream(self.ctx, ctypes.c_void_p(int(stream_handle))), "set_stream")
+
+    # ------------------------------------------------------------------ steps
+    def reset(self) -> None:
+        self._keep.clear()
+        self._check(self.lib.bruno_reset(self.ctx), "reset")
+
+    def load_fastq(self, data, nbytes: Optional[int] = None, is_device: bool = False) -> None:
+        """Adds one FASTQ file (bytes / uint8 array on the host, or a device address)."""
+        if is_device:
+            self._check(self.lib.bruno_load_fastq(self.ctx, ctypes.c_void_p(int(data)), int(nbytes), 1), "load_fastq")
+            return
+        arr = np.frombuffer(data, dtype=np.uint8) if isinstance(data, (bytes, bytearray, memoryview)) else data
+        arr = np.ascontiguousarray(arr, dtype=np.uint8)
+        self._keep.append(arr)
+        self._check(self.lib.bruno_load_fastq(self.ctx, arr.ctypes.data_as(ctypes.c_void_p), arr.nbytes, 0),
+                    "load_fastq")
+
+    def compute_biedge_freqencies(self) -> int:
+        self._check(self.lib.bruno_compute_biedge_freqencies(self.ctx), "compute_biedge_freqencies")
+        return self.sizes()["n_k2"]
+
+    def local_insert_by_freqencies(self, threshes: Optional[Sequence[int]] = None) -> int:
+        p = None
+        if threshes is not None:
+            t = (ctypes.c_uint64 * 6)(*[int(min(v, 2**64 - 1)) for v in threshes])
+            p = ctypes.cast(t, ctypes.c_void_p)
+        self._check(self.lib.bruno_local_insert_by_freqencies(self.ctx, p), "local_insert_by_freqencies")
+        return self.sizes()["n_nodes"]
+
+    def extract_chains(self) -> None:
+        self._check(self.lib.bruno_extract_chains(self.ctx), "extract_chains")
+
+    def _rank(self, min_update: bool) -> int:
+        it = ctypes.c_uint64()
+        self._check(self.lib.bruno_list_rank(self.ctx, int(min_update), ctypes.byref(it)), "list_rank")
+        return it.value
+
+    def list_rank_min_update(self) -> int:
+        return self._rank(True)
+
+    def list_rank(self) -> int:
+        return self._rank(False)
+
+    def to_compressed_chains(self) -> None:
+        self._check(self.lib.bruno_to_compressed_chains(self.ctx), "to_compressed_chains")
+
+    def build_and_compact(self, data, nbytes: Optional[int] = None, is_device: bool = False) -> None:
+        """The whole plain path; host bytes are copied in, device bytes are read in place."""
+        if is_device:
+            self._check(self.lib.bruno_build_and_compact(self.ctx, ctypes.c_void_p(int(data)), int(nbytes), 1),
+                        "build_and_compact")
+            return
+        arr = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8) if isinstance(data, (bytes, bytearray))
+                                   else data, dtype=np.uint8)
+        self._keep = [arr]
+        self._check(self.lib.bruno_build_and_compact(self.ctx, arr.ctypes.data_as(ctypes.c_void_p), arr.nbytes, 0),
+                    "build_and_compact")
+
+    def run(self, *files) -> "Graph":
+        """load every file, then count, filter, extract, rank and compress"""
+        self.reset()
+        for f in files:
+            self.load_fastq(f)
+        self.compute_biedge_freqencies()
+        self.local_insert_by_freqencies()
+        self.extract_chains()
+        self._rank(self.config.min_update)
+        self.to_compressed_chains()
+        return self
+
+    # ------------------------------------------------------------------ results
+    def sizes(self) -> dict:
+        s = _Sizes()
+        self._check(self.lib.bruno_get_sizes(self.ctx, ctypes.byref(s)), "get_sizes")
+        d = {n: getattr(s, n) for n, _ in _Sizes._fields_ if n != "filter_flag_hist"}
+        d["filter_flag_hist"] = list(s.filter_flag_hist)
+        return d
+
+    PHASES = ("parse", "count_k2mers", "filter_insert", "chainmap", "list_rank", "compress",
+              "k_hll", "k_table_init", "k_count")
+
+    def phase_ms(self) -> dict:
+        a = (ctypes.c_double * 9)()
+        self._check(self.lib.bruno_phase_ms(self.ctx, a, 9), "phase_ms")
+        return dict(zip(self.PHASES, list(a)))
+
+    def _ptr(self, a: np.ndarray):
+        return a.ctypes.data_as(ctypes.c_void_p)
+
+    def _triple(self, fn, what):
+        n = ctypes.c_size_t()
+        self._check(fn(self.ctx, None, None, None, 0, ctypes.byref(n)), what)
+        keys = np.zeros((n.value, self.words), np.uint64)
+        edges = np.zeros(n.value, np.uint8)
+        counts = np.zeros(n.value, np.uint32)
+        if n.value:
+            self._check(fn(self.ctx, self._ptr(keys), self._ptr(edges), self._ptr(counts), n.value, ctypes.byref(n)),
+                        what)
+        return keys, edges, counts
+
+    def k2(self):
+        """raw canonical (k-mer, biedge) counts: keys (n, words), edges, counts"""
+        return self._triple(self.lib.bruno_copy_k2, "copy_k2")
+
+    def filtered(self):
+        return self._triple(self.lib.bruno_copy_filtered, "copy_filtered")
+
+    def nodes(self):
+        """graph nodes: keys (n, words), counts (n, 9) = out ACGT, in ACGT, self; flags"""
+        n = ctypes.c_size_t()
+        self._check(self.lib.bruno_copy_nodes(self.ctx, None, None, None, 0, ctypes.byref(n)), "copy_nodes")
+        keys = np.zeros((n.value, self.words), np.uint64)
+        counts = np.zeros((n.value, 9), np.uint16)
+        flags = np.zeros(n.value, np.uint8)
+        if n.value:
+            self._check(self.lib.bruno_copy_nodes(self.ctx, self._ptr(keys), self._ptr(counts), self._ptr(flags),
+                                                  n.value, ctypes.byref(n)), "copy_nodes")
+        return keys, counts, flags
+
+    def ranked(self):
+        """listranked chain nodes: K (n, words), rep (n, words), dist"""
+        n = ctypes.c_size_t()
+        self._check(self.lib.bruno_copy_ranked(self.ctx, None, None, None, 0, ctypes.byref(n)), "copy_ranked")
+        K = np.zeros((n.value, self.words), np.uint64)
+        rep = np.zeros((n.value, self.words), np.uint64)
+        dist = np.zeros(n.value, np.int32)
+        if n.value:
+            self._check(self.lib.bruno_copy_ranked(self.ctx, self._ptr(K), self._ptr(rep), self._ptr(dist), n.value,
+                                                   ctypes.byref(n)), "copy_ranked")
+        return K, rep, dist
+
+    def chains(self):
+        """compacted chains: reps (n, words), offsets (n+1), chars (uint8)"""
+        nc, nch = ctypes.c_size_t(), ctypes.c_size_t()
+        self._check(self.lib.bruno_copy_chains(self.ctx, None, None, None, 0, 0, ctypes.byref(nc), ctypes.byref(nch)),
+                    "copy_chains")
+        reps = np.zeros((nc.value, self.words), np.uint64)
+        offs = np.zeros(nc.value + 1, np.uint64)
+        chars = np.zeros(max(1, nch.value), np.uint8)
+        if nc.value:
+            self._check(self.lib.bruno_copy_chains(self.ctx, self._ptr(reps), self._ptr(offs), self._ptr(chars),
+                                                   nc.value, chars.size, ctypes.byref(nc), ctypes.byref(nch)),
+                        "copy_chains")
+        return reps, offs, chars[:nch.value]
+
+    def chain_strings(self) -> list[str]:
+        reps, offs, chars = self.chains()
+        b = chars.tobytes()
+        return [b[offs[i]:offs[i + 1]].decode() for i in range(len(reps))]
+
+
+class PinnedBuffer:
+    """Page-locked host memory from the library (fast host<->device copies)."""
+
+    def __init__(self, nbytes: int):
+        self.lib = load_library()
+        p = ctypes.c_void_p()
+        st = self.lib.bruno_host_alloc(nbytes, ctypes.byref(p))
+        if st != 0:
+            raise BrunoError(st, "host_alloc")
+        self.ptr, self.nbytes = p.value, nbytes
+        self.array = np.ctypeslib.as_array((ctypes.c_uint8 * nbytes).from_address(p.value))
+
+    def free(self) -> None:
+        if self.ptr:
+            self.lib.bruno_host_free(ctypes.c_void_p(self.ptr))
+            self.ptr = None

@@ -1,0 +1,872 @@
+/*
+ * build.cu -- FASTQ -> k-mer table -> graph nodes.
+ *
+ *  k_tile_stats / k_index_lines   FASTQ record split (4-line records, trailing blank lines
+ *                                 ignored), one pass over the bytes each.
+ *  k_hll                          HyperLogLog estimate of distinct canonical k-mers, used to
+ *                                 size the table.
+ *  k_count                        debruijn_kmer_simple_biedge_parser + lex_less +
+ *                                 compute_biedge_freqencies: one warp per read packs the
+ *                                 read to 2-bit words with ballots, every lane then cuts its
+ *                                 k-mers out of the packed words, canonicalises them with the
+ *                                 biedge and counts the pair in the k-mer's table slot.
+ *  k_filter                       local_insert_by_freqencies: per k-mer, the (k+1)-mer sums,
+ *                                 the per-entry flags, the compaction and the node update,
+ *                                 all in registers; the node replaces the counts in place.
+ *                                 IsBranchPoint / IsChainNode are decided in the same pass.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "internal.cuh"
+
+namespace bg {
+
+namespace {
+
+constexpr int TILE = 65536;          /* bytes per FASTQ tile */
+constexpr int TPB = 256;
+
+__device__ __forceinline__ int base_code(unsigned char c) {
+  /* A/a 0, C/c 1, G/g 2, T/t 3, anything else (N, IUPAC, ...) -1 */
+  switch (c | 0x20) {
+    case 'a': return 0;
+    case 'c': return 1;
+    case 'g': return 2;
+    case 't': return 3;
+    default: return -1;
+  }
+}
+
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(~0u, v, o);
+  return v;
+}
+
+/* block-wide exclusive prefix sum of one value per thread (blockDim.x == TPB); every
+ * thread also receives the block total */
+__device__ __forceinline__ uint32_t block_exscan(uint32_t v, uint32_t &total) {
+  __shared__ uint32_t ws[TPB / 32 + 1];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(~0u, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[w] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (int i = 0; i < TPB / 32; ++i) { uint32_t t = ws[i]; ws[i] = run; run += t; }
+    ws[TPB / 32] = run;
+  }
+  __syncthreads();
+  const uint32_t r = ws[w] + x - v;
+  total = ws[TPB / 32];
+  __syncthreads();
+  return r;
+}
+
+/* ============================================================ FASTQ splitting */
+
+/* newline count and last non-whitespace byte of each tile */
+__global__ void __launch_bounds__(TPB) k_tile_stats(const unsigned char *buf, uint64_t n, uint64_t *tile_cnt,
+                                                     DevCounters *ctr) {
+  const uint64_t t0 = (uint64_t)blockIdx.x * TILE;
+  const uint64_t t1 = (n < t0 + TILE ? n : t0 + TILE);
+  unsigned long long cnt = 0;
+  long long lastnw = -1;
+  for (uint64_t p = t0 + threadIdx.x; p < t1; p += TPB) {
+    unsigned char c = buf[p];
+    cnt += (c == '\n');
+    if (c != '\n' && c != '\r') lastnw = (long long)p;
+  }
+  __shared__ unsigned long long sc[TPB / 32];
+  __shared__ long long sl[TPB / 32];
+  cnt = warp_sum(cnt);
+  for (int o = 16; o > 0; o >>= 1) lastnw = max(lastnw, __shfl_down_sync(~0u, lastnw, o));
+  if ((threadIdx.x & 31) == 0) { sc[threadIdx.x >> 5] = cnt; sl[threadIdx.x >> 5] = lastnw; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long c = 0; long long l = -1;
+    for (int i = 0; i < TPB / 32; ++i) { c += sc[i]; l = max(l, sl[i]); }
+    tile_cnt[blockIdx.x] = c;
+    if (l >= 0) atomicMax(&ctr->last_nonws, l);
+  }
+}
+
+/* Assigns a global line number to every newline and records each read's sequence span.
+ * Line j ends at the j-th newline; records are lines 4r..4r+3 (header, sequence, '+',
+ * quality).  Newlines after the last non-blank byte are trailing and ignored. */
+__global__ void __launch_bounds__(TPB) k_index_lines(const unsigned char *buf, uint64_t n, const uint64_t *tile_base,
+                                                      uint64_t *rstart, uint64_t *rend, uint64_t rbase,
+                                                      uint64_t rcap, DevCounters *ctr) {
+  const uint64_t t0 = (uint64_t)blockIdx.x * TILE;
+  const uint64_t t1 = (n < t0 + TILE ? n : t0 + TILE);
+  const long long E = ctr->last_nonws + 1;  /* effective end (exclusive) */
+  uint64_t base = tile_base[blockIdx.x];
+  if (blockIdx.x == 0 && threadIdx.x == 0 && E > 0 && buf[0] != '@') atomicMin(&ctr->bad_line, 0ull);
+  /* stripes of TPB*16 bytes, 16 consecutive bytes per thread, in byte order */
+  for (uint64_t s0 = t0; s0 < t1; s0 += (uint64_t)TPB * 16) {
+    const uint64_t g0 = s0 + (uint64_t)threadIdx.x * 16;
+    unsigned char b[16];
+    uint32_t m = 0;
+    #pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      uint64_t p = g0 + i;
+      b[i] = (p < t1) ? buf[p] : 0;
+      m |= (uint32_t)(b[i] == '\n') << i;
+    }
+    uint32_t total;
+    const uint32_t rank = block_exscan(__popc(m), total);
+    uint64_t j = base + rank;
+    while (m) {
+      int i = __ffs(m) - 1;
+      m &= m - 1;
+      const uint64_t p = g0 + i;
+      if ((long long)p < E) {
+        const uint64_t ln = j;  /* this newline ends line ln */
+        atomicMax(&ctr->n_newlines_eff, (unsigned long long)(ln + 1));
+        const uint64_t r = ln >> 2;
+        const unsigned role = (unsigned)(ln & 3);
+        if (role == 0 && rbase + r < rcap) rstart[rbase + r] = (uint64_t)(buf + p + 1);
+        if (role == 1 && rbase + r < rcap) {
+          uint64_t e = p;
+          if (e > 0 && buf[e - 1] == '\r') --e;
+          rend[rbase + r] = (uint64_t)(buf + e);
+        }
+        /* the first byte of line ln+1 */
+        const unsigned nrole = (unsigned)((ln + 1) & 3);
+        if (nrole == 0 || nrole == 2) {
+          unsigned char c = ((long long)(p + 1) < E) ? buf[p + 1] : 0;
+          if (c != (nrole == 0 ? '@' : '+')) atomicMin(&ctr->bad_line, (unsigned long long)(ln + 1));
+        }
+      }
+      ++j;
+    }
+    base += total;
+  }
+}
+
+/* ============================================================ k-mer extraction */
+
+/* Per-warp staging of one chunk of a read as 2-bit words.  Chunk c covers k-mer start
+ * positions [1024c, 1024c + 1024); word wi holds bases [1024c - 32 + 32wi, +32). */
+constexpr int CHUNK_POS = 1024;
+constexpr int CHUNK_WORDS = 40;  /* (32 + 1024 + 63 + 1) / 32 rounded up, plus 3 spare */
+
+struct ReadView {
+  const unsigned char *s;
+  uint32_t L;
+};
+
+/* Loads the bases of chunk [p0, pend) plus flanks into words[]; returns nothing.  All
+ * bases are known to be ACGT (the read passed the N filter). */
+__device__ __forceinline__ void stage_chunk(const ReadView &rv, uint32_t p0, uint32_t pend, int k, uint64_t *words,
+                                            int lane) {
+  const long long c0 = (long long)p0 - 32;
+  const long long cend = ((long long)rv.L < (long long)pend + k + 1) ? (long long)rv.L : (long long)pend + k + 1;
+  const int nw = (int)((cend - c0 + 31) >> 5);
+  for (int wi = 0; wi < nw; ++wi) {
+    const long long c = c0 + 32 * wi + lane;
+    unsigned code = 0;
+    if (c >= 0 && c < (long long)rv.L) code = (unsigned)base_code(rv.s[c]);
+    const unsigned m0 = __ballot_sync(~0u, code & 1u), m1 = __ballot_sync(~0u, code & 2u);
+    if (lane == 0) {
+      /* interleave: base i -> bits (62-2i, 63-2i), high bit from m1 */
+      uint64_t z = 0;
+      uint64_t a = m0, b = m1;
+      a = (a | (a << 16)) & 0x0000FFFF0000FFFFull; a = (a | (a << 8)) & 0x00FF00FF00FF00FFull;
+      a = (a | (a << 4)) & 0x0F0F0F0F0F0F0F0Full; a = (a | (a << 2)) & 0x3333333333333333ull;
+      a = (a | (a << 1)) & 0x5555555555555555ull;
+      b = (b | (b << 16)) & 0x0000FFFF0000FFFFull; b = (b | (b << 8)) & 0x00FF00FF00FF00FFull;
+      b = (b | (b << 4)) & 0x0F0F0F0F0F0F0F0Full; b = (b | (b << 2)) & 0x3333333333333333ull;
+      b = (b | (b << 1)) & 0x5555555555555555ull;
+      z = (a << 1) | b;   /* bit 2i+1 = m0_i, bit 2i = m1_i */
+      words[wi] = __brevll(z);
+    }
+  }
+  if (lane < 3) words[nw + lane] = 0;
+  __syncwarp();
+}
+
+__device__ __forceinline__ unsigned base_at(const uint64_t *w, int i) {
+  return (unsigned)(w[i >> 5] >> (62 - 2 * (i & 31))) & 3u;
+}
+
+/* ============================================================ distinct estimate */
+
+constexpr int HLL_P = 14;
+constexpr int HLL_M = 1 << HLL_P;
+
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_hll(const uint64_t *rstart, const uint64_t *rend, uint64_t nreads, int k,
+                                              uint8_t *partial) {
+  __shared__ uint64_t sw[TPB / 32][CHUNK_WORDS];
+  __shared__ unsigned int reg[HLL_M / 4];
+  for (int i = threadIdx.x; i < HLL_M / 4; i += TPB) reg[i] = 0;
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint64_t *words = sw[warp];
+  for (uint64_t r = (uint64_t)blockIdx.x * (TPB / 32) + warp; r < nreads; r += (uint64_t)gridDim.x * (TPB / 32)) {
+    ReadView rv{(const unsigned char *)rstart[r], (uint32_t)(rend[r] - rstart[r])};
+    if (rv.L < (uint32_t)k + 2) continue;
+    bool bad = false;
+    for (uint32_t i = lane; i < rv.L; i += 32) bad |= base_code(rv.s[i]) < 0;
+    if (__any_sync(~0u, bad)) continue;
+    const uint32_t npos = rv.L - k + 1;
+    for (uint32_t p0 = 0; p0 < npos; p0 += CHUNK_POS) {
+      const uint32_t pend = min(npos, p0 + CHUNK_POS);
+      __syncwarp();
+      stage_chunk(rv, p0, pend, k, words, lane);
+      for (uint32_t pb = p0; pb < pend; pb += 32) {
+        const uint32_t p = pb + lane;
+        if (p < pend) {
+          KT x = KOps<KT>::extract(words, (int)(p - p0 + 32), k);
+          KT y = KOps<KT>::rc(x, k);
+          if (!KOps<KT>::lt(x, y)) x = y;
+          const uint64_t h = mix64(KOps<KT>::hash(x) ^ 0x6a09e667f3bcc909ull);
+          const unsigned idx = (unsigned)(h >> (64 - HLL_P));
+          const unsigned rho = (unsigned)__clzll((h << HLL_P) | (1ull << (HLL_P - 1))) + 1u;
+          /* byte-wise max inside a 32-bit word */
+          unsigned int *wp = &reg[idx >> 2];
+          const int sh = (idx & 3) * 8;
+          unsigned int old = *((volatile unsigned int *)wp);
+          while (((old >> sh) & 0xFFu) < rho) {
+            unsigned int nv = (old & ~(0xFFu << sh)) | (rho << sh);
+            unsigned int got = atomicCAS(wp, old, nv);
+            if (got == old) break;
+            old = got;
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  uint32_t *dst = (uint32_t *)(partial + (uint64_t)blockIdx.x * HLL_M);
+  for (int i = threadIdx.x; i < HLL_M / 4; i += TPB) dst[i] = reg[i];
+}
+
+__global__ void k_hll_merge(const uint8_t *partial, int nblocks, DevCounters *ctr) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < HLL_M; i += gridDim.x * blockDim.x) {
+    unsigned m = 0;
+    for (int b = 0; b < nblocks; ++b) m = max(m, (unsigned)partial[(uint64_t)b * HLL_M + i]);
+    ctr->hll[i] = m;
+  }
+}
+
+/* ============================================================ counting */
+
+struct CountArgs {
+  const uint64_t *rstart, *rend;
+  uint64_t nreads;
+  int k;
+  uint64_t *table;
+  uint64_t nslots;
+  uint32_t max_probe;
+  DevCounters *ctr;
+};
+
+__device__ __forceinline__ uint64_t ld_cg(const uint64_t *p) { return __ldcg((const unsigned long long *)p); }
+__device__ __forceinline__ uint32_t ld_cg32(const uint32_t *p) { return __ldcg(p); }
+
+/* One count into entry list e[0..n): returns true when done, false when the slot is full. */
+__device__ __forceinline__ bool count_in_entries(uint32_t *e, int n, unsigned code, unsigned long long &claims) {
+  for (int i = 0; i < n; ++i) {
+    uint32_t w = ld_cg32(e + i);
+    if (w == 0) {
+      const uint32_t nw = (code << E_CODE_SHIFT) | (1u << E_COUNT_SHIFT);
+      const uint32_t old = atomicCAS(e + i, 0u, nw);
+      if (old == 0) { ++claims; return true; }
+      w = old;
+    }
+    if (entry_code(w) == code) {
+      const uint32_t old = atomicAdd(e + i, 1u << E_COUNT_SHIFT);
+      if (old >> 31) atomicOr(e + i, E_BIG);  /* count reached 2^25: remember it stays large */
+      return true;
+    }
+  }
+  return false;
+}
+
+/* slot key helpers (KW1: one word; KW2: lo, hi with flags in hi) */
+__device__ __forceinline__ bool key_claim(KW1, uint64_t *slot, KW1 want, bool cont, KW1 &seen, bool &was_empty) {
+  const uint64_t nk = want.v | (cont ? KEY_CONT : 0);
+  const uint64_t old = atomicCAS((unsigned long long *)slot, KEY_EMPTY, nk);
+  was_empty = (old == KEY_EMPTY);
+  seen.v = was_empty ? nk : old;
+  return was_empty;
+}
+
+__device__ __forceinline__ unsigned long long cas128(uint64_t *addr, uint64_t cmp_lo, uint64_t cmp_hi, uint64_t new_lo,
+                                                     uint64_t new_hi, uint64_t &old_hi) {
+  unsigned long long olo, ohi;
+  asm volatile(
+      "{\n\t.reg .b128 d, b, c;\n\t"
+      "mov.b128 b, {%2, %3};\n\t"
+      "mov.b128 c, {%4, %5};\n\t"
+      "atom.global.cas.b128 d, [%6], b, c;\n\t"
+      "mov.b128 {%0, %1}, d;\n\t}"
+      : "=l"(olo), "=l"(ohi)
+      : "l"(cmp_lo), "l"(cmp_hi), "l"(new_lo), "l"(new_hi), "l"(addr)
+      : "memory");
+  old_hi = ohi;
+  return olo;
+}
+
+__device__ __forceinline__ bool key_claim(KW2, uint64_t *slot, KW2 want, bool cont, KW2 &seen, bool &was_empty) {
+  const uint64_t nhi = want.hi | (cont ? KEY_CONT : 0);
+  uint64_t ohi;
+  const uint64_t olo = cas128(slot, KEY_EMPTY, KEY_EMPTY, want.lo, nhi, ohi);
+  was_empty = (olo == KEY_EMPTY && ohi == KEY_EMPTY);
+  seen = was_empty ? KW2{want.lo, nhi} : KW2{olo, ohi};
+  return was_empty;
+}
+
+__device__ __forceinline__ KW1 key_read(KW1, const uint64_t *slot) { return {ld_cg(slot)}; }
+__device__ __forceinline__ KW2 key_read(KW2, const uint64_t *slot) {
+  /* the claim writes both words in one 128-bit atomic, so a 16-byte load sees either
+   * the empty key or the whole claimed key */
+  ulonglong2 v = __ldcg((const ulonglong2 *)slot);
+  return {v.x, v.y};
+}
+__device__ __forceinline__ bool key_is_empty(KW1 k) { return k.v == KEY_EMPTY; }
+__device__ __forceinline__ bool key_is_empty(KW2 k) { return k.hi == KEY_EMPTY && k.lo == KEY_EMPTY; }
+__device__ __forceinline__ bool key_matches(KW1 k, KW1 want, bool cont) { return k.v == (want.v | (cont ? KEY_CONT : 0)); }
+__device__ __forceinline__ bool key_matches(KW2 k, KW2 want, bool cont) {
+  return k.lo == want.lo && k.hi == (want.hi | (cont ? KEY_CONT : 0));
+}
+__device__ __forceinline__ bool key_dead(KW1 k) { return (k.v & KEY_DEAD_BIT) != 0; }
+__device__ __forceinline__ bool key_dead(KW2 k) { return (k.hi & KEY_DEAD_BIT) != 0; }
+__device__ __forceinline__ bool key_cont(KW1 k) { return (k.v & KEY_CONT) != 0; }
+__device__ __forceinline__ bool key_cont(KW2 k) { return (k.hi & KEY_CONT) != 0; }
+
+/* Counts one canonical (k-mer, biedge code) occurrence.  Returns false if the probe limit
+ * was reached. */
+template <class KT>
+__device__ __forceinline__ bool table_count(uint64_t *table, uint64_t nslots, uint32_t max_probe, KT x, unsigned code,
+                                            unsigned long long &slot_claims, unsigned long long &entry_claims) {
+  constexpr int SU = Slot<KT>::U64, NE = Slot<KT>::ENTRIES, KWD = Slot<KT>::KEYW;
+  uint64_t i = __umul64hi(KOps<KT>::hash(x), nslots);
+  bool seen_primary = false;
+  for (uint32_t probe = 0; probe < max_probe; ++probe) {
+    uint64_t *slot = table + i * SU;
+    KT key = key_read(KT{}, slot);
+    if (key_is_empty(key)) {
+      bool was_empty;
+      key_claim(KT{}, slot, x, seen_primary, key, was_empty);
+      if (was_empty) ++slot_claims;
+    }
+    if (key_matches(key, x, seen_primary)) {
+      seen_primary = true;
+      if (count_in_entries((uint32_t *)(slot + KWD), NE, code, entry_claims)) return true;
+    }
+    if (++i == nslots) i = 0;
+  }
+  return false;
+}
+
+template <class KT>
+__global__ void __launch_bounds__(TPB, 4) k_count(CountArgs a) {
+  __shared__ uint64_t sw[TPB / 32][CHUNK_WORDS];
+  __shared__ unsigned long long s_inst, s_used, s_slots, s_entries;
+  __shared__ int s_full;
+  if (threadIdx.x == 0) { s_inst = s_used = s_slots = s_entries = 0; s_full = 0; }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = a.k;
+  uint64_t *words = sw[warp];
+  unsigned long long inst = 0, used = 0, slots = 0, entries = 0;
+  bool full = false;
+  for (uint64_t r = (uint64_t)blockIdx.x * (TPB / 32) + warp; r < a.nreads; r += (uint64_t)gridDim.x * (TPB / 32)) {
+    ReadView rv{(const unsigned char *)a.rstart[r], (uint32_t)(a.rend[r] - a.rstart[r])};
+    if (rv.L < (uint32_t)k + 2) continue;          /* shorter than the k+2 window */
+    bool bad = false;
+    for (uint32_t i = lane; i < rv.L; i += 32) bad |= base_code(rv.s[i]) < 0;
+    if (__any_sync(~0u, bad)) continue;            /* reads containing N are dropped */
+    used += (lane == 0);
+    const uint32_t npos = rv.L - k + 1;
+    for (uint32_t p0 = 0; p0 < npos; p0 += CHUNK_POS) {
+      const uint32_t pend = min(npos, p0 + CHUNK_POS);
+      __syncwarp();
+      stage_chunk(rv, p0, pend, k, words, lane);
+      for (uint32_t pb = p0; pb < pend; pb += 32) {
+        const uint32_t p = pb + lane;
+        if (p >= pend) continue;
+        const int lp = (int)(p - p0 + 32);
+        KT x = KOps<KT>::extract(words, lp, k);
+        /* biedge in DNA: base before and after the k-mer in the read (0 = read end) */
+        unsigned in5 = (p > 0) ? base_at(words, lp - 1) + 1u : 0u;
+        unsigned out5 = (p + k < rv.L) ? base_at(words, lp + k) + 1u : 0u;
+        /* lex_less: keep if x < rc(x), else flip the k-mer and reverse-complement the
+         * biedge (in' = comp(out), out' = comp(in); comp of a DNA code c is 3-c) */
+        KT y = KOps<KT>::rc(x, k);
+        if (!KOps<KT>::lt(x, y)) {
+          x = y;
+          unsigned ni = out5 ? (4u - out5) + 1u : 0u, no = in5 ? (4u - in5) + 1u : 0u;
+          in5 = ni; out5 = no;
+        }
+        ++inst;
+        if (!table_count<KT>(a.table, a.nslots, a.max_probe, x, biedge_code(in5, out5), slots, entries)) full = true;
+      }
+    }
+  }
+  inst = warp_sum(inst); used = warp_sum(used); slots = warp_sum(slots); entries = warp_sum(entries);
+  if (lane == 0) {
+    atomicAdd(&s_inst, inst); atomicAdd(&s_used, used); atomicAdd(&s_slots, slots); atomicAdd(&s_entries, entries);
+  }
+  if (full) s_full = 1;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicAdd(&a.ctr->n_instances, s_inst); atomicAdd(&a.ctr->n_reads_used, s_used);
+    atomicAdd(&a.ctr->n_slots_claimed, s_slots); atomicAdd(&a.ctr->n_entries, s_entries);
+    if (s_full) atomicOr(&a.ctr->err, (unsigned long long)DERR_TABLE_FULL);
+  }
+}
+
+/* table initialisation: every key word EMPTY, every entry 0 */
+template <class KT>
+__global__ void k_table_init(uint64_t *table, uint64_t nslots) {
+  constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t *s = table + i * SU;
+    #pragma unroll
+    for (int w = 0; w < SU; ++w) s[w] = (w < KWD) ? KEY_EMPTY : 0ull;
+  }
+}
+
+/* ============================================================ raw (k+2)-mer dump */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_dump_k2(const uint64_t *table, uint64_t nslots, uint64_t *keys, uint8_t *edges,
+                                                  uint32_t *counts, uint64_t cap, DevCounters *ctr) {
+  constexpr int SU = Slot<KT>::U64, NE = Slot<KT>::ENTRIES, KWD = Slot<KT>::KEYW;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t *s = table + i * SU;
+    KT key = KOps<KT>::load(s);
+    if (key_dead(key)) continue;
+    ((uint64_t *)&key)[KWD - 1] &= ~KEY_CONT;  /* continuation slots belong to the same k-mer */
+    const uint32_t *e = (const uint32_t *)(s + KWD);
+    for (int j = 0; j < NE; ++j) {
+      if (e[j] == 0) continue;
+      unsigned long long o = atomicAdd(&ctr->n_k2_dump, 1ull);
+      if (o < cap) {
+        KOps<KT>::store(keys + o * KWD, key);
+        edges[o] = code_biedge(entry_code(e[j]));
+        counts[o] = entry_count(e[j]);
+      }
+    }
+  }
+}
+
+/* ============================================================ filter + insert */
+
+struct FilterArgs {
+  uint64_t *table;
+  uint64_t nslots;
+  int k;
+  uint64_t t[6];
+  int thresholding;
+  uint32_t max_probe;
+  uint64_t *f_keys; uint8_t *f_edges; uint32_t *f_counts; uint64_t f_cap;
+  DevCounters *ctr;
+};
+
+/* local_insert_by_freqencies (debruijn_graph_map.hpp:1258-1623) for one k-mer block, from
+ * its entries in registers; writes the node (compact_multi_biedge counts) over the slot. */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
+  constexpr int SU = Slot<KT>::U64, NE = Slot<KT>::ENTRIES, KWD = Slot<KT>::KEYW;
+  __shared__ unsigned long long s_hist[16], s_nodes, s_branch, s_chain;
+  if (threadIdx.x < 16) s_hist[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_nodes = s_branch = s_chain = 0;
+  __syncthreads();
+  const int k = a.k;
+  unsigned long long nodes = 0, branch = 0, chain = 0;
+  unsigned hist[16];
+  #pragma unroll
+  for (int f = 0; f < 16; ++f) hist[f] = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.nslots; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t *s = a.table + i * SU;
+    KT key = KOps<KT>::load(s);
+    if (key_dead(key) || key_cont(key)) continue;
+    /* gather the k-mer's entries: this slot, then continuation slots along the probe run */
+    uint32_t cnt[25];
+    uint8_t code[25];
+    int ne = 0;
+    const uint32_t *e = (const uint32_t *)(s + KWD);
+    bool full = true;
+    for (int j = 0; j < NE; ++j) {
+      uint32_t w = e[j];
+      if (w == 0) { full = false; break; }
+      code[ne] = (uint8_t)entry_code(w); cnt[ne] = entry_count(w); ++ne;
+    }
+    if (full) {
+      uint64_t j = i;
+      for (uint32_t probe = 1; probe < a.max_probe; ++probe) {
+        if (++j == a.nslots) j = 0;
+        uint64_t *s2 = a.table + j * SU;
+        KT k2 = KOps<KT>::load(s2);
+        if (key_is_empty(k2)) break;
+        if (!key_matches(k2, key, true)) continue;
+        const uint32_t *e2 = (const uint32_t *)(s2 + KWD);
+        for (int q = 0; q < NE && ne < 25; ++q) {
+          uint32_t w = e2[q];
+          if (w == 0) break;
+          code[ne] = (uint8_t)entry_code(w); cnt[ne] = entry_count(w); ++ne;
+        }
+        /* the continuation slot is folded into this node */
+        if (KWD == 1) s2[0] = KEY_TOMB; else { s2[0] = KEY_TOMB; s2[1] = KEY_TOMB; }
+      }
+    }
+    /* step 4: per-block sums (:1460-1507) */
+    const bool kpal = k_palindrome(key, k);
+    const bool high = km1_high_palindrome(key, k), low = km1_low_palindrome(key, k);
+    const unsigned first = KOps<KT>::first(key, k), last = KOps<KT>::last(key);
+    const bool oddk = (k & 1) != 0;
+    uint64_t k_f = 0, k1in[4] = {0, 0, 0, 0}, k1out[4] = {0, 0, 0, 0};
+    for (int q = 0; q < ne; ++q) {
+      const uint64_t c = cnt[q];
+      const unsigned in5 = code_in5(code[q]), out5 = code_out5(code[q]);
+      k_f += c;
+      if (in5) {
+        const unsigned ch = in5 - 1;
+        const bool split = oddk && last == 3u - ch && high && !kpal;
+        k1in[ch] += split ? ((c + 1) >> 1) : c;
+      }
+      if (out5) {
+        const unsigned ch = out5 - 1;
+        const bool split = oddk && first == 3u - ch && low && !kpal;
+        k1out[ch] += split ? ((c + 1) >> 1) : c;
+      }
+    }
+    /* caps at FreqType max (:1401-1407) */
+    const uint64_t cmax = 0xFFFF;
+    k_f = min(cmax, k_f);
+    #pragma unroll
+    for (int c = 0; c < 4; ++c) { k1in[c] = min(cmax, k1in[c]); k1out[c] = min(cmax, k1out[c]); }
+    /* step 5: flags (:1410-1448), step 6: trim (:1563-1594), step 7: node update (:256-285) */
+    uint64_t nc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    bool any = false;
+    for (int q = 0; q < ne; ++q) {
+      const uint64_t cnt16 = min(cmax, (uint64_t)cnt[q]);
+      unsigned in5 = code_in5(code[q]), out5 = code_out5(code[q]);
+      unsigned f = 0;
+      if (a.thresholding) {
+        if (cnt16 < a.t[4] || cnt16 >= a.t[5]) f |= 4;
+        if (k_f < a.t[0] || k_f >= a.t[1]) f |= 8;
+        uint64_t k1 = in5 ? k1in[in5 - 1] : a.t[3];
+        if (k1 < a.t[2] || k1 >= a.t[3]) f |= 2;
+        k1 = out5 ? k1out[out5 - 1] : a.t[3];
+        if (k1 < a.t[2] || k1 >= a.t[3]) f |= 1;
+      }
+      ++hist[f];
+      if (f >= 3) continue;
+      if (f == 1) out5 = 0;
+      if (f == 2) in5 = 0;
+      any = true;
+      if (out5) nc[out5 - 1] += cnt16;
+      if (in5) nc[4 + in5 - 1] += cnt16;
+      nc[8] += cnt16;
+      if (a.f_keys) {
+        unsigned long long o = atomicAdd(&a.ctr->n_filtered, 1ull);
+        if (o < a.f_cap) {
+          KOps<KT>::store(a.f_keys + o * KWD, key);
+          a.f_edges[o] = code_biedge(biedge_code(in5, out5));
+          a.f_counts[o] = cnt[q];
+        }
+      }
+    }
+    if (!any) {  /* no kept entry: the k-mer never enters the graph */
+      if (KWD == 1) s[0] = KEY_TOMB; else { s[0] = KEY_TOMB; s[1] = KEY_TOMB; }
+      continue;
+    }
+    uint16_t c16[9];
+    #pragma unroll
+    for (int q = 0; q < 9; ++q) c16[q] = (uint16_t)min(cmax, nc[q]);
+    /* IsBranchPoint / IsChainNode (debruijn_graph_filters.hpp:57-220) */
+    unsigned din = 0, dout = 0;
+    bool k1pal = false;
+    #pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      dout += c16[c] > 0;
+      din += c16[4 + c] > 0;
+      if (oddk && c16[c] > 0 && low && (first == 3u - c || first == (unsigned)c)) k1pal = true;
+      if (oddk && c16[4 + c] > 0 && high && (last == 3u - c || last == (unsigned)c)) k1pal = true;
+    }
+    const bool is_branch = din >= 2 || dout >= 2 || kpal || k1pal;
+    const uint32_t flags = is_branch ? NF_BRANCH : NF_CHAIN;
+    ++nodes; branch += is_branch; chain += !is_branch;
+    uint64_t *pw = s + KWD;
+    pw[0] = (uint64_t)c16[0] | ((uint64_t)c16[1] << 16) | ((uint64_t)c16[2] << 32) | ((uint64_t)c16[3] << 48);
+    pw[1] = (uint64_t)c16[4] | ((uint64_t)c16[5] << 16) | ((uint64_t)c16[6] << 32) | ((uint64_t)c16[7] << 48);
+    pw[2] = (uint64_t)c16[8] | ((uint64_t)flags << 16) | (0xFFFFFFFFull << 32);
+  }
+  nodes = warp_sum(nodes); branch = warp_sum(branch); chain = warp_sum(chain);
+  if ((threadIdx.x & 31) == 0) { atomicAdd(&s_nodes, nodes); atomicAdd(&s_branch, branch); atomicAdd(&s_chain, chain); }
+  #pragma unroll
+  for (int f = 0; f < 16; ++f) {
+    unsigned long long h = warp_sum(hist[f]);
+    if ((threadIdx.x & 31) == 0 && h) atomicAdd(&s_hist[f], h);
+  }
+  __syncthreads();
+  if (threadIdx.x < 16 && s_hist[threadIdx.x]) atomicAdd(&a.ctr->flag_hist[threadIdx.x], s_hist[threadIdx.x]);
+  if (threadIdx.x == 0) {
+    atomicAdd(&a.ctr->n_nodes, s_nodes); atomicAdd(&a.ctr->n_branch, s_branch); atomicAdd(&a.ctr->n_chain, s_chain);
+  }
+}
+
+/* live graph nodes -> arrays */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_dump_nodes(const uint64_t *table, uint64_t nslots, uint64_t *keys,
+                                                     uint16_t *counts, uint8_t *flags, uint64_t cap,
+                                                     unsigned long long *n) {
+  constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t *s = table + i * SU;
+    KT key = KOps<KT>::load(s);
+    if (key_dead(key)) continue;
+    unsigned long long o = atomicAdd(n, 1ull);
+    if (o >= cap) continue;
+    KOps<KT>::store(keys + o * KWD, key);
+    const uint64_t *pw = s + KWD;
+    for (int q = 0; q < 4; ++q) {
+      counts[o * 9 + q] = (uint16_t)(pw[0] >> (16 * q));
+      counts[o * 9 + 4 + q] = (uint16_t)(pw[1] >> (16 * q));
+    }
+    counts[o * 9 + 8] = (uint16_t)pw[2];
+    if (flags) flags[o] = (uint8_t)(pw[2] >> 16);
+  }
+}
+
+/* ============================================================ scan */
+__global__ void __launch_bounds__(1024) k_scan_single(const uint64_t *in, uint64_t *out, uint64_t n,
+                                                       unsigned long long *total) {
+  __shared__ uint64_t part[1024];
+  const uint64_t per = (n + 1023) / 1024;
+  const uint64_t b = threadIdx.x * per, e = min(n, b + per);
+  uint64_t s = 0;
+  for (uint64_t i = b; i < e; ++i) s += in[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    uint64_t v = (threadIdx.x >= (unsigned)o) ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint64_t run = part[threadIdx.x] - s;
+  for (uint64_t i = b; i < e; ++i) { uint64_t v = in[i]; out[i] = run; run += v; }
+  if (threadIdx.x == 1023 && total) *total = part[1023];
+}
+
+int num_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+template <class KT>
+bruno_status count_typed(Ctx *c);
+template <class KT>
+bruno_status filter_typed(Ctx *c, const uint64_t *thr);
+
+}  // namespace
+
+void scan_u64(const uint64_t *in, uint64_t *out, uint64_t n, unsigned long long *total_dev, cudaStream_t s) {
+  k_scan_single<<<1, 1024, 0, s>>>(in, out, n, total_dev);
+}
+
+/* ------------------------------------------------------------ read index */
+bruno_status run_index_reads(Ctx *c) {
+  bruno_status st;
+  /* first pass: sizes for every segment */
+  uint64_t total_tiles = 0;
+  for (auto &sg : c->segs) total_tiles = std::max<uint64_t>(total_tiles, (sg.n + TILE - 1) / TILE);
+  if ((st = ensure(c, c->tile_cnt, std::max<uint64_t>(1, total_tiles) * 8)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->tile_base, std::max<uint64_t>(1, total_tiles) * 8)) != BRUNO_OK) return st;
+  /* the read arrays need the record count first; newline counts give an upper bound */
+  uint64_t rcap = 0;
+  for (size_t si = 0; si < c->segs.size(); ++si) {
+    const Segment &sg = c->segs[si];
+    if (sg.n == 0) continue;
+    const uint64_t tiles = (sg.n + TILE - 1) / TILE;
+    cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
+    long long neg = -1;
+    unsigned long long nb = ~0ull;
+    cudaMemcpyAsync(&c->dctr->last_nonws, &neg, sizeof(neg), cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(&c->dctr->bad_line, &nb, sizeof(nb), cudaMemcpyHostToDevice, c->stream);
+    c->launches += 3;
+    k_tile_stats<<<(unsigned)tiles, TPB, 0, c->stream>>>((const unsigned char *)sg.ptr, sg.n, (uint64_t *)c->tile_cnt.p,
+                                                          c->dctr);
+    scan_u64((const uint64_t *)c->tile_cnt.p, (uint64_t *)c->tile_base.p, tiles, &c->dctr->n_records, c->stream);
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    /* n_records temporarily holds the total newline count: records <= newlines / 4 + 1 */
+    const uint64_t upper = c->hctr->n_records / 4 + 1;
+    /* grow keeping the spans of earlier files */
+    if ((st = ensure(c, c->rstart, (rcap + upper) * 8, true)) != BRUNO_OK) return st;
+    if ((st = ensure(c, c->rend, (rcap + upper) * 8, true)) != BRUNO_OK) return st;
+    k_index_lines<<<(unsigned)tiles, TPB, 0, c->stream>>>((const unsigned char *)sg.ptr, sg.n,
+                                                           (const uint64_t *)c->tile_base.p, (uint64_t *)c->rstart.p,
+                                                           (uint64_t *)c->rend.p, rcap, rcap + upper, c->dctr);
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    const DevCounters &h = *c->hctr;
+    if (h.last_nonws < 0) continue;  /* empty or blank file */
+    const uint64_t lines = h.n_newlines_eff + 1;
+    if (h.bad_line != ~0ull || (lines & 3) != 0)
+      return set_err(c, BRUNO_ERR_BAD_INPUT, "malformed FASTQ in file " + std::to_string(si) + " near line " +
+                                                 std::to_string(h.bad_line != ~0ull ? h.bad_line : lines));
+    rcap += lines / 4;
+  }
+  c->n_reads = rcap;
+  return BRUNO_OK;
+}
+
+/* ------------------------------------------------------------ counting */
+namespace {
+template <class KT>
+bruno_status count_typed(Ctx *c) {
+  bruno_status st;
+  const int sms = num_sms();
+  const uint64_t nreads = c->n_reads;
+  /* distinct-count estimate -> slots */
+  uint64_t slots = c->cfg.table_slots;
+  cudaEventRecord(c->kev[0], c->stream);
+  if (slots == 0) {
+    const int hb = std::max(1, std::min<int>(sms * 2, (int)((nreads + 7) / 8)));
+    if ((st = ensure(c, c->blk_cnt, (size_t)hb * HLL_M)) != BRUNO_OK) return st;
+    k_hll<KT><<<hb, TPB, 0, c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k,
+                                         (uint8_t *)c->blk_cnt.p);
+    k_hll_merge<<<HLL_M / 256, 256, 0, c->stream>>>((const uint8_t *)c->blk_cnt.p, hb, c->dctr);
+    c->launches += 2;
+    if ((st = sync_counters(c, true)) != BRUNO_OK) return st;
+    double sum = 0; int zeros = 0;
+    for (int i = 0; i < HLL_M; ++i) { sum += std::ldexp(1.0, -(int)c->hctr->hll[i]); zeros += c->hctr->hll[i] == 0; }
+    const double m = HLL_M, alpha = 0.7213 / (1.0 + 1.079 / m);
+    double est = alpha * m * m / sum;
+    if (est <= 2.5 * m && zeros > 0) est = m * std::log(m / zeros);
+    const double load = c->cfg.max_load > 0 ? c->cfg.max_load : 0.5;
+    /* a k-mer with more than one slot's worth of biedges takes continuation slots */
+    slots = (uint64_t)(est * 1.04 / load) + 1024;
+  }
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    const size_t bytes = slots * Slot<KT>::U64 * 8;
+    if ((st = ensure(c, c->table, bytes)) != BRUNO_OK) return st;
+    c->nslots = slots;
+    cudaEventRecord(c->kev[1], c->stream);
+    k_table_init<KT><<<sms * 8, TPB, 0, c->stream>>>((uint64_t *)c->table.p, slots);
+    cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
+    cudaEventRecord(c->kev[2], c->stream);
+    CountArgs a{(const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k, (uint64_t *)c->table.p,
+                slots, 4096u, c->dctr};
+    const int grid = std::max(1, std::min<int>(sms * 8, (int)((nreads + 7) / 8)));
+    k_count<KT><<<grid, TPB, 0, c->stream>>>(a);
+    cudaEventRecord(c->kev[3], c->stream);
+    c->launches += 2;
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    float ms[3] = {0, 0, 0};
+    cudaEventElapsedTime(&ms[0], c->kev[0], c->kev[1]);
+    cudaEventElapsedTime(&ms[1], c->kev[1], c->kev[2]);
+    cudaEventElapsedTime(&ms[2], c->kev[2], c->kev[3]);
+    for (int q = 0; q < 3; ++q) c->phase_ms[6 + q] = ms[q];
+    if (!(c->hctr->err & DERR_TABLE_FULL)) {
+      c->n_instances = c->hctr->n_instances;
+      c->n_reads_used = c->hctr->n_reads_used;
+      c->n_entries = c->hctr->n_entries;
+      return BRUNO_OK;
+    }
+    slots *= 2;  /* the estimate was too low: grow and count again */
+  }
+  return set_err(c, BRUNO_ERR_TABLE_FULL, "k-mer table full after regrowth");
+}
+
+template <class KT>
+bruno_status dump_k2_typed(Ctx *c) {
+  bruno_status st;
+  const uint64_t n = c->n_entries;
+  if ((st = ensure(c, c->k2_keys, std::max<uint64_t>(1, n) * 8 * Slot<KT>::KEYW)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->k2_edges, std::max<uint64_t>(1, n))) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->k2_counts, std::max<uint64_t>(1, n) * 4)) != BRUNO_OK) return st;
+  cudaMemsetAsync(&c->dctr->n_k2_dump, 0, 8, c->stream);
+  c->launches += 1;
+  k_dump_k2<KT><<<num_sms() * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, (uint64_t *)c->k2_keys.p,
+                                                       (uint8_t *)c->k2_edges.p, (uint32_t *)c->k2_counts.p, n, c->dctr);
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  c->n_k2 = std::min<uint64_t>(n, c->hctr->n_k2_dump);
+  c->k2_dumped = true;
+  return BRUNO_OK;
+}
+
+template <class KT>
+bruno_status filter_typed(Ctx *c, const uint64_t *thr) {
+  bruno_status st;
+  FilterArgs a{};
+  a.table = (uint64_t *)c->table.p;
+  a.nslots = c->nslots;
+  a.k = c->cfg.k;
+  for (int i = 0; i < 6; ++i) a.t[i] = thr[i];
+  a.thresholding = c->cfg.thresholding;
+  a.max_probe = 4096u;
+  a.ctr = c->dctr;
+  if (c->cfg.keep_filtered) {
+    const uint64_t n = std::max<uint64_t>(1, c->n_entries);
+    if ((st = ensure(c, c->f_keys, n * 8 * Slot<KT>::KEYW)) != BRUNO_OK) return st;
+    if ((st = ensure(c, c->f_edges, n)) != BRUNO_OK) return st;
+    if ((st = ensure(c, c->f_counts, n * 4)) != BRUNO_OK) return st;
+    a.f_keys = (uint64_t *)c->f_keys.p; a.f_edges = (uint8_t *)c->f_edges.p; a.f_counts = (uint32_t *)c->f_counts.p;
+    a.f_cap = n;
+  }
+  cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
+  k_filter<KT><<<num_sms() * 8, TPB, 0, c->stream>>>(a);
+  c->launches += 1;
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  const DevCounters &h = *c->hctr;
+  c->n_nodes = h.n_nodes; c->n_branch = h.n_branch; c->n_chain = h.n_chain;
+  c->n_filtered = std::min<uint64_t>(h.n_filtered, a.f_cap);
+  for (int f = 0; f < 16; ++f) c->flag_hist[f] = h.flag_hist[f];
+  return BRUNO_OK;
+}
+}  // namespace
+
+bruno_status run_count(Ctx *c) { return c->W == 1 ? count_typed<KW1>(c) : count_typed<KW2>(c); }
+bruno_status run_dump_k2(Ctx *c) { return c->W == 1 ? dump_k2_typed<KW1>(c) : dump_k2_typed<KW2>(c); }
+bruno_status run_filter(Ctx *c, const uint64_t *thresh) {
+  return c->W == 1 ? filter_typed<KW1>(c, thresh) : filter_typed<KW2>(c, thresh);
+}
+
+bruno_status run_copy_nodes(Ctx *c, uint64_t *keys, uint16_t *counts, uint8_t *flags, size_t cap, size_t *n) {
+  bruno_status st;
+  *n = c->n_nodes;
+  if (!keys && !counts && !flags) return BRUNO_OK;
+  if (cap < c->n_nodes) return set_err(c, BRUNO_ERR_CAPACITY, "node buffers too small");
+  const uint64_t nn = std::max<uint64_t>(1, c->n_nodes);
+  Buf dk, dc, df;
+  if ((st = ensure(c, dk, nn * 8 * c->W)) != BRUNO_OK) return st;
+  if ((st = ensure(c, dc, nn * 18)) != BRUNO_OK) return st;
+  if ((st = ensure(c, df, nn)) != BRUNO_OK) return st;
+  cudaMemsetAsync(&c->dctr->n_k2_dump, 0, 8, c->stream);
+  if (c->W == 1)
+    k_dump_nodes<KW1><<<num_sms() * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, (uint64_t *)dk.p,
+                                                            (uint16_t *)dc.p, (uint8_t *)df.p, nn, &c->dctr->n_k2_dump);
+  else
+    k_dump_nodes<KW2><<<num_sms() * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, (uint64_t *)dk.p,
+                                                            (uint16_t *)dc.p, (uint8_t *)df.p, nn, &c->dctr->n_k2_dump);
+  bruno_status r = BRUNO_OK;
+  if (keys) r = cuda_check(c, cudaMemcpyAsync(keys, dk.p, c->n_nodes * 8 * c->W, cudaMemcpyDeviceToHost, c->stream), "copy");
+  if (r == BRUNO_OK && counts)
+    r = cuda_check(c, cudaMemcpyAsync(counts, dc.p, c->n_nodes * 18, cudaMemcpyDeviceToHost, c->stream), "copy");
+  if (r == BRUNO_OK && flags)
+    r = cuda_check(c, cudaMemcpyAsync(flags, df.p, c->n_nodes, cudaMemcpyDeviceToHost, c->stream), "copy");
+  if (r == BRUNO_OK) r = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  cudaFree(dk.p); cudaFree(dc.p); cudaFree(df.p);
+  return r;
+}
+
+}  // namespace bg

@@ -1,0 +1,362 @@
+/*
+ * capi.cu -- the C ABI (include/bruno_gb300.h): context lifetime, device memory, the
+ * pipeline state machine and the copy-outs.  All device work is stream-ordered on the
+ * context's stream; the host synchronises only to read small counters between phases.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstddef>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "internal.cuh"
+
+namespace bg {
+
+bruno_status set_err(Ctx *c, bruno_status s, const std::string &msg) {
+  if (c) c->err = msg;
+  return s;
+}
+
+bruno_status cuda_check(Ctx *c, cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return BRUNO_OK;
+  return set_err(c, e == cudaErrorMemoryAllocation ? BRUNO_ERR_OOM : BRUNO_ERR_CUDA,
+                 std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bruno_status ensure(Ctx *c, Buf &b, size_t bytes, bool preserve) {
+  if (bytes <= b.bytes && b.p) return BRUNO_OK;
+  void *p = nullptr;
+  size_t want = std::max(bytes, (size_t)256);
+  cudaError_t e = cudaMalloc(&p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(c, BRUNO_ERR_OOM, "cudaMalloc of " + std::to_string(want) + " bytes failed");
+  }
+  if (preserve && b.p && b.bytes) cudaMemcpyAsync(p, b.p, b.bytes, cudaMemcpyDeviceToDevice, c->stream);
+  if (b.p) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(b.p);
+  }
+  b.p = p;
+  b.bytes = want;
+  return BRUNO_OK;
+}
+
+static void release(Buf &b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+bruno_status sync_counters(Ctx *c, bool with_hll) {
+  const size_t n = with_hll ? sizeof(DevCounters) : offsetof(DevCounters, hll);
+  cudaError_t e = cudaMemcpyAsync(c->hctr, c->dctr, n, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  return cuda_check(c, e, "device phase");
+}
+
+static void record(Ctx *c, int i) { cudaEventRecord(c->ev[i], c->stream); }
+static double elapsed(Ctx *c, int a, int b) {
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, c->ev[a], c->ev[b]) != cudaSuccess) { cudaGetLastError(); return 0; }
+  return ms;
+}
+
+}  // namespace bg
+
+using namespace bg;
+
+struct bruno_ctx : public Ctx {};
+
+extern "C" {
+
+bruno_status bruno_ctx_create(const bruno_cfg *cfg, bruno_ctx **out) {
+  if (!cfg || !out) return BRUNO_ERR_ARG;
+  *out = nullptr;
+  if (cfg->k < 3 || cfg->k > 63) return BRUNO_ERR_ARG;
+  bruno_ctx *c = new (std::nothrow) bruno_ctx();
+  if (!c) return BRUNO_ERR_OOM;
+  c->cfg = *cfg;
+  c->W = cfg->k <= 31 ? 1 : 2;
+  bruno_status st = cuda_check(c, cudaSetDevice(cfg->device), "cudaSetDevice");
+  if (st == BRUNO_OK) st = cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
+  c->own_stream = true;
+  if (st == BRUNO_OK) st = cuda_check(c, cudaMalloc(&c->dctr, sizeof(DevCounters)), "counters");
+  if (st == BRUNO_OK) st = cuda_check(c, cudaMallocHost(&c->hctr, sizeof(DevCounters)), "pinned counters");
+  for (int i = 0; i < 8 && st == BRUNO_OK; ++i) st = cuda_check(c, cudaEventCreate(&c->ev[i]), "event");
+  for (int i = 0; i < 4 && st == BRUNO_OK; ++i) st = cuda_check(c, cudaEventCreate(&c->kev[i]), "event");
+  if (st != BRUNO_OK) { bruno_ctx_destroy(c); return st; }
+  cudaMemsetAsync(c->dctr, 0, sizeof(DevCounters), c->stream);
+  *out = c;
+  return BRUNO_OK;
+}
+
+bruno_status bruno_ctx_destroy(bruno_ctx *c) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  Buf *bufs[] = {&c->rstart, &c->rend, &c->tile_cnt, &c->tile_base, &c->table, &c->k2_keys, &c->k2_edges, &c->k2_counts,
+                 &c->f_keys, &c->f_edges, &c->f_counts, &c->blk_cnt, &c->blk_base, &c->ckey, &c->cslot, &c->cedge,
+                 &c->cstate, &c->pend, &c->pay, &c->unf0, &c->unf1, &c->removed, &c->r_K, &c->r_rep, &c->r_dist,
+                 &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars};
+  for (Buf *b : bufs) release(*b);
+  for (Buf &b : c->seg_bufs) release(b);
+  if (c->dctr) cudaFree(c->dctr);
+  if (c->hctr) cudaFreeHost(c->hctr);
+  for (int i = 0; i < 8; ++i) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  for (int i = 0; i < 4; ++i) if (c->kev[i]) cudaEventDestroy(c->kev[i]);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return BRUNO_OK;
+}
+
+bruno_status bruno_set_stream(bruno_ctx *c, void *stream) {
+  if (!c) return BRUNO_ERR_ARG;
+  cudaStreamSynchronize(c->stream);
+  if (stream) {
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    c->stream = (cudaStream_t)stream;
+    c->own_stream = false;
+  } else if (!c->own_stream) {
+    bruno_status st = cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
+    if (st != BRUNO_OK) return st;
+    c->own_stream = true;
+  }
+  return BRUNO_OK;
+}
+
+const char *bruno_last_error(const bruno_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+bruno_status bruno_reset(bruno_ctx *c) {
+  if (!c) return BRUNO_ERR_ARG;
+  c->segs.clear();
+  c->stage = 0;
+  c->n_reads = c->n_reads_used = c->n_instances = c->n_entries = 0;
+  c->n_k2 = c->n_filtered = 0;
+  c->k2_dumped = false;
+  c->n_nodes = c->n_branch = c->n_chain = 0;
+  c->iterations = c->n_cycle = c->n_isolated = c->multi = 0;
+  c->n_ranked = c->n_heads = c->n_chain_chars = 0;
+  c->chains_clean = true;
+  c->launches = 0;
+  std::memset(c->flag_hist, 0, sizeof(c->flag_hist));
+  std::memset(c->phase_ms, 0, sizeof(c->phase_ms));
+  c->err.clear();
+  return BRUNO_OK;
+}
+
+bruno_status bruno_load_fastq(bruno_ctx *c, const char *buf, size_t nbytes, int32_t is_device) {
+  if (!c || (!buf && nbytes)) return BRUNO_ERR_ARG;
+  if (c->stage > 1) return set_err(c, BRUNO_ERR_ARG, "load_fastq after counting; call bruno_reset first");
+  if (is_device) {
+    c->segs.push_back({buf, nbytes});
+  } else {
+    const size_t i = c->segs.size();
+    if (c->seg_bufs.size() <= i) c->seg_bufs.resize(i + 1);
+    bruno_status st = ensure(c, c->seg_bufs[i], nbytes + 1);
+    if (st != BRUNO_OK) return st;
+    st = cuda_check(c, cudaMemcpyAsync(c->seg_bufs[i].p, buf, nbytes, cudaMemcpyHostToDevice, c->stream), "H2D FASTQ");
+    if (st != BRUNO_OK) return st;
+    c->segs.push_back({(const char *)c->seg_bufs[i].p, nbytes});
+  }
+  c->stage = 1;
+  return BRUNO_OK;
+}
+
+bruno_status bruno_compute_biedge_freqencies(bruno_ctx *c) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (c->stage != 1) return set_err(c, BRUNO_ERR_ARG, "compute_biedge_freqencies needs loaded FASTQ");
+  record(c, 0);
+  bruno_status st = run_index_reads(c);
+  if (st != BRUNO_OK) return st;
+  record(c, 1);
+  st = run_count(c);
+  if (st != BRUNO_OK) return st;
+  record(c, 2);
+  if (c->cfg.keep_k2 && (st = run_dump_k2(c)) != BRUNO_OK) return st;
+  cudaEventSynchronize(c->ev[2]);
+  c->phase_ms[0] = elapsed(c, 0, 1);
+  c->phase_ms[1] = elapsed(c, 1, 2);
+  c->stage = 2;
+  return BRUNO_OK;
+}
+
+bruno_status bruno_local_insert_by_freqencies(bruno_ctx *c, const uint64_t *thresh) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (c->stage != 2) return set_err(c, BRUNO_ERR_ARG, "local_insert_by_freqencies needs counted (k+2)-mers");
+  record(c, 2);
+  bruno_status st = run_filter(c, thresh ? thresh : c->cfg.thresh);
+  if (st != BRUNO_OK) return st;
+  record(c, 3);
+  cudaEventSynchronize(c->ev[3]);
+  c->phase_ms[2] = elapsed(c, 2, 3);
+  c->stage = 3;
+  return BRUNO_OK;
+}
+
+bruno_status bruno_extract_chains(bruno_ctx *c) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (c->stage != 3) return set_err(c, BRUNO_ERR_ARG, "extract_chains needs the filtered graph");
+  record(c, 3);
+  bruno_status st = run_extract_chains(c);
+  if (st != BRUNO_OK) return st;
+  record(c, 4);
+  cudaEventSynchronize(c->ev[4]);
+  c->phase_ms[3] = elapsed(c, 3, 4);
+  c->stage = 4;
+  return BRUNO_OK;
+}
+
+bruno_status bruno_list_rank(bruno_ctx *c, int32_t min_update, uint64_t *iterations) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (c->stage != 4) return set_err(c, BRUNO_ERR_ARG, "list_rank needs extracted chains");
+  record(c, 4);
+  bruno_status st = run_list_rank(c, min_update);
+  if (st != BRUNO_OK) return st;
+  record(c, 5);
+  cudaEventSynchronize(c->ev[5]);
+  c->phase_ms[4] = elapsed(c, 4, 5);
+  if (iterations) *iterations = c->iterations;
+  c->stage = 5;
+  return BRUNO_OK;
+}
+
+bruno_status bruno_to_compressed_chains(bruno_ctx *c) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (c->stage != 5) return set_err(c, BRUNO_ERR_ARG, "to_compressed_chains needs ranked chains");
+  record(c, 5);
+  bruno_status st = run_compress(c);
+  if (st != BRUNO_OK) return st;
+  record(c, 6);
+  cudaEventSynchronize(c->ev[6]);
+  c->phase_ms[5] = elapsed(c, 5, 6);
+  c->stage = 6;
+  if (!c->chains_clean)
+    return set_err(c, BRUNO_ERR_INVARIANT,
+                   "chain pointers are not mutually consistent (asymmetric edge filtering); the listranked "
+                   "nodes are valid, the compacted sequences are not");
+  return BRUNO_OK;
+}
+
+bruno_status bruno_build_and_compact(bruno_ctx *c, const char *buf, size_t nbytes, int32_t is_device) {
+  if (!c) return BRUNO_ERR_ARG;
+  bruno_status st = bruno_reset(c);
+  if (st == BRUNO_OK) st = bruno_load_fastq(c, buf, nbytes, is_device);
+  if (st == BRUNO_OK) st = bruno_compute_biedge_freqencies(c);
+  if (st == BRUNO_OK) st = bruno_local_insert_by_freqencies(c, nullptr);
+  if (st == BRUNO_OK) st = bruno_extract_chains(c);
+  if (st == BRUNO_OK) st = bruno_list_rank(c, c->cfg.min_update, nullptr);
+  if (st == BRUNO_OK) st = bruno_to_compressed_chains(c);
+  return st;
+}
+
+bruno_status bruno_get_sizes(bruno_ctx *c, bruno_sizes *o) {
+  if (!c || !o) return BRUNO_ERR_ARG;
+  std::memset(o, 0, sizeof(*o));
+  o->n_reads = c->n_reads;
+  o->n_reads_used = c->n_reads_used;
+  o->n_instances = c->n_instances;
+  o->n_k2 = c->n_entries;
+  o->n_filtered = c->n_filtered;
+  o->n_nodes = c->n_nodes;
+  o->n_branch = c->n_branch;
+  o->n_chain_nodes = c->n_chain;
+  o->iterations = c->iterations;
+  o->n_cycle_nodes = c->n_cycle;
+  o->n_isolated = c->n_isolated;
+  o->n_ranked = c->n_ranked;
+  o->n_chains = c->n_heads;
+  o->n_chain_chars = c->n_chain_chars;
+  o->table_slots = c->nslots;
+  o->collisions = c->multi;
+  o->launches = c->launches;
+  for (int f = 0; f < 16; ++f) o->filter_flag_hist[f] = c->flag_hist[f];
+  return BRUNO_OK;
+}
+
+static bruno_status copy_d2h(Ctx *c, void *dst, const void *src, size_t bytes) {
+  if (!dst || !bytes) return BRUNO_OK;
+  return cuda_check(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream), "D2H copy");
+}
+
+static bruno_status copy_triple(Ctx *c, uint64_t n, const Buf &k, const Buf &e, const Buf &cnt, uint64_t *keys,
+                                uint8_t *edges, uint32_t *counts, size_t cap, size_t *out_n) {
+  if (out_n) *out_n = n;
+  if (!keys && !edges && !counts) return BRUNO_OK;
+  if (cap < n) return set_err(c, BRUNO_ERR_CAPACITY, "copy buffer too small");
+  bruno_status st = copy_d2h(c, keys, k.p, n * 8 * c->W);
+  if (st == BRUNO_OK) st = copy_d2h(c, edges, e.p, n);
+  if (st == BRUNO_OK) st = copy_d2h(c, counts, cnt.p, n * 4);
+  if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  return st;
+}
+
+bruno_status bruno_copy_k2(bruno_ctx *c, uint64_t *keys, uint8_t *edges, uint32_t *counts, size_t cap, size_t *n) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (!c->k2_dumped) return set_err(c, BRUNO_ERR_ARG, "raw (k+2)-mer counts need cfg.keep_k2 and a counted build");
+  return copy_triple(c, c->n_k2, c->k2_keys, c->k2_edges, c->k2_counts, keys, edges, counts, cap, n);
+}
+
+bruno_status bruno_copy_filtered(bruno_ctx *c, uint64_t *keys, uint8_t *edges, uint32_t *counts, size_t cap, size_t *n) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (!c->cfg.keep_filtered || c->stage < 3) return set_err(c, BRUNO_ERR_ARG, "filtered entries need cfg.keep_filtered");
+  return copy_triple(c, c->n_filtered, c->f_keys, c->f_edges, c->f_counts, keys, edges, counts, cap, n);
+}
+
+bruno_status bruno_copy_nodes(bruno_ctx *c, uint64_t *keys, uint16_t *counts, uint8_t *flags, size_t cap, size_t *n) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (c->stage < 3) return set_err(c, BRUNO_ERR_ARG, "nodes exist after local_insert_by_freqencies");
+  return run_copy_nodes(c, keys, counts, flags, cap, n);
+}
+
+bruno_status bruno_copy_ranked(bruno_ctx *c, uint64_t *K, uint64_t *rep, int32_t *dist, size_t cap, size_t *n) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (c->stage < 6) return set_err(c, BRUNO_ERR_ARG, "ranked nodes exist after to_compressed_chains");
+  if (n) *n = c->n_ranked;
+  if (!K && !rep && !dist) return BRUNO_OK;
+  if (cap < c->n_ranked) return set_err(c, BRUNO_ERR_CAPACITY, "copy buffer too small");
+  bruno_status st = copy_d2h(c, K, c->r_K.p, c->n_ranked * 8 * c->W);
+  if (st == BRUNO_OK) st = copy_d2h(c, rep, c->r_rep.p, c->n_ranked * 8 * c->W);
+  if (st == BRUNO_OK) st = copy_d2h(c, dist, c->r_dist.p, c->n_ranked * 4);
+  if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  return st;
+}
+
+bruno_status bruno_copy_chains(bruno_ctx *c, uint64_t *reps, uint64_t *offsets, char *chars, size_t cap_chains,
+                               size_t cap_chars, size_t *n_chains, size_t *n_chars) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (c->stage < 6) return set_err(c, BRUNO_ERR_ARG, "chains exist after to_compressed_chains");
+  if (n_chains) *n_chains = c->n_heads;
+  if (n_chars) *n_chars = c->n_chain_chars;
+  if (!reps && !offsets && !chars) return BRUNO_OK;
+  if ((reps || offsets) && cap_chains < c->n_heads) return set_err(c, BRUNO_ERR_CAPACITY, "chain buffer too small");
+  if (chars && cap_chars < c->n_chain_chars) return set_err(c, BRUNO_ERR_CAPACITY, "char buffer too small");
+  bruno_status st = copy_d2h(c, reps, c->ch_rep.p, c->n_heads * 8 * c->W);
+  if (st == BRUNO_OK) st = copy_d2h(c, offsets, c->head_off.p, (c->n_heads + 1) * 8);
+  if (st == BRUNO_OK) st = copy_d2h(c, chars, c->ch_chars.p, c->n_chain_chars);
+  if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  return st;
+}
+
+bruno_status bruno_host_alloc(size_t bytes, void **out) {
+  if (!out) return BRUNO_ERR_ARG;
+  *out = nullptr;
+  cudaError_t e = cudaMallocHost(out, std::max<size_t>(bytes, 1));
+  if (e != cudaSuccess) { cudaGetLastError(); return BRUNO_ERR_OOM; }
+  return BRUNO_OK;
+}
+
+bruno_status bruno_host_free(void *p) {
+  if (p && cudaFreeHost(p) != cudaSuccess) { cudaGetLastError(); return BRUNO_ERR_CUDA; }
+  return BRUNO_OK;
+}
+
+bruno_status bruno_phase_ms(bruno_ctx *c, double *ms, size_t n) {
+  if (!c || !ms) return BRUNO_ERR_ARG;
+  for (size_t i = 0; i < n && i < 9; ++i) ms[i] = c->phase_ms[i];
+  return BRUNO_OK;
+}
+}  // extern "C"

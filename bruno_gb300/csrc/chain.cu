@@ -1,0 +1,614 @@
+/*
+ * chain.cu -- graph nodes -> chain map -> list ranking -> compacted chains.
+ *
+ *  k_chain_count/assign  dense chain indices for IsChainNode nodes, in slot order
+ *  k_chain_init          to_simple_biedge (debruijn_chain_node.hpp:83-111): neighbours are
+ *                        resolved once to chain indices (+ strand flip), so ranking never
+ *                        hashes k-mers again
+ *  k_termini             setup_chain_termini (debruijn_chain_graph.hpp:485-596) with
+ *                        terminus_update (debruijn_chain_operations.hpp:57-93)
+ *  k_lr_*                list_rank_min_update / list_rank (debruijn_chain_graph.hpp:793-1310):
+ *                        round-synchronous pointer jumping with the reference's update rule
+ *                        chain_update (debruijn_chain_operations.hpp:107-256).  Updates that
+ *                        meet at one (node, side) in a round are reduced to the one with the
+ *                        largest (distance, terminal mark); for the reference's chains this
+ *                        equals applying them one after another in any order.
+ *  k_separate            separate_cycles(iterations) and separate_isolated (:670-777)
+ *  k_ranked / k_fill     to_listranked_chain_node (debruijn_chain_operations.hpp:260-309) and
+ *                        to_compressed_chains (debruijn_chain_graph.hpp:1778-1856): every
+ *                        chain is one head node with distance 0 plus one base per node, so
+ *                        the sequence is scattered straight to its offset, no sort.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "internal.cuh"
+
+namespace bg {
+
+namespace {
+
+constexpr int TPB = 256;
+constexpr int CHS = TPB * 16;           /* slots per block in the chain-index passes */
+constexpr uint32_t DM = 0x7FFFFFFFu;    /* dist_mask (debruijn_chain_node.hpp:53) */
+constexpr uint32_t TM = 0x80000000u;    /* term_mask */
+constexpr uint32_t NONE32 = 0xFFFFFFFFu;
+
+__device__ __forceinline__ bool ptcn(uint32_t x) { return (x ^ TM) > TM; }       /* points_to_chain_node */
+__device__ __forceinline__ bool term(uint32_t x) { return (x & DM) == 0; }       /* is_chain_terminal */
+
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(~0u, v, o);
+  return v;
+}
+
+__device__ __forceinline__ uint32_t block_exscan(uint32_t v, uint32_t &total) {
+  __shared__ uint32_t ws[TPB / 32 + 1];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(~0u, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[w] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (int i = 0; i < TPB / 32; ++i) { uint32_t t = ws[i]; ws[i] = run; run += t; }
+    ws[TPB / 32] = run;
+  }
+  __syncthreads();
+  const uint32_t r = ws[w] + x - v;
+  total = ws[TPB / 32];
+  __syncthreads();
+  return r;
+}
+
+/* warp-aggregated append: returns this lane's slot in `list` (valid lanes only) */
+__device__ __forceinline__ unsigned long long warp_append(bool want, unsigned long long *counter) {
+  const unsigned m = __ballot_sync(~0u, want);
+  if (!m) return 0;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(m));
+  base = __shfl_sync(~0u, base, leader);
+  return base + __popc(m & ((1u << lane) - 1));
+}
+
+template <class KT>
+__device__ __forceinline__ bool slot_dead(const uint64_t *s) {
+  return (s[Slot<KT>::KEYW - 1] & KEY_DEAD_BIT) != 0;
+}
+template <class KT>
+__device__ __forceinline__ uint32_t slot_flags(const uint64_t *s) {
+  return (uint32_t)(s[Slot<KT>::KEYW + 2] >> 16) & 0xFFFFu;
+}
+template <class KT>
+__device__ __forceinline__ uint32_t slot_aux(const uint64_t *s) {
+  return (uint32_t)(s[Slot<KT>::KEYW + 2] >> 32);
+}
+
+/* slot index of a live node with canonical key x, -1 if absent */
+template <class KT>
+__device__ __forceinline__ long long table_find(const uint64_t *table, uint64_t nslots, uint32_t max_probe, KT x) {
+  constexpr int SU = Slot<KT>::U64;
+  uint64_t i = __umul64hi(KOps<KT>::hash(x), nslots);
+  for (uint32_t p = 0; p < max_probe; ++p) {
+    const uint64_t *s = table + i * SU;
+    KT key = KOps<KT>::load(s);
+    if (KOps<KT>::eq(key, x)) return (long long)i;
+    if (Slot<KT>::KEYW == 1 ? (((uint64_t *)&key)[0] == KEY_EMPTY) : (((uint64_t *)&key)[1] == KEY_EMPTY && ((uint64_t *)&key)[0] == KEY_EMPTY))
+      return -1;
+    if (++i == nslots) i = 0;
+  }
+  return -1;
+}
+
+/* ================================================================ chain indices */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_chain_count(const uint64_t *table, uint64_t nslots, uint64_t *blk_cnt) {
+  constexpr int SU = Slot<KT>::U64;
+  const uint64_t b0 = (uint64_t)blockIdx.x * CHS;
+  unsigned long long c = 0;
+  for (int j = 0; j < 16; ++j) {
+    const uint64_t i = b0 + (uint64_t)j * TPB + threadIdx.x;
+    if (i < nslots) {
+      const uint64_t *s = table + i * SU;
+      c += !slot_dead<KT>(s) && (slot_flags<KT>(s) & NF_CHAIN);
+    }
+  }
+  __shared__ unsigned long long sc[TPB / 32];
+  c = warp_sum(c);
+  if ((threadIdx.x & 31) == 0) sc[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int i = 0; i < TPB / 32; ++i) t += sc[i];
+    blk_cnt[blockIdx.x] = t;
+  }
+}
+
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_chain_assign(uint64_t *table, uint64_t nslots, const uint64_t *blk_base,
+                                                       uint64_t *ckey, uint64_t *cslot) {
+  constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
+  const uint64_t b0 = (uint64_t)blockIdx.x * CHS;
+  uint64_t run = blk_base[blockIdx.x];
+  for (int j = 0; j < 16; ++j) {
+    const uint64_t i = b0 + (uint64_t)j * TPB + threadIdx.x;
+    bool is = false;
+    uint64_t *s = nullptr;
+    if (i < nslots) {
+      s = table + i * SU;
+      is = !slot_dead<KT>(s) && (slot_flags<KT>(s) & NF_CHAIN);
+    }
+    uint32_t tot;
+    const uint32_t r = block_exscan(is ? 1u : 0u, tot);
+    if (is) {
+      const uint64_t idx = run + r;
+      for (int w = 0; w < KWD; ++w) ckey[idx * KWD + w] = s[w];
+      cslot[idx] = i;
+      s[KWD + 2] = (s[KWD + 2] & 0xFFFFFFFFull) | (idx << 32);
+    }
+    run += tot;
+  }
+}
+
+/* ================================================================ chain init */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, uint64_t nslots, int k, const uint64_t *ckey,
+                                                     const uint64_t *cslot, uint64_t M, ChainState *cs, uint8_t *cedge,
+                                                     uint32_t max_probe) {
+  constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (uint64_t)gridDim.x * blockDim.x) {
+    const KT K = KOps<KT>::load(ckey + i * KWD);
+    const uint64_t *pw = table + cslot[i] * SU + KWD;
+    int inc = -1, outc = -1;
+    for (int c = 0; c < 4; ++c) {
+      if ((pw[0] >> (16 * c)) & 0xFFFFu) outc = c;
+      if ((pw[1] >> (16 * c)) & 0xFFFFu) inc = c;
+    }
+    ChainState st;
+    st.pad = 0;
+    if (inc >= 0) {  /* in neighbour: nextReverseFromChar(c) */
+      KT n = KOps<KT>::prepend((unsigned)inc, K, k), y = KOps<KT>::rc(n, k);
+      const bool flip = !KOps<KT>::lt(n, y);
+      const long long j = table_find<KT>(table, nslots, max_probe, flip ? y : n);
+      if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN))
+        st.inP = (uint64_t)slot_aux<KT>(table + j * SU) | (flip ? PF_FLIP : 0);
+      else
+        st.inP = PF_EXT | i;
+      st.inD = 1;
+    } else {
+      st.inP = PF_BLANK; st.inD = TM;
+    }
+    if (outc >= 0) {  /* out neighbour: nextFromChar(c) */
+      KT n = KOps<KT>::append(K, (unsigned)outc, k), y = KOps<KT>::rc(n, k);
+      const bool flip = !KOps<KT>::lt(n, y);
+      const long long j = table_find<KT>(table, nslots, max_probe, flip ? y : n);
+      if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN))
+        st.outP = (uint64_t)slot_aux<KT>(table + j * SU) | (flip ? PF_FLIP : 0);
+      else
+        st.outP = PF_EXT | PF_EXTOUT | i;
+      st.outD = 1;
+    } else {
+      st.outP = PF_BLANK; st.outD = TM;
+    }
+    cs[i] = st;
+    cedge[i] = (uint8_t)((inc >= 0 ? (4 | inc) : 0) | (outc >= 0 ? (32 | (outc << 3)) : 0));
+  }
+}
+
+/* neighbours of branch nodes get their facing side set to branch_neighbor (0) */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_termini(const uint64_t *table, uint64_t nslots, int k, ChainState *cs,
+                                                  uint32_t max_probe) {
+  constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t *s = table + i * SU;
+    if (slot_dead<KT>(s) || !(slot_flags<KT>(s) & NF_BRANCH)) continue;
+    const KT K = KOps<KT>::load(s);
+    const uint64_t *pw = s + KWD;
+    for (int c = 0; c < 4; ++c) {
+      if ((pw[0] >> (16 * c)) & 0xFFFFu) {  /* out neighbour receives (branch, IN) */
+        KT n = KOps<KT>::append(K, (unsigned)c, k), y = KOps<KT>::rc(n, k);
+        const bool flip = !KOps<KT>::lt(n, y);
+        const long long j = table_find<KT>(table, nslots, max_probe, flip ? y : n);
+        if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN)) {
+          const uint32_t idx = slot_aux<KT>(table + j * SU);
+          if (flip) cs[idx].outD = 0; else cs[idx].inD = 0;
+        }
+      }
+      if ((pw[1] >> (16 * c)) & 0xFFFFu) {  /* in neighbour receives (branch, OUT) */
+        KT n = KOps<KT>::prepend((unsigned)c, K, k), y = KOps<KT>::rc(n, k);
+        const bool flip = !KOps<KT>::lt(n, y);
+        const long long j = table_find<KT>(table, nslots, max_probe, flip ? y : n);
+        if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN)) {
+          const uint32_t idx = slot_aux<KT>(table + j * SU);
+          if (flip) cs[idx].inD = 0; else cs[idx].outD = 0;
+        }
+      }
+    }
+  }
+}
+
+/* ================================================================ list ranking */
+struct Upd { uint32_t t; int side; uint64_t P; uint32_t D; };  /* side 0 = in, 1 = out */
+
+/* The updates node x sends this round (debruijn_chain_graph.hpp:1107-1142 for min_update,
+ * :857-895 otherwise), already put on the target's canonical strand as lex_less does
+ * (debruijn_chain_operations.hpp:500-504).  Targets outside the chain map are dropped. */
+__device__ __forceinline__ int make_updates(uint32_t x, const ChainState &st, int min_update, Upd u[2]) {
+  int n = 0;
+  const uint32_t l = st.inD, r = st.outD, dist = (l & DM) + (r & DM);
+  const bool send_l = min_update ? ptcn(l) : !term(l);
+  const bool send_r = min_update ? ptcn(r) : !term(r);
+  if (send_l && !(st.inP & (PF_EXT | PF_BLANK))) {
+    uint64_t P = term(r) ? (uint64_t)x : st.outP;
+    int side = 1;  /* OUT */
+    if (st.inP & PF_FLIP) { P ^= PF_FLIP; side = 0; }
+    u[n++] = {(uint32_t)st.inP, side, P, ptcn(r) ? dist : (dist | TM)};
+  }
+  if (send_r && !(st.outP & (PF_EXT | PF_BLANK))) {
+    uint64_t P = term(l) ? (uint64_t)x : st.inP;
+    int side = 0;  /* IN */
+    if (st.outP & PF_FLIP) { P ^= PF_FLIP; side = 1; }
+    u[n++] = {(uint32_t)st.outP, side, P, ptcn(l) ? dist : (dist | TM)};
+  }
+  return n;
+}
+__device__ __forceinline__ unsigned long long upd_key(uint32_t x, uint32_t D) {
+  const uint64_t rank = ((uint64_t)(D & DM) << 1) | (D >> 31);
+  return (rank << 32) | x;
+}
+
+__global__ void __launch_bounds__(TPB) k_lr_init(const ChainState *cs, uint64_t M, uint32_t *unf, unsigned long long *n) {
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < M; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    bool u = false;
+    if (i < M) u = ptcn(cs[i].inD) || ptcn(cs[i].outD);
+    const unsigned long long o = warp_append(u, n);
+    if (u) unf[o] = (uint32_t)i;
+  }
+}
+
+__global__ void __launch_bounds__(TPB) k_lr_propose(const ChainState *cs, const uint32_t *unf, uint64_t nu, int min_update,
+                                                     unsigned long long *pend, DevCounters *ctr) {
+  unsigned long long multi = 0;
+  for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nu; q += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t x = unf[q];
+    const ChainState st = cs[x];
+    Upd u[2];
+    const int n = make_updates(x, st, min_update, u);
+    for (int j = 0; j < n; ++j) {
+      const unsigned long long old = atomicMax(&pend[2ull * u[j].t + u[j].side], upd_key(x, u[j].D));
+      multi += old != 0;
+    }
+  }
+  multi = warp_sum(multi);
+  if ((threadIdx.x & 31) == 0 && multi) atomicAdd(&ctr->lr_multi, multi);
+}
+
+__global__ void __launch_bounds__(TPB) k_lr_commit(const ChainState *cs, const uint32_t *unf, uint64_t nu, int min_update,
+                                                    unsigned long long *pend, Payload *pay) {
+  for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nu; q += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t x = unf[q];
+    const ChainState st = cs[x];
+    Upd u[2];
+    const int n = make_updates(x, st, min_update, u);
+    for (int j = 0; j < n; ++j) {
+      const uint64_t slot = 2ull * u[j].t + u[j].side;
+      if (pend[slot] != upd_key(x, u[j].D)) continue;   /* another update won this side */
+      const uint32_t tD = u[j].side ? cs[u[j].t].outD : cs[u[j].t].inD;
+      if (ptcn(tD)) pay[slot] = Payload{u[j].P, u[j].D, 0};
+      else pend[slot] = 0;                                /* chain_update ignores it */
+    }
+  }
+}
+
+__global__ void __launch_bounds__(TPB) k_lr_apply(ChainState *cs, const uint32_t *unf, uint64_t nu,
+                                                   unsigned long long *pend, const Payload *pay, uint32_t maxd,
+                                                   uint32_t *next, DevCounters *ctr) {
+  unsigned long long applied = 0, cycles = 0;
+  for (uint64_t q0 = (uint64_t)blockIdx.x * blockDim.x; q0 < nu; q0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t q = q0 + threadIdx.x;
+    bool keep = false;
+    uint32_t x = 0;
+    if (q < nu) {
+      x = unf[q];
+      ChainState st = cs[x];
+      bool dirty = false;
+      for (int side = 0; side < 2; ++side) {
+        const uint64_t slot = 2ull * x + side;
+        if (!pend[slot]) continue;
+        const Payload pl = pay[slot];
+        pend[slot] = 0;
+        uint32_t &D = side ? st.outD : st.inD;
+        uint64_t &P = side ? st.outP : st.inP;
+        const uint32_t d = pl.D & DM;
+        if (ptcn(D)) {      /* chain_update: farther target replaces, equal distance re-marks */
+          if (d > D) P = pl.P;
+          if (d >= D) { D = pl.D; ++applied; dirty = true; }
+        }
+      }
+      if (dirty) cs[x] = st;
+      keep = ptcn(st.inD) || ptcn(st.outD);
+      cycles += keep && (st.inD & DM) == maxd && (st.outD & DM) == maxd;
+    }
+    const unsigned long long o = warp_append(keep, &ctr->lr_remaining);
+    if (keep) next[o] = x;
+  }
+  applied = warp_sum(applied); cycles = warp_sum(cycles);
+  if ((threadIdx.x & 31) == 0) {
+    if (applied) atomicAdd(&ctr->lr_applied, applied);
+    if (cycles) atomicAdd(&ctr->lr_cycles, cycles);
+  }
+}
+
+/* separate_cycles(iterations) when anything is unfinished, then separate_isolated */
+__global__ void __launch_bounds__(TPB) k_separate(const ChainState *cs, uint64_t M, int any_unfinished, uint32_t maxd,
+                                                   uint8_t *removed, DevCounters *ctr) {
+  unsigned long long ncy = 0, niso = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (uint64_t)gridDim.x * blockDim.x) {
+    const ChainState st = cs[i];
+    uint8_t r = 0;
+    if (any_unfinished && (st.inD & DM) == maxd && (st.outD & DM) == maxd) { r = 1; ++ncy; }
+    else if (st.inD == TM && st.outD == TM) { r = 2; ++niso; }
+    removed[i] = r;
+  }
+  ncy = warp_sum(ncy); niso = warp_sum(niso);
+  if ((threadIdx.x & 31) == 0) {
+    if (ncy) atomicAdd(&ctr->n_cycle, ncy);
+    if (niso) atomicAdd(&ctr->n_isolated, niso);
+  }
+}
+
+/* ================================================================ emission */
+template <class KT>
+__device__ __forceinline__ KT ptr_kmer(uint64_t P, const uint64_t *ckey, const uint8_t *cedge, int k) {
+  constexpr int KWD = KOps<KT>::WORDS;
+  const uint32_t o = (uint32_t)P;
+  KT base = KOps<KT>::load(ckey + (uint64_t)o * KWD);
+  if (P & PF_EXT) {
+    const uint8_t e = cedge[o];
+    base = (P & PF_EXTOUT) ? KOps<KT>::append(base, (e >> 3) & 3u, k) : KOps<KT>::prepend(e & 3u, base, k);
+  }
+  return (P & PF_FLIP) ? KOps<KT>::rc(base, k) : base;
+}
+
+struct EmitArgs {
+  const uint64_t *ckey;
+  const uint8_t *cedge;
+  const ChainState *cs;
+  const uint8_t *removed;
+  uint64_t M;
+  int k;
+  uint64_t *rK, *rrep;
+  int32_t *rdist;
+  uint32_t *rep_idx;   /* per chain node: chain index of its representative, NONE32 if external */
+  int32_t *dist_of;    /* per chain node: rank distance */
+  uint32_t *head_of;   /* per chain node: chain ordinal if it is a head */
+  uint32_t *heads;     /* per chain ordinal: head node */
+  uint64_t *head_len;  /* per chain ordinal: k - 1 + nodes */
+  uint64_t *ch_rep;
+  DevCounters *ctr;
+};
+
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_ranked(EmitArgs a) {
+  constexpr int KWD = KOps<KT>::WORDS;
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < a.M; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    const bool live = i < a.M && a.removed[i] == 0;
+    KT K{}, rep{};
+    int32_t dist = 0;
+    bool head = false;
+    if (live) {
+      const ChainState st = a.cs[i];
+      const KT key = KOps<KT>::load(a.ckey + i * KWD);
+      const KT L = term(st.inD) ? key : ptr_kmer<KT>(st.inP, a.ckey, a.cedge, a.k);
+      const KT R = KOps<KT>::rc(term(st.outD) ? key : ptr_kmer<KT>(st.outP, a.ckey, a.cedge, a.k), a.k);
+      const bool sense = KOps<KT>::le(L, R);
+      K = sense ? key : KOps<KT>::rc(key, a.k);
+      rep = sense ? L : R;
+      dist = (int32_t)(sense ? (st.inD & DM) : (st.outD & DM));
+      const uint32_t sd = sense ? st.inD : st.outD;
+      const uint64_t sp = sense ? st.inP : st.outP;
+      a.rep_idx[i] = term(sd) ? (uint32_t)i : ((sp & (PF_EXT | PF_BLANK)) ? NONE32 : (uint32_t)sp);
+      a.dist_of[i] = dist;
+      head = dist == 0;
+    }
+    const unsigned long long o = warp_append(live, &a.ctr->n_ranked);
+    if (live) {
+      KOps<KT>::store(a.rK + o * KWD, K);
+      KOps<KT>::store(a.rrep + o * KWD, rep);
+      a.rdist[o] = dist;
+    }
+    const unsigned long long h = warp_append(head, &a.ctr->n_heads);
+    if (i < a.M) a.head_of[i] = head ? (uint32_t)h : NONE32;
+    if (head) {
+      const ChainState st = a.cs[i];
+      a.heads[h] = (uint32_t)i;
+      a.head_len[h] = (uint64_t)(a.k - 1) + (st.inD & DM) + (st.outD & DM) + 1;
+      KOps<KT>::store(a.ch_rep + h * KWD, rep);
+    }
+  }
+}
+
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_fill(EmitArgs a, const uint64_t *ch_off, char *chars, uint32_t *seen) {
+  constexpr int KWD = KOps<KT>::WORDS;
+  const char ACGT[4] = {'A', 'C', 'G', 'T'};
+  bool bad = false;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.M; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (a.removed[i]) continue;
+    const uint32_t ri = a.rep_idx[i];
+    const uint32_t h = (ri == NONE32) ? NONE32 : a.head_of[ri];
+    if (h == NONE32) { bad = true; continue; }
+    const uint64_t off = ch_off[h], len = ch_off[h + 1] - off;
+    const int32_t d = a.dist_of[i];
+    const ChainState st = a.cs[i];
+    const KT key = KOps<KT>::load(a.ckey + i * KWD);
+    const KT L = term(st.inD) ? key : ptr_kmer<KT>(st.inP, a.ckey, a.cedge, a.k);
+    const KT R = KOps<KT>::rc(term(st.outD) ? key : ptr_kmer<KT>(st.outP, a.ckey, a.cedge, a.k), a.k);
+    const bool sense = KOps<KT>::le(L, R);
+    const KT K = sense ? key : KOps<KT>::rc(key, a.k);
+    atomicAdd(&seen[h], 1u);
+    if (d == 0) {   /* the representative itself: all k bases */
+      for (int q = 0; q < a.k; ++q) chars[off + q] = ACGT[KOps<KT>::base_lsb(K, a.k - 1 - q)];
+    } else {        /* one base per node: the last base of K on the representative's strand */
+      const uint64_t pos = (uint64_t)(a.k - 1) + (uint64_t)d;
+      if (pos >= len) { bad = true; continue; }
+      chars[off + pos] = ACGT[KOps<KT>::last(K)];
+    }
+  }
+  if (bad) atomicOr(&a.ctr->err, (unsigned long long)DERR_UNCLEAN_CHAINS);
+}
+
+__global__ void k_check_chains(const uint64_t *ch_off, const uint32_t *seen, uint64_t nh, int k, DevCounters *ctr) {
+  for (uint64_t h = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (uint64_t)gridDim.x * blockDim.x)
+    if ((uint64_t)seen[h] + (uint64_t)(k - 1) != ch_off[h + 1] - ch_off[h])
+      atomicOr(&ctr->err, (unsigned long long)DERR_UNCLEAN_CHAINS);
+}
+
+int sms_count() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+template <class KT>
+bruno_status extract_typed(Ctx *c) {
+  bruno_status st;
+  const uint64_t nb = (c->nslots + CHS - 1) / CHS;
+  if ((st = ensure(c, c->blk_cnt, nb * 8)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->blk_base, nb * 8)) != BRUNO_OK) return st;
+  k_chain_count<KT><<<(unsigned)nb, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, (uint64_t *)c->blk_cnt.p);
+  scan_u64((const uint64_t *)c->blk_cnt.p, (uint64_t *)c->blk_base.p, nb, nullptr, c->stream);
+  const uint64_t M = c->n_chain, Mb = std::max<uint64_t>(1, M);
+  const int KWD = Slot<KT>::KEYW;
+  if ((st = ensure(c, c->ckey, Mb * 8 * KWD)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->cslot, Mb * 8)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->cedge, Mb)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->cstate, Mb * sizeof(ChainState))) != BRUNO_OK) return st;
+  k_chain_assign<KT><<<(unsigned)nb, TPB, 0, c->stream>>>((uint64_t *)c->table.p, c->nslots, (const uint64_t *)c->blk_base.p,
+                                                          (uint64_t *)c->ckey.p, (uint64_t *)c->cslot.p);
+  const int sms = sms_count();
+  k_chain_init<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, c->cfg.k,
+                                                   (const uint64_t *)c->ckey.p, (const uint64_t *)c->cslot.p, M,
+                                                   (ChainState *)c->cstate.p, (uint8_t *)c->cedge.p, 4096u);
+  k_termini<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, c->cfg.k,
+                                                (ChainState *)c->cstate.p, 4096u);
+  c->launches += 5;
+  return cuda_check(c, cudaGetLastError(), "extract_chains");
+}
+
+template <class KT>
+bruno_status compress_typed(Ctx *c) {
+  bruno_status st;
+  const uint64_t M = c->n_chain, Mb = std::max<uint64_t>(1, M);
+  const int KWD = Slot<KT>::KEYW;
+  if ((st = ensure(c, c->r_K, Mb * 8 * KWD)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->r_rep, Mb * 8 * KWD)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->r_dist, Mb * 4)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->rep_idx, Mb * 4)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->head_of, Mb * 4)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->heads, Mb * 4)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->head_len, (Mb + 1) * 8)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->head_off, (Mb + 1) * 8)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->ch_rep, Mb * 8 * KWD)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->pay, Mb * 8)) != BRUNO_OK) return st;   /* reused: dist_of + seen */
+  cudaMemsetAsync(&c->dctr->n_ranked, 0, 8, c->stream);
+  cudaMemsetAsync(&c->dctr->n_heads, 0, 8, c->stream);
+  cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
+  EmitArgs a{};
+  a.ckey = (const uint64_t *)c->ckey.p; a.cedge = (const uint8_t *)c->cedge.p; a.cs = (const ChainState *)c->cstate.p;
+  a.removed = (const uint8_t *)c->removed.p; a.M = M; a.k = c->cfg.k;
+  a.rK = (uint64_t *)c->r_K.p; a.rrep = (uint64_t *)c->r_rep.p; a.rdist = (int32_t *)c->r_dist.p;
+  a.rep_idx = (uint32_t *)c->rep_idx.p; a.dist_of = (int32_t *)c->pay.p; a.head_of = (uint32_t *)c->head_of.p;
+  a.heads = (uint32_t *)c->heads.p; a.head_len = (uint64_t *)c->head_len.p; a.ch_rep = (uint64_t *)c->ch_rep.p;
+  a.ctr = c->dctr;
+  const int sms = sms_count();
+  k_ranked<KT><<<sms * 8, TPB, 0, c->stream>>>(a);
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  c->n_ranked = c->hctr->n_ranked;
+  c->n_heads = c->hctr->n_heads;
+  const uint64_t nh = c->n_heads;
+  /* offsets: exclusive scan of per-chain lengths, total into n_chain_chars */
+  cudaMemsetAsync((uint64_t *)c->head_len.p + nh, 0, 8, c->stream);
+  scan_u64((const uint64_t *)c->head_len.p, (uint64_t *)c->head_off.p, nh + 1, &c->dctr->n_chain_chars, c->stream);
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  c->n_chain_chars = c->hctr->n_chain_chars;
+  if ((st = ensure(c, c->ch_chars, std::max<uint64_t>(1, c->n_chain_chars))) != BRUNO_OK) return st;
+  uint32_t *seen = (uint32_t *)((int32_t *)c->pay.p + Mb);
+  cudaMemsetAsync(seen, 0, Mb * 4, c->stream);
+  k_fill<KT><<<sms * 8, TPB, 0, c->stream>>>(a, (const uint64_t *)c->head_off.p, (char *)c->ch_chars.p, seen);
+  c->launches += 5;  /* k_ranked, scan, k_fill, k_check_chains, scan of heads */
+  k_check_chains<<<sms * 2, TPB, 0, c->stream>>>((const uint64_t *)c->head_off.p, seen, nh, c->cfg.k, c->dctr);
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  c->chains_clean = !(c->hctr->err & DERR_UNCLEAN_CHAINS);
+  return BRUNO_OK;
+}
+
+}  // namespace
+
+bruno_status run_extract_chains(Ctx *c) { return c->W == 1 ? extract_typed<KW1>(c) : extract_typed<KW2>(c); }
+
+bruno_status run_list_rank(Ctx *c, int min_update) {
+  bruno_status st;
+  const uint64_t M = c->n_chain, Mb = std::max<uint64_t>(1, M);
+  if ((st = ensure(c, c->unf0, Mb * 4)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->unf1, Mb * 4)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->pend, Mb * 16)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->pay, Mb * 2 * sizeof(Payload))) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->removed, Mb)) != BRUNO_OK) return st;
+  cudaMemsetAsync(c->pend.p, 0, Mb * 16, c->stream);
+  cudaMemsetAsync(&c->dctr->lr_remaining, 0, 8, c->stream);
+  cudaMemsetAsync(&c->dctr->lr_multi, 0, 8, c->stream);
+  const int sms = sms_count();
+  ChainState *cs = (ChainState *)c->cstate.p;
+  uint32_t *cur = (uint32_t *)c->unf0.p, *nxt = (uint32_t *)c->unf1.p;
+  k_lr_init<<<sms * 8, TPB, 0, c->stream>>>(cs, M, cur, &c->dctr->lr_remaining);
+  c->launches += 2;  /* k_lr_init, k_separate */
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  uint64_t remaining = c->hctr->lr_remaining;
+  bool all_compacted = remaining == 0;
+  uint64_t iterations = 0;
+  while (!all_compacted) {
+    const int g = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 8, (remaining + TPB - 1) / TPB));
+    k_lr_propose<<<g, TPB, 0, c->stream>>>(cs, cur, remaining, min_update, (unsigned long long *)c->pend.p, c->dctr);
+    k_lr_commit<<<g, TPB, 0, c->stream>>>(cs, cur, remaining, min_update, (unsigned long long *)c->pend.p,
+                                          (Payload *)c->pay.p);
+    cudaMemsetAsync(&c->dctr->lr_applied, 0, 24, c->stream);  /* applied, remaining, cycles */
+    const uint32_t maxd = 1u << (iterations + 1);
+    k_lr_apply<<<g, TPB, 0, c->stream>>>(cs, cur, remaining, (unsigned long long *)c->pend.p, (const Payload *)c->pay.p,
+                                         maxd, nxt, c->dctr);
+    c->launches += 3;
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    const uint64_t applied = c->hctr->lr_applied, cycles = c->hctr->lr_cycles;
+    remaining = c->hctr->lr_remaining;
+    std::swap(cur, nxt);
+    ++iterations;
+    if (iterations >= 30) all_compacted = true;
+    else all_compacted = applied == 0 || cycles == remaining;
+  }
+  c->iterations = iterations;
+  c->multi = c->hctr->lr_multi;
+  cudaMemsetAsync(&c->dctr->n_cycle, 0, 16, c->stream);
+  k_separate<<<sms * 8, TPB, 0, c->stream>>>(cs, M, remaining > 0 ? 1 : 0, (uint32_t)(1u << iterations),
+                                             (uint8_t *)c->removed.p, c->dctr);
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  c->n_cycle = c->hctr->n_cycle;
+  c->n_isolated = c->hctr->n_isolated;
+  return BRUNO_OK;
+}
+
+bruno_status run_compress(Ctx *c) { return c->W == 1 ? compress_typed<KW1>(c) : compress_typed<KW2>(c); }
+
+}  // namespace bg

@@ -1,0 +1,121 @@
+/*
+ * internal.cuh -- context state shared by the library's translation units.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/bruno_gb300.h"
+#include "kmer.cuh"
+
+namespace bg {
+
+/* device error word bits */
+constexpr uint32_t DERR_TABLE_FULL = 1u;
+constexpr uint32_t DERR_BAD_INPUT = 2u;
+constexpr uint32_t DERR_INVARIANT = 4u;
+constexpr uint32_t DERR_UNCLEAN_CHAINS = 8u;
+
+/* Small counters written by kernels, read back by the host between phases. */
+struct DevCounters {
+  unsigned long long err;
+  unsigned long long n_newlines_eff;   /* newlines before the end of the last non-blank line */
+  long long last_nonws;                /* index of the last byte that is not \n or \r, -1 if none */
+  unsigned long long bad_line;         /* first malformed line, ~0 if none */
+  unsigned long long n_records;
+  unsigned long long n_instances, n_reads_used, n_slots_claimed, n_entries;
+  unsigned long long n_nodes, n_branch, n_chain, n_filtered, n_k2_dump;
+  unsigned long long flag_hist[16];
+  unsigned long long lr_applied, lr_remaining, lr_cycles, lr_multi;
+  unsigned long long n_cycle, n_isolated, n_ranked, n_heads, n_chain_chars;
+  unsigned int hll[1 << 14];           /* HyperLogLog registers, p = 14 */
+};
+
+struct Segment { const char *ptr; uint64_t n; };
+
+/* chain state of one chain node, 32 B: pointers encode a chain index (bits 0..31) plus
+ * PF_FLIP (the target k-mer, on this node's strand, is the reverse complement of the
+ * target's canonical key), PF_EXT (the target is the non-chain in- (PF_EXTOUT clear) or
+ * out-neighbour of the chain node in bits 0..31) and PF_BLANK (Kmer(), no neighbour). */
+struct ChainState { uint64_t inP, outP; uint32_t inD, outD; uint64_t pad; };
+constexpr uint64_t PF_FLIP = 1ull << 32, PF_EXT = 1ull << 33, PF_EXTOUT = 1ull << 34, PF_BLANK = 1ull << 35;
+struct Payload { uint64_t P; uint32_t D; uint32_t pad; };
+
+struct Buf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+struct Ctx {
+  bruno_cfg cfg{};
+  int W = 1;                     /* key words */
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  int stage = 0;                 /* 0 empty, 1 loaded, 2 counted, 3 filtered, 4 chains, 5 ranked, 6 compressed */
+
+  std::vector<Segment> segs;
+  std::vector<Buf> seg_bufs;     /* device copies of host-loaded files */
+
+  DevCounters *dctr = nullptr;   /* device */
+  DevCounters *hctr = nullptr;   /* pinned host mirror */
+
+  /* read index */
+  Buf rstart, rend, tile_cnt, tile_base;   /* read spans as device byte addresses */
+  uint64_t n_reads = 0, n_reads_used = 0, n_instances = 0;
+
+  /* k-mer table */
+  Buf table;
+  uint64_t nslots = 0, n_entries = 0;
+
+  /* dumps */
+  Buf k2_keys, k2_edges, k2_counts;
+  uint64_t n_k2 = 0;
+  Buf f_keys, f_edges, f_counts;
+  uint64_t n_filtered = 0;
+  bool k2_dumped = false;
+
+  /* nodes */
+  uint64_t n_nodes = 0, n_branch = 0, n_chain = 0;
+  uint64_t flag_hist[16] = {0};
+  Buf blk_cnt, blk_base;
+
+  /* chains */
+  Buf ckey, cslot, cedge, cstate, pend, pay, unf0, unf1, removed;
+  uint64_t iterations = 0, n_cycle = 0, n_isolated = 0, multi = 0;
+
+  /* emission */
+  Buf r_K, r_rep, r_dist, rep_idx, head_of, heads, head_len, head_off, ch_rep, ch_off, ch_chars;
+  uint64_t n_ranked = 0, n_heads = 0, n_chain_chars = 0;
+  bool chains_clean = true;
+
+  cudaEvent_t ev[8] = {nullptr};
+  cudaEvent_t kev[4] = {nullptr};  /* around k_hll, k_table_init, k_count */
+  double phase_ms[9] = {0};        /* 6 phases, then k_hll, k_table_init, k_count */
+  uint64_t launches = 0;           /* kernels launched since the last reset */
+};
+
+/* --------------------------------------------------------------- host helpers */
+bruno_status set_err(Ctx *c, bruno_status s, const std::string &msg);
+bruno_status cuda_check(Ctx *c, cudaError_t e, const char *what);
+bruno_status ensure(Ctx *c, Buf &b, size_t bytes, bool preserve = false);
+bruno_status sync_counters(Ctx *c, bool with_hll = false);
+
+/* exclusive scan of n uint64 values (in may equal out); writes the total to *total_dev */
+void scan_u64(const uint64_t *in, uint64_t *out, uint64_t n, unsigned long long *total_dev, cudaStream_t s);
+
+/* -------------------------------------------------------------- phase launchers */
+bruno_status run_index_reads(Ctx *c);        /* FASTQ line structure -> read spans */
+bruno_status run_count(Ctx *c);              /* distinct-count estimate, table, counting */
+bruno_status run_dump_k2(Ctx *c);            /* optional raw (k+2)-mer copy */
+bruno_status run_filter(Ctx *c, const uint64_t *thresh);
+bruno_status run_extract_chains(Ctx *c);
+bruno_status run_list_rank(Ctx *c, int min_update);
+bruno_status run_compress(Ctx *c);
+bruno_status run_copy_nodes(Ctx *c, uint64_t *keys, uint16_t *counts, uint8_t *flags, size_t cap, size_t *n);
+
+}  // namespace bg

@@ -1,0 +1,168 @@
+/*
+ * bruno_gb300.h -- C ABI of the GB300 de Bruijn graph-construction library.
+ *
+ * One context builds one graph on one GPU: FASTQ bytes -> canonical (k-mer, biedge) pairs
+ * -> (k+2)-mer edge-frequency counts -> frequency filter -> graph nodes with 9 uint16 edge
+ * counters -> chain nodes -> list ranking -> compacted chains.  Every entry point replaces
+ * one step of ParBLiSS/bruno's src/debruijn API (cited beside it) and computes the same
+ * result bit for bit; the reference's MPI distribution disappears because all tables live
+ * in one device's memory.
+ *
+ * Conventions
+ *  - Plain C types only.  A CUDA stream is passed as `void *` (a cudaStream_t).
+ *  - k-mers are 2-bit packed (A0 C1 G2 T3), first base in the most significant bits.
+ *    Arrays of k-mers hold `words` uint64 per k-mer: 1 for k <= 31, 2 for k >= 32 (low word
+ *    first).  A biedge byte holds the DNA16 code (A1 C2 G4 T8, 0 = none) of the base before
+ *    the k-mer in its high nibble and of the base after it in its low nibble.
+ *  - Every call returns a bruno_status; the context keeps a message for the last failure
+ *    (bruno_last_error).  Kernels never trap: device-side failures (table full, malformed
+ *    input, ranking that does not converge) set a status word that the host reads.
+ *  - The context owns all device memory it allocates.  Copy-out calls use the size-query
+ *    pattern: pass dst == NULL to learn the element count, then pass buffers of that size.
+ *  - Calls on one context are stream-ordered on the context's stream and are not
+ *    thread-safe; use one context per host thread.
+ */
+#ifndef BRUNO_GB300_H_
+#define BRUNO_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bruno_status {
+  BRUNO_OK = 0,
+  BRUNO_ERR_ARG = 1,              /* invalid argument or call order */
+  BRUNO_ERR_BAD_INPUT = 2,        /* malformed FASTQ */
+  BRUNO_ERR_OOM = 3,              /* device allocation failed */
+  BRUNO_ERR_TABLE_FULL = 4,       /* hash table probe limit hit even after regrowth */
+  BRUNO_ERR_RANK_NOT_CONVERGED = 5,/* list ranking stopped at the 30-round cap */
+  BRUNO_ERR_INVARIANT = 6,        /* an internal invariant failed (reported, never trapped) */
+  BRUNO_ERR_CUDA = 7,             /* a CUDA runtime call failed */
+  BRUNO_ERR_CAPACITY = 8          /* caller buffer too small */
+} bruno_status;
+
+typedef struct bruno_cfg {
+  int32_t k;                /* k-mer length, 3..63 (compile-time pK of the reference driver) */
+  int32_t thresholding;     /* -T: 1 = build_index_thresholded, 0 = build_index */
+  uint64_t thresh[6];       /* k_lo, k_hi, k1_lo, k1_hi, k2_lo, k2_hi; lower bounds inclusive,
+                               upper bounds exclusive (debruijn_graph_map.hpp:1261) */
+  int32_t min_update;       /* -R: 1 = list_rank_min_update, 0 = list_rank */
+  int32_t device;           /* CUDA device ordinal */
+  uint64_t table_slots;     /* 0 = size the k-mer table from a distinct-count estimate */
+  double max_load;          /* target table load when sizing (0 = 0.5) */
+  int32_t keep_k2;          /* 1: keep enough state to copy out the raw (k+2)-mer counts */
+  int32_t keep_filtered;    /* 1: record the filtered (k+2)-mer entries for copy-out */
+} bruno_cfg;
+
+typedef struct bruno_sizes {
+  uint64_t n_reads;         /* FASTQ records */
+  uint64_t n_reads_used;    /* records that produced k-mers (no N, length >= k+2) */
+  uint64_t n_instances;     /* (k-mer, biedge) pairs */
+  uint64_t n_k2;            /* distinct canonical (k-mer, biedge) entries */
+  uint64_t n_filtered;      /* entries kept by the filter */
+  uint64_t n_nodes;         /* graph nodes */
+  uint64_t n_branch;        /* IsBranchPoint nodes */
+  uint64_t n_chain_nodes;   /* IsChainNode nodes */
+  uint64_t iterations;      /* list-ranking rounds */
+  uint64_t n_cycle_nodes;   /* removed as cycles */
+  uint64_t n_isolated;      /* removed as isolated */
+  uint64_t n_ranked;        /* listranked chain nodes */
+  uint64_t n_chains;        /* compacted chains */
+  uint64_t n_chain_chars;   /* total bases over all compacted chains */
+  uint64_t table_slots;     /* k-mer table slots in use */
+  uint64_t collisions;      /* list-ranking sides that got >1 update in one round */
+  uint64_t filter_flag_hist[16]; /* k_del[] histogram (debruijn_graph_map.hpp:1568) */
+  uint64_t launches;        /* kernels launched by the last build */
+} bruno_sizes;
+
+typedef struct bruno_ctx bruno_ctx;
+
+/* Context lifetime.  Replaces constructing debruijn_graph / debruijn_chain_graph
+ * (debruijn_graph.hpp:45-60, debruijn_chain_graph.hpp:162-168) on an MPI communicator. */
+bruno_status bruno_ctx_create(const bruno_cfg *cfg, bruno_ctx **out);
+bruno_status bruno_ctx_destroy(bruno_ctx *ctx);
+/* Runs all later calls on `stream` (a cudaStream_t; NULL = the context's own stream). */
+bruno_status bruno_set_stream(bruno_ctx *ctx, void *stream);
+const char *bruno_last_error(const bruno_ctx *ctx);
+/* Drops all graph state so the context can build another graph (keeps allocations). */
+bruno_status bruno_reset(bruno_ctx *ctx);
+
+/* Adds one FASTQ file's bytes.  Replaces partitioned_file::read_file + parse_file_data
+ * (compact_dbg_io.hpp:165-195, compact_dbg_freq_construct_clean.cpp:321-323).  If
+ * is_device != 0, `buf` is a device pointer that must stay valid until
+ * bruno_compute_biedge_freqencies returns; otherwise the bytes are copied to the device. */
+bruno_status bruno_load_fastq(bruno_ctx *ctx, const char *buf, size_t nbytes, int32_t is_device);
+
+/* Parses every loaded file into canonical (k-mer, biedge) pairs and counts each distinct
+ * pair.  Replaces debruijn_kmer_simple_biedge_parser (debruijn_biedge_loader.hpp:393-623)
+ * followed by debruijn_graph_map::compute_biedge_freqencies (debruijn_graph_map.hpp:1085). */
+bruno_status bruno_compute_biedge_freqencies(bruno_ctx *ctx);
+
+/* Frequency filter and node insertion.  Replaces
+ * debruijn_graph_map::local_insert_by_freqencies(k2_counter, threshes)
+ * (debruijn_graph_map.hpp:1258-1623); thresh == NULL uses cfg.thresh.  With
+ * cfg.thresholding == 0 it is the unthresholded build_index insert
+ * (compact_dbg_build.hpp:34-62).  Also classifies every node (IsBranchPoint / IsChainNode,
+ * debruijn_graph_filters.hpp:142-220). */
+bruno_status bruno_local_insert_by_freqencies(bruno_ctx *ctx, const uint64_t *thresh);
+
+/* Builds the chain map and marks termini next to branch points.  Replaces
+ * debruijn_chain_graph::extract_chains (debruijn_chain_graph.hpp:604-667). */
+bruno_status bruno_extract_chains(bruno_ctx *ctx);
+
+/* List ranking.  min_update != 0 replaces list_rank_min_update (debruijn_chain_graph.hpp:
+ * 1040-1310), otherwise list_rank (:793-994); both end with separate_cycles and
+ * separate_isolated.  *iterations receives the round count the reference returns. */
+bruno_status bruno_list_rank(bruno_ctx *ctx, int32_t min_update, uint64_t *iterations);
+
+/* Listranked chain nodes and compacted chain sequences on the device.  Replaces
+ * to_ranked_chain_nodes (debruijn_chain_graph.hpp:1760-1773) and to_compressed_chains
+ * (:1778-1856). */
+bruno_status bruno_to_compressed_chains(bruno_ctx *ctx);
+
+/* The whole plain path in one call: load (host or device bytes), count, filter, extract,
+ * rank, compress.  Equivalent to the reference driver's build_index_thresholded ->
+ * extract_chains -> list_rank[_min_update] -> to_ranked_chain_nodes sequence
+ * (compact_dbg_freq_construct_clean.cpp:491-737). */
+bruno_status bruno_build_and_compact(bruno_ctx *ctx, const char *buf, size_t nbytes, int32_t is_device);
+
+bruno_status bruno_get_sizes(bruno_ctx *ctx, bruno_sizes *out);
+
+/* Copy-outs to host memory (device order, not sorted).  `n` receives the element count;
+ * dst pointers may be NULL to query it. */
+/* Raw (k+2)-mer counts: LocalK2CountMapType::to_vector (debruijn_graph_map.hpp:1268).
+ * Needs cfg.keep_k2 and must be called before bruno_local_insert_by_freqencies. */
+bruno_status bruno_copy_k2(bruno_ctx *ctx, uint64_t *keys, uint8_t *edges, uint32_t *counts,
+                           size_t cap, size_t *n);
+/* Filtered entries (k2counts after :1594).  Needs cfg.keep_filtered. */
+bruno_status bruno_copy_filtered(bruno_ctx *ctx, uint64_t *keys, uint8_t *edges, uint32_t *counts,
+                                 size_t cap, size_t *n);
+/* Graph nodes: k-mer and counts[9] = out A C G T, in A C G T, self (debruijn_graph_node.hpp:157);
+ * flags bit 0 = IsBranchPoint, bit 1 = IsChainNode. */
+bruno_status bruno_copy_nodes(bruno_ctx *ctx, uint64_t *keys, uint16_t *counts, uint8_t *flags,
+                              size_t cap, size_t *n);
+/* listranked_chain_node<K> = (K on the representative's strand, representative, distance)
+ * (debruijn_chain_node.hpp:155-156). */
+bruno_status bruno_copy_ranked(bruno_ctx *ctx, uint64_t *K, uint64_t *rep, int32_t *dist,
+                               size_t cap, size_t *n);
+/* Compacted chains: representative k-mer per chain, offsets[n_chains + 1] into `chars`. */
+bruno_status bruno_copy_chains(bruno_ctx *ctx, uint64_t *reps, uint64_t *offsets, char *chars,
+                               size_t cap_chains, size_t cap_chars, size_t *n_chains, size_t *n_chars);
+
+/* Page-locked host memory, for fast host<->device copies of FASTQ input and results. */
+bruno_status bruno_host_alloc(size_t bytes, void **out);
+bruno_status bruno_host_free(void *p);
+
+/* Device times of the last build, milliseconds, from CUDA events on the context's stream:
+ * ms[0..5] = phases parse, count_k2mers, filter_insert, chainmap, list_rank, compress;
+ * ms[6..8] = kernels k_hll (distinct-count estimate), k_table_init, k_count.  Writes
+ * min(n, 9) values. */
+bruno_status bruno_phase_ms(bruno_ctx *ctx, double *ms, size_t n);
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BRUNO_GB300_H_ */

@@ -1,0 +1,74 @@
+"""The drop-in boundary: the C header, the shared library and the Python binding agree
+(no GPU needed: nothing here launches a kernel)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+import bruno_gb300 as bg
+from bruno_gb300 import build
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "bruno_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build_library()
+    return bg.load_library()
+
+
+def declared():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(bruno_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_header_matches_binding():
+    assert declared() == sorted(bg.EXPORTS)
+
+
+def test_library_exports_every_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", bg.LIB_PATH], capture_output=True, text=True).stdout
+    syms = {l.split()[-1] for l in out.splitlines() if l.strip()}
+    missing = [s for s in declared() if s not in syms]
+    assert not missing, missing
+
+
+def test_struct_layout_matches_header(tmp_path):
+    src = tmp_path / "layout.c"
+    src.write_text(f'''
+#include <stdio.h>
+#include <stddef.h>
+#include "{HEADER}"
+int main(void) {{
+  printf("%zu %zu %zu %zu %zu\\n", sizeof(bruno_cfg), offsetof(bruno_cfg, thresh), offsetof(bruno_cfg, table_slots),
+         offsetof(bruno_cfg, keep_filtered), sizeof(bruno_sizes));
+  return 0;
+}}''')
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-o", str(exe), str(src)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    C = bg._Cfg
+    want = [ctypes.sizeof(C), C.thresh.offset, C.table_slots.offset, C.keep_filtered.offset, ctypes.sizeof(bg._Sizes)]
+    assert got == want
+
+
+def test_bad_config_rejected_without_gpu(lib):
+    """k outside 3..63 is refused before any CUDA call"""
+    cfg = bg.GraphConfig(k=64).to_c()
+    h = ctypes.c_void_p()
+    assert lib.bruno_ctx_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
+    assert lib.bruno_ctx_create(None, ctypes.byref(h)) == 1
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    with pytest.raises(bg.BrunoError):
+        bg._lib_backup = bg._lib
+        try:
+            bg._lib = None
+            bg.load_library(str(tmp_path / "absent.so"))
+        finally:
+            bg._lib = bg._lib_backup

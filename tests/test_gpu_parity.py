@@ -1,0 +1,134 @@
+"""Parity of the CUDA library with the CPU oracle, through the C ABI.  Integer path: every
+comparison is bit-exact, after sorting (table order is not part of the contract)."""
+import numpy as np
+import pytest
+
+import bruno_gb300 as bg
+from bruno_gb300 import synth
+from oracle import oracle
+from conftest import fixture_bytes
+from helpers import assert_same, chain_set, sort_k2, sort_nodes, sort_ranked
+
+pytestmark = pytest.mark.gpu
+
+FASTQS = ["test.unitiqs.fastq", "test.star.unitiqs.fastq", "test.star2.unitiqs.fastq", "test.short.unitiqs.fastq",
+          "test.debruijn.small.fastq", "test.medium.fastq", "debruijn.palindrome.fastq", "debruijn.palindrome2.fastq",
+          "debruijn.palindrome_chr14.fastq", "debruijn.shifted_cycle_chr14.fastq", "debruijn.bubble.fastq",
+          "debruijn.bubble2.fastq", "natural.fastq", "natural.withN.fastq"]
+OPTIONS = {
+    "u": (False, (), True), "tl1": (True, (1,), True), "tl2": (True, (2,), True),
+    "tl2_norank": (True, (2,), False), "tl3": (True, (3,), True),
+}
+
+
+def gpu_run(data, k, thr_on, thresh, mu, files=None, **kw):
+    g = bg.Graph(k=k, thresholding=thr_on, thresh=thresh, min_update=mu, keep_k2=True, keep_filtered=True, **kw)
+    g.reset()
+    for f in (files or [data]):
+        g.load_fastq(f)
+    g.compute_biedge_freqencies()
+    k2 = g.k2()
+    g.local_insert_by_freqencies()
+    g.extract_chains()
+    it = g.list_rank_min_update() if mu else g.list_rank()
+    g.to_compressed_chains()
+    out = dict(sizes=g.sizes(), k2=k2, filtered=g.filtered(), nodes=g.nodes(), ranked=g.ranked(),
+               chains=g.chains(), iterations=it)
+    g.close()
+    return out
+
+
+def compare(gpu, ref):
+    s = gpu["sizes"]
+    for n in ("n_reads", "n_reads_used", "n_instances", "n_nodes", "n_branch", "n_chain_nodes", "iterations",
+              "n_cycle_nodes", "n_isolated", "n_ranked", "n_chains"):
+        assert s[n] == ref[n], (n, s[n], ref[n])
+    assert gpu["iterations"] == ref["iterations"]
+    assert s["filter_flag_hist"] == ref["filter_flag_hist"]
+    assert_same(sort_k2(*gpu["k2"]), ref["k2"], "k2 counts")
+    assert_same(sort_k2(*gpu["filtered"]), ref["filtered"], "filtered k2")
+    assert_same(sort_nodes(*gpu["nodes"]), ref["nodes"], "graph nodes")
+    assert_same(sort_ranked(*gpu["ranked"]), ref["ranked"], "listranked chain nodes")
+    assert chain_set(*gpu["chains"]) == chain_set(*ref["chains"]), "compacted chains"
+
+
+@pytest.mark.parametrize("opt", sorted(OPTIONS))
+@pytest.mark.parametrize("fname", FASTQS)
+def test_fixture_parity(fname, opt):
+    thr_on, lo, mu = OPTIONS[opt]
+    thr = bg.thresholds(lo)
+    data = fixture_bytes(fname)
+    ref = oracle.run(data, k=31, thresholding=thr_on, thresh=thr, min_update=mu, keep_k2=True, keep_filtered=True)
+    compare(gpu_run(data, 31, thr_on, thr, mu), ref)
+
+
+def test_known_answer_on_gpu():
+    g = bg.Graph(k=31, thresholding=False).run(fixture_bytes("test.unitiqs.fastq"))
+    expect = sorted(l for l in fixture_bytes("test.unitiqs.fasta").decode().splitlines() if l and l[0] != ">")
+    assert sorted(g.chain_strings()) == expect
+
+
+def test_plain_small_workload_parity():
+    """the 1 Mbp / 100k x 100 bp / 1% / k=31 / -L 2 workload, every output"""
+    w = synth.WORKLOADS["plain-small"]
+    fq = synth.make_fastq(w)
+    thr = bg.thresholds(w.lower)
+    ref = oracle.run(fq, k=31, thresh=thr, min_update=True, threads=16, keep_k2=True, keep_filtered=True)
+    compare(gpu_run(fq, 31, True, thr, True), ref)
+
+
+def test_repeat_rich_workload_parity():
+    """a scaled-down plain-scale genome (repeats, 30x, -L 3), both ranking variants"""
+    w = synth.Workload("rep", 2_000_000, 150, 400_000, 0.005, 31, (3,), 0.02, (1000, 10000), (2, 8), (0.01, 0.01), 3)
+    fq = synth.make_fastq(w)
+    thr = bg.thresholds(w.lower)
+    for mu in (True, False):
+        ref = oracle.run(fq, k=31, thresh=thr, min_update=mu, threads=16, keep_k2=True, keep_filtered=True)
+        compare(gpu_run(fq, 31, True, thr, mu), ref)
+
+
+def test_two_files_count_into_one_table():
+    a, b = fixture_bytes("debruijn.bubble.fastq"), fixture_bytes("debruijn.palindrome_chr14.fastq")
+    thr = bg.thresholds([2])
+    ref = oracle.run(a + b, k=31, thresh=thr, keep_k2=True, keep_filtered=True)
+    compare(gpu_run(None, 31, True, thr, True, files=[a, b]), ref)
+
+
+def test_small_table_regrows():
+    """a deliberately undersized table hits the probe limit, regrows and stays exact"""
+    data = fixture_bytes("debruijn.palindrome_chr14.fastq")
+    thr = bg.thresholds([2])
+    ref = oracle.run(data, k=31, thresh=thr, keep_k2=True, keep_filtered=True)
+    out = gpu_run(data, 31, True, thr, True, table_slots=1024)
+    assert out["sizes"]["table_slots"] > 1024
+    compare(out, ref)
+
+
+def test_malformed_fastq_is_bad_input():
+    data = fixture_bytes("test.medium.fastq").replace(b"\n+\n", b"\n-\n", 1)
+    with pytest.raises(bg.BrunoError) as e:
+        bg.Graph(k=31).run(data)
+    assert e.value.status == 2
+
+
+def test_device_resident_input():
+    torch = pytest.importorskip("torch")
+    data = fixture_bytes("debruijn.bubble.fastq")
+    dev = torch.frombuffer(bytearray(data), dtype=torch.uint8).cuda()
+    thr = bg.thresholds([2])
+    g = bg.Graph(k=31, thresh=thr)
+    g.build_and_compact(dev.data_ptr(), nbytes=dev.numel(), is_device=True)
+    torch.cuda.synchronize()
+    ref = oracle.run(data, k=31, thresh=thr)
+    assert chain_set(*g.chains()) == chain_set(*ref["chains"])
+    assert_same(sort_ranked(*g.ranked()), ref["ranked"], "ranked")
+
+
+def test_context_reuse_gives_identical_results():
+    data = fixture_bytes("debruijn.palindrome_chr14.fastq")
+    g = bg.Graph(k=31, thresh=bg.thresholds([2]))
+    g.build_and_compact(data)
+    first = (chain_set(*g.chains()), sort_ranked(*g.ranked()))
+    g.build_and_compact(data)
+    assert chain_set(*g.chains()) == first[0]
+    assert_same(sort_ranked(*g.ranked()), first[1], "second build")

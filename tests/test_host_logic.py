@@ -1,0 +1,51 @@
+"""Host-side logic: threshold parsing, configuration, k-mer decoding, the generator."""
+import numpy as np
+import pytest
+
+import bruno_gb300 as bg
+from bruno_gb300 import synth
+
+
+def test_thresholds_single_value_is_k1_lower_bound():
+    # compact_dbg_freq_construct_clean.cpp:940-945
+    assert bg.thresholds([3]) == [0, 65536, 3, 65536, 0, 65536]
+
+
+def test_thresholds_three_values():
+    assert bg.thresholds([1, 2, 3], [100, 200, 300]) == [1, 100, 2, 200, 3, 300]
+
+
+def test_thresholds_capped_at_count_max_plus_one():
+    assert bg.thresholds([70000]) == [0, 65536, 65536, 65536, 0, 65536]
+
+
+def test_thresholds_reject_two_values():
+    with pytest.raises(ValueError):
+        bg.thresholds([1, 2])
+
+
+def test_config_roundtrip():
+    c = bg.GraphConfig(k=63, thresh=bg.thresholds([3]), min_update=False, table_slots=123).to_c()
+    assert (c.k, c.min_update, c.table_slots, list(c.thresh)) == (63, 0, 123, bg.thresholds([3]))
+
+
+def test_decode_kmers():
+    assert bg.decode_kmers(np.array([[0b00011011]], np.uint64), 4) == ["ACGT"]
+    v = (1 << 124) | 3
+    assert bg.decode_kmers(np.array([[v & (2**64 - 1), v >> 64]], np.uint64), 63) == ["C" + "A" * 61 + "T"]
+
+
+def test_generator_deterministic_and_thread_independent():
+    w = synth.Workload("t", 50_000, 100, 2_000, 0.01, 31, (2,), 0.05, (100, 500), (2, 4), (0.01, 0.02), seed=7)
+    a = synth.make_fastq(w, threads=1)
+    b = synth.make_fastq(w, threads=4)
+    assert np.array_equal(a, b)
+    assert a.nbytes == synth.fastq_size(w)
+    lines = a.tobytes().split(b"\n")
+    assert lines[0] == b"@r0" and lines[2] == b"+" and len(lines[1]) == 100 and set(lines[3]) == {ord("I")}
+
+
+def test_workloads_match_configs():
+    s, m = synth.WORKLOADS["plain-small"], synth.WORKLOADS["plain-scale"]
+    assert (s.genome_len, s.n_reads, s.read_len, s.sub_rate, s.k) == (1_000_000, 100_000, 100, 0.01, 31)
+    assert (m.genome_len, m.read_len, m.k, round(m.coverage)) == (50_000_000, 150, 31, 30)
