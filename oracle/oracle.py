@@ -46,8 +46,25 @@ class _Res(ctypes.Structure):
     ]
 
 
-def build() -> None:
-    subprocess.run(["make", "-s", "-C", HERE], check=True, capture_output=True)
+def build(force: bool = False) -> None:
+    """Same recipe as oracle/Makefile, with g++ called directly (no make needed)."""
+    os.makedirs(os.path.join(HERE, "_build"), exist_ok=True)
+    src = [os.path.join(HERE, "bruno_oracle.cpp"), os.path.join(HERE, "bruno_oracle.h")]
+    flags = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter"]
+    jobs = []
+    if force or not _fresh(LIB, src):
+        jobs.append(["g++", *flags, "-shared", "-o", LIB, src[0], "-lpthread"])
+    if force or not _fresh(CLI, src + [os.path.join(HERE, "oracle_main.cpp")]):
+        jobs.append(["g++", *flags, "-o", CLI, os.path.join(HERE, "oracle_main.cpp"), src[0], "-lpthread"])
+    procs = [subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True) for j in jobs]
+    for p, j in zip(procs, jobs):
+        out, err = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError(f"oracle build failed: {' '.join(j)}\n{err}")
+
+
+def _fresh(target, deps) -> bool:
+    return os.path.exists(target) and all(os.path.getmtime(d) <= os.path.getmtime(target) for d in deps)
 
 
 _lib = None

@@ -6,7 +6,9 @@ import numpy as np
 
 
 def sort_k2(keys, edges, counts):
-    order = np.lexsort((edges,) + tuple(keys.T))
+    """by (k-mer, edge, count): after trimming, two filtered entries of one k-mer can share
+    an edge byte, so the count breaks the tie"""
+    order = np.lexsort((counts, edges) + tuple(keys.T))
     return keys[order], edges[order], counts[order]
 
 
