@@ -172,7 +172,8 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()   # a real (non-default) stream shared by the library and the events
+    torch.cuda.set_stream(stream)
 
     # workload in pinned host memory, and a device-resident copy
     n = synth.fastq_size(w)
