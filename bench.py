@@ -39,7 +39,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="plain-scale")
-    ap.add_argument("--cpu-sample", type=float, default=0.01, help="fraction of reads in the CPU baseline sample")
+    ap.add_argument("--cpu-sample", type=float, default=0.2, help="fraction of reads in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 

@@ -40,6 +40,7 @@ class _Cfg(ctypes.Structure):
         ("k", ctypes.c_int32), ("thresholding", ctypes.c_int32), ("thresh", ctypes.c_uint64 * 6),
         ("min_update", ctypes.c_int32), ("device", ctypes.c_int32), ("table_slots", ctypes.c_uint64),
         ("max_load", ctypes.c_double), ("keep_k2", ctypes.c_int32), ("keep_filtered", ctypes.c_int32),
+        ("exact_ranking", ctypes.c_int32),
     ]
 
 
@@ -143,6 +144,7 @@ class GraphConfig:
     max_load: float = 0.5
     keep_k2: bool = False
     keep_filtered: bool = False
+    exact_ranking: bool = False
 
     def to_c(self) -> _Cfg:
         c = _Cfg()
@@ -151,6 +153,7 @@ class GraphConfig:
             c.thresh[i] = int(min(v, 2**64 - 1))
         c.table_slots, c.max_load = self.table_slots, self.max_load
         c.keep_k2, c.keep_filtered = int(self.keep_k2), int(self.keep_filtered)
+        c.exact_ranking = int(self.exact_ranking)
         return c
 
 

@@ -72,17 +72,39 @@ __device__ __forceinline__ uint32_t block_exscan(uint32_t v, uint32_t &total) {
 
 /* ============================================================ FASTQ splitting */
 
-/* newline count and last non-whitespace byte of each tile */
+/* per 4 bytes: 0xFF in every byte equal to c (SIMD compare) */
+__device__ __forceinline__ uint32_t bytes_eq(uint32_t w, uint32_t c4) { return __vcmpeq4(w, c4); }
+
+/* 16 bytes at p (16-byte aligned if `aligned`, bounds-checked against n) as 4 words */
+__device__ __forceinline__ uint4 load16(const unsigned char *buf, uint64_t p, uint64_t n, bool aligned) {
+  if (aligned && p + 16 <= n) return *(const uint4 *)(buf + p);
+  uint32_t w[4] = {0, 0, 0, 0};
+  for (int i = 0; i < 16; ++i)
+    if (p + i < n) w[i >> 2] |= (uint32_t)buf[p + i] << (8 * (i & 3));
+  return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+/* newline count and last non-whitespace byte of each tile (16 bytes per thread-load) */
 __global__ void __launch_bounds__(TPB) k_tile_stats(const unsigned char *buf, uint64_t n, uint64_t *tile_cnt,
-                                                     DevCounters *ctr) {
+                                                     DevCounters *ctr, bool aligned) {
   const uint64_t t0 = (uint64_t)blockIdx.x * TILE;
   const uint64_t t1 = (n < t0 + TILE ? n : t0 + TILE);
   unsigned long long cnt = 0;
   long long lastnw = -1;
-  for (uint64_t p = t0 + threadIdx.x; p < t1; p += TPB) {
-    unsigned char c = buf[p];
-    cnt += (c == '\n');
-    if (c != '\n' && c != '\r') lastnw = (long long)p;
+  for (uint64_t p = t0 + 16ull * threadIdx.x; p < t1; p += 16ull * TPB) {
+    const uint4 v = load16(buf, p, t1, aligned);
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+    #pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t nl = bytes_eq(w[q], 0x0A0A0A0Au), cr = bytes_eq(w[q], 0x0D0D0D0Du);
+      cnt += __popc(nl) >> 3;
+      uint32_t keep = ~(nl | cr);
+      /* bytes beyond the tile end are zero padding, not data */
+      const uint64_t base = p + 4 * q;
+      if (base >= t1) keep = 0;
+      else if (base + 4 > t1) keep &= (1u << (8 * (t1 - base))) - 1u;
+      if (keep) lastnw = max(lastnw, (long long)(base + ((31 - __clz(keep)) >> 3)));
+    }
   }
   __shared__ unsigned long long sc[TPB / 32];
   __shared__ long long sl[TPB / 32];
@@ -103,7 +125,7 @@ __global__ void __launch_bounds__(TPB) k_tile_stats(const unsigned char *buf, ui
  * quality).  Newlines after the last non-blank byte are trailing and ignored. */
 __global__ void __launch_bounds__(TPB) k_index_lines(const unsigned char *buf, uint64_t n, const uint64_t *tile_base,
                                                       uint64_t *rstart, uint64_t *rend, uint64_t rbase,
-                                                      uint64_t rcap, DevCounters *ctr) {
+                                                      uint64_t rcap, DevCounters *ctr, bool aligned) {
   const uint64_t t0 = (uint64_t)blockIdx.x * TILE;
   const uint64_t t1 = (n < t0 + TILE ? n : t0 + TILE);
   const long long E = ctr->last_nonws + 1;  /* effective end (exclusive) */
@@ -112,13 +134,16 @@ __global__ void __launch_bounds__(TPB) k_index_lines(const unsigned char *buf, u
   /* stripes of TPB*16 bytes, 16 consecutive bytes per thread, in byte order */
   for (uint64_t s0 = t0; s0 < t1; s0 += (uint64_t)TPB * 16) {
     const uint64_t g0 = s0 + (uint64_t)threadIdx.x * 16;
-    unsigned char b[16];
     uint32_t m = 0;
-    #pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      uint64_t p = g0 + i;
-      b[i] = (p < t1) ? buf[p] : 0;
-      m |= (uint32_t)(b[i] == '\n') << i;
+    if (g0 < t1) {
+      const uint4 v = load16(buf, g0, t1, aligned);
+      const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+      #pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t nl = bytes_eq(w[q], 0x0A0A0A0Au);   /* 0xFF per newline byte */
+        #pragma unroll
+        for (int b = 0; b < 4; ++b) m |= ((nl >> (8 * b + 7)) & 1u) << (4 * q + b);
+      }
     }
     uint32_t total;
     const uint32_t rank = block_exscan(__popc(m), total);
@@ -273,10 +298,18 @@ struct CountArgs {
 __device__ __forceinline__ uint64_t ld_cg(const uint64_t *p) { return __ldcg((const unsigned long long *)p); }
 __device__ __forceinline__ uint32_t ld_cg32(const uint32_t *p) { return __ldcg(p); }
 
-/* One count into entry list e[0..n): returns true when done, false when the slot is full. */
-__device__ __forceinline__ bool count_in_entries(uint32_t *e, int n, unsigned code, unsigned long long &claims) {
-  for (int i = 0; i < n; ++i) {
-    uint32_t w = ld_cg32(e + i);
+/* One count into the entry words e[0..n) of a slot whose current contents were read into
+ * `seen`.  Returns true when counted, false when every entry holds another biedge (slot
+ * full).  A free entry is claimed with CAS; a stale free entry (claimed since the read)
+ * shows up as a failed CAS returning the claimer's word.  Increments are fire-and-forget
+ * while the count is below 2^24; above that the returned value is checked so that the
+ * `big` bit is set before the 26-bit count can wrap. */
+template <int NE>
+__device__ __forceinline__ bool count_in_entries(uint32_t *e, const uint32_t *seen, unsigned code,
+                                                 unsigned long long &claims) {
+  #pragma unroll
+  for (int i = 0; i < NE; ++i) {
+    uint32_t w = seen[i];
     if (w == 0) {
       const uint32_t nw = (code << E_CODE_SHIFT) | (1u << E_COUNT_SHIFT);
       const uint32_t old = atomicCAS(e + i, 0u, nw);
@@ -284,8 +317,12 @@ __device__ __forceinline__ bool count_in_entries(uint32_t *e, int n, unsigned co
       w = old;
     }
     if (entry_code(w) == code) {
-      const uint32_t old = atomicAdd(e + i, 1u << E_COUNT_SHIFT);
-      if (old >> 31) atomicOr(e + i, E_BIG);  /* count reached 2^25: remember it stays large */
+      if ((w >> E_COUNT_SHIFT) < (1u << 24) && !(w & E_BIG)) {
+        atomicAdd(e + i, 1u << E_COUNT_SHIFT);          /* result unused: a reduction */
+      } else {
+        const uint32_t old = atomicAdd(e + i, 1u << E_COUNT_SHIFT);
+        if (old >> 31) atomicOr(e + i, E_BIG);
+      }
       return true;
     }
   }
@@ -354,7 +391,17 @@ __device__ __forceinline__ bool table_count(uint64_t *table, uint64_t nslots, ui
   bool seen_primary = false;
   for (uint32_t probe = 0; probe < max_probe; ++probe) {
     uint64_t *slot = table + i * SU;
-    KT key = key_read(KT{}, slot);
+    /* the whole slot in one go: key words and entry words share one 32-byte sector */
+    uint64_t raw[SU];
+    #pragma unroll
+    for (int q = 0; q < SU; q += 2) {
+      const ulonglong2 v = __ldcg((const ulonglong2 *)(slot + q));
+      raw[q] = v.x; raw[q + 1] = v.y;
+    }
+    KT key = KOps<KT>::load(raw);
+    uint32_t seen[NE];
+    #pragma unroll
+    for (int q = 0; q < NE; ++q) seen[q] = (uint32_t)(raw[KWD + q / 2] >> (32 * (q & 1)));
     if (key_is_empty(key)) {
       bool was_empty;
       key_claim(KT{}, slot, x, seen_primary, key, was_empty);
@@ -362,7 +409,7 @@ __device__ __forceinline__ bool table_count(uint64_t *table, uint64_t nslots, ui
     }
     if (key_matches(key, x, seen_primary)) {
       seen_primary = true;
-      if (count_in_entries((uint32_t *)(slot + KWD), NE, code, entry_claims)) return true;
+      if (count_in_entries<NE>((uint32_t *)(slot + KWD), seen, code, entry_claims)) return true;
     }
     if (++i == nslots) i = 0;
   }
@@ -474,8 +521,113 @@ struct FilterArgs {
   DevCounters *ctr;
 };
 
-/* local_insert_by_freqencies (debruijn_graph_map.hpp:1258-1623) for one k-mer block, from
- * its entries in registers; writes the node (compact_multi_biedge counts) over the slot. */
+struct FilterTally {
+  unsigned long long nodes = 0, branch = 0, chain = 0;
+  unsigned hist[16];
+};
+
+/* local_insert_by_freqencies (debruijn_graph_map.hpp:1258-1623) for one k-mer block: the
+ * entry words w[0..ne) of the k-mer, all in registers when CAP is the slot capacity.
+ * Writes the node (compact_multi_biedge counts, flags) over the slot, or a tombstone. */
+template <class KT, int CAP>
+__device__ __forceinline__ void filter_kmer(uint64_t *s, KT key, const uint32_t *w, int ne, const FilterArgs &a,
+                                            FilterTally &t) {
+  constexpr int KWD = Slot<KT>::KEYW;
+  const int k = a.k;
+  /* step 4: per-block sums (:1460-1507) */
+  const bool kpal = k_palindrome(key, k);
+  const bool high = km1_high_palindrome(key, k), low = km1_low_palindrome(key, k);
+  const unsigned first = KOps<KT>::first(key, k), last = KOps<KT>::last(key);
+  const bool oddk = (k & 1) != 0;
+  uint64_t k_f = 0, k1in[4] = {0, 0, 0, 0}, k1out[4] = {0, 0, 0, 0};
+  #pragma unroll
+  for (int q = 0; q < CAP; ++q) {
+    if (q >= ne) break;
+    const uint64_t c = entry_count(w[q]);
+    const unsigned code = entry_code(w[q]);
+    const unsigned in5 = code_in5(code), out5 = code_out5(code);
+    k_f += c;
+    if (in5) {
+      const unsigned ch = in5 - 1;
+      const bool split = oddk && last == 3u - ch && high && !kpal;
+      k1in[ch] += split ? ((c + 1) >> 1) : c;
+    }
+    if (out5) {
+      const unsigned ch = out5 - 1;
+      const bool split = oddk && first == 3u - ch && low && !kpal;
+      k1out[ch] += split ? ((c + 1) >> 1) : c;
+    }
+  }
+  /* caps at FreqType max (:1401-1407) */
+  const uint64_t cmax = 0xFFFF;
+  k_f = min(cmax, k_f);
+  #pragma unroll
+  for (int c = 0; c < 4; ++c) { k1in[c] = min(cmax, k1in[c]); k1out[c] = min(cmax, k1out[c]); }
+  /* step 5: flags (:1410-1448), step 6: trim (:1563-1594), step 7: node update (:256-285) */
+  uint64_t nc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  bool any = false;
+  #pragma unroll
+  for (int q = 0; q < CAP; ++q) {
+    if (q >= ne) break;
+    const uint32_t cnt = entry_count(w[q]);
+    const uint64_t cnt16 = min(cmax, (uint64_t)cnt);
+    const unsigned code = entry_code(w[q]);
+    unsigned in5 = code_in5(code), out5 = code_out5(code);
+    unsigned f = 0;
+    if (a.thresholding) {
+      if (cnt16 < a.t[4] || cnt16 >= a.t[5]) f |= 4;
+      if (k_f < a.t[0] || k_f >= a.t[1]) f |= 8;
+      uint64_t k1 = in5 ? k1in[in5 - 1] : a.t[3];
+      if (k1 < a.t[2] || k1 >= a.t[3]) f |= 2;
+      k1 = out5 ? k1out[out5 - 1] : a.t[3];
+      if (k1 < a.t[2] || k1 >= a.t[3]) f |= 1;
+    }
+    ++t.hist[f];
+    if (f >= 3) continue;
+    if (f == 1) out5 = 0;
+    if (f == 2) in5 = 0;
+    any = true;
+    #pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      nc[c] += (out5 == (unsigned)c + 1) ? cnt16 : 0;
+      nc[4 + c] += (in5 == (unsigned)c + 1) ? cnt16 : 0;
+    }
+    nc[8] += cnt16;
+    if (a.f_keys) {
+      unsigned long long o = atomicAdd(&a.ctr->n_filtered, 1ull);
+      if (o < a.f_cap) {
+        KOps<KT>::store(a.f_keys + o * KWD, key);
+        a.f_edges[o] = code_biedge(biedge_code(in5, out5));
+        a.f_counts[o] = cnt;
+      }
+    }
+  }
+  if (!any) {  /* no kept entry: the k-mer never enters the graph */
+    if (KWD == 1) s[0] = KEY_TOMB; else { s[0] = KEY_TOMB; s[1] = KEY_TOMB; }
+    return;
+  }
+  uint16_t c16[9];
+  #pragma unroll
+  for (int q = 0; q < 9; ++q) c16[q] = (uint16_t)min(cmax, nc[q]);
+  /* IsBranchPoint / IsChainNode (debruijn_graph_filters.hpp:57-220) */
+  unsigned din = 0, dout = 0;
+  bool k1pal = false;
+  #pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    dout += c16[c] > 0;
+    din += c16[4 + c] > 0;
+    if (oddk && c16[c] > 0 && low && (first == 3u - c || first == (unsigned)c)) k1pal = true;
+    if (oddk && c16[4 + c] > 0 && high && (last == 3u - c || last == (unsigned)c)) k1pal = true;
+  }
+  const bool is_branch = din >= 2 || dout >= 2 || kpal || k1pal;
+  const uint32_t flags = is_branch ? NF_BRANCH : NF_CHAIN;
+  ++t.nodes; t.branch += is_branch; t.chain += !is_branch;
+  uint64_t *pw = s + KWD;
+  pw[0] = (uint64_t)c16[0] | ((uint64_t)c16[1] << 16) | ((uint64_t)c16[2] << 32) | ((uint64_t)c16[3] << 48);
+  pw[1] = (uint64_t)c16[4] | ((uint64_t)c16[5] << 16) | ((uint64_t)c16[6] << 32) | ((uint64_t)c16[7] << 48);
+  pw[2] = (uint64_t)c16[8] | ((uint64_t)flags << 16) | (0xFFFFFFFFull << 32);
+}
+
 template <class KT>
 __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
   constexpr int SU = Slot<KT>::U64, NE = Slot<KT>::ENTRIES, KWD = Slot<KT>::KEYW;
@@ -483,132 +635,56 @@ __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
   if (threadIdx.x < 16) s_hist[threadIdx.x] = 0;
   if (threadIdx.x == 0) s_nodes = s_branch = s_chain = 0;
   __syncthreads();
-  const int k = a.k;
-  unsigned long long nodes = 0, branch = 0, chain = 0;
-  unsigned hist[16];
+  FilterTally t;
   #pragma unroll
-  for (int f = 0; f < 16; ++f) hist[f] = 0;
+  for (int f = 0; f < 16; ++f) t.hist[f] = 0;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.nslots; i += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t *s = a.table + i * SU;
-    KT key = KOps<KT>::load(s);
-    if (key_dead(key) || key_cont(key)) continue;
-    /* gather the k-mer's entries: this slot, then continuation slots along the probe run */
-    uint32_t cnt[25];
-    uint8_t code[25];
-    int ne = 0;
-    const uint32_t *e = (const uint32_t *)(s + KWD);
-    bool full = true;
-    for (int j = 0; j < NE; ++j) {
-      uint32_t w = e[j];
-      if (w == 0) { full = false; break; }
-      code[ne] = (uint8_t)entry_code(w); cnt[ne] = entry_count(w); ++ne;
-    }
-    if (full) {
-      uint64_t j = i;
-      for (uint32_t probe = 1; probe < a.max_probe; ++probe) {
-        if (++j == a.nslots) j = 0;
-        uint64_t *s2 = a.table + j * SU;
-        KT k2 = KOps<KT>::load(s2);
-        if (key_is_empty(k2)) break;
-        if (!key_matches(k2, key, true)) continue;
-        const uint32_t *e2 = (const uint32_t *)(s2 + KWD);
-        for (int q = 0; q < NE && ne < 25; ++q) {
-          uint32_t w = e2[q];
-          if (w == 0) break;
-          code[ne] = (uint8_t)entry_code(w); cnt[ne] = entry_count(w); ++ne;
-        }
-        /* the continuation slot is folded into this node */
-        if (KWD == 1) s2[0] = KEY_TOMB; else { s2[0] = KEY_TOMB; s2[1] = KEY_TOMB; }
-      }
-    }
-    /* step 4: per-block sums (:1460-1507) */
-    const bool kpal = k_palindrome(key, k);
-    const bool high = km1_high_palindrome(key, k), low = km1_low_palindrome(key, k);
-    const unsigned first = KOps<KT>::first(key, k), last = KOps<KT>::last(key);
-    const bool oddk = (k & 1) != 0;
-    uint64_t k_f = 0, k1in[4] = {0, 0, 0, 0}, k1out[4] = {0, 0, 0, 0};
-    for (int q = 0; q < ne; ++q) {
-      const uint64_t c = cnt[q];
-      const unsigned in5 = code_in5(code[q]), out5 = code_out5(code[q]);
-      k_f += c;
-      if (in5) {
-        const unsigned ch = in5 - 1;
-        const bool split = oddk && last == 3u - ch && high && !kpal;
-        k1in[ch] += split ? ((c + 1) >> 1) : c;
-      }
-      if (out5) {
-        const unsigned ch = out5 - 1;
-        const bool split = oddk && first == 3u - ch && low && !kpal;
-        k1out[ch] += split ? ((c + 1) >> 1) : c;
-      }
-    }
-    /* caps at FreqType max (:1401-1407) */
-    const uint64_t cmax = 0xFFFF;
-    k_f = min(cmax, k_f);
+    uint64_t raw[SU];
     #pragma unroll
-    for (int c = 0; c < 4; ++c) { k1in[c] = min(cmax, k1in[c]); k1out[c] = min(cmax, k1out[c]); }
-    /* step 5: flags (:1410-1448), step 6: trim (:1563-1594), step 7: node update (:256-285) */
-    uint64_t nc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    bool any = false;
-    for (int q = 0; q < ne; ++q) {
-      const uint64_t cnt16 = min(cmax, (uint64_t)cnt[q]);
-      unsigned in5 = code_in5(code[q]), out5 = code_out5(code[q]);
-      unsigned f = 0;
-      if (a.thresholding) {
-        if (cnt16 < a.t[4] || cnt16 >= a.t[5]) f |= 4;
-        if (k_f < a.t[0] || k_f >= a.t[1]) f |= 8;
-        uint64_t k1 = in5 ? k1in[in5 - 1] : a.t[3];
-        if (k1 < a.t[2] || k1 >= a.t[3]) f |= 2;
-        k1 = out5 ? k1out[out5 - 1] : a.t[3];
-        if (k1 < a.t[2] || k1 >= a.t[3]) f |= 1;
-      }
-      ++hist[f];
-      if (f >= 3) continue;
-      if (f == 1) out5 = 0;
-      if (f == 2) in5 = 0;
-      any = true;
-      if (out5) nc[out5 - 1] += cnt16;
-      if (in5) nc[4 + in5 - 1] += cnt16;
-      nc[8] += cnt16;
-      if (a.f_keys) {
-        unsigned long long o = atomicAdd(&a.ctr->n_filtered, 1ull);
-        if (o < a.f_cap) {
-          KOps<KT>::store(a.f_keys + o * KWD, key);
-          a.f_edges[o] = code_biedge(biedge_code(in5, out5));
-          a.f_counts[o] = cnt[q];
-        }
-      }
+    for (int q = 0; q < SU; q += 2) {
+      const ulonglong2 v = *(const ulonglong2 *)(s + q);
+      raw[q] = v.x; raw[q + 1] = v.y;
     }
-    if (!any) {  /* no kept entry: the k-mer never enters the graph */
-      if (KWD == 1) s[0] = KEY_TOMB; else { s[0] = KEY_TOMB; s[1] = KEY_TOMB; }
+    const KT key = KOps<KT>::load(raw);
+    if (key_dead(key) || key_cont(key)) continue;
+    uint32_t w[NE];
+    int ne = 0;
+    #pragma unroll
+    for (int q = 0; q < NE; ++q) {
+      w[q] = (uint32_t)(raw[KWD + q / 2] >> (32 * (q & 1)));
+      ne += w[q] != 0;
+    }
+    if (ne < NE) {       /* the common case: every entry of the k-mer is in this slot */
+      filter_kmer<KT, NE>(s, key, w, ne, a, t);
       continue;
     }
-    uint16_t c16[9];
+    /* more entries in continuation slots further along the probe run */
+    uint32_t all[25];
     #pragma unroll
-    for (int q = 0; q < 9; ++q) c16[q] = (uint16_t)min(cmax, nc[q]);
-    /* IsBranchPoint / IsChainNode (debruijn_graph_filters.hpp:57-220) */
-    unsigned din = 0, dout = 0;
-    bool k1pal = false;
-    #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      dout += c16[c] > 0;
-      din += c16[4 + c] > 0;
-      if (oddk && c16[c] > 0 && low && (first == 3u - c || first == (unsigned)c)) k1pal = true;
-      if (oddk && c16[4 + c] > 0 && high && (last == 3u - c || last == (unsigned)c)) k1pal = true;
+    for (int q = 0; q < NE; ++q) all[q] = w[q];
+    uint64_t j = i;
+    for (uint32_t probe = 1; probe < a.max_probe; ++probe) {
+      if (++j == a.nslots) j = 0;
+      uint64_t *s2 = a.table + j * SU;
+      const KT k2 = KOps<KT>::load(s2);
+      if (key_is_empty(k2)) break;
+      if (!key_matches(k2, key, true)) continue;
+      const uint32_t *e2 = (const uint32_t *)(s2 + KWD);
+      for (int q = 0; q < NE && ne < 25; ++q) {
+        if (e2[q] == 0) break;
+        all[ne++] = e2[q];
+      }
+      /* the continuation slot is folded into this node */
+      if (KWD == 1) s2[0] = KEY_TOMB; else { s2[0] = KEY_TOMB; s2[1] = KEY_TOMB; }
     }
-    const bool is_branch = din >= 2 || dout >= 2 || kpal || k1pal;
-    const uint32_t flags = is_branch ? NF_BRANCH : NF_CHAIN;
-    ++nodes; branch += is_branch; chain += !is_branch;
-    uint64_t *pw = s + KWD;
-    pw[0] = (uint64_t)c16[0] | ((uint64_t)c16[1] << 16) | ((uint64_t)c16[2] << 32) | ((uint64_t)c16[3] << 48);
-    pw[1] = (uint64_t)c16[4] | ((uint64_t)c16[5] << 16) | ((uint64_t)c16[6] << 32) | ((uint64_t)c16[7] << 48);
-    pw[2] = (uint64_t)c16[8] | ((uint64_t)flags << 16) | (0xFFFFFFFFull << 32);
+    filter_kmer<KT, 25>(s, key, all, ne, a, t);
   }
-  nodes = warp_sum(nodes); branch = warp_sum(branch); chain = warp_sum(chain);
+  unsigned long long nodes = warp_sum(t.nodes), branch = warp_sum(t.branch), chain = warp_sum(t.chain);
   if ((threadIdx.x & 31) == 0) { atomicAdd(&s_nodes, nodes); atomicAdd(&s_branch, branch); atomicAdd(&s_chain, chain); }
   #pragma unroll
   for (int f = 0; f < 16; ++f) {
-    unsigned long long h = warp_sum(hist[f]);
+    unsigned long long h = warp_sum(t.hist[f]);
     if ((threadIdx.x & 31) == 0 && h) atomicAdd(&s_hist[f], h);
   }
   __syncthreads();
@@ -704,8 +780,9 @@ bruno_status run_index_reads(Ctx *c) {
     cudaMemcpyAsync(&c->dctr->last_nonws, &neg, sizeof(neg), cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(&c->dctr->bad_line, &nb, sizeof(nb), cudaMemcpyHostToDevice, c->stream);
     c->launches += 3;
+    const bool aligned = ((uintptr_t)sg.ptr & 15) == 0;
     k_tile_stats<<<(unsigned)tiles, TPB, 0, c->stream>>>((const unsigned char *)sg.ptr, sg.n, (uint64_t *)c->tile_cnt.p,
-                                                          c->dctr);
+                                                          c->dctr, aligned);
     scan_u64((const uint64_t *)c->tile_cnt.p, (uint64_t *)c->tile_base.p, tiles, &c->dctr->n_records, c->stream);
     if ((st = sync_counters(c)) != BRUNO_OK) return st;
     /* n_records temporarily holds the total newline count: records <= newlines / 4 + 1 */
@@ -715,7 +792,8 @@ bruno_status run_index_reads(Ctx *c) {
     if ((st = ensure(c, c->rend, (rcap + upper) * 8, true)) != BRUNO_OK) return st;
     k_index_lines<<<(unsigned)tiles, TPB, 0, c->stream>>>((const unsigned char *)sg.ptr, sg.n,
                                                            (const uint64_t *)c->tile_base.p, (uint64_t *)c->rstart.p,
-                                                           (uint64_t *)c->rend.p, rcap, rcap + upper, c->dctr);
+                                                           (uint64_t *)c->rend.p, rcap, rcap + upper, c->dctr,
+                                                           aligned);
     if ((st = sync_counters(c)) != BRUNO_OK) return st;
     const DevCounters &h = *c->hctr;
     if (h.last_nonws < 0) continue;  /* empty or blank file */
@@ -740,7 +818,7 @@ bruno_status count_typed(Ctx *c) {
   uint64_t slots = c->cfg.table_slots;
   cudaEventRecord(c->kev[0], c->stream);
   if (slots == 0) {
-    const int hb = std::max(1, std::min<int>(sms * 2, (int)((nreads + 7) / 8)));
+    const int hb = std::max(1, std::min<int>(sms * 8, (int)((nreads + 7) / 8)));
     if ((st = ensure(c, c->blk_cnt, (size_t)hb * HLL_M)) != BRUNO_OK) return st;
     k_hll<KT><<<hb, TPB, 0, c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k,
                                          (uint8_t *)c->blk_cnt.p);

@@ -82,6 +82,7 @@ bruno_status bruno_ctx_create(const bruno_cfg *cfg, bruno_ctx **out) {
   if (!c) return BRUNO_ERR_OOM;
   c->cfg = *cfg;
   c->W = cfg->k <= 31 ? 1 : 2;
+  c->exact_ranking = cfg->exact_ranking != 0;
   bruno_status st = cuda_check(c, cudaSetDevice(cfg->device), "cudaSetDevice");
   if (st == BRUNO_OK) st = cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
   c->own_stream = true;

@@ -346,6 +346,167 @@ __global__ void __launch_bounds__(TPB) k_lr_apply(ChainState *cs, const uint32_t
   }
 }
 
+/* ================================================================ O(M) ranking
+ * For chain maps whose pointers are mutually consistent (every chain-pointing side of a
+ * node is answered by the facing side of its target), the chain map is a union of simple
+ * paths and cycles and the reference's round-synchronous rule has a closed form: a side
+ * at distance a > 0 from its path's end is marked in round floor(log2 a) and ends as
+ * (that end node, a | term_mask); terminal sides never change; cycle nodes never finish
+ * and their distances are 2^rounds when the loop stops; the loop runs
+ * floor(log2(n_max - 1)) + 1 rounds for the longest path (1 if only cycles remain);
+ * separate_cycles then removes exactly the cycle nodes.  list_rank and
+ * list_rank_min_update reach the same state on such maps.  So the ranks are computed with
+ * a ruling set: rulers (every path end plus a hashed 1/32 sample) walk to their
+ * neighbouring rulers, the ruler lists are ranked by pointer jumping, and every node adds
+ * its offset to its ruler's ranks. */
+constexpr uint32_t RULER_SAMPLE = 32;
+struct Near { uint32_t r; uint32_t df; };          /* ruler ordinal; distance | flip << 31 */
+struct Jump { uint32_t t; uint32_t fd; uint64_t d; }; /* ruler ordinal; flip | done << 1; distance */
+constexpr uint32_t NEAR_NONE = 0xFFFFFFFFu, NEAR_END = 0xFFFFFFFEu;
+
+__device__ __forceinline__ bool side_terminal(uint32_t D) { return (D & DM) == 0; }
+__device__ __forceinline__ uint64_t side_ptr(const ChainState &s, int side) { return side ? s.outP : s.inP; }
+__device__ __forceinline__ uint32_t side_dist(const ChainState &s, int side) { return side ? s.outD : s.inD; }
+
+/* consistency check + ruler selection */
+__global__ void __launch_bounds__(TPB) k_fast_check(const ChainState *cs, uint64_t M, uint32_t *rid, uint32_t *rnode,
+                                                     Near *near, DevCounters *ctr) {
+  unsigned long long bad = 0;
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < M; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t v = i0 + threadIdx.x;
+    bool ruler = false;
+    if (v < M) {
+      const ChainState st = cs[v];
+      bool term_side = false;
+      for (int s = 0; s < 2; ++s) {
+        const uint32_t D = side_dist(st, s);
+        const uint64_t P = side_ptr(st, s);
+        near[2 * v + s] = Near{side_terminal(D) ? NEAR_END : NEAR_NONE, 0};
+        if (side_terminal(D)) { term_side = true; continue; }
+        if (D != 1 || (P & (PF_EXT | PF_BLANK))) { ++bad; continue; }
+        const uint32_t t = (uint32_t)P;
+        const int f = (P & PF_FLIP) ? 1 : 0;
+        const ChainState ts = cs[t];
+        const int facing = f ? s : 1 - s;
+        const uint64_t back = side_ptr(ts, facing);
+        if (side_dist(ts, facing) != 1 || (back & (PF_EXT | PF_BLANK)) || (uint32_t)back != (uint32_t)v ||
+            (((back & PF_FLIP) ? 1 : 0) != f))
+          ++bad;
+      }
+      ruler = term_side || (mix64(v * 0x9e3779b97f4a7c15ull + 0x632be59bd9b4e019ull) % RULER_SAMPLE) == 0;
+    }
+    const unsigned long long o = warp_append(ruler, &ctr->lr_remaining);
+    if (v < M) rid[v] = ruler ? (uint32_t)o : NONE32;
+    if (ruler) rnode[o] = (uint32_t)v;
+  }
+  bad = warp_sum(bad);
+  if ((threadIdx.x & 31) == 0 && bad) atomicAdd(&ctr->lr_multi, bad);
+}
+
+/* every ruler walks both ways to the next ruler, labelling the nodes it passes */
+__global__ void __launch_bounds__(TPB) k_fast_walk(const ChainState *cs, const uint32_t *rid, const uint32_t *rnode,
+                                                    uint64_t R, uint64_t M, Near *near) {
+  for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 2 * R; q += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t ord = (uint32_t)(q >> 1), r = rnode[ord];
+    const int s0 = (int)(q & 1);
+    ChainState st = cs[r];
+    if (side_terminal(side_dist(st, s0))) continue;
+    uint32_t cur = r, dist = 0, flip = 0;
+    int dir = s0;
+    for (uint64_t steps = 0; steps < M; ++steps) {
+      const uint64_t P = side_ptr(st, dir);
+      const uint32_t nxt = (uint32_t)P;
+      const uint32_t f = (P & PF_FLIP) ? 1u : 0u;
+      flip ^= f;
+      ++dist;
+      const int ndir = f ? 1 - dir : dir;      /* travel direction in the next node's frame */
+      const int entered = 1 - ndir;             /* the side we came in through */
+      near[2ull * nxt + entered] = Near{ord, dist | (flip << 31)};
+      const uint32_t nr = rid[nxt];
+      if (nr != NONE32) { near[2ull * r + s0] = Near{nr, dist | (flip << 31)}; break; }
+      cur = nxt;
+      dir = ndir;
+      st = cs[cur];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(TPB) k_fast_jinit(const uint32_t *rnode, const Near *near, uint64_t R, Jump *E) {
+  for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 2 * R; q += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t ord = (uint32_t)(q >> 1), v = rnode[ord];
+    const Near n = near[2ull * v + (q & 1)];
+    if (n.r == NEAR_END) E[q] = Jump{ord, 2u, 0};                      /* done, points at itself */
+    else if (n.r == NEAR_NONE) E[q] = Jump{ord, 0u, 0};                /* unreachable: stays undone */
+    else E[q] = Jump{n.r, n.df >> 31, (uint64_t)(n.df & DM)};
+  }
+}
+
+__global__ void __launch_bounds__(TPB) k_fast_jump(const Jump *E, Jump *F, uint64_t R, DevCounters *ctr) {
+  unsigned long long undone = 0;
+  for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 2 * R; q += (uint64_t)gridDim.x * blockDim.x) {
+    Jump e = E[q];
+    if (!(e.fd & 2u)) {
+      const int s = (int)(q & 1);
+      const uint32_t f = e.fd & 1u;
+      const Jump n = E[2ull * e.t + (f ? 1 - s : s)];   /* continue in the same travel direction */
+      const uint64_t sum = e.d + n.d;   /* saturate: only ruler cycles keep growing */
+      e = Jump{n.t, (f ^ (n.fd & 1u)) | (n.fd & 2u), sum > 0xFFFFFFFFFFFFull ? 0xFFFFFFFFFFFFull : sum};
+    }
+    undone += !(e.fd & 2u);
+    F[q] = e;
+  }
+  undone = warp_sum(undone);
+  if ((threadIdx.x & 31) == 0 && undone) atomicAdd(&ctr->lr_applied, undone);
+}
+
+__global__ void __launch_bounds__(TPB) k_fast_final(ChainState *cs, uint64_t M, const uint32_t *rid,
+                                                     const uint32_t *rnode, const Near *near, const Jump *E,
+                                                     uint8_t *removed, unsigned long long *nmax, DevCounters *ctr) {
+  unsigned long long ncy = 0, niso = 0, mx = 0;
+  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < M; v += (uint64_t)gridDim.x * blockDim.x) {
+    ChainState st = cs[v];
+    bool cyc = false;
+    uint64_t len = 1;
+    uint64_t P[2] = {st.inP, st.outP};
+    uint32_t D[2] = {st.inD, st.outD};
+    for (int s = 0; s < 2; ++s) {
+      if (side_terminal(D[s])) continue;
+      Jump e;
+      uint32_t flip = 0, d0 = 0;
+      if (rid[v] != NONE32) {
+        e = E[2ull * rid[v] + s];
+      } else {
+        const Near n = near[2ull * v + s];
+        if (n.r >= NEAR_END) { cyc = true; continue; }
+        flip = n.df >> 31;
+        d0 = n.df & DM;
+        e = E[2ull * n.r + (flip ? 1 - s : s)];
+      }
+      if (!(e.fd & 2u)) { cyc = true; continue; }
+      const uint64_t dist = d0 + e.d;
+      len += dist;
+      P[s] = (uint64_t)rnode[e.t] | (((flip ^ (e.fd & 1u)) != 0) ? PF_FLIP : 0ull);
+      D[s] = (uint32_t)dist | TM;
+    }
+    uint8_t r = 0;
+    if (cyc) { r = 1; ++ncy; }
+    else {
+      st.inP = P[0]; st.outP = P[1]; st.inD = D[0]; st.outD = D[1];
+      cs[v] = st;
+      mx = max(mx, (unsigned long long)len);
+      if (st.inD == TM && st.outD == TM) { r = 2; ++niso; }
+    }
+    removed[v] = r;
+  }
+  ncy = warp_sum(ncy); niso = warp_sum(niso);
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_down_sync(~0u, mx, o));
+  if ((threadIdx.x & 31) == 0) {
+    if (ncy) atomicAdd(&ctr->n_cycle, ncy);
+    if (niso) atomicAdd(&ctr->n_isolated, niso);
+    if (mx) atomicMax(nmax, mx);
+  }
+}
+
 /* separate_cycles(iterations) when anything is unfinished, then separate_isolated */
 __global__ void __launch_bounds__(TPB) k_separate(const ChainState *cs, uint64_t M, int any_unfinished, uint32_t maxd,
                                                    uint8_t *removed, DevCounters *ctr) {
@@ -560,8 +721,69 @@ bruno_status compress_typed(Ctx *c) {
 
 bruno_status run_extract_chains(Ctx *c) { return c->W == 1 ? extract_typed<KW1>(c) : extract_typed<KW2>(c); }
 
+/* The ruling-set ranking; returns false (and changes nothing) if the chain map is not
+ * mutually consistent, in which case the round-synchronous path runs. */
+static bruno_status fast_list_rank(Ctx *c, bool &used) {
+  bruno_status st;
+  used = false;
+  const uint64_t M = c->n_chain, Mb = std::max<uint64_t>(1, M);
+  if (M >= (1ull << 30)) return BRUNO_OK;
+  const int sms = sms_count();
+  ChainState *cs = (ChainState *)c->cstate.p;
+  if ((st = ensure(c, c->unf0, Mb * 4)) != BRUNO_OK) return st;        /* rid */
+  if ((st = ensure(c, c->unf1, Mb * 4)) != BRUNO_OK) return st;        /* rnode */
+  if ((st = ensure(c, c->pend, Mb * 16)) != BRUNO_OK) return st;       /* near[2M] */
+  if ((st = ensure(c, c->removed, Mb)) != BRUNO_OK) return st;
+  uint32_t *rid = (uint32_t *)c->unf0.p, *rnode = (uint32_t *)c->unf1.p;
+  Near *near = (Near *)c->pend.p;
+  cudaMemsetAsync(&c->dctr->lr_applied, 0, 32, c->stream);   /* applied, remaining, cycles, multi */
+  k_fast_check<<<sms * 8, TPB, 0, c->stream>>>(cs, M, rid, rnode, near, c->dctr);
+  c->launches += 1;
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  if (c->hctr->lr_multi != 0) return BRUNO_OK;                /* inconsistent pointers */
+  const uint64_t R = c->hctr->lr_remaining, Rb = std::max<uint64_t>(1, R);
+  if ((st = ensure(c, c->pay, Rb * 2 * sizeof(Jump) * 2)) != BRUNO_OK) return st;
+  Jump *E = (Jump *)c->pay.p, *F = E + 2 * Rb;
+  const int gw = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 16, (2 * R + TPB - 1) / TPB));
+  k_fast_walk<<<gw, TPB, 0, c->stream>>>(cs, rid, rnode, R, M, near);
+  k_fast_jinit<<<gw, TPB, 0, c->stream>>>(rnode, near, R, E);
+  c->launches += 2;
+  uint64_t prev = ~0ull;
+  for (int round = 0; round < 64; ++round) {
+    cudaMemsetAsync(&c->dctr->lr_applied, 0, 8, c->stream);
+    k_fast_jump<<<gw, TPB, 0, c->stream>>>(E, F, R, c->dctr);
+    c->launches += 1;
+    std::swap(E, F);
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    const uint64_t undone = c->hctr->lr_applied;
+    if (undone == 0 || undone == prev) break;   /* only ruler cycles keep sides undone */
+    prev = undone;
+  }
+  cudaMemsetAsync(&c->dctr->n_cycle, 0, 16, c->stream);
+  cudaMemsetAsync(&c->dctr->n_heads, 0, 8, c->stream);        /* longest path, in nodes */
+  k_fast_final<<<sms * 8, TPB, 0, c->stream>>>(cs, M, rid, rnode, near, E, (uint8_t *)c->removed.p,
+                                                &c->dctr->n_heads, c->dctr);
+  c->launches += 1;
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  c->n_cycle = c->hctr->n_cycle;
+  c->n_isolated = c->hctr->n_isolated;
+  const uint64_t nmax = c->hctr->n_heads;
+  uint64_t it = 0;
+  if (nmax >= 2) { uint64_t x = nmax - 1; while (x >>= 1) ++it; ++it; }  /* floor(log2(nmax-1)) + 1 */
+  else if (c->n_cycle > 0) it = 1;
+  c->iterations = it;
+  c->multi = 0;
+  used = true;
+  return BRUNO_OK;
+}
+
 bruno_status run_list_rank(Ctx *c, int min_update) {
   bruno_status st;
+  if (!c->exact_ranking) {
+    bool used = false;
+    if ((st = fast_list_rank(c, used)) != BRUNO_OK) return st;
+    if (used) return BRUNO_OK;
+  }
   const uint64_t M = c->n_chain, Mb = std::max<uint64_t>(1, M);
   if ((st = ensure(c, c->unf0, Mb * 4)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->unf1, Mb * 4)) != BRUNO_OK) return st;

@@ -87,6 +87,7 @@ struct Ctx {
   /* chains */
   Buf ckey, cslot, cedge, cstate, pend, pay, unf0, unf1, removed;
   uint64_t iterations = 0, n_cycle = 0, n_isolated = 0, multi = 0;
+  bool exact_ranking = false;    /* force the round-synchronous ranking (tests) */
 
   /* emission */
   Buf r_K, r_rep, r_dist, rep_idx, head_of, heads, head_len, head_off, ch_rep, ch_off, ch_chars;

@@ -55,6 +55,8 @@ typedef struct bruno_cfg {
   double max_load;          /* target table load when sizing (0 = 0.5) */
   int32_t keep_k2;          /* 1: keep enough state to copy out the raw (k+2)-mer counts */
   int32_t keep_filtered;    /* 1: record the filtered (k+2)-mer entries for copy-out */
+  int32_t exact_ranking;    /* 1: always run the round-synchronous ranking; 0: use the O(M)
+                               ruling-set ranking whenever the chain map is consistent */
 } bruno_cfg;
 
 typedef struct bruno_sizes {
