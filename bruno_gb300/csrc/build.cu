@@ -130,6 +130,7 @@ __global__ void __launch_bounds__(TPB) k_index_lines(const unsigned char *buf, u
   const uint64_t t1 = (n < t0 + TILE ? n : t0 + TILE);
   const long long E = ctr->last_nonws + 1;  /* effective end (exclusive) */
   uint64_t base = tile_base[blockIdx.x];
+  unsigned long long nl_eff = 0;  /* newlines ending lines before E, max over this thread */
   if (blockIdx.x == 0 && threadIdx.x == 0 && E > 0 && buf[0] != '@') atomicMin(&ctr->bad_line, 0ull);
   /* stripes of TPB*16 bytes, 16 consecutive bytes per thread, in byte order */
   for (uint64_t s0 = t0; s0 < t1; s0 += (uint64_t)TPB * 16) {
@@ -154,7 +155,7 @@ __global__ void __launch_bounds__(TPB) k_index_lines(const unsigned char *buf, u
       const uint64_t p = g0 + i;
       if ((long long)p < E) {
         const uint64_t ln = j;  /* this newline ends line ln */
-        atomicMax(&ctr->n_newlines_eff, (unsigned long long)(ln + 1));
+        nl_eff = ln + 1;
         const uint64_t r = ln >> 2;
         const unsigned role = (unsigned)(ln & 3);
         if (role == 0 && rbase + r < rcap) rstart[rbase + r] = (uint64_t)(buf + p + 1);
@@ -174,6 +175,15 @@ __global__ void __launch_bounds__(TPB) k_index_lines(const unsigned char *buf, u
     }
     base += total;
   }
+  __shared__ unsigned long long snl[TPB / 32];
+  for (int o = 16; o > 0; o >>= 1) nl_eff = max(nl_eff, __shfl_down_sync(~0u, nl_eff, o));
+  if ((threadIdx.x & 31) == 0) snl[threadIdx.x >> 5] = nl_eff;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long m = 0;
+    for (int i = 0; i < TPB / 32; ++i) m = max(m, snl[i]);
+    if (m) atomicMax(&ctr->n_newlines_eff, m);
+  }
 }
 
 /* ============================================================ k-mer extraction */
@@ -188,17 +198,22 @@ struct ReadView {
   uint32_t L;
 };
 
-/* Loads the bases of chunk [p0, pend) plus flanks into words[]; returns nothing.  All
- * bases are known to be ACGT (the read passed the N filter). */
-__device__ __forceinline__ void stage_chunk(const ReadView &rv, uint32_t p0, uint32_t pend, int k, uint64_t *words,
+/* Loads the bases of chunk [p0, pend) plus flanks into words[]; returns true if any of
+ * those bases is not A/C/G/T (the read must then be dropped). */
+__device__ __forceinline__ bool stage_chunk(const ReadView &rv, uint32_t p0, uint32_t pend, int k, uint64_t *words,
                                             int lane) {
+  bool bad = false;
   const long long c0 = (long long)p0 - 32;
   const long long cend = ((long long)rv.L < (long long)pend + k + 1) ? (long long)rv.L : (long long)pend + k + 1;
   const int nw = (int)((cend - c0 + 31) >> 5);
   for (int wi = 0; wi < nw; ++wi) {
     const long long c = c0 + 32 * wi + lane;
     unsigned code = 0;
-    if (c >= 0 && c < (long long)rv.L) code = (unsigned)base_code(rv.s[c]);
+    if (c >= 0 && c < (long long)rv.L) {
+      const int bc = base_code(rv.s[c]);
+      bad |= bc < 0;
+      code = (unsigned)bc & 3u;
+    }
     const unsigned m0 = __ballot_sync(~0u, code & 1u), m1 = __ballot_sync(~0u, code & 2u);
     if (lane == 0) {
       /* interleave: base i -> bits (62-2i, 63-2i), high bit from m1 */
@@ -216,6 +231,7 @@ __device__ __forceinline__ void stage_chunk(const ReadView &rv, uint32_t p0, uin
   }
   if (lane < 3) words[nw + lane] = 0;
   __syncwarp();
+  return __any_sync(~0u, bad);
 }
 
 __device__ __forceinline__ unsigned base_at(const uint64_t *w, int i) {
@@ -224,29 +240,32 @@ __device__ __forceinline__ unsigned base_at(const uint64_t *w, int i) {
 
 /* ============================================================ distinct estimate */
 
-constexpr int HLL_P = 14;
+constexpr int HLL_P = 12;
 constexpr int HLL_M = 1 << HLL_P;
 
 template <class KT>
 __global__ void __launch_bounds__(TPB) k_hll(const uint64_t *rstart, const uint64_t *rend, uint64_t nreads, int k,
                                               uint8_t *partial) {
   __shared__ uint64_t sw[TPB / 32][CHUNK_WORDS];
-  __shared__ unsigned int reg[HLL_M / 4];
-  for (int i = threadIdx.x; i < HLL_M / 4; i += TPB) reg[i] = 0;
+  __shared__ unsigned int reg[HLL_M];
+  for (int i = threadIdx.x; i < HLL_M; i += TPB) reg[i] = 0;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint64_t *words = sw[warp];
   for (uint64_t r = (uint64_t)blockIdx.x * (TPB / 32) + warp; r < nreads; r += (uint64_t)gridDim.x * (TPB / 32)) {
     ReadView rv{(const unsigned char *)rstart[r], (uint32_t)(rend[r] - rstart[r])};
     if (rv.L < (uint32_t)k + 2) continue;
-    bool bad = false;
-    for (uint32_t i = lane; i < rv.L; i += 32) bad |= base_code(rv.s[i]) < 0;
-    if (__any_sync(~0u, bad)) continue;
     const uint32_t npos = rv.L - k + 1;
+    const bool one_chunk = npos <= CHUNK_POS;
+    if (!one_chunk) {
+      bool bad = false;
+      for (uint32_t i = lane; i < rv.L; i += 32) bad |= base_code(rv.s[i]) < 0;
+      if (__any_sync(~0u, bad)) continue;
+    }
     for (uint32_t p0 = 0; p0 < npos; p0 += CHUNK_POS) {
       const uint32_t pend = min(npos, p0 + CHUNK_POS);
       __syncwarp();
-      stage_chunk(rv, p0, pend, k, words, lane);
+      if (stage_chunk(rv, p0, pend, k, words, lane) && one_chunk) break;
       for (uint32_t pb = p0; pb < pend; pb += 32) {
         const uint32_t p = pb + lane;
         if (p < pend) {
@@ -256,23 +275,14 @@ __global__ void __launch_bounds__(TPB) k_hll(const uint64_t *rstart, const uint6
           const uint64_t h = mix64(KOps<KT>::hash(x) ^ 0x6a09e667f3bcc909ull);
           const unsigned idx = (unsigned)(h >> (64 - HLL_P));
           const unsigned rho = (unsigned)__clzll((h << HLL_P) | (1ull << (HLL_P - 1))) + 1u;
-          /* byte-wise max inside a 32-bit word */
-          unsigned int *wp = &reg[idx >> 2];
-          const int sh = (idx & 3) * 8;
-          unsigned int old = *((volatile unsigned int *)wp);
-          while (((old >> sh) & 0xFFu) < rho) {
-            unsigned int nv = (old & ~(0xFFu << sh)) | (rho << sh);
-            unsigned int got = atomicCAS(wp, old, nv);
-            if (got == old) break;
-            old = got;
-          }
+          if (rho > reg[idx]) atomicMax(&reg[idx], rho);
         }
       }
     }
   }
   __syncthreads();
-  uint32_t *dst = (uint32_t *)(partial + (uint64_t)blockIdx.x * HLL_M);
-  for (int i = threadIdx.x; i < HLL_M / 4; i += TPB) dst[i] = reg[i];
+  uint8_t *dst = partial + (uint64_t)blockIdx.x * HLL_M;
+  for (int i = threadIdx.x; i < HLL_M; i += TPB) dst[i] = (uint8_t)reg[i];
 }
 
 __global__ void k_hll_merge(const uint8_t *partial, int nblocks, DevCounters *ctr) {
@@ -296,6 +306,16 @@ struct CountArgs {
 };
 
 __device__ __forceinline__ uint64_t ld_cg(const uint64_t *p) { return __ldcg((const unsigned long long *)p); }
+
+/* one slot (4 or 8 words) with 256-bit relaxed loads: a single L2 request per 32 bytes */
+template <int SU>
+__device__ __forceinline__ void ld_slot(const uint64_t *slot, uint64_t *raw) {
+  #pragma unroll
+  for (int q = 0; q < SU; q += 4)
+    asm volatile("ld.relaxed.gpu.global.v4.u64 {%0, %1, %2, %3}, [%4];"
+                 : "=l"(raw[q]), "=l"(raw[q + 1]), "=l"(raw[q + 2]), "=l"(raw[q + 3])
+                 : "l"(slot + q) : "memory");
+}
 __device__ __forceinline__ uint32_t ld_cg32(const uint32_t *p) { return __ldcg(p); }
 
 /* One count into the entry words e[0..n) of a slot whose current contents were read into
@@ -381,23 +401,17 @@ __device__ __forceinline__ bool key_dead(KW2 k) { return (k.hi & KEY_DEAD_BIT) !
 __device__ __forceinline__ bool key_cont(KW1 k) { return (k.v & KEY_CONT) != 0; }
 __device__ __forceinline__ bool key_cont(KW2 k) { return (k.hi & KEY_CONT) != 0; }
 
-/* Counts one canonical (k-mer, biedge code) occurrence.  Returns false if the probe limit
- * was reached. */
+/* Counts one canonical (k-mer, biedge code) occurrence whose first probe slot `i` was
+ * already read into raw[].  Returns false if the probe limit was reached. */
 template <class KT>
 __device__ __forceinline__ bool table_count(uint64_t *table, uint64_t nslots, uint32_t max_probe, KT x, unsigned code,
-                                            unsigned long long &slot_claims, unsigned long long &entry_claims) {
+                                            uint64_t i, uint64_t *raw, unsigned long long &slot_claims,
+                                            unsigned long long &entry_claims) {
   constexpr int SU = Slot<KT>::U64, NE = Slot<KT>::ENTRIES, KWD = Slot<KT>::KEYW;
-  uint64_t i = __umul64hi(KOps<KT>::hash(x), nslots);
   bool seen_primary = false;
   for (uint32_t probe = 0; probe < max_probe; ++probe) {
     uint64_t *slot = table + i * SU;
-    /* the whole slot in one go: key words and entry words share one 32-byte sector */
-    uint64_t raw[SU];
-    #pragma unroll
-    for (int q = 0; q < SU; q += 2) {
-      const ulonglong2 v = __ldcg((const ulonglong2 *)(slot + q));
-      raw[q] = v.x; raw[q + 1] = v.y;
-    }
+    if (probe) ld_slot<SU>(slot, raw);
     KT key = KOps<KT>::load(raw);
     uint32_t seen[NE];
     #pragma unroll
@@ -416,8 +430,29 @@ __device__ __forceinline__ bool table_count(uint64_t *table, uint64_t nslots, ui
   return false;
 }
 
+/* the canonical (k-mer, biedge code) at read position p of a staged chunk */
+template <class KT>
+__device__ __forceinline__ void kmer_at(const uint64_t *words, uint32_t p, uint32_t p0, uint32_t L, int k, KT &x,
+                                        unsigned &code) {
+  const int lp = (int)(p - p0 + 32);
+  x = KOps<KT>::extract(words, lp, k);
+  /* biedge in DNA: base before and after the k-mer in the read (0 = read end) */
+  unsigned in5 = (p > 0) ? base_at(words, lp - 1) + 1u : 0u;
+  unsigned out5 = (p + k < L) ? base_at(words, lp + k) + 1u : 0u;
+  /* lex_less: keep if x < rc(x), else flip the k-mer and reverse-complement the biedge
+   * (in' = comp(out), out' = comp(in); comp of a DNA code c is 3-c) */
+  KT y = KOps<KT>::rc(x, k);
+  if (!KOps<KT>::lt(x, y)) {
+    x = y;
+    const unsigned ni = out5 ? 5u - out5 : 0u, no = in5 ? 5u - in5 : 0u;
+    in5 = ni; out5 = no;
+  }
+  code = biedge_code(in5, out5);
+}
+
 template <class KT>
 __global__ void __launch_bounds__(TPB, 4) k_count(CountArgs a) {
+  constexpr int SU = Slot<KT>::U64;
   __shared__ uint64_t sw[TPB / 32][CHUNK_WORDS];
   __shared__ unsigned long long s_inst, s_used, s_slots, s_entries;
   __shared__ int s_full;
@@ -431,33 +466,42 @@ __global__ void __launch_bounds__(TPB, 4) k_count(CountArgs a) {
   for (uint64_t r = (uint64_t)blockIdx.x * (TPB / 32) + warp; r < a.nreads; r += (uint64_t)gridDim.x * (TPB / 32)) {
     ReadView rv{(const unsigned char *)a.rstart[r], (uint32_t)(a.rend[r] - a.rstart[r])};
     if (rv.L < (uint32_t)k + 2) continue;          /* shorter than the k+2 window */
-    bool bad = false;
-    for (uint32_t i = lane; i < rv.L; i += 32) bad |= base_code(rv.s[i]) < 0;
-    if (__any_sync(~0u, bad)) continue;            /* reads containing N are dropped */
-    used += (lane == 0);
     const uint32_t npos = rv.L - k + 1;
+    const bool one_chunk = npos <= CHUNK_POS;
+    if (!one_chunk) {                               /* long read: N filter first */
+      bool bad = false;
+      for (uint32_t i = lane; i < rv.L; i += 32) bad |= base_code(rv.s[i]) < 0;
+      if (__any_sync(~0u, bad)) continue;
+    }
     for (uint32_t p0 = 0; p0 < npos; p0 += CHUNK_POS) {
       const uint32_t pend = min(npos, p0 + CHUNK_POS);
       __syncwarp();
-      stage_chunk(rv, p0, pend, k, words, lane);
-      for (uint32_t pb = p0; pb < pend; pb += 32) {
-        const uint32_t p = pb + lane;
-        if (p >= pend) continue;
-        const int lp = (int)(p - p0 + 32);
-        KT x = KOps<KT>::extract(words, lp, k);
-        /* biedge in DNA: base before and after the k-mer in the read (0 = read end) */
-        unsigned in5 = (p > 0) ? base_at(words, lp - 1) + 1u : 0u;
-        unsigned out5 = (p + k < rv.L) ? base_at(words, lp + k) + 1u : 0u;
-        /* lex_less: keep if x < rc(x), else flip the k-mer and reverse-complement the
-         * biedge (in' = comp(out), out' = comp(in); comp of a DNA code c is 3-c) */
-        KT y = KOps<KT>::rc(x, k);
-        if (!KOps<KT>::lt(x, y)) {
-          x = y;
-          unsigned ni = out5 ? (4u - out5) + 1u : 0u, no = in5 ? (4u - in5) + 1u : 0u;
-          in5 = ni; out5 = no;
+      if (stage_chunk(rv, p0, pend, k, words, lane) && one_chunk) break;   /* reads with N are dropped */
+      if (p0 == 0) used += (lane == 0);
+      /* two k-mers per lane in flight: both first-probe slots are read before either is used */
+      for (uint32_t pb = p0; pb < pend; pb += 64) {
+        const uint32_t pa = pb + lane, pc = pb + 32 + lane;
+        KT xa{}, xc{};
+        unsigned ca = 0, cc = 0;
+        uint64_t ia = 0, ic = 0, ra[SU], rc[SU];
+        if (pa < pend) {
+          kmer_at<KT>(words, pa, p0, rv.L, k, xa, ca);
+          ia = __umul64hi(KOps<KT>::hash(xa), a.nslots);
+          ld_slot<SU>(a.table + ia * SU, ra);
         }
-        ++inst;
-        if (!table_count<KT>(a.table, a.nslots, a.max_probe, x, biedge_code(in5, out5), slots, entries)) full = true;
+        if (pc < pend) {
+          kmer_at<KT>(words, pc, p0, rv.L, k, xc, cc);
+          ic = __umul64hi(KOps<KT>::hash(xc), a.nslots);
+          ld_slot<SU>(a.table + ic * SU, rc);
+        }
+        if (pa < pend) {
+          ++inst;
+          if (!table_count<KT>(a.table, a.nslots, a.max_probe, xa, ca, ia, ra, slots, entries)) full = true;
+        }
+        if (pc < pend) {
+          ++inst;
+          if (!table_count<KT>(a.table, a.nslots, a.max_probe, xc, cc, ic, rc, slots, entries)) full = true;
+        }
       }
     }
   }

@@ -32,7 +32,7 @@ struct DevCounters {
   unsigned long long flag_hist[16];
   unsigned long long lr_applied, lr_remaining, lr_cycles, lr_multi;
   unsigned long long n_cycle, n_isolated, n_ranked, n_heads, n_chain_chars;
-  unsigned int hll[1 << 14];           /* HyperLogLog registers, p = 14 */
+  unsigned int hll[1 << 12];           /* HyperLogLog registers, p = 12 */
 };
 
 struct Segment { const char *ptr; uint64_t n; };
