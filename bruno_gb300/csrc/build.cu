@@ -518,15 +518,14 @@ __global__ void __launch_bounds__(TPB, 4) k_count(CountArgs a) {
   }
 }
 
-/* table initialisation: every key word EMPTY, every entry 0 */
+/* table initialisation: every key word EMPTY, every entry 0; written as one flat word
+ * array so that every warp store is 256 contiguous bytes */
 template <class KT>
 __global__ void k_table_init(uint64_t *table, uint64_t nslots) {
   constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t *s = table + i * SU;
-    #pragma unroll
-    for (int w = 0; w < SU; ++w) s[w] = (w < KWD) ? KEY_EMPTY : 0ull;
-  }
+  const uint64_t nw = nslots * SU;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += (uint64_t)gridDim.x * blockDim.x)
+    table[i] = ((int)(i % SU) < KWD) ? KEY_EMPTY : 0ull;
 }
 
 /* ============================================================ raw (k+2)-mer dump */
@@ -554,7 +553,22 @@ __global__ void __launch_bounds__(TPB) k_dump_k2(const uint64_t *table, uint64_t
 
 /* ============================================================ filter + insert */
 
+/* warp-aggregated append among the lanes that reach this call together */
+__device__ __forceinline__ unsigned long long append_active(bool want, unsigned long long *counter) {
+  const unsigned act = __activemask();
+  const unsigned m = __ballot_sync(act, want);
+  const int lane = threadIdx.x & 31;
+  if (!m) return 0;
+  const int leader = __ffs(m) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(m));
+  base = __shfl_sync(act, base, leader);
+  return base + __popc(m & ((1u << lane) - 1));
+}
+
 struct FilterArgs {
+  uint32_t *chain_list, *branch_list;   /* slot indices of chain / branch nodes */
+  uint64_t list_cap;
   uint64_t *table;
   uint64_t nslots;
   int k;
@@ -566,7 +580,7 @@ struct FilterArgs {
 };
 
 struct FilterTally {
-  unsigned long long nodes = 0, branch = 0, chain = 0;
+  unsigned long long nodes = 0, branch = 0, chain = 0;   /* branch/chain: statistics only */
   unsigned hist[16];
 };
 
@@ -574,8 +588,8 @@ struct FilterTally {
  * entry words w[0..ne) of the k-mer, all in registers when CAP is the slot capacity.
  * Writes the node (compact_multi_biedge counts, flags) over the slot, or a tombstone. */
 template <class KT, int CAP>
-__device__ __forceinline__ void filter_kmer(uint64_t *s, KT key, const uint32_t *w, int ne, const FilterArgs &a,
-                                            FilterTally &t) {
+__device__ __forceinline__ void filter_kmer(uint64_t *s, uint64_t slot_index, KT key, const uint32_t *w, int ne,
+                                            const FilterArgs &a, FilterTally &t) {
   constexpr int KWD = Slot<KT>::KEYW;
   const int k = a.k;
   /* step 4: per-block sums (:1460-1507) */
@@ -666,10 +680,17 @@ __device__ __forceinline__ void filter_kmer(uint64_t *s, KT key, const uint32_t 
   const bool is_branch = din >= 2 || dout >= 2 || kpal || k1pal;
   const uint32_t flags = is_branch ? NF_BRANCH : NF_CHAIN;
   ++t.nodes; t.branch += is_branch; t.chain += !is_branch;
+  /* chain nodes get their chain index right here (the order of appends is arbitrary and
+   * never observable: every output is keyed by k-mer) */
+  const unsigned long long oc = append_active(!is_branch, &a.ctr->n_chain);
+  const unsigned long long ob = append_active(is_branch, &a.ctr->n_branch);
+  uint32_t aux = 0xFFFFFFFFu;
+  if (!is_branch && oc < a.list_cap) { a.chain_list[oc] = (uint32_t)slot_index; aux = (uint32_t)oc; }
+  if (is_branch && ob < a.list_cap) a.branch_list[ob] = (uint32_t)slot_index;
   uint64_t *pw = s + KWD;
   pw[0] = (uint64_t)c16[0] | ((uint64_t)c16[1] << 16) | ((uint64_t)c16[2] << 32) | ((uint64_t)c16[3] << 48);
   pw[1] = (uint64_t)c16[4] | ((uint64_t)c16[5] << 16) | ((uint64_t)c16[6] << 32) | ((uint64_t)c16[7] << 48);
-  pw[2] = (uint64_t)c16[8] | ((uint64_t)flags << 16) | (0xFFFFFFFFull << 32);
+  pw[2] = (uint64_t)c16[8] | ((uint64_t)flags << 16) | ((uint64_t)aux << 32);
 }
 
 template <class KT>
@@ -685,11 +706,7 @@ __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.nslots; i += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t *s = a.table + i * SU;
     uint64_t raw[SU];
-    #pragma unroll
-    for (int q = 0; q < SU; q += 2) {
-      const ulonglong2 v = *(const ulonglong2 *)(s + q);
-      raw[q] = v.x; raw[q + 1] = v.y;
-    }
+    ld_slot<SU>(s, raw);
     const KT key = KOps<KT>::load(raw);
     if (key_dead(key) || key_cont(key)) continue;
     uint32_t w[NE];
@@ -700,7 +717,7 @@ __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
       ne += w[q] != 0;
     }
     if (ne < NE) {       /* the common case: every entry of the k-mer is in this slot */
-      filter_kmer<KT, NE>(s, key, w, ne, a, t);
+      filter_kmer<KT, NE>(s, i, key, w, ne, a, t);
       continue;
     }
     /* more entries in continuation slots further along the probe run */
@@ -722,7 +739,7 @@ __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
       /* the continuation slot is folded into this node */
       if (KWD == 1) s2[0] = KEY_TOMB; else { s2[0] = KEY_TOMB; s2[1] = KEY_TOMB; }
     }
-    filter_kmer<KT, 25>(s, key, all, ne, a, t);
+    filter_kmer<KT, 25>(s, i, key, all, ne, a, t);
   }
   unsigned long long nodes = warp_sum(t.nodes), branch = warp_sum(t.branch), chain = warp_sum(t.chain);
   if ((threadIdx.x & 31) == 0) { atomicAdd(&s_nodes, nodes); atomicAdd(&s_branch, branch); atomicAdd(&s_chain, chain); }
@@ -733,9 +750,7 @@ __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
   }
   __syncthreads();
   if (threadIdx.x < 16 && s_hist[threadIdx.x]) atomicAdd(&a.ctr->flag_hist[threadIdx.x], s_hist[threadIdx.x]);
-  if (threadIdx.x == 0) {
-    atomicAdd(&a.ctr->n_nodes, s_nodes); atomicAdd(&a.ctr->n_branch, s_branch); atomicAdd(&a.ctr->n_chain, s_chain);
-  }
+  if (threadIdx.x == 0) atomicAdd(&a.ctr->n_nodes, s_nodes);
 }
 
 /* live graph nodes -> arrays */
@@ -902,6 +917,7 @@ bruno_status count_typed(Ctx *c) {
       c->n_instances = c->hctr->n_instances;
       c->n_reads_used = c->hctr->n_reads_used;
       c->n_entries = c->hctr->n_entries;
+      c->n_slots_claimed = c->hctr->n_slots_claimed;
       return BRUNO_OK;
     }
     slots *= 2;  /* the estimate was too low: grow and count again */
@@ -937,6 +953,13 @@ bruno_status filter_typed(Ctx *c, const uint64_t *thr) {
   a.thresholding = c->cfg.thresholding;
   a.max_probe = 4096u;
   a.ctr = c->dctr;
+  /* every node is a chain or a branch node: lists sized by the claimed slots */
+  const uint64_t cap = std::max<uint64_t>(1, c->n_slots_claimed);
+  if ((st = ensure(c, c->chain_list, cap * 4)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->branch_list, cap * 4)) != BRUNO_OK) return st;
+  a.chain_list = (uint32_t *)c->chain_list.p;
+  a.branch_list = (uint32_t *)c->branch_list.p;
+  a.list_cap = cap;
   if (c->cfg.keep_filtered) {
     const uint64_t n = std::max<uint64_t>(1, c->n_entries);
     if ((st = ensure(c, c->f_keys, n * 8 * Slot<KT>::KEYW)) != BRUNO_OK) return st;

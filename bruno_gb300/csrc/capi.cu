@@ -86,6 +86,9 @@ bruno_status bruno_ctx_create(const bruno_cfg *cfg, bruno_ctx **out) {
   bruno_status st = cuda_check(c, cudaSetDevice(cfg->device), "cudaSetDevice");
   if (st == BRUNO_OK) st = cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
   c->own_stream = true;
+  /* The k-mer table is read at random, one 32-byte slot per probe: ask L2 to fetch only
+   * the sector that missed (a hint for this process's context only). */
+  if (st == BRUNO_OK) { cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, 32); cudaGetLastError(); }
   if (st == BRUNO_OK) st = cuda_check(c, cudaMalloc(&c->dctr, sizeof(DevCounters)), "counters");
   if (st == BRUNO_OK) st = cuda_check(c, cudaMallocHost(&c->hctr, sizeof(DevCounters)), "pinned counters");
   for (int i = 0; i < 8 && st == BRUNO_OK; ++i) st = cuda_check(c, cudaEventCreate(&c->ev[i]), "event");
@@ -102,7 +105,7 @@ bruno_status bruno_ctx_destroy(bruno_ctx *c) {
   Buf *bufs[] = {&c->rstart, &c->rend, &c->tile_cnt, &c->tile_base, &c->table, &c->k2_keys, &c->k2_edges, &c->k2_counts,
                  &c->f_keys, &c->f_edges, &c->f_counts, &c->blk_cnt, &c->blk_base, &c->ckey, &c->cslot, &c->cedge,
                  &c->cstate, &c->pend, &c->pay, &c->unf0, &c->unf1, &c->removed, &c->r_K, &c->r_rep, &c->r_dist,
-                 &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars};
+                 &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list};
   for (Buf *b : bufs) release(*b);
   for (Buf &b : c->seg_bufs) release(b);
   if (c->dctr) cudaFree(c->dctr);

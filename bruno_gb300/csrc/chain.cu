@@ -1,7 +1,7 @@
 /*
  * chain.cu -- graph nodes -> chain map -> list ranking -> compacted chains.
  *
- *  k_chain_count/assign  dense chain indices for IsChainNode nodes, in slot order
+ *  k_chain_keys          chain index -> k-mer and slot (the filter listed the chain nodes)
  *  k_chain_init          to_simple_biedge (debruijn_chain_node.hpp:83-111): neighbours are
  *                        resolved once to chain indices (+ strand flip), so ranking never
  *                        hashes k-mers again
@@ -106,52 +106,16 @@ __device__ __forceinline__ long long table_find(const uint64_t *table, uint64_t 
 }
 
 /* ================================================================ chain indices */
+/* chain index i -> its slot (listed by the filter, which also stored i in the slot) */
 template <class KT>
-__global__ void __launch_bounds__(TPB) k_chain_count(const uint64_t *table, uint64_t nslots, uint64_t *blk_cnt) {
-  constexpr int SU = Slot<KT>::U64;
-  const uint64_t b0 = (uint64_t)blockIdx.x * CHS;
-  unsigned long long c = 0;
-  for (int j = 0; j < 16; ++j) {
-    const uint64_t i = b0 + (uint64_t)j * TPB + threadIdx.x;
-    if (i < nslots) {
-      const uint64_t *s = table + i * SU;
-      c += !slot_dead<KT>(s) && (slot_flags<KT>(s) & NF_CHAIN);
-    }
-  }
-  __shared__ unsigned long long sc[TPB / 32];
-  c = warp_sum(c);
-  if ((threadIdx.x & 31) == 0) sc[threadIdx.x >> 5] = c;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long t = 0;
-    for (int i = 0; i < TPB / 32; ++i) t += sc[i];
-    blk_cnt[blockIdx.x] = t;
-  }
-}
-
-template <class KT>
-__global__ void __launch_bounds__(TPB) k_chain_assign(uint64_t *table, uint64_t nslots, const uint64_t *blk_base,
-                                                       uint64_t *ckey, uint64_t *cslot) {
+__global__ void __launch_bounds__(TPB) k_chain_keys(const uint64_t *table, const uint32_t *chain_list, uint64_t M,
+                                                     uint64_t *ckey, uint64_t *cslot) {
   constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
-  const uint64_t b0 = (uint64_t)blockIdx.x * CHS;
-  uint64_t run = blk_base[blockIdx.x];
-  for (int j = 0; j < 16; ++j) {
-    const uint64_t i = b0 + (uint64_t)j * TPB + threadIdx.x;
-    bool is = false;
-    uint64_t *s = nullptr;
-    if (i < nslots) {
-      s = table + i * SU;
-      is = !slot_dead<KT>(s) && (slot_flags<KT>(s) & NF_CHAIN);
-    }
-    uint32_t tot;
-    const uint32_t r = block_exscan(is ? 1u : 0u, tot);
-    if (is) {
-      const uint64_t idx = run + r;
-      for (int w = 0; w < KWD; ++w) ckey[idx * KWD + w] = s[w];
-      cslot[idx] = i;
-      s[KWD + 2] = (s[KWD + 2] & 0xFFFFFFFFull) | (idx << 32);
-    }
-    run += tot;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t sl = chain_list[i];
+    const uint64_t *s = table + sl * SU;
+    for (int w = 0; w < KWD; ++w) ckey[i * KWD + w] = s[w];
+    cslot[i] = sl;
   }
 }
 
@@ -203,11 +167,10 @@ __global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, uint6
 /* neighbours of branch nodes get their facing side set to branch_neighbor (0) */
 template <class KT>
 __global__ void __launch_bounds__(TPB) k_termini(const uint64_t *table, uint64_t nslots, int k, ChainState *cs,
-                                                  uint32_t max_probe) {
+                                                  uint32_t max_probe, const uint32_t *branch_list, uint64_t nb) {
   constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t *s = table + i * SU;
-    if (slot_dead<KT>(s) || !(slot_flags<KT>(s) & NF_BRANCH)) continue;
+  for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nb; q += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t *s = table + (uint64_t)branch_list[q] * SU;
     const KT K = KOps<KT>::load(s);
     const uint64_t *pw = s + KWD;
     for (int c = 0; c < 4; ++c) {
@@ -647,26 +610,23 @@ int sms_count() {
 template <class KT>
 bruno_status extract_typed(Ctx *c) {
   bruno_status st;
-  const uint64_t nb = (c->nslots + CHS - 1) / CHS;
-  if ((st = ensure(c, c->blk_cnt, nb * 8)) != BRUNO_OK) return st;
-  if ((st = ensure(c, c->blk_base, nb * 8)) != BRUNO_OK) return st;
-  k_chain_count<KT><<<(unsigned)nb, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, (uint64_t *)c->blk_cnt.p);
-  scan_u64((const uint64_t *)c->blk_cnt.p, (uint64_t *)c->blk_base.p, nb, nullptr, c->stream);
   const uint64_t M = c->n_chain, Mb = std::max<uint64_t>(1, M);
   const int KWD = Slot<KT>::KEYW;
   if ((st = ensure(c, c->ckey, Mb * 8 * KWD)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->cslot, Mb * 8)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->cedge, Mb)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->cstate, Mb * sizeof(ChainState))) != BRUNO_OK) return st;
-  k_chain_assign<KT><<<(unsigned)nb, TPB, 0, c->stream>>>((uint64_t *)c->table.p, c->nslots, (const uint64_t *)c->blk_base.p,
-                                                          (uint64_t *)c->ckey.p, (uint64_t *)c->cslot.p);
   const int sms = sms_count();
+  k_chain_keys<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, (const uint32_t *)c->chain_list.p, M,
+                                                   (uint64_t *)c->ckey.p, (uint64_t *)c->cslot.p);
   k_chain_init<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, c->cfg.k,
                                                    (const uint64_t *)c->ckey.p, (const uint64_t *)c->cslot.p, M,
                                                    (ChainState *)c->cstate.p, (uint8_t *)c->cedge.p, 4096u);
-  k_termini<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, c->cfg.k,
-                                                (ChainState *)c->cstate.p, 4096u);
-  c->launches += 5;
+  if (c->n_branch)
+    k_termini<KT><<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>(sms * 8, (c->n_branch + TPB - 1) / TPB)), TPB, 0,
+                    c->stream>>>((const uint64_t *)c->table.p, c->nslots, c->cfg.k, (ChainState *)c->cstate.p, 4096u,
+                                 (const uint32_t *)c->branch_list.p, c->n_branch);
+  c->launches += 3;
   return cuda_check(c, cudaGetLastError(), "extract_chains");
 }
 

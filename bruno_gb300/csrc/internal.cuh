@@ -70,7 +70,8 @@ struct Ctx {
 
   /* k-mer table */
   Buf table;
-  uint64_t nslots = 0, n_entries = 0;
+  uint64_t nslots = 0, n_entries = 0, n_slots_claimed = 0;
+  Buf chain_list, branch_list;   /* slot indices, filled by the filter */
 
   /* dumps */
   Buf k2_keys, k2_edges, k2_counts;
