@@ -249,7 +249,7 @@ def main():
     # roofline of the dominant kernel, k_count: algorithmic bytes per launch = the read
     # sequence bytes + 16 B of read span per read + one 32 B sector read and one 32 B
     # write-back per (k-mer, biedge) instance
-    k_count_ms = statistics.mean(p["k_count"] for p in kms)
+    k_count_ms = statistics.mean(p["count_insert"] for p in kms)
     alg_bytes = sizes["n_reads"] * w.read_len + 16 * sizes["n_reads"] + 64 * inst_step
     peak, peak_src = measured_peak()
     achieved = alg_bytes / (k_count_ms / 1e3) / 1e9

@@ -40,7 +40,7 @@ class _Cfg(ctypes.Structure):
         ("k", ctypes.c_int32), ("thresholding", ctypes.c_int32), ("thresh", ctypes.c_uint64 * 6),
         ("min_update", ctypes.c_int32), ("device", ctypes.c_int32), ("table_slots", ctypes.c_uint64),
         ("max_load", ctypes.c_double), ("keep_k2", ctypes.c_int32), ("keep_filtered", ctypes.c_int32),
-        ("exact_ranking", ctypes.c_int32),
+        ("exact_ranking", ctypes.c_int32), ("direct_count", ctypes.c_int32),
     ]
 
 
@@ -145,6 +145,7 @@ class GraphConfig:
     keep_k2: bool = False
     keep_filtered: bool = False
     exact_ranking: bool = False
+    direct_count: bool = False
 
     def to_c(self) -> _Cfg:
         c = _Cfg()
@@ -154,6 +155,7 @@ class GraphConfig:
         c.table_slots, c.max_load = self.table_slots, self.max_load
         c.keep_k2, c.keep_filtered = int(self.keep_k2), int(self.keep_filtered)
         c.exact_ranking = int(self.exact_ranking)
+        c.direct_count = int(self.direct_count)
         return c
 
 
@@ -278,7 +280,7 @@ class Graph:
         return d
 
     PHASES = ("parse", "count_k2mers", "filter_insert", "chainmap", "list_rank", "compress",
-              "k_hll", "k_table_init", "k_count")
+              "count_estimate", "count_table_init", "count_insert")
 
     def phase_ms(self) -> dict:
         a = (ctypes.c_double * 9)()

@@ -300,7 +300,7 @@ struct CountArgs {
   uint64_t nreads;
   int k;
   uint64_t *table;
-  uint64_t nslots;
+  TableGeom g;
   uint32_t max_probe;
   DevCounters *ctr;
 };
@@ -404,13 +404,14 @@ __device__ __forceinline__ bool key_cont(KW2 k) { return (k.hi & KEY_CONT) != 0;
 /* Counts one canonical (k-mer, biedge code) occurrence whose first probe slot `i` was
  * already read into raw[].  Returns false if the probe limit was reached. */
 template <class KT>
-__device__ __forceinline__ bool table_count(uint64_t *table, uint64_t nslots, uint32_t max_probe, KT x, unsigned code,
-                                            uint64_t i, uint64_t *raw, unsigned long long &slot_claims,
-                                            unsigned long long &entry_claims) {
+__device__ __forceinline__ bool table_count(uint64_t *table, const TableGeom &g, uint32_t max_probe, KT x,
+                                            unsigned code, uint64_t home, uint64_t *raw,
+                                            unsigned long long &slot_claims, unsigned long long &entry_claims) {
   constexpr int SU = Slot<KT>::U64, NE = Slot<KT>::ENTRIES, KWD = Slot<KT>::KEYW;
   bool seen_primary = false;
-  for (uint32_t probe = 0; probe < max_probe; ++probe) {
-    uint64_t *slot = table + i * SU;
+  Probe pr(g, home);
+  for (uint32_t probe = 0; probe < max_probe; ++probe, pr.next()) {
+    uint64_t *slot = table + pr.i * SU;
     if (probe) ld_slot<SU>(slot, raw);
     KT key = KOps<KT>::load(raw);
     uint32_t seen[NE];
@@ -425,7 +426,6 @@ __device__ __forceinline__ bool table_count(uint64_t *table, uint64_t nslots, ui
       seen_primary = true;
       if (count_in_entries<NE>((uint32_t *)(slot + KWD), seen, code, entry_claims)) return true;
     }
-    if (++i == nslots) i = 0;
   }
   return false;
 }
@@ -486,21 +486,21 @@ __global__ void __launch_bounds__(TPB, 4) k_count(CountArgs a) {
         uint64_t ia = 0, ic = 0, ra[SU], rc[SU];
         if (pa < pend) {
           kmer_at<KT>(words, pa, p0, rv.L, k, xa, ca);
-          ia = __umul64hi(KOps<KT>::hash(xa), a.nslots);
+          ia = table_home(a.g, xa);
           ld_slot<SU>(a.table + ia * SU, ra);
         }
         if (pc < pend) {
           kmer_at<KT>(words, pc, p0, rv.L, k, xc, cc);
-          ic = __umul64hi(KOps<KT>::hash(xc), a.nslots);
+          ic = table_home(a.g, xc);
           ld_slot<SU>(a.table + ic * SU, rc);
         }
         if (pa < pend) {
           ++inst;
-          if (!table_count<KT>(a.table, a.nslots, a.max_probe, xa, ca, ia, ra, slots, entries)) full = true;
+          if (!table_count<KT>(a.table, a.g, a.max_probe, xa, ca, ia, ra, slots, entries)) full = true;
         }
         if (pc < pend) {
           ++inst;
-          if (!table_count<KT>(a.table, a.nslots, a.max_probe, xc, cc, ic, rc, slots, entries)) full = true;
+          if (!table_count<KT>(a.table, a.g, a.max_probe, xc, cc, ic, rc, slots, entries)) full = true;
         }
       }
     }
@@ -516,6 +516,217 @@ __global__ void __launch_bounds__(TPB, 4) k_count(CountArgs a) {
     atomicAdd(&a.ctr->n_slots_claimed, s_slots); atomicAdd(&a.ctr->n_entries, s_entries);
     if (s_full) atomicOr(&a.ctr->err, (unsigned long long)DERR_TABLE_FULL);
   }
+}
+
+/* ============================================================ partitioned counting
+ * k <= 31.  Phase A (k_extract) turns every read into canonical (k-mer, biedge) instances
+ * and writes each as one 8-byte record [low 54 bits of bj_fwd(k-mer) | biedge code:5]
+ * into one of 256 hash buckets (the bucket is the top 8 bits of the mix); the block sorts
+ * its records by bucket in shared memory first, so every bucket grows by contiguous runs.
+ * The distinct-count estimate rides along.  Phase B (k_insert) then fills the table one
+ * partition at a time -- a partition is one or more buckets and a contiguous slot region
+ * small enough to stay in L2 -- so the random slot traffic of counting stays on chip. */
+constexpr int NBUCKET_BITS = 8, NBUCKET = 1 << NBUCKET_BITS;
+constexpr int LOW_BITS = 62 - NBUCKET_BITS;          /* 54 */
+constexpr int REC_CAP = 2048;                         /* records per block flush */
+constexpr int EMIT = REC_CAP / (TPB / 32);            /* positions per warp per round */
+
+__global__ void __launch_bounds__(TPB) k_kmer_upper(const uint64_t *rstart, const uint64_t *rend, uint64_t nreads,
+                                                     int k, DevCounters *ctr) {
+  unsigned long long n = 0;
+  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nreads; r += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t L = rend[r] - rstart[r];
+    if (L >= (uint64_t)k + 2) n += L - k + 1;
+  }
+  n = warp_sum(n);
+  if ((threadIdx.x & 31) == 0 && n) atomicAdd(&ctr->n_upper, n);
+}
+
+struct ExtractSmem {
+  uint64_t words[TPB / 32][CHUNK_WORDS];
+  uint64_t rec[REC_CAP], sorted[REC_CAP];
+  unsigned int hll[HLL_M];
+  uint32_t pcnt[NBUCKET], pcur[NBUCKET], pstart[NBUCKET];
+  unsigned long long gbase[NBUCKET];
+  uint8_t part[REC_CAP], spart[REC_CAP];
+  uint32_t n;
+  int overflow;
+};
+
+__global__ void __launch_bounds__(TPB) k_extract(const uint64_t *rstart, const uint64_t *rend, uint64_t nreads, int k,
+                                                  uint64_t *records, uint64_t cap, unsigned long long *bucket_cnt,
+                                                  uint8_t *hll_partial, DevCounters *ctr) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  ExtractSmem &S = *reinterpret_cast<ExtractSmem *>(smem_raw);
+  for (int i = threadIdx.x; i < HLL_M; i += TPB) S.hll[i] = 0;
+  for (int i = threadIdx.x; i < NBUCKET; i += TPB) S.pcnt[i] = 0;
+  if (threadIdx.x == 0) { S.n = 0; S.overflow = 0; }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint64_t *words = S.words[warp];
+  const uint64_t stride = (uint64_t)gridDim.x * (TPB / 32);
+  /* per-warp cursor over its reads */
+  uint64_t r = (uint64_t)blockIdx.x * (TPB / 32) + warp;
+  ReadView rv{nullptr, 0};
+  uint32_t npos = 0, pc = 0, p0 = 0, pend = 0;
+  bool staged = false, one_chunk = true, fresh = false, active = r < nreads;
+  unsigned long long inst = 0, used = 0;
+  if (active) {
+    rv = ReadView{(const unsigned char *)rstart[r], (uint32_t)(rend[r] - rstart[r])};
+    npos = rv.L >= (uint32_t)k + 2 ? rv.L - k + 1 : 0;
+    fresh = true;
+  }
+  for (;;) {
+    uint32_t budget = EMIT;
+    while (active && budget > 0) {
+      if (fresh) {   /* a new read: long reads get the N filter up front */
+        fresh = false; pc = 0; staged = false;
+        one_chunk = npos <= CHUNK_POS;
+        if (npos && !one_chunk) {
+          bool bad = false;
+          for (uint32_t i = lane; i < rv.L; i += 32) bad |= base_code(rv.s[i]) < 0;
+          if (__any_sync(~0u, bad)) npos = 0;
+          else used += (lane == 0);
+        }
+      }
+      if (pc >= npos) {   /* next read */
+        r += stride;
+        if (r >= nreads) { active = false; break; }
+        rv = ReadView{(const unsigned char *)rstart[r], (uint32_t)(rend[r] - rstart[r])};
+        npos = rv.L >= (uint32_t)k + 2 ? rv.L - k + 1 : 0;
+        fresh = true;
+        continue;
+      }
+      if (!staged || pc >= pend) {
+        p0 = (pc / CHUNK_POS) * CHUNK_POS;
+        pend = min(npos, p0 + CHUNK_POS);
+        __syncwarp();
+        const bool bad = stage_chunk(rv, p0, pend, k, words, lane);
+        staged = true;
+        if (one_chunk) {
+          if (bad) { npos = 0; continue; }   /* reads containing N are dropped */
+          used += (lane == 0);
+        }
+      }
+      const uint32_t e = min(pend, pc + budget);
+      for (uint32_t pb = pc; pb < e; pb += 32) {
+        const uint32_t p = pb + lane;
+        const bool valid = p < e;
+        uint64_t rec = 0;
+        unsigned bucket = 0;
+        if (valid) {
+          KW1 x; unsigned code;
+          kmer_at<KW1>(words, p, p0, rv.L, k, x, code);
+          const uint64_t h = bj_fwd(x.v);
+          bucket = (unsigned)(h >> LOW_BITS);
+          rec = ((h & ((1ull << LOW_BITS) - 1)) << 5) | code;
+          const unsigned idx = (unsigned)(h >> (62 - HLL_P));
+          const unsigned rho = (unsigned)__clzll((h << (2 + HLL_P)) | (1ull << (1 + HLL_P))) + 1u;
+          if (rho > S.hll[idx]) atomicMax(&S.hll[idx], rho);
+          ++inst;
+        }
+        const unsigned m = __ballot_sync(~0u, valid);
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&S.n, (uint32_t)__popc(m));
+        base = __shfl_sync(~0u, base, 0);
+        if (valid) {
+          const uint32_t o = base + __popc(m & ((1u << lane) - 1));
+          S.rec[o] = rec;
+          S.part[o] = (uint8_t)bucket;
+        }
+      }
+      budget -= e - pc;
+      pc = e;
+    }
+    __syncthreads();
+    /* flush: group the block's records by bucket and append each group to its bucket */
+    const uint32_t n = S.n;
+    for (uint32_t i = threadIdx.x; i < n; i += TPB) atomicAdd(&S.pcnt[S.part[i]], 1u);
+    __syncthreads();
+    {
+      const uint32_t v = S.pcnt[threadIdx.x];
+      uint32_t tot;
+      const uint32_t st = block_exscan(v, tot);
+      S.pstart[threadIdx.x] = st;
+      S.pcur[threadIdx.x] = st;
+      if (v) {
+        const unsigned long long old = atomicAdd(&bucket_cnt[threadIdx.x], (unsigned long long)v);
+        if (old + v > cap) S.overflow = 1;
+        S.gbase[threadIdx.x] = (unsigned long long)threadIdx.x * cap + old;
+      }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += TPB) {
+      const unsigned b = S.part[i];
+      const uint32_t pos = atomicAdd(&S.pcur[b], 1u);
+      S.sorted[pos] = S.rec[i];
+      S.spart[pos] = (uint8_t)b;
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += TPB) {
+      const unsigned b = S.spart[i];
+      const unsigned long long dst = S.gbase[b] + (i - S.pstart[b]);
+      if (dst < (unsigned long long)(b + 1) * cap) records[dst] = S.sorted[i];
+    }
+    __syncthreads();
+    S.pcnt[threadIdx.x] = 0;
+    if (threadIdx.x == 0) S.n = 0;
+    if (!__syncthreads_or(active)) break;
+  }
+  inst = warp_sum(inst); used = warp_sum(used);
+  if (lane == 0) {
+    if (inst) atomicAdd(&ctr->n_instances, inst);
+    if (used) atomicAdd(&ctr->n_reads_used, used);
+  }
+  if (threadIdx.x == 0 && S.overflow) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
+  uint8_t *dst = hll_partial + (uint64_t)blockIdx.x * HLL_M;
+  for (int i = threadIdx.x; i < HLL_M; i += TPB) dst[i] = (uint8_t)S.hll[i];
+}
+
+/* one table partition: keys EMPTY, entries 0 (stays in L2 for the inserts that follow) */
+template <class KT>
+__global__ void k_part_init(uint64_t *table, uint64_t first_slot, uint64_t nslots) {
+  constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
+  uint64_t *t = table + first_slot * SU;
+  const uint64_t nw = nslots * SU;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += (uint64_t)gridDim.x * blockDim.x)
+    t[i] = ((int)(i % SU) < KWD) ? KEY_EMPTY : 0ull;
+}
+
+/* Phase B: the records of the buckets of partition q (blockIdx.y picks the bucket) */
+__global__ void __launch_bounds__(TPB) k_insert(const uint64_t *records, const unsigned long long *bucket_cnt,
+                                                 uint64_t cap, int bucket0, uint64_t *table, TableGeom g,
+                                                 uint32_t max_probe, DevCounters *ctr) {
+  constexpr int SU = Slot<KW1>::U64;
+  const int b = bucket0 + (int)blockIdx.y;
+  const uint64_t n = min((unsigned long long)cap, bucket_cnt[b]);
+  const uint64_t *rb = records + (uint64_t)b * cap;
+  unsigned long long slots = 0, entries = 0;
+  bool full = false;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += 2 * stride) {
+    /* two records in flight per thread */
+    const uint64_t j = i + stride;
+    const uint64_t r0 = __ldcs(rb + i), r1 = j < n ? __ldcs(rb + j) : 0;
+    const uint64_t h0 = ((uint64_t)b << LOW_BITS) | (r0 >> 5), h1 = ((uint64_t)b << LOW_BITS) | (r1 >> 5);
+    const uint64_t q0 = g.pbits ? (h0 >> (62 - g.pbits)) : 0, q1 = g.pbits ? (h1 >> (62 - g.pbits)) : 0;
+    const uint64_t home0 = q0 * g.region + __umul64hi(h0 << (2 + g.pbits), g.region);
+    const uint64_t home1 = q1 * g.region + __umul64hi(h1 << (2 + g.pbits), g.region);
+    uint64_t ra[SU], rc[SU];
+    ld_slot<SU>(table + home0 * SU, ra);
+    if (j < n) ld_slot<SU>(table + home1 * SU, rc);
+    if (!table_count<KW1>(table, g, max_probe, KW1{bj_inv(h0)}, (unsigned)(r0 & 31), home0, ra, slots, entries))
+      full = true;
+    if (j < n &&
+        !table_count<KW1>(table, g, max_probe, KW1{bj_inv(h1)}, (unsigned)(r1 & 31), home1, rc, slots, entries))
+      full = true;
+  }
+  slots = warp_sum(slots); entries = warp_sum(entries);
+  if ((threadIdx.x & 31) == 0) {
+    if (slots) atomicAdd(&ctr->n_slots_claimed, slots);
+    if (entries) atomicAdd(&ctr->n_entries, entries);
+  }
+  if (full) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
 }
 
 /* table initialisation: every key word EMPTY, every entry 0; written as one flat word
@@ -553,24 +764,12 @@ __global__ void __launch_bounds__(TPB) k_dump_k2(const uint64_t *table, uint64_t
 
 /* ============================================================ filter + insert */
 
-/* warp-aggregated append among the lanes that reach this call together */
-__device__ __forceinline__ unsigned long long append_active(bool want, unsigned long long *counter) {
-  const unsigned act = __activemask();
-  const unsigned m = __ballot_sync(act, want);
-  const int lane = threadIdx.x & 31;
-  if (!m) return 0;
-  const int leader = __ffs(m) - 1;
-  unsigned long long base = 0;
-  if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(m));
-  base = __shfl_sync(act, base, leader);
-  return base + __popc(m & ((1u << lane) - 1));
-}
-
 struct FilterArgs {
   uint32_t *chain_list, *branch_list;   /* slot indices of chain / branch nodes */
   uint64_t list_cap;
   uint64_t *table;
   uint64_t nslots;
+  TableGeom g;
   int k;
   uint64_t t[6];
   int thresholding;
@@ -580,8 +779,9 @@ struct FilterArgs {
 };
 
 struct FilterTally {
-  unsigned long long nodes = 0, branch = 0, chain = 0;   /* branch/chain: statistics only */
+  unsigned long long nodes = 0, branch = 0, chain = 0;
   unsigned hist[16];
+  int kind = 0;          /* the last k-mer: 0 not a node, 1 chain node, 2 branch node */
 };
 
 /* local_insert_by_freqencies (debruijn_graph_map.hpp:1258-1623) for one k-mer block: the
@@ -680,69 +880,91 @@ __device__ __forceinline__ void filter_kmer(uint64_t *s, uint64_t slot_index, KT
   const bool is_branch = din >= 2 || dout >= 2 || kpal || k1pal;
   const uint32_t flags = is_branch ? NF_BRANCH : NF_CHAIN;
   ++t.nodes; t.branch += is_branch; t.chain += !is_branch;
-  /* chain nodes get their chain index right here (the order of appends is arbitrary and
-   * never observable: every output is keyed by k-mer) */
-  const unsigned long long oc = append_active(!is_branch, &a.ctr->n_chain);
-  const unsigned long long ob = append_active(is_branch, &a.ctr->n_branch);
-  uint32_t aux = 0xFFFFFFFFu;
-  if (!is_branch && oc < a.list_cap) { a.chain_list[oc] = (uint32_t)slot_index; aux = (uint32_t)oc; }
-  if (is_branch && ob < a.list_cap) a.branch_list[ob] = (uint32_t)slot_index;
+  /* chain nodes get their chain index (slot aux) when the block flushes its node list */
+  t.kind = is_branch ? 2 : 1;
   uint64_t *pw = s + KWD;
   pw[0] = (uint64_t)c16[0] | ((uint64_t)c16[1] << 16) | ((uint64_t)c16[2] << 32) | ((uint64_t)c16[3] << 48);
   pw[1] = (uint64_t)c16[4] | ((uint64_t)c16[5] << 16) | ((uint64_t)c16[6] << 32) | ((uint64_t)c16[7] << 48);
-  pw[2] = (uint64_t)c16[8] | ((uint64_t)flags << 16) | ((uint64_t)aux << 32);
+  pw[2] = (uint64_t)c16[8] | ((uint64_t)flags << 16) | (0xFFFFFFFFull << 32);
 }
 
 template <class KT>
 __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
   constexpr int SU = Slot<KT>::U64, NE = Slot<KT>::ENTRIES, KWD = Slot<KT>::KEYW;
-  __shared__ unsigned long long s_hist[16], s_nodes, s_branch, s_chain;
+  __shared__ unsigned long long s_hist[16], s_nodes;
+  /* block-local node lists, flushed to the global chain / branch lists once per stripe */
+  __shared__ uint32_t s_chain[TPB], s_branch[TPB];
+  __shared__ uint32_t s_nc, s_nb;
+  __shared__ unsigned long long s_base_c, s_base_b;
   if (threadIdx.x < 16) s_hist[threadIdx.x] = 0;
-  if (threadIdx.x == 0) s_nodes = s_branch = s_chain = 0;
-  __syncthreads();
+  if (threadIdx.x == 0) s_nodes = 0;
   FilterTally t;
   #pragma unroll
   for (int f = 0; f < 16; ++f) t.hist[f] = 0;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.nslots; i += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t *s = a.table + i * SU;
-    uint64_t raw[SU];
-    ld_slot<SU>(s, raw);
-    const KT key = KOps<KT>::load(raw);
-    if (key_dead(key) || key_cont(key)) continue;
-    uint32_t w[NE];
-    int ne = 0;
-    #pragma unroll
-    for (int q = 0; q < NE; ++q) {
-      w[q] = (uint32_t)(raw[KWD + q / 2] >> (32 * (q & 1)));
-      ne += w[q] != 0;
-    }
-    if (ne < NE) {       /* the common case: every entry of the k-mer is in this slot */
-      filter_kmer<KT, NE>(s, i, key, w, ne, a, t);
-      continue;
-    }
-    /* more entries in continuation slots further along the probe run */
-    uint32_t all[25];
-    #pragma unroll
-    for (int q = 0; q < NE; ++q) all[q] = w[q];
-    uint64_t j = i;
-    for (uint32_t probe = 1; probe < a.max_probe; ++probe) {
-      if (++j == a.nslots) j = 0;
-      uint64_t *s2 = a.table + j * SU;
-      const KT k2 = KOps<KT>::load(s2);
-      if (key_is_empty(k2)) break;
-      if (!key_matches(k2, key, true)) continue;
-      const uint32_t *e2 = (const uint32_t *)(s2 + KWD);
-      for (int q = 0; q < NE && ne < 25; ++q) {
-        if (e2[q] == 0) break;
-        all[ne++] = e2[q];
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < a.nslots; base += (uint64_t)gridDim.x * blockDim.x) {
+    if (threadIdx.x == 0) { s_nc = 0; s_nb = 0; }
+    __syncthreads();
+    const uint64_t i = base + threadIdx.x;
+    t.kind = 0;
+    if (i < a.nslots) {
+      uint64_t *s = a.table + i * SU;
+      uint64_t raw[SU];
+      ld_slot<SU>(s, raw);
+      const KT key = KOps<KT>::load(raw);
+      if (!key_dead(key) && !key_cont(key)) {
+        uint32_t w[NE];
+        int ne = 0;
+        #pragma unroll
+        for (int q = 0; q < NE; ++q) {
+          w[q] = (uint32_t)(raw[KWD + q / 2] >> (32 * (q & 1)));
+          ne += w[q] != 0;
+        }
+        if (ne < NE) {   /* the common case: every entry of the k-mer is in this slot */
+          filter_kmer<KT, NE>(s, i, key, w, ne, a, t);
+        } else {         /* more entries in continuation slots further along the probe run */
+          uint32_t all[25];
+          #pragma unroll
+          for (int q = 0; q < NE; ++q) all[q] = w[q];
+          Probe pr(a.g, i);
+          for (uint32_t probe = 1; probe < a.max_probe; ++probe) {
+            pr.next();
+            uint64_t *s2 = a.table + pr.i * SU;
+            const KT k2 = KOps<KT>::load(s2);
+            if (key_is_empty(k2)) break;
+            if (!key_matches(k2, key, true)) continue;
+            const uint32_t *e2 = (const uint32_t *)(s2 + KWD);
+            for (int q = 0; q < NE && ne < 25; ++q) {
+              if (e2[q] == 0) break;
+              all[ne++] = e2[q];
+            }
+            /* the continuation slot is folded into this node */
+            if (KWD == 1) s2[0] = KEY_TOMB; else { s2[0] = KEY_TOMB; s2[1] = KEY_TOMB; }
+          }
+          filter_kmer<KT, 25>(s, i, key, all, ne, a, t);
+        }
       }
-      /* the continuation slot is folded into this node */
-      if (KWD == 1) s2[0] = KEY_TOMB; else { s2[0] = KEY_TOMB; s2[1] = KEY_TOMB; }
     }
-    filter_kmer<KT, 25>(s, i, key, all, ne, a, t);
+    if (t.kind == 1) s_chain[atomicAdd(&s_nc, 1u)] = (uint32_t)i;
+    if (t.kind == 2) s_branch[atomicAdd(&s_nb, 1u)] = (uint32_t)i;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      s_base_c = s_nc ? atomicAdd(&a.ctr->n_chain, (unsigned long long)s_nc) : 0;
+      s_base_b = s_nb ? atomicAdd(&a.ctr->n_branch, (unsigned long long)s_nb) : 0;
+    }
+    __syncthreads();
+    if (threadIdx.x < s_nc) {
+      const unsigned long long o = s_base_c + threadIdx.x;
+      const uint32_t sl = s_chain[threadIdx.x];
+      if (o < a.list_cap) {
+        a.chain_list[o] = sl;
+        uint64_t *pw = a.table + (uint64_t)sl * SU + KWD;
+        pw[2] = (pw[2] & 0xFFFFFFFFull) | (o << 32);   /* chain index */
+      }
+    }
+    if (threadIdx.x < s_nb && s_base_b + threadIdx.x < a.list_cap) a.branch_list[s_base_b + threadIdx.x] = s_branch[threadIdx.x];
   }
-  unsigned long long nodes = warp_sum(t.nodes), branch = warp_sum(t.branch), chain = warp_sum(t.chain);
-  if ((threadIdx.x & 31) == 0) { atomicAdd(&s_nodes, nodes); atomicAdd(&s_branch, branch); atomicAdd(&s_chain, chain); }
+  unsigned long long nodes = warp_sum(t.nodes);
+  if ((threadIdx.x & 31) == 0) atomicAdd(&s_nodes, nodes);
   #pragma unroll
   for (int f = 0; f < 16; ++f) {
     unsigned long long h = warp_sum(t.hist[f]);
@@ -868,12 +1090,28 @@ bruno_status run_index_reads(Ctx *c) {
 
 /* ------------------------------------------------------------ counting */
 namespace {
+double hll_estimate(const unsigned int *reg) {
+  double sum = 0; int zeros = 0;
+  for (int i = 0; i < HLL_M; ++i) { sum += std::ldexp(1.0, -(int)reg[i]); zeros += reg[i] == 0; }
+  const double m = HLL_M, alpha = 0.7213 / (1.0 + 1.079 / m);
+  double est = alpha * m * m / sum;
+  if (est <= 2.5 * m && zeros > 0) est = m * std::log(m / zeros);
+  return est;
+}
+
+uint64_t slots_for(const Ctx *c, double distinct) {
+  const double load = c->cfg.max_load > 0 ? c->cfg.max_load : 0.5;
+  /* a k-mer with more than one slot's worth of biedges takes continuation slots */
+  return (uint64_t)(distinct * 1.04 / load) + 1024;
+}
+
+/* the direct count: every instance probes the whole table (k > 31, or a degenerate input
+ * whose instances crowd one hash bucket) */
 template <class KT>
-bruno_status count_typed(Ctx *c) {
+bruno_status count_direct(Ctx *c) {
   bruno_status st;
   const int sms = num_sms();
   const uint64_t nreads = c->n_reads;
-  /* distinct-count estimate -> slots */
   uint64_t slots = c->cfg.table_slots;
   cudaEventRecord(c->kev[0], c->stream);
   if (slots == 0) {
@@ -884,36 +1122,30 @@ bruno_status count_typed(Ctx *c) {
     k_hll_merge<<<HLL_M / 256, 256, 0, c->stream>>>((const uint8_t *)c->blk_cnt.p, hb, c->dctr);
     c->launches += 2;
     if ((st = sync_counters(c, true)) != BRUNO_OK) return st;
-    double sum = 0; int zeros = 0;
-    for (int i = 0; i < HLL_M; ++i) { sum += std::ldexp(1.0, -(int)c->hctr->hll[i]); zeros += c->hctr->hll[i] == 0; }
-    const double m = HLL_M, alpha = 0.7213 / (1.0 + 1.079 / m);
-    double est = alpha * m * m / sum;
-    if (est <= 2.5 * m && zeros > 0) est = m * std::log(m / zeros);
-    const double load = c->cfg.max_load > 0 ? c->cfg.max_load : 0.5;
-    /* a k-mer with more than one slot's worth of biedges takes continuation slots */
-    slots = (uint64_t)(est * 1.04 / load) + 1024;
+    slots = slots_for(c, hll_estimate(c->hctr->hll));
   }
   for (int attempt = 0; attempt < 4; ++attempt) {
     const size_t bytes = slots * Slot<KT>::U64 * 8;
     if ((st = ensure(c, c->table, bytes)) != BRUNO_OK) return st;
     c->nslots = slots;
+    c->geom = TableGeom{slots, slots, 0};
     cudaEventRecord(c->kev[1], c->stream);
     k_table_init<KT><<<sms * 8, TPB, 0, c->stream>>>((uint64_t *)c->table.p, slots);
     cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
     cudaEventRecord(c->kev[2], c->stream);
     CountArgs a{(const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k, (uint64_t *)c->table.p,
-                slots, 4096u, c->dctr};
+                c->geom, 4096u, c->dctr};
     const int grid = std::max(1, std::min<int>(sms * 8, (int)((nreads + 7) / 8)));
     k_count<KT><<<grid, TPB, 0, c->stream>>>(a);
     cudaEventRecord(c->kev[3], c->stream);
     c->launches += 2;
     if ((st = sync_counters(c)) != BRUNO_OK) return st;
-    float ms[3] = {0, 0, 0};
-    cudaEventElapsedTime(&ms[0], c->kev[0], c->kev[1]);
-    cudaEventElapsedTime(&ms[1], c->kev[1], c->kev[2]);
-    cudaEventElapsedTime(&ms[2], c->kev[2], c->kev[3]);
-    for (int q = 0; q < 3; ++q) c->phase_ms[6 + q] = ms[q];
     if (!(c->hctr->err & DERR_TABLE_FULL)) {
+      float ms[3] = {0, 0, 0};
+      cudaEventElapsedTime(&ms[0], c->kev[0], c->kev[1]);
+      cudaEventElapsedTime(&ms[1], c->kev[1], c->kev[2]);
+      cudaEventElapsedTime(&ms[2], c->kev[2], c->kev[3]);
+      for (int q = 0; q < 3; ++q) c->phase_ms[6 + q] = ms[q];
       c->n_instances = c->hctr->n_instances;
       c->n_reads_used = c->hctr->n_reads_used;
       c->n_entries = c->hctr->n_entries;
@@ -923,6 +1155,92 @@ bruno_status count_typed(Ctx *c) {
     slots *= 2;  /* the estimate was too low: grow and count again */
   }
   return set_err(c, BRUNO_ERR_TABLE_FULL, "k-mer table full after regrowth");
+}
+
+/* the partitioned count (k <= 31); returns with used = false if a bucket overflowed */
+bruno_status count_partitioned(Ctx *c, bool &used) {
+  bruno_status st;
+  used = false;
+  const int sms = num_sms();
+  const uint64_t nreads = c->n_reads;
+  cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
+  cudaEventRecord(c->kev[0], c->stream);
+  k_kmer_upper<<<sms * 4, TPB, 0, c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads,
+                                               c->cfg.k, c->dctr);
+  c->launches += 1;
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  const uint64_t upper = c->hctr->n_upper;
+  const uint64_t cap = upper / NBUCKET + upper / (NBUCKET * 12) + 4096;  /* hashing spreads buckets within ~0.1% */
+  if ((st = ensure(c, c->records, (size_t)NBUCKET * cap * 8)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->bucket_cnt, NBUCKET * 8)) != BRUNO_OK) return st;
+  cudaMemsetAsync(c->bucket_cnt.p, 0, NBUCKET * 8, c->stream);
+  const int eb = std::max(1, std::min<int>(sms * 2, (int)((nreads + 7) / 8)));
+  if ((st = ensure(c, c->blk_cnt, (size_t)eb * HLL_M)) != BRUNO_OK) return st;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_extract, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
+    attr = true;
+  }
+  k_extract<<<eb, TPB, sizeof(ExtractSmem), c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p,
+                                                          nreads, c->cfg.k, (uint64_t *)c->records.p, cap,
+                                                          (unsigned long long *)c->bucket_cnt.p, (uint8_t *)c->blk_cnt.p,
+                                                          c->dctr);
+  k_hll_merge<<<HLL_M / 256, 256, 0, c->stream>>>((const uint8_t *)c->blk_cnt.p, eb, c->dctr);
+  c->launches += 2;
+  cudaEventRecord(c->kev[1], c->stream);
+  if ((st = sync_counters(c, true)) != BRUNO_OK) return st;
+  if (c->hctr->err & DERR_TABLE_FULL) return BRUNO_OK;   /* a bucket overflowed: count directly */
+  c->n_instances = c->hctr->n_instances;
+  c->n_reads_used = c->hctr->n_reads_used;
+  uint64_t slots = c->cfg.table_slots ? c->cfg.table_slots : slots_for(c, hll_estimate(c->hctr->hll));
+  /* partitions of at most ~48 MB so that one stays in L2 while it fills */
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    const double bytes = (double)slots * 32.0;
+    int pt = 0;
+    while (pt < NBUCKET_BITS && bytes / (double)(1ull << pt) > 48.0 * 1024 * 1024) ++pt;
+    const uint64_t region = std::max<uint64_t>(64, (slots + (1ull << pt) - 1) >> pt);
+    c->geom = TableGeom{region << pt, region, pt};
+    c->nslots = c->geom.nslots;
+    if ((st = ensure(c, c->table, c->nslots * 32)) != BRUNO_OK) return st;
+    cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
+    cudaMemsetAsync(&c->dctr->n_slots_claimed, 0, 16, c->stream);
+    cudaEventRecord(c->kev[2], c->stream);
+    const int G = 1 << (NBUCKET_BITS - pt);
+    const int gx = std::max(1, (sms * 8 + G - 1) / G);
+    for (int q = 0; q < (1 << pt); ++q) {
+      k_part_init<KW1><<<sms * 2, TPB, 0, c->stream>>>((uint64_t *)c->table.p, (uint64_t)q * region, region);
+      k_insert<<<dim3(gx, G), TPB, 0, c->stream>>>((const uint64_t *)c->records.p,
+                                                    (const unsigned long long *)c->bucket_cnt.p, cap, q * G,
+                                                    (uint64_t *)c->table.p, c->geom, 4096u, c->dctr);
+    }
+    c->launches += 2 << pt;
+    cudaEventRecord(c->kev[3], c->stream);
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    if (!(c->hctr->err & DERR_TABLE_FULL)) {
+      float ms[3] = {0, 0, 0};
+      cudaEventElapsedTime(&ms[0], c->kev[0], c->kev[1]);   /* phase A (extract + estimate) */
+      cudaEventElapsedTime(&ms[2], c->kev[2], c->kev[3]);   /* phase B (init + insert) */
+      c->phase_ms[6] = ms[0];
+      c->phase_ms[7] = 0;
+      c->phase_ms[8] = ms[2];
+      c->n_entries = c->hctr->n_entries;
+      c->n_slots_claimed = c->hctr->n_slots_claimed;
+      used = true;
+      return BRUNO_OK;
+    }
+    slots *= 2;
+  }
+  return set_err(c, BRUNO_ERR_TABLE_FULL, "k-mer table full after regrowth");
+}
+
+template <class KT>
+bruno_status count_typed(Ctx *c) {
+  if (sizeof(KT) == 8 && !c->force_direct_count) {
+    bool used = false;
+    bruno_status st = count_partitioned(c, used);
+    if (st != BRUNO_OK || used) return st;
+  }
+  return count_direct<KT>(c);
 }
 
 template <class KT>
@@ -948,6 +1266,7 @@ bruno_status filter_typed(Ctx *c, const uint64_t *thr) {
   FilterArgs a{};
   a.table = (uint64_t *)c->table.p;
   a.nslots = c->nslots;
+  a.g = c->geom;
   a.k = c->cfg.k;
   for (int i = 0; i < 6; ++i) a.t[i] = thr[i];
   a.thresholding = c->cfg.thresholding;

@@ -83,6 +83,7 @@ bruno_status bruno_ctx_create(const bruno_cfg *cfg, bruno_ctx **out) {
   c->cfg = *cfg;
   c->W = cfg->k <= 31 ? 1 : 2;
   c->exact_ranking = cfg->exact_ranking != 0;
+  c->force_direct_count = cfg->direct_count != 0;
   bruno_status st = cuda_check(c, cudaSetDevice(cfg->device), "cudaSetDevice");
   if (st == BRUNO_OK) st = cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
   c->own_stream = true;

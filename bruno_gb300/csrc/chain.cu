@@ -91,16 +91,15 @@ __device__ __forceinline__ uint32_t slot_aux(const uint64_t *s) {
 
 /* slot index of a live node with canonical key x, -1 if absent */
 template <class KT>
-__device__ __forceinline__ long long table_find(const uint64_t *table, uint64_t nslots, uint32_t max_probe, KT x) {
+__device__ __forceinline__ long long table_find(const uint64_t *table, const TableGeom &g, uint32_t max_probe, KT x) {
   constexpr int SU = Slot<KT>::U64;
-  uint64_t i = __umul64hi(KOps<KT>::hash(x), nslots);
-  for (uint32_t p = 0; p < max_probe; ++p) {
-    const uint64_t *s = table + i * SU;
+  Probe pr(g, table_home(g, x));
+  for (uint32_t p = 0; p < max_probe; ++p, pr.next()) {
+    const uint64_t *s = table + pr.i * SU;
     KT key = KOps<KT>::load(s);
-    if (KOps<KT>::eq(key, x)) return (long long)i;
+    if (KOps<KT>::eq(key, x)) return (long long)pr.i;
     if (Slot<KT>::KEYW == 1 ? (((uint64_t *)&key)[0] == KEY_EMPTY) : (((uint64_t *)&key)[1] == KEY_EMPTY && ((uint64_t *)&key)[0] == KEY_EMPTY))
       return -1;
-    if (++i == nslots) i = 0;
   }
   return -1;
 }
@@ -121,7 +120,7 @@ __global__ void __launch_bounds__(TPB) k_chain_keys(const uint64_t *table, const
 
 /* ================================================================ chain init */
 template <class KT>
-__global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, uint64_t nslots, int k, const uint64_t *ckey,
+__global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, TableGeom g, int k, const uint64_t *ckey,
                                                      const uint64_t *cslot, uint64_t M, ChainState *cs, uint8_t *cedge,
                                                      uint32_t max_probe) {
   constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
@@ -138,7 +137,7 @@ __global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, uint6
     if (inc >= 0) {  /* in neighbour: nextReverseFromChar(c) */
       KT n = KOps<KT>::prepend((unsigned)inc, K, k), y = KOps<KT>::rc(n, k);
       const bool flip = !KOps<KT>::lt(n, y);
-      const long long j = table_find<KT>(table, nslots, max_probe, flip ? y : n);
+      const long long j = table_find<KT>(table, g, max_probe, flip ? y : n);
       if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN))
         st.inP = (uint64_t)slot_aux<KT>(table + j * SU) | (flip ? PF_FLIP : 0);
       else
@@ -150,7 +149,7 @@ __global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, uint6
     if (outc >= 0) {  /* out neighbour: nextFromChar(c) */
       KT n = KOps<KT>::append(K, (unsigned)outc, k), y = KOps<KT>::rc(n, k);
       const bool flip = !KOps<KT>::lt(n, y);
-      const long long j = table_find<KT>(table, nslots, max_probe, flip ? y : n);
+      const long long j = table_find<KT>(table, g, max_probe, flip ? y : n);
       if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN))
         st.outP = (uint64_t)slot_aux<KT>(table + j * SU) | (flip ? PF_FLIP : 0);
       else
@@ -166,7 +165,7 @@ __global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, uint6
 
 /* neighbours of branch nodes get their facing side set to branch_neighbor (0) */
 template <class KT>
-__global__ void __launch_bounds__(TPB) k_termini(const uint64_t *table, uint64_t nslots, int k, ChainState *cs,
+__global__ void __launch_bounds__(TPB) k_termini(const uint64_t *table, TableGeom g, int k, ChainState *cs,
                                                   uint32_t max_probe, const uint32_t *branch_list, uint64_t nb) {
   constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
   for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nb; q += (uint64_t)gridDim.x * blockDim.x) {
@@ -177,7 +176,7 @@ __global__ void __launch_bounds__(TPB) k_termini(const uint64_t *table, uint64_t
       if ((pw[0] >> (16 * c)) & 0xFFFFu) {  /* out neighbour receives (branch, IN) */
         KT n = KOps<KT>::append(K, (unsigned)c, k), y = KOps<KT>::rc(n, k);
         const bool flip = !KOps<KT>::lt(n, y);
-        const long long j = table_find<KT>(table, nslots, max_probe, flip ? y : n);
+        const long long j = table_find<KT>(table, g, max_probe, flip ? y : n);
         if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN)) {
           const uint32_t idx = slot_aux<KT>(table + j * SU);
           if (flip) cs[idx].outD = 0; else cs[idx].inD = 0;
@@ -186,7 +185,7 @@ __global__ void __launch_bounds__(TPB) k_termini(const uint64_t *table, uint64_t
       if ((pw[1] >> (16 * c)) & 0xFFFFu) {  /* in neighbour receives (branch, OUT) */
         KT n = KOps<KT>::prepend((unsigned)c, K, k), y = KOps<KT>::rc(n, k);
         const bool flip = !KOps<KT>::lt(n, y);
-        const long long j = table_find<KT>(table, nslots, max_probe, flip ? y : n);
+        const long long j = table_find<KT>(table, g, max_probe, flip ? y : n);
         if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN)) {
           const uint32_t idx = slot_aux<KT>(table + j * SU);
           if (flip) cs[idx].inD = 0; else cs[idx].outD = 0;
@@ -619,12 +618,12 @@ bruno_status extract_typed(Ctx *c) {
   const int sms = sms_count();
   k_chain_keys<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, (const uint32_t *)c->chain_list.p, M,
                                                    (uint64_t *)c->ckey.p, (uint64_t *)c->cslot.p);
-  k_chain_init<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, c->cfg.k,
+  k_chain_init<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->geom, c->cfg.k,
                                                    (const uint64_t *)c->ckey.p, (const uint64_t *)c->cslot.p, M,
                                                    (ChainState *)c->cstate.p, (uint8_t *)c->cedge.p, 4096u);
   if (c->n_branch)
     k_termini<KT><<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>(sms * 8, (c->n_branch + TPB - 1) / TPB)), TPB, 0,
-                    c->stream>>>((const uint64_t *)c->table.p, c->nslots, c->cfg.k, (ChainState *)c->cstate.p, 4096u,
+                    c->stream>>>((const uint64_t *)c->table.p, c->geom, c->cfg.k, (ChainState *)c->cstate.p, 4096u,
                                  (const uint32_t *)c->branch_list.p, c->n_branch);
   c->launches += 3;
   return cuda_check(c, cudaGetLastError(), "extract_chains");

@@ -32,6 +32,7 @@ struct DevCounters {
   unsigned long long flag_hist[16];
   unsigned long long lr_applied, lr_remaining, lr_cycles, lr_multi;
   unsigned long long n_cycle, n_isolated, n_ranked, n_heads, n_chain_chars;
+  unsigned long long n_upper;          /* k-mer positions of all reads long enough */
   unsigned int hll[1 << 12];           /* HyperLogLog registers, p = 12 */
 };
 
@@ -70,7 +71,10 @@ struct Ctx {
 
   /* k-mer table */
   Buf table;
+  TableGeom geom{0, 0, 0};
   uint64_t nslots = 0, n_entries = 0, n_slots_claimed = 0;
+  Buf records, bucket_cnt;       /* partitioned counting: 8-byte records per hash bucket */
+  int force_direct_count = 0;    /* tests: count straight into the table */
   Buf chain_list, branch_list;   /* slot indices, filled by the filter */
 
   /* dumps */

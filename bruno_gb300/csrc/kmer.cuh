@@ -155,6 +155,65 @@ __device__ __forceinline__ bool k_palindrome(KT x, int k) {
   return KOps<KT>::eq(x, KOps<KT>::rc(x, k));
 }
 
+/* ---------------------------------------------------------------- table layout
+ * The table is 2^pbits partitions of `region` slots; a key probes linearly inside its
+ * partition.  For k <= 31 the position comes from a bijective mix of the 62-bit k-mer
+ * (so an 8-byte record can carry the k-mer as mixed bits: partition bits implicit), for
+ * k > 31 from a 64-bit hash with one partition. */
+constexpr uint64_t M62 = (1ull << 62) - 1;
+constexpr uint64_t BJ_C1 = 0x3C79AC492BA7B653ull & M62;   /* odd */
+constexpr uint64_t BJ_C2 = 0x1C69B3F74AC4AE35ull & M62;   /* odd */
+__host__ __device__ constexpr uint64_t inv_odd64(uint64_t c) {
+  /* inverse of an odd number modulo 2^64 by Newton iteration (also an inverse mod 2^62) */
+  uint64_t x = c;
+  for (int i = 0; i < 6; ++i) x *= 2 - c * x;
+  return x;
+}
+constexpr uint64_t BJ_I1 = inv_odd64(BJ_C1), BJ_I2 = inv_odd64(BJ_C2);
+
+__host__ __device__ __forceinline__ uint64_t bj_fwd(uint64_t x) {   /* 62-bit -> 62-bit bijection */
+  x ^= x >> 31; x = (x * BJ_C1) & M62;
+  x ^= x >> 29; x = (x * BJ_C2) & M62;
+  x ^= x >> 32;
+  return x;
+}
+__host__ __device__ __forceinline__ uint64_t xs_inv(uint64_t y, int s) {  /* inverse of y = x ^ (x >> s) */
+  uint64_t x = y;
+  for (int t = s; t < 62; t += s) x = y ^ (x >> s);
+  return x;
+}
+__host__ __device__ __forceinline__ uint64_t bj_inv(uint64_t h) {
+  uint64_t x = xs_inv(h, 32);
+  x = (x * BJ_I2) & M62;
+  x = xs_inv(x, 29);
+  x = (x * BJ_I1) & M62;
+  return xs_inv(x, 31);
+}
+
+struct TableGeom {
+  uint64_t nslots;   /* region << pbits */
+  uint64_t region;
+  int pbits;
+};
+
+__device__ __forceinline__ uint64_t table_home(const TableGeom &g, KW1 x) {
+  const uint64_t h = bj_fwd(x.v);
+  const uint64_t q = g.pbits ? (h >> (62 - g.pbits)) : 0;
+  return q * g.region + __umul64hi(h << (2 + g.pbits), g.region);
+}
+__device__ __forceinline__ uint64_t table_home(const TableGeom &g, KW2 x) {
+  return __umul64hi(KOps<KW2>::hash(x), g.region);   /* pbits == 0 */
+}
+/* linear probing inside one partition */
+struct Probe {
+  uint64_t i, lo, hi;
+  __device__ __forceinline__ Probe(const TableGeom &g, uint64_t start) : i(start) {
+    lo = g.pbits ? (start / g.region) * g.region : 0;
+    hi = lo + g.region;
+  }
+  __device__ __forceinline__ void next() { if (++i == hi) i = lo; }
+};
+
 /* ---------------------------------------------------------------- table slots */
 template <class KT> struct Slot;
 

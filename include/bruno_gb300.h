@@ -57,6 +57,8 @@ typedef struct bruno_cfg {
   int32_t keep_filtered;    /* 1: record the filtered (k+2)-mer entries for copy-out */
   int32_t exact_ranking;    /* 1: always run the round-synchronous ranking; 0: use the O(M)
                                ruling-set ranking whenever the chain map is consistent */
+  int32_t direct_count;     /* 1: count every instance straight into the whole table; 0: for
+                               k <= 31 count through hash-partitioned records (L2-resident) */
 } bruno_cfg;
 
 typedef struct bruno_sizes {
@@ -160,8 +162,9 @@ bruno_status bruno_host_free(void *p);
 
 /* Device times of the last build, milliseconds, from CUDA events on the context's stream:
  * ms[0..5] = phases parse, count_k2mers, filter_insert, chainmap, list_rank, compress;
- * ms[6..8] = kernels k_hll (distinct-count estimate), k_table_init, k_count.  Writes
- * min(n, 9) values. */
+ * ms[6..8] = counting sub-steps: distinct-count estimate (with the record extraction on
+ * the partitioned path), whole-table initialisation (direct path only), and the counting
+ * itself (the partition-by-partition inserts, or k_count).  Writes min(n, 9) values. */
 bruno_status bruno_phase_ms(bruno_ctx *ctx, double *ms, size_t n);
 #ifdef __cplusplus
 }

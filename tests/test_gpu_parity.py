@@ -52,15 +52,18 @@ def compare(gpu, ref):
     assert chain_set(*gpu["chains"]) == chain_set(*ref["chains"]), "compacted chains"
 
 
-@pytest.mark.parametrize("exact", [False, True], ids=["ruling_set", "round_sync"])
+PATHS = {"fast": {}, "round_sync": {"exact_ranking": True}, "direct_count": {"direct_count": True}}
+
+
+@pytest.mark.parametrize("path", sorted(PATHS))
 @pytest.mark.parametrize("opt", sorted(OPTIONS))
 @pytest.mark.parametrize("fname", FASTQS)
-def test_fixture_parity(fname, opt, exact):
+def test_fixture_parity(fname, opt, path):
     thr_on, lo, mu = OPTIONS[opt]
     thr = bg.thresholds(lo)
     data = fixture_bytes(fname)
     ref = oracle.run(data, k=31, thresholding=thr_on, thresh=thr, min_update=mu, keep_k2=True, keep_filtered=True)
-    compare(gpu_run(data, 31, thr_on, thr, mu, exact_ranking=exact), ref)
+    compare(gpu_run(data, 31, thr_on, thr, mu, **PATHS[path]), ref)
 
 
 def test_known_answer_on_gpu():
@@ -83,9 +86,9 @@ def test_repeat_rich_workload_parity():
     w = synth.Workload("rep", 2_000_000, 150, 400_000, 0.005, 31, (3,), 0.02, (1000, 10000), (2, 8), (0.01, 0.01), 3)
     fq = synth.make_fastq(w)
     thr = bg.thresholds(w.lower)
-    for mu, exact in ((True, False), (False, False), (True, True)):
+    for mu, kw in ((True, {}), (False, {}), (True, {"exact_ranking": True}), (True, {"direct_count": True})):
         ref = oracle.run(fq, k=31, thresh=thr, min_update=mu, threads=16, keep_k2=True, keep_filtered=True)
-        compare(gpu_run(fq, 31, True, thr, mu, exact_ranking=exact), ref)
+        compare(gpu_run(fq, 31, True, thr, mu, **kw), ref)
 
 
 def test_two_files_count_into_one_table():

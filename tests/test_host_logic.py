@@ -49,3 +49,43 @@ def test_workloads_match_configs():
     s, m = synth.WORKLOADS["plain-small"], synth.WORKLOADS["plain-scale"]
     assert (s.genome_len, s.n_reads, s.read_len, s.sub_rate, s.k) == (1_000_000, 100_000, 100, 0.01, 31)
     assert (m.genome_len, m.read_len, m.k, round(m.coverage)) == (50_000_000, 150, 31, 30)
+
+
+def test_partition_mix_is_a_bijection():
+    """the 62-bit mix that lets an 8-byte record carry a k-mer (kmer.cuh bj_fwd/bj_inv),
+    restated here with the constants read from the source"""
+    import os
+    import random
+    import re
+    src = open(os.path.join(os.path.dirname(bg.__file__), "csrc", "kmer.cuh")).read()
+    c1 = int(re.search(r"BJ_C1 = (0x[0-9A-Fa-f]+)ull", src).group(1), 16)
+    c2 = int(re.search(r"BJ_C2 = (0x[0-9A-Fa-f]+)ull", src).group(1), 16)
+    m = (1 << 62) - 1
+    c1, c2 = c1 & m, c2 & m
+    assert c1 & 1 and c2 & 1
+
+    def inv(c):
+        x = c
+        for _ in range(6):
+            x = (x * (2 - c * x)) % (1 << 64)
+        return x
+
+    def fwd(x):
+        x ^= x >> 31; x = (x * c1) & m; x ^= x >> 29; x = (x * c2) & m; x ^= x >> 32
+        return x
+
+    def xs_inv(y, s):
+        x, t = y, s
+        while t < 62:
+            x, t = y ^ (x >> s), t + s
+        return x
+
+    def back(h):
+        x = xs_inv(h, 32); x = (x * inv(c2)) & m; x = xs_inv(x, 29); x = (x * inv(c1)) & m
+        return xs_inv(x, 31)
+
+    rnd = random.Random(5)
+    for _ in range(20000):
+        v = rnd.getrandbits(62)
+        h = fwd(v)
+        assert h <= m and back(h) == v
