@@ -962,6 +962,7 @@ __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
       }
     }
     if (threadIdx.x < s_nb && s_base_b + threadIdx.x < a.list_cap) a.branch_list[s_base_b + threadIdx.x] = s_branch[threadIdx.x];
+    __syncthreads();   /* every thread has read s_nc / s_nb before the next stripe resets them */
   }
   unsigned long long nodes = warp_sum(t.nodes);
   if ((threadIdx.x & 31) == 0) atomicAdd(&s_nodes, nodes);

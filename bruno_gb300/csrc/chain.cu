@@ -107,11 +107,15 @@ __device__ __forceinline__ long long table_find(const uint64_t *table, const Tab
 /* ================================================================ chain indices */
 /* chain index i -> its slot (listed by the filter, which also stored i in the slot) */
 template <class KT>
-__global__ void __launch_bounds__(TPB) k_chain_keys(const uint64_t *table, const uint32_t *chain_list, uint64_t M,
-                                                     uint64_t *ckey, uint64_t *cslot) {
+__global__ void __launch_bounds__(TPB) k_chain_keys(const uint64_t *table, uint64_t nslots, const uint32_t *chain_list,
+                                                     uint64_t M, uint64_t *ckey, uint64_t *cslot, DevCounters *ctr) {
   constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t sl = chain_list[i];
+    uint64_t sl = chain_list[i];
+    if (sl >= nslots) {   /* a list entry that was never written: report, never dereference */
+      atomicOr(&ctr->err, (unsigned long long)DERR_INVARIANT);
+      sl = 0;
+    }
     const uint64_t *s = table + sl * SU;
     for (int w = 0; w < KWD; ++w) ckey[i * KWD + w] = s[w];
     cslot[i] = sl;
@@ -138,7 +142,7 @@ __global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, Table
       KT n = KOps<KT>::prepend((unsigned)inc, K, k), y = KOps<KT>::rc(n, k);
       const bool flip = !KOps<KT>::lt(n, y);
       const long long j = table_find<KT>(table, g, max_probe, flip ? y : n);
-      if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN))
+      if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN) && slot_aux<KT>(table + j * SU) < M)
         st.inP = (uint64_t)slot_aux<KT>(table + j * SU) | (flip ? PF_FLIP : 0);
       else
         st.inP = PF_EXT | i;
@@ -150,7 +154,7 @@ __global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, Table
       KT n = KOps<KT>::append(K, (unsigned)outc, k), y = KOps<KT>::rc(n, k);
       const bool flip = !KOps<KT>::lt(n, y);
       const long long j = table_find<KT>(table, g, max_probe, flip ? y : n);
-      if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN))
+      if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN) && slot_aux<KT>(table + j * SU) < M)
         st.outP = (uint64_t)slot_aux<KT>(table + j * SU) | (flip ? PF_FLIP : 0);
       else
         st.outP = PF_EXT | PF_EXTOUT | i;
@@ -165,7 +169,7 @@ __global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, Table
 
 /* neighbours of branch nodes get their facing side set to branch_neighbor (0) */
 template <class KT>
-__global__ void __launch_bounds__(TPB) k_termini(const uint64_t *table, TableGeom g, int k, ChainState *cs,
+__global__ void __launch_bounds__(TPB) k_termini(const uint64_t *table, TableGeom g, int k, ChainState *cs, uint64_t M,
                                                   uint32_t max_probe, const uint32_t *branch_list, uint64_t nb) {
   constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
   for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nb; q += (uint64_t)gridDim.x * blockDim.x) {
@@ -179,7 +183,7 @@ __global__ void __launch_bounds__(TPB) k_termini(const uint64_t *table, TableGeo
         const long long j = table_find<KT>(table, g, max_probe, flip ? y : n);
         if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN)) {
           const uint32_t idx = slot_aux<KT>(table + j * SU);
-          if (flip) cs[idx].outD = 0; else cs[idx].inD = 0;
+          if (idx < M) { if (flip) cs[idx].outD = 0; else cs[idx].inD = 0; }
         }
       }
       if ((pw[1] >> (16 * c)) & 0xFFFFu) {  /* in neighbour receives (branch, OUT) */
@@ -188,7 +192,7 @@ __global__ void __launch_bounds__(TPB) k_termini(const uint64_t *table, TableGeo
         const long long j = table_find<KT>(table, g, max_probe, flip ? y : n);
         if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN)) {
           const uint32_t idx = slot_aux<KT>(table + j * SU);
-          if (flip) cs[idx].inD = 0; else cs[idx].outD = 0;
+          if (idx < M) { if (flip) cs[idx].inD = 0; else cs[idx].outD = 0; }
         }
       }
     }
@@ -616,17 +620,21 @@ bruno_status extract_typed(Ctx *c) {
   if ((st = ensure(c, c->cedge, Mb)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->cstate, Mb * sizeof(ChainState))) != BRUNO_OK) return st;
   const int sms = sms_count();
-  k_chain_keys<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, (const uint32_t *)c->chain_list.p, M,
-                                                   (uint64_t *)c->ckey.p, (uint64_t *)c->cslot.p);
+  cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
+  k_chain_keys<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots,
+                                                   (const uint32_t *)c->chain_list.p, M, (uint64_t *)c->ckey.p,
+                                                   (uint64_t *)c->cslot.p, c->dctr);
   k_chain_init<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->geom, c->cfg.k,
                                                    (const uint64_t *)c->ckey.p, (const uint64_t *)c->cslot.p, M,
                                                    (ChainState *)c->cstate.p, (uint8_t *)c->cedge.p, 4096u);
   if (c->n_branch)
     k_termini<KT><<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>(sms * 8, (c->n_branch + TPB - 1) / TPB)), TPB, 0,
-                    c->stream>>>((const uint64_t *)c->table.p, c->geom, c->cfg.k, (ChainState *)c->cstate.p, 4096u,
+                    c->stream>>>((const uint64_t *)c->table.p, c->geom, c->cfg.k, (ChainState *)c->cstate.p, M, 4096u,
                                  (const uint32_t *)c->branch_list.p, c->n_branch);
   c->launches += 3;
-  return cuda_check(c, cudaGetLastError(), "extract_chains");
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  if (c->hctr->err & DERR_INVARIANT) return set_err(c, BRUNO_ERR_INVARIANT, "chain list incomplete");
+  return BRUNO_OK;
 }
 
 template <class KT>
