@@ -238,6 +238,52 @@ __device__ __forceinline__ unsigned base_at(const uint64_t *w, int i) {
   return (unsigned)(w[i >> 5] >> (62 - 2 * (i & 31))) & 3u;
 }
 
+/* The k-mers of read positions [pc, e) of a staged chunk, cut into 32 contiguous runs
+ * (one per lane).  Each lane extracts its first k-mer and its reverse complement once,
+ * then rolls both one base at a time: fwd' = fwd.c, rc' = comp(c).rc without its last
+ * base.  fn(valid, canonical k-mer, biedge code) is called in lock-step by the whole warp,
+ * valid == false for lanes whose run is over. */
+template <class KT, class F>
+__device__ __forceinline__ void for_each_kmer_run(const uint64_t *words, uint32_t pc, uint32_t e, uint32_t p0,
+                                                  uint32_t L, int k, int lane, F &&fn) {
+  const uint32_t n = e - pc, r = (n + 31) >> 5;
+  const uint32_t s = pc + lane * r, send = min(e, s + r);
+  KT fwd{}, rev{};
+  unsigned prev = 0;  /* base before the current k-mer */
+  if (s < send) {
+    const int lp = (int)(s - p0 + 32);
+    fwd = KOps<KT>::extract(words, lp, k);
+    rev = KOps<KT>::rc(fwd, k);
+    prev = s > 0 ? base_at(words, lp - 1) : 0u;
+  }
+  for (uint32_t j = 0; j < r; ++j) {
+    const uint32_t p = s + j;
+    const bool valid = p < send;
+    KT x{};
+    unsigned code = 0, nb = 0;
+    if (valid) {
+      const bool has_out = p + k < L;
+      nb = has_out ? base_at(words, (int)(p - p0 + 32) + k) : 0u;
+      unsigned in5 = p > 0 ? prev + 1u : 0u, out5 = has_out ? nb + 1u : 0u;
+      /* lex_less: keep if fwd < rc(fwd), else flip and reverse-complement the biedge */
+      if (KOps<KT>::lt(fwd, rev)) {
+        x = fwd;
+      } else {
+        x = rev;
+        const unsigned ni = out5 ? 5u - out5 : 0u, no = in5 ? 5u - in5 : 0u;
+        in5 = ni; out5 = no;
+      }
+      code = biedge_code(in5, out5);
+    }
+    fn(valid, x, code);
+    if (valid) {
+      prev = KOps<KT>::first(fwd, k);
+      fwd = KOps<KT>::append(fwd, nb, k);
+      rev = KOps<KT>::prepend(3u - nb, rev, k);
+    }
+  }
+}
+
 /* ============================================================ distinct estimate */
 
 constexpr int HLL_P = 12;
@@ -266,18 +312,13 @@ __global__ void __launch_bounds__(TPB) k_hll(const uint64_t *rstart, const uint6
       const uint32_t pend = min(npos, p0 + CHUNK_POS);
       __syncwarp();
       if (stage_chunk(rv, p0, pend, k, words, lane) && one_chunk) break;
-      for (uint32_t pb = p0; pb < pend; pb += 32) {
-        const uint32_t p = pb + lane;
-        if (p < pend) {
-          KT x = KOps<KT>::extract(words, (int)(p - p0 + 32), k);
-          KT y = KOps<KT>::rc(x, k);
-          if (!KOps<KT>::lt(x, y)) x = y;
-          const uint64_t h = mix64(KOps<KT>::hash(x) ^ 0x6a09e667f3bcc909ull);
-          const unsigned idx = (unsigned)(h >> (64 - HLL_P));
-          const unsigned rho = (unsigned)__clzll((h << HLL_P) | (1ull << (HLL_P - 1))) + 1u;
-          if (rho > reg[idx]) atomicMax(&reg[idx], rho);
-        }
-      }
+      for_each_kmer_run<KT>(words, p0, pend, p0, rv.L, k, lane, [&](bool valid, KT x, unsigned) {
+        if (!valid) return;
+        const uint64_t h = KOps<KT>::hash(x);
+        const unsigned idx = (unsigned)(h >> (64 - HLL_P));
+        const unsigned rho = (unsigned)__clzll((h << HLL_P) | (1ull << (HLL_P - 1))) + 1u;
+        if (rho > reg[idx]) atomicMax(&reg[idx], rho);
+      });
     }
   }
   __syncthreads();
@@ -406,10 +447,11 @@ __device__ __forceinline__ bool key_cont(KW2 k) { return (k.hi & KEY_CONT) != 0;
 template <class KT>
 __device__ __forceinline__ bool table_count(uint64_t *table, const TableGeom &g, uint32_t max_probe, KT x,
                                             unsigned code, uint64_t home, uint64_t *raw,
-                                            unsigned long long &slot_claims, unsigned long long &entry_claims) {
+                                            unsigned long long &slot_claims, unsigned long long &entry_claims,
+                                            uint64_t part_lo = ~0ull) {
   constexpr int SU = Slot<KT>::U64, NE = Slot<KT>::ENTRIES, KWD = Slot<KT>::KEYW;
   bool seen_primary = false;
-  Probe pr(g, home);
+  Probe pr(g, home, part_lo);
   for (uint32_t probe = 0; probe < max_probe; ++probe, pr.next()) {
     uint64_t *slot = table + pr.i * SU;
     if (probe) ld_slot<SU>(slot, raw);
@@ -609,14 +651,10 @@ __global__ void __launch_bounds__(TPB) k_extract(const uint64_t *rstart, const u
         }
       }
       const uint32_t e = min(pend, pc + budget);
-      for (uint32_t pb = pc; pb < e; pb += 32) {
-        const uint32_t p = pb + lane;
-        const bool valid = p < e;
+      for_each_kmer_run<KW1>(words, pc, e, p0, rv.L, k, lane, [&](bool valid, KW1 x, unsigned code) {
         uint64_t rec = 0;
         unsigned bucket = 0;
         if (valid) {
-          KW1 x; unsigned code;
-          kmer_at<KW1>(words, p, p0, rv.L, k, x, code);
           const uint64_t h = bj_fwd(x.v);
           bucket = (unsigned)(h >> LOW_BITS);
           rec = ((h & ((1ull << LOW_BITS) - 1)) << 5) | code;
@@ -634,7 +672,7 @@ __global__ void __launch_bounds__(TPB) k_extract(const uint64_t *rstart, const u
           S.rec[o] = rec;
           S.part[o] = (uint8_t)bucket;
         }
-      }
+      });
       budget -= e - pc;
       pc = e;
     }
@@ -693,7 +731,9 @@ __global__ void k_part_init(uint64_t *table, uint64_t first_slot, uint64_t nslot
     t[i] = ((int)(i % SU) < KWD) ? KEY_EMPTY : 0ull;
 }
 
-/* Phase B: the records of the buckets of partition q (blockIdx.y picks the bucket) */
+/* Phase B: the records of the buckets of partition q (blockIdx.y picks the bucket); four
+ * records in flight per thread: their slot reads are all issued before any is used */
+constexpr int INS_BATCH = 4;
 __global__ void __launch_bounds__(TPB) k_insert(const uint64_t *records, const unsigned long long *bucket_cnt,
                                                  uint64_t cap, int bucket0, uint64_t *table, TableGeom g,
                                                  uint32_t max_probe, DevCounters *ctr) {
@@ -701,25 +741,33 @@ __global__ void __launch_bounds__(TPB) k_insert(const uint64_t *records, const u
   const int b = bucket0 + (int)blockIdx.y;
   const uint64_t n = min((unsigned long long)cap, bucket_cnt[b]);
   const uint64_t *rb = records + (uint64_t)b * cap;
+  /* every record of bucket b lives in partition q = b >> (8 - pbits) */
+  const uint64_t lo = (uint64_t)(b >> (NBUCKET_BITS - g.pbits)) * g.region;
   unsigned long long slots = 0, entries = 0;
   bool full = false;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += 2 * stride) {
-    /* two records in flight per thread */
-    const uint64_t j = i + stride;
-    const uint64_t r0 = __ldcs(rb + i), r1 = j < n ? __ldcs(rb + j) : 0;
-    const uint64_t h0 = ((uint64_t)b << LOW_BITS) | (r0 >> 5), h1 = ((uint64_t)b << LOW_BITS) | (r1 >> 5);
-    const uint64_t q0 = g.pbits ? (h0 >> (62 - g.pbits)) : 0, q1 = g.pbits ? (h1 >> (62 - g.pbits)) : 0;
-    const uint64_t home0 = q0 * g.region + __umul64hi(h0 << (2 + g.pbits), g.region);
-    const uint64_t home1 = q1 * g.region + __umul64hi(h1 << (2 + g.pbits), g.region);
-    uint64_t ra[SU], rc[SU];
-    ld_slot<SU>(table + home0 * SU, ra);
-    if (j < n) ld_slot<SU>(table + home1 * SU, rc);
-    if (!table_count<KW1>(table, g, max_probe, KW1{bj_inv(h0)}, (unsigned)(r0 & 31), home0, ra, slots, entries))
-      full = true;
-    if (j < n &&
-        !table_count<KW1>(table, g, max_probe, KW1{bj_inv(h1)}, (unsigned)(r1 & 31), home1, rc, slots, entries))
-      full = true;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += INS_BATCH * stride) {
+    uint64_t rec[INS_BATCH], home[INS_BATCH], raw[INS_BATCH][SU];
+    #pragma unroll
+    for (int q = 0; q < INS_BATCH; ++q) {
+      const uint64_t j = i + q * stride;
+      rec[q] = j < n ? __ldcs(rb + j) : ~0ull;
+    }
+    #pragma unroll
+    for (int q = 0; q < INS_BATCH; ++q) {
+      if (rec[q] == ~0ull) continue;
+      const uint64_t h = ((uint64_t)b << LOW_BITS) | (rec[q] >> 5);
+      home[q] = lo + __umul64hi(h << (2 + g.pbits), g.region);
+      ld_slot<SU>(table + home[q] * SU, raw[q]);
+    }
+    #pragma unroll
+    for (int q = 0; q < INS_BATCH; ++q) {
+      if (rec[q] == ~0ull) continue;
+      const uint64_t h = ((uint64_t)b << LOW_BITS) | (rec[q] >> 5);
+      if (!table_count<KW1>(table, g, max_probe, KW1{bj_inv(h)}, (unsigned)(rec[q] & 31), home[q], raw[q], slots,
+                            entries, lo))
+        full = true;
+    }
   }
   slots = warp_sum(slots); entries = warp_sum(entries);
   if ((threadIdx.x & 31) == 0) {

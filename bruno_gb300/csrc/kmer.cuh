@@ -207,8 +207,9 @@ __device__ __forceinline__ uint64_t table_home(const TableGeom &g, KW2 x) {
 /* linear probing inside one partition */
 struct Probe {
   uint64_t i, lo, hi;
-  __device__ __forceinline__ Probe(const TableGeom &g, uint64_t start) : i(start) {
-    lo = g.pbits ? (start / g.region) * g.region : 0;
+  /* part_lo: the first slot of the partition if the caller knows it (saves a division) */
+  __device__ __forceinline__ Probe(const TableGeom &g, uint64_t start, uint64_t part_lo = ~0ull) : i(start) {
+    lo = part_lo != ~0ull ? part_lo : (g.pbits ? (start / g.region) * g.region : 0);
     hi = lo + g.region;
   }
   __device__ __forceinline__ void next() { if (++i == hi) i = lo; }
