@@ -733,7 +733,7 @@ __global__ void k_part_init(uint64_t *table, uint64_t first_slot, uint64_t nslot
 
 /* Phase B: the records of the buckets of partition q (blockIdx.y picks the bucket); four
  * records in flight per thread: their slot reads are all issued before any is used */
-constexpr int INS_BATCH = 4;
+constexpr int INS_BATCH = 2;
 __global__ void __launch_bounds__(TPB) k_insert(const uint64_t *records, const unsigned long long *bucket_cnt,
                                                  uint64_t cap, int bucket0, uint64_t *table, TableGeom g,
                                                  uint32_t max_probe, DevCounters *ctr) {

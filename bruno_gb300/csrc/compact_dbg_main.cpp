@@ -1,0 +1,204 @@
+/*
+ * compact_dbg_main.cpp -- command-line driver on the GB300 library, with the flags and
+ * output files of the reference driver test/test/compact_dbg_freq_construct_clean.cpp
+ * (main :848-1030, do_work :431-840, built with -DNCLEAN):
+ *
+ *   -T          thresholding (build_index_thresholded), else build_index
+ *   -L n [-L n -L n], -U ...  lower / upper thresholds (one value = (k+1)-mer bound,
+ *               three values = k, k+1, k+2; :937-961)
+ *   -R          list_rank_min_update, else list_rank
+ *   -B          benchmark: only .chain.fasta and .branch.fasta
+ *   -O prefix   output prefix
+ *   -k K        k-mer length (the reference's compile-time pK)
+ *   files...    FASTQ files, all counted into one table
+ *
+ * Outputs: <prefix>.chain.fasta (print_chain_string, compact_dbg_io.hpp:323-363),
+ * <prefix>.chain.components (print_chain_nodes, :463-498), <prefix>.branch.fasta
+ * (print_branch_fasta, :254-299), and unless -B <prefix>.branch.edges
+ * (print_branch_edge_frequencies, compact_dbg_stats.hpp:219-262) and <prefix>.graph.all.
+ * Like the reference, records are sorted before printing; the .chain.fasta has no newline
+ * before its first record and none after its last.
+ */
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "bruno_gb300.hpp"
+
+namespace {
+
+bool read_file(const char *fn, std::string &out) {
+  FILE *f = fopen(fn, "rb");
+  if (!f) return false;
+  char buf[1 << 16];
+  size_t n;
+  while ((n = fread(buf, 1, sizeof(buf), f)) > 0) out.append(buf, n);
+  fclose(f);
+  return true;
+}
+
+struct Kmer {
+  uint64_t w[2] = {0, 0};
+  bool operator<(const Kmer &o) const { return w[1] != o.w[1] ? w[1] < o.w[1] : w[0] < o.w[0]; }
+  bool operator==(const Kmer &o) const { return w[0] == o.w[0] && w[1] == o.w[1]; }
+};
+
+Kmer load(const uint64_t *p, int words) {
+  Kmer k;
+  k.w[0] = p[0];
+  if (words > 1) k.w[1] = p[1];
+  return k;
+}
+
+unsigned base(const Kmer &x, int i) {  /* i counted from the last base */
+  return (unsigned)((i < 32 ? x.w[0] >> (2 * i) : x.w[1] >> (2 * (i - 32))) & 3u);
+}
+
+std::string ascii(const Kmer &x, int k) {
+  std::string s(k, 'A');
+  for (int i = 0; i < k; ++i) s[k - 1 - i] = "ACGT"[base(x, i)];
+  return s;
+}
+
+Kmer rc(const Kmer &x, int k) {
+  Kmer y;
+  for (int i = 0; i < k; ++i) {
+    const unsigned b = 3u - base(x, i);   /* base i from the end becomes base i from the start */
+    const int pos = k - 1 - i;             /* its index from the end in the result */
+    if (pos < 32) y.w[0] |= (uint64_t)b << (2 * pos); else y.w[1] |= (uint64_t)b << (2 * (pos - 32));
+  }
+  return y;
+}
+
+Kmer canonical(const Kmer &x, int k) {
+  Kmer y = rc(x, k);
+  return x < y ? x : y;
+}
+
+bool write(const std::string &fn, const std::string &s) {
+  FILE *f = fopen(fn.c_str(), "wb");
+  if (!f) return false;
+  fwrite(s.data(), 1, s.size(), f);
+  fclose(f);
+  return true;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  bruno_cfg cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.k = 31;
+  std::vector<uint64_t> lo, hi;
+  std::string prefix = "./output";
+  bool benchmark = false;
+  std::vector<const char *> files;
+  for (int i = 1; i < argc; ++i) {
+    std::string a = argv[i];
+    if (a == "-T") cfg.thresholding = 1;
+    else if (a == "-R") cfg.min_update = 1;
+    else if (a == "-B") benchmark = true;
+    else if (a == "-L" && i + 1 < argc) lo.push_back(strtoull(argv[++i], nullptr, 10));
+    else if (a == "-U" && i + 1 < argc) hi.push_back(strtoull(argv[++i], nullptr, 10));
+    else if (a == "-O" && i + 1 < argc) prefix = argv[++i];
+    else if (a == "-k" && i + 1 < argc) cfg.k = atoi(argv[++i]);
+    else if (a == "-d" && i + 1 < argc) cfg.device = atoi(argv[++i]);
+    else if (!a.empty() && a[0] == '-') { fprintf(stderr, "unknown flag %s\n", a.c_str()); return 1; }
+    else files.push_back(argv[i]);
+  }
+  if (files.empty()) {
+    fprintf(stderr, "usage: %s [-T] [-L n].. [-U n].. [-R] [-B] [-O prefix] [-k K] reads.fastq..\n", argv[0]);
+    return 1;
+  }
+  const std::vector<uint64_t> t = bruno_gb300::thresholds(lo, hi);
+  std::copy(t.begin(), t.end(), cfg.thresh);
+  const int k = cfg.k, words = k <= 31 ? 1 : 2;
+  try {
+    std::vector<std::string> data(files.size());
+    for (size_t i = 0; i < files.size(); ++i)
+      if (!read_file(files[i], data[i])) { fprintf(stderr, "cannot read %s\n", files[i]); return 1; }
+    const auto t0 = std::chrono::steady_clock::now();
+    bruno_gb300::context ctx(cfg);
+    bruno_gb300::debruijn_graph idx(ctx);
+    bruno_gb300::debruijn_chain_graph chainmap(ctx);
+    for (auto &d : data) idx.get_map().load_fastq(d.data(), d.size());
+    idx.get_map().compute_biedge_freqencies();                  /* build_index_thresholded */
+    idx.get_map().local_insert_by_freqencies(t);
+    chainmap.extract_chains(idx);                               /* do_work :549 */
+    const size_t iterations = cfg.min_update ? chainmap.list_rank_min_update() : chainmap.list_rank();
+    bruno_gb300::listranked_chain_nodes ranked = chainmap.to_ranked_chain_nodes();
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::vector<uint64_t> nkeys;
+    std::vector<uint16_t> ncounts;
+    std::vector<uint8_t> nflags;
+    idx.get_map().to_vector(nkeys, ncounts, nflags);
+    const bruno_sizes s = ctx.sizes();
+    printf("reads %llu used %llu instances %llu nodes %llu branch %llu chain %llu iterations %zu cycle %llu "
+           "isolated %llu chains %llu  (%.3f s)\n",
+           (unsigned long long)s.n_reads, (unsigned long long)s.n_reads_used, (unsigned long long)s.n_instances,
+           (unsigned long long)s.n_nodes, (unsigned long long)s.n_branch, (unsigned long long)s.n_chain_nodes,
+           iterations, (unsigned long long)s.n_cycle_nodes, (unsigned long long)s.n_isolated,
+           (unsigned long long)s.n_chains, secs);
+
+    /* .chain.fasta: sorted by chain_rep_less (rep, |dist|) */
+    const size_t n = ranked.size();
+    std::vector<size_t> order(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+      const Kmer ra = load(&ranked.rep[a * words], words), rb = load(&ranked.rep[b * words], words);
+      if (!(ra == rb)) return ra < rb;
+      const int da = std::abs(ranked.dist[a]), db = std::abs(ranked.dist[b]);
+      if (da != db) return da < db;
+      return load(&ranked.K[a * words], words) < load(&ranked.K[b * words], words);
+    });
+    std::string fa;
+    for (size_t i : order) {
+      const Kmer K = load(&ranked.K[i * words], words);
+      if (ranked.dist[i] == 0) {
+        fa += "\n>" + ascii(canonical(K, k), k) + "\n" + ascii(load(&ranked.rep[i * words], words), k);
+      } else {
+        fa += "ACGT"[base(K, 0)];
+      }
+    }
+    if (!write(prefix + ".chain.fasta", fa.empty() ? fa : fa.substr(1))) return 1;
+    /* .chain.components: sorted by K (chain_node_less) */
+    if (!benchmark) {
+      std::sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+        return load(&ranked.K[a * words], words) < load(&ranked.K[b * words], words);
+      });
+      std::string cc;
+      for (size_t i : order) {
+        const Kmer K = load(&ranked.K[i * words], words), c = canonical(K, k);
+        cc += ascii(c, k) + "\t" + ascii(load(&ranked.rep[i * words], words), k) + "\t" +
+              std::to_string(ranked.dist[i]) + "\t" + (K == c ? "1" : "0") + "\n";
+      }
+      if (!write(prefix + ".chain.components", cc)) return 1;
+    }
+    /* nodes sorted by k-mer: .branch.fasta, .branch.edges, .graph.all */
+    std::vector<size_t> nord(nflags.size());
+    std::iota(nord.begin(), nord.end(), 0);
+    std::sort(nord.begin(), nord.end(),
+              [&](size_t a, size_t b) { return load(&nkeys[a * words], words) < load(&nkeys[b * words], words); });
+    std::string bf, be, ga;
+    for (size_t i : nord) {
+      const std::string a = ascii(load(&nkeys[i * words], words), k);
+      const uint16_t *c = &ncounts[i * 9];
+      std::string line = a;
+      for (int j = 4; j < 8; ++j) line += "\t" + std::to_string(c[j]);
+      for (int j = 0; j < 4; ++j) line += "\t" + std::to_string(c[j]);
+      line += "\t" + std::to_string(c[8]) + "\n";
+      if (nflags[i] & 1) { bf += ">" + a + "\n" + a + "\n"; be += line; }
+      ga += line;
+    }
+    if (!write(prefix + ".branch.fasta", bf)) return 1;
+    if (!benchmark && (!write(prefix + ".branch.edges", be) || !write(prefix + ".graph.all", ga))) return 1;
+  } catch (const bruno_gb300::error &e) {
+    fprintf(stderr, "error: %s\n", e.what());
+    return 2;
+  }
+  return 0;
+}

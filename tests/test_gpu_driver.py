@@ -1,0 +1,36 @@
+"""The reference driver's integration tests, restated: run the GB300 driver and the oracle
+driver with the same flags on the same FASTQ and diff every output file (the reference's
+test_compact_debruijn_graph_*.sh compare outputs of variants and rank counts the same way)."""
+import os
+import subprocess
+
+import pytest
+
+from bruno_gb300 import build
+from oracle import oracle
+from conftest import DATA
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    ("test.unitiqs.fastq", []),
+    ("test.star.unitiqs.fastq", ["-T", "-L", "2", "-R"]),
+    ("debruijn.palindrome_chr14.fastq", ["-T", "-L", "2", "-R"]),
+    ("debruijn.shifted_cycle_chr14.fastq", ["-T", "-L", "2"]),
+    ("debruijn.bubble.fastq", ["-T", "-L", "1", "-L", "2", "-L", "1", "-R"]),
+    ("natural.withN.fastq", []),
+]
+OUTPUTS = [".chain.fasta", ".chain.components", ".branch.fasta", ".branch.edges", ".graph.all"]
+
+
+@pytest.mark.parametrize("fname,flags", CASES)
+def test_driver_outputs_identical(tmp_path, fname, flags):
+    drv = build.build_driver()
+    oracle.build()
+    fq = os.path.join(DATA, fname)
+    subprocess.run([drv, *flags, "-O", str(tmp_path / "gpu"), fq], check=True, capture_output=True)
+    subprocess.run([oracle.CLI, *flags, "-O", str(tmp_path / "ref"), fq], check=True, capture_output=True)
+    for ext in OUTPUTS:
+        a = open(tmp_path / ("gpu" + ext), "rb").read()
+        b = open(tmp_path / ("ref" + ext), "rb").read()
+        assert a == b, f"{fname} {' '.join(flags)}: {ext} differs"
