@@ -9,7 +9,8 @@ emission -- over the 50 Mbp / 30x / 150 bp / k=31 / -L 3 synthetic workload.
           stream, which is torch's current stream).
   e2e     the same through the C ABI with pinned host buffers: the FASTQ host->device copy
           and the device->host read of the compacted chains are inside the timed region.
-  roofline  the dominant kernel (k_count) against the measured HBM copy bandwidth.
+  roofline  the dominant kernel (k_insert, per table partition) against the measured HBM
+          copy bandwidth, with k_extract beside it.
   cpu_baseline  the CPU oracle (a restatement of the reference's CPU path) on a bounded
           sample of the same workload, with every host thread.
 
@@ -246,19 +247,26 @@ def main():
     e2e_value = inst_step * args.steps * world / (ems / 1e3)
     d2h = nch + 8 * (nc + 1) + 8 * g.words * nc
 
-    # roofline of the dominant kernel, k_count: algorithmic bytes per launch = the read
-    # sequence bytes + 16 B of read span per read + one 32 B sector read and one 32 B
-    # write-back per (k-mer, biedge) instance
-    k_count_ms = statistics.mean(p["count_insert"] for p in kms)
-    alg_bytes = sizes["n_reads"] * w.read_len + 16 * sizes["n_reads"] + 64 * inst_step
+    # roofline of the dominant kernel, k_insert (phase B of k <= 31 counting; one launch per
+    # table partition, each preceded by the partition's init).  Algorithmic bytes per launch:
+    # the partition's 8-byte records read once + its slot region (32 B a slot) written back
+    # once.  Phase A (k_extract) is reported beside it: the FASTQ bytes and 16 B of read
+    # span per read read once, 8 B per record written once.
+    parts = max(1, sizes["table_partitions"])
+    insert_ms = statistics.mean(p["count_insert"] for p in kms)
+    launch_ms = insert_ms / parts
+    alg_bytes = (8 * inst_step + 32 * sizes["table_slots"]) / parts
     peak, peak_src = measured_peak()
-    achieved = alg_bytes / (k_count_ms / 1e3) / 1e9
+    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+    extract_ms = statistics.mean(p["count_estimate"] for p in kms)
+    extract_bytes = n + 16 * sizes["n_reads"] + 8 * inst_step
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "k_count_traffic.json")
+    tpath = os.path.join(ROOT, "profiles", "k_insert_traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             tj = json.load(f)
-        traffic = tj.get("bytes_per_instance", 0) * inst_step if tj.get("bytes_per_instance") else None
+        if tj.get("bytes_per_record"):
+            traffic = tj["bytes_per_record"] * inst_step / parts
     phases = {k: round(statistics.mean(p[k] for p in kms), 3) for k in kms[0]}
 
     if rank == 0:
@@ -268,12 +276,16 @@ def main():
                 "config": workload_config(w),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n, "d2h_bytes_per_step": d2h,
                         "ms_per_step": ems / args.steps},
-                "roofline": {"bound": "hbm", "kernel": "k_count", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "roofline": {"bound": "hbm", "kernel": "k_insert", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
-                             "alg_bytes_per_launch": alg_bytes, "launch_ms": k_count_ms},
+                             "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms, "launches_per_step": parts,
+                             "next": {"kernel": "k_extract", "achieved": extract_bytes / (extract_ms / 1e3) / 1e9,
+                                      "frac": extract_bytes / (extract_ms / 1e3) / 1e9 / peak,
+                                      "alg_bytes_per_launch": extract_bytes, "launch_ms": extract_ms}},
                 "gpu_launches": launches, "clocks": clk.summary(), "phase_ms": phases,
                 "sizes": {k: sizes[k] for k in ("n_reads", "n_instances", "n_k2", "n_nodes", "n_branch",
-                                                "n_chain_nodes", "iterations", "n_chains", "table_slots")}}
+                                                "n_chain_nodes", "iterations", "n_chains", "table_slots",
+                                                "table_partitions")}}
         if not args.no_cpu_baseline:
             b = cpu_baseline(w, args.cpu_sample, os.cpu_count() or 1)
             line["cpu_baseline"] = {k: b[k] for k in ("value", "unit", "cores", "kind", "sample")}

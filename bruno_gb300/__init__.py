@@ -49,7 +49,8 @@ class _Sizes(ctypes.Structure):
         "n_reads", "n_reads_used", "n_instances", "n_k2", "n_filtered", "n_nodes", "n_branch",
         "n_chain_nodes", "iterations", "n_cycle_nodes", "n_isolated", "n_ranked", "n_chains",
         "n_chain_chars", "table_slots", "collisions")] + [("filter_flag_hist", ctypes.c_uint64 * 16),
-                                                    ("launches", ctypes.c_uint64)]
+                                                    ("launches", ctypes.c_uint64),
+                                                    ("table_partitions", ctypes.c_uint64)]
 
 
 _lib: Optional[ctypes.CDLL] = None

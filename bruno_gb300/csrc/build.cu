@@ -460,9 +460,22 @@ __device__ __forceinline__ bool table_count(uint64_t *table, const TableGeom &g,
     #pragma unroll
     for (int q = 0; q < NE; ++q) seen[q] = (uint32_t)(raw[KWD + q / 2] >> (32 * (q & 1)));
     if (key_is_empty(key)) {
-      bool was_empty;
-      key_claim(KT{}, slot, x, seen_primary, key, was_empty);
-      if (was_empty) ++slot_claims;
+      if constexpr (KWD == 1) {
+        /* claim the key and its first entry together: one 128-bit CAS of (key, entries 0-1)
+         * from (EMPTY, 0) -- the entries of an unclaimed slot are always zero */
+        const uint64_t nk = ((const uint64_t *)&x)[0] | (seen_primary ? KEY_CONT : 0);
+        const uint64_t ne0 = (uint64_t)((code << E_CODE_SHIFT) | (1u << E_COUNT_SHIFT));
+        uint64_t ohi;
+        const uint64_t olo = cas128(slot, KEY_EMPTY, 0ull, nk, ne0, ohi);
+        if (olo == KEY_EMPTY && ohi == 0) { ++slot_claims; ++entry_claims; return true; }
+        ((uint64_t *)&key)[0] = olo;          /* claimed meanwhile: count against what is there */
+        seen[0] = (uint32_t)ohi;
+        seen[1] = (uint32_t)(ohi >> 32);
+      } else {
+        bool was_empty;
+        key_claim(KT{}, slot, x, seen_primary, key, was_empty);
+        if (was_empty) ++slot_claims;
+      }
     }
     if (key_matches(key, x, seen_primary)) {
       seen_primary = true;
@@ -528,11 +541,13 @@ __global__ void __launch_bounds__(TPB, 4) k_count(CountArgs a) {
         uint64_t ia = 0, ic = 0, ra[SU], rc[SU];
         if (pa < pend) {
           kmer_at<KT>(words, pa, p0, rv.L, k, xa, ca);
+          xa = table_key(xa);
           ia = table_home(a.g, xa);
           ld_slot<SU>(a.table + ia * SU, ra);
         }
         if (pc < pend) {
           kmer_at<KT>(words, pc, p0, rv.L, k, xc, cc);
+          xc = table_key(xc);
           ic = table_home(a.g, xc);
           ld_slot<SU>(a.table + ic * SU, rc);
         }
@@ -731,8 +746,9 @@ __global__ void k_part_init(uint64_t *table, uint64_t first_slot, uint64_t nslot
     t[i] = ((int)(i % SU) < KWD) ? KEY_EMPTY : 0ull;
 }
 
-/* Phase B: the records of the buckets of partition q (blockIdx.y picks the bucket); four
- * records in flight per thread: their slot reads are all issued before any is used */
+/* Phase B: the records of the buckets of partition q (blockIdx.y picks the bucket); two
+ * records in flight per thread (their slot reads are issued before either is used) and
+ * the next two already loading */
 constexpr int INS_BATCH = 2;
 __global__ void __launch_bounds__(TPB) k_insert(const uint64_t *records, const unsigned long long *bucket_cnt,
                                                  uint64_t cap, int bucket0, uint64_t *table, TableGeom g,
@@ -746,12 +762,21 @@ __global__ void __launch_bounds__(TPB) k_insert(const uint64_t *records, const u
   unsigned long long slots = 0, entries = 0;
   bool full = false;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += INS_BATCH * stride) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  /* the next batch of records is loaded while this one is counted */
+  uint64_t nxt[INS_BATCH];
+  #pragma unroll
+  for (int q = 0; q < INS_BATCH; ++q) {
+    const uint64_t j = i + q * stride;
+    nxt[q] = j < n ? __ldcs(rb + j) : ~0ull;
+  }
+  for (; i < n; i += INS_BATCH * stride) {
     uint64_t rec[INS_BATCH], home[INS_BATCH], raw[INS_BATCH][SU];
     #pragma unroll
     for (int q = 0; q < INS_BATCH; ++q) {
-      const uint64_t j = i + q * stride;
-      rec[q] = j < n ? __ldcs(rb + j) : ~0ull;
+      rec[q] = nxt[q];
+      const uint64_t j = i + (INS_BATCH + q) * stride;
+      nxt[q] = j < n ? __ldcs(rb + j) : ~0ull;
     }
     #pragma unroll
     for (int q = 0; q < INS_BATCH; ++q) {
@@ -764,8 +789,8 @@ __global__ void __launch_bounds__(TPB) k_insert(const uint64_t *records, const u
     for (int q = 0; q < INS_BATCH; ++q) {
       if (rec[q] == ~0ull) continue;
       const uint64_t h = ((uint64_t)b << LOW_BITS) | (rec[q] >> 5);
-      if (!table_count<KW1>(table, g, max_probe, KW1{bj_inv(h)}, (unsigned)(rec[q] & 31), home[q], raw[q], slots,
-                            entries, lo))
+      if (!table_count<KW1>(table, g, max_probe, KW1{h}, (unsigned)(rec[q] & 31), home[q], raw[q], slots, entries,
+                            lo))
         full = true;
     }
   }
@@ -797,6 +822,7 @@ __global__ void __launch_bounds__(TPB) k_dump_k2(const uint64_t *table, uint64_t
     KT key = KOps<KT>::load(s);
     if (key_dead(key)) continue;
     ((uint64_t *)&key)[KWD - 1] &= ~KEY_CONT;  /* continuation slots belong to the same k-mer */
+    key = key_kmer(key);
     const uint32_t *e = (const uint32_t *)(s + KWD);
     for (int j = 0; j < NE; ++j) {
       if (e[j] == 0) continue;
@@ -836,10 +862,11 @@ struct FilterTally {
  * entry words w[0..ne) of the k-mer, all in registers when CAP is the slot capacity.
  * Writes the node (compact_multi_biedge counts, flags) over the slot, or a tombstone. */
 template <class KT, int CAP>
-__device__ __forceinline__ void filter_kmer(uint64_t *s, uint64_t slot_index, KT key, const uint32_t *w, int ne,
+__device__ __forceinline__ void filter_kmer(uint64_t *s, uint64_t slot_index, KT tkey, const uint32_t *w, int ne,
                                             const FilterArgs &a, FilterTally &t) {
   constexpr int KWD = Slot<KT>::KEYW;
   const int k = a.k;
+  const KT key = key_kmer(tkey);   /* the canonical k-mer */
   /* step 4: per-block sums (:1460-1507) */
   const bool kpal = k_palindrome(key, k);
   const bool high = km1_high_palindrome(key, k), low = km1_low_palindrome(key, k);
@@ -1036,7 +1063,7 @@ __global__ void __launch_bounds__(TPB) k_dump_nodes(const uint64_t *table, uint6
     if (key_dead(key)) continue;
     unsigned long long o = atomicAdd(n, 1ull);
     if (o >= cap) continue;
-    KOps<KT>::store(keys + o * KWD, key);
+    KOps<KT>::store(keys + o * KWD, key_kmer(key));
     const uint64_t *pw = s + KWD;
     for (int q = 0; q < 4; ++q) {
       counts[o * 9 + q] = (uint16_t)(pw[0] >> (16 * q));
@@ -1213,7 +1240,6 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
   const int sms = num_sms();
   const uint64_t nreads = c->n_reads;
   cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
-  cudaEventRecord(c->kev[0], c->stream);
   k_kmer_upper<<<sms * 4, TPB, 0, c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads,
                                                c->cfg.k, c->dctr);
   c->launches += 1;
@@ -1230,6 +1256,7 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
     cudaFuncSetAttribute(k_extract, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
     attr = true;
   }
+  cudaEventRecord(c->kev[0], c->stream);
   k_extract<<<eb, TPB, sizeof(ExtractSmem), c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p,
                                                           nreads, c->cfg.k, (uint64_t *)c->records.p, cap,
                                                           (unsigned long long *)c->bucket_cnt.p, (uint8_t *)c->blk_cnt.p,
@@ -1255,7 +1282,11 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
     cudaMemsetAsync(&c->dctr->n_slots_claimed, 0, 16, c->stream);
     cudaEventRecord(c->kev[2], c->stream);
     const int G = 1 << (NBUCKET_BITS - pt);
-    const int gx = std::max(1, (sms * 8 + G - 1) / G);
+    static int ins_occ = 0;   /* resident k_insert blocks per SM: one full wave per partition */
+    if (!ins_occ && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ins_occ, k_insert, TPB, 0) != cudaSuccess ||
+                     ins_occ < 1))
+      ins_occ = 4;
+    const int gx = std::max(1, (sms * ins_occ + G - 1) / G);
     for (int q = 0; q < (1 << pt); ++q) {
       k_part_init<KW1><<<sms * 2, TPB, 0, c->stream>>>((uint64_t *)c->table.p, (uint64_t)q * region, region);
       k_insert<<<dim3(gx, G), TPB, 0, c->stream>>>((const uint64_t *)c->records.p,

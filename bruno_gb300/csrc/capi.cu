@@ -278,6 +278,7 @@ bruno_status bruno_get_sizes(bruno_ctx *c, bruno_sizes *o) {
   o->table_slots = c->nslots;
   o->collisions = c->multi;
   o->launches = c->launches;
+  o->table_partitions = 1ull << c->geom.pbits;
   for (int f = 0; f < 16; ++f) o->filter_flag_hist[f] = c->flag_hist[f];
   return BRUNO_OK;
 }

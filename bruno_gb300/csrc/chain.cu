@@ -91,8 +91,10 @@ __device__ __forceinline__ uint32_t slot_aux(const uint64_t *s) {
 
 /* slot index of a live node with canonical key x, -1 if absent */
 template <class KT>
-__device__ __forceinline__ long long table_find(const uint64_t *table, const TableGeom &g, uint32_t max_probe, KT x) {
+__device__ __forceinline__ long long table_find(const uint64_t *table, const TableGeom &g, uint32_t max_probe,
+                                                KT kmer) {
   constexpr int SU = Slot<KT>::U64;
+  const KT x = table_key(kmer);
   Probe pr(g, table_home(g, x));
   for (uint32_t p = 0; p < max_probe; ++p, pr.next()) {
     const uint64_t *s = table + pr.i * SU;
@@ -117,7 +119,7 @@ __global__ void __launch_bounds__(TPB) k_chain_keys(const uint64_t *table, uint6
       sl = 0;
     }
     const uint64_t *s = table + sl * SU;
-    for (int w = 0; w < KWD; ++w) ckey[i * KWD + w] = s[w];
+    KOps<KT>::store(ckey + i * KWD, key_kmer(KOps<KT>::load(s)));
     cslot[i] = sl;
   }
 }
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(TPB) k_termini(const uint64_t *table, TableGeo
   constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
   for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nb; q += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t *s = table + (uint64_t)branch_list[q] * SU;
-    const KT K = KOps<KT>::load(s);
+    const KT K = key_kmer(KOps<KT>::load(s));
     const uint64_t *pw = s + KWD;
     for (int c = 0; c < 4; ++c) {
       if ((pw[0] >> (16 * c)) & 0xFFFFu) {  /* out neighbour receives (branch, IN) */

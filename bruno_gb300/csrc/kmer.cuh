@@ -196,13 +196,21 @@ struct TableGeom {
   int pbits;
 };
 
-__device__ __forceinline__ uint64_t table_home(const TableGeom &g, KW1 x) {
-  const uint64_t h = bj_fwd(x.v);
+/* The table stores a key derived from the canonical k-mer: for k <= 31 the 62-bit mix
+ * bj_fwd(k-mer) (so counting records never need inverting), for k > 31 the k-mer itself. */
+__device__ __forceinline__ KW1 table_key(KW1 x) { return {bj_fwd(x.v)}; }
+__device__ __forceinline__ KW2 table_key(KW2 x) { return x; }
+__device__ __forceinline__ KW1 key_kmer(KW1 t) { return {bj_inv(t.v)}; }
+__device__ __forceinline__ KW2 key_kmer(KW2 t) { return t; }
+
+/* home slot of a table key */
+__device__ __forceinline__ uint64_t table_home(const TableGeom &g, KW1 t) {
+  const uint64_t h = t.v;
   const uint64_t q = g.pbits ? (h >> (62 - g.pbits)) : 0;
   return q * g.region + __umul64hi(h << (2 + g.pbits), g.region);
 }
-__device__ __forceinline__ uint64_t table_home(const TableGeom &g, KW2 x) {
-  return __umul64hi(KOps<KW2>::hash(x), g.region);   /* pbits == 0 */
+__device__ __forceinline__ uint64_t table_home(const TableGeom &g, KW2 t) {
+  return __umul64hi(KOps<KW2>::hash(t), g.region);   /* pbits == 0 */
 }
 /* linear probing inside one partition */
 struct Probe {

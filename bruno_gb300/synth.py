@@ -55,6 +55,9 @@ WORKLOADS = {
     # 50 Mbp + 2% repeats (1-10 kbp, 2-8 copies, 1% divergence), 30x 150 bp, 0.5% subs, k=31, -L 3
     "plain-scale": Workload("plain-scale", 50_000_000, 150, 10_000_000, 0.005, 31, (3,), 0.02, (1000, 10000),
                             (2, 8), (0.01, 0.01)),
+    # the plain-scale mix at a fifth of the genome (profiling case: 10 Mbp, 2M x 150 bp, k=31, -L 3)
+    "plain-medium": Workload("plain-medium", 10_000_000, 150, 2_000_000, 0.005, 31, (3,), 0.02, (1000, 10000),
+                             (2, 8), (0.01, 0.01), 5),
     # 200 Mbp + 5% repeats (1-20 kbp, 2-16 copies, 1-3% divergence), 30x 150 bp, k=63, -L 3
     "large-k": Workload("large-k", 200_000_000, 150, 40_000_000, 0.005, 63, (3,), 0.05, (1000, 20000), (2, 16),
                         (0.01, 0.03)),

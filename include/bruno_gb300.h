@@ -80,6 +80,7 @@ typedef struct bruno_sizes {
   uint64_t collisions;      /* list-ranking sides that got >1 update in one round */
   uint64_t filter_flag_hist[16]; /* k_del[] histogram (debruijn_graph_map.hpp:1568) */
   uint64_t launches;        /* kernels launched by the last build */
+  uint64_t table_partitions; /* slot regions the k-mer table was filled in (1 = one region) */
 } bruno_sizes;
 
 typedef struct bruno_ctx bruno_ctx;
