@@ -62,6 +62,7 @@ EXPORTS = (
     "bruno_extract_chains", "bruno_list_rank", "bruno_to_compressed_chains", "bruno_build_and_compact",
     "bruno_get_sizes", "bruno_copy_k2", "bruno_copy_filtered", "bruno_copy_nodes", "bruno_copy_ranked",
     "bruno_copy_chains", "bruno_host_alloc", "bruno_host_free", "bruno_phase_ms",
+    "bruno_count_biedges_noalloc",
 )
 
 
@@ -87,6 +88,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "bruno_copy_chains": [P, P, P, P, SZ, SZ, PSZ, PSZ],
         "bruno_host_alloc": [SZ, ctypes.POINTER(P)], "bruno_host_free": [P],
         "bruno_phase_ms": [P, ctypes.POINTER(ctypes.c_double), SZ],
+        "bruno_count_biedges_noalloc": [I32, I32, P, P, SZ, P, P, P, SZ, PSZ, P],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -19,7 +19,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
+#include <mutex>
 
 #include "internal.cuh"
 
@@ -1413,4 +1415,138 @@ bruno_status run_copy_nodes(Ctx *c, uint64_t *keys, uint16_t *counts, uint8_t *f
   return r;
 }
 
+/* ================================================================ allocation-free counting
+ * bruno_count_biedges_noalloc counts (k-mer, biedge) pairs that the caller already holds in
+ * device memory and allocates nothing: its hash table lives in the fixed file-scope array
+ * below, whose address is looked up once per device.  Layout of the array: a 64 KiB header
+ * holding a DevCounters (the call uses err, n_slots_claimed, n_entries and n_k2_dump), then
+ * the table slots, 32 B each for k <= 31 and 64 B for k <= 63.  Each call sizes its table to
+ * max(256, 2n) slots, so the load stays at or below one half and an empty slot always exists
+ * (a pair adds at most one slot). */
+constexpr size_t NOALLOC_BYTES = BRUNO_NOALLOC_SCRATCH_BYTES;
+constexpr size_t NOALLOC_HDR = 64u << 10;
+static_assert(sizeof(DevCounters) <= NOALLOC_HDR, "scratch header too small");
+static_assert(BRUNO_NOALLOC_MAX_PAIRS_K31 == (NOALLOC_BYTES - NOALLOC_HDR) / 32 / 2, "K31 limit");
+static_assert(BRUNO_NOALLOC_MAX_PAIRS_K63 == (NOALLOC_BYTES - NOALLOC_HDR) / 64 / 2, "K63 limit");
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+namespace {
+/* DNA16 nibble -> 0 (none), 1..4 (A C G T); 5 for anything else */
+__device__ __forceinline__ unsigned dna16_to5(unsigned nib) {
+  return nib == 0 ? 0u : nib == 1 ? 1u : nib == 2 ? 2u : nib == 4 ? 3u : nib == 8 ? 4u : 5u;
+}
+
+/* the table insert of the direct counting path, fed from a pair array instead of reads */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_count_pairs(const uint64_t *kmers, const uint8_t *edges, uint64_t n, int k,
+                                                      uint64_t *table, TableGeom g, uint32_t max_probe,
+                                                      DevCounters *ctr) {
+  constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
+  /* bits above 2k in the most significant word must be clear */
+  const int top_bits = KWD == 1 ? 2 * k : 2 * k - 64;
+  const uint64_t top_mask = top_bits >= 64 ? 0ull : ~0ull << top_bits;
+  unsigned long long slots = 0, entries = 0;
+  bool bad = false, full = false;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const KT x = KOps<KT>::load(kmers + i * KWD);
+    const unsigned e = edges[i];
+    const unsigned in5 = dna16_to5(e >> 4), out5 = dna16_to5(e & 15u);
+    if (in5 > 4 || out5 > 4 || (((const uint64_t *)&x)[KWD - 1] & top_mask)) { bad = true; continue; }
+    const KT key = table_key(x);
+    const uint64_t home = table_home(g, key);
+    uint64_t raw[SU];
+    ld_slot<SU>(table + home * SU, raw);
+    if (!table_count<KT>(table, g, max_probe, key, biedge_code(in5, out5), home, raw, slots, entries)) full = true;
+  }
+  slots = warp_sum(slots); entries = warp_sum(entries);
+  if ((threadIdx.x & 31) == 0) {
+    if (slots) atomicAdd(&ctr->n_slots_claimed, slots);
+    if (entries) atomicAdd(&ctr->n_entries, entries);
+  }
+  if (bad) atomicOr(&ctr->err, (unsigned long long)DERR_BAD_INPUT);
+  if (full) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
+}
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_base[NOALLOC_MAX_DEVICES];   /* device address of the array, per device */
+
+/* once per device, with that device current: the array's device address */
+bruno_status noalloc_setup(int device, unsigned char **base) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_base[device]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return BRUNO_ERR_CUDA;
+    g_noalloc_base[device] = (unsigned char *)p;
+  }
+  *base = g_noalloc_base[device];
+  return BRUNO_OK;
+}
+
+template <class KT>
+bruno_status count_pairs_noalloc(unsigned char *base, int k, const uint64_t *kmers, const uint8_t *edges, uint64_t n,
+                                 uint64_t *out_kmers, uint8_t *out_edges, uint32_t *out_counts, size_t out_cap,
+                                 size_t *n_out, cudaStream_t stream) {
+  constexpr int SU = Slot<KT>::U64;
+  DevCounters *ctr = (DevCounters *)base;
+  uint64_t *table = (uint64_t *)(base + NOALLOC_HDR);
+  const uint64_t nslots = std::max<uint64_t>(256, 2 * n);
+  const TableGeom g{nslots, nslots, 0};
+  const int sms = num_sms();
+  /* what must start at zero: the counters; the slots used get EMPTY keys and zero entries */
+  if (cudaMemsetAsync(ctr, 0, offsetof(DevCounters, flag_hist), stream) != cudaSuccess) return BRUNO_ERR_CUDA;
+  k_table_init<KT><<<(unsigned)std::min<uint64_t>((nslots * SU + TPB - 1) / TPB, (uint64_t)sms * 8), TPB, 0, stream>>>(
+      table, nslots);
+  if (n)
+    k_count_pairs<KT><<<(unsigned)std::min<uint64_t>((n + TPB - 1) / TPB, (uint64_t)sms * 8), TPB, 0, stream>>>(
+        kmers, edges, n, k, table, g, (uint32_t)nslots, ctr);
+  const bool dump = out_kmers || out_edges || out_counts;
+  if (dump)
+    k_dump_k2<KT><<<(unsigned)std::min<uint64_t>((nslots + TPB - 1) / TPB, (uint64_t)sms * 8), TPB, 0, stream>>>(
+        table, nslots, out_kmers, out_edges, out_counts, out_cap, ctr);
+  if (cudaGetLastError() != cudaSuccess) return BRUNO_ERR_CUDA;
+  DevCounters h;
+  if (cudaMemcpyAsync(&h, ctr, offsetof(DevCounters, flag_hist), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+      cudaStreamSynchronize(stream) != cudaSuccess)
+    return BRUNO_ERR_CUDA;
+  if (h.err & DERR_BAD_INPUT) return BRUNO_ERR_BAD_INPUT;
+  if (h.err & DERR_TABLE_FULL) return BRUNO_ERR_TABLE_FULL;
+  *n_out = dump ? h.n_k2_dump : h.n_entries;
+  if (dump && h.n_k2_dump > out_cap) return BRUNO_ERR_CAPACITY;
+  return BRUNO_OK;
+}
+}  // namespace
+
+bruno_status count_biedges_noalloc(int32_t device, int32_t k, const uint64_t *kmers, const uint8_t *edges, size_t n,
+                                   uint64_t *out_kmers, uint8_t *out_edges, uint32_t *out_counts, size_t out_cap,
+                                   size_t *n_out, void *stream) {
+  if (!n_out || k < 3 || k > 63 || (n && (!kmers || !edges))) return BRUNO_ERR_ARG;
+  const bool dump = out_kmers || out_edges || out_counts;
+  if (dump && (!out_kmers || !out_edges || !out_counts)) return BRUNO_ERR_ARG;
+  *n_out = 0;
+  if (n > (k <= 31 ? (size_t)BRUNO_NOALLOC_MAX_PAIRS_K31 : (size_t)BRUNO_NOALLOC_MAX_PAIRS_K63))
+    return BRUNO_ERR_CAPACITY;
+  int ndev = 0, prev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || cudaGetDevice(&prev) != cudaSuccess) return BRUNO_ERR_CUDA;
+  if (device < 0 || device >= ndev || device >= NOALLOC_MAX_DEVICES) return BRUNO_ERR_ARG;
+  if (device != prev && cudaSetDevice(device) != cudaSuccess) return BRUNO_ERR_CUDA;
+  unsigned char *base = nullptr;
+  bruno_status st = noalloc_setup(device, &base);
+  if (st == BRUNO_OK)
+    st = k <= 31 ? count_pairs_noalloc<KW1>(base, k, kmers, edges, n, out_kmers, out_edges, out_counts, out_cap,
+                                            n_out, (cudaStream_t)stream)
+                 : count_pairs_noalloc<KW2>(base, k, kmers, edges, n, out_kmers, out_edges, out_counts, out_cap,
+                                            n_out, (cudaStream_t)stream);
+  if (device != prev) cudaSetDevice(prev);
+  return st;
+}
+
 }  // namespace bg
+
+extern "C" bruno_status bruno_count_biedges_noalloc(int32_t device, int32_t k, const uint64_t *kmers,
+                                                    const uint8_t *edges, size_t n, uint64_t *out_kmers,
+                                                    uint8_t *out_edges, uint32_t *out_counts, size_t out_cap,
+                                                    size_t *n_out, void *stream) {
+  return bg::count_biedges_noalloc(device, k, kmers, edges, n, out_kmers, out_edges, out_counts, out_cap, n_out,
+                                   stream);
+}

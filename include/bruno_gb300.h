@@ -167,6 +167,40 @@ bruno_status bruno_host_free(void *p);
  * the partitioned path), whole-table initialisation (direct path only), and the counting
  * itself (the partition-by-partition inserts, or k_count).  Writes min(n, 9) values. */
 bruno_status bruno_phase_ms(bruno_ctx *ctx, double *ms, size_t n);
+
+/* ---------------------------------------------------------------------------------------
+ * Allocation-free pair counting.  This entry point has no counterpart in the reference; it
+ * exists for callers that may not allocate device memory themselves or through this
+ * library: a host application that has already handed the whole device to its own memory
+ * pool, a plugin framework that only lends fixed buffers and forbids allocation calls, or a
+ * latency-sensitive loop that must not stop for an allocator.  Every other entry point
+ * allocates through its context, so such callers cannot use them.
+ *
+ * It counts the n (k-mer, biedge) pairs kmers[i], edges[i] -- the pairs the reference's
+ * parser emits and debruijn_graph_map::compute_biedge_freqencies (debruijn_graph_map.hpp:
+ * 1085-1141) counts: k-mers in the packing above (`words` uint64 each, bits above 2k zero),
+ * biedges as DNA16 bytes -- and writes every distinct pair once with its count to out_kmers,
+ * out_edges, out_counts (capacity out_cap pairs, in no particular order).  *n_out receives
+ * the number of distinct pairs.  All five arrays are DEVICE pointers; passing NULL for all
+ * three outputs only counts.  The working hash table lives in one fixed device array of
+ * BRUNO_NOALLOC_SCRATCH_BYTES inside the library, so n is limited to
+ * BRUNO_NOALLOC_MAX_PAIRS_K31 pairs for k <= 31 and BRUNO_NOALLOC_MAX_PAIRS_K63 for
+ * 32 <= k <= 63; a larger n returns BRUNO_ERR_CAPACITY before any work is queued.  Other
+ * errors: BRUNO_ERR_ARG (bad k, device or pointers), BRUNO_ERR_BAD_INPUT (an edge nibble that
+ * is not 0/1/2/4/8, or k-mer bits above 2k), BRUNO_ERR_CAPACITY (more distinct pairs than
+ * out_cap; *n_out still holds the count), BRUNO_ERR_CUDA.
+ *
+ * The work runs on `stream` (a cudaStream_t, NULL = the default stream) of `device`; the
+ * call waits for it before returning and leaves the caller's current device as it was.
+ * There is one scratch array per device: two calls whose GPU work can overlap on the same
+ * device (from two host threads, or on two streams without ordering between them) use the
+ * same table at the same time and corrupt each other's counts.  Serialise them. */
+#define BRUNO_NOALLOC_SCRATCH_BYTES (32u << 20)
+#define BRUNO_NOALLOC_MAX_PAIRS_K31 ((((32u << 20) - (64u << 10)) / 32u) / 2u)
+#define BRUNO_NOALLOC_MAX_PAIRS_K63 ((((32u << 20) - (64u << 10)) / 64u) / 2u)
+bruno_status bruno_count_biedges_noalloc(int32_t device, int32_t k, const uint64_t *kmers, const uint8_t *edges,
+                                         size_t n, uint64_t *out_kmers, uint8_t *out_edges, uint32_t *out_counts,
+                                         size_t out_cap, size_t *n_out, void *stream);
 #ifdef __cplusplus
 }
 #endif
