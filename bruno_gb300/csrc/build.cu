@@ -580,16 +580,13 @@ __global__ void __launch_bounds__(TPB, 4) k_count(CountArgs a) {
 /* ============================================================ partitioned counting
  * k <= 31.  Phase A (k_extract) turns every read into canonical (k-mer, biedge) instances
  * and writes each as one 8-byte record [low 54 bits of bj_fwd(k-mer) | biedge code:5]
- * into one of 256 hash buckets (the bucket is the top 8 bits of the mix); the block sorts
+ * into one of 256 hash buckets (the bucket is the top 8 bits of the mix); the block queues
  * its records by bucket in shared memory first, so every bucket grows by contiguous runs.
  * The distinct-count estimate rides along.  Phase B (k_insert) then fills the table one
  * partition at a time -- a partition is one or more buckets and a contiguous slot region
  * small enough to stay in L2 -- so the random slot traffic of counting stays on chip. */
 constexpr int NBUCKET_BITS = 8, NBUCKET = 1 << NBUCKET_BITS;
 constexpr int LOW_BITS = 62 - NBUCKET_BITS;          /* 54 */
-constexpr int REC_CAP = 2048;                         /* records per block flush */
-constexpr int EMIT = REC_CAP / (TPB / 32);            /* positions per warp per round */
-
 __global__ void __launch_bounds__(TPB) k_kmer_upper(const uint64_t *rstart, const uint64_t *rend, uint64_t nreads,
                                                      int k, DevCounters *ctr) {
   unsigned long long n = 0;
@@ -601,141 +598,178 @@ __global__ void __launch_bounds__(TPB) k_kmer_upper(const uint64_t *rstart, cons
   if ((threadIdx.x & 31) == 0 && n) atomicAdd(&ctr->n_upper, n);
 }
 
+/* Phase A runs one thread per read: each thread validates its read (any base that is not
+ * A/C/G/T, either case, drops the read), then rolls the forward k-mer and its reverse
+ * complement through the read one base at a time, so every k-mer costs a handful of
+ * integer operations.  Records go to per-bucket shared-memory queues; after every round of
+ * XROUND records per thread the block appends each queue to its bucket with one atomic. */
+constexpr int XTPB = 512;                  /* threads per block */
+constexpr int XROUND = 8;                  /* records per thread between two flushes */
+constexpr int XQ = 32;                     /* queue capacity per bucket (mean fill 16) */
+
 struct ExtractSmem {
-  uint64_t words[TPB / 32][CHUNK_WORDS];
-  uint64_t rec[REC_CAP], sorted[REC_CAP];
+  uint64_t q[NBUCKET][XQ];
   unsigned int hll[HLL_M];
-  uint32_t pcnt[NBUCKET], pcur[NBUCKET], pstart[NBUCKET];
-  unsigned long long gbase[NBUCKET];
-  uint8_t part[REC_CAP], spart[REC_CAP];
-  uint32_t n;
+  unsigned int cnt[NBUCKET];
+  unsigned long long base[NBUCKET];
   int overflow;
 };
 
-__global__ void __launch_bounds__(TPB) k_extract(const uint64_t *rstart, const uint64_t *rend, uint64_t nreads, int k,
-                                                  uint64_t *records, uint64_t cap, unsigned long long *bucket_cnt,
-                                                  uint8_t *hll_partial, DevCounters *ctr) {
+/* bytes of one read's sequence through aligned 8-byte loads; no load goes past the word
+ * that holds the last base, so nothing outside the read's own line is touched beyond its
+ * last word */
+struct SeqCursor {
+  const uint64_t *w, *wlast;
+  uint64_t cur, nxt;
+  int left;
+  __device__ __forceinline__ void init(const unsigned char *s, const unsigned char *e) {
+    const uint64_t *w0 = (const uint64_t *)((uintptr_t)s & ~(uintptr_t)7);
+    wlast = (const uint64_t *)((uintptr_t)(e - 1) & ~(uintptr_t)7);
+    const int off = (int)((uintptr_t)s & 7);
+    cur = __ldg(w0) >> (8 * off);
+    left = 8 - off;
+    w = w0 + 1;
+    nxt = w <= wlast ? __ldg(w) : 0ull;
+  }
+  __device__ __forceinline__ unsigned next() {
+    if (left == 0) {
+      cur = nxt; left = 8; ++w;
+      nxt = w <= wlast ? __ldg(w) : 0ull;
+    }
+    const unsigned b = (unsigned)cur & 0xFFu;
+    cur >>= 8; --left;
+    return b;
+  }
+};
+
+/* true if every byte of [s, e) is A, C, G or T in either case */
+__device__ __forceinline__ bool seq_valid(const unsigned char *s, const unsigned char *e) {
+  const uintptr_t a0 = (uintptr_t)s & ~(uintptr_t)7, a1 = (uintptr_t)e;
+  bool ok = true;
+  for (uintptr_t a = a0; a < a1 && ok; a += 8) {
+    const uint64_t x = __ldg((const uint64_t *)a) | 0x2020202020202020ull;
+    /* bytes of this word that belong to the read */
+    const int lo = a < (uintptr_t)s ? (int)((uintptr_t)s - a) : 0;
+    const int hi = a + 8 > a1 ? (int)(a1 - a) : 8;
+    const uint64_t in = (hi == 8 ? ~0ull : ((1ull << (8 * hi)) - 1)) & (~0ull << (8 * lo));
+    uint32_t v[2];
+    #pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const uint32_t y = (uint32_t)(x >> (32 * h));
+      v[h] = __vcmpeq4(y, 0x61616161u) | __vcmpeq4(y, 0x63636363u) | __vcmpeq4(y, 0x67676767u) |
+             __vcmpeq4(y, 0x74747474u);
+    }
+    const uint64_t good = (uint64_t)v[0] | ((uint64_t)v[1] << 32);
+    ok = (good & in) == in;
+  }
+  return ok;
+}
+
+__global__ void __launch_bounds__(XTPB, 2) k_extract(const uint64_t *rstart, const uint64_t *rend, uint64_t nreads,
+                                                      int k, uint64_t *records, uint64_t cap,
+                                                      unsigned long long *bucket_cnt, uint8_t *hll_partial,
+                                                      DevCounters *ctr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ExtractSmem &S = *reinterpret_cast<ExtractSmem *>(smem_raw);
-  for (int i = threadIdx.x; i < HLL_M; i += TPB) S.hll[i] = 0;
-  for (int i = threadIdx.x; i < NBUCKET; i += TPB) S.pcnt[i] = 0;
-  if (threadIdx.x == 0) { S.n = 0; S.overflow = 0; }
+  const int tid = threadIdx.x;
+  for (int i = tid; i < HLL_M; i += XTPB) S.hll[i] = 0;
+  for (int i = tid; i < NBUCKET; i += XTPB) S.cnt[i] = 0;
+  if (tid == 0) S.overflow = 0;
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  uint64_t *words = S.words[warp];
-  const uint64_t stride = (uint64_t)gridDim.x * (TPB / 32);
-  /* per-warp cursor over its reads */
-  uint64_t r = (uint64_t)blockIdx.x * (TPB / 32) + warp;
-  ReadView rv{nullptr, 0};
-  uint32_t npos = 0, pc = 0, p0 = 0, pend = 0;
-  bool staged = false, one_chunk = true, fresh = false, active = r < nreads;
+  const uint64_t stride = (uint64_t)gridDim.x * XTPB;
+  const uint64_t kmask = (k == 32) ? ~0ull : ((1ull << (2 * k)) - 1);
+  const int top = 2 * k - 2;
+  uint64_t r = (uint64_t)blockIdx.x * XTPB + tid;
   unsigned long long inst = 0, used = 0;
-  if (active) {
-    rv = ReadView{(const unsigned char *)rstart[r], (uint32_t)(rend[r] - rstart[r])};
-    npos = rv.L >= (uint32_t)k + 2 ? rv.L - k + 1 : 0;
-    fresh = true;
-  }
+  SeqCursor sc;
+  uint32_t L = 0, i = 0;
+  uint64_t fwd = 0, rev = 0;
+  unsigned left = 0;
+  /* advance to the next usable read of this thread */
+  auto next_read = [&]() -> bool {
+    for (; r < nreads; r += stride) {
+      const unsigned char *s = (const unsigned char *)rstart[r], *e = (const unsigned char *)rend[r];
+      const uint32_t len = (uint32_t)(e - s);
+      if (len < (uint32_t)k + 2 || !seq_valid(s, e)) continue;
+      ++used;
+      sc.init(s, e);
+      L = len; i = 0; fwd = 0; rev = 0; left = 0;
+      return true;
+    }
+    return false;
+  };
+  auto emit = [&](unsigned in5, unsigned out5) {
+    uint64_t x = fwd;
+    if (!(fwd < rev)) {   /* lex_less: flip the k-mer and reverse-complement the biedge */
+      x = rev;
+      const unsigned ni = out5 ? 5u - out5 : 0u, no = in5 ? 5u - in5 : 0u;
+      in5 = ni; out5 = no;
+    }
+    const uint64_t h = bj_fwd(x);
+    const unsigned bucket = (unsigned)(h >> LOW_BITS);
+    const uint64_t rec = ((h & ((1ull << LOW_BITS) - 1)) << 5) | biedge_code(in5, out5);
+    const unsigned idx = (unsigned)(h >> (62 - HLL_P));
+    const unsigned rho = (unsigned)__clzll((h << (2 + HLL_P)) | (1ull << (1 + HLL_P))) + 1u;
+    if (rho > S.hll[idx]) atomicMax(&S.hll[idx], rho);
+    const unsigned pos = atomicAdd(&S.cnt[bucket], 1u);
+    if (pos < (unsigned)XQ) {
+      S.q[bucket][pos] = rec;
+    } else {   /* queue full this round: append straight to the bucket */
+      const unsigned long long o = atomicAdd(&bucket_cnt[bucket], 1ull);
+      if (o < cap) records[(uint64_t)bucket * cap + o] = rec;
+      else S.overflow = 1;
+    }
+    ++inst;
+  };
+  bool active = next_read();
   for (;;) {
-    uint32_t budget = EMIT;
-    while (active && budget > 0) {
-      if (fresh) {   /* a new read: long reads get the N filter up front */
-        fresh = false; pc = 0; staged = false;
-        one_chunk = npos <= CHUNK_POS;
-        if (npos && !one_chunk) {
-          bool bad = false;
-          for (uint32_t i = lane; i < rv.L; i += 32) bad |= base_code(rv.s[i]) < 0;
-          if (__any_sync(~0u, bad)) npos = 0;
-          else used += (lane == 0);
-        }
+    int emitted = 0;
+    while (active && emitted < XROUND) {
+      const unsigned byte = sc.next();
+      const unsigned c = ((byte >> 1) ^ (byte >> 2)) & 3u;   /* A0 C1 G2 T3, either case */
+      if (i >= (uint32_t)k) {   /* the k-mer ending before base i, its out-base is base i */
+        emit(i > (uint32_t)k ? left + 1u : 0u, c + 1u);
+        ++emitted;
       }
-      if (pc >= npos) {   /* next read */
+      left = (unsigned)(fwd >> top) & 3u;
+      fwd = ((fwd << 2) | c) & kmask;
+      rev = (rev >> 2) | ((uint64_t)(3u - c) << top);
+      if (++i == L) {   /* the last k-mer has no out-base */
+        emit(left + 1u, 0u);
+        ++emitted;
         r += stride;
-        if (r >= nreads) { active = false; break; }
-        rv = ReadView{(const unsigned char *)rstart[r], (uint32_t)(rend[r] - rstart[r])};
-        npos = rv.L >= (uint32_t)k + 2 ? rv.L - k + 1 : 0;
-        fresh = true;
-        continue;
-      }
-      if (!staged || pc >= pend) {
-        p0 = (pc / CHUNK_POS) * CHUNK_POS;
-        pend = min(npos, p0 + CHUNK_POS);
-        __syncwarp();
-        const bool bad = stage_chunk(rv, p0, pend, k, words, lane);
-        staged = true;
-        if (one_chunk) {
-          if (bad) { npos = 0; continue; }   /* reads containing N are dropped */
-          used += (lane == 0);
-        }
-      }
-      const uint32_t e = min(pend, pc + budget);
-      for_each_kmer_run<KW1>(words, pc, e, p0, rv.L, k, lane, [&](bool valid, KW1 x, unsigned code) {
-        uint64_t rec = 0;
-        unsigned bucket = 0;
-        if (valid) {
-          const uint64_t h = bj_fwd(x.v);
-          bucket = (unsigned)(h >> LOW_BITS);
-          rec = ((h & ((1ull << LOW_BITS) - 1)) << 5) | code;
-          const unsigned idx = (unsigned)(h >> (62 - HLL_P));
-          const unsigned rho = (unsigned)__clzll((h << (2 + HLL_P)) | (1ull << (1 + HLL_P))) + 1u;
-          if (rho > S.hll[idx]) atomicMax(&S.hll[idx], rho);
-          ++inst;
-        }
-        const unsigned m = __ballot_sync(~0u, valid);
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&S.n, (uint32_t)__popc(m));
-        base = __shfl_sync(~0u, base, 0);
-        if (valid) {
-          const uint32_t o = base + __popc(m & ((1u << lane) - 1));
-          S.rec[o] = rec;
-          S.part[o] = (uint8_t)bucket;
-        }
-      });
-      budget -= e - pc;
-      pc = e;
-    }
-    __syncthreads();
-    /* flush: group the block's records by bucket and append each group to its bucket */
-    const uint32_t n = S.n;
-    for (uint32_t i = threadIdx.x; i < n; i += TPB) atomicAdd(&S.pcnt[S.part[i]], 1u);
-    __syncthreads();
-    {
-      const uint32_t v = S.pcnt[threadIdx.x];
-      uint32_t tot;
-      const uint32_t st = block_exscan(v, tot);
-      S.pstart[threadIdx.x] = st;
-      S.pcur[threadIdx.x] = st;
-      if (v) {
-        const unsigned long long old = atomicAdd(&bucket_cnt[threadIdx.x], (unsigned long long)v);
-        if (old + v > cap) S.overflow = 1;
-        S.gbase[threadIdx.x] = (unsigned long long)threadIdx.x * cap + old;
+        active = next_read();
       }
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < n; i += TPB) {
-      const unsigned b = S.part[i];
-      const uint32_t pos = atomicAdd(&S.pcur[b], 1u);
-      S.sorted[pos] = S.rec[i];
-      S.spart[pos] = (uint8_t)b;
+    if (tid < NBUCKET) {
+      const unsigned f = min(S.cnt[tid], (unsigned)XQ);
+      if (f) {
+        const unsigned long long old = atomicAdd(&bucket_cnt[tid], (unsigned long long)f);
+        if (old + f > cap) S.overflow = 1;
+        S.base[tid] = (unsigned long long)tid * cap + old;
+      }
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < n; i += TPB) {
-      const unsigned b = S.spart[i];
-      const unsigned long long dst = S.gbase[b] + (i - S.pstart[b]);
-      if (dst < (unsigned long long)(b + 1) * cap) records[dst] = S.sorted[i];
+    for (int x = tid; x < NBUCKET * XQ; x += XTPB) {
+      const int b = x / XQ, j = x % XQ;
+      if ((unsigned)j < min(S.cnt[b], (unsigned)XQ)) {
+        const unsigned long long dst = S.base[b] + j;
+        if (dst < (unsigned long long)(b + 1) * cap) records[dst] = S.q[b][j];
+      }
     }
     __syncthreads();
-    S.pcnt[threadIdx.x] = 0;
-    if (threadIdx.x == 0) S.n = 0;
+    if (tid < NBUCKET) S.cnt[tid] = 0;
     if (!__syncthreads_or(active)) break;
   }
   inst = warp_sum(inst); used = warp_sum(used);
-  if (lane == 0) {
+  if ((tid & 31) == 0) {
     if (inst) atomicAdd(&ctr->n_instances, inst);
     if (used) atomicAdd(&ctr->n_reads_used, used);
   }
-  if (threadIdx.x == 0 && S.overflow) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
+  if (tid == 0 && S.overflow) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
   uint8_t *dst = hll_partial + (uint64_t)blockIdx.x * HLL_M;
-  for (int i = threadIdx.x; i < HLL_M; i += TPB) dst[i] = (uint8_t)S.hll[i];
+  for (int x = tid; x < HLL_M; x += XTPB) dst[x] = (uint8_t)S.hll[x];
 }
 
 /* one table partition: keys EMPTY, entries 0 (stays in L2 for the inserts that follow) */
@@ -1251,7 +1285,7 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
   if ((st = ensure(c, c->records, (size_t)NBUCKET * cap * 8)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->bucket_cnt, NBUCKET * 8)) != BRUNO_OK) return st;
   cudaMemsetAsync(c->bucket_cnt.p, 0, NBUCKET * 8, c->stream);
-  const int eb = std::max(1, std::min<int>(sms * 2, (int)((nreads + 7) / 8)));
+  const int eb = std::max(1, std::min<int>(sms * 2, (int)((nreads + XTPB - 1) / XTPB)));
   if ((st = ensure(c, c->blk_cnt, (size_t)eb * HLL_M)) != BRUNO_OK) return st;
   static bool attr = false;
   if (!attr) {
@@ -1259,7 +1293,7 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
     attr = true;
   }
   cudaEventRecord(c->kev[0], c->stream);
-  k_extract<<<eb, TPB, sizeof(ExtractSmem), c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p,
+  k_extract<<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p,
                                                           nreads, c->cfg.k, (uint64_t *)c->records.p, cap,
                                                           (unsigned long long *)c->bucket_cnt.p, (uint8_t *)c->blk_cnt.p,
                                                           c->dctr);
