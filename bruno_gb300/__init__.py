@@ -148,7 +148,7 @@ class GraphConfig:
     keep_k2: bool = False
     keep_filtered: bool = False
     exact_ranking: bool = False
-    direct_count: bool = False
+    direct_count: int = 0          # 0 automatic, 1 whole-table counting, 2 L2 partitions (k <= 31)
 
     def to_c(self) -> _Cfg:
         c = _Cfg()

@@ -838,6 +838,196 @@ __global__ void __launch_bounds__(TPB) k_insert(const uint64_t *records, const u
   if (full) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
 }
 
+/* ------------------------------------------- shared-memory counting of small partitions
+ * When the table is cut into 2^pbits partitions (pbits >= 8) of at most PART_SLOTS slots, a
+ * partition fits in one CTA's shared memory.  k_split first splits every bucket into its
+ * 2^(pbits-8) partitions (bucket b = partitions [b << s, (b+1) << s), picked by the next s
+ * bits of the mix); k_count_local then gives each partition to one CTA, which counts the
+ * partition's records into shared memory with shared-memory atomics and writes the finished
+ * slot region to the table once, in coalesced 16-byte stores. */
+constexpr int PART_SLOTS = 3072;           /* 96 KB of slots */
+constexpr int PTPB = 256;
+constexpr int MAX_SPLIT_BITS = 10;
+constexpr int SPLIT_QWORDS = 8192;         /* queue words of k_split (64 KB) */
+
+struct SplitSmem {
+  uint64_t q[SPLIT_QWORDS];
+  unsigned int cnt[1 << MAX_SPLIT_BITS];
+  unsigned long long base[1 << MAX_SPLIT_BITS];
+  int overflow;
+};
+
+/* bucket blockIdx.y -> its 2^sbits partitions; every block takes one contiguous share.
+ * Queue capacity qc = min(32, SPLIT_QWORDS >> sbits); a round reads `per_round` records per
+ * thread so that a queue is about half full when the block flushes. */
+__global__ void __launch_bounds__(XTPB) k_split(const uint64_t *records, const unsigned long long *bucket_cnt,
+                                                 uint64_t cap, int sbits, uint64_t *out, uint64_t cap2,
+                                                 unsigned long long *sub_cnt, DevCounters *ctr) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SplitSmem &S = *reinterpret_cast<SplitSmem *>(smem_raw);
+  const int tid = threadIdx.x, nq = 1 << sbits, b = blockIdx.y;
+  const int qc = min(32, SPLIT_QWORDS >> sbits);
+  const int per_round = max(1, (qc / 2) * nq / XTPB);
+  for (int i = tid; i < nq; i += XTPB) S.cnt[i] = 0;
+  if (tid == 0) S.overflow = 0;
+  __syncthreads();
+  const uint64_t n = min((unsigned long long)cap, bucket_cnt[b]);
+  const uint64_t per = (n + gridDim.x - 1) / gridDim.x;
+  const uint64_t lo = min(n, (uint64_t)blockIdx.x * per), hi = min(n, lo + per);
+  const uint64_t *rb = records + (uint64_t)b * cap;
+  const int shift = 5 + LOW_BITS - sbits;
+  for (uint64_t r0 = lo; r0 < hi; r0 += (uint64_t)XTPB * per_round) {
+    for (int j = 0; j < per_round; ++j) {
+      const uint64_t i = r0 + (uint64_t)j * XTPB + tid;
+      if (i < hi) {
+        const uint64_t rec = __ldcs(rb + i);
+        const unsigned sq = (unsigned)(rec >> shift) & (unsigned)(nq - 1);
+        const unsigned pos = atomicAdd(&S.cnt[sq], 1u);
+        if (pos < (unsigned)qc) {
+          S.q[sq * qc + pos] = rec;
+        } else {
+          const uint64_t part = ((uint64_t)b << sbits) | sq;
+          const unsigned long long o = atomicAdd(&sub_cnt[part], 1ull);
+          if (o < cap2) out[part * cap2 + o] = rec;
+          else S.overflow = 1;
+        }
+      }
+    }
+    __syncthreads();
+    for (int q = tid; q < nq; q += XTPB) {
+      const unsigned f = min(S.cnt[q], (unsigned)qc);
+      if (f) {
+        const uint64_t part = ((uint64_t)b << sbits) | (unsigned)q;
+        const unsigned long long old = atomicAdd(&sub_cnt[part], (unsigned long long)f);
+        if (old + f > cap2) S.overflow = 1;
+        S.base[q] = part * cap2 + old;
+      }
+    }
+    __syncthreads();
+    for (int x = tid; x < nq * qc; x += XTPB) {
+      const int q = x / qc, j = x - q * qc;
+      if ((unsigned)j < min(S.cnt[q], (unsigned)qc)) {
+        const uint64_t part = ((uint64_t)b << sbits) | (unsigned)q;
+        const unsigned long long dst = S.base[q] + j;
+        if (dst < (part + 1) * cap2) out[dst] = S.q[x];
+      }
+    }
+    __syncthreads();
+    for (int q = tid; q < nq; q += XTPB) S.cnt[q] = 0;
+    __syncthreads();
+  }
+  if (tid == 0 && S.overflow) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
+}
+
+__device__ __forceinline__ void sm_ld_slot(uint32_t a, uint64_t *raw) {
+  asm volatile("ld.volatile.shared.v2.u64 {%0, %1}, [%2];" : "=l"(raw[0]), "=l"(raw[1]) : "r"(a) : "memory");
+  asm volatile("ld.volatile.shared.v2.u64 {%0, %1}, [%2];" : "=l"(raw[2]), "=l"(raw[3]) : "r"(a + 16) : "memory");
+}
+__device__ __forceinline__ uint64_t sm_cas128(uint32_t a, uint64_t cmp_lo, uint64_t cmp_hi, uint64_t new_lo,
+                                              uint64_t new_hi, uint64_t &old_hi) {
+  uint64_t olo, ohi;
+  asm volatile(
+      "{\n\t.reg .b128 d, b, c;\n\t"
+      "mov.b128 b, {%2, %3};\n\t"
+      "mov.b128 c, {%4, %5};\n\t"
+      "atom.shared.cas.b128 d, [%6], b, c;\n\t"
+      "mov.b128 {%0, %1}, d;\n\t}"
+      : "=l"(olo), "=l"(ohi)
+      : "l"(cmp_lo), "l"(cmp_hi), "l"(new_lo), "l"(new_hi), "r"(a)
+      : "memory");
+  old_hi = ohi;
+  return olo;
+}
+
+/* count_in_entries on a slot in shared memory */
+__device__ __forceinline__ bool sm_count_entries(uint32_t *e, const uint32_t *seen, unsigned code,
+                                                 unsigned long long &claims) {
+  #pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    uint32_t w = seen[i];
+    if (w == 0) {
+      const uint32_t nw = (code << E_CODE_SHIFT) | (1u << E_COUNT_SHIFT);
+      const uint32_t old = atomicCAS(e + i, 0u, nw);
+      if (old == 0) { ++claims; return true; }
+      w = old;
+    }
+    if (entry_code(w) == code) {
+      const uint32_t old = atomicAdd(e + i, 1u << E_COUNT_SHIFT);
+      if (old >> 31) atomicOr(e + i, E_BIG);
+      return true;
+    }
+  }
+  return false;
+}
+
+/* one record into the partition held in shared memory; false if the region is full */
+__device__ __forceinline__ bool sm_count(uint64_t *sm, uint32_t sm_base, uint32_t region, uint64_t h, unsigned code,
+                                         uint32_t home, unsigned long long &slot_claims,
+                                         unsigned long long &entry_claims) {
+  bool seen_primary = false;
+  uint32_t j = home;
+  for (uint32_t probe = 0; probe < region; ++probe) {
+    uint64_t raw[4];
+    sm_ld_slot(sm_base + j * 32u, raw);
+    uint64_t key = raw[0];
+    uint32_t seen[6];
+    #pragma unroll
+    for (int q = 0; q < 6; ++q) seen[q] = (uint32_t)(raw[1 + q / 2] >> (32 * (q & 1)));
+    const uint64_t want = h | (seen_primary ? KEY_CONT : 0);
+    if (key == KEY_EMPTY) {
+      const uint64_t ne0 = (uint64_t)((code << E_CODE_SHIFT) | (1u << E_COUNT_SHIFT));
+      uint64_t ohi;
+      const uint64_t olo = sm_cas128(sm_base + j * 32u, KEY_EMPTY, 0ull, want, ne0, ohi);
+      if (olo == KEY_EMPTY && ohi == 0) { ++slot_claims; ++entry_claims; return true; }
+      key = olo;
+      seen[0] = (uint32_t)ohi;
+      seen[1] = (uint32_t)(ohi >> 32);
+    }
+    if (key == want) {
+      seen_primary = true;
+      if (sm_count_entries((uint32_t *)(sm + (uint64_t)j * 4 + 1), seen, code, entry_claims)) return true;
+    }
+    j = (j + 1 == region) ? 0u : j + 1;
+  }
+  return false;
+}
+
+/* one CTA per partition: clear the slots, count the partition's records, write back */
+__global__ void __launch_bounds__(PTPB) k_count_local(const uint64_t *recs, const unsigned long long *rec_cnt,
+                                                       uint64_t rcap, int sbits, uint64_t *table, TableGeom g,
+                                                       DevCounters *ctr) {
+  extern __shared__ __align__(16) uint64_t sm[];
+  const uint64_t part = blockIdx.x;
+  const uint32_t region = (uint32_t)g.region;
+  const int tid = threadIdx.x;
+  for (uint32_t w = tid; w < region * 4u; w += PTPB) sm[w] = (w & 3u) == 0 ? KEY_EMPTY : 0ull;
+  __syncthreads();
+  const uint32_t sm_base = (uint32_t)__cvta_generic_to_shared(sm);
+  const uint64_t n = min((unsigned long long)rcap, rec_cnt[part]);
+  const uint64_t *rp = recs + part * rcap;
+  const uint64_t bucket_hi = (part >> sbits) << LOW_BITS;   /* bucket bits of the mix */
+  unsigned long long slots = 0, entries = 0;
+  bool full = false;
+  uint64_t nxt = tid < n ? __ldcs(rp + tid) : 0ull;
+  for (uint64_t i = tid; i < n; i += PTPB) {
+    const uint64_t rec = nxt;
+    nxt = i + PTPB < n ? __ldcs(rp + i + PTPB) : 0ull;
+    const uint64_t h = bucket_hi | (rec >> 5);
+    const uint32_t home = (uint32_t)__umul64hi(h << (2 + g.pbits), g.region);
+    if (!sm_count(sm, sm_base, region, h, (unsigned)(rec & 31), home, slots, entries)) full = true;
+  }
+  __syncthreads();
+  ulonglong2 *dst = reinterpret_cast<ulonglong2 *>(table + part * g.region * 4);
+  const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(sm);
+  for (uint32_t v = tid; v < region * 2u; v += PTPB) dst[v] = src[v];
+  slots = warp_sum(slots); entries = warp_sum(entries);
+  if ((tid & 31) == 0) {
+    if (slots) atomicAdd(&ctr->n_slots_claimed, slots);
+    if (entries) atomicAdd(&ctr->n_entries, entries);
+  }
+  if (full) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
+}
+
 /* table initialisation: every key word EMPTY, every entry 0; written as one flat word
  * array so that every warp store is 256 contiguous bytes */
 template <class KT>
@@ -1305,37 +1495,89 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
   c->n_instances = c->hctr->n_instances;
   c->n_reads_used = c->hctr->n_reads_used;
   uint64_t slots = c->cfg.table_slots ? c->cfg.table_slots : slots_for(c, hll_estimate(c->hctr->hll));
-  /* partitions of at most ~48 MB so that one stays in L2 while it fills */
+  static bool part_attr = false;
+  if (!part_attr) {
+    cudaFuncSetAttribute(k_count_local, cudaFuncAttributeMaxDynamicSharedMemorySize, PART_SLOTS * 32);
+    cudaFuncSetAttribute(k_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SplitSmem));
+    part_attr = true;
+  }
   for (int attempt = 0; attempt < 4; ++attempt) {
-    const double bytes = (double)slots * 32.0;
-    int pt = 0;
-    while (pt < NBUCKET_BITS && bytes / (double)(1ull << pt) > 48.0 * 1024 * 1024) ++pt;
-    const uint64_t region = std::max<uint64_t>(64, (slots + (1ull << pt) - 1) >> pt);
-    c->geom = TableGeom{region << pt, region, pt};
-    c->nslots = c->geom.nslots;
-    if ((st = ensure(c, c->table, c->nslots * 32)) != BRUNO_OK) return st;
+    /* shared-memory path: 2^pb partitions (pb >= 8) small enough for one CTA's shared memory */
+    int pb = NBUCKET_BITS;
+    while (pb < NBUCKET_BITS + MAX_SPLIT_BITS && (slots + (1ull << pb) - 1) >> pb > (uint64_t)PART_SLOTS) ++pb;
+    const uint64_t region_c = std::max<uint64_t>(64, (slots + (1ull << pb) - 1) >> pb);
+    bool counted = false;
     cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
     cudaMemsetAsync(&c->dctr->n_slots_claimed, 0, 16, c->stream);
-    cudaEventRecord(c->kev[2], c->stream);
-    const int G = 1 << (NBUCKET_BITS - pt);
-    static int ins_occ = 0;   /* resident k_insert blocks per SM: one full wave per partition */
-    if (!ins_occ && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ins_occ, k_insert, TPB, 0) != cudaSuccess ||
-                     ins_occ < 1))
-      ins_occ = 4;
-    const int gx = std::max(1, (sms * ins_occ + G - 1) / G);
-    for (int q = 0; q < (1 << pt); ++q) {
-      k_part_init<KW1><<<sms * 2, TPB, 0, c->stream>>>((uint64_t *)c->table.p, (uint64_t)q * region, region);
-      k_insert<<<dim3(gx, G), TPB, 0, c->stream>>>((const uint64_t *)c->records.p,
-                                                    (const unsigned long long *)c->bucket_cnt.p, cap, q * G,
-                                                    (uint64_t *)c->table.p, c->geom, 4096u, c->dctr);
+    if (region_c <= (uint64_t)PART_SLOTS && c->force_direct_count != 2) {
+      c->geom = TableGeom{region_c << pb, region_c, pb};
+      c->nslots = c->geom.nslots;
+      if ((st = ensure(c, c->table, c->nslots * 32)) != BRUNO_OK) return st;
+      const int sbits = pb - NBUCKET_BITS;
+      const uint64_t nparts = 1ull << pb;
+      const uint64_t *recs = (const uint64_t *)c->records.p;
+      const unsigned long long *cnts = (const unsigned long long *)c->bucket_cnt.p;
+      uint64_t rcap = cap;
+      cudaEventRecord(c->kev[2], c->stream);
+      bool split_ok = true;
+      if (sbits > 0) {
+        const uint64_t cap2 = (cap >> sbits) + (cap >> sbits) / 8 + 1024;
+        if ((st = ensure(c, c->records2, (size_t)(nparts * cap2 * 8))) != BRUNO_OK) return st;
+        if ((st = ensure(c, c->sub_cnt, (size_t)(nparts * 8))) != BRUNO_OK) return st;
+        cudaMemsetAsync(c->sub_cnt.p, 0, nparts * 8, c->stream);
+        const int gx = std::max(1, (sms * 16 + NBUCKET - 1) / NBUCKET);
+        k_split<<<dim3(gx, NBUCKET), XTPB, sizeof(SplitSmem), c->stream>>>((const uint64_t *)c->records.p,
+                                                          (const unsigned long long *)c->bucket_cnt.p, cap, sbits,
+                                                          (uint64_t *)c->records2.p, cap2,
+                                                          (unsigned long long *)c->sub_cnt.p, c->dctr);
+        c->launches += 1;
+        if ((st = sync_counters(c)) != BRUNO_OK) return st;
+        split_ok = !(c->hctr->err & DERR_TABLE_FULL);   /* a skewed bucket: use the L2 path below */
+        recs = (const uint64_t *)c->records2.p;
+        cnts = (const unsigned long long *)c->sub_cnt.p;
+        rcap = cap2;
+      }
+      if (split_ok) {
+        k_count_local<<<(unsigned)nparts, PTPB, (unsigned)(region_c * 32), c->stream>>>(
+            recs, cnts, rcap, sbits, (uint64_t *)c->table.p, c->geom, c->dctr);
+        c->launches += 1;
+        cudaEventRecord(c->kev[3], c->stream);
+        if ((st = cuda_check(c, cudaGetLastError(), "k_count_local")) != BRUNO_OK) return st;
+        counted = true;
+      } else {
+        cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
+      }
     }
-    c->launches += 2 << pt;
-    cudaEventRecord(c->kev[3], c->stream);
+    if (!counted) {
+      /* L2 path: partitions of at most ~48 MB (a whole number of buckets) filled one at a time */
+      const double bytes = (double)slots * 32.0;
+      int pt = 0;
+      while (pt < NBUCKET_BITS && bytes / (double)(1ull << pt) > 48.0 * 1024 * 1024) ++pt;
+      const uint64_t region = std::max<uint64_t>(64, (slots + (1ull << pt) - 1) >> pt);
+      c->geom = TableGeom{region << pt, region, pt};
+      c->nslots = c->geom.nslots;
+      if ((st = ensure(c, c->table, c->nslots * 32)) != BRUNO_OK) return st;
+      cudaEventRecord(c->kev[2], c->stream);
+      const int G = 1 << (NBUCKET_BITS - pt);
+      static int ins_occ = 0;   /* resident k_insert blocks per SM: one full wave per partition */
+      if (!ins_occ && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ins_occ, k_insert, TPB, 0) != cudaSuccess ||
+                       ins_occ < 1))
+        ins_occ = 4;
+      const int gx = std::max(1, (sms * ins_occ + G - 1) / G);
+      for (int q = 0; q < (1 << pt); ++q) {
+        k_part_init<KW1><<<sms * 2, TPB, 0, c->stream>>>((uint64_t *)c->table.p, (uint64_t)q * region, region);
+        k_insert<<<dim3(gx, G), TPB, 0, c->stream>>>((const uint64_t *)c->records.p,
+                                                      (const unsigned long long *)c->bucket_cnt.p, cap, q * G,
+                                                      (uint64_t *)c->table.p, c->geom, 4096u, c->dctr);
+      }
+      c->launches += 2 << pt;
+      cudaEventRecord(c->kev[3], c->stream);
+    }
     if ((st = sync_counters(c)) != BRUNO_OK) return st;
     if (!(c->hctr->err & DERR_TABLE_FULL)) {
       float ms[3] = {0, 0, 0};
       cudaEventElapsedTime(&ms[0], c->kev[0], c->kev[1]);   /* phase A (extract + estimate) */
-      cudaEventElapsedTime(&ms[2], c->kev[2], c->kev[3]);   /* phase B (init + insert) */
+      cudaEventElapsedTime(&ms[2], c->kev[2], c->kev[3]);   /* phase B (split + count, or init + insert) */
       c->phase_ms[6] = ms[0];
       c->phase_ms[7] = 0;
       c->phase_ms[8] = ms[2];
@@ -1344,14 +1586,14 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
       used = true;
       return BRUNO_OK;
     }
-    slots *= 2;
+    slots = std::max<uint64_t>(slots, c->nslots) * 2;   /* grow from the size actually used */
   }
   return set_err(c, BRUNO_ERR_TABLE_FULL, "k-mer table full after regrowth");
 }
 
 template <class KT>
 bruno_status count_typed(Ctx *c) {
-  if (sizeof(KT) == 8 && !c->force_direct_count) {
+  if (sizeof(KT) == 8 && c->force_direct_count != 1) {
     bool used = false;
     bruno_status st = count_partitioned(c, used);
     if (st != BRUNO_OK || used) return st;

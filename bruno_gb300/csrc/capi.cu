@@ -83,7 +83,7 @@ bruno_status bruno_ctx_create(const bruno_cfg *cfg, bruno_ctx **out) {
   c->cfg = *cfg;
   c->W = cfg->k <= 31 ? 1 : 2;
   c->exact_ranking = cfg->exact_ranking != 0;
-  c->force_direct_count = cfg->direct_count != 0;
+  c->force_direct_count = cfg->direct_count;
   bruno_status st = cuda_check(c, cudaSetDevice(cfg->device), "cudaSetDevice");
   if (st == BRUNO_OK) st = cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
   c->own_stream = true;
@@ -106,7 +106,8 @@ bruno_status bruno_ctx_destroy(bruno_ctx *c) {
   Buf *bufs[] = {&c->rstart, &c->rend, &c->tile_cnt, &c->tile_base, &c->table, &c->k2_keys, &c->k2_edges, &c->k2_counts,
                  &c->f_keys, &c->f_edges, &c->f_counts, &c->blk_cnt, &c->blk_base, &c->ckey, &c->cslot, &c->cedge,
                  &c->cstate, &c->pend, &c->pay, &c->unf0, &c->unf1, &c->removed, &c->r_K, &c->r_rep, &c->r_dist,
-                 &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list};
+                 &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list,
+                 &c->records, &c->bucket_cnt, &c->records2, &c->sub_cnt};
   for (Buf *b : bufs) release(*b);
   for (Buf &b : c->seg_bufs) release(b);
   if (c->dctr) cudaFree(c->dctr);

@@ -74,7 +74,8 @@ struct Ctx {
   TableGeom geom{0, 0, 0};
   uint64_t nslots = 0, n_entries = 0, n_slots_claimed = 0;
   Buf records, bucket_cnt;       /* partitioned counting: 8-byte records per hash bucket */
-  int force_direct_count = 0;    /* tests: count straight into the table */
+  Buf records2, sub_cnt;         /* the same records split per table partition */
+  int force_direct_count = 0;    /* cfg.direct_count: 0 automatic, 1 whole table, 2 L2 partitions */
   Buf chain_list, branch_list;   /* slot indices, filled by the filter */
 
   /* dumps */

@@ -57,8 +57,11 @@ typedef struct bruno_cfg {
   int32_t keep_filtered;    /* 1: record the filtered (k+2)-mer entries for copy-out */
   int32_t exact_ranking;    /* 1: always run the round-synchronous ranking; 0: use the O(M)
                                ruling-set ranking whenever the chain map is consistent */
-  int32_t direct_count;     /* 1: count every instance straight into the whole table; 0: for
-                               k <= 31 count through hash-partitioned records (L2-resident) */
+  int32_t direct_count;     /* counting path for k <= 31: 0 = automatic (hash-partitioned records
+                               counted partition by partition in a cluster's shared memory, or
+                               through L2 when a partition is too large for that), 1 = every
+                               instance straight into the whole table, 2 = the L2 partitions
+                               always.  k > 31 always counts straight into the table. */
 } bruno_cfg;
 
 typedef struct bruno_sizes {

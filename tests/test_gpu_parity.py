@@ -52,7 +52,8 @@ def compare(gpu, ref):
     assert chain_set(*gpu["chains"]) == chain_set(*ref["chains"]), "compacted chains"
 
 
-PATHS = {"fast": {}, "round_sync": {"exact_ranking": True}, "direct_count": {"direct_count": True}}
+PATHS = {"fast": {}, "round_sync": {"exact_ranking": True}, "direct_count": {"direct_count": 1},
+         "l2_partitions": {"direct_count": 2}}
 
 
 @pytest.mark.parametrize("path", sorted(PATHS))
@@ -86,7 +87,7 @@ def test_repeat_rich_workload_parity():
     w = synth.Workload("rep", 2_000_000, 150, 400_000, 0.005, 31, (3,), 0.02, (1000, 10000), (2, 8), (0.01, 0.01), 3)
     fq = synth.make_fastq(w)
     thr = bg.thresholds(w.lower)
-    for mu, kw in ((True, {}), (False, {}), (True, {"exact_ranking": True}), (True, {"direct_count": True})):
+    for mu, kw in ((True, {}), (False, {}), (True, {"exact_ranking": True}), (True, {"direct_count": 1}), (True, {"direct_count": 2})):
         ref = oracle.run(fq, k=31, thresh=thr, min_update=mu, threads=16, keep_k2=True, keep_filtered=True)
         compare(gpu_run(fq, 31, True, thr, mu, **kw), ref)
 
