@@ -9,8 +9,8 @@ emission -- over the 50 Mbp / 30x / 150 bp / k=31 / -L 3 synthetic workload.
           stream, which is torch's current stream).
   e2e     the same through the C ABI with pinned host buffers: the FASTQ host->device copy
           and the device->host read of the compacted chains are inside the timed region.
-  roofline  the dominant kernel (k_insert, per table partition) against the measured HBM
-          copy bandwidth, with k_extract beside it.
+  roofline  the dominant kernel (by time) against the measured HBM copy bandwidth, with the
+          other large kernels beside it.
   cpu_baseline  the CPU oracle (a restatement of the reference's CPU path) on a bounded
           sample of the same workload, with every host thread.
 
@@ -247,26 +247,31 @@ def main():
     e2e_value = inst_step * args.steps * world / (ems / 1e3)
     d2h = nch + 8 * (nc + 1) + 8 * g.words * nc
 
-    # roofline of the dominant kernel, k_insert (phase B of k <= 31 counting; one launch per
-    # table partition, each preceded by the partition's init).  Algorithmic bytes per launch:
-    # the partition's 8-byte records read once + its slot region (32 B a slot) written back
-    # once.  Phase A (k_extract) is reported beside it: the FASTQ bytes and 16 B of read
-    # span per read read once, 8 B per record written once.
-    parts = max(1, sizes["table_partitions"])
-    insert_ms = statistics.mean(p["count_insert"] for p in kms)
-    launch_ms = insert_ms / parts
-    alg_bytes = (8 * inst_step + 32 * sizes["table_slots"]) / parts
+    # Roofline of the dominant kernel.  Each candidate's algorithmic bytes per launch (one
+    # launch per step each) and its CUDA-event time on the library's stream:
+    #   k_extract      FASTQ bytes + 16 B read span per read read once, 8 B per record written
+    #   k_split        8 B per record read and written once
+    #   k_count_local  8 B per record read once + 32 B per table slot written once
+    #   k_filter       32 B per table slot read once + 32 B per graph node written once
+    mean = lambda key: statistics.mean(p[key] for p in kms)
     peak, peak_src = measured_peak()
-    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
-    extract_ms = statistics.mean(p["count_estimate"] for p in kms)
-    extract_bytes = n + 16 * sizes["n_reads"] + 8 * inst_step
+    slots = sizes["table_slots"]
+    kern = {
+        "k_extract": (n + 16 * sizes["n_reads"] + 8 * inst_step, mean("count_estimate")),
+        "k_split": (16 * inst_step, mean("count_split")),
+        "k_count_local": (8 * inst_step + 32 * slots, mean("count_insert") - mean("count_split")),
+        "k_filter": (32 * slots + 32 * sizes["n_nodes"], mean("filter_insert")),
+    }
+    kernels = {k: {"alg_bytes_per_launch": b, "launch_ms": t, "achieved": b / (t / 1e3) / 1e9 if t > 0 else None,
+                   "frac": b / (t / 1e3) / 1e9 / peak if t > 0 else None} for k, (b, t) in kern.items()}
+    top = max(kernels, key=lambda k: kernels[k]["launch_ms"])
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "k_insert_traffic.json")
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             tj = json.load(f)
-        if tj.get("bytes_per_record"):
-            traffic = tj["bytes_per_record"] * inst_step / parts
+        if top in tj and tj[top].get("bytes_per_record"):
+            traffic = tj[top]["bytes_per_record"] * inst_step
     phases = {k: round(statistics.mean(p[k] for p in kms), 3) for k in kms[0]}
 
     if rank == 0:
@@ -276,12 +281,10 @@ def main():
                 "config": workload_config(w),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n, "d2h_bytes_per_step": d2h,
                         "ms_per_step": ems / args.steps},
-                "roofline": {"bound": "hbm", "kernel": "k_insert", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
-                             "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms, "launches_per_step": parts,
-                             "next": {"kernel": "k_extract", "achieved": extract_bytes / (extract_ms / 1e3) / 1e9,
-                                      "frac": extract_bytes / (extract_ms / 1e3) / 1e9 / peak,
-                                      "alg_bytes_per_launch": extract_bytes, "launch_ms": extract_ms}},
+                "roofline": {"bound": "hbm", "kernel": top, "achieved": kernels[top]["achieved"], "peak": peak,
+                             "unit": "GB/s", "frac": kernels[top]["frac"], "peak_source": peak_src,
+                             "traffic": traffic, "alg_bytes_per_launch": kernels[top]["alg_bytes_per_launch"],
+                             "launch_ms": kernels[top]["launch_ms"], "kernels": kernels},
                 "gpu_launches": launches, "clocks": clk.summary(), "phase_ms": phases,
                 "sizes": {k: sizes[k] for k in ("n_reads", "n_instances", "n_k2", "n_nodes", "n_branch",
                                                 "n_chain_nodes", "iterations", "n_chains", "table_slots",

@@ -283,11 +283,11 @@ class Graph:
         return d
 
     PHASES = ("parse", "count_k2mers", "filter_insert", "chainmap", "list_rank", "compress",
-              "count_estimate", "count_table_init", "count_insert")
+              "count_estimate", "count_table_init", "count_insert", "count_split")
 
     def phase_ms(self) -> dict:
-        a = (ctypes.c_double * 9)()
-        self._check(self.lib.bruno_phase_ms(self.ctx, a, 9), "phase_ms")
+        a = (ctypes.c_double * len(self.PHASES))()
+        self._check(self.lib.bruno_phase_ms(self.ctx, a, len(self.PHASES)), "phase_ms")
         return dict(zip(self.PHASES, list(a)))
 
     def _ptr(self, a: np.ndarray):

@@ -1506,7 +1506,7 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
     int pb = NBUCKET_BITS;
     while (pb < NBUCKET_BITS + MAX_SPLIT_BITS && (slots + (1ull << pb) - 1) >> pb > (uint64_t)PART_SLOTS) ++pb;
     const uint64_t region_c = std::max<uint64_t>(64, (slots + (1ull << pb) - 1) >> pb);
-    bool counted = false;
+    bool counted = false, counted_local = false;
     cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
     cudaMemsetAsync(&c->dctr->n_slots_claimed, 0, 16, c->stream);
     if (region_c <= (uint64_t)PART_SLOTS && c->force_direct_count != 2) {
@@ -1520,6 +1520,7 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
       uint64_t rcap = cap;
       cudaEventRecord(c->kev[2], c->stream);
       bool split_ok = true;
+      cudaEventRecord(c->kev[4], c->stream);
       if (sbits > 0) {
         const uint64_t cap2 = (cap >> sbits) + (cap >> sbits) / 8 + 1024;
         if ((st = ensure(c, c->records2, (size_t)(nparts * cap2 * 8))) != BRUNO_OK) return st;
@@ -1531,6 +1532,7 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
                                                           (uint64_t *)c->records2.p, cap2,
                                                           (unsigned long long *)c->sub_cnt.p, c->dctr);
         c->launches += 1;
+        cudaEventRecord(c->kev[4], c->stream);
         if ((st = sync_counters(c)) != BRUNO_OK) return st;
         split_ok = !(c->hctr->err & DERR_TABLE_FULL);   /* a skewed bucket: use the L2 path below */
         recs = (const uint64_t *)c->records2.p;
@@ -1543,7 +1545,7 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
         c->launches += 1;
         cudaEventRecord(c->kev[3], c->stream);
         if ((st = cuda_check(c, cudaGetLastError(), "k_count_local")) != BRUNO_OK) return st;
-        counted = true;
+        counted = counted_local = true;
       } else {
         cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
       }
@@ -1581,6 +1583,12 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
       c->phase_ms[6] = ms[0];
       c->phase_ms[7] = 0;
       c->phase_ms[8] = ms[2];
+      c->phase_ms[9] = 0;
+      if (counted_local) {   /* the split alone; phase B minus the split is k_count_local */
+        float sp = 0;
+        cudaEventElapsedTime(&sp, c->kev[2], c->kev[4]);
+        c->phase_ms[9] = sp;
+      }
       c->n_entries = c->hctr->n_entries;
       c->n_slots_claimed = c->hctr->n_slots_claimed;
       used = true;

@@ -93,7 +93,7 @@ bruno_status bruno_ctx_create(const bruno_cfg *cfg, bruno_ctx **out) {
   if (st == BRUNO_OK) st = cuda_check(c, cudaMalloc(&c->dctr, sizeof(DevCounters)), "counters");
   if (st == BRUNO_OK) st = cuda_check(c, cudaMallocHost(&c->hctr, sizeof(DevCounters)), "pinned counters");
   for (int i = 0; i < 8 && st == BRUNO_OK; ++i) st = cuda_check(c, cudaEventCreate(&c->ev[i]), "event");
-  for (int i = 0; i < 4 && st == BRUNO_OK; ++i) st = cuda_check(c, cudaEventCreate(&c->kev[i]), "event");
+  for (int i = 0; i < 5 && st == BRUNO_OK; ++i) st = cuda_check(c, cudaEventCreate(&c->kev[i]), "event");
   if (st != BRUNO_OK) { bruno_ctx_destroy(c); return st; }
   cudaMemsetAsync(c->dctr, 0, sizeof(DevCounters), c->stream);
   *out = c;
@@ -113,7 +113,7 @@ bruno_status bruno_ctx_destroy(bruno_ctx *c) {
   if (c->dctr) cudaFree(c->dctr);
   if (c->hctr) cudaFreeHost(c->hctr);
   for (int i = 0; i < 8; ++i) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
-  for (int i = 0; i < 4; ++i) if (c->kev[i]) cudaEventDestroy(c->kev[i]);
+  for (int i = 0; i < 5; ++i) if (c->kev[i]) cudaEventDestroy(c->kev[i]);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return BRUNO_OK;
@@ -363,7 +363,7 @@ bruno_status bruno_host_free(void *p) {
 
 bruno_status bruno_phase_ms(bruno_ctx *c, double *ms, size_t n) {
   if (!c || !ms) return BRUNO_ERR_ARG;
-  for (size_t i = 0; i < n && i < 9; ++i) ms[i] = c->phase_ms[i];
+  for (size_t i = 0; i < n && i < 10; ++i) ms[i] = c->phase_ms[i];
   return BRUNO_OK;
 }
 }  // extern "C"

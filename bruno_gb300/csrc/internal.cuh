@@ -101,8 +101,8 @@ struct Ctx {
   bool chains_clean = true;
 
   cudaEvent_t ev[8] = {nullptr};
-  cudaEvent_t kev[4] = {nullptr};  /* around k_hll, k_table_init, k_count */
-  double phase_ms[9] = {0};        /* 6 phases, then k_hll, k_table_init, k_count */
+  cudaEvent_t kev[5] = {nullptr};  /* counting sub-steps */
+  double phase_ms[10] = {0};       /* 6 phases, then estimate/extract, table init, count, split */
   uint64_t launches = 0;           /* kernels launched since the last reset */
 };
 

@@ -166,9 +166,10 @@ bruno_status bruno_host_free(void *p);
 
 /* Device times of the last build, milliseconds, from CUDA events on the context's stream:
  * ms[0..5] = phases parse, count_k2mers, filter_insert, chainmap, list_rank, compress;
- * ms[6..8] = counting sub-steps: distinct-count estimate (with the record extraction on
- * the partitioned path), whole-table initialisation (direct path only), and the counting
- * itself (the partition-by-partition inserts, or k_count).  Writes min(n, 9) values. */
+ * ms[6..9] = counting sub-steps: distinct-count estimate (with the record extraction on
+ * the partitioned path), whole-table initialisation (direct path only), the counting
+ * itself (split + per-partition counts, the L2 partition inserts, or k_count), and the
+ * record split alone (shared-memory partition path only).  Writes min(n, 10) values. */
 bruno_status bruno_phase_ms(bruno_ctx *ctx, double *ms, size_t n);
 
 /* ---------------------------------------------------------------------------------------
