@@ -42,6 +42,10 @@ def parse_args():
     ap.add_argument("--workload", default="plain-scale")
     ap.add_argument("--cpu-sample", type=float, default=0.2, help="fraction of reads in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--api", default="build", choices=["build", "steps"],
+                    help="build: bruno_build_and_compact (one call); steps: the reference's call sequence "
+                         "(load, compute_biedge_freqencies, local_insert_by_freqencies, extract_chains, "
+                         "list_rank_min_update, to_compressed_chains)")
     return ap.parse_args()
 
 
@@ -188,7 +192,16 @@ def main():
     g.set_stream(stream.cuda_stream)
 
     def step_device():
-        g.build_and_compact(dev.data_ptr(), nbytes=n, is_device=True)
+        if args.api == "build":
+            g.build_and_compact(dev.data_ptr(), nbytes=n, is_device=True)
+        else:
+            g.reset()
+            g.load_fastq(dev.data_ptr(), nbytes=n, is_device=True)
+            g.compute_biedge_freqencies()
+            g.local_insert_by_freqencies()
+            g.extract_chains()
+            g.list_rank_min_update()
+            g.to_compressed_chains()
 
     def barrier():
         torch.cuda.synchronize()
@@ -278,7 +291,8 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded generator, " + w.name + ")",
-                "config": workload_config(w),
+                "config": dict(workload_config(w), api="bruno_build_and_compact" if args.api == "build"
+                               else "step calls"),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n, "d2h_bytes_per_step": d2h,
                         "ms_per_step": ems / args.steps},
                 "roofline": {"bound": "hbm", "kernel": top, "achieved": kernels[top]["achieved"], "peak": peak,

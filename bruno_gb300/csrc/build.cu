@@ -838,6 +838,220 @@ __global__ void __launch_bounds__(TPB) k_insert(const uint64_t *records, const u
   if (full) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
 }
 
+struct FilterArgs {
+  uint32_t *chain_list, *branch_list;   /* slot indices of chain / branch nodes */
+  uint64_t list_cap;
+  uint64_t *table;
+  uint64_t nslots;
+  TableGeom g;
+  int k;
+  uint64_t t[6];
+  int thresholding;
+  uint32_t max_probe;
+  uint64_t *f_keys; uint8_t *f_edges; uint32_t *f_counts; uint64_t f_cap;
+  DevCounters *ctr;
+};
+
+/* per-thread k_del[] histogram in registers: 16-bit bins, four to a word (every update is
+ * an unrolled select, so nothing is indexed at run time); `n` counts the updates so the
+ * owner can drain the bins before one could wrap */
+struct FlagHist {
+  uint64_t p[4];
+  uint32_t n;
+  __device__ __forceinline__ void clear() {
+    #pragma unroll
+    for (int i = 0; i < 4; ++i) p[i] = 0;
+    n = 0;
+  }
+  __device__ __forceinline__ void add(unsigned f) {
+    const uint64_t inc = 1ull << (16 * (f & 3u));
+    #pragma unroll
+    for (int i = 0; i < 4; ++i) p[i] += ((f >> 2) == (unsigned)i) ? inc : 0ull;
+    ++n;
+  }
+  __device__ __forceinline__ unsigned long long get(int f) const { return (p[f >> 2] >> (16 * (f & 3))) & 0xFFFFull; }
+  static constexpr uint32_t DRAIN = 60000;   /* drain at or above this many updates */
+};
+
+struct FilterTally {
+  unsigned long long nodes = 0, branch = 0, chain = 0;
+  FlagHist hist;
+  int kind = 0;          /* the last k-mer: 0 not a node, 1 chain node, 2 branch node */
+};
+
+/* v[c] for a run-time c in 0..3, as selects */
+__device__ __forceinline__ uint32_t pick4(const uint32_t *v, unsigned c) {
+  return c == 0 ? v[0] : c == 1 ? v[1] : c == 2 ? v[2] : v[3];
+}
+
+/* local_insert_by_freqencies (debruijn_graph_map.hpp:1258-1623) for one k-mer block: the
+ * entry words w[0..ne) of the k-mer, all in registers when CAP is the slot capacity.
+ * Writes the node (compact_multi_biedge counts, flags) over the slot, or a tombstone. */
+/* Quick drop: a (k+1)-mer count is at most the k-mer's total, so when the total is below
+ * the (k+1)-mer lower bound every entry gets flags 2 and 1 (debruijn_graph_map.hpp:
+ * 1423-1448) and none is kept.  Tallies the flags exactly as the full pass would, writes
+ * the tombstone and returns true; false when the k-mer needs the full pass. */
+template <class KT, int CAP>
+__device__ __forceinline__ bool filter_quick(uint64_t *s, const uint32_t *w, int ne, const FilterArgs &a,
+                                             FilterTally &t) {
+  constexpr int KWD = Slot<KT>::KEYW;
+  if (!a.thresholding) return false;
+  const uint32_t cmax32 = 0xFFFFu;
+  uint32_t kf = 0;
+  #pragma unroll
+  for (int q = 0; q < CAP; ++q) {
+    if (q >= ne) break;
+    kf += entry_count(w[q]);
+  }
+  kf = min(cmax32, kf);
+  if (kf >= a.t[2]) return false;
+  const unsigned fk = 3u | ((kf < a.t[0] || kf >= a.t[1]) ? 8u : 0u);
+  #pragma unroll
+  for (int q = 0; q < CAP; ++q) {
+    if (q >= ne) break;
+    const uint32_t c16 = min(cmax32, entry_count(w[q]));
+    t.hist.add(fk | ((c16 < a.t[4] || c16 >= a.t[5]) ? 4u : 0u));
+  }
+  if (KWD == 1) s[0] = KEY_TOMB; else { s[0] = KEY_TOMB; s[1] = KEY_TOMB; }
+  return true;
+}
+
+template <class KT, int CAP, bool QUICK = true>
+__device__ __forceinline__ void filter_kmer(uint64_t *s, uint64_t slot_index, KT tkey, const uint32_t *w, int ne,
+                                            const FilterArgs &a, FilterTally &t) {
+  constexpr int KWD = Slot<KT>::KEYW;
+  const int k = a.k;
+  if (QUICK && filter_quick<KT, CAP>(s, w, ne, a, t)) return;
+  const KT key = key_kmer(tkey);   /* the canonical k-mer */
+  /* step 4: per-block sums (:1460-1507) */
+  const bool kpal = k_palindrome(key, k);
+  const bool high = km1_high_palindrome(key, k), low = km1_low_palindrome(key, k);
+  const unsigned first = KOps<KT>::first(key, k), last = KOps<KT>::last(key);
+  const bool oddk = (k & 1) != 0;
+  /* sums fit 32 bits: at most 25 entries of at most 2^26 each */
+  uint32_t k_f = 0, k1in[4] = {0, 0, 0, 0}, k1out[4] = {0, 0, 0, 0};
+  #pragma unroll
+  for (int q = 0; q < CAP; ++q) {
+    if (q >= ne) break;
+    const uint32_t c = entry_count(w[q]);
+    const unsigned code = entry_code(w[q]);
+    const unsigned in5 = code_in5(code), out5 = code_out5(code);
+    k_f += c;
+    if (in5) {
+      const unsigned ch = in5 - 1;
+      const bool split = oddk && last == 3u - ch && high && !kpal;
+      const uint32_t v = split ? ((c + 1) >> 1) : c;
+      #pragma unroll
+      for (int cc = 0; cc < 4; ++cc) k1in[cc] += (ch == (unsigned)cc) ? v : 0u;
+    }
+    if (out5) {
+      const unsigned ch = out5 - 1;
+      const bool split = oddk && first == 3u - ch && low && !kpal;
+      const uint32_t v = split ? ((c + 1) >> 1) : c;
+      #pragma unroll
+      for (int cc = 0; cc < 4; ++cc) k1out[cc] += (ch == (unsigned)cc) ? v : 0u;
+    }
+  }
+  /* caps at FreqType max (:1401-1407) */
+  const uint32_t cmax32 = 0xFFFFu;
+  k_f = min(cmax32, k_f);
+  #pragma unroll
+  for (int c = 0; c < 4; ++c) { k1in[c] = min(cmax32, k1in[c]); k1out[c] = min(cmax32, k1out[c]); }
+  /* step 5: flags (:1410-1448), step 6: trim (:1563-1594), step 7: node update (:256-285);
+   * node sums fit 32 bits (at most 25 entries of at most 65535) */
+  uint32_t nc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  bool any = false;
+  #pragma unroll
+  for (int q = 0; q < CAP; ++q) {
+    if (q >= ne) break;
+    const uint32_t cnt = entry_count(w[q]);
+    const uint32_t cnt16 = min(cmax32, cnt);
+    const unsigned code = entry_code(w[q]);
+    unsigned in5 = code_in5(code), out5 = code_out5(code);
+    unsigned f = 0;
+    if (a.thresholding) {
+      if (cnt16 < a.t[4] || cnt16 >= a.t[5]) f |= 4;
+      if (k_f < a.t[0] || k_f >= a.t[1]) f |= 8;
+      uint64_t k1 = in5 ? (uint64_t)pick4(k1in, in5 - 1) : a.t[3];
+      if (k1 < a.t[2] || k1 >= a.t[3]) f |= 2;
+      k1 = out5 ? (uint64_t)pick4(k1out, out5 - 1) : a.t[3];
+      if (k1 < a.t[2] || k1 >= a.t[3]) f |= 1;
+    }
+    t.hist.add(f);
+    if (f >= 3) continue;
+    if (f == 1) out5 = 0;
+    if (f == 2) in5 = 0;
+    any = true;
+    #pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      nc[c] += (out5 == (unsigned)c + 1) ? cnt16 : 0u;
+      nc[4 + c] += (in5 == (unsigned)c + 1) ? cnt16 : 0u;
+    }
+    nc[8] += cnt16;
+    if (a.f_keys) {
+      unsigned long long o = atomicAdd(&a.ctr->n_filtered, 1ull);
+      if (o < a.f_cap) {
+        KOps<KT>::store(a.f_keys + o * KWD, key);
+        a.f_edges[o] = code_biedge(biedge_code(in5, out5));
+        a.f_counts[o] = cnt;
+      }
+    }
+  }
+  if (!any) {  /* no kept entry: the k-mer never enters the graph */
+    if (KWD == 1) s[0] = KEY_TOMB; else { s[0] = KEY_TOMB; s[1] = KEY_TOMB; }
+    return;
+  }
+  uint16_t c16[9];
+  #pragma unroll
+  for (int q = 0; q < 9; ++q) c16[q] = (uint16_t)min(cmax32, nc[q]);
+  /* IsBranchPoint / IsChainNode (debruijn_graph_filters.hpp:57-220) */
+  unsigned din = 0, dout = 0;
+  bool k1pal = false;
+  #pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    dout += c16[c] > 0;
+    din += c16[4 + c] > 0;
+    if (oddk && c16[c] > 0 && low && (first == 3u - c || first == (unsigned)c)) k1pal = true;
+    if (oddk && c16[4 + c] > 0 && high && (last == 3u - c || last == (unsigned)c)) k1pal = true;
+  }
+  const bool is_branch = din >= 2 || dout >= 2 || kpal || k1pal;
+  const uint32_t flags = is_branch ? NF_BRANCH : NF_CHAIN;
+  ++t.nodes; t.branch += is_branch; t.chain += !is_branch;
+  /* chain nodes get their chain index (slot aux) when the block flushes its node list */
+  t.kind = is_branch ? 2 : 1;
+  uint64_t *pw = s + KWD;
+  pw[0] = (uint64_t)c16[0] | ((uint64_t)c16[1] << 16) | ((uint64_t)c16[2] << 32) | ((uint64_t)c16[3] << 48);
+  pw[1] = (uint64_t)c16[4] | ((uint64_t)c16[5] << 16) | ((uint64_t)c16[6] << 32) | ((uint64_t)c16[7] << 48);
+  pw[2] = (uint64_t)c16[8] | ((uint64_t)flags << 16) | (0xFFFFFFFFull << 32);
+}
+
+/* A k-mer with more biedges than one slot holds: gather the entries of its continuation
+ * slots (further along its probe run, tombstoned as they are folded in) and filter them
+ * together.  Rare, so kept out of line to leave the common path its registers. */
+template <class KT>
+__device__ __noinline__ void filter_wide_global(uint64_t *s, uint64_t i, KT key, const uint32_t *w,
+                                                const FilterArgs &a, FilterTally &t) {
+  constexpr int SU = Slot<KT>::U64, NE = Slot<KT>::ENTRIES, KWD = Slot<KT>::KEYW;
+  uint32_t all[25];
+  int ne = NE;
+  for (int q = 0; q < NE; ++q) all[q] = w[q];
+  Probe pr(a.g, i);
+  for (uint32_t probe = 1; probe < a.max_probe; ++probe) {
+    pr.next();
+    uint64_t *s2 = a.table + pr.i * SU;
+    const KT k2 = KOps<KT>::load(s2);
+    if (key_is_empty(k2)) break;
+    if (!key_matches(k2, key, true)) continue;
+    const uint32_t *e2 = (const uint32_t *)(s2 + KWD);
+    for (int q = 0; q < NE && ne < 25; ++q) {
+      if (e2[q] == 0) break;
+      all[ne++] = e2[q];
+    }
+    if (KWD == 1) s2[0] = KEY_TOMB; else { s2[0] = KEY_TOMB; s2[1] = KEY_TOMB; }
+  }
+  filter_kmer<KT, 25>(s, i, key, all, ne, a, t);
+}
+
 /* ------------------------------------------- shared-memory counting of small partitions
  * When the table is cut into 2^pbits partitions (pbits >= 8) of at most PART_SLOTS slots, a
  * partition fits in one CTA's shared memory.  k_split first splits every bucket into its
@@ -1064,217 +1278,115 @@ __global__ void __launch_bounds__(TPB) k_dump_k2(const uint64_t *table, uint64_t
 
 /* ============================================================ filter + insert */
 
-struct FilterArgs {
-  uint32_t *chain_list, *branch_list;   /* slot indices of chain / branch nodes */
-  uint64_t list_cap;
-  uint64_t *table;
-  uint64_t nslots;
-  TableGeom g;
-  int k;
-  uint64_t t[6];
-  int thresholding;
-  uint32_t max_probe;
-  uint64_t *f_keys; uint8_t *f_edges; uint32_t *f_counts; uint64_t f_cap;
-  DevCounters *ctr;
-};
-
-struct FilterTally {
-  unsigned long long nodes = 0, branch = 0, chain = 0;
-  unsigned hist[16];
-  int kind = 0;          /* the last k-mer: 0 not a node, 1 chain node, 2 branch node */
-};
-
-/* local_insert_by_freqencies (debruijn_graph_map.hpp:1258-1623) for one k-mer block: the
- * entry words w[0..ne) of the k-mer, all in registers when CAP is the slot capacity.
- * Writes the node (compact_multi_biedge counts, flags) over the slot, or a tombstone. */
-template <class KT, int CAP>
-__device__ __forceinline__ void filter_kmer(uint64_t *s, uint64_t slot_index, KT tkey, const uint32_t *w, int ne,
-                                            const FilterArgs &a, FilterTally &t) {
-  constexpr int KWD = Slot<KT>::KEYW;
-  const int k = a.k;
-  const KT key = key_kmer(tkey);   /* the canonical k-mer */
-  /* step 4: per-block sums (:1460-1507) */
-  const bool kpal = k_palindrome(key, k);
-  const bool high = km1_high_palindrome(key, k), low = km1_low_palindrome(key, k);
-  const unsigned first = KOps<KT>::first(key, k), last = KOps<KT>::last(key);
-  const bool oddk = (k & 1) != 0;
-  uint64_t k_f = 0, k1in[4] = {0, 0, 0, 0}, k1out[4] = {0, 0, 0, 0};
-  #pragma unroll
-  for (int q = 0; q < CAP; ++q) {
-    if (q >= ne) break;
-    const uint64_t c = entry_count(w[q]);
-    const unsigned code = entry_code(w[q]);
-    const unsigned in5 = code_in5(code), out5 = code_out5(code);
-    k_f += c;
-    if (in5) {
-      const unsigned ch = in5 - 1;
-      const bool split = oddk && last == 3u - ch && high && !kpal;
-      k1in[ch] += split ? ((c + 1) >> 1) : c;
-    }
-    if (out5) {
-      const unsigned ch = out5 - 1;
-      const bool split = oddk && first == 3u - ch && low && !kpal;
-      k1out[ch] += split ? ((c + 1) >> 1) : c;
-    }
-  }
-  /* caps at FreqType max (:1401-1407) */
-  const uint64_t cmax = 0xFFFF;
-  k_f = min(cmax, k_f);
-  #pragma unroll
-  for (int c = 0; c < 4; ++c) { k1in[c] = min(cmax, k1in[c]); k1out[c] = min(cmax, k1out[c]); }
-  /* step 5: flags (:1410-1448), step 6: trim (:1563-1594), step 7: node update (:256-285) */
-  uint64_t nc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  bool any = false;
-  #pragma unroll
-  for (int q = 0; q < CAP; ++q) {
-    if (q >= ne) break;
-    const uint32_t cnt = entry_count(w[q]);
-    const uint64_t cnt16 = min(cmax, (uint64_t)cnt);
-    const unsigned code = entry_code(w[q]);
-    unsigned in5 = code_in5(code), out5 = code_out5(code);
-    unsigned f = 0;
-    if (a.thresholding) {
-      if (cnt16 < a.t[4] || cnt16 >= a.t[5]) f |= 4;
-      if (k_f < a.t[0] || k_f >= a.t[1]) f |= 8;
-      uint64_t k1 = in5 ? k1in[in5 - 1] : a.t[3];
-      if (k1 < a.t[2] || k1 >= a.t[3]) f |= 2;
-      k1 = out5 ? k1out[out5 - 1] : a.t[3];
-      if (k1 < a.t[2] || k1 >= a.t[3]) f |= 1;
-    }
-    ++t.hist[f];
-    if (f >= 3) continue;
-    if (f == 1) out5 = 0;
-    if (f == 2) in5 = 0;
-    any = true;
-    #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      nc[c] += (out5 == (unsigned)c + 1) ? cnt16 : 0;
-      nc[4 + c] += (in5 == (unsigned)c + 1) ? cnt16 : 0;
-    }
-    nc[8] += cnt16;
-    if (a.f_keys) {
-      unsigned long long o = atomicAdd(&a.ctr->n_filtered, 1ull);
-      if (o < a.f_cap) {
-        KOps<KT>::store(a.f_keys + o * KWD, key);
-        a.f_edges[o] = code_biedge(biedge_code(in5, out5));
-        a.f_counts[o] = cnt;
-      }
-    }
-  }
-  if (!any) {  /* no kept entry: the k-mer never enters the graph */
-    if (KWD == 1) s[0] = KEY_TOMB; else { s[0] = KEY_TOMB; s[1] = KEY_TOMB; }
-    return;
-  }
-  uint16_t c16[9];
-  #pragma unroll
-  for (int q = 0; q < 9; ++q) c16[q] = (uint16_t)min(cmax, nc[q]);
-  /* IsBranchPoint / IsChainNode (debruijn_graph_filters.hpp:57-220) */
-  unsigned din = 0, dout = 0;
-  bool k1pal = false;
-  #pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    dout += c16[c] > 0;
-    din += c16[4 + c] > 0;
-    if (oddk && c16[c] > 0 && low && (first == 3u - c || first == (unsigned)c)) k1pal = true;
-    if (oddk && c16[4 + c] > 0 && high && (last == 3u - c || last == (unsigned)c)) k1pal = true;
-  }
-  const bool is_branch = din >= 2 || dout >= 2 || kpal || k1pal;
-  const uint32_t flags = is_branch ? NF_BRANCH : NF_CHAIN;
-  ++t.nodes; t.branch += is_branch; t.chain += !is_branch;
-  /* chain nodes get their chain index (slot aux) when the block flushes its node list */
-  t.kind = is_branch ? 2 : 1;
-  uint64_t *pw = s + KWD;
-  pw[0] = (uint64_t)c16[0] | ((uint64_t)c16[1] << 16) | ((uint64_t)c16[2] << 32) | ((uint64_t)c16[3] << 48);
-  pw[1] = (uint64_t)c16[4] | ((uint64_t)c16[5] << 16) | ((uint64_t)c16[6] << 32) | ((uint64_t)c16[7] << 48);
-  pw[2] = (uint64_t)c16[8] | ((uint64_t)flags << 16) | (0xFFFFFFFFull << 32);
-}
-
+/* The filter over the whole table, for counts that did not filter as they went.  A block
+ * takes chunks of FCHUNK slots: pass 1 quick-drops what it can and lists the k-mers that need
+ * the full filter, pass 2 runs those with every lane busy and lists the nodes, and each chunk
+ * appends its chain / branch node lists with one reservation each. */
+constexpr int FCHUNK = TPB * 8;
 template <class KT>
 __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
   constexpr int SU = Slot<KT>::U64, NE = Slot<KT>::ENTRIES, KWD = Slot<KT>::KEYW;
   __shared__ unsigned long long s_hist[16], s_nodes;
-  /* block-local node lists, flushed to the global chain / branch lists once per stripe */
-  __shared__ uint32_t s_chain[TPB], s_branch[TPB];
-  __shared__ uint32_t s_nc, s_nb;
+  __shared__ uint16_t s_cand[FCHUNK];
+  __shared__ uint32_t s_chain[FCHUNK], s_branch[FCHUNK];
+  __shared__ uint32_t s_nc, s_nb, s_ncand;
   __shared__ unsigned long long s_base_c, s_base_b;
-  if (threadIdx.x < 16) s_hist[threadIdx.x] = 0;
-  if (threadIdx.x == 0) s_nodes = 0;
+  const int tid = threadIdx.x, lane = tid & 31;
+  if (tid < 16) s_hist[tid] = 0;
+  if (tid == 0) s_nodes = 0;
   FilterTally t;
-  #pragma unroll
-  for (int f = 0; f < 16; ++f) t.hist[f] = 0;
-  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < a.nslots; base += (uint64_t)gridDim.x * blockDim.x) {
-    if (threadIdx.x == 0) { s_nc = 0; s_nb = 0; }
+  t.hist.clear();
+  for (uint64_t c0 = (uint64_t)blockIdx.x * FCHUNK; c0 < a.nslots; c0 += (uint64_t)gridDim.x * FCHUNK) {
+    if (tid == 0) { s_nc = 0; s_nb = 0; s_ncand = 0; }
     __syncthreads();
-    const uint64_t i = base + threadIdx.x;
-    t.kind = 0;
-    if (i < a.nslots) {
+    if (t.hist.n >= FlagHist::DRAIN) {   /* drain the 16-bit bins long before they could wrap */
+      #pragma unroll
+      for (int f = 0; f < 16; ++f)
+        if (t.hist.get(f)) atomicAdd(&s_hist[f], t.hist.get(f));
+      t.hist.clear();
+    }
+    /* pass 1 */
+    #pragma unroll 2
+    for (int r = 0; r < FCHUNK / TPB; ++r) {
+      const uint32_t off = (uint32_t)(r * TPB + tid);
+      const uint64_t i = c0 + off;
+      bool full_pass = false;
+      if (i < a.nslots) {
+        uint64_t *s = a.table + i * SU;
+        uint64_t raw[SU];
+        ld_slot<SU>(s, raw);
+        const KT key = KOps<KT>::load(raw);
+        if (!key_dead(key) && !key_cont(key)) {
+          uint32_t w[NE];
+          int ne = 0;
+          #pragma unroll
+          for (int q = 0; q < NE; ++q) {
+            w[q] = (uint32_t)(raw[KWD + q / 2] >> (32 * (q & 1)));
+            ne += w[q] != 0;
+          }
+          full_pass = ne == NE || !filter_quick<KT, NE>(s, w, ne, a, t);
+        }
+      }
+      const unsigned m = __ballot_sync(~0u, full_pass);
+      if (m) {
+        const int leader = __ffs(m) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(&s_ncand, (unsigned)__popc(m));
+        base = __shfl_sync(~0u, base, leader);
+        if (full_pass) s_cand[base + __popc(m & ((1u << lane) - 1))] = (uint16_t)off;
+      }
+    }
+    __syncthreads();
+    /* pass 2 */
+    const unsigned ncand = s_ncand;
+    for (unsigned x = tid; x < ncand; x += TPB) {
+      const uint64_t i = c0 + s_cand[x];
       uint64_t *s = a.table + i * SU;
       uint64_t raw[SU];
       ld_slot<SU>(s, raw);
       const KT key = KOps<KT>::load(raw);
-      if (!key_dead(key) && !key_cont(key)) {
-        uint32_t w[NE];
-        int ne = 0;
-        #pragma unroll
-        for (int q = 0; q < NE; ++q) {
-          w[q] = (uint32_t)(raw[KWD + q / 2] >> (32 * (q & 1)));
-          ne += w[q] != 0;
-        }
-        if (ne < NE) {   /* the common case: every entry of the k-mer is in this slot */
-          filter_kmer<KT, NE>(s, i, key, w, ne, a, t);
-        } else {         /* more entries in continuation slots further along the probe run */
-          uint32_t all[25];
-          #pragma unroll
-          for (int q = 0; q < NE; ++q) all[q] = w[q];
-          Probe pr(a.g, i);
-          for (uint32_t probe = 1; probe < a.max_probe; ++probe) {
-            pr.next();
-            uint64_t *s2 = a.table + pr.i * SU;
-            const KT k2 = KOps<KT>::load(s2);
-            if (key_is_empty(k2)) break;
-            if (!key_matches(k2, key, true)) continue;
-            const uint32_t *e2 = (const uint32_t *)(s2 + KWD);
-            for (int q = 0; q < NE && ne < 25; ++q) {
-              if (e2[q] == 0) break;
-              all[ne++] = e2[q];
-            }
-            /* the continuation slot is folded into this node */
-            if (KWD == 1) s2[0] = KEY_TOMB; else { s2[0] = KEY_TOMB; s2[1] = KEY_TOMB; }
-          }
-          filter_kmer<KT, 25>(s, i, key, all, ne, a, t);
-        }
+      uint32_t w[NE];
+      int ne = 0;
+      #pragma unroll
+      for (int q = 0; q < NE; ++q) {
+        w[q] = (uint32_t)(raw[KWD + q / 2] >> (32 * (q & 1)));
+        ne += w[q] != 0;
       }
+      t.kind = 0;
+      if (ne < NE) filter_kmer<KT, NE, false>(s, i, key, w, ne, a, t);
+      else filter_wide_global<KT>(s, i, key, w, a, t);   /* continuation slots */
+      if (t.kind == 1) s_chain[atomicAdd(&s_nc, 1u)] = (uint32_t)i;
+      if (t.kind == 2) s_branch[atomicAdd(&s_nb, 1u)] = (uint32_t)i;
     }
-    if (t.kind == 1) s_chain[atomicAdd(&s_nc, 1u)] = (uint32_t)i;
-    if (t.kind == 2) s_branch[atomicAdd(&s_nb, 1u)] = (uint32_t)i;
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
       s_base_c = s_nc ? atomicAdd(&a.ctr->n_chain, (unsigned long long)s_nc) : 0;
       s_base_b = s_nb ? atomicAdd(&a.ctr->n_branch, (unsigned long long)s_nb) : 0;
     }
     __syncthreads();
-    if (threadIdx.x < s_nc) {
-      const unsigned long long o = s_base_c + threadIdx.x;
-      const uint32_t sl = s_chain[threadIdx.x];
+    for (unsigned x = tid; x < s_nc; x += TPB) {
+      const unsigned long long o = s_base_c + x;
+      const uint32_t sl = s_chain[x];
       if (o < a.list_cap) {
         a.chain_list[o] = sl;
         uint64_t *pw = a.table + (uint64_t)sl * SU + KWD;
         pw[2] = (pw[2] & 0xFFFFFFFFull) | (o << 32);   /* chain index */
       }
     }
-    if (threadIdx.x < s_nb && s_base_b + threadIdx.x < a.list_cap) a.branch_list[s_base_b + threadIdx.x] = s_branch[threadIdx.x];
-    __syncthreads();   /* every thread has read s_nc / s_nb before the next stripe resets them */
+    for (unsigned x = tid; x < s_nb; x += TPB)
+      if (s_base_b + x < a.list_cap) a.branch_list[s_base_b + x] = s_branch[x];
+    __syncthreads();   /* every thread has read s_nc / s_nb before the next chunk resets them */
   }
   unsigned long long nodes = warp_sum(t.nodes);
-  if ((threadIdx.x & 31) == 0) atomicAdd(&s_nodes, nodes);
+  if (lane == 0) atomicAdd(&s_nodes, nodes);
   #pragma unroll
   for (int f = 0; f < 16; ++f) {
-    unsigned long long h = warp_sum(t.hist[f]);
-    if ((threadIdx.x & 31) == 0 && h) atomicAdd(&s_hist[f], h);
+    unsigned long long h = warp_sum(t.hist.get(f));
+    if (lane == 0 && h) atomicAdd(&s_hist[f], h);
   }
   __syncthreads();
-  if (threadIdx.x < 16 && s_hist[threadIdx.x]) atomicAdd(&a.ctr->flag_hist[threadIdx.x], s_hist[threadIdx.x]);
-  if (threadIdx.x == 0) atomicAdd(&a.ctr->n_nodes, s_nodes);
+  if (tid < 16 && s_hist[tid]) atomicAdd(&a.ctr->flag_hist[tid], s_hist[tid]);
+  if (tid == 0) atomicAdd(&a.ctr->n_nodes, s_nodes);
 }
 
 /* live graph nodes -> arrays */

@@ -67,6 +67,45 @@ def test_fixture_parity(fname, opt, path):
     compare(gpu_run(data, 31, thr_on, thr, mu, **PATHS[path]), ref)
 
 
+def one_call_run(data, k, thr_on, thresh, mu, **kw):
+    """the whole path in one bruno_build_and_compact call, no raw-count copy-outs"""
+    g = bg.Graph(k=k, thresholding=thr_on, thresh=thresh, min_update=mu, **kw)
+    g.build_and_compact(data)
+    out = dict(sizes=g.sizes(), nodes=g.nodes(), ranked=g.ranked(), chains=g.chains())
+    g.close()
+    return out
+
+
+def compare_one_call(gpu, ref):
+    s = gpu["sizes"]
+    for n in ("n_reads", "n_reads_used", "n_instances", "n_k2", "n_nodes", "n_branch", "n_chain_nodes",
+              "iterations", "n_cycle_nodes", "n_isolated", "n_ranked", "n_chains"):
+        assert s[n] == ref[n], (n, s[n], ref[n])
+    assert s["filter_flag_hist"] == ref["filter_flag_hist"]
+    assert_same(sort_nodes(*gpu["nodes"]), ref["nodes"], "graph nodes")
+    assert_same(sort_ranked(*gpu["ranked"]), ref["ranked"], "listranked chain nodes")
+    assert chain_set(*gpu["chains"]) == chain_set(*ref["chains"]), "compacted chains"
+
+
+@pytest.mark.parametrize("opt", sorted(OPTIONS))
+@pytest.mark.parametrize("fname", FASTQS)
+def test_fixture_parity_one_call(fname, opt):
+    thr_on, lo, mu = OPTIONS[opt]
+    thr = bg.thresholds(lo)
+    data = fixture_bytes(fname)
+    ref = oracle.run(data, k=31, thresholding=thr_on, thresh=thr, min_update=mu, keep_k2=True)
+    compare_one_call(one_call_run(data, 31, thr_on, thr, mu), ref)
+
+
+def test_repeat_rich_workload_parity_one_call():
+    w = synth.Workload("rep", 2_000_000, 150, 400_000, 0.005, 31, (3,), 0.02, (1000, 10000), (2, 8), (0.01, 0.01), 3)
+    fq = synth.make_fastq(w)
+    thr = bg.thresholds(w.lower)
+    for mu in (True, False):
+        ref = oracle.run(fq, k=31, thresh=thr, min_update=mu, threads=16, keep_k2=True)
+        compare_one_call(one_call_run(fq, 31, True, thr, mu), ref)
+
+
 def test_known_answer_on_gpu():
     g = bg.Graph(k=31, thresholding=False).run(fixture_bytes("test.unitiqs.fastq"))
     expect = sorted(l for l in fixture_bytes("test.unitiqs.fasta").decode().splitlines() if l and l[0] != ">")
