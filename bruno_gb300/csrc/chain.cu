@@ -328,17 +328,16 @@ __global__ void __launch_bounds__(TPB) k_lr_apply(ChainState *cs, const uint32_t
  * neighbouring rulers, the ruler lists are ranked by pointer jumping, and every node adds
  * its offset to its ruler's ranks. */
 constexpr uint32_t RULER_SAMPLE = 32;
-struct Near { uint32_t r; uint32_t df; };          /* ruler ordinal; distance | flip << 31 */
 struct Jump { uint32_t t; uint32_t fd; uint64_t d; }; /* ruler ordinal; flip | done << 1; distance */
-constexpr uint32_t NEAR_NONE = 0xFFFFFFFFu, NEAR_END = 0xFFFFFFFEu;
 
 __device__ __forceinline__ bool side_terminal(uint32_t D) { return (D & DM) == 0; }
 __device__ __forceinline__ uint64_t side_ptr(const ChainState &s, int side) { return side ? s.outP : s.inP; }
 __device__ __forceinline__ uint32_t side_dist(const ChainState &s, int side) { return side ? s.outD : s.inD; }
 
-/* consistency check + ruler selection */
-__global__ void __launch_bounds__(TPB) k_fast_check(const ChainState *cs, uint64_t M, uint32_t *rid, uint32_t *rnode,
-                                                     Near *near, DevCounters *ctr) {
+/* Consistency check and ruler selection.  A ruler's ordinal goes into its ChainState's
+ * spare word (NONE32 for other nodes), so a walk learns that it reached a ruler from the
+ * same 32-byte read that gives it the next pointer. */
+__global__ void __launch_bounds__(TPB) k_fast_check(ChainState *cs, uint64_t M, uint32_t *rnode, DevCounters *ctr) {
   unsigned long long bad = 0;
   for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < M; i0 += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t v = i0 + threadIdx.x;
@@ -349,7 +348,6 @@ __global__ void __launch_bounds__(TPB) k_fast_check(const ChainState *cs, uint64
       for (int s = 0; s < 2; ++s) {
         const uint32_t D = side_dist(st, s);
         const uint64_t P = side_ptr(st, s);
-        near[2 * v + s] = Near{side_terminal(D) ? NEAR_END : NEAR_NONE, 0};
         if (side_terminal(D)) { term_side = true; continue; }
         if (D != 1 || (P & (PF_EXT | PF_BLANK))) { ++bad; continue; }
         const uint32_t t = (uint32_t)P;
@@ -364,48 +362,36 @@ __global__ void __launch_bounds__(TPB) k_fast_check(const ChainState *cs, uint64
       ruler = term_side || (mix64(v * 0x9e3779b97f4a7c15ull + 0x632be59bd9b4e019ull) % RULER_SAMPLE) == 0;
     }
     const unsigned long long o = warp_append(ruler, &ctr->lr_remaining);
-    if (v < M) rid[v] = ruler ? (uint32_t)o : NONE32;
+    if (v < M) cs[v].pad = ruler ? o : (uint64_t)NONE32;
     if (ruler) rnode[o] = (uint32_t)v;
   }
   bad = warp_sum(bad);
   if ((threadIdx.x & 31) == 0 && bad) atomicAdd(&ctr->lr_multi, bad);
 }
 
-/* every ruler walks both ways to the next ruler, labelling the nodes it passes */
-__global__ void __launch_bounds__(TPB) k_fast_walk(const ChainState *cs, const uint32_t *rid, const uint32_t *rnode,
-                                                    uint64_t R, uint64_t M, Near *near) {
+/* Walk 1: every non-terminal ruler side walks to the next ruler and records (that ruler,
+ * flip parity, gap) -- the first pointer-jumping link.  A terminal side is a finished link
+ * to itself.  One read per step; the grid is one resident wave, so each thread walks several
+ * sides and the geometric walk lengths average out. */
+__global__ void __launch_bounds__(TPB) k_fast_walk(const ChainState *cs, const uint32_t *rnode, uint64_t R, uint64_t M,
+                                                    Jump *E0) {
   for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 2 * R; q += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t ord = (uint32_t)(q >> 1), r = rnode[ord];
     const int s0 = (int)(q & 1);
     ChainState st = cs[r];
-    if (side_terminal(side_dist(st, s0))) continue;
-    uint32_t cur = r, dist = 0, flip = 0;
+    if (side_terminal(side_dist(st, s0))) { E0[q] = Jump{ord, 2u, 0}; continue; }
+    uint32_t flip = 0;
     int dir = s0;
-    for (uint64_t steps = 0; steps < M; ++steps) {
+    Jump out{ord, 0u, 0};   /* unreachable in a consistent map: every walk meets a ruler */
+    for (uint64_t dist = 1; dist <= M; ++dist) {
       const uint64_t P = side_ptr(st, dir);
-      const uint32_t nxt = (uint32_t)P;
       const uint32_t f = (P & PF_FLIP) ? 1u : 0u;
       flip ^= f;
-      ++dist;
-      const int ndir = f ? 1 - dir : dir;      /* travel direction in the next node's frame */
-      const int entered = 1 - ndir;             /* the side we came in through */
-      near[2ull * nxt + entered] = Near{ord, dist | (flip << 31)};
-      const uint32_t nr = rid[nxt];
-      if (nr != NONE32) { near[2ull * r + s0] = Near{nr, dist | (flip << 31)}; break; }
-      cur = nxt;
-      dir = ndir;
-      st = cs[cur];
+      dir = f ? 1 - dir : dir;   /* travel direction in the next node's frame */
+      st = cs[(uint32_t)P];
+      if ((uint32_t)st.pad != NONE32) { out = Jump{(uint32_t)st.pad, flip, dist}; break; }
     }
-  }
-}
-
-__global__ void __launch_bounds__(TPB) k_fast_jinit(const uint32_t *rnode, const Near *near, uint64_t R, Jump *E) {
-  for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 2 * R; q += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t ord = (uint32_t)(q >> 1), v = rnode[ord];
-    const Near n = near[2ull * v + (q & 1)];
-    if (n.r == NEAR_END) E[q] = Jump{ord, 2u, 0};                      /* done, points at itself */
-    else if (n.r == NEAR_NONE) E[q] = Jump{ord, 0u, 0};                /* unreachable: stays undone */
-    else E[q] = Jump{n.r, n.df >> 31, (uint64_t)(n.df & DM)};
+    E0[q] = out;
   }
 }
 
@@ -427,41 +413,80 @@ __global__ void __launch_bounds__(TPB) k_fast_jump(const Jump *E, Jump *F, uint6
   if ((threadIdx.x & 31) == 0 && undone) atomicAdd(&ctr->lr_applied, undone);
 }
 
-__global__ void __launch_bounds__(TPB) k_fast_final(ChainState *cs, uint64_t M, const uint32_t *rid,
-                                                     const uint32_t *rnode, const Near *near, const Jump *E,
-                                                     uint8_t *removed, unsigned long long *nmax, DevCounters *ctr) {
+/* final state of one side: the path end in that direction, its flip, the distance */
+__device__ __forceinline__ void fast_side(const uint32_t *rnode, const Jump &e, uint32_t flip, uint64_t d,
+                                          uint64_t &P, uint32_t &D) {
+  P = (uint64_t)rnode[e.t] | (((flip ^ (e.fd & 1u)) != 0) ? PF_FLIP : 0ull);
+  D = (uint32_t)d | TM;
+}
+
+/* rulers on paths: both non-terminal sides point at their path ends */
+__global__ void __launch_bounds__(TPB) k_fast_rulers(const ChainState *cs, ChainState *cs2, const uint32_t *rnode,
+                                                      uint64_t R, const Jump *E) {
+  for (uint64_t a = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; a < R; a += (uint64_t)gridDim.x * blockDim.x) {
+    const Jump e0 = E[2 * a], e1 = E[2 * a + 1];
+    if (!(e0.fd & 2u) || !(e1.fd & 2u)) continue;   /* a ruler cycle: left for the cycle pass */
+    const uint32_t v = rnode[a];
+    ChainState st = cs[v];
+    if (!side_terminal(st.inD)) fast_side(rnode, e0, 0, e0.d, st.inP, st.inD);
+    if (!side_terminal(st.outD)) fast_side(rnode, e1, 0, e1.d, st.outP, st.outD);
+    cs2[v] = st;
+  }
+}
+
+/* Walk 2: each segment between two rulers on a path is walked once more, from its end with
+ * the smaller ordinal (from side 1 when both ends are the same ruler), and every node on it
+ * gets its final state: the side facing the walk's start leads past the start ruler to the
+ * end E[start side'] and the other side past the far ruler to E[start side].  The walk reads
+ * the chain map and writes the final states into a second array, so no step waits behind a
+ * store to the array it reads. */
+__global__ void __launch_bounds__(TPB) k_fast_fill(const ChainState *cs, ChainState *cs2, const uint32_t *rnode,
+                                                    uint64_t R, const Jump *E0, const Jump *E) {
+  for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 2 * R; q += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t ord = (uint32_t)(q >> 1);
+    const int s0 = (int)(q & 1);
+    const Jump link = E0[q];
+    if (link.fd & 2u) continue;                                   /* terminal side */
+    if (!(link.t > ord || (link.t == ord && s0 == 1))) continue;  /* walked from the other end */
+    const Jump ef = E[q], eb = E[q ^ 1];
+    if (!(ef.fd & 2u) || !(eb.fd & 2u)) continue;                 /* a ruler cycle */
+    const uint64_t Pb_t = rnode[eb.t], Pf_t = rnode[ef.t];
+    ChainState st = cs[rnode[ord]];
+    uint32_t flip = 0;
+    int dir = s0;
+    for (uint64_t j = 1; j < link.d; ++j) {
+      const uint64_t P = side_ptr(st, dir);
+      const uint32_t v = (uint32_t)P;
+      const uint32_t f = (P & PF_FLIP) ? 1u : 0u;
+      flip ^= f;
+      dir = f ? 1 - dir : dir;
+      st = cs[v];
+      ChainState w;
+      w.pad = st.pad;
+      /* side 1-dir faces the walk's start ruler, side dir leads on to the far ruler */
+      const uint64_t Pb = Pb_t | (((flip ^ (eb.fd & 1u)) != 0) ? PF_FLIP : 0ull);
+      const uint64_t Pf = Pf_t | (((flip ^ (ef.fd & 1u)) != 0) ? PF_FLIP : 0ull);
+      const uint32_t Db = (uint32_t)(j + eb.d) | TM, Df = (uint32_t)(ef.d - j) | TM;
+      if (dir) { w.inP = Pb; w.inD = Db; w.outP = Pf; w.outD = Df; }
+      else { w.outP = Pb; w.outD = Db; w.inP = Pf; w.inD = Df; }
+      cs2[v] = w;
+    }
+  }
+}
+
+/* removed[] (1 = cycle: the node got no final state, 2 = isolated: both sides terminal), the
+ * counts, and the longest path in nodes.  cs2 starts as all ones, which no final state is. */
+constexpr uint32_t CS2_UNSET = 0xFFFFFFFFu;
+__global__ void __launch_bounds__(TPB) k_fast_mark(const ChainState *cs2, uint64_t M, uint8_t *removed,
+                                                    unsigned long long *nmax, DevCounters *ctr) {
   unsigned long long ncy = 0, niso = 0, mx = 0;
   for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < M; v += (uint64_t)gridDim.x * blockDim.x) {
-    ChainState st = cs[v];
-    bool cyc = false;
-    uint64_t len = 1;
-    uint64_t P[2] = {st.inP, st.outP};
-    uint32_t D[2] = {st.inD, st.outD};
-    for (int s = 0; s < 2; ++s) {
-      if (side_terminal(D[s])) continue;
-      Jump e;
-      uint32_t flip = 0, d0 = 0;
-      if (rid[v] != NONE32) {
-        e = E[2ull * rid[v] + s];
-      } else {
-        const Near n = near[2ull * v + s];
-        if (n.r >= NEAR_END) { cyc = true; continue; }
-        flip = n.df >> 31;
-        d0 = n.df & DM;
-        e = E[2ull * n.r + (flip ? 1 - s : s)];
-      }
-      if (!(e.fd & 2u)) { cyc = true; continue; }
-      const uint64_t dist = d0 + e.d;
-      len += dist;
-      P[s] = (uint64_t)rnode[e.t] | (((flip ^ (e.fd & 1u)) != 0) ? PF_FLIP : 0ull);
-      D[s] = (uint32_t)dist | TM;
-    }
+    const ChainState st = cs2[v];
+    const bool cyc = st.inD == CS2_UNSET;
     uint8_t r = 0;
     if (cyc) { r = 1; ++ncy; }
     else {
-      st.inP = P[0]; st.outP = P[1]; st.inD = D[0]; st.outD = D[1];
-      cs[v] = st;
-      mx = max(mx, (unsigned long long)len);
+      mx = max(mx, 1ull + (st.inD & DM) + (st.outD & DM));
       if (st.inD == TM && st.outD == TM) { r = 2; ++niso; }
     }
     removed[v] = r;
@@ -699,40 +724,50 @@ static bruno_status fast_list_rank(Ctx *c, bool &used) {
   if (M >= (1ull << 30)) return BRUNO_OK;
   const int sms = sms_count();
   ChainState *cs = (ChainState *)c->cstate.p;
-  if ((st = ensure(c, c->unf0, Mb * 4)) != BRUNO_OK) return st;        /* rid */
   if ((st = ensure(c, c->unf1, Mb * 4)) != BRUNO_OK) return st;        /* rnode */
-  if ((st = ensure(c, c->pend, Mb * 16)) != BRUNO_OK) return st;       /* near[2M] */
   if ((st = ensure(c, c->removed, Mb)) != BRUNO_OK) return st;
-  uint32_t *rid = (uint32_t *)c->unf0.p, *rnode = (uint32_t *)c->unf1.p;
-  Near *near = (Near *)c->pend.p;
+  uint32_t *rnode = (uint32_t *)c->unf1.p;
   cudaMemsetAsync(&c->dctr->lr_applied, 0, 32, c->stream);   /* applied, remaining, cycles, multi */
-  k_fast_check<<<sms * 8, TPB, 0, c->stream>>>(cs, M, rid, rnode, near, c->dctr);
+  k_fast_check<<<sms * 8, TPB, 0, c->stream>>>(cs, M, rnode, c->dctr);
   c->launches += 1;
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   if (c->hctr->lr_multi != 0) return BRUNO_OK;                /* inconsistent pointers */
   const uint64_t R = c->hctr->lr_remaining, Rb = std::max<uint64_t>(1, R);
-  if ((st = ensure(c, c->pay, Rb * 2 * sizeof(Jump) * 2)) != BRUNO_OK) return st;
-  Jump *E = (Jump *)c->pay.p, *F = E + 2 * Rb;
-  const int gw = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 16, (2 * R + TPB - 1) / TPB));
-  k_fast_walk<<<gw, TPB, 0, c->stream>>>(cs, rid, rnode, R, M, near);
-  k_fast_jinit<<<gw, TPB, 0, c->stream>>>(rnode, near, R, E);
-  c->launches += 2;
+  if ((st = ensure(c, c->pay, Rb * 2 * sizeof(Jump) * 3)) != BRUNO_OK) return st;
+  Jump *E0 = (Jump *)c->pay.p, *E = E0 + 2 * Rb, *F = E + 2 * Rb;
+  static int walk_occ = 0;   /* resident walk blocks per SM: the walks run as one wave */
+  if (!walk_occ && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&walk_occ, k_fast_walk, TPB, 0) != cudaSuccess ||
+                    walk_occ < 1))
+    walk_occ = 4;
+  const int gw = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * walk_occ, (2 * R + TPB - 1) / TPB));
+  k_fast_walk<<<gw, TPB, 0, c->stream>>>(cs, rnode, R, M, E0);
+  c->launches += 1;
+  const Jump *src = E0;
   uint64_t prev = ~0ull;
   for (int round = 0; round < 64; ++round) {
     cudaMemsetAsync(&c->dctr->lr_applied, 0, 8, c->stream);
-    k_fast_jump<<<gw, TPB, 0, c->stream>>>(E, F, R, c->dctr);
+    k_fast_jump<<<gw, TPB, 0, c->stream>>>(src, E, R, c->dctr);
     c->launches += 1;
+    src = E;
     std::swap(E, F);
     if ((st = sync_counters(c)) != BRUNO_OK) return st;
     const uint64_t undone = c->hctr->lr_applied;
     if (undone == 0 || undone == prev) break;   /* only ruler cycles keep sides undone */
     prev = undone;
   }
+  /* final states go to a second chain-state array (all ones = unset), which then becomes
+   * the chain map; a node left unset is a cycle node, whose state nothing reads again */
+  if ((st = ensure(c, c->cstate2, Mb * sizeof(ChainState))) != BRUNO_OK) return st;
+  ChainState *cs2 = (ChainState *)c->cstate2.p;
+  cudaMemsetAsync(cs2, 0xFF, M * sizeof(ChainState), c->stream);
+  k_fast_fill<<<gw, TPB, 0, c->stream>>>(cs, cs2, rnode, R, E0, src);
+  k_fast_rulers<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 8, (R + TPB - 1) / TPB)), TPB, 0,
+                  c->stream>>>(cs, cs2, rnode, R, src);
   cudaMemsetAsync(&c->dctr->n_cycle, 0, 16, c->stream);
   cudaMemsetAsync(&c->dctr->n_heads, 0, 8, c->stream);        /* longest path, in nodes */
-  k_fast_final<<<sms * 8, TPB, 0, c->stream>>>(cs, M, rid, rnode, near, E, (uint8_t *)c->removed.p,
-                                                &c->dctr->n_heads, c->dctr);
-  c->launches += 1;
+  k_fast_mark<<<sms * 8, TPB, 0, c->stream>>>(cs2, M, (uint8_t *)c->removed.p, &c->dctr->n_heads, c->dctr);
+  c->launches += 3;
+  std::swap(c->cstate, c->cstate2);
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   c->n_cycle = c->hctr->n_cycle;
   c->n_isolated = c->hctr->n_isolated;
