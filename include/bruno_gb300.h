@@ -196,9 +196,13 @@ bruno_status bruno_phase_ms(bruno_ctx *ctx, double *ms, size_t n);
  *
  * The work runs on `stream` (a cudaStream_t, NULL = the default stream) of `device`; the
  * call waits for it before returning and leaves the caller's current device as it was.
- * There is one scratch array per device: two calls whose GPU work can overlap on the same
- * device (from two host threads, or on two streams without ordering between them) use the
- * same table at the same time and corrupt each other's counts.  Serialise them. */
+ * There is one scratch array per device, held by every GPU that loads the library until the
+ * process exits, and it keeps the last call's contents: each call first clears its counters
+ * and the table slots it uses.  Two calls whose GPU work can overlap on the same device (from
+ * two host threads, or on two streams without ordering between them) use the same table at
+ * the same time and corrupt each other's counts.  Serialise them.  The first call on a device
+ * does a one-time set-up for that device (it looks up the array's device address); make that
+ * first call before any stream capture. */
 #define BRUNO_NOALLOC_SCRATCH_BYTES (32u << 20)
 #define BRUNO_NOALLOC_MAX_PAIRS_K31 ((((32u << 20) - (64u << 10)) / 32u) / 2u)
 #define BRUNO_NOALLOC_MAX_PAIRS_K63 ((((32u << 20) - (64u << 10)) / 64u) / 2u)
