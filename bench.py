@@ -287,6 +287,18 @@ def main():
             traffic = tj[top]["bytes_per_record"] * inst_step
     phases = {k: round(statistics.mean(p[k] for p in kms), 3) for k in kms[0]}
 
+    # The whole path against the HBM roofline, with the path's algorithmic bytes:
+    #   FASTQ once + one random 64-byte read-modify-write per (k-mer, biedge) instance + one
+    #   scan of the distinct entries (16 B each at k <= 31, 32 B above) + one 64-byte update
+    #   per kept entry + one scan of the node table (32 / 48 B a node) + three 32-byte touches
+    #   per chain node + the emitted chains (sequence bytes + 24-byte listranked records),
+    # over the device-resident step time.
+    s2, s1 = (16, 32) if w.k <= 31 else (32, 48)
+    kept = sum(sizes["filter_flag_hist"][:3])
+    path_bytes = (n + 64 * inst_step + s2 * sizes["n_k2"] + 64 * kept + s1 * sizes["n_nodes"]
+                  + 96 * sizes["n_chain_nodes"] + sizes["n_chain_chars"] + 24 * sizes["n_ranked"])
+    path_achieved = path_bytes / (ms / args.steps / 1e3) / 1e9
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -299,6 +311,8 @@ def main():
                              "unit": "GB/s", "frac": kernels[top]["frac"], "peak_source": peak_src,
                              "traffic": traffic, "alg_bytes_per_launch": kernels[top]["alg_bytes_per_launch"],
                              "launch_ms": kernels[top]["launch_ms"], "kernels": kernels},
+                "path_roofline": {"bound": "hbm", "alg_bytes_per_step": path_bytes, "achieved": path_achieved,
+                                  "peak": peak, "unit": "GB/s", "frac": path_achieved / peak},
                 "gpu_launches": launches, "clocks": clk.summary(), "phase_ms": phases,
                 "sizes": {k: sizes[k] for k in ("n_reads", "n_instances", "n_k2", "n_nodes", "n_branch",
                                                 "n_chain_nodes", "iterations", "n_chains", "table_slots",

@@ -853,7 +853,9 @@ std::string ascii_words(const uint64_t *p, int k, int words) {
 extern "C" int oracle_run(const char *fastq, size_t nbytes, const oracle_cfg *cfg, oracle_result **out) {
   if (!cfg || !out || cfg->k < 3 || cfg->k > 63) return 1;
   oracle_result *r = (oracle_result *)calloc(1, sizeof(oracle_result));
-  r->words = cfg->k <= 32 ? 1 : 2;
+  /* exported arrays use the GB300 library's layout (2 words from k = 32 on) so the two
+   * compare directly; k = 32 still computes in one 64-bit word, as Kmer<32> does */
+  r->words = cfg->k <= 31 ? 1 : 2;
   oracle_cfg c = *cfg;
   if (!c.thresholding) {
     /* build_index: no flags (every entry kept with both edges) */

@@ -13,7 +13,8 @@
  *
  * k-mer words: a k-mer of length k (1..63) is 2-bit packed, first character in the most
  * significant bits, A=0 C=1 G=2 T=3.  Arrays of k-mers use `words` uint64 per k-mer
- * (1 for k <= 32, 2 for k > 32; for 2 words the low word comes first).
+ * (1 for k <= 31, 2 for k >= 32 -- the GB300 library's layout; for 2 words the low word
+ * comes first).
  */
 #ifndef BRUNO_ORACLE_H_
 #define BRUNO_ORACLE_H_

@@ -176,3 +176,34 @@ def test_context_reuse_gives_identical_results():
     g.build_and_compact(data)
     assert chain_set(*g.chains()) == first[0]
     assert_same(sort_ranked(*g.ranked()), first[1], "second build")
+
+
+@pytest.mark.parametrize("k", [32, 33, 45, 63])
+def test_large_k_workload_parity(k):
+    """128-bit keys (k >= 32): a repeat-rich 300 kbp genome at 25x, every output, both
+    ranking variants and the round-synchronous ranking"""
+    w = synth.Workload(f"k{k}", 300_000, 150, 50_000, 0.005, k, (3,), 0.03, (500, 4000), (2, 6), (0.01, 0.02), 7)
+    fq = synth.make_fastq(w)
+    thr = bg.thresholds(w.lower)
+    for mu, kw in ((True, {}), (False, {}), (True, {"exact_ranking": True})):
+        ref = oracle.run(fq, k=k, thresh=thr, min_update=mu, threads=16, keep_k2=True, keep_filtered=True)
+        compare(gpu_run(fq, k, True, thr, mu, **kw), ref)
+
+
+@pytest.mark.parametrize("k", [33, 63])
+@pytest.mark.parametrize("fname", ["debruijn.palindrome_chr14.fastq", "debruijn.bubble.fastq", "natural.fastq"])
+def test_large_k_fixture_parity(fname, k):
+    data = fixture_bytes(fname)
+    for thr_on, lo in ((False, ()), (True, (2,))):
+        thr = bg.thresholds(lo)
+        ref = oracle.run(data, k=k, thresholding=thr_on, thresh=thr, min_update=True, keep_k2=True,
+                         keep_filtered=True)
+        compare(gpu_run(data, k, thr_on, thr, True), ref)
+
+
+def test_large_k_one_call_parity():
+    w = synth.Workload("k63one", 300_000, 150, 50_000, 0.005, 63, (3,), 0.03, (500, 4000), (2, 6), (0.01, 0.02), 8)
+    fq = synth.make_fastq(w)
+    thr = bg.thresholds(w.lower)
+    ref = oracle.run(fq, k=63, thresh=thr, min_update=True, threads=16, keep_k2=True)
+    compare_one_call(one_call_run(fq, 63, True, thr, True), ref)
