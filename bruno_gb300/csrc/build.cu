@@ -1060,9 +1060,10 @@ __device__ __noinline__ void filter_wide_global(uint64_t *s, uint64_t i, KT key,
  * partition's records into shared memory with shared-memory atomics and writes the finished
  * slot region to the table once, in coalesced 16-byte stores. */
 constexpr int PART_SLOTS = 3072;           /* 96 KB of slots */
-constexpr int PTPB = 256;
+constexpr int PTPB = 512;
 constexpr int MAX_SPLIT_BITS = 10;
 constexpr int SPLIT_QWORDS = 8192;         /* queue words of k_split (64 KB) */
+constexpr int SPLIT_ROUND = 8;             /* records per thread per round: 4096 a block, half the queue words */
 
 struct SplitSmem {
   uint64_t q[SPLIT_QWORDS];
@@ -1072,16 +1073,15 @@ struct SplitSmem {
 };
 
 /* bucket blockIdx.y -> its 2^sbits partitions; every block takes one contiguous share.
- * Queue capacity qc = min(32, SPLIT_QWORDS >> sbits); a round reads `per_round` records per
- * thread so that a queue is about half full when the block flushes. */
+ * Queue capacity qc = SPLIT_QWORDS >> sbits; a round reads SPLIT_ROUND records per thread,
+ * half the queue words, so a queue is about half full when the block flushes. */
 __global__ void __launch_bounds__(XTPB) k_split(const uint64_t *records, const unsigned long long *bucket_cnt,
                                                  uint64_t cap, int sbits, uint64_t *out, uint64_t cap2,
                                                  unsigned long long *sub_cnt, DevCounters *ctr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SplitSmem &S = *reinterpret_cast<SplitSmem *>(smem_raw);
   const int tid = threadIdx.x, nq = 1 << sbits, b = blockIdx.y;
-  const int qc = min(32, SPLIT_QWORDS >> sbits);
-  const int per_round = max(1, (qc / 2) * nq / XTPB);
+  const int qc = SPLIT_QWORDS >> sbits;   /* a round fills every queue about half */
   for (int i = tid; i < nq; i += XTPB) S.cnt[i] = 0;
   if (tid == 0) S.overflow = 0;
   __syncthreads();
@@ -1090,11 +1090,18 @@ __global__ void __launch_bounds__(XTPB) k_split(const uint64_t *records, const u
   const uint64_t lo = min(n, (uint64_t)blockIdx.x * per), hi = min(n, lo + per);
   const uint64_t *rb = records + (uint64_t)b * cap;
   const int shift = 5 + LOW_BITS - sbits;
-  for (uint64_t r0 = lo; r0 < hi; r0 += (uint64_t)XTPB * per_round) {
-    for (int j = 0; j < per_round; ++j) {
+  for (uint64_t r0 = lo; r0 < hi; r0 += (uint64_t)XTPB * SPLIT_ROUND) {
+    uint64_t recs[SPLIT_ROUND];   /* every load of the round is in flight before the first push */
+    #pragma unroll
+    for (int j = 0; j < SPLIT_ROUND; ++j) {
+      const uint64_t i = r0 + (uint64_t)j * XTPB + tid;
+      recs[j] = i < hi ? __ldcs(rb + i) : 0ull;
+    }
+    #pragma unroll
+    for (int j = 0; j < SPLIT_ROUND; ++j) {
       const uint64_t i = r0 + (uint64_t)j * XTPB + tid;
       if (i < hi) {
-        const uint64_t rec = __ldcs(rb + i);
+        const uint64_t rec = recs[j];
         const unsigned sq = (unsigned)(rec >> shift) & (unsigned)(nq - 1);
         const unsigned pos = atomicAdd(&S.cnt[sq], 1u);
         if (pos < (unsigned)qc) {
