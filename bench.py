@@ -49,6 +49,19 @@ def parse_args():
     return ap.parse_args()
 
 
+def max_over_ranks(x: float, world: int) -> float:
+    """The largest value over all ranks (the slowest rank's time); a no-op for one rank.
+    Uses a device tensor under NCCL and a host tensor under gloo."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -223,11 +236,7 @@ def main():
             launches += g.sizes()["launches"]
         end.record(stream)
         barrier()
-    ms = start.elapsed_time(end)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(start.elapsed_time(end), world)
     inst_step = sizes["n_instances"]
     value = inst_step * args.steps * world / (ms / 1e3)
 
@@ -252,11 +261,7 @@ def main():
         step_e2e()
     e1.record(stream)
     barrier()
-    ems = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ems], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ems = float(t.item())
+    ems = max_over_ranks(e0.elapsed_time(e1), world)
     e2e_value = inst_step * args.steps * world / (ems / 1e3)
     d2h = nch + 8 * (nc + 1) + 8 * g.words * nc
 
