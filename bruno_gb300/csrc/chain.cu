@@ -334,9 +334,12 @@ __device__ __forceinline__ bool side_terminal(uint32_t D) { return (D & DM) == 0
 __device__ __forceinline__ uint64_t side_ptr(const ChainState &s, int side) { return side ? s.outP : s.inP; }
 __device__ __forceinline__ uint32_t side_dist(const ChainState &s, int side) { return side ? s.outD : s.inD; }
 
-/* Consistency check and ruler selection.  A ruler's ordinal goes into its ChainState's
- * spare word (NONE32 for other nodes), so a walk learns that it reached a ruler from the
- * same 32-byte read that gives it the next pointer. */
+/* Ruler selection and the local half of the consistency check (every non-terminal side is a
+ * chain pointer at distance 1).  A ruler's ordinal goes into its ChainState's spare word
+ * (NONE32 for other nodes), so a walk learns that it reached a ruler from the same 32-byte
+ * read that gives it the next pointer.  The other half -- every chain pointer is answered by
+ * the facing side of its target -- is checked by the first walk for every node it passes and
+ * by the marking pass for the nodes no walk reaches. */
 __global__ void __launch_bounds__(TPB) k_fast_check(ChainState *cs, uint64_t M, uint32_t *rnode, DevCounters *ctr) {
   unsigned long long bad = 0;
   for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < M; i0 += (uint64_t)gridDim.x * blockDim.x) {
@@ -347,17 +350,8 @@ __global__ void __launch_bounds__(TPB) k_fast_check(ChainState *cs, uint64_t M, 
       bool term_side = false;
       for (int s = 0; s < 2; ++s) {
         const uint32_t D = side_dist(st, s);
-        const uint64_t P = side_ptr(st, s);
         if (side_terminal(D)) { term_side = true; continue; }
-        if (D != 1 || (P & (PF_EXT | PF_BLANK))) { ++bad; continue; }
-        const uint32_t t = (uint32_t)P;
-        const int f = (P & PF_FLIP) ? 1 : 0;
-        const ChainState ts = cs[t];
-        const int facing = f ? s : 1 - s;
-        const uint64_t back = side_ptr(ts, facing);
-        if (side_dist(ts, facing) != 1 || (back & (PF_EXT | PF_BLANK)) || (uint32_t)back != (uint32_t)v ||
-            (((back & PF_FLIP) ? 1 : 0) != f))
-          ++bad;
+        if (D != 1 || (side_ptr(st, s) & (PF_EXT | PF_BLANK))) ++bad;
       }
       ruler = term_side || (mix64(v * 0x9e3779b97f4a7c15ull + 0x632be59bd9b4e019ull) % RULER_SAMPLE) == 0;
     }
@@ -369,30 +363,45 @@ __global__ void __launch_bounds__(TPB) k_fast_check(ChainState *cs, uint64_t M, 
   if ((threadIdx.x & 31) == 0 && bad) atomicAdd(&ctr->lr_multi, bad);
 }
 
+/* the facing side of a chain pointer's target answers it: distance 1, a chain pointer back
+ * to the source with the same flip */
+__device__ __forceinline__ bool answers(const ChainState &t, int facing, uint32_t src, uint32_t f) {
+  const uint64_t back = side_ptr(t, facing);
+  return side_dist(t, facing) == 1 && !(back & (PF_EXT | PF_BLANK)) && (uint32_t)back == src &&
+         (((back & PF_FLIP) ? 1u : 0u) == f);
+}
+
 /* Walk 1: every non-terminal ruler side walks to the next ruler and records (that ruler,
  * flip parity, gap) -- the first pointer-jumping link.  A terminal side is a finished link
- * to itself.  One read per step; the grid is one resident wave, so each thread walks several
- * sides and the geometric walk lengths average out. */
+ * to itself.  One read per step, which also checks that the node stepped to points back; the
+ * grid is one resident wave, so each thread walks several sides and the geometric walk
+ * lengths average out. */
 __global__ void __launch_bounds__(TPB) k_fast_walk(const ChainState *cs, const uint32_t *rnode, uint64_t R, uint64_t M,
-                                                    Jump *E0) {
+                                                    Jump *E0, DevCounters *ctr) {
+  unsigned long long bad = 0;
   for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 2 * R; q += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t ord = (uint32_t)(q >> 1), r = rnode[ord];
     const int s0 = (int)(q & 1);
     ChainState st = cs[r];
     if (side_terminal(side_dist(st, s0))) { E0[q] = Jump{ord, 2u, 0}; continue; }
-    uint32_t flip = 0;
+    uint32_t flip = 0, cur = r;
     int dir = s0;
     Jump out{ord, 0u, 0};   /* unreachable in a consistent map: every walk meets a ruler */
     for (uint64_t dist = 1; dist <= M; ++dist) {
       const uint64_t P = side_ptr(st, dir);
-      const uint32_t f = (P & PF_FLIP) ? 1u : 0u;
+      if (side_dist(st, dir) != 1 || (P & (PF_EXT | PF_BLANK))) { ++bad; break; }
+      const uint32_t f = (P & PF_FLIP) ? 1u : 0u, nxt = (uint32_t)P;
       flip ^= f;
       dir = f ? 1 - dir : dir;   /* travel direction in the next node's frame */
-      st = cs[(uint32_t)P];
+      st = cs[nxt];
+      if (!answers(st, 1 - dir, cur, f)) { ++bad; break; }
+      cur = nxt;
       if ((uint32_t)st.pad != NONE32) { out = Jump{(uint32_t)st.pad, flip, dist}; break; }
     }
     E0[q] = out;
   }
+  bad = warp_sum(bad);
+  if ((threadIdx.x & 31) == 0 && bad) atomicAdd(&ctr->lr_multi, bad);
 }
 
 __global__ void __launch_bounds__(TPB) k_fast_jump(const Jump *E, Jump *F, uint64_t R, DevCounters *ctr) {
@@ -477,23 +486,36 @@ __global__ void __launch_bounds__(TPB) k_fast_fill(const ChainState *cs, ChainSt
 /* removed[] (1 = cycle: the node got no final state, 2 = isolated: both sides terminal), the
  * counts, and the longest path in nodes.  cs2 starts as all ones, which no final state is. */
 constexpr uint32_t CS2_UNSET = 0xFFFFFFFFu;
-__global__ void __launch_bounds__(TPB) k_fast_mark(const ChainState *cs2, uint64_t M, uint8_t *removed,
-                                                    unsigned long long *nmax, DevCounters *ctr) {
-  unsigned long long ncy = 0, niso = 0, mx = 0;
+__global__ void __launch_bounds__(TPB) k_fast_mark(const ChainState *cs, const ChainState *cs2, uint64_t M,
+                                                    uint8_t *removed, unsigned long long *nmax, DevCounters *ctr) {
+  unsigned long long ncy = 0, niso = 0, mx = 0, bad = 0;
   for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < M; v += (uint64_t)gridDim.x * blockDim.x) {
     const ChainState st = cs2[v];
     const bool cyc = st.inD == CS2_UNSET;
     uint8_t r = 0;
-    if (cyc) { r = 1; ++ncy; }
+    if (cyc) {
+      r = 1; ++ncy;
+      /* no walk reached this node: check its pointers here (consistent only on a cycle) */
+      const ChainState o = cs[v];
+      for (int s = 0; s < 2; ++s) {
+        const uint32_t D = side_dist(o, s);
+        const uint64_t P = side_ptr(o, s);
+        if (side_terminal(D)) continue;
+        if (D != 1 || (P & (PF_EXT | PF_BLANK))) { ++bad; continue; }
+        const uint32_t f = (P & PF_FLIP) ? 1u : 0u;
+        if (!answers(cs[(uint32_t)P], f ? s : 1 - s, (uint32_t)v, f)) ++bad;
+      }
+    }
     else {
       mx = max(mx, 1ull + (st.inD & DM) + (st.outD & DM));
       if (st.inD == TM && st.outD == TM) { r = 2; ++niso; }
     }
     removed[v] = r;
   }
-  ncy = warp_sum(ncy); niso = warp_sum(niso);
+  ncy = warp_sum(ncy); niso = warp_sum(niso); bad = warp_sum(bad);
   for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_down_sync(~0u, mx, o));
   if ((threadIdx.x & 31) == 0) {
+    if (bad) atomicAdd(&ctr->lr_multi, bad);
     if (ncy) atomicAdd(&ctr->n_cycle, ncy);
     if (niso) atomicAdd(&ctr->n_isolated, niso);
     if (mx) atomicMax(nmax, mx);
@@ -740,8 +762,10 @@ static bruno_status fast_list_rank(Ctx *c, bool &used) {
                     walk_occ < 1))
     walk_occ = 4;
   const int gw = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * walk_occ, (2 * R + TPB - 1) / TPB));
-  k_fast_walk<<<gw, TPB, 0, c->stream>>>(cs, rnode, R, M, E0);
+  k_fast_walk<<<gw, TPB, 0, c->stream>>>(cs, rnode, R, M, E0, c->dctr);
   c->launches += 1;
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  if (c->hctr->lr_multi != 0) return BRUNO_OK;                /* a pointer not answered by its target */
   const Jump *src = E0;
   uint64_t prev = ~0ull;
   for (int round = 0; round < 64; ++round) {
@@ -765,10 +789,11 @@ static bruno_status fast_list_rank(Ctx *c, bool &used) {
                   c->stream>>>(cs, cs2, rnode, R, src);
   cudaMemsetAsync(&c->dctr->n_cycle, 0, 16, c->stream);
   cudaMemsetAsync(&c->dctr->n_heads, 0, 8, c->stream);        /* longest path, in nodes */
-  k_fast_mark<<<sms * 8, TPB, 0, c->stream>>>(cs2, M, (uint8_t *)c->removed.p, &c->dctr->n_heads, c->dctr);
+  k_fast_mark<<<sms * 8, TPB, 0, c->stream>>>(cs, cs2, M, (uint8_t *)c->removed.p, &c->dctr->n_heads, c->dctr);
   c->launches += 3;
-  std::swap(c->cstate, c->cstate2);
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  if (c->hctr->lr_multi != 0) return BRUNO_OK;   /* an unreached node is not on a consistent cycle */
+  std::swap(c->cstate, c->cstate2);              /* the final states become the chain map */
   c->n_cycle = c->hctr->n_cycle;
   c->n_isolated = c->hctr->n_isolated;
   const uint64_t nmax = c->hctr->n_heads;
