@@ -104,7 +104,7 @@ bruno_status bruno_ctx_destroy(bruno_ctx *c) {
   if (!c) return BRUNO_ERR_ARG;
   if (c->stream) cudaStreamSynchronize(c->stream);
   Buf *bufs[] = {&c->rstart, &c->rend, &c->tile_cnt, &c->tile_base, &c->table, &c->k2_keys, &c->k2_edges, &c->k2_counts,
-                 &c->f_keys, &c->f_edges, &c->f_counts, &c->blk_cnt, &c->blk_base, &c->ckey, &c->cslot, &c->cedge,
+                 &c->f_keys, &c->f_edges, &c->f_counts, &c->blk_cnt, &c->blk_base, &c->ckey, &c->cedge,
                  &c->cstate, &c->cstate2, &c->pend, &c->pay, &c->unf0, &c->unf1, &c->removed, &c->r_K, &c->r_rep, &c->r_dist,
                  &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list,
                  &c->records, &c->bucket_cnt, &c->records2, &c->sub_cnt};

@@ -1,10 +1,9 @@
 /*
  * chain.cu -- graph nodes -> chain map -> list ranking -> compacted chains.
  *
- *  k_chain_keys          chain index -> k-mer and slot (the filter listed the chain nodes)
- *  k_chain_init          to_simple_biedge (debruijn_chain_node.hpp:83-111): neighbours are
- *                        resolved once to chain indices (+ strand flip), so ranking never
- *                        hashes k-mers again
+ *  k_chain_init          to_simple_biedge (debruijn_chain_node.hpp:83-111) for every chain
+ *                        node the filter listed: neighbours are resolved once to chain
+ *                        indices (+ strand flip), so ranking never hashes k-mers again
  *  k_termini             setup_chain_termini (debruijn_chain_graph.hpp:485-596) with
  *                        terminus_update (debruijn_chain_operations.hpp:57-93)
  *  k_lr_*                list_rank_min_update / list_rank (debruijn_chain_graph.hpp:793-1310):
@@ -14,6 +13,9 @@
  *                        largest (distance, terminal mark); for the reference's chains this
  *                        equals applying them one after another in any order.
  *  k_separate            separate_cycles(iterations) and separate_isolated (:670-777)
+ *  k_fast_*              the same ranking in O(M) when the chain map is mutually consistent
+ *                        (ruling set: walks between rulers, pointer jumping over rulers, a
+ *                        second walk that writes every node's final state)
  *  k_ranked / k_fill     to_listranked_chain_node (debruijn_chain_operations.hpp:260-309) and
  *                        to_compressed_chains (debruijn_chain_graph.hpp:1778-1856): every
  *                        chain is one head node with distance 0 plus one base per node, so
@@ -106,11 +108,14 @@ __device__ __forceinline__ long long table_find(const uint64_t *table, const Tab
   return -1;
 }
 
-/* ================================================================ chain indices */
-/* chain index i -> its slot (listed by the filter, which also stored i in the slot) */
+/* ================================================================ chain init */
+/* chain index i (listed by the filter, which also stored i in the slot) -> its k-mer, its
+ * chain-map record and its edge byte; one read of its own slot gives key and counters */
 template <class KT>
-__global__ void __launch_bounds__(TPB) k_chain_keys(const uint64_t *table, uint64_t nslots, const uint32_t *chain_list,
-                                                     uint64_t M, uint64_t *ckey, uint64_t *cslot, DevCounters *ctr) {
+__global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, uint64_t nslots, TableGeom g, int k,
+                                                     const uint32_t *chain_list, uint64_t M, uint64_t *ckey,
+                                                     ChainState *cs, uint8_t *cedge, uint32_t max_probe,
+                                                     DevCounters *ctr) {
   constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t sl = chain_list[i];
@@ -119,20 +124,9 @@ __global__ void __launch_bounds__(TPB) k_chain_keys(const uint64_t *table, uint6
       sl = 0;
     }
     const uint64_t *s = table + sl * SU;
-    KOps<KT>::store(ckey + i * KWD, key_kmer(KOps<KT>::load(s)));
-    cslot[i] = sl;
-  }
-}
-
-/* ================================================================ chain init */
-template <class KT>
-__global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, TableGeom g, int k, const uint64_t *ckey,
-                                                     const uint64_t *cslot, uint64_t M, ChainState *cs, uint8_t *cedge,
-                                                     uint32_t max_probe) {
-  constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (uint64_t)gridDim.x * blockDim.x) {
-    const KT K = KOps<KT>::load(ckey + i * KWD);
-    const uint64_t *pw = table + cslot[i] * SU + KWD;
+    const KT K = key_kmer(KOps<KT>::load(s));
+    KOps<KT>::store(ckey + i * KWD, K);
+    const uint64_t *pw = s + KWD;
     int inc = -1, outc = -1;
     for (int c = 0; c < 4; ++c) {
       if ((pw[0] >> (16 * c)) & 0xFFFFu) outc = c;
@@ -665,22 +659,18 @@ bruno_status extract_typed(Ctx *c) {
   const uint64_t M = c->n_chain, Mb = std::max<uint64_t>(1, M);
   const int KWD = Slot<KT>::KEYW;
   if ((st = ensure(c, c->ckey, Mb * 8 * KWD)) != BRUNO_OK) return st;
-  if ((st = ensure(c, c->cslot, Mb * 8)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->cedge, Mb)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->cstate, Mb * sizeof(ChainState))) != BRUNO_OK) return st;
   const int sms = sms_count();
   cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
-  k_chain_keys<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots,
+  k_chain_init<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, c->geom, c->cfg.k,
                                                    (const uint32_t *)c->chain_list.p, M, (uint64_t *)c->ckey.p,
-                                                   (uint64_t *)c->cslot.p, c->dctr);
-  k_chain_init<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->geom, c->cfg.k,
-                                                   (const uint64_t *)c->ckey.p, (const uint64_t *)c->cslot.p, M,
-                                                   (ChainState *)c->cstate.p, (uint8_t *)c->cedge.p, 4096u);
+                                                   (ChainState *)c->cstate.p, (uint8_t *)c->cedge.p, 4096u, c->dctr);
   if (c->n_branch)
     k_termini<KT><<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>(sms * 8, (c->n_branch + TPB - 1) / TPB)), TPB, 0,
                     c->stream>>>((const uint64_t *)c->table.p, c->geom, c->cfg.k, (ChainState *)c->cstate.p, M, 4096u,
                                  (const uint32_t *)c->branch_list.p, c->n_branch);
-  c->launches += 3;
+  c->launches += 2;
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   if (c->hctr->err & DERR_INVARIANT) return set_err(c, BRUNO_ERR_INVARIANT, "chain list incomplete");
   return BRUNO_OK;

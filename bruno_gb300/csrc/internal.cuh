@@ -91,7 +91,7 @@ struct Ctx {
   Buf blk_cnt, blk_base;
 
   /* chains */
-  Buf ckey, cslot, cedge, cstate, cstate2, pend, pay, unf0, unf1, removed;
+  Buf ckey, cedge, cstate, cstate2, pend, pay, unf0, unf1, removed;
   uint64_t iterations = 0, n_cycle = 0, n_isolated = 0, multi = 0;
   bool exact_ranking = false;    /* force the round-synchronous ranking (tests) */
 
