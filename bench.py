@@ -27,6 +27,8 @@ import subprocess
 import sys
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -42,6 +44,12 @@ def parse_args():
     ap.add_argument("--workload", default="plain-scale")
     ap.add_argument("--cpu-sample", type=float, default=0.2, help="fraction of reads in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--samples", type=int, default=None,
+                    help="batched / served: number of distinct samples (256 / 48)")
+    ap.add_argument("--workers", type=int, default=8, help="served: pool workers")
+    ap.add_argument("--rates", type=float, nargs="+", default=[10, 50, 100, 200, 500], help="served: requests/s")
+    ap.add_argument("--requests", type=int, default=200, help="served: most requests per rate")
+    ap.add_argument("--seconds", type=float, default=4.0, help="served: target seconds per rate")
     ap.add_argument("--api", default="build", choices=["build", "steps"],
                     help="build: bruno_build_and_compact (one call); steps: the reference's call sequence "
                          "(load, compute_biedge_freqencies, local_insert_by_freqencies, extract_chains, "
@@ -176,9 +184,158 @@ def run_reference(args, w):
     print(json.dumps(line), flush=True)
 
 
+def _pinned_copies(bg, fqs):
+    bufs = []
+    for fq in fqs:
+        b = bg.PinnedBuffer(max(1, fq.nbytes))
+        b.array[:fq.nbytes] = fq
+        bufs.append(b)
+    return bufs
+
+
+def _plain_loop(bg, cfg, bufs, sizes):
+    """the plain path looped over the samples: one context, one build after another"""
+    g = bg.Graph(cfg)
+    outs = []
+    t0 = time.perf_counter()
+    for b, n in zip(bufs, sizes):
+        g.build_and_compact(b.array[:n])
+        outs.append((g.sizes(), g.chains()))
+    dt = time.perf_counter() - t0
+    g.close()
+    return dt, outs
+
+
+def _same_as_plain(res, plain):
+    sizes, chains = plain
+    keys = ("n_instances", "n_k2", "n_nodes", "n_chain_nodes", "n_ranked", "n_chains", "n_chain_chars")
+    if res["status"] != 0 or any(res["sizes"][k] != sizes[k] for k in keys):
+        return False
+    a, b = res["chains"], chains
+    return (np.array_equal(np.sort(a[0], axis=0), np.sort(b[0], axis=0)) and a[1][-1] == b[1][-1]
+            and sorted(bytes(a[2][a[1][i]:a[1][i + 1]]) for i in range(len(a[0])))
+            == sorted(bytes(b[2][b[1][i]:b[1][i + 1]]) for i in range(len(b[0]))))
+
+
+def run_batched(args):
+    """Config 3: 256 independent samples of uneven size built as one batch through the pool,
+    against the plain path looped over the same samples on the same GPU."""
+    import bruno_gb300 as bg
+    from bruno_gb300 import synth
+    samples = synth.sample_set(args.samples or 256, seed=3, max_genome=2_000_000)
+    fqs = [synth.make_fastq(w) for w in samples]
+    sizes = [fq.nbytes for fq in fqs]
+    bufs = _pinned_copies(bg, fqs)
+    cfg = bg.GraphConfig(k=31, thresh=bg.thresholds([2]), min_update=True)
+    _plain_loop(bg, cfg, bufs[:8], sizes[:8])                 # warm-up
+    plain_s, plain = _plain_loop(bg, cfg, bufs, sizes)
+
+    def batch(workers, idx):
+        pool = bg.Pool(cfg, workers=workers)
+        t0 = time.perf_counter()
+        tickets = [pool.submit(bufs[i].array[:sizes[i]]) for i in idx]
+        res = [pool.wait(t) for t in tickets]
+        dt = time.perf_counter() - t0
+        pool.close()
+        return dt, res
+    # autotune the worker count on the first quarter of the batch
+    probe = list(range(0, len(fqs), 4))
+    tune = {wk: len(probe) / batch(wk, probe)[0] for wk in (4, 8, 12, 16, 24)}
+    workers = max(tune, key=tune.get)
+    batch(workers, probe)                                       # warm-up of the chosen size
+    dt, res = batch(workers, range(len(fqs)))
+    exact = all(_same_as_plain(r, p) for r, p in zip(res, plain))
+    lat = sorted(r["queue_ms"] + r["run_ms"] for r in res)
+    line = {"metric": "graphs/s batched", "value": len(fqs) / dt, "unit": "graphs/s", "n_gpus": 1,
+            "higher_is_better": True, "data": "synthetic (seeded generator, sample_set seed 3)",
+            "config": {"workload": f"batched: {len(fqs)} samples, genome log-uniform 5 kbp-2 Mbp, 20-60x, "
+                                   "100-250 bp reads, 0.5-2% substitutions, k=31, -L 2",
+                       "fastq_bytes": int(sum(sizes))},
+            "plain_loop_graphs_per_s": len(fqs) / plain_s, "speedup_vs_plain_loop": plain_s / dt,
+            "workers": workers, "autotune_graphs_per_s": {str(k): v for k, v in tune.items()},
+            "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
+            "bit_exact_vs_plain": exact}
+    print(json.dumps(line), flush=True)
+    for b in bufs:
+        b.free()
+
+
+def run_served(args):
+    """Config 4: Poisson arrivals of build-and-compact requests (samples up to 20 Mbp) admitted
+    to the pool as workers and memory free up; p50/p99 latency (arrival to result on the host)
+    and throughput at each arrival rate, against the plain path looped on the same GPU."""
+    import threading
+    import bruno_gb300 as bg
+    from bruno_gb300 import synth
+    samples = synth.sample_set(args.samples or 48, seed=4, max_genome=20_000_000)
+    fqs = [synth.make_fastq(w) for w in samples]
+    sizes = [fq.nbytes for fq in fqs]
+    bufs = _pinned_copies(bg, fqs)
+    cfg = bg.GraphConfig(k=31, thresh=bg.thresholds([2]), min_update=True)
+    _plain_loop(bg, cfg, bufs[:4], sizes[:4])
+    plain_s, plain = _plain_loop(bg, cfg, bufs, sizes)
+    pool = bg.Pool(cfg, workers=args.workers)
+    for t in [pool.submit(bufs[i].array[:sizes[i]]) for i in range(min(8, len(bufs)))]:
+        pool.wait(t)
+    rng = np.random.default_rng(5)
+    rates = {}
+    exact = True
+    for rate in args.rates:
+        n = max(20, min(args.requests, int(rate * args.seconds)))
+        order = rng.integers(0, len(fqs), n)
+        gaps = rng.exponential(1.0 / rate, n)
+        lat, got, lock = [], [], threading.Lock()
+
+        def collect(t, i, t_arr):
+            r = pool.wait(t)
+            done = time.perf_counter()
+            with lock:
+                lat.append(1e3 * (done - t_arr))
+                got.append((i, r))
+        waiters = []
+        t0 = time.perf_counter()
+        t_next = t0
+        for i, gap in zip(order, gaps):
+            t_next += gap
+            delay = t_next - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            t_arr = time.perf_counter()
+            tk = pool.submit(bufs[i].array[:sizes[i]])
+            th = threading.Thread(target=collect, args=(tk, int(i), t_arr))
+            th.start()
+            waiters.append(th)
+        for th in waiters:
+            th.join()
+        wall = time.perf_counter() - t0
+        lat.sort()
+        bad = [int(i) for i, r in got if not _same_as_plain(r, plain[i])]   # checked after the timed run
+        rates[str(rate)] = {"requests": n, "graphs_per_s": n / wall, "p50_ms": lat[len(lat) // 2],
+                            "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                            "statuses": sorted({r["status"] for _, r in got}), "mismatched": sorted(set(bad))}
+        exact = exact and not bad
+    pool.close()
+    best = max(v["graphs_per_s"] for v in rates.values())
+    line = {"metric": "graphs/s served", "value": best, "unit": "graphs/s", "n_gpus": 1, "higher_is_better": True,
+            "data": "synthetic (seeded generator, sample_set seed 4)",
+            "config": {"workload": f"served: Poisson arrivals, {len(fqs)} distinct requests (genome log-uniform "
+                                   "5 kbp-20 Mbp, 20-60x, 100-250 bp, 0.5-2% substitutions, k=31, -L 2), "
+                                   "admission by free HBM", "workers": args.workers},
+            "plain_loop_graphs_per_s": len(fqs) / plain_s, "rates": rates, "bit_exact_vs_plain": exact}
+    print(json.dumps(line), flush=True)
+    for b in bufs:
+        b.free()
+
+
 def main():
     args = parse_args()
     from bruno_gb300 import synth
+    if args.workload == "batched" and args.impl != "reference":
+        run_batched(args)
+        return
+    if args.workload == "served" and args.impl != "reference":
+        run_served(args)
+        return
     w = synth.WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, w)

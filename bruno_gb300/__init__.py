@@ -53,6 +53,13 @@ class _Sizes(ctypes.Structure):
                                                     ("table_partitions", ctypes.c_uint64)]
 
 
+class _PoolResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("worker", ctypes.c_int32), ("words", ctypes.c_int32), ("sizes", _Sizes),
+                ("n_chains", ctypes.c_uint64), ("n_chars", ctypes.c_uint64), ("reps", ctypes.POINTER(ctypes.c_uint64)),
+                ("offsets", ctypes.POINTER(ctypes.c_uint64)), ("chars", ctypes.POINTER(ctypes.c_char)),
+                ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double)]
+
+
 _lib: Optional[ctypes.CDLL] = None
 
 # every entry point of include/bruno_gb300.h
@@ -62,7 +69,8 @@ EXPORTS = (
     "bruno_extract_chains", "bruno_list_rank", "bruno_to_compressed_chains", "bruno_build_and_compact",
     "bruno_get_sizes", "bruno_copy_k2", "bruno_copy_filtered", "bruno_copy_nodes", "bruno_copy_ranked",
     "bruno_copy_chains", "bruno_host_alloc", "bruno_host_free", "bruno_phase_ms",
-    "bruno_count_biedges_noalloc",
+    "bruno_count_biedges_noalloc", "bruno_pool_create", "bruno_pool_submit", "bruno_pool_wait",
+    "bruno_pool_result_free", "bruno_pool_destroy",
 )
 
 
@@ -89,6 +97,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "bruno_host_alloc": [SZ, ctypes.POINTER(P)], "bruno_host_free": [P],
         "bruno_phase_ms": [P, ctypes.POINTER(ctypes.c_double), SZ],
         "bruno_count_biedges_noalloc": [I32, I32, P, P, SZ, P, P, P, SZ, PSZ, P],
+        "bruno_pool_create": [ctypes.POINTER(_Cfg), I32, U64, ctypes.POINTER(P)],
+        "bruno_pool_submit": [P, P, SZ, ctypes.POINTER(U64)],
+        "bruno_pool_wait": [P, U64, ctypes.POINTER(_PoolResult)], "bruno_pool_result_free": [ctypes.POINTER(_PoolResult)],
+        "bruno_pool_destroy": [P],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -371,3 +383,62 @@ class PinnedBuffer:
         if self.ptr:
             self.lib.bruno_host_free(ctypes.c_void_p(self.ptr))
             self.ptr = None
+
+
+class Pool:
+    """Many graph builds at once on one GPU (bruno_pool_*): `workers` host threads, each with its
+    own context and stream, run the whole plain path for submitted FASTQ buffers; every result
+    equals the plain path's for that input alone.  Submit a batch and wait for each ticket, or
+    submit requests as they arrive and wait for them when needed."""
+
+    def __init__(self, config: Optional[GraphConfig] = None, workers: int = 8, mem_budget: int = 0, **kw):
+        self.lib = load_library()
+        self.config = config or GraphConfig(**kw)
+        c = self.config.to_c()
+        self.pool = ctypes.c_void_p()
+        st = self.lib.bruno_pool_create(ctypes.byref(c), workers, mem_budget, ctypes.byref(self.pool))
+        if st != 0:
+            raise BrunoError(st, "pool_create")
+        self._bufs = {}
+
+    def submit(self, data) -> int:
+        """queues one FASTQ (bytes or a uint8 host array, pinned for fast copies); the buffer is
+        kept alive here until its result is collected"""
+        arr = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8) if isinstance(data, (bytes, bytearray))
+                                   else data, dtype=np.uint8)
+        t = ctypes.c_uint64()
+        st = self.lib.bruno_pool_submit(self.pool, arr.ctypes.data_as(ctypes.c_void_p), arr.nbytes, ctypes.byref(t))
+        if st != 0:
+            raise BrunoError(st, "pool_submit")
+        self._bufs[t.value] = arr
+        return t.value
+
+    def wait(self, ticket: int) -> dict:
+        """the build's status, sizes, compacted chains (reps, offsets, chars) and timings"""
+        r = _PoolResult()
+        st = self.lib.bruno_pool_wait(self.pool, ticket, ctypes.byref(r))
+        self._bufs.pop(ticket, None)
+        if st != 0:
+            raise BrunoError(st, "pool_wait")
+        try:
+            out = {"status": r.status, "worker": r.worker, "queue_ms": r.queue_ms, "run_ms": r.run_ms}
+            if r.status == 0:
+                nc, nch, w = int(r.n_chains), int(r.n_chars), int(r.words)
+                out["sizes"] = {n: getattr(r.sizes, n) for n, _ in _Sizes._fields_ if n != "filter_flag_hist"}
+                out["chains"] = (np.ctypeslib.as_array(r.reps, (max(1, nc * w),))[:nc * w].reshape(nc, w).copy(),
+                                 np.ctypeslib.as_array(r.offsets, (nc + 1,)).copy(),
+                                 np.frombuffer(ctypes.string_at(r.chars, nch), np.uint8).copy())
+            return out
+        finally:
+            self.lib.bruno_pool_result_free(ctypes.byref(r))
+
+    def close(self) -> None:
+        if getattr(self, "pool", None):
+            self.lib.bruno_pool_destroy(self.pool)
+            self.pool = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -22,7 +22,7 @@ INCLUDE = os.path.join(REPO, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
-CUDA_SOURCES = ["build.cu", "chain.cu", "capi.cu"]
+CUDA_SOURCES = ["build.cu", "chain.cu", "capi.cu", "pool.cu"]
 
 
 def _nvcc() -> str:

@@ -1441,13 +1441,14 @@ __global__ void __launch_bounds__(1024) k_scan_single(const uint64_t *in, uint64
 }
 
 int num_sms() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
+  /* function-local statics below are initialised once, thread-safely (contexts may run on
+   * several host threads) */
+  static const int sms = [] {
+    int dev = 0, n = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+  }();
   return sms;
 }
 
@@ -1596,11 +1597,11 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
   cudaMemsetAsync(c->bucket_cnt.p, 0, NBUCKET * 8, c->stream);
   const int eb = std::max(1, std::min<int>(sms * 2, (int)((nreads + XTPB - 1) / XTPB)));
   if ((st = ensure(c, c->blk_cnt, (size_t)eb * HLL_M)) != BRUNO_OK) return st;
-  static bool attr = false;
-  if (!attr) {
+  static const bool attr = [] {
     cudaFuncSetAttribute(k_extract, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   cudaEventRecord(c->kev[0], c->stream);
   k_extract<<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p,
                                                           nreads, c->cfg.k, (uint64_t *)c->records.p, cap,
@@ -1614,12 +1615,12 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
   c->n_instances = c->hctr->n_instances;
   c->n_reads_used = c->hctr->n_reads_used;
   uint64_t slots = c->cfg.table_slots ? c->cfg.table_slots : slots_for(c, hll_estimate(c->hctr->hll));
-  static bool part_attr = false;
-  if (!part_attr) {
+  static const bool part_attr = [] {
     cudaFuncSetAttribute(k_count_local, cudaFuncAttributeMaxDynamicSharedMemorySize, PART_SLOTS * 32);
     cudaFuncSetAttribute(k_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SplitSmem));
-    part_attr = true;
-  }
+    return true;
+  }();
+  (void)part_attr;
   for (int attempt = 0; attempt < 4; ++attempt) {
     /* shared-memory path: 2^pb partitions (pb >= 8) small enough for one CTA's shared memory */
     int pb = NBUCKET_BITS;
@@ -1680,10 +1681,10 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
       if ((st = ensure(c, c->table, c->nslots * 32)) != BRUNO_OK) return st;
       cudaEventRecord(c->kev[2], c->stream);
       const int G = 1 << (NBUCKET_BITS - pt);
-      static int ins_occ = 0;   /* resident k_insert blocks per SM: one full wave per partition */
-      if (!ins_occ && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ins_occ, k_insert, TPB, 0) != cudaSuccess ||
-                       ins_occ < 1))
-        ins_occ = 4;
+      static const int ins_occ = [] {   /* resident k_insert blocks per SM: one full wave per partition */
+        int o = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_insert, TPB, 0) == cudaSuccess && o > 0 ? o : 4;
+      }();
       const int gx = std::max(1, (sms * ins_occ + G - 1) / G);
       for (int q = 0; q < (1 << pt); ++q) {
         k_part_init<KW1><<<sms * 2, TPB, 0, c->stream>>>((uint64_t *)c->table.p, (uint64_t)q * region, region);
@@ -1814,7 +1815,7 @@ bruno_status run_copy_nodes(Ctx *c, uint64_t *keys, uint16_t *counts, uint8_t *f
   if (r == BRUNO_OK && flags)
     r = cuda_check(c, cudaMemcpyAsync(flags, df.p, c->n_nodes, cudaMemcpyDeviceToHost, c->stream), "copy");
   if (r == BRUNO_OK) r = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
-  cudaFree(dk.p); cudaFree(dc.p); cudaFree(df.p);
+  cudaFreeAsync(dk.p, c->stream); cudaFreeAsync(dc.p, c->stream); cudaFreeAsync(df.p, c->stream);
   return r;
 }
 

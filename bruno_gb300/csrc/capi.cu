@@ -26,20 +26,20 @@ bruno_status cuda_check(Ctx *c, cudaError_t e, const char *what) {
                  std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+/* Buffers grow with 1/8 headroom, so a context reused for inputs of varying size rarely
+ * reallocates, and they are allocated and released in the order of the context's stream:
+ * growing never waits for the work of other contexts on the device. */
 bruno_status ensure(Ctx *c, Buf &b, size_t bytes, bool preserve) {
   if (bytes <= b.bytes && b.p) return BRUNO_OK;
   void *p = nullptr;
-  size_t want = std::max(bytes, (size_t)256);
-  cudaError_t e = cudaMalloc(&p, want);
+  size_t want = std::max(bytes + bytes / 8, (size_t)256);
+  cudaError_t e = cudaMallocAsync(&p, want, c->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
-    return set_err(c, BRUNO_ERR_OOM, "cudaMalloc of " + std::to_string(want) + " bytes failed");
+    return set_err(c, BRUNO_ERR_OOM, "device allocation of " + std::to_string(want) + " bytes failed");
   }
   if (preserve && b.p && b.bytes) cudaMemcpyAsync(p, b.p, b.bytes, cudaMemcpyDeviceToDevice, c->stream);
-  if (b.p) {
-    cudaStreamSynchronize(c->stream);
-    cudaFree(b.p);
-  }
+  if (b.p) cudaFreeAsync(b.p, c->stream);
   b.p = p;
   b.bytes = want;
   return BRUNO_OK;

@@ -643,13 +643,12 @@ __global__ void k_check_chains(const uint64_t *ch_off, const uint32_t *seen, uin
 }
 
 int sms_count() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
+  static const int sms = [] {
+    int dev = 0, n = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+  }();
   return sms;
 }
 
@@ -747,10 +746,10 @@ static bruno_status fast_list_rank(Ctx *c, bool &used) {
   const uint64_t R = c->hctr->lr_remaining, Rb = std::max<uint64_t>(1, R);
   if ((st = ensure(c, c->pay, Rb * 2 * sizeof(Jump) * 3)) != BRUNO_OK) return st;
   Jump *E0 = (Jump *)c->pay.p, *E = E0 + 2 * Rb, *F = E + 2 * Rb;
-  static int walk_occ = 0;   /* resident walk blocks per SM: the walks run as one wave */
-  if (!walk_occ && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&walk_occ, k_fast_walk, TPB, 0) != cudaSuccess ||
-                    walk_occ < 1))
-    walk_occ = 4;
+  static const int walk_occ = [] {   /* resident walk blocks per SM: the walks run as one wave */
+    int o = 0;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_fast_walk, TPB, 0) == cudaSuccess && o > 0 ? o : 4;
+  }();
   const int gw = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * walk_occ, (2 * R + TPB - 1) / TPB));
   k_fast_walk<<<gw, TPB, 0, c->stream>>>(cs, rnode, R, M, E0, c->dctr);
   c->launches += 1;

@@ -64,6 +64,24 @@ WORKLOADS = {
 }
 
 
+def sample_set(n: int, seed: int, max_genome: int = 2_000_000, min_genome: int = 5_000, k: int = 31,
+               lower: tuple = (2,)) -> list:
+    """Independent samples of uneven size for the batched and served forms: genome length
+    log-uniform in [min_genome, max_genome], coverage uniform in [20, 60]x, one read length per
+    sample uniform in 100..250 bp, substitutions uniform in [0.5%, 2%]; every sample has its own
+    seed.  (Batched: 256 samples up to 2 Mbp; served: the same shape up to 20 Mbp.)"""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        g = int(round(np.exp(rng.uniform(np.log(min_genome), np.log(max_genome)))))
+        cov = float(rng.uniform(20.0, 60.0))
+        L = int(rng.integers(100, 251))
+        sub = float(rng.uniform(0.005, 0.02))
+        out.append(Workload(f"sample{i}", g, L, max(1, int(round(cov * g / L))), sub, k, lower,
+                            seed=int(rng.integers(1, 2**31))))
+    return out
+
+
 def _lib() -> ctypes.CDLL:
     if not os.path.exists(_LIB):
         raise RuntimeError(f"synthetic generator not built: {_LIB}")

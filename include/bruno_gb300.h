@@ -173,6 +173,39 @@ bruno_status bruno_host_free(void *p);
 bruno_status bruno_phase_ms(bruno_ctx *ctx, double *ms, size_t n);
 
 /* ---------------------------------------------------------------------------------------
+ * Many builds at once.  No counterpart in the reference (one graph per MPI job there): a pool
+ * of `workers` host threads, each with its own context and stream, runs
+ * bruno_build_and_compact for submitted FASTQ buffers, so several small graphs share the GPU.
+ * Each result is exactly what the plain path gives for that input alone.  Batched use:
+ * submit every sample, then wait for each.  Served use: submit requests as they arrive; a
+ * request starts when a worker is free and its device-memory estimate (20 B per FASTQ byte +
+ * 64 MiB) fits `mem_budget` bytes (0 = 80% of the device memory free at creation) together with
+ * what the other workers hold; a request larger than the budget runs once no other is busy, and
+ * one that runs out of device memory beside others is retried once on its own.
+ * Buffers are host memory (pinned for fast copies) and must stay valid until the request's
+ * bruno_pool_wait returns.  The pool's functions may be called from several host threads. */
+typedef struct bruno_pool bruno_pool;
+typedef struct bruno_pool_result {
+  bruno_status status;      /* of the build */
+  int32_t worker;           /* worker that ran it */
+  int32_t words;            /* uint64 words per k-mer in reps */
+  bruno_sizes sizes;
+  uint64_t n_chains, n_chars;
+  uint64_t *reps;           /* n_chains x words: representative k-mer of each compacted chain */
+  uint64_t *offsets;        /* n_chains + 1 offsets into chars */
+  char *chars;              /* the chain sequences */
+  double queue_ms;          /* submit -> start on a worker */
+  double run_ms;            /* start -> result on the host */
+} bruno_pool_result;
+bruno_status bruno_pool_create(const bruno_cfg *cfg, int32_t workers, uint64_t mem_budget, bruno_pool **out);
+bruno_status bruno_pool_submit(bruno_pool *pool, const char *buf, size_t nbytes, uint64_t *ticket);
+/* Blocks until the request is done; the result's arrays belong to the caller. */
+bruno_status bruno_pool_wait(bruno_pool *pool, uint64_t ticket, bruno_pool_result *out);
+bruno_status bruno_pool_result_free(bruno_pool_result *result);
+/* Finishes every queued request, then stops the workers. */
+bruno_status bruno_pool_destroy(bruno_pool *pool);
+
+/* ---------------------------------------------------------------------------------------
  * Allocation-free pair counting.  This entry point has no counterpart in the reference; it
  * exists for callers that may not allocate device memory themselves or through this
  * library: a host application that has already handed the whole device to its own memory

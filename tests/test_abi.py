@@ -56,6 +56,32 @@ int main(void) {{
     assert got == want
 
 
+def test_pool_result_layout_matches_header(tmp_path):
+    src = tmp_path / "layout2.c"
+    src.write_text(f'''
+#include <stdio.h>
+#include <stddef.h>
+#include "{HEADER}"
+int main(void) {{
+  printf("%zu %zu %zu %zu %zu\\n", sizeof(bruno_pool_result), offsetof(bruno_pool_result, sizes),
+         offsetof(bruno_pool_result, n_chains), offsetof(bruno_pool_result, chars),
+         offsetof(bruno_pool_result, run_ms));
+  return 0;
+}}''')
+    exe = tmp_path / "layout2"
+    subprocess.run(["gcc", "-std=c99", "-o", str(exe), str(src)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    R = bg._PoolResult
+    assert got == [ctypes.sizeof(R), R.sizes.offset, R.n_chains.offset, R.chars.offset, R.run_ms.offset]
+
+
+def test_pool_bad_arguments_rejected_without_gpu(lib):
+    cfg = bg.GraphConfig().to_c()
+    h = ctypes.c_void_p()
+    assert lib.bruno_pool_create(ctypes.byref(cfg), 0, 0, ctypes.byref(h)) == 1
+    assert lib.bruno_pool_create(None, 4, 0, ctypes.byref(h)) == 1
+
+
 def test_bad_config_rejected_without_gpu(lib):
     """k outside 3..63 is refused before any CUDA call"""
     cfg = bg.GraphConfig(k=64).to_c()
