@@ -413,9 +413,11 @@ def main():
     step_e2e()
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2e_phases = []
     e0.record(stream)
     for _ in range(args.steps):
         step_e2e()
+        e2e_phases.append(g.phase_ms())
     e1.record(stream)
     barrier()
     ems = max_over_ranks(e0.elapsed_time(e1), world)
@@ -468,7 +470,11 @@ def main():
                 "config": dict(workload_config(w), api="bruno_build_and_compact" if args.api == "build"
                                else "step calls"),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n, "d2h_bytes_per_step": d2h,
-                        "ms_per_step": ems / args.steps},
+                        "ms_per_step": ems / args.steps,
+                        "h2d_ms": statistics.mean(p["h2d"] for p in e2e_phases),
+                        "device_ms": statistics.mean(sum(p[k] for k in ("parse", "count_k2mers", "filter_insert",
+                                                                        "chainmap", "list_rank", "compress"))
+                                                     for p in e2e_phases)},
                 "roofline": {"bound": "hbm", "kernel": top, "achieved": kernels[top]["achieved"], "peak": peak,
                              "unit": "GB/s", "frac": kernels[top]["frac"], "peak_source": peak_src,
                              "traffic": traffic, "alg_bytes_per_launch": kernels[top]["alg_bytes_per_launch"],

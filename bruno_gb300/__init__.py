@@ -295,7 +295,7 @@ class Graph:
         return d
 
     PHASES = ("parse", "count_k2mers", "filter_insert", "chainmap", "list_rank", "compress",
-              "count_estimate", "count_table_init", "count_insert", "count_split")
+              "count_estimate", "count_table_init", "count_insert", "count_split", "h2d")
 
     def phase_ms(self) -> dict:
         a = (ctypes.c_double * len(self.PHASES))()

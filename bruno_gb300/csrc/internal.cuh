@@ -75,6 +75,7 @@ struct Ctx {
   uint64_t nslots = 0, n_entries = 0, n_slots_claimed = 0;
   Buf records, bucket_cnt;       /* partitioned counting: 8-byte records per hash bucket */
   Buf records2, sub_cnt;         /* the same records split per table partition */
+  bool h2d_pending = false;      /* ev[7] marks the start of this build's host-to-device copies */
   int force_direct_count = 0;    /* cfg.direct_count: 0 automatic, 1 whole table, 2 L2 partitions */
   Buf chain_list, branch_list;   /* slot indices, filled by the filter */
 
@@ -102,7 +103,8 @@ struct Ctx {
 
   cudaEvent_t ev[8] = {nullptr};
   cudaEvent_t kev[5] = {nullptr};  /* counting sub-steps */
-  double phase_ms[10] = {0};       /* 6 phases, then estimate/extract, table init, count, split */
+  double phase_ms[11] = {0};       /* 6 phases, then estimate/extract, table init, count, split,
+                                      and the host-to-device copies of the FASTQ input */
   uint64_t launches = 0;           /* kernels launched since the last reset */
 };
 

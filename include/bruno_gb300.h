@@ -169,7 +169,8 @@ bruno_status bruno_host_free(void *p);
  * ms[6..9] = counting sub-steps: distinct-count estimate (with the record extraction on
  * the partitioned path), whole-table initialisation (direct path only), the counting
  * itself (split + per-partition counts, the L2 partition inserts, or k_count), and the
- * record split alone (shared-memory partition path only).  Writes min(n, 10) values. */
+ * record split alone (shared-memory partition path only); ms[10] = the host-to-device
+ * copies of FASTQ bytes given in host memory.  Writes min(n, 11) values. */
 bruno_status bruno_phase_ms(bruno_ctx *ctx, double *ms, size_t n);
 
 /* ---------------------------------------------------------------------------------------
