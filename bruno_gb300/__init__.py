@@ -68,7 +68,7 @@ EXPORTS = (
     "bruno_load_fastq", "bruno_compute_biedge_freqencies", "bruno_local_insert_by_freqencies",
     "bruno_extract_chains", "bruno_list_rank", "bruno_to_compressed_chains", "bruno_build_and_compact",
     "bruno_get_sizes", "bruno_copy_k2", "bruno_copy_filtered", "bruno_copy_nodes", "bruno_copy_ranked",
-    "bruno_copy_chains", "bruno_host_alloc", "bruno_host_free", "bruno_phase_ms",
+    "bruno_copy_chains", "bruno_copy_chain_edges", "bruno_host_alloc", "bruno_host_free", "bruno_phase_ms",
     "bruno_count_biedges_noalloc", "bruno_pool_create", "bruno_pool_submit", "bruno_pool_wait",
     "bruno_pool_result_free", "bruno_pool_destroy",
 )
@@ -94,6 +94,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "bruno_copy_k2": [P, P, P, P, SZ, PSZ], "bruno_copy_filtered": [P, P, P, P, SZ, PSZ],
         "bruno_copy_nodes": [P, P, P, P, SZ, PSZ], "bruno_copy_ranked": [P, P, P, P, SZ, PSZ],
         "bruno_copy_chains": [P, P, P, P, SZ, SZ, PSZ, PSZ],
+        "bruno_copy_chain_edges": [P, P, P, SZ, PSZ],
         "bruno_host_alloc": [SZ, ctypes.POINTER(P)], "bruno_host_free": [P],
         "bruno_phase_ms": [P, ctypes.POINTER(ctypes.c_double), SZ],
         "bruno_count_biedges_noalloc": [I32, I32, P, P, SZ, P, P, P, SZ, PSZ, P],
@@ -360,6 +361,20 @@ class Graph:
                                                    nc.value, chars.size, ctypes.byref(nc), ctypes.byref(nch)),
                         "copy_chains")
         return reps, offs, chars[:nch.value]
+
+    def chain_edges(self):
+        """print_chain_frequencies records, sorted by L as the reference prints them:
+        L (n, words), R (n, words), freqs (n, 11) = L in ACGT, R out ACGT, mean, min, max"""
+        n = ctypes.c_size_t()
+        self._check(self.lib.bruno_copy_chain_edges(self.ctx, None, None, 0, ctypes.byref(n)), "copy_chain_edges")
+        ends = np.zeros((n.value, 2, self.words), np.uint64)
+        freqs = np.zeros((n.value, 11), np.uint16)
+        if n.value:
+            self._check(self.lib.bruno_copy_chain_edges(self.ctx, self._ptr(ends), self._ptr(freqs), n.value,
+                                                        ctypes.byref(n)), "copy_chain_edges")
+        L, R = ends[:, 0, :], ends[:, 1, :]
+        order = np.lexsort(tuple(L[:, w] for w in range(self.words)))   # last key = high word first
+        return L[order], R[order], freqs[order]
 
     def chain_strings(self) -> list[str]:
         reps, offs, chars = self.chains()

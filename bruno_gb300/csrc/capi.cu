@@ -106,7 +106,7 @@ bruno_status bruno_ctx_destroy(bruno_ctx *c) {
   Buf *bufs[] = {&c->rstart, &c->rend, &c->tile_cnt, &c->tile_base, &c->table, &c->k2_keys, &c->k2_edges, &c->k2_counts,
                  &c->f_keys, &c->f_edges, &c->f_counts, &c->blk_cnt, &c->blk_base, &c->ckey, &c->cedge,
                  &c->cstate, &c->cstate2, &c->pend, &c->pay, &c->unf0, &c->unf1, &c->removed, &c->r_K, &c->r_rep, &c->r_dist,
-                 &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list,
+                 &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list, &c->e_ends, &c->e_freqs,
                  &c->records, &c->bucket_cnt, &c->records2, &c->sub_cnt};
   for (Buf *b : bufs) release(*b);
   for (Buf &b : c->seg_bufs) release(b);
@@ -148,6 +148,8 @@ bruno_status bruno_reset(bruno_ctx *c) {
   c->iterations = c->n_cycle = c->n_isolated = c->multi = 0;
   c->n_ranked = c->n_heads = c->n_chain_chars = 0;
   c->chains_clean = true;
+  c->n_chain_edges = 0;
+  c->chain_edges_done = false;
   c->launches = 0;
   std::memset(c->flag_hist, 0, sizeof(c->flag_hist));
   std::memset(c->phase_ms, 0, sizeof(c->phase_ms));
@@ -350,6 +352,20 @@ bruno_status bruno_copy_chains(bruno_ctx *c, uint64_t *reps, uint64_t *offsets, 
   bruno_status st = copy_d2h(c, reps, c->ch_rep.p, c->n_heads * 8 * c->W);
   if (st == BRUNO_OK) st = copy_d2h(c, offsets, c->head_off.p, (c->n_heads + 1) * 8);
   if (st == BRUNO_OK) st = copy_d2h(c, chars, c->ch_chars.p, c->n_chain_chars);
+  if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  return st;
+}
+
+bruno_status bruno_copy_chain_edges(bruno_ctx *c, uint64_t *ends, uint16_t *freqs, size_t cap, size_t *n) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (c->stage < 6) return set_err(c, BRUNO_ERR_ARG, "chain edges exist after to_compressed_chains");
+  bruno_status st = BRUNO_OK;
+  if (!c->chain_edges_done && (st = run_chain_edges(c)) != BRUNO_OK) return st;
+  if (n) *n = c->n_chain_edges;
+  if (!ends && !freqs) return BRUNO_OK;
+  if (cap < c->n_chain_edges) return set_err(c, BRUNO_ERR_CAPACITY, "copy buffer too small");
+  st = copy_d2h(c, ends, c->e_ends.p, c->n_chain_edges * 2 * 8 * c->W);
+  if (st == BRUNO_OK) st = copy_d2h(c, freqs, c->e_freqs.p, c->n_chain_edges * 11 * 2);
   if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
   return st;
 }

@@ -20,6 +20,9 @@
  *                        to_compressed_chains (debruijn_chain_graph.hpp:1778-1856): every
  *                        chain is one head node with distance 0 plus one base per node, so
  *                        the sequence is scattered straight to its offset, no sort.
+ *  k_chain_freq /        compute_freq_map and print_chain_frequencies
+ *  k_chain_edges         (compact_dbg_stats.hpp:783-816, 879-1065), on demand: the chain
+ *                        ends' edge counts and each chain's node-frequency summary
  */
 #include <cuda_runtime.h>
 
@@ -642,6 +645,95 @@ __global__ void k_check_chains(const uint64_t *ch_off, const uint32_t *seen, uin
       atomicOr(&ctr->err, (unsigned long long)DERR_UNCLEAN_CHAINS);
 }
 
+/* ================================================================ chain end edges */
+/* compute_freq_map (compact_dbg_stats.hpp:783-816) per chain-map node: every listranked node
+ * adds its self frequency (count, sum, min, max; freq_summary, debruijn_chain_operations.hpp:
+ * 447-459) under the canonical k-mer of its representative.  That k-mer is the chain-map node
+ * rep_idx names; a representative reached through an external pointer is looked up in the
+ * table, and one that is no chain node is dropped, since only chain-map nodes' summaries are
+ * ever read. */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_chain_freq(EmitArgs a, const uint64_t *table, TableGeom g, uint32_t max_probe,
+                                                     const uint32_t *chain_list, unsigned long long *sum,
+                                                     uint32_t *cnt, uint32_t *mn, uint32_t *mx) {
+  constexpr int SU = Slot<KT>::U64, KWD = KOps<KT>::WORDS;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.M; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (a.removed[i]) continue;
+    uint32_t t = a.rep_idx[i];
+    if (t == NONE32) {
+      const ChainState st = a.cs[i];
+      const KT key = KOps<KT>::load(a.ckey + i * KWD);
+      const KT L = term(st.inD) ? key : ptr_kmer<KT>(st.inP, a.ckey, a.cedge, a.k);
+      const KT R = KOps<KT>::rc(term(st.outD) ? key : ptr_kmer<KT>(st.outP, a.ckey, a.cedge, a.k), a.k);
+      const KT rep = KOps<KT>::le(L, R) ? L : R, y = KOps<KT>::rc(rep, a.k);
+      const long long j = table_find<KT>(table, g, max_probe, KOps<KT>::le(rep, y) ? rep : y);
+      if (j < 0 || !(slot_flags<KT>(table + j * SU) & NF_CHAIN)) continue;
+      t = slot_aux<KT>(table + j * SU);
+      if (t >= a.M) continue;
+    }
+    const uint32_t f = (uint32_t)(table[(uint64_t)chain_list[i] * SU + KWD + 2] & 0xFFFFu);
+    atomicAdd(&sum[t], (unsigned long long)f);
+    atomicAdd(&cnt[t], 1u);
+    atomicMin(&mn[t], f);
+    atomicMax(&mx[t], f);
+  }
+}
+
+/* print_chain_frequencies (compact_dbg_stats.hpp:879-1065): one record per chain-map node that
+ * IsCanonicalTerminusOrIsolated (debruijn_chain_filters.hpp:125-147) accepts.  L and R are the
+ * chain's ends on one strand (:947-962); L's in-edges (A C G T) come from the canonical k-mer's
+ * in-counters, or its out-counters T G C A when L is not canonical, and R's out-edges the other
+ * way round (:973-1007); the summary is the one of canonical(L), which is this node, with the
+ * mean (float)sum / (float)count truncated to the count type (:1009-1013).  An R that is not a
+ * graph node (only in chains whose pointers are not mutually consistent) gets zero counts. */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_chain_edges(EmitArgs a, const uint64_t *table, TableGeom g, uint32_t max_probe,
+                                                      const uint32_t *chain_list, const unsigned long long *sum,
+                                                      const uint32_t *cnt, const uint32_t *mn, const uint32_t *mx,
+                                                      uint64_t *ends, uint16_t *freqs, unsigned long long *n_out) {
+  constexpr int SU = Slot<KT>::U64, KWD = KOps<KT>::WORDS;
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < a.M; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    bool sel = false;
+    KT L{}, R{};
+    if (i < a.M && a.removed[i] == 0) {
+      const ChainState st = a.cs[i];
+      const KT K = KOps<KT>::load(a.ckey + i * KWD);
+      const bool ti = term(st.inD), to = term(st.outD);
+      if (ti && to) {
+        sel = true; L = K; R = K;
+      } else if (ti) {
+        const KT o = ptr_kmer<KT>(st.outP, a.ckey, a.cedge, a.k);
+        sel = KOps<KT>::le(K, KOps<KT>::rc(o, a.k)); L = K; R = o;
+      } else if (to) {
+        const KT in = ptr_kmer<KT>(st.inP, a.ckey, a.cedge, a.k), rk = KOps<KT>::rc(K, a.k);
+        sel = KOps<KT>::lt(rk, in); L = rk; R = KOps<KT>::rc(in, a.k);
+      }
+    }
+    const unsigned long long o = warp_append(sel, n_out);
+    if (!sel) continue;
+    uint16_t f[11];
+    const uint64_t *pl = table + (uint64_t)chain_list[i] * SU + KWD;   /* canonical(L) is this node */
+    const bool lc = KOps<KT>::le(L, KOps<KT>::rc(L, a.k));
+    for (int b = 0; b < 4; ++b) f[b] = lc ? (uint16_t)(pl[1] >> (16 * b)) : (uint16_t)(pl[0] >> (16 * (3 - b)));
+    const KT yR = KOps<KT>::rc(R, a.k);
+    const bool rcn = KOps<KT>::le(R, yR);
+    const long long j = table_find<KT>(table, g, max_probe, rcn ? R : yR);
+    for (int b = 0; b < 4; ++b) {
+      if (j < 0) { f[4 + b] = 0; continue; }
+      const uint64_t *pr = table + (uint64_t)j * SU + KWD;
+      f[4 + b] = rcn ? (uint16_t)(pr[0] >> (16 * b)) : (uint16_t)(pr[1] >> (16 * (3 - b)));
+    }
+    const uint32_t c = cnt[i];
+    f[8] = c ? (uint16_t)__float2uint_rz(__fdiv_rn(__ull2float_rn(sum[i]), __ull2float_rn((unsigned long long)c))) : 0;
+    f[9] = c ? (uint16_t)mn[i] : 0;
+    f[10] = c ? (uint16_t)mx[i] : 0;
+    KOps<KT>::store(ends + o * 2 * KWD, L);
+    KOps<KT>::store(ends + o * 2 * KWD + KWD, R);
+    for (int q = 0; q < 11; ++q) freqs[o * 11 + q] = f[q];
+  }
+}
+
 int sms_count() {
   static const int sms = [] {
     int dev = 0, n = 0;
@@ -719,6 +811,41 @@ bruno_status compress_typed(Ctx *c) {
   k_check_chains<<<sms * 2, TPB, 0, c->stream>>>((const uint64_t *)c->head_off.p, seen, nh, c->cfg.k, c->dctr);
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   c->chains_clean = !(c->hctr->err & DERR_UNCLEAN_CHAINS);
+  return BRUNO_OK;
+}
+
+template <class KT>
+bruno_status chain_edges_typed(Ctx *c) {
+  bruno_status st;
+  const uint64_t M = c->n_chain, Mb = std::max<uint64_t>(1, M);
+  const int KWD = Slot<KT>::KEYW;
+  if ((st = ensure(c, c->e_ends, Mb * 2 * 8 * KWD)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->e_freqs, Mb * 11 * 2)) != BRUNO_OK) return st;
+  Buf acc;   /* per chain-map node: sum (u64), then count, min, max (u32) */
+  if ((st = ensure(c, acc, Mb * 20)) != BRUNO_OK) return st;
+  unsigned long long *sum = (unsigned long long *)acc.p;
+  uint32_t *cnt = (uint32_t *)(sum + Mb), *mn = cnt + Mb, *mx = mn + Mb;
+  cudaMemsetAsync(sum, 0, Mb * 12, c->stream);   /* sum and count */
+  cudaMemsetAsync(mn, 0xFF, Mb * 4, c->stream);
+  cudaMemsetAsync(mx, 0, Mb * 4, c->stream);
+  cudaMemsetAsync(&c->dctr->n_chain_edges, 0, 8, c->stream);
+  EmitArgs a{};
+  a.ckey = (const uint64_t *)c->ckey.p; a.cedge = (const uint8_t *)c->cedge.p; a.cs = (const ChainState *)c->cstate.p;
+  a.removed = (const uint8_t *)c->removed.p; a.M = M; a.k = c->cfg.k;
+  a.rep_idx = (uint32_t *)c->rep_idx.p;
+  const int sms = sms_count();
+  const uint64_t *table = (const uint64_t *)c->table.p;
+  const uint32_t *cl = (const uint32_t *)c->chain_list.p;
+  k_chain_freq<KT><<<sms * 8, TPB, 0, c->stream>>>(a, table, c->geom, 4096u, cl, sum, cnt, mn, mx);
+  k_chain_edges<KT><<<sms * 8, TPB, 0, c->stream>>>(a, table, c->geom, 4096u, cl, sum, cnt, mn, mx,
+                                                    (uint64_t *)c->e_ends.p, (uint16_t *)c->e_freqs.p,
+                                                    &c->dctr->n_chain_edges);
+  c->launches += 2;
+  st = sync_counters(c);
+  cudaFreeAsync(acc.p, c->stream);
+  if (st != BRUNO_OK) return st;
+  c->n_chain_edges = c->hctr->n_chain_edges;
+  c->chain_edges_done = true;
   return BRUNO_OK;
 }
 
@@ -850,5 +977,7 @@ bruno_status run_list_rank(Ctx *c, int min_update) {
 }
 
 bruno_status run_compress(Ctx *c) { return c->W == 1 ? compress_typed<KW1>(c) : compress_typed<KW2>(c); }
+
+bruno_status run_chain_edges(Ctx *c) { return c->W == 1 ? chain_edges_typed<KW1>(c) : chain_edges_typed<KW2>(c); }
 
 }  // namespace bg

@@ -14,8 +14,9 @@
  *
  * Outputs: <prefix>.chain.fasta (print_chain_string, compact_dbg_io.hpp:323-363),
  * <prefix>.chain.components (print_chain_nodes, :463-498), <prefix>.branch.fasta
- * (print_branch_fasta, :254-299), and unless -B <prefix>.branch.edges
- * (print_branch_edge_frequencies, compact_dbg_stats.hpp:219-262) and <prefix>.graph.all.
+ * (print_branch_fasta, :254-299), and unless -B <prefix>.chain.edges
+ * (print_chain_frequencies, compact_dbg_stats.hpp:879-1065), <prefix>.branch.edges
+ * (print_branch_edge_frequencies, :219-262) and <prefix>.graph.all.
  * Like the reference, records are sorted before printing; the .chain.fasta has no newline
  * before its first record and none after its last.
  */
@@ -177,6 +178,22 @@ int main(int argc, char **argv) {
               std::to_string(ranked.dist[i]) + "\t" + (K == c ? "1" : "0") + "\n";
       }
       if (!write(prefix + ".chain.components", cc)) return 1;
+      /* .chain.edges: sorted by L; every value is followed by a tab */
+      std::vector<uint64_t> ends;
+      std::vector<uint16_t> ef;
+      const size_t ne = chainmap.chain_edges(ends, ef);
+      std::vector<size_t> eo(ne);
+      std::iota(eo.begin(), eo.end(), 0);
+      std::sort(eo.begin(), eo.end(), [&](size_t a, size_t b) {
+        return load(&ends[a * 2 * words], words) < load(&ends[b * 2 * words], words);
+      });
+      std::string ce;
+      for (size_t i : eo) {
+        ce += ascii(load(&ends[i * 2 * words], words), k) + "\t" + ascii(load(&ends[i * 2 * words + words], words), k);
+        for (int j = 0; j < 11; ++j) ce += "\t" + std::to_string(ef[i * 11 + j]);
+        ce += "\t\n";
+      }
+      if (!write(prefix + ".chain.edges", ce)) return 1;
     }
     /* nodes sorted by k-mer: .branch.fasta, .branch.edges, .graph.all */
     std::vector<size_t> nord(nflags.size());

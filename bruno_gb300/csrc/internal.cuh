@@ -33,6 +33,7 @@ struct DevCounters {
   unsigned long long lr_applied, lr_remaining, lr_cycles, lr_multi;
   unsigned long long n_cycle, n_isolated, n_ranked, n_heads, n_chain_chars;
   unsigned long long n_upper;          /* k-mer positions of all reads long enough */
+  unsigned long long n_chain_edges;    /* chain-end records appended */
   unsigned int hll[1 << 12];           /* HyperLogLog registers, p = 12 */
 };
 
@@ -100,6 +101,9 @@ struct Ctx {
   Buf r_K, r_rep, r_dist, rep_idx, head_of, heads, head_len, head_off, ch_rep, ch_off, ch_chars;
   uint64_t n_ranked = 0, n_heads = 0, n_chain_chars = 0;
   bool chains_clean = true;
+  Buf e_ends, e_freqs;           /* chain-end records (L, R; 11 counts each), built on demand */
+  uint64_t n_chain_edges = 0;
+  bool chain_edges_done = false;
 
   cudaEvent_t ev[8] = {nullptr};
   cudaEvent_t kev[5] = {nullptr};  /* counting sub-steps */
@@ -125,6 +129,7 @@ bruno_status run_filter(Ctx *c, const uint64_t *thresh);
 bruno_status run_extract_chains(Ctx *c);
 bruno_status run_list_rank(Ctx *c, int min_update);
 bruno_status run_compress(Ctx *c);
+bruno_status run_chain_edges(Ctx *c);
 bruno_status run_copy_nodes(Ctx *c, uint64_t *keys, uint16_t *counts, uint8_t *flags, size_t cap, size_t *n);
 
 }  // namespace bg

@@ -159,6 +159,16 @@ bruno_status bruno_copy_ranked(bruno_ctx *ctx, uint64_t *K, uint64_t *rep, int32
 /* Compacted chains: representative k-mer per chain, offsets[n_chains + 1] into `chars`. */
 bruno_status bruno_copy_chains(bruno_ctx *ctx, uint64_t *reps, uint64_t *offsets, char *chars,
                                size_t cap_chains, size_t cap_chars, size_t *n_chains, size_t *n_chars);
+/* Chain end edges and frequency summaries, the records print_chain_frequencies
+ * (test/common/compact_dbg_stats.hpp:879-1065) prints to <prefix>.chain.edges, with the
+ * summaries of compute_freq_map (:783-816).  One record per chain-map node that
+ * IsCanonicalTerminusOrIsolated (src/debruijn/debruijn_chain_filters.hpp:125-147) accepts:
+ * ends[2 * words] = L then R, the chain's two ends on one strand; freqs[11] = L's in-edge
+ * counts A C G T, R's out-edge counts A C G T, then the mean (float sum / float count,
+ * truncated), min and max of the self frequencies of the chain's nodes.  Records come in no
+ * particular order (the reference sorts them by L before printing).  Computed on the device at
+ * the first call after bruno_to_compressed_chains, which may pass NULL buffers to query n. */
+bruno_status bruno_copy_chain_edges(bruno_ctx *ctx, uint64_t *ends, uint16_t *freqs, size_t cap, size_t *n);
 
 /* Page-locked host memory, for fast host<->device copies of FASTQ input and results. */
 bruno_status bruno_host_alloc(size_t bytes, void **out);

@@ -163,6 +163,17 @@ class debruijn_chain_graph {
     }
     return out;
   }
+  /* print_chain_frequencies' records (compact_dbg_stats.hpp:879-1065), unordered:
+   * ends = L, R per record (2 * words), freqs = 11 per record */
+  size_t chain_edges(std::vector<uint64_t> &ends, std::vector<uint16_t> &freqs) {
+    compress();
+    size_t n = 0;
+    check(bruno_copy_chain_edges(c_.get(), nullptr, nullptr, 0, &n), c_.get(), "copy_chain_edges");
+    ends.resize(n * 2 * c_.words());
+    freqs.resize(n * 11);
+    check(bruno_copy_chain_edges(c_.get(), ends.data(), freqs.data(), n, &n), c_.get(), "copy_chain_edges");
+    return n;
+  }
 
  private:
   size_t rank(int min_update) {

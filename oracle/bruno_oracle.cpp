@@ -768,6 +768,85 @@ struct Run {
     res->seconds[ORACLE_T_COMPRESS] = now() - t0;
   }
 
+  /* ================================================== chain end edges
+   * The records print_chain_frequencies (compact_dbg_stats.hpp:879-1065) prints, with the
+   * frequency summaries of compute_freq_map (:783-816):
+   *   - freq_map: every listranked node adds (1, f, f, f) under its chain representative,
+   *     f = get_self_frequency of its canonical k-mer; keys are canonical
+   *     (CanonicalHashMapParams), summaries reduce as freq_summary
+   *     (debruijn_chain_operations.hpp:447-459): count and sum add, min, max;
+   *   - chain_rep: the chain-map nodes IsCanonicalTerminusOrIsolated accepts
+   *     (debruijn_chain_filters.hpp:125-147);
+   *   - per selected node, L and R on one strand (:947-962), L's in-edges and R's out-edges
+   *     taken from the canonical k-mer's counters, reversed and complemented when the end is
+   *     not canonical (:973-1007), and the summary of canonical(L) with the mean as
+   *     (float)sum / (float)count stored in the count type (:1009-1013);
+   *   - records sorted by L (:1019-1029).
+   * A chain end that is not a graph node (possible only when chain pointers are not mutually
+   * consistent) gets zero counts, where the reference's lookup would fail. */
+  struct FreqSum { uint64_t count = 0, sum = 0; uint16_t mn = 0xFFFF, mx = 0; };
+  struct EdgeRec { W L, R; uint16_t f[11]; };
+
+  const Node *node_of(W canon) { return nodes[shard(canon)].find(KmerKey<W>{canon}); }
+  W canon_of(W x) const { W y = ko.rc(x); return x < y ? x : y; }
+
+  void chain_edges() {
+    OAMap<KmerKey<W>, FreqSum> freq;
+    for (int s = 0; s < T; ++s)
+      for (size_t i = 0; i < chain[s].keys.size(); ++i) {
+        if (chain[s].state[i] != 1) continue;
+        const W key = chain[s].keys[i].v;
+        const ChainNode<W> &x = chain[s].vals[i];
+        const W L = is_chain_terminal(x.inD) ? key : x.inK;
+        const W R = is_chain_terminal(x.outD) ? ko.rc(key) : ko.rc(x.outK);
+        const W rep = L <= R ? L : R;
+        const Node *nd = node_of(key);
+        const uint16_t f = nd ? nd->c[8] : 0;
+        bool ins;
+        FreqSum &q = freq.get(KmerKey<W>{canon_of(rep)}, &ins);
+        q.count += 1; q.sum += f;
+        q.mn = std::min(q.mn, f); q.mx = std::max(q.mx, f);
+      }
+    std::vector<EdgeRec> out;
+    for (int s = 0; s < T; ++s)
+      for (size_t i = 0; i < chain[s].keys.size(); ++i) {
+        if (chain[s].state[i] != 1) continue;
+        const W K = chain[s].keys[i].v;
+        const ChainNode<W> &x = chain[s].vals[i];
+        const bool ti = is_chain_terminal(x.inD), to = is_chain_terminal(x.outD);
+        EdgeRec e;
+        if (ti && to) { e.L = K; e.R = K; }
+        else if (ti) { if (!(K <= ko.rc(x.outK))) continue; e.L = K; e.R = x.outK; }
+        else if (to) { if (!(ko.rc(K) < x.inK)) continue; e.L = ko.rc(K); e.R = ko.rc(x.inK); }
+        else continue;
+        const W cL = canon_of(e.L), cR = canon_of(e.R);
+        const Node *nl = node_of(cL), *nr = node_of(cR);
+        for (int b = 0; b < 4; ++b) {
+          e.f[b] = !nl ? 0 : (cL == e.L ? nl->c[4 + b] : nl->c[3 - b]);
+          e.f[4 + b] = !nr ? 0 : (cR == e.R ? nr->c[b] : nr->c[7 - b]);
+        }
+        const FreqSum *q = freq.find(KmerKey<W>{cL});
+        if (q && q->count) {
+          e.f[8] = (uint16_t)(static_cast<float>(q->sum) / static_cast<float>(q->count));
+          e.f[9] = q->mn; e.f[10] = q->mx;
+        } else {
+          e.f[8] = e.f[9] = e.f[10] = 0;
+        }
+        out.push_back(e);
+      }
+    std::sort(out.begin(), out.end(), [](const EdgeRec &a, const EdgeRec &b) { return a.L < b.L; });
+    const int w = res->words;
+    res->n_chain_edges = out.size();
+    res->edge_L = (uint64_t *)calloc(out.size() * w + 1, 8);
+    res->edge_R = (uint64_t *)calloc(out.size() * w + 1, 8);
+    res->edge_freqs = (uint16_t *)calloc(out.size() * 11 + 1, 2);
+    for (size_t i = 0; i < out.size(); ++i) {
+      store_word(res->edge_L + i * w, out[i].L, w);
+      store_word(res->edge_R + i * w, out[i].R, w);
+      memcpy(res->edge_freqs + i * 11, out[i].f, 22);
+    }
+  }
+
   /* ====================================================== table outputs */
   void export_tables() {
     const int w = res->words;
@@ -825,6 +904,7 @@ struct Run {
     extract_chains();
     list_rank();
     emit();
+    chain_edges();
     export_tables();
     return 0;
   }
@@ -875,6 +955,7 @@ extern "C" void oracle_free(oracle_result *r) {
   free(r->node_keys); free(r->node_counts); free(r->node_flags);
   free(r->ranked_K); free(r->ranked_rep); free(r->ranked_dist);
   free(r->chain_rep); free(r->chain_offsets); free(r->chain_chars);
+  free(r->edge_L); free(r->edge_R); free(r->edge_freqs);
   free(r);
 }
 
@@ -939,6 +1020,21 @@ extern "C" int oracle_write_outputs(const oracle_result *r, int32_t k, const cha
       s += std::to_string(r->ranked_dist[i]); s += "\t"; s += is_canon(K) ? "1" : "0"; s += "\n";
     }
     FILE *f = fopen((p + ".chain.components").c_str(), "wb");
+    if (!f) return 1;
+    fwrite(s.data(), 1, s.size(), f);
+    fclose(f);
+  }
+  /* .chain.edges: print_chain_frequencies (compact_dbg_stats.hpp:1034-1057), each value
+   * followed by a tab, records already sorted by L. */
+  if (!benchmark) {
+    std::string s;
+    for (size_t i = 0; i < r->n_chain_edges; ++i) {
+      s += ascii_words(r->edge_L + i * w, k, w); s += "\t";
+      s += ascii_words(r->edge_R + i * w, k, w); s += "\t";
+      for (int j = 0; j < 11; ++j) { s += std::to_string(r->edge_freqs[i * 11 + j]); s += "\t"; }
+      s += "\n";
+    }
+    FILE *f = fopen((p + ".chain.edges").c_str(), "wb");
     if (!f) return 1;
     fwrite(s.data(), 1, s.size(), f);
     fclose(f);

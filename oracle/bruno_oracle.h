@@ -77,6 +77,12 @@ typedef struct oracle_result {
   uint64_t *chain_offsets;  /* n_chains + 1 offsets into chain_chars */
   char *chain_chars;        /* concatenated chain sequences (to_compressed_chains strings) */
 
+  uint64_t n_chain_edges;   /* print_chain_frequencies records, one per chain, sorted by L */
+  uint64_t *edge_L;         /* chain end on the representative's strand (the selected terminus) */
+  uint64_t *edge_R;         /* the other end, same strand */
+  uint16_t *edge_freqs;     /* 11 per record: L in-edges A C G T, R out-edges A C G T,
+                               mean, min, max of the chain's node frequencies */
+
   double seconds[ORACLE_T_NUM];
 } oracle_result;
 
@@ -86,7 +92,7 @@ void oracle_free(oracle_result *r);
 
 /* Writes the reference driver's text outputs for a finished run:
  * <prefix>.chain.fasta, <prefix>.chain.components, <prefix>.branch.fasta and, unless
- * benchmark != 0, <prefix>.branch.edges and <prefix>.graph.all. */
+ * benchmark != 0, <prefix>.chain.edges, <prefix>.branch.edges and <prefix>.graph.all. */
 int oracle_write_outputs(const oracle_result *r, int32_t k, const char *prefix, int32_t benchmark);
 
 #ifdef __cplusplus

@@ -42,6 +42,8 @@ class _Res(ctypes.Structure):
         ("ranked_dist", ctypes.POINTER(ctypes.c_int32)),
         ("n_chains", ctypes.c_uint64), ("chain_rep", _U64P), ("chain_offsets", _U64P),
         ("chain_chars", ctypes.POINTER(ctypes.c_char)),
+        ("n_chain_edges", ctypes.c_uint64), ("edge_L", _U64P), ("edge_R", _U64P),
+        ("edge_freqs", ctypes.POINTER(ctypes.c_uint16)),
         ("seconds", ctypes.c_double * 6),
     ]
 
@@ -134,6 +136,9 @@ def run(fastq, k: int = 31, thresholding: bool = True, thresh=None, min_update: 
         nchars = int(offs[-1])
         chars = ctypes.string_at(r.chain_chars, nchars) if nchars else b""
         out["chains"] = (_arr(r.chain_rep, r.n_chains * w, np.uint64, (r.n_chains, w)), offs, chars)
+        ne = r.n_chain_edges
+        out["chain_edges"] = (_arr(r.edge_L, ne * w, np.uint64, (ne, w)), _arr(r.edge_R, ne * w, np.uint64, (ne, w)),
+                              _arr(r.edge_freqs, ne * 11, np.uint16, (ne, 11)))
         if write_prefix:
             lib.oracle_write_outputs(rp, k, write_prefix.encode(), int(benchmark))
         return out

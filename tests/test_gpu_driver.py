@@ -20,7 +20,7 @@ CASES = [
     ("debruijn.bubble.fastq", ["-T", "-L", "1", "-L", "2", "-L", "1", "-R"]),
     ("natural.withN.fastq", []),
 ]
-OUTPUTS = [".chain.fasta", ".chain.components", ".branch.fasta", ".branch.edges", ".graph.all"]
+OUTPUTS = [".chain.fasta", ".chain.components", ".chain.edges", ".branch.fasta", ".branch.edges", ".graph.all"]
 
 
 @pytest.mark.parametrize("fname,flags", CASES)

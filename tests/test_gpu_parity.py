@@ -33,7 +33,7 @@ def gpu_run(data, k, thr_on, thresh, mu, files=None, **kw):
     it = g.list_rank_min_update() if mu else g.list_rank()
     g.to_compressed_chains()
     out = dict(sizes=g.sizes(), k2=k2, filtered=g.filtered(), nodes=g.nodes(), ranked=g.ranked(),
-               chains=g.chains(), iterations=it)
+               chains=g.chains(), chain_edges=g.chain_edges(), iterations=it)
     g.close()
     return out
 
@@ -50,6 +50,7 @@ def compare(gpu, ref):
     assert_same(sort_nodes(*gpu["nodes"]), ref["nodes"], "graph nodes")
     assert_same(sort_ranked(*gpu["ranked"]), ref["ranked"], "listranked chain nodes")
     assert chain_set(*gpu["chains"]) == chain_set(*ref["chains"]), "compacted chains"
+    assert_same(gpu["chain_edges"], ref["chain_edges"], "chain end edges")
 
 
 PATHS = {"fast": {}, "round_sync": {"exact_ranking": True}, "direct_count": {"direct_count": 1},
@@ -71,7 +72,7 @@ def one_call_run(data, k, thr_on, thresh, mu, **kw):
     """the whole path in one bruno_build_and_compact call, no raw-count copy-outs"""
     g = bg.Graph(k=k, thresholding=thr_on, thresh=thresh, min_update=mu, **kw)
     g.build_and_compact(data)
-    out = dict(sizes=g.sizes(), nodes=g.nodes(), ranked=g.ranked(), chains=g.chains())
+    out = dict(sizes=g.sizes(), nodes=g.nodes(), ranked=g.ranked(), chains=g.chains(), chain_edges=g.chain_edges())
     g.close()
     return out
 
@@ -85,6 +86,7 @@ def compare_one_call(gpu, ref):
     assert_same(sort_nodes(*gpu["nodes"]), ref["nodes"], "graph nodes")
     assert_same(sort_ranked(*gpu["ranked"]), ref["ranked"], "listranked chain nodes")
     assert chain_set(*gpu["chains"]) == chain_set(*ref["chains"]), "compacted chains"
+    assert_same(gpu["chain_edges"], ref["chain_edges"], "chain end edges")
 
 
 @pytest.mark.parametrize("opt", sorted(OPTIONS))

@@ -96,6 +96,71 @@ def test_compacted_files_consistent(tmp_path):
     assert sum(len(s) - 30 for s in seqs) == len(comps)
 
 
+def _ascii(words, k):
+    v = 0
+    for i, w in enumerate(words):
+        v |= int(w) << (64 * i)
+    return "".join("ACGT"[(v >> (2 * (k - 1 - j))) & 3] for j in range(k))
+
+
+_RC = str.maketrans("ACGT", "TGCA")
+
+
+def _rc(s):
+    return s.translate(_RC)[::-1]
+
+
+@pytest.mark.parametrize("fname,k,thr_on,lo,mu", [
+    ("debruijn.palindrome_chr14.fastq", 31, True, (2,), True),
+    ("debruijn.bubble.fastq", 31, True, (1, 2, 1), True),
+    ("debruijn.shifted_cycle_chr14.fastq", 31, True, (2,), False),
+    ("test.star.unitiqs.fastq", 31, False, (), True),
+    ("debruijn.bubble.fastq", 45, True, (2,), True),
+    ("debruijn.palindrome_chr14.fastq", 32, False, (), False),
+])
+def test_chain_edges_follow_chain_strings(tmp_path, fname, k, thr_on, lo, mu):
+    """print_chain_frequencies (compact_dbg_stats.hpp:879-1065) derived a second way: for every
+    compacted chain L is its first k-mer and R its last, on the chain's strand; L's in-edges
+    and R's out-edges are the graph counters of those k-mers read on that strand; the summary
+    is over the self frequencies of the chain's listranked nodes, mean = float32 sum / float32
+    count, truncated.  Lines sorted by L, every value followed by a tab."""
+    r = oracle.run(fixture_bytes(fname), k=k, thresholding=thr_on, thresh=bg.thresholds(lo), min_update=mu,
+                   write_prefix=str(tmp_path / "p"))
+    keys, counts, _ = r["nodes"]
+    node = {_ascii(keys[i], k): counts[i] for i in range(len(keys))}
+    K, rep, _ = r["ranked"]
+    selfs = {}
+    for i in range(len(K)):
+        selfs.setdefault(_ascii(rep[i], k), []).append(int(node[min(_ascii(K[i], k), _rc(_ascii(K[i], k)))][8]))
+    lines = []
+    for s in chain_strings(r):
+        L, R = s[:k], s[-k:]
+        cl, cr = node[min(L, _rc(L))], node[min(R, _rc(R))]
+        lin = list(cl[4:8]) if L <= _rc(L) else [cl[3], cl[2], cl[1], cl[0]]
+        rout = list(cr[0:4]) if R <= _rc(R) else [cr[7], cr[6], cr[5], cr[4]]
+        f = selfs[L]
+        mean = int(np.float32(sum(f)) / np.float32(len(f)))
+        lines.append(f"{L}\t{R}\t" + "".join(f"{int(v)}\t" for v in lin + rout + [mean, min(f), max(f)]) + "\n")
+    got = open(tmp_path / "p.chain.edges").read()
+    assert got == "".join(sorted(lines))
+    assert len(lines) == r["n_chains"] > 0
+
+
+def test_chain_edges_select_one_terminus_per_chain():
+    """IsCanonicalTerminusOrIsolated (debruijn_chain_filters.hpp:125-147) keeps exactly one
+    chain-map node per chain whose representative is a chain node; with k and k+2 bounds the
+    filter can trim an edge on one side only, leaving chains whose representative lies outside
+    the chain map, and those get no record"""
+    from bruno_gb300 import synth
+    fq = synth.make_fastq(synth.sample_set(1, 3, max_genome=50_000)[0])
+    r = oracle.run(fq, k=31, thresh=[2, 65536, 2, 65536, 2, 65536])
+    K, rep, dist = r["ranked"]
+    headed = {tuple(rep[i]) for i in range(len(K)) if dist[i] == 0}
+    L = r["chain_edges"][0]
+    assert len(L) == len(headed) < r["n_chains"]
+    assert {tuple(x) for x in L} == headed
+
+
 def test_malformed_fastq_rejected():
     r = oracle.run(fixture_bytes("test.medium.fastq").replace(b"\n+\n", b"\n-\n", 1), k=31)
     assert r["status"] == 2
