@@ -639,10 +639,169 @@ __global__ void __launch_bounds__(TPB) k_fill(EmitArgs a, const uint64_t *ch_off
   if (bad) atomicOr(&a.ctr->err, (unsigned long long)DERR_UNCLEAN_CHAINS);
 }
 
-__global__ void k_check_chains(const uint64_t *ch_off, const uint32_t *seen, uint64_t nh, int k, DevCounters *ctr) {
+/* every chain got one node per position after the representative's k bases: node counts
+ * match the lengths, and no character stayed unwritten (the buffer starts zeroed), so no two
+ * nodes shared a position */
+__global__ void k_check_chains(const uint64_t *ch_off, const uint32_t *seen, uint64_t nh, int k, const char *chars,
+                               uint64_t nchars, DevCounters *ctr) {
+  bool bad = false;
   for (uint64_t h = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (uint64_t)gridDim.x * blockDim.x)
-    if ((uint64_t)seen[h] + (uint64_t)(k - 1) != ch_off[h + 1] - ch_off[h])
-      atomicOr(&ctr->err, (unsigned long long)DERR_UNCLEAN_CHAINS);
+    if ((uint64_t)seen[h] + (uint64_t)(k - 1) != ch_off[h + 1] - ch_off[h]) bad = true;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nchars; i += (uint64_t)gridDim.x * blockDim.x)
+    if (chars[i] == 0) bad = true;
+  if (bad) atomicOr(&ctr->err, (unsigned long long)DERR_UNCLEAN_CHAINS);
+}
+
+/* ================================================================ general emission
+ * When the chain pointers are not mutually consistent (a filter with separate k and k+2 bounds
+ * can trim an edge on one side only), a representative can be a k-mer outside the chain map,
+ * a group can hold no distance-0 node, and several chains can share one representative.
+ * to_compressed_chains (debruijn_chain_graph.hpp:1778-1856) still groups the listranked nodes
+ * by representative, orders each group by (|distance|, K) (chain_rep_less,
+ * debruijn_chain_operations.hpp:332-340) and prints the representative for a distance-0 node
+ * and K's last base for every other one (print_chain_as_fasta, :359-384).  These kernels do
+ * the same without a sort: group ids (the heads' groups first, then a hash on the
+ * representative k-mer), a histogram per group over distances whose scans give every
+ * (group, distance) bucket its character offset, and a rank by K inside a bucket. */
+constexpr uint32_t GID_OWNER = 0x80000000u;   /* gid holds the index of the group's first node */
+
+template <class KT>
+__device__ __forceinline__ void node_ranked(const EmitArgs &a, uint64_t i, KT &K, KT &rep, int32_t &dist) {
+  constexpr int KWD = KOps<KT>::WORDS;
+  const ChainState st = a.cs[i];
+  const KT key = KOps<KT>::load(a.ckey + i * KWD);
+  const KT L = term(st.inD) ? key : ptr_kmer<KT>(st.inP, a.ckey, a.cedge, a.k);
+  const KT R = KOps<KT>::rc(term(st.outD) ? key : ptr_kmer<KT>(st.outP, a.ckey, a.cedge, a.k), a.k);
+  const bool sense = KOps<KT>::le(L, R);
+  K = sense ? key : KOps<KT>::rc(key, a.k);
+  rep = sense ? L : R;
+  dist = (int32_t)(sense ? (st.inD & DM) : (st.outD & DM));
+}
+
+/* group of every live node: its head's group when the head's representative is its own,
+ * otherwise the first node that claimed its representative in the hash table */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_gen_group(EmitArgs a, const uint64_t *ch_rep, uint32_t *gid, uint32_t *gtab,
+                                                    uint64_t tmask) {
+  constexpr int KWD = KOps<KT>::WORDS;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.M; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (a.removed[i]) continue;
+    KT K, rep;
+    int32_t d;
+    node_ranked<KT>(a, i, K, rep, d);
+    const uint32_t t = a.rep_idx[i];
+    const uint32_t h = t == NONE32 ? NONE32 : a.head_of[t];
+    if (h != NONE32 && KOps<KT>::eq(KOps<KT>::load(ch_rep + (uint64_t)h * KWD), rep)) { gid[i] = h; continue; }
+    uint64_t s = KOps<KT>::hash(rep) & tmask;
+    uint32_t owner = (uint32_t)i;
+    for (uint64_t p = 0; p <= tmask; ++p, s = (s + 1) & tmask) {
+      uint32_t o = gtab[s];
+      if (o == 0) {
+        o = atomicCAS(gtab + s, 0u, (uint32_t)i + 1);
+        if (o == 0) break;                     /* claimed: this node owns the group */
+      }
+      KT Ko, repo;
+      int32_t dd;
+      node_ranked<KT>(a, o - 1, Ko, repo, dd);
+      if (KOps<KT>::eq(repo, rep)) { owner = o - 1; break; }
+    }
+    gid[i] = GID_OWNER | owner;
+  }
+}
+
+/* owners take the next group ids (after the heads' groups) and write their representative */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_gen_owner(EmitArgs a, uint32_t *gid, uint32_t *own_gid, uint64_t base,
+                                                    uint64_t *ch_rep, unsigned long long *n_new) {
+  constexpr int KWD = KOps<KT>::WORDS;
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < a.M; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    const bool own = i < a.M && a.removed[i] == 0 && gid[i] == (GID_OWNER | (uint32_t)i);
+    const unsigned long long o = warp_append(own, n_new);
+    if (!own) continue;
+    own_gid[i] = (uint32_t)(base + o);
+    KT K, rep;
+    int32_t d;
+    node_ranked<KT>(a, i, K, rep, d);
+    KOps<KT>::store(ch_rep + (base + o) * KWD, rep);
+  }
+}
+
+/* final group ids; the largest distance of every group */
+__global__ void __launch_bounds__(TPB) k_gen_resolve(const uint8_t *removed, const int32_t *dist_of, uint64_t M,
+                                                      uint32_t *gid, const uint32_t *own_gid, uint32_t *gmax) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (removed[i]) continue;
+    uint32_t g = gid[i];
+    if (g & GID_OWNER) g = own_gid[g & ~GID_OWNER];
+    gid[i] = g;
+    atomicMax(gmax + g, (uint32_t)abs(dist_of[i]));
+  }
+}
+
+__global__ void k_gen_binlen(const uint32_t *gmax, uint64_t G, uint64_t *hlen) {
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < G; g += (uint64_t)gridDim.x * blockDim.x)
+    hlen[g] = (uint64_t)gmax[g] + 1;
+}
+
+/* (group, distance) bins: node counts and character counts (k for distance 0, else 1) */
+__global__ void __launch_bounds__(TPB) k_gen_hist(const uint8_t *removed, const int32_t *dist_of, uint64_t M, int k,
+                                                   const uint32_t *gid, const uint64_t *hoff, uint64_t *ncnt,
+                                                   uint64_t *wcnt) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (removed[i]) continue;
+    const uint32_t d = (uint32_t)abs(dist_of[i]);
+    const uint64_t x = hoff[gid[i]] + d;
+    atomicAdd((unsigned long long *)(ncnt + x), 1ull);
+    atomicAdd((unsigned long long *)(wcnt + x), d == 0 ? (unsigned long long)k : 1ull);
+  }
+}
+
+__global__ void __launch_bounds__(TPB) k_gen_place(const uint8_t *removed, const int32_t *dist_of, uint64_t M,
+                                                    const uint32_t *gid, const uint64_t *hoff, const uint64_t *noff,
+                                                    uint32_t *cur, uint32_t *members) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (removed[i]) continue;
+    const uint64_t x = hoff[gid[i]] + (uint32_t)abs(dist_of[i]);
+    members[noff[x] + atomicAdd(cur + x, 1u)] = (uint32_t)i;
+  }
+}
+
+/* every node's characters: its bin's offset plus its rank by K among the bin's nodes */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_gen_fill(EmitArgs a, const uint32_t *gid, const uint64_t *hoff,
+                                                   const uint64_t *noff, const uint64_t *woff, const uint32_t *members,
+                                                   char *chars) {
+  const char ACGT[4] = {'A', 'C', 'G', 'T'};
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.M; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (a.removed[i]) continue;
+    KT K, rep;
+    int32_t d;
+    node_ranked<KT>(a, i, K, rep, d);
+    const uint32_t ad = (uint32_t)abs(d);
+    const uint64_t x = hoff[gid[i]] + ad;
+    uint64_t rank = 0;
+    for (uint64_t q = noff[x]; q < noff[x + 1]; ++q) {
+      const uint32_t j = members[q];
+      if (j == (uint32_t)i) continue;
+      KT Kj, rj;
+      int32_t dj;
+      node_ranked<KT>(a, j, Kj, rj, dj);
+      if (KOps<KT>::lt(Kj, K)) ++rank;
+    }
+    if (ad == 0) {
+      const uint64_t pos = woff[x] + rank * (uint64_t)a.k;
+      for (int q = 0; q < a.k; ++q) chars[pos + q] = ACGT[KOps<KT>::base_lsb(rep, a.k - 1 - q)];
+    } else {
+      chars[woff[x] + rank] = ACGT[KOps<KT>::last(K)];
+    }
+  }
+}
+
+__global__ void k_gen_offsets(const uint64_t *hoff, const uint64_t *woff, uint64_t G, uint64_t total,
+                              uint64_t *ch_off) {
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += (uint64_t)gridDim.x * blockDim.x)
+    ch_off[g] = g < G ? woff[hoff[g]] : total;
 }
 
 /* ================================================================ chain end edges */
@@ -767,6 +926,75 @@ bruno_status extract_typed(Ctx *c) {
   return BRUNO_OK;
 }
 
+/* the general emission over every live node (run when the scatter's check failed) */
+template <class KT>
+bruno_status general_emission(Ctx *c, EmitArgs a) {
+  bruno_status st;
+  const uint64_t M = c->n_chain, Mb = std::max<uint64_t>(1, M);
+  const int sms = sms_count();
+  uint64_t T = 64;
+  while (T < 2 * Mb) T <<= 1;
+  Buf bgid, bown, btab, bgmax, bhoff, bn, bw, bcur, bmem;
+  auto release = [&] {
+    for (Buf *b : {&bgid, &bown, &btab, &bgmax, &bhoff, &bn, &bw, &bcur, &bmem})
+      if (b->p) cudaFreeAsync(b->p, c->stream);
+  };
+  if ((st = ensure(c, bgid, Mb * 4)) != BRUNO_OK || (st = ensure(c, bown, Mb * 4)) != BRUNO_OK ||
+      (st = ensure(c, btab, T * 4)) != BRUNO_OK || (st = ensure(c, bgmax, Mb * 4)) != BRUNO_OK) {
+    release();
+    return st;
+  }
+  uint32_t *gid = (uint32_t *)bgid.p, *own = (uint32_t *)bown.p, *gmax = (uint32_t *)bgmax.p;
+  const int32_t *dist_of = a.dist_of;
+  cudaMemsetAsync(btab.p, 0, T * 4, c->stream);
+  cudaMemsetAsync(gmax, 0, Mb * 4, c->stream);
+  cudaMemsetAsync(&c->dctr->n_groups, 0, 16, c->stream);
+  k_gen_group<KT><<<sms * 8, TPB, 0, c->stream>>>(a, (const uint64_t *)c->ch_rep.p, gid, (uint32_t *)btab.p, T - 1);
+  k_gen_owner<KT><<<sms * 8, TPB, 0, c->stream>>>(a, gid, own, c->n_heads, (uint64_t *)c->ch_rep.p,
+                                                  &c->dctr->n_groups);
+  k_gen_resolve<<<sms * 8, TPB, 0, c->stream>>>(a.removed, dist_of, M, gid, own, gmax);
+  c->launches += 3;
+  if ((st = sync_counters(c)) != BRUNO_OK) { release(); return st; }
+  const uint64_t G = c->n_heads + c->hctr->n_groups;
+  if ((st = ensure(c, bhoff, (G + 1) * 8)) != BRUNO_OK) { release(); return st; }
+  uint64_t *hoff = (uint64_t *)bhoff.p;
+  cudaMemsetAsync(hoff + G, 0, 8, c->stream);
+  k_gen_binlen<<<sms * 2, TPB, 0, c->stream>>>(gmax, G, hoff);
+  scan_u64(hoff, hoff, G + 1, &c->dctr->n_hist, c->stream);
+  c->launches += 2;
+  if ((st = sync_counters(c)) != BRUNO_OK) { release(); return st; }
+  const uint64_t H = c->hctr->n_hist;
+  if ((st = ensure(c, bn, (H + 1) * 8)) != BRUNO_OK || (st = ensure(c, bw, (H + 1) * 8)) != BRUNO_OK ||
+      (st = ensure(c, bcur, std::max<uint64_t>(1, H) * 4)) != BRUNO_OK || (st = ensure(c, bmem, Mb * 4)) != BRUNO_OK) {
+    release();
+    return st;
+  }
+  uint64_t *noff = (uint64_t *)bn.p, *woff = (uint64_t *)bw.p;
+  cudaMemsetAsync(noff, 0, (H + 1) * 8, c->stream);
+  cudaMemsetAsync(woff, 0, (H + 1) * 8, c->stream);
+  cudaMemsetAsync(bcur.p, 0, std::max<uint64_t>(1, H) * 4, c->stream);
+  k_gen_hist<<<sms * 8, TPB, 0, c->stream>>>(a.removed, dist_of, M, c->cfg.k, gid, hoff, noff, woff);
+  scan_u64(noff, noff, H + 1, nullptr, c->stream);
+  scan_u64(woff, woff, H + 1, &c->dctr->n_chain_chars, c->stream);
+  k_gen_place<<<sms * 8, TPB, 0, c->stream>>>(a.removed, dist_of, M, gid, hoff, noff, (uint32_t *)bcur.p,
+                                              (uint32_t *)bmem.p);
+  c->launches += 4;
+  if ((st = sync_counters(c)) != BRUNO_OK) { release(); return st; }
+  const uint64_t total = c->hctr->n_chain_chars;
+  if ((st = ensure(c, c->ch_chars, std::max<uint64_t>(1, total))) != BRUNO_OK) { release(); return st; }
+  k_gen_fill<KT><<<sms * 8, TPB, 0, c->stream>>>(a, gid, hoff, noff, woff, (const uint32_t *)bmem.p,
+                                                 (char *)c->ch_chars.p);
+  k_gen_offsets<<<sms * 2, TPB, 0, c->stream>>>(hoff, woff, G, total, (uint64_t *)c->head_off.p);
+  c->launches += 2;
+  st = sync_counters(c);
+  release();
+  if (st != BRUNO_OK) return st;
+  c->n_heads = G;
+  c->n_chain_chars = total;
+  c->chains_clean = true;
+  return BRUNO_OK;
+}
+
 template <class KT>
 bruno_status compress_typed(Ctx *c) {
   bruno_status st;
@@ -804,13 +1032,16 @@ bruno_status compress_typed(Ctx *c) {
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   c->n_chain_chars = c->hctr->n_chain_chars;
   if ((st = ensure(c, c->ch_chars, std::max<uint64_t>(1, c->n_chain_chars))) != BRUNO_OK) return st;
+  cudaMemsetAsync(c->ch_chars.p, 0, c->n_chain_chars, c->stream);
   uint32_t *seen = (uint32_t *)((int32_t *)c->pay.p + Mb);
   cudaMemsetAsync(seen, 0, Mb * 4, c->stream);
   k_fill<KT><<<sms * 8, TPB, 0, c->stream>>>(a, (const uint64_t *)c->head_off.p, (char *)c->ch_chars.p, seen);
   c->launches += 5;  /* k_ranked, scan, k_fill, k_check_chains, scan of heads */
-  k_check_chains<<<sms * 2, TPB, 0, c->stream>>>((const uint64_t *)c->head_off.p, seen, nh, c->cfg.k, c->dctr);
+  k_check_chains<<<sms * 2, TPB, 0, c->stream>>>((const uint64_t *)c->head_off.p, seen, nh, c->cfg.k,
+                                                 (const char *)c->ch_chars.p, c->n_chain_chars, c->dctr);
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   c->chains_clean = !(c->hctr->err & DERR_UNCLEAN_CHAINS);
+  if (!c->chains_clean) return general_emission<KT>(c, a);
   return BRUNO_OK;
 }
 

@@ -34,6 +34,7 @@ struct DevCounters {
   unsigned long long n_cycle, n_isolated, n_ranked, n_heads, n_chain_chars;
   unsigned long long n_upper;          /* k-mer positions of all reads long enough */
   unsigned long long n_chain_edges;    /* chain-end records appended */
+  unsigned long long n_groups, n_hist; /* general emission: representative groups, histogram bins */
   unsigned int hll[1 << 12];           /* HyperLogLog registers, p = 12 */
 };
 

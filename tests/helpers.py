@@ -34,3 +34,22 @@ def assert_same(a, b, what):
         if not np.array_equal(x, y):
             bad = np.nonzero(np.any((x != y).reshape(len(x), -1), axis=1))[0]
             raise AssertionError(f"{what}: {len(bad)} rows differ, first at {bad[:5]}")
+
+
+def compress_ranked(K, rep, dist, k):
+    """to_compressed_chains (debruijn_chain_graph.hpp:1778-1856) restated over listranked
+    nodes: sort by chain_rep_less (rep, |dist|, K), group by rep, print the representative for
+    a distance-0 node and K's last base for every other one; returned like chain_set"""
+    order = np.lexsort(tuple(K.T) + (np.abs(dist),) + tuple(rep.T))
+    out = {}
+    for i in order:
+        r = tuple(int(x) for x in rep[i][::-1])
+        if dist[i] == 0:
+            v = 0
+            for w, x in enumerate(rep[i]):
+                v |= int(x) << (64 * w)
+            s = "".join("ACGT"[(v >> (2 * (k - 1 - j))) & 3] for j in range(k))
+        else:
+            s = "ACGT"[int(K[i][0]) & 3]
+        out[r] = out.get(r, "") + s
+    return sorted(out.items())

@@ -19,6 +19,7 @@ CASES = [
     ("debruijn.shifted_cycle_chr14.fastq", ["-T", "-L", "2"]),
     ("debruijn.bubble.fastq", ["-T", "-L", "1", "-L", "2", "-L", "1", "-R"]),
     ("natural.withN.fastq", []),
+    ("debruijn.palindrome_chr14.fastq", ["-T", "-L", "2", "-L", "2", "-L", "2", "-R"]),
 ]
 OUTPUTS = [".chain.fasta", ".chain.components", ".chain.edges", ".branch.fasta", ".branch.edges", ".graph.all"]
 

@@ -7,7 +7,7 @@ import bruno_gb300 as bg
 from bruno_gb300 import synth
 from oracle import oracle
 from conftest import fixture_bytes
-from helpers import assert_same, chain_set, sort_k2, sort_nodes, sort_ranked
+from helpers import assert_same, chain_set, compress_ranked, sort_k2, sort_nodes, sort_ranked
 
 pytestmark = pytest.mark.gpu
 
@@ -17,7 +17,7 @@ FASTQS = ["test.unitiqs.fastq", "test.star.unitiqs.fastq", "test.star2.unitiqs.f
           "debruijn.bubble2.fastq", "natural.fastq", "natural.withN.fastq"]
 OPTIONS = {
     "u": (False, (), True), "tl1": (True, (1,), True), "tl2": (True, (2,), True),
-    "tl2_norank": (True, (2,), False), "tl3": (True, (3,), True),
+    "tl2_norank": (True, (2,), False), "tl3": (True, (3,), True), "tl222": (True, (2, 2, 2), True),
 }
 
 
@@ -209,3 +209,24 @@ def test_large_k_one_call_parity():
     thr = bg.thresholds(w.lower)
     ref = oracle.run(fq, k=63, thresh=thr, min_update=True, threads=16, keep_k2=True)
     compare_one_call(one_call_run(fq, 63, True, thr, True), ref)
+
+
+@pytest.mark.parametrize("k", [31, 45])
+@pytest.mark.parametrize("seed", [3, 4, 5])
+@pytest.mark.parametrize("mu", [True, False])
+def test_inconsistent_chain_pointers_emission(seed, mu, k):
+    """separate k and k+2 lower bounds trim some edges on one side only, so some chains have a
+    representative outside the chain map (no distance-0 node) and chains can share one.  The
+    reference's ranking of such maps depends on its update order (the oracle's result changes
+    with its shard count, and so does the device's with its table layout), so these inputs pin
+    the emission: the compacted chains must be to_compressed_chains of the listranked nodes,
+    and everything before the ranking must equal the oracle's."""
+    fq = synth.make_fastq(synth.sample_set(1, seed, max_genome=200_000, k=k)[0])
+    thr = [2, 65536, 2, 65536, 2, 65536]
+    a = gpu_run(fq, k, True, thr, mu)
+    K, rep, dist = a["ranked"]
+    assert a["sizes"]["n_chains"] > int((dist == 0).sum())      # the case this test is about
+    assert chain_set(*a["chains"]) == compress_ranked(K, rep, dist, k)
+    ref = oracle.run(fq, k=k, thresh=thr, min_update=mu, keep_k2=True, keep_filtered=True)
+    assert_same(sort_nodes(*a["nodes"]), ref["nodes"], "graph nodes")
+    assert a["sizes"]["n_chain_nodes"] == ref["n_chain_nodes"]

@@ -161,6 +161,18 @@ def test_chain_edges_select_one_terminus_per_chain():
     assert {tuple(x) for x in L} == headed
 
 
+@pytest.mark.parametrize("seed,k", [(3, 31), (4, 45)])
+def test_compress_ranked_restatement(seed, k):
+    """the test helper restating to_compressed_chains over listranked nodes gives the oracle's
+    own compaction, also when chains lack a distance-0 node or share a representative"""
+    from bruno_gb300 import synth
+    from helpers import chain_set, compress_ranked
+    fq = synth.make_fastq(synth.sample_set(1, seed, max_genome=100_000, k=k)[0])
+    r = oracle.run(fq, k=k, thresh=[2, 65536, 2, 65536, 2, 65536])
+    assert r["n_chains"] > int((r["ranked"][2] == 0).sum())
+    assert chain_set(*r["chains"]) == compress_ranked(*r["ranked"], k)
+
+
 def test_malformed_fastq_rejected():
     r = oracle.run(fixture_bytes("test.medium.fastq").replace(b"\n+\n", b"\n-\n", 1), k=31)
     assert r["status"] == 2
