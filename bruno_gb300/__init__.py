@@ -50,7 +50,8 @@ class _Sizes(ctypes.Structure):
         "n_chain_nodes", "iterations", "n_cycle_nodes", "n_isolated", "n_ranked", "n_chains",
         "n_chain_chars", "table_slots", "collisions")] + [("filter_flag_hist", ctypes.c_uint64 * 16),
                                                     ("launches", ctypes.c_uint64),
-                                                    ("table_partitions", ctypes.c_uint64)]
+                                                    ("table_partitions", ctypes.c_uint64),
+                                                    ("grouped_chains", ctypes.c_uint64)]
 
 
 class _PoolResult(ctypes.Structure):
@@ -68,7 +69,7 @@ EXPORTS = (
     "bruno_load_fastq", "bruno_compute_biedge_freqencies", "bruno_local_insert_by_freqencies",
     "bruno_extract_chains", "bruno_list_rank", "bruno_to_compressed_chains", "bruno_build_and_compact",
     "bruno_get_sizes", "bruno_copy_k2", "bruno_copy_filtered", "bruno_copy_nodes", "bruno_copy_ranked",
-    "bruno_copy_chains", "bruno_copy_chain_edges", "bruno_host_alloc", "bruno_host_free", "bruno_phase_ms",
+    "bruno_copy_chains", "bruno_copy_chain_edges", "bruno_copy_chain_summaries", "bruno_host_alloc", "bruno_host_free", "bruno_phase_ms",
     "bruno_count_biedges_noalloc", "bruno_pool_create", "bruno_pool_submit", "bruno_pool_wait",
     "bruno_pool_result_free", "bruno_pool_destroy",
 )
@@ -95,6 +96,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "bruno_copy_nodes": [P, P, P, P, SZ, PSZ], "bruno_copy_ranked": [P, P, P, P, SZ, PSZ],
         "bruno_copy_chains": [P, P, P, P, SZ, SZ, PSZ, PSZ],
         "bruno_copy_chain_edges": [P, P, P, SZ, PSZ],
+        "bruno_copy_chain_summaries": [P, P, P, P, SZ, PSZ],
         "bruno_host_alloc": [SZ, ctypes.POINTER(P)], "bruno_host_free": [P],
         "bruno_phase_ms": [P, ctypes.POINTER(ctypes.c_double), SZ],
         "bruno_count_biedges_noalloc": [I32, I32, P, P, SZ, P, P, P, SZ, PSZ, P],
@@ -375,6 +377,23 @@ class Graph:
         L, R = ends[:, 0, :], ends[:, 1, :]
         order = np.lexsort(tuple(L[:, w] for w in range(self.words)))   # last key = high word first
         return L[order], R[order], freqs[order]
+
+    def chain_summaries(self):
+        """to_summarized_chains records sorted by the 5' terminus (the representative), as the
+        reference orders them: kmers (n, 4, words) = prev at 5', 5', 3', next at 3';
+        dist (n,); flags (n, 2) = 5' and 3' end point to a branch"""
+        n = ctypes.c_size_t()
+        self._check(self.lib.bruno_copy_chain_summaries(self.ctx, None, None, None, 0, ctypes.byref(n)),
+                    "copy_chain_summaries")
+        kmers = np.zeros((n.value, 4, self.words), np.uint64)
+        dist = np.zeros(n.value, np.uint32)
+        flags = np.zeros((n.value, 2), np.uint8)
+        if n.value:
+            self._check(self.lib.bruno_copy_chain_summaries(self.ctx, self._ptr(kmers), self._ptr(dist),
+                                                            self._ptr(flags), n.value, ctypes.byref(n)),
+                        "copy_chain_summaries")
+        order = np.lexsort(tuple(kmers[:, 1, w] for w in range(self.words)))
+        return kmers[order], dist[order], flags[order]
 
     def chain_strings(self) -> list[str]:
         reps, offs, chars = self.chains()

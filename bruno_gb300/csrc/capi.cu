@@ -106,7 +106,7 @@ bruno_status bruno_ctx_destroy(bruno_ctx *c) {
   Buf *bufs[] = {&c->rstart, &c->rend, &c->tile_cnt, &c->tile_base, &c->table, &c->k2_keys, &c->k2_edges, &c->k2_counts,
                  &c->f_keys, &c->f_edges, &c->f_counts, &c->blk_cnt, &c->blk_base, &c->ckey, &c->cedge,
                  &c->cstate, &c->cstate2, &c->pend, &c->pay, &c->unf0, &c->unf1, &c->removed, &c->r_K, &c->r_rep, &c->r_dist,
-                 &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list, &c->e_ends, &c->e_freqs,
+                 &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list, &c->e_ends, &c->e_freqs, &c->s_kmers, &c->s_dist, &c->s_flags,
                  &c->records, &c->bucket_cnt, &c->records2, &c->sub_cnt};
   for (Buf *b : bufs) release(*b);
   for (Buf &b : c->seg_bufs) release(b);
@@ -150,6 +150,9 @@ bruno_status bruno_reset(bruno_ctx *c) {
   c->chains_clean = true;
   c->n_chain_edges = 0;
   c->chain_edges_done = false;
+  c->n_summaries = 0;
+  c->summaries_done = false;
+  c->general_emission = false;
   c->launches = 0;
   std::memset(c->flag_hist, 0, sizeof(c->flag_hist));
   std::memset(c->phase_ms, 0, sizeof(c->phase_ms));
@@ -288,6 +291,7 @@ bruno_status bruno_get_sizes(bruno_ctx *c, bruno_sizes *o) {
   o->collisions = c->multi;
   o->launches = c->launches;
   o->table_partitions = 1ull << c->geom.pbits;
+  o->grouped_chains = c->general_emission ? 1 : 0;
   for (int f = 0; f < 16; ++f) o->filter_flag_hist[f] = c->flag_hist[f];
   return BRUNO_OK;
 }
@@ -366,6 +370,22 @@ bruno_status bruno_copy_chain_edges(bruno_ctx *c, uint64_t *ends, uint16_t *freq
   if (cap < c->n_chain_edges) return set_err(c, BRUNO_ERR_CAPACITY, "copy buffer too small");
   st = copy_d2h(c, ends, c->e_ends.p, c->n_chain_edges * 2 * 8 * c->W);
   if (st == BRUNO_OK) st = copy_d2h(c, freqs, c->e_freqs.p, c->n_chain_edges * 11 * 2);
+  if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  return st;
+}
+
+bruno_status bruno_copy_chain_summaries(bruno_ctx *c, uint64_t *kmers, uint32_t *dist, uint8_t *flags, size_t cap,
+                                        size_t *n) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (c->stage < 6) return set_err(c, BRUNO_ERR_ARG, "chain summaries exist after to_compressed_chains");
+  bruno_status st = BRUNO_OK;
+  if (!c->summaries_done && (st = run_chain_summaries(c)) != BRUNO_OK) return st;
+  if (n) *n = c->n_summaries;
+  if (!kmers && !dist && !flags) return BRUNO_OK;
+  if (cap < c->n_summaries) return set_err(c, BRUNO_ERR_CAPACITY, "copy buffer too small");
+  st = copy_d2h(c, kmers, c->s_kmers.p, c->n_summaries * 4 * 8 * c->W);
+  if (st == BRUNO_OK) st = copy_d2h(c, dist, c->s_dist.p, c->n_summaries * 4);
+  if (st == BRUNO_OK) st = copy_d2h(c, flags, c->s_flags.p, c->n_summaries * 2);
   if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
   return st;
 }

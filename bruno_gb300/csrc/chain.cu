@@ -20,6 +20,9 @@
  *                        to_compressed_chains (debruijn_chain_graph.hpp:1778-1856): every
  *                        chain is one head node with distance 0 plus one base per node, so
  *                        the sequence is scattered straight to its offset, no sort.
+ *  k_gen_*               the same emission for chain maps whose pointers are not mutually
+ *                        consistent: groups by representative, distance histograms, ranks
+ *  k_chain_summary       to_summarized_chains (debruijn_chain_graph.hpp:1876-2005), on demand
  *  k_chain_freq /        compute_freq_map and print_chain_frequencies
  *  k_chain_edges         (compact_dbg_stats.hpp:783-816, 879-1065), on demand: the chain
  *                        ends' edge counts and each chain's node-frequency summary
@@ -804,6 +807,67 @@ __global__ void k_gen_offsets(const uint64_t *hoff, const uint64_t *woff, uint64
     ch_off[g] = g < G ? woff[hoff[g]] : total;
 }
 
+/* ================================================================ chain summaries
+ * to_summarized_chains (debruijn_chain_graph.hpp:1876-2005) on a consistent chain map: every
+ * chain's head (distance 0, its representative) is the 5' terminus and the node its far side
+ * points to (itself for a one-node chain) the 3' terminus; read on the representative's
+ * strand they give (prev at 5', 5', 3', next at 3', distance, 5' flag, 3' flag) as
+ * make_summarized_chain and transform::reverse_complement build them
+ * (debruijn_chain_node.hpp:201-268).  A missing neighbour reads as the all-A Kmer(). */
+template <class KT>
+__device__ __forceinline__ KT side_kmer(uint64_t P, const EmitArgs &a) {
+  return (P & PF_BLANK) ? KT{} : ptr_kmer<KT>(P, a.ckey, a.cedge, a.k);
+}
+
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_chain_summary(EmitArgs a, const uint32_t *heads, uint64_t nh, uint64_t *kmers,
+                                                        uint32_t *dist, uint8_t *flags, DevCounters *ctr) {
+  constexpr int KWD = KOps<KT>::WORDS;
+  bool bad = false;
+  for (uint64_t h = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t H = heads[h];
+    if (H >= a.M) { bad = true; continue; }
+    const ChainState st = a.cs[H];
+    const KT key = KOps<KT>::load(a.ckey + (uint64_t)H * KWD);
+    const KT L = term(st.inD) ? key : ptr_kmer<KT>(st.inP, a.ckey, a.cedge, a.k);
+    const KT R = KOps<KT>::rc(term(st.outD) ? key : ptr_kmer<KT>(st.outP, a.ckey, a.cedge, a.k), a.k);
+    const bool sense = KOps<KT>::le(L, R);
+    const KT rep = sense ? L : R;
+    const uint64_t P5 = sense ? st.inP : st.outP, Pf = sense ? st.outP : st.inP;
+    const uint32_t D5 = sense ? st.inD : st.outD, Df = sense ? st.outD : st.inD;
+    const KT s5 = side_kmer<KT>(P5, a);
+    const KT prev = sense ? s5 : KOps<KT>::rc(s5, a.k);
+    ChainState tt = st;
+    KT keyT = key;
+    bool senseT = sense;
+    if (!term(Df)) {   /* the far side points to the 3' terminus */
+      const uint32_t T = (uint32_t)Pf;
+      if ((Pf & (PF_EXT | PF_BLANK)) || T >= a.M) { bad = true; continue; }
+      tt = a.cs[T];
+      keyT = KOps<KT>::load(a.ckey + (uint64_t)T * KWD);
+      const KT LT = term(tt.inD) ? keyT : ptr_kmer<KT>(tt.inP, a.ckey, a.cedge, a.k);
+      const KT RT = KOps<KT>::rc(term(tt.outD) ? keyT : ptr_kmer<KT>(tt.outP, a.ckey, a.cedge, a.k), a.k);
+      senseT = KOps<KT>::le(LT, RT);
+      if (!KOps<KT>::eq(senseT ? LT : RT, rep)) { bad = true; continue; }
+    }
+    const uint64_t P3 = senseT ? tt.outP : tt.inP;
+    const uint32_t D3 = senseT ? tt.outD : tt.inD;
+    if (!term(D3)) { bad = true; continue; }
+    const KT s3 = side_kmer<KT>(P3, a);
+    const KT next = senseT ? s3 : KOps<KT>::rc(s3, a.k);
+    const KT K3 = senseT ? keyT : KOps<KT>::rc(keyT, a.k);
+    uint64_t *o = kmers + h * 4 * KWD;
+    KOps<KT>::store(o, prev);
+    KOps<KT>::store(o + KWD, rep);
+    KOps<KT>::store(o + 2 * KWD, K3);
+    KOps<KT>::store(o + 3 * KWD, next);
+    dist[h] = (st.inD & DM) + (st.outD & DM);
+    flags[2 * h] = D5 == TM ? 0 : 1;
+    flags[2 * h + 1] = D3 == TM ? 0 : 1;
+  }
+  if (bad) atomicOr(&ctr->err, (unsigned long long)DERR_UNCLEAN_CHAINS);
+}
+
 /* ================================================================ chain end edges */
 /* compute_freq_map (compact_dbg_stats.hpp:783-816) per chain-map node: every listranked node
  * adds its self frequency (count, sum, min, max; freq_summary, debruijn_chain_operations.hpp:
@@ -992,6 +1056,7 @@ bruno_status general_emission(Ctx *c, EmitArgs a) {
   c->n_heads = G;
   c->n_chain_chars = total;
   c->chains_clean = true;
+  c->general_emission = true;
   return BRUNO_OK;
 }
 
@@ -1042,6 +1107,35 @@ bruno_status compress_typed(Ctx *c) {
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   c->chains_clean = !(c->hctr->err & DERR_UNCLEAN_CHAINS);
   if (!c->chains_clean) return general_emission<KT>(c, a);
+  return BRUNO_OK;
+}
+
+template <class KT>
+bruno_status chain_summaries_typed(Ctx *c) {
+  bruno_status st;
+  if (c->general_emission)
+    return set_err(c, BRUNO_ERR_INVARIANT,
+                   "chain summaries need mutually consistent chain pointers (the reference's pairing of "
+                   "termini is order-dependent otherwise)");
+  const uint64_t nh = c->n_heads, nb = std::max<uint64_t>(1, nh);
+  const int KWD = Slot<KT>::KEYW;
+  if ((st = ensure(c, c->s_kmers, nb * 4 * 8 * KWD)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->s_dist, nb * 4)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->s_flags, nb * 2)) != BRUNO_OK) return st;
+  cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
+  EmitArgs a{};
+  a.ckey = (const uint64_t *)c->ckey.p; a.cedge = (const uint8_t *)c->cedge.p; a.cs = (const ChainState *)c->cstate.p;
+  a.removed = (const uint8_t *)c->removed.p; a.M = c->n_chain; a.k = c->cfg.k;
+  const int sms = sms_count();
+  k_chain_summary<KT><<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>(sms * 8, (nh + TPB - 1) / TPB)), TPB, 0,
+                        c->stream>>>(a, (const uint32_t *)c->heads.p, nh, (uint64_t *)c->s_kmers.p,
+                                     (uint32_t *)c->s_dist.p, (uint8_t *)c->s_flags.p, c->dctr);
+  c->launches += 1;
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  if (c->hctr->err & DERR_UNCLEAN_CHAINS)
+    return set_err(c, BRUNO_ERR_INVARIANT, "a chain's termini do not pair up");
+  c->n_summaries = nh;
+  c->summaries_done = true;
   return BRUNO_OK;
 }
 
@@ -1210,5 +1304,8 @@ bruno_status run_list_rank(Ctx *c, int min_update) {
 bruno_status run_compress(Ctx *c) { return c->W == 1 ? compress_typed<KW1>(c) : compress_typed<KW2>(c); }
 
 bruno_status run_chain_edges(Ctx *c) { return c->W == 1 ? chain_edges_typed<KW1>(c) : chain_edges_typed<KW2>(c); }
+bruno_status run_chain_summaries(Ctx *c) {
+  return c->W == 1 ? chain_summaries_typed<KW1>(c) : chain_summaries_typed<KW2>(c);
+}
 
 }  // namespace bg

@@ -15,7 +15,8 @@
  * Outputs: <prefix>.chain.fasta (print_chain_string, compact_dbg_io.hpp:323-363),
  * <prefix>.chain.components (print_chain_nodes, :463-498), <prefix>.branch.fasta
  * (print_branch_fasta, :254-299), and unless -B <prefix>.chain.edges
- * (print_chain_frequencies, compact_dbg_stats.hpp:879-1065), <prefix>.branch.edges
+ * (print_chain_frequencies, compact_dbg_stats.hpp:879-1065), <prefix>.chain.summary
+ * (print_chain_summaries, compact_dbg_io.hpp:528-556; k-mers printed as bases), <prefix>.branch.edges
  * (print_branch_edge_frequencies, :219-262) and <prefix>.graph.all.
  * Like the reference, records are sorted before printing; the .chain.fasta has no newline
  * before its first record and none after its last.
@@ -194,6 +195,33 @@ int main(int argc, char **argv) {
         ce += "\t\n";
       }
       if (!write(prefix + ".chain.edges", ce)) return 1;
+      /* .chain.summary: sorted by the 5' terminus (the representative), space separated; only
+       * for mutually consistent chain pointers, where the reference's pairing is well defined */
+      std::vector<uint64_t> sk;
+      std::vector<uint32_t> sd;
+      std::vector<uint8_t> sf;
+      size_t ns = 0;
+      bool have_summaries = true;
+      try {
+        ns = chainmap.to_summarized_chains(sk, sd, sf);
+      } catch (const bruno_gb300::error &e) {
+        if (e.status != BRUNO_ERR_INVARIANT) throw;
+        fprintf(stderr, "no .chain.summary: %s\n", e.what());
+        have_summaries = false;
+      }
+      if (have_summaries) {
+        std::vector<size_t> so(ns);
+        std::iota(so.begin(), so.end(), 0);
+        std::sort(so.begin(), so.end(), [&](size_t a, size_t b) {
+          return load(&sk[(a * 4 + 1) * words], words) < load(&sk[(b * 4 + 1) * words], words);
+        });
+        std::string cs;
+        for (size_t i : so) {
+          for (int j = 0; j < 4; ++j) cs += ascii(load(&sk[(i * 4 + j) * words], words), k) + " ";
+          cs += std::to_string(sd[i]) + " " + std::to_string(sf[2 * i]) + " " + std::to_string(sf[2 * i + 1]) + "\n";
+        }
+        if (!write(prefix + ".chain.summary", cs)) return 1;
+      }
     }
     /* nodes sorted by k-mer: .branch.fasta, .branch.edges, .graph.all */
     std::vector<size_t> nord(nflags.size());

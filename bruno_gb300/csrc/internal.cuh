@@ -102,9 +102,13 @@ struct Ctx {
   Buf r_K, r_rep, r_dist, rep_idx, head_of, heads, head_len, head_off, ch_rep, ch_off, ch_chars;
   uint64_t n_ranked = 0, n_heads = 0, n_chain_chars = 0;
   bool chains_clean = true;
+  bool general_emission = false; /* the compaction grouped by representative (inconsistent map) */
   Buf e_ends, e_freqs;           /* chain-end records (L, R; 11 counts each), built on demand */
   uint64_t n_chain_edges = 0;
   bool chain_edges_done = false;
+  Buf s_kmers, s_dist, s_flags;  /* chain summaries, built on demand */
+  uint64_t n_summaries = 0;
+  bool summaries_done = false;
 
   cudaEvent_t ev[8] = {nullptr};
   cudaEvent_t kev[5] = {nullptr};  /* counting sub-steps */
@@ -131,6 +135,7 @@ bruno_status run_extract_chains(Ctx *c);
 bruno_status run_list_rank(Ctx *c, int min_update);
 bruno_status run_compress(Ctx *c);
 bruno_status run_chain_edges(Ctx *c);
+bruno_status run_chain_summaries(Ctx *c);
 bruno_status run_copy_nodes(Ctx *c, uint64_t *keys, uint16_t *counts, uint8_t *flags, size_t cap, size_t *n);
 
 }  // namespace bg

@@ -84,6 +84,9 @@ typedef struct bruno_sizes {
   uint64_t filter_flag_hist[16]; /* k_del[] histogram (debruijn_graph_map.hpp:1568) */
   uint64_t launches;        /* kernels launched by the last build */
   uint64_t table_partitions; /* slot regions the k-mer table was filled in (1 = one region) */
+  uint64_t grouped_chains;  /* 1: the chain pointers were not mutually consistent (separate k and
+                               k+2 bounds can trim an edge on one side only) and the compaction
+                               grouped the nodes by representative */
 } bruno_sizes;
 
 typedef struct bruno_ctx bruno_ctx;
@@ -169,6 +172,19 @@ bruno_status bruno_copy_chains(bruno_ctx *ctx, uint64_t *reps, uint64_t *offsets
  * particular order (the reference sorts them by L before printing).  Computed on the device at
  * the first call after bruno_to_compressed_chains, which may pass NULL buffers to query n. */
 bruno_status bruno_copy_chain_edges(bruno_ctx *ctx, uint64_t *ends, uint16_t *freqs, size_t cap, size_t *n);
+/* Chain summaries: debruijn_chain_graph::to_summarized_chains()
+ * (src/debruijn/debruijn_chain_graph.hpp:1876-2005), the records print_chain_summaries
+ * (test/common/compact_dbg_io.hpp:528-556) prints to <prefix>.chain.summary.  One per chain:
+ * kmers[4 * words] = the 5' terminus's outer neighbour, the 5' terminus (the chain's
+ * representative), the 3' terminus, the 3' terminus's outer neighbour, all on the
+ * representative's strand (a missing neighbour is the all-A k-mer); dist = distance between the
+ * termini; flags[2] = 1 where the 5' / 3' end points to a branch node, 0 where it has no
+ * neighbour.  Records come in no particular order (the reference's are sorted by the
+ * representative).  BRUNO_ERR_INVARIANT when the chain pointers are not mutually consistent
+ * (the compaction had to group by representative): the reference's pairing of termini then
+ * depends on its sort order.  Computed at the first call after bruno_to_compressed_chains. */
+bruno_status bruno_copy_chain_summaries(bruno_ctx *ctx, uint64_t *kmers, uint32_t *dist, uint8_t *flags, size_t cap,
+                                        size_t *n);
 
 /* Page-locked host memory, for fast host<->device copies of FASTQ input and results. */
 bruno_status bruno_host_alloc(size_t bytes, void **out);

@@ -174,6 +174,19 @@ class debruijn_chain_graph {
     check(bruno_copy_chain_edges(c_.get(), ends.data(), freqs.data(), n, &n), c_.get(), "copy_chain_edges");
     return n;
   }
+  /* to_summarized_chains' records (debruijn_chain_graph.hpp:1876-2005), unordered:
+   * kmers = prev at 5', 5', 3', next at 3' per record (4 * words), dist, flags (2 per record) */
+  size_t to_summarized_chains(std::vector<uint64_t> &kmers, std::vector<uint32_t> &dist, std::vector<uint8_t> &flags) {
+    compress();
+    size_t n = 0;
+    check(bruno_copy_chain_summaries(c_.get(), nullptr, nullptr, nullptr, 0, &n), c_.get(), "copy_chain_summaries");
+    kmers.resize(n * 4 * c_.words());
+    dist.resize(n);
+    flags.resize(n * 2);
+    check(bruno_copy_chain_summaries(c_.get(), kmers.data(), dist.data(), flags.data(), n, &n), c_.get(),
+          "copy_chain_summaries");
+    return n;
+  }
 
  private:
   size_t rank(int min_update) {

@@ -847,6 +847,106 @@ struct Run {
     }
   }
 
+  /* ================================================== chain summaries
+   * to_summarized_chains() (debruijn_chain_graph.hpp:1876-2005): the chain-map termini
+   * (IsTerminusOrIsolated, debruijn_chain_filters.hpp:84-92) sorted by get_chain_rep
+   * (debruijn_chain_operations.hpp:512-522); a terminus terminal on both sides makes a
+   * summary with itself, two consecutive termini with one representative make one summary
+   * oriented so that the 5' terminus is the representative (the four cases of :1937-2000);
+   * make_summarized_chain and transform::reverse_complement (debruijn_chain_node.hpp:201-268):
+   * (prev at 5', 5', 3', next at 3', dist of the 5' node, 5' and 3' ends point to a branch).
+   * The single-rank run: no left shift from a next rank.  A case the reference throws on
+   * leaves summaries_ok = 0. */
+  struct Term { W K; ChainNode<W> x; };
+  struct Summary { W prev, t5, t3, next; uint32_t dist; uint8_t f5, f3; };
+
+  W chain_rep_of(const Term &t) const {
+    const W L = is_chain_terminal(t.x.inD) ? t.K : t.x.inK;
+    const W R = is_chain_terminal(t.x.outD) ? ko.rc(t.K) : ko.rc(t.x.outK);
+    return L <= R ? L : R;
+  }
+  Term rc_term(const Term &t) const {   /* (K, biedge) -> (rc K, reverse_complement(biedge)) */
+    Term r = t;
+    r.K = ko.rc(t.K);
+    r.x.inK = ko.rc(t.x.outK); r.x.outK = ko.rc(t.x.inK);
+    r.x.inD = t.x.outD; r.x.outD = t.x.inD;
+    return r;
+  }
+  Summary make_summary(const Term &f, const Term &s) const {
+    return Summary{f.x.inK, f.K, s.K, s.x.outK, get_chain_dist(f.x.inD) + get_chain_dist(f.x.outD),
+                   (uint8_t)(points_to_self(f.x.inD) ? 0 : 1), (uint8_t)(points_to_self(s.x.outD) ? 0 : 1)};
+  }
+
+  void chain_summaries() {
+    std::vector<Term> termini;
+    for (int s = 0; s < T; ++s)
+      for (size_t i = 0; i < chain[s].keys.size(); ++i) {
+        if (chain[s].state[i] != 1) continue;
+        const ChainNode<W> &x = chain[s].vals[i];
+        if (is_chain_terminal(x.inD) || is_chain_terminal(x.outD)) termini.push_back({chain[s].keys[i].v, x});
+      }
+    std::vector<std::pair<W, size_t>> order;
+    for (size_t i = 0; i < termini.size(); ++i) order.emplace_back(chain_rep_of(termini[i]), i);
+    std::sort(order.begin(), order.end(), [](const std::pair<W, size_t> &a, const std::pair<W, size_t> &b) {
+      return a.first < b.first || (a.first == b.first && a.second < b.second);
+    });
+    std::vector<Summary> out;
+    bool ok = true;
+    auto both = [](const Term &t) { return is_chain_terminal(t.x.inD) && is_chain_terminal(t.x.outD); };
+    if (!order.empty()) {
+      Term first = termini[order[0].second];
+      W first_rep = order[0].first;
+      if (both(first)) out.push_back(make_summary(first, first));
+      for (size_t i = 1; i < order.size() && ok; ++i) {
+        const W rep = order[i].first;
+        if (rep != first_rep) {
+          first = termini[order[i].second];
+          first_rep = rep;
+          if (both(first)) out.push_back(make_summary(first, first));
+          continue;
+        }
+        const Term &second = termini[order[i].second];
+        const bool f2 = is_chain_terminal(first.x.inD), f3 = is_chain_terminal(first.x.outD);
+        const bool s2 = is_chain_terminal(second.x.inD), s3 = is_chain_terminal(second.x.outD);
+        if (f2 && s3) {
+          if (first.K == rep) out.push_back(make_summary(first, second));
+          else if (ko.rc(second.K) == rep) out.push_back(make_summary(rc_term(second), rc_term(first)));
+          else ok = false;
+        } else if (f2 && s2) {
+          if (first.K == rep) out.push_back(make_summary(first, rc_term(second)));
+          else if (second.K == rep) out.push_back(make_summary(second, rc_term(first)));
+          else ok = false;
+        } else if (f3 && s3) {
+          if (ko.rc(first.K) == rep) out.push_back(make_summary(rc_term(first), second));
+          else if (ko.rc(second.K) == rep) out.push_back(make_summary(rc_term(second), first));
+          else ok = false;
+        } else if (f3 && s2) {
+          if (ko.rc(first.K) == rep) out.push_back(make_summary(rc_term(first), rc_term(second)));
+          else if (second.K == rep) out.push_back(make_summary(second, first));
+          else ok = false;
+        } else {
+          ok = false;
+        }
+      }
+    }
+    const int w = res->words;
+    res->summaries_ok = ok ? 1 : 0;
+    if (!ok) out.clear();
+    res->n_summaries = out.size();
+    res->sum_kmers = (uint64_t *)calloc(out.size() * 4 * w + 1, 8);
+    res->sum_dist = (uint32_t *)calloc(out.size() + 1, 4);
+    res->sum_flags = (uint8_t *)calloc(out.size() * 2 + 1, 1);
+    for (size_t i = 0; i < out.size(); ++i) {
+      store_word(res->sum_kmers + (i * 4 + 0) * w, out[i].prev, w);
+      store_word(res->sum_kmers + (i * 4 + 1) * w, out[i].t5, w);
+      store_word(res->sum_kmers + (i * 4 + 2) * w, out[i].t3, w);
+      store_word(res->sum_kmers + (i * 4 + 3) * w, out[i].next, w);
+      res->sum_dist[i] = out[i].dist;
+      res->sum_flags[2 * i] = out[i].f5;
+      res->sum_flags[2 * i + 1] = out[i].f3;
+    }
+  }
+
   /* ====================================================== table outputs */
   void export_tables() {
     const int w = res->words;
@@ -905,6 +1005,7 @@ struct Run {
     list_rank();
     emit();
     chain_edges();
+    chain_summaries();
     export_tables();
     return 0;
   }
@@ -956,6 +1057,7 @@ extern "C" void oracle_free(oracle_result *r) {
   free(r->ranked_K); free(r->ranked_rep); free(r->ranked_dist);
   free(r->chain_rep); free(r->chain_offsets); free(r->chain_chars);
   free(r->edge_L); free(r->edge_R); free(r->edge_freqs);
+  free(r->sum_kmers); free(r->sum_dist); free(r->sum_flags);
   free(r);
 }
 
@@ -1035,6 +1137,21 @@ extern "C" int oracle_write_outputs(const oracle_result *r, int32_t k, const cha
       s += "\n";
     }
     FILE *f = fopen((p + ".chain.edges").c_str(), "wb");
+    if (!f) return 1;
+    fwrite(s.data(), 1, s.size(), f);
+    fclose(f);
+  }
+  /* .chain.summary: print_chain_summaries (compact_dbg_io.hpp:528-556), space separated.
+   * The reference prints the four k-mers with kmerind's Kmer stream operator, which is not part
+   * of the reference sources; they are printed here as their bases. */
+  if (!benchmark && r->summaries_ok) {
+    std::string s;
+    for (size_t i = 0; i < r->n_summaries; ++i) {
+      for (int j = 0; j < 4; ++j) { s += ascii_words(r->sum_kmers + (i * 4 + j) * w, k, w); s += " "; }
+      s += std::to_string(r->sum_dist[i]) + " " + std::to_string(r->sum_flags[2 * i]) + " " +
+           std::to_string(r->sum_flags[2 * i + 1]) + "\n";
+    }
+    FILE *f = fopen((p + ".chain.summary").c_str(), "wb");
     if (!f) return 1;
     fwrite(s.data(), 1, s.size(), f);
     fclose(f);

@@ -83,6 +83,12 @@ typedef struct oracle_result {
   uint16_t *edge_freqs;     /* 11 per record: L in-edges A C G T, R out-edges A C G T,
                                mean, min, max of the chain's node frequencies */
 
+  uint64_t n_summaries;     /* to_summarized_chains records, in the reference's order (by rep) */
+  uint64_t *sum_kmers;      /* 4 k-mers per record: prev at 5', 5' terminus, 3' terminus, next at 3' */
+  uint32_t *sum_dist;       /* distance between the termini */
+  uint8_t *sum_flags;       /* 2 per record: 5' and 3' terminal points to a branch (1) or nothing (0) */
+  int32_t summaries_ok;     /* 0 when the pairing met a case the reference throws on */
+
   double seconds[ORACLE_T_NUM];
 } oracle_result;
 
@@ -92,7 +98,8 @@ void oracle_free(oracle_result *r);
 
 /* Writes the reference driver's text outputs for a finished run:
  * <prefix>.chain.fasta, <prefix>.chain.components, <prefix>.branch.fasta and, unless
- * benchmark != 0, <prefix>.chain.edges, <prefix>.branch.edges and <prefix>.graph.all. */
+ * benchmark != 0, <prefix>.chain.edges, <prefix>.chain.summary (when summaries_ok),
+ * <prefix>.branch.edges and <prefix>.graph.all. */
 int oracle_write_outputs(const oracle_result *r, int32_t k, const char *prefix, int32_t benchmark);
 
 #ifdef __cplusplus

@@ -44,6 +44,8 @@ class _Res(ctypes.Structure):
         ("chain_chars", ctypes.POINTER(ctypes.c_char)),
         ("n_chain_edges", ctypes.c_uint64), ("edge_L", _U64P), ("edge_R", _U64P),
         ("edge_freqs", ctypes.POINTER(ctypes.c_uint16)),
+        ("n_summaries", ctypes.c_uint64), ("sum_kmers", _U64P), ("sum_dist", ctypes.POINTER(ctypes.c_uint32)),
+        ("sum_flags", ctypes.POINTER(ctypes.c_uint8)), ("summaries_ok", ctypes.c_int32),
         ("seconds", ctypes.c_double * 6),
     ]
 
@@ -136,6 +138,9 @@ def run(fastq, k: int = 31, thresholding: bool = True, thresh=None, min_update: 
         nchars = int(offs[-1])
         chars = ctypes.string_at(r.chain_chars, nchars) if nchars else b""
         out["chains"] = (_arr(r.chain_rep, r.n_chains * w, np.uint64, (r.n_chains, w)), offs, chars)
+        ns = r.n_summaries
+        out["summaries"] = (_arr(r.sum_kmers, ns * 4 * w, np.uint64, (ns, 4, w)), _arr(r.sum_dist, ns, np.uint32),
+                            _arr(r.sum_flags, ns * 2, np.uint8, (ns, 2))) if r.summaries_ok else None
         ne = r.n_chain_edges
         out["chain_edges"] = (_arr(r.edge_L, ne * w, np.uint64, (ne, w)), _arr(r.edge_R, ne * w, np.uint64, (ne, w)),
                               _arr(r.edge_freqs, ne * 11, np.uint16, (ne, 11)))

@@ -33,9 +33,29 @@ def gpu_run(data, k, thr_on, thresh, mu, files=None, **kw):
     it = g.list_rank_min_update() if mu else g.list_rank()
     g.to_compressed_chains()
     out = dict(sizes=g.sizes(), k2=k2, filtered=g.filtered(), nodes=g.nodes(), ranked=g.ranked(),
-               chains=g.chains(), chain_edges=g.chain_edges(), iterations=it)
+               chains=g.chains(), chain_edges=g.chain_edges(), summaries=summaries_or_none(g), iterations=it)
     g.close()
     return out
+
+
+def summaries_or_none(g):
+    """chain summaries, or None where the library declines them (inconsistent chain pointers)"""
+    try:
+        return g.chain_summaries()
+    except bg.BrunoError as e:
+        assert e.status == 6 and "mutually consistent" in e.message, e
+        return None
+
+
+def compare_summaries(gpu, ref):
+    """to_summarized_chains: equal to the oracle's whenever the chains are consistent; the
+    library declines only where the compaction had to group chains by representative"""
+    if gpu["summaries"] is None:
+        assert gpu["sizes"]["grouped_chains"] == 1
+        return
+    assert gpu["sizes"]["grouped_chains"] == 0
+    assert ref["summaries"] is not None
+    assert_same(gpu["summaries"], ref["summaries"], "chain summaries")
 
 
 def compare(gpu, ref):
@@ -51,6 +71,7 @@ def compare(gpu, ref):
     assert_same(sort_ranked(*gpu["ranked"]), ref["ranked"], "listranked chain nodes")
     assert chain_set(*gpu["chains"]) == chain_set(*ref["chains"]), "compacted chains"
     assert_same(gpu["chain_edges"], ref["chain_edges"], "chain end edges")
+    compare_summaries(gpu, ref)
 
 
 PATHS = {"fast": {}, "round_sync": {"exact_ranking": True}, "direct_count": {"direct_count": 1},
@@ -72,7 +93,8 @@ def one_call_run(data, k, thr_on, thresh, mu, **kw):
     """the whole path in one bruno_build_and_compact call, no raw-count copy-outs"""
     g = bg.Graph(k=k, thresholding=thr_on, thresh=thresh, min_update=mu, **kw)
     g.build_and_compact(data)
-    out = dict(sizes=g.sizes(), nodes=g.nodes(), ranked=g.ranked(), chains=g.chains(), chain_edges=g.chain_edges())
+    out = dict(sizes=g.sizes(), nodes=g.nodes(), ranked=g.ranked(), chains=g.chains(), chain_edges=g.chain_edges(),
+               summaries=summaries_or_none(g))
     g.close()
     return out
 
@@ -87,6 +109,7 @@ def compare_one_call(gpu, ref):
     assert_same(sort_ranked(*gpu["ranked"]), ref["ranked"], "listranked chain nodes")
     assert chain_set(*gpu["chains"]) == chain_set(*ref["chains"]), "compacted chains"
     assert_same(gpu["chain_edges"], ref["chain_edges"], "chain end edges")
+    compare_summaries(gpu, ref)
 
 
 @pytest.mark.parametrize("opt", sorted(OPTIONS))

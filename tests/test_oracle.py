@@ -146,6 +146,46 @@ def test_chain_edges_follow_chain_strings(tmp_path, fname, k, thr_on, lo, mu):
     assert len(lines) == r["n_chains"] > 0
 
 
+@pytest.mark.parametrize("fname,k,thr_on,lo,mu", [
+    ("debruijn.palindrome_chr14.fastq", 31, True, (2,), True),
+    ("debruijn.bubble.fastq", 31, True, (1, 2, 1), False),
+    ("test.star.unitiqs.fastq", 31, False, (), True),
+    ("debruijn.bubble.fastq", 45, True, (2,), True),
+])
+def test_chain_summaries_follow_chain_strings(tmp_path, fname, k, thr_on, lo, mu):
+    """to_summarized_chains (debruijn_chain_graph.hpp:1876-2005) derived a second way: one line
+    per compacted chain, 5' terminus = its first k-mer (the representative), 3' = its last,
+    distance = length - k; the outer neighbour of an end is the one graph edge leaving it on
+    the chain's strand (flag 1), or else (flag 0) Kmer(), all A, read on the strand of the end's
+    canonical k-mer -- all T where the chain runs on the other strand, since
+    transform::reverse_complement turns the missing neighbour around with the rest."""
+    r = oracle.run(fixture_bytes(fname), k=k, thresholding=thr_on, thresh=bg.thresholds(lo), min_update=mu,
+                   write_prefix=str(tmp_path / "p"))
+    assert r["summaries"] is not None
+    keys, counts, _ = r["nodes"]
+    node = {_ascii(keys[i], k): counts[i] for i in range(len(keys))}
+
+    def edge(x, side):   # the bases of x's in- (side 0) or out-edges (side 1), x on its own strand
+        c = node[min(x, _rc(x))]
+        canon = x <= _rc(x)
+        if side == 0:
+            cnt = list(c[4:8]) if canon else [c[3], c[2], c[1], c[0]]
+        else:
+            cnt = list(c[0:4]) if canon else [c[7], c[6], c[5], c[4]]
+        return ["ACGT"[b] for b in range(4) if cnt[b]]
+
+    lines = []
+    for s in chain_strings(r):
+        t5, t3 = s[:k], s[-k:]
+        pin, pout = edge(t5, 0), edge(t3, 1)
+        assert len(pin) <= 1 and len(pout) <= 1
+        prev = pin[0] + t5[:-1] if pin else ("A" if t5 <= _rc(t5) else "T") * k
+        nxt = t3[1:] + pout[0] if pout else ("A" if t3 <= _rc(t3) else "T") * k
+        lines.append(f"{prev} {t5} {t3} {nxt} {len(s) - k} {len(pin)} {len(pout)}\n")
+    assert open(tmp_path / "p.chain.summary").read() == "".join(sorted(lines, key=lambda l: l.split()[1]))
+    assert len(lines) == r["n_chains"] > 0
+
+
 def test_chain_edges_select_one_terminus_per_chain():
     """IsCanonicalTerminusOrIsolated (debruijn_chain_filters.hpp:125-147) keeps exactly one
     chain-map node per chain whose representative is a chain node; with k and k+2 bounds the
