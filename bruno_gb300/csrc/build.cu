@@ -1062,26 +1062,30 @@ __device__ __noinline__ void filter_wide_global(uint64_t *s, uint64_t i, KT key,
 constexpr int PART_SLOTS = 3072;           /* 96 KB of slots */
 constexpr int PTPB = 512;
 constexpr int MAX_SPLIT_BITS = 10;
-constexpr int SPLIT_QWORDS = 8192;         /* queue words of k_split (64 KB) */
-constexpr int SPLIT_ROUND = 8;             /* records per thread per round: 4096 a block, half the queue words */
+constexpr int SPLIT_ROUND = 16;            /* records per thread per round */
+constexpr int SPLIT_REC = XTPB * SPLIT_ROUND;   /* 8192 records a round */
 
 struct SplitSmem {
-  uint64_t q[SPLIT_QWORDS];
-  unsigned int cnt[1 << MAX_SPLIT_BITS];
-  unsigned long long base[1 << MAX_SPLIT_BITS];
+  uint64_t buf[SPLIT_REC];                        /* the round's records, ordered by partition */
+  unsigned int cnt[1 << MAX_SPLIT_BITS];          /* records per partition this round */
+  unsigned int start[1 << MAX_SPLIT_BITS];        /* their first position in buf */
+  unsigned long long base[1 << MAX_SPLIT_BITS];   /* their first position in the output */
+  unsigned int wsum[XTPB / 32];
   int overflow;
 };
 
-/* bucket blockIdx.y -> its 2^sbits partitions; every block takes one contiguous share.
- * Queue capacity qc = SPLIT_QWORDS >> sbits; a round reads SPLIT_ROUND records per thread,
- * half the queue words, so a queue is about half full when the block flushes. */
-__global__ void __launch_bounds__(XTPB) k_split(const uint64_t *records, const unsigned long long *bucket_cnt,
+/* bucket blockIdx.y -> its 2^sbits partitions; every block takes one contiguous share and
+ * moves it in rounds of SPLIT_REC records, a counting sort each: the records stay in
+ * registers while a shared-memory histogram gives each its rank in its partition, a block
+ * scan turns the histogram into offsets, one reservation per partition and round claims the
+ * output run, and the records, scattered into partition order in shared memory, go out in
+ * one coalesced pass. */
+__global__ void __launch_bounds__(XTPB, 2) k_split(const uint64_t *records, const unsigned long long *bucket_cnt,
                                                  uint64_t cap, int sbits, uint64_t *out, uint64_t cap2,
                                                  unsigned long long *sub_cnt, DevCounters *ctr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SplitSmem &S = *reinterpret_cast<SplitSmem *>(smem_raw);
-  const int tid = threadIdx.x, nq = 1 << sbits, b = blockIdx.y;
-  const int qc = SPLIT_QWORDS >> sbits;   /* a round fills every queue about half */
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nq = 1 << sbits, b = blockIdx.y;
   for (int i = tid; i < nq; i += XTPB) S.cnt[i] = 0;
   if (tid == 0) S.overflow = 0;
   __syncthreads();
@@ -1090,8 +1094,9 @@ __global__ void __launch_bounds__(XTPB) k_split(const uint64_t *records, const u
   const uint64_t lo = min(n, (uint64_t)blockIdx.x * per), hi = min(n, lo + per);
   const uint64_t *rb = records + (uint64_t)b * cap;
   const int shift = 5 + LOW_BITS - sbits;
-  for (uint64_t r0 = lo; r0 < hi; r0 += (uint64_t)XTPB * SPLIT_ROUND) {
-    uint64_t recs[SPLIT_ROUND];   /* every load of the round is in flight before the first push */
+  for (uint64_t r0 = lo; r0 < hi; r0 += SPLIT_REC) {
+    uint64_t recs[SPLIT_ROUND];   /* every load of the round is in flight before the first use */
+    uint32_t pos[SPLIT_ROUND];    /* partition << 16 | rank in it; ~0 past the end */
     #pragma unroll
     for (int j = 0; j < SPLIT_ROUND; ++j) {
       const uint64_t i = r0 + (uint64_t)j * XTPB + tid;
@@ -1100,42 +1105,67 @@ __global__ void __launch_bounds__(XTPB) k_split(const uint64_t *records, const u
     #pragma unroll
     for (int j = 0; j < SPLIT_ROUND; ++j) {
       const uint64_t i = r0 + (uint64_t)j * XTPB + tid;
+      pos[j] = ~0u;
       if (i < hi) {
-        const uint64_t rec = recs[j];
-        const unsigned sq = (unsigned)(rec >> shift) & (unsigned)(nq - 1);
-        const unsigned pos = atomicAdd(&S.cnt[sq], 1u);
-        if (pos < (unsigned)qc) {
-          S.q[sq * qc + pos] = rec;
-        } else {
-          const uint64_t part = ((uint64_t)b << sbits) | sq;
-          const unsigned long long o = atomicAdd(&sub_cnt[part], 1ull);
-          if (o < cap2) out[part * cap2 + o] = rec;
-          else S.overflow = 1;
+        const unsigned sq = (unsigned)(recs[j] >> shift) & (unsigned)(nq - 1);
+        pos[j] = (sq << 16) | atomicAdd(&S.cnt[sq], 1u);
+      }
+    }
+    __syncthreads();
+    /* exclusive scan of the histogram (two partitions a thread) and the reservations */
+    const int q0 = 2 * tid;
+    const unsigned c0 = q0 < nq ? S.cnt[q0] : 0u, c1 = q0 + 1 < nq ? S.cnt[q0 + 1] : 0u;
+    if (q0 < nq) S.cnt[q0] = 0;
+    if (q0 + 1 < nq) S.cnt[q0 + 1] = 0;
+    const unsigned v = c0 + c1;
+    unsigned x = v;
+    #pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(~0u, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) S.wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      const unsigned w = lane < XTPB / 32 ? S.wsum[lane] : 0u;
+      unsigned z = w;
+      #pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(~0u, z, o);
+        if (lane >= o) z += y;
+      }
+      if (lane < XTPB / 32) S.wsum[lane] = z - w;
+    }
+    __syncthreads();
+    const unsigned ex = S.wsum[wid] + x - v;
+    #pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int q = q0 + h;
+      const unsigned c = h ? c1 : c0;
+      if (q < nq) {
+        S.start[q] = h ? ex + c0 : ex;
+        if (c) {
+          const uint64_t part = ((uint64_t)b << sbits) | (unsigned)q;
+          const unsigned long long old = atomicAdd(&sub_cnt[part], (unsigned long long)c);
+          if (old + c > cap2) S.overflow = 1;
+          S.base[q] = part * cap2 + old;
         }
       }
     }
     __syncthreads();
-    for (int q = tid; q < nq; q += XTPB) {
-      const unsigned f = min(S.cnt[q], (unsigned)qc);
-      if (f) {
-        const uint64_t part = ((uint64_t)b << sbits) | (unsigned)q;
-        const unsigned long long old = atomicAdd(&sub_cnt[part], (unsigned long long)f);
-        if (old + f > cap2) S.overflow = 1;
-        S.base[q] = part * cap2 + old;
-      }
+    #pragma unroll
+    for (int j = 0; j < SPLIT_ROUND; ++j)
+      if (pos[j] != ~0u) S.buf[S.start[pos[j] >> 16] + (pos[j] & 0xFFFFu)] = recs[j];
+    __syncthreads();
+    const unsigned nr = (unsigned)min((uint64_t)SPLIT_REC, hi - r0);
+    for (unsigned y = tid; y < nr; y += XTPB) {
+      const uint64_t rec = S.buf[y];
+      const unsigned q = (unsigned)(rec >> shift) & (unsigned)(nq - 1);
+      const uint64_t part = ((uint64_t)b << sbits) | q;
+      const unsigned long long dst = S.base[q] + (y - S.start[q]);
+      if (dst < (part + 1) * cap2) out[dst] = rec;
     }
-    __syncthreads();
-    for (int x = tid; x < nq * qc; x += XTPB) {
-      const int q = x / qc, j = x - q * qc;
-      if ((unsigned)j < min(S.cnt[q], (unsigned)qc)) {
-        const uint64_t part = ((uint64_t)b << sbits) | (unsigned)q;
-        const unsigned long long dst = S.base[q] + j;
-        if (dst < (part + 1) * cap2) out[dst] = S.q[x];
-      }
-    }
-    __syncthreads();
-    for (int q = tid; q < nq; q += XTPB) S.cnt[q] = 0;
-    __syncthreads();
+    /* the next round writes buf, start and base only after its first two barriers */
   }
   if (tid == 0 && S.overflow) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
 }
