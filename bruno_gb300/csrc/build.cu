@@ -351,14 +351,6 @@ struct CountArgs {
 __device__ __forceinline__ uint64_t ld_cg(const uint64_t *p) { return __ldcg((const unsigned long long *)p); }
 
 /* one slot (4 or 8 words) with 256-bit relaxed loads: a single L2 request per 32 bytes */
-template <int SU>
-__device__ __forceinline__ void ld_slot(const uint64_t *slot, uint64_t *raw) {
-  #pragma unroll
-  for (int q = 0; q < SU; q += 4)
-    asm volatile("ld.relaxed.gpu.global.v4.u64 {%0, %1, %2, %3}, [%4];"
-                 : "=l"(raw[q]), "=l"(raw[q + 1]), "=l"(raw[q + 2]), "=l"(raw[q + 3])
-                 : "l"(slot + q) : "memory");
-}
 __device__ __forceinline__ uint32_t ld_cg32(const uint32_t *p) { return __ldcg(p); }
 
 /* One count into the entry words e[0..n) of a slot whose current contents were read into
@@ -433,16 +425,6 @@ __device__ __forceinline__ KW2 key_read(KW2, const uint64_t *slot) {
   ulonglong2 v = __ldcg((const ulonglong2 *)slot);
   return {v.x, v.y};
 }
-__device__ __forceinline__ bool key_is_empty(KW1 k) { return k.v == KEY_EMPTY; }
-__device__ __forceinline__ bool key_is_empty(KW2 k) { return k.hi == KEY_EMPTY && k.lo == KEY_EMPTY; }
-__device__ __forceinline__ bool key_matches(KW1 k, KW1 want, bool cont) { return k.v == (want.v | (cont ? KEY_CONT : 0)); }
-__device__ __forceinline__ bool key_matches(KW2 k, KW2 want, bool cont) {
-  return k.lo == want.lo && k.hi == (want.hi | (cont ? KEY_CONT : 0));
-}
-__device__ __forceinline__ bool key_dead(KW1 k) { return (k.v & KEY_DEAD_BIT) != 0; }
-__device__ __forceinline__ bool key_dead(KW2 k) { return (k.hi & KEY_DEAD_BIT) != 0; }
-__device__ __forceinline__ bool key_cont(KW1 k) { return (k.v & KEY_CONT) != 0; }
-__device__ __forceinline__ bool key_cont(KW2 k) { return (k.hi & KEY_CONT) != 0; }
 
 /* Counts one canonical (k-mer, biedge code) occurrence whose first probe slot `i` was
  * already read into raw[].  Returns false if the probe limit was reached. */

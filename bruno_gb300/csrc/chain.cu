@@ -114,6 +114,39 @@ __device__ __forceinline__ long long table_find(const uint64_t *table, const Tab
   return -1;
 }
 
+/* Two lookups in lockstep: both first probes are in flight together, and each probe reads
+ * the whole slot (key, counters, flags, aux) in 32-byte loads.  found = slot index or -1. */
+template <class KT>
+__device__ __forceinline__ void table_find2(const uint64_t *table, const TableGeom &g, uint32_t max_probe,
+                                            const KT *want, const bool *has, long long *found,
+                                            uint64_t (*raw)[Slot<KT>::U64]) {
+  constexpr int SU = Slot<KT>::U64;
+  KT x[2];
+  uint64_t pos[2], lo[2], hi[2];
+  bool done[2];
+  #pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    found[q] = -1;
+    done[q] = !has[q];
+    x[q] = table_key(want[q]);
+    const Probe pr(g, table_home(g, x[q]));
+    pos[q] = pr.i; lo[q] = pr.lo; hi[q] = pr.hi;
+  }
+  for (uint32_t p = 0; p < max_probe && !(done[0] && done[1]); ++p) {
+    #pragma unroll
+    for (int q = 0; q < 2; ++q)
+      if (!done[q]) ld_slot<SU>(table + pos[q] * SU, raw[q]);
+    #pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (done[q]) continue;
+      const KT key = KOps<KT>::load(raw[q]);
+      if (KOps<KT>::eq(key, x[q])) { found[q] = (long long)pos[q]; done[q] = true; }
+      else if (key_is_empty(key)) done[q] = true;
+      else if (++pos[q] == hi[q]) pos[q] = lo[q];
+    }
+  }
+}
+
 /* ================================================================ chain init */
 /* chain index i (listed by the filter, which also stored i in the slot) -> its k-mer, its
  * chain-map record and its edge byte; one read of its own slot gives key and counters */
@@ -129,40 +162,44 @@ __global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, uint6
       atomicOr(&ctr->err, (unsigned long long)DERR_INVARIANT);
       sl = 0;
     }
-    const uint64_t *s = table + sl * SU;
-    const KT K = key_kmer(KOps<KT>::load(s));
+    uint64_t own[SU];
+    ld_slot<SU>(table + sl * SU, own);
+    const KT K = key_kmer(KOps<KT>::load(own));
     KOps<KT>::store(ckey + i * KWD, K);
-    const uint64_t *pw = s + KWD;
+    const uint64_t *pw = own + KWD;
     int inc = -1, outc = -1;
     for (int c = 0; c < 4; ++c) {
       if ((pw[0] >> (16 * c)) & 0xFFFFu) outc = c;
       if ((pw[1] >> (16 * c)) & 0xFFFFu) inc = c;
     }
+    /* in neighbour nextReverseFromChar(c), out neighbour nextFromChar(c), canonical */
+    KT want[2];
+    bool has[2] = {inc >= 0, outc >= 0}, flip[2] = {false, false};
+    #pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const KT n = q == 0 ? KOps<KT>::prepend((unsigned)max(inc, 0), K, k) : KOps<KT>::append(K, (unsigned)max(outc, 0), k);
+      const KT y = KOps<KT>::rc(n, k);
+      flip[q] = !KOps<KT>::lt(n, y);
+      want[q] = flip[q] ? y : n;
+    }
+    long long found[2];
+    uint64_t raw[2][SU];
+    table_find2<KT>(table, g, max_probe, want, has, found, raw);
     ChainState st;
     st.pad = 0;
-    if (inc >= 0) {  /* in neighbour: nextReverseFromChar(c) */
-      KT n = KOps<KT>::prepend((unsigned)inc, K, k), y = KOps<KT>::rc(n, k);
-      const bool flip = !KOps<KT>::lt(n, y);
-      const long long j = table_find<KT>(table, g, max_probe, flip ? y : n);
-      if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN) && slot_aux<KT>(table + j * SU) < M)
-        st.inP = (uint64_t)slot_aux<KT>(table + j * SU) | (flip ? PF_FLIP : 0);
-      else
-        st.inP = PF_EXT | i;
-      st.inD = 1;
-    } else {
-      st.inP = PF_BLANK; st.inD = TM;
-    }
-    if (outc >= 0) {  /* out neighbour: nextFromChar(c) */
-      KT n = KOps<KT>::append(K, (unsigned)outc, k), y = KOps<KT>::rc(n, k);
-      const bool flip = !KOps<KT>::lt(n, y);
-      const long long j = table_find<KT>(table, g, max_probe, flip ? y : n);
-      if (j >= 0 && (slot_flags<KT>(table + j * SU) & NF_CHAIN) && slot_aux<KT>(table + j * SU) < M)
-        st.outP = (uint64_t)slot_aux<KT>(table + j * SU) | (flip ? PF_FLIP : 0);
-      else
-        st.outP = PF_EXT | PF_EXTOUT | i;
-      st.outD = 1;
-    } else {
-      st.outP = PF_BLANK; st.outD = TM;
+    #pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      uint64_t P;
+      uint32_t D;
+      if (!has[q]) {
+        P = PF_BLANK; D = TM;
+      } else {
+        const uint32_t fl = (uint32_t)(raw[q][KWD + 2] >> 16) & 0xFFFFu, aux = (uint32_t)(raw[q][KWD + 2] >> 32);
+        if (found[q] >= 0 && (fl & NF_CHAIN) && aux < M) P = (uint64_t)aux | (flip[q] ? PF_FLIP : 0);
+        else P = PF_EXT | (q ? PF_EXTOUT : 0) | i;
+        D = 1;
+      }
+      if (q == 0) { st.inP = P; st.inD = D; } else { st.outP = P; st.outD = D; }
     }
     cs[i] = st;
     cedge[i] = (uint8_t)((inc >= 0 ? (4 | inc) : 0) | (outc >= 0 ? (32 | (outc << 3)) : 0));

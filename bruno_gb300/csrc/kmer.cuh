@@ -257,4 +257,26 @@ __device__ __forceinline__ uint32_t entry_count(uint32_t e) {
   return (e & E_BIG) ? E_COUNT_BIG : (e >> E_COUNT_SHIFT);
 }
 
+/* a whole slot in 32-byte loads */
+template <int SU>
+__device__ __forceinline__ void ld_slot(const uint64_t *slot, uint64_t *raw) {
+  #pragma unroll
+  for (int q = 0; q < SU; q += 4)
+    asm volatile("ld.relaxed.gpu.global.v4.u64 {%0, %1, %2, %3}, [%4];"
+                 : "=l"(raw[q]), "=l"(raw[q + 1]), "=l"(raw[q + 2]), "=l"(raw[q + 3])
+                 : "l"(slot + q) : "memory");
+}
+
+/* slot key states */
+__device__ __forceinline__ bool key_is_empty(KW1 k) { return k.v == KEY_EMPTY; }
+__device__ __forceinline__ bool key_is_empty(KW2 k) { return k.hi == KEY_EMPTY && k.lo == KEY_EMPTY; }
+__device__ __forceinline__ bool key_matches(KW1 k, KW1 want, bool cont) { return k.v == (want.v | (cont ? KEY_CONT : 0)); }
+__device__ __forceinline__ bool key_matches(KW2 k, KW2 want, bool cont) {
+  return k.lo == want.lo && k.hi == (want.hi | (cont ? KEY_CONT : 0));
+}
+__device__ __forceinline__ bool key_dead(KW1 k) { return (k.v & KEY_DEAD_BIT) != 0; }
+__device__ __forceinline__ bool key_dead(KW2 k) { return (k.hi & KEY_DEAD_BIT) != 0; }
+__device__ __forceinline__ bool key_cont(KW1 k) { return (k.v & KEY_CONT) != 0; }
+__device__ __forceinline__ bool key_cont(KW2 k) { return (k.hi & KEY_CONT) != 0; }
+
 }  // namespace bg
