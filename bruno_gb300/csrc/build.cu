@@ -1185,8 +1185,13 @@ __device__ __forceinline__ bool sm_count_entries(uint32_t *e, const uint32_t *se
       w = old;
     }
     if (entry_code(w) == code) {
-      const uint32_t old = atomicAdd(e + i, 1u << E_COUNT_SHIFT);
-      if (old >> 31) atomicOr(e + i, E_BIG);
+      if ((w >> E_COUNT_SHIFT) < (1u << 24) && !(w & E_BIG)) {
+        atomicAdd(e + i, 1u << E_COUNT_SHIFT);   /* result unused: a partition holds far fewer
+                                                    than 2^24 records, so this cannot reach E_BIG */
+      } else {
+        const uint32_t old = atomicAdd(e + i, 1u << E_COUNT_SHIFT);
+        if (old >> 31) atomicOr(e + i, E_BIG);
+      }
       return true;
     }
   }
