@@ -40,7 +40,7 @@ class _Cfg(ctypes.Structure):
         ("k", ctypes.c_int32), ("thresholding", ctypes.c_int32), ("thresh", ctypes.c_uint64 * 6),
         ("min_update", ctypes.c_int32), ("device", ctypes.c_int32), ("table_slots", ctypes.c_uint64),
         ("max_load", ctypes.c_double), ("keep_k2", ctypes.c_int32), ("keep_filtered", ctypes.c_int32),
-        ("exact_ranking", ctypes.c_int32), ("direct_count", ctypes.c_int32),
+        ("exact_ranking", ctypes.c_int32), ("direct_count", ctypes.c_int32), ("edge_filter", ctypes.c_int32),
     ]
 
 
@@ -164,6 +164,7 @@ class GraphConfig:
     keep_filtered: bool = False
     exact_ranking: bool = False
     direct_count: int = 0          # 0 automatic, 1 whole-table counting, 2 L2 partitions (k <= 31)
+    edge_filter: bool = False      # the blocked driver's (k+1)-mer filter build (k <= 31)
 
     def to_c(self) -> _Cfg:
         c = _Cfg()
@@ -174,6 +175,7 @@ class GraphConfig:
         c.keep_k2, c.keep_filtered = int(self.keep_k2), int(self.keep_filtered)
         c.exact_ranking = int(self.exact_ranking)
         c.direct_count = int(self.direct_count)
+        c.edge_filter = int(self.edge_filter)
         return c
 
 

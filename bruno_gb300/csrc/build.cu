@@ -647,10 +647,124 @@ __device__ __forceinline__ bool seq_valid(const unsigned char *s, const unsigned
   return ok;
 }
 
+/* ------------------------------------------------ the (k+1)-mer edge filter
+ * The blocked driver's build_index_thresholded (compact_debruijn_graph_block_construct.cpp:
+ * 417-470): compute_edge_frequency (debruijn_biedge_filters.hpp:128-177) counts every
+ * canonical (k+1)-mer of the N-filtered reads at least k+1 long in a saturating uint16
+ * counter and erases those outside [lo, hi); transform_biedges_by_frequency (:331-423)
+ * clears every biedge edge whose (k+1)-mer is gone and filter_isolated_nodes (:66-75) drops
+ * pairs left without edges; the rest are inserted unthresholded.  The (k+1)-mers (k <= 31,
+ * so at most 64 bits) live in an open-addressing table of (key, count) slots keyed by the
+ * canonical (k+1)-mer itself: all ones and all ones but the lowest bit are never canonical
+ * (their reverse complements are smaller), so they mark empty and erased slots. */
+constexpr uint64_t K1_EMPTY = ~0ull, K1_TOMB = ~1ull;
+
+struct K1Roll {   /* forward and reverse-complement (k+1)-mer of a read, base by base */
+  uint64_t fw = 0, rv = 0, mask;
+  int top;
+  __device__ __forceinline__ explicit K1Roll(int k1) : mask(k1 == 32 ? ~0ull : ((1ull << (2 * k1)) - 1)), top(2 * k1 - 2) {}
+  __device__ __forceinline__ uint64_t push(unsigned c) {   /* the canonical (k+1)-mer ending here */
+    fw = ((fw << 2) | c) & mask;
+    rv = (rv >> 2) | ((uint64_t)(3u - c) << top);
+    return fw < rv ? fw : rv;
+  }
+};
+
+__device__ __forceinline__ uint64_t k1_home(uint64_t x, uint64_t nslots) { return __umul64hi(mix64(x), nslots); }
+
+/* true if the (k+1)-mer x is in the table (erased slots are stepped over) */
+__device__ __forceinline__ bool k1_exists(const uint64_t *tab, uint64_t nslots, uint64_t x) {
+  uint64_t i = k1_home(x, nslots);
+  for (uint64_t p = 0; p < nslots; ++p) {
+    const uint64_t key = __ldg(tab + 2 * i);
+    if (key == x) return true;
+    if (key == K1_EMPTY) return false;
+    if (++i == nslots) i = 0;
+  }
+  return false;
+}
+
+/* distinct (k+1)-mer estimate: HyperLogLog registers per block */
+__global__ void __launch_bounds__(TPB) k_k1_hll(const uint64_t *rstart, const uint64_t *rend, uint64_t nreads, int k,
+                                                 uint8_t *partial) {
+  __shared__ unsigned int reg[HLL_M];
+  for (int i = threadIdx.x; i < HLL_M; i += TPB) reg[i] = 0;
+  __syncthreads();
+  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nreads; r += (uint64_t)gridDim.x * blockDim.x) {
+    const unsigned char *s = (const unsigned char *)rstart[r], *e = (const unsigned char *)rend[r];
+    const uint32_t L = (uint32_t)(e - s);
+    if (L < (uint32_t)k + 1 || !seq_valid(s, e)) continue;
+    SeqCursor sc;
+    sc.init(s, e);
+    K1Roll roll(k + 1);
+    for (uint32_t i = 0; i < L; ++i) {
+      const unsigned byte = sc.next();
+      const uint64_t x = roll.push(((byte >> 1) ^ (byte >> 2)) & 3u);
+      if (i < (uint32_t)k) continue;
+      const uint64_t h = mix64(x);
+      const unsigned idx = (unsigned)(h >> (64 - HLL_P));
+      const unsigned rho = (unsigned)__clzll((h << HLL_P) | (1ull << (HLL_P - 1))) + 1u;
+      if (rho > reg[idx]) atomicMax(&reg[idx], rho);
+    }
+  }
+  __syncthreads();
+  uint8_t *dst = partial + (uint64_t)blockIdx.x * HLL_M;
+  for (int i = threadIdx.x; i < HLL_M; i += TPB) dst[i] = (uint8_t)reg[i];
+}
+
+/* count every (k+1)-mer; a probe run longer than max_probe reports a full table */
+__global__ void __launch_bounds__(TPB) k_k1_count(const uint64_t *rstart, const uint64_t *rend, uint64_t nreads, int k,
+                                                   uint64_t *tab, uint64_t nslots, uint32_t max_probe,
+                                                   DevCounters *ctr) {
+  bool full = false;
+  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nreads; r += (uint64_t)gridDim.x * blockDim.x) {
+    const unsigned char *s = (const unsigned char *)rstart[r], *e = (const unsigned char *)rend[r];
+    const uint32_t L = (uint32_t)(e - s);
+    if (L < (uint32_t)k + 1 || !seq_valid(s, e)) continue;
+    SeqCursor sc;
+    sc.init(s, e);
+    K1Roll roll(k + 1);
+    for (uint32_t i = 0; i < L; ++i) {
+      const unsigned byte = sc.next();
+      const uint64_t x = roll.push(((byte >> 1) ^ (byte >> 2)) & 3u);
+      if (i < (uint32_t)k) continue;
+      uint64_t j = k1_home(x, nslots);
+      bool done = false;
+      for (uint32_t p = 0; p < max_probe && !done; ++p) {
+        unsigned long long *slot = (unsigned long long *)(tab + 2 * j);
+        unsigned long long key = *(volatile unsigned long long *)slot;
+        if (key == K1_EMPTY) key = atomicCAS(slot, K1_EMPTY, (unsigned long long)x);
+        if (key == K1_EMPTY || key == x) { atomicAdd(slot + 1, 1ull); done = true; }
+        else if (++j == nslots) j = 0;
+      }
+      full |= !done;
+    }
+  }
+  if (full) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
+}
+
+__global__ void k_k1_init(uint64_t *tab, uint64_t nslots) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < 2 * nslots; i += (uint64_t)gridDim.x * blockDim.x)
+    tab[i] = (i & 1) ? 0ull : K1_EMPTY;
+}
+
+/* erase the (k+1)-mers whose saturated count lies outside [lo, hi) */
+__global__ void __launch_bounds__(TPB) k_k1_threshold(uint64_t *tab, uint64_t nslots, uint64_t lo, uint64_t hi) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (tab[2 * i] == K1_EMPTY) continue;
+    const uint64_t c = min(tab[2 * i + 1], (uint64_t)0xFFFFu);
+    if (c < lo || c >= hi) tab[2 * i] = K1_TOMB;
+  }
+}
+
+/* EF: the (k+1)-mer edge filter above -- each edge whose (k+1)-mer is not in k1tab is cleared
+ * and a pair without edges is not emitted; a read's (k+1)-mer at each position is looked up
+ * once, as the out edge of one k-mer and the in edge of the next */
+template <bool EF>
 __global__ void __launch_bounds__(XTPB, 2) k_extract(const uint64_t *rstart, const uint64_t *rend, uint64_t nreads,
                                                       int k, uint64_t *records, uint64_t cap,
                                                       unsigned long long *bucket_cnt, uint8_t *hll_partial,
-                                                      DevCounters *ctr) {
+                                                      const uint64_t *k1tab, uint64_t k1slots, DevCounters *ctr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ExtractSmem &S = *reinterpret_cast<ExtractSmem *>(smem_raw);
   const int tid = threadIdx.x;
@@ -693,6 +807,8 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract(const uint64_t *rstart, con
     const unsigned idx = (unsigned)(h >> (62 - HLL_P));
     const unsigned rho = (unsigned)__clzll((h << (2 + HLL_P)) | (1ull << (1 + HLL_P))) + 1u;
     if (rho > S.hll[idx]) atomicMax(&S.hll[idx], rho);
+    ++inst;
+    if (EF && in5 == 0 && out5 == 0) return;   /* filter_isolated_nodes */
     const unsigned pos = atomicAdd(&S.cnt[bucket], 1u);
     if (pos < (unsigned)XQ) {
       S.q[bucket][pos] = rec;
@@ -701,8 +817,8 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract(const uint64_t *rstart, con
       if (o < cap) records[(uint64_t)bucket * cap + o] = rec;
       else S.overflow = 1;
     }
-    ++inst;
   };
+  bool ef_in_ok = false;   /* EF: the previous position's (k+1)-mer was kept */
   bool active = next_read();
   for (;;) {
     int emitted = 0;
@@ -710,14 +826,22 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract(const uint64_t *rstart, con
       const unsigned byte = sc.next();
       const unsigned c = ((byte >> 1) ^ (byte >> 2)) & 3u;   /* A0 C1 G2 T3, either case */
       if (i >= (uint32_t)k) {   /* the k-mer ending before base i, its out-base is base i */
-        emit(i > (uint32_t)k ? left + 1u : 0u, c + 1u);
+        unsigned in5 = i > (uint32_t)k ? left + 1u : 0u, out5 = c + 1u;
+        if (EF) {
+          const uint64_t f1 = (fwd << 2) | c, r1 = ((uint64_t)(3u - c) << (2 * k)) | rev;
+          const bool out_ok = k1_exists(k1tab, k1slots, f1 < r1 ? f1 : r1);
+          if (!ef_in_ok) in5 = 0;
+          if (!out_ok) out5 = 0;
+          ef_in_ok = out_ok;
+        }
+        emit(in5, out5);
         ++emitted;
       }
       left = (unsigned)(fwd >> top) & 3u;
       fwd = ((fwd << 2) | c) & kmask;
       rev = (rev >> 2) | ((uint64_t)(3u - c) << top);
       if (++i == L) {   /* the last k-mer has no out-base */
-        emit(left + 1u, 0u);
+        emit(EF && !ef_in_ok ? 0u : left + 1u, 0u);
         ++emitted;
         r += stride;
         active = next_read();
@@ -1615,15 +1739,21 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
   const int eb = std::max(1, std::min<int>(sms * 2, (int)((nreads + XTPB - 1) / XTPB)));
   if ((st = ensure(c, c->blk_cnt, (size_t)eb * HLL_M)) != BRUNO_OK) return st;
   static const bool attr = [] {
-    cudaFuncSetAttribute(k_extract, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
+    cudaFuncSetAttribute(k_extract<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
+    cudaFuncSetAttribute(k_extract<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
     return true;
   }();
   (void)attr;
   cudaEventRecord(c->kev[0], c->stream);
-  k_extract<<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p,
-                                                          nreads, c->cfg.k, (uint64_t *)c->records.p, cap,
-                                                          (unsigned long long *)c->bucket_cnt.p, (uint8_t *)c->blk_cnt.p,
-                                                          c->dctr);
+  if (c->cfg.edge_filter)
+    k_extract<true><<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
+        (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k, (uint64_t *)c->records.p, cap,
+        (unsigned long long *)c->bucket_cnt.p, (uint8_t *)c->blk_cnt.p, (const uint64_t *)c->k1tab.p, c->k1slots,
+        c->dctr);
+  else
+    k_extract<false><<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
+        (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k, (uint64_t *)c->records.p, cap,
+        (unsigned long long *)c->bucket_cnt.p, (uint8_t *)c->blk_cnt.p, nullptr, 0, c->dctr);
   k_hll_merge<<<HLL_M / 256, 256, 0, c->stream>>>((const uint8_t *)c->blk_cnt.p, eb, c->dctr);
   c->launches += 2;
   cudaEventRecord(c->kev[1], c->stream);
@@ -1736,8 +1866,50 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
   return set_err(c, BRUNO_ERR_TABLE_FULL, "k-mer table full after regrowth");
 }
 
+/* compute_edge_frequency: the (k+1)-mer table, sized from its own distinct estimate and
+ * regrown if a probe run overflows, then thresholded */
+bruno_status build_k1_table(Ctx *c) {
+  bruno_status st;
+  const int sms = num_sms();
+  const uint64_t nreads = c->n_reads;
+  const int hb = std::max(1, std::min<int>(sms * 4, (int)((nreads + TPB - 1) / TPB)));
+  if ((st = ensure(c, c->blk_cnt, (size_t)hb * HLL_M)) != BRUNO_OK) return st;
+  k_k1_hll<<<hb, TPB, 0, c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k,
+                                      (uint8_t *)c->blk_cnt.p);
+  k_hll_merge<<<HLL_M / 256, 256, 0, c->stream>>>((const uint8_t *)c->blk_cnt.p, hb, c->dctr);
+  c->launches += 2;
+  if ((st = sync_counters(c, true)) != BRUNO_OK) return st;
+  uint64_t slots = (uint64_t)(hll_estimate(c->hctr->hll) * 2.2) + 1024;
+  const int gb = std::max(1, std::min<int>(sms * 8, (int)((nreads + TPB - 1) / TPB)));
+  for (int attempt = 0; attempt < 4; ++attempt, slots *= 2) {
+    if ((st = ensure(c, c->k1tab, slots * 16)) != BRUNO_OK) return st;
+    c->k1slots = slots;
+    k_k1_init<<<sms * 8, TPB, 0, c->stream>>>((uint64_t *)c->k1tab.p, slots);
+    cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
+    k_k1_count<<<gb, TPB, 0, c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k,
+                                          (uint64_t *)c->k1tab.p, slots, 4096u, c->dctr);
+    c->launches += 2;
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    if (c->hctr->err & DERR_TABLE_FULL) continue;
+    const uint64_t lo = c->cfg.thresh[2], hi = c->cfg.thresh[3];
+    if (lo > 0 || hi < 65536) {
+      k_k1_threshold<<<sms * 8, TPB, 0, c->stream>>>((uint64_t *)c->k1tab.p, slots, lo, hi);
+      c->launches += 1;
+    }
+    return BRUNO_OK;
+  }
+  return set_err(c, BRUNO_ERR_TABLE_FULL, "(k+1)-mer table full after regrowth");
+}
+
 template <class KT>
 bruno_status count_typed(Ctx *c) {
+  if (c->cfg.edge_filter) {   /* the (k+1)-mer filter works on the partitioned path (k <= 31) */
+    bruno_status st = build_k1_table(c);
+    if (st != BRUNO_OK) return st;
+    bool used = false;
+    if ((st = count_partitioned(c, used)) != BRUNO_OK) return st;
+    return used ? BRUNO_OK : set_err(c, BRUNO_ERR_TABLE_FULL, "a hash bucket overflowed under the (k+1)-mer filter");
+  }
   if (sizeof(KT) == 8 && c->force_direct_count != 1) {
     bool used = false;
     bruno_status st = count_partitioned(c, used);
@@ -1772,7 +1944,7 @@ bruno_status filter_typed(Ctx *c, const uint64_t *thr) {
   a.g = c->geom;
   a.k = c->cfg.k;
   for (int i = 0; i < 6; ++i) a.t[i] = thr[i];
-  a.thresholding = c->cfg.thresholding;
+  a.thresholding = c->cfg.thresholding && !c->cfg.edge_filter;   /* the (k+1)-mer path inserts unthresholded */
   a.max_probe = 4096u;
   a.ctr = c->dctr;
   /* every node is a chain or a branch node: lists sized by the claimed slots */

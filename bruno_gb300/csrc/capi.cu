@@ -78,9 +78,11 @@ bruno_status bruno_ctx_create(const bruno_cfg *cfg, bruno_ctx **out) {
   if (!cfg || !out) return BRUNO_ERR_ARG;
   *out = nullptr;
   if (cfg->k < 3 || cfg->k > 63) return BRUNO_ERR_ARG;
+  if (cfg->edge_filter && cfg->thresholding && (cfg->k > 31 || cfg->direct_count == 1)) return BRUNO_ERR_ARG;
   bruno_ctx *c = new (std::nothrow) bruno_ctx();
   if (!c) return BRUNO_ERR_OOM;
   c->cfg = *cfg;
+  if (!c->cfg.thresholding) c->cfg.edge_filter = 0;   /* build_index: no filter at all */
   c->W = cfg->k <= 31 ? 1 : 2;
   c->exact_ranking = cfg->exact_ranking != 0;
   c->force_direct_count = cfg->direct_count;
@@ -106,7 +108,7 @@ bruno_status bruno_ctx_destroy(bruno_ctx *c) {
   Buf *bufs[] = {&c->rstart, &c->rend, &c->tile_cnt, &c->tile_base, &c->table, &c->k2_keys, &c->k2_edges, &c->k2_counts,
                  &c->f_keys, &c->f_edges, &c->f_counts, &c->blk_cnt, &c->blk_base, &c->ckey, &c->cedge,
                  &c->cstate, &c->cstate2, &c->pend, &c->pay, &c->unf0, &c->unf1, &c->removed, &c->r_K, &c->r_rep, &c->r_dist,
-                 &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list, &c->e_ends, &c->e_freqs, &c->s_kmers, &c->s_dist, &c->s_flags,
+                 &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list, &c->e_ends, &c->e_freqs, &c->s_kmers, &c->s_dist, &c->s_flags, &c->k1tab,
                  &c->records, &c->bucket_cnt, &c->records2, &c->sub_cnt};
   for (Buf *b : bufs) release(*b);
   for (Buf &b : c->seg_bufs) release(b);

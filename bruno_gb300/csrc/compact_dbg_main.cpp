@@ -8,6 +8,9 @@
  *               three values = k, k+1, k+2; :937-961)
  *   -R          list_rank_min_update, else list_rank
  *   -B          benchmark: only .chain.fasta and .branch.fasta
+ *   -E          with -T: the (k+1)-mer edge filter of the blocked driver
+ *               test/test/compact_debruijn_graph_block_construct.cpp (build_index_thresholded
+ *               :417-470; -L / -U bound the (k+1)-mer counts) instead of the (k+2)-mer filter
  *   -O prefix   output prefix
  *   -k K        k-mer length (the reference's compile-time pK)
  *   files...    FASTQ files, all counted into one table
@@ -104,6 +107,7 @@ int main(int argc, char **argv) {
     if (a == "-T") cfg.thresholding = 1;
     else if (a == "-R") cfg.min_update = 1;
     else if (a == "-B") benchmark = true;
+    else if (a == "-E") cfg.edge_filter = 1;
     else if (a == "-L" && i + 1 < argc) lo.push_back(strtoull(argv[++i], nullptr, 10));
     else if (a == "-U" && i + 1 < argc) hi.push_back(strtoull(argv[++i], nullptr, 10));
     else if (a == "-O" && i + 1 < argc) prefix = argv[++i];
@@ -113,7 +117,7 @@ int main(int argc, char **argv) {
     else files.push_back(argv[i]);
   }
   if (files.empty()) {
-    fprintf(stderr, "usage: %s [-T] [-L n].. [-U n].. [-R] [-B] [-O prefix] [-k K] reads.fastq..\n", argv[0]);
+    fprintf(stderr, "usage: %s [-T] [-E] [-L n].. [-U n].. [-R] [-B] [-O prefix] [-k K] reads.fastq..\n", argv[0]);
     return 1;
   }
   const std::vector<uint64_t> t = bruno_gb300::thresholds(lo, hi);

@@ -80,6 +80,8 @@ struct Ctx {
   bool h2d_pending = false;      /* ev[7] marks the start of this build's host-to-device copies */
   int force_direct_count = 0;    /* cfg.direct_count: 0 automatic, 1 whole table, 2 L2 partitions */
   Buf chain_list, branch_list;   /* slot indices, filled by the filter */
+  Buf k1tab;                     /* the (k+1)-mer edge filter's (key, count) table */
+  uint64_t k1slots = 0;
 
   /* dumps */
   Buf k2_keys, k2_edges, k2_counts;

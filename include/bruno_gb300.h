@@ -62,6 +62,13 @@ typedef struct bruno_cfg {
                                through L2 when a partition is too large for that), 1 = every
                                instance straight into the whole table, 2 = the L2 partitions
                                always.  k > 31 always counts straight into the table. */
+  int32_t edge_filter;      /* with thresholding: 1 = the blocked driver's build_index_thresholded
+                               (test/test/compact_debruijn_graph_block_construct.cpp:417-470):
+                               canonical (k+1)-mers counted (saturating uint16) and kept in
+                               [thresh[2], thresh[3]), biedge edges whose (k+1)-mer is gone
+                               cleared, pairs left without edges dropped, the rest inserted
+                               unthresholded; k <= 31, not with direct_count = 1.  0 = the
+                               (k+2)-mer count filter (local_insert_by_freqencies). */
 } bruno_cfg;
 
 typedef struct bruno_sizes {

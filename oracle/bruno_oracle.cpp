@@ -334,6 +334,69 @@ struct Run {
    * biedge_generating_iterator::operator* (:356-372), then compute_biedge_freqencies
    * (debruijn_graph_map.hpp:1085-1141): transform_input = lex_less, distribute to the
    * owning shard, count into a uint32 (non-saturating) k2 counter. */
+  /* ------------------------------------------------ (k+1)-mer edge filter
+   * compute_edge_frequency (debruijn_biedge_filters.hpp:128-177) with KmerParser over the
+   * N-filtered reads: every (k+1)-mer of a read at least k+1 long, canonical (lex_less), in a
+   * saturating uint16 counter (CountType of compact_debruijn_graph_block_construct.cpp:151);
+   * entries with count < lo or >= hi are erased when lo > 0 or hi < 65536 (:163-171).  The
+   * keys are 128-bit so every k up to 63 fits. */
+  std::vector<OAMap<KmerKey<u128>, uint32_t>> k1;
+
+  int shard1(u128 x) const { return (int)((hash_word(x) >> 40) % (uint64_t)T); }
+
+  void count_k1mers(const char *buf, const std::vector<ReadSpan> &seqs) {
+    const int k = ko.k;
+    const KOps<u128> k1o(k + 1);
+    std::vector<std::vector<std::vector<u128>>> out(T, std::vector<std::vector<u128>>(T));
+    parallel(T, [&](int t) {
+      size_t b = seqs.size() * t / T, e = seqs.size() * (t + 1) / T;
+      std::vector<int> codes;
+      for (size_t r = b; r < e; ++r) {
+        const unsigned char *s = (const unsigned char *)buf + seqs[r].off;
+        const uint32_t L = seqs[r].len;
+        codes.resize(L);
+        bool ok = true;
+        for (uint32_t i = 0; i < L; ++i) { codes[i] = char_code(s[i]); ok &= codes[i] >= 0; }
+        if (!ok || L < (uint32_t)k + 1) continue;
+        u128 x = 0;
+        for (int i = 0; i < k; ++i) x = (x << 2) | (u128)codes[i];
+        for (uint32_t p = 0; p + k + 1 <= L; ++p) {
+          x = ((x << 2) | (u128)codes[p + k]) & k1o.mask;
+          const u128 y = k1o.rc(x), c = x < y ? x : y;
+          out[t][shard1(c)].push_back(c);
+        }
+      }
+    });
+    const uint64_t lo = cfg.thresh[2], hi = cfg.thresh[3];
+    const bool erase = lo > 0 || hi < 65536;
+    k1.resize(T);
+    parallel(T, [&](int s) {
+      size_t total = 0;
+      for (int t = 0; t < T; ++t) total += out[t][s].size();
+      k1[s].init(total / 4 + 16);
+      for (int t = 0; t < T; ++t) {
+        for (const u128 &x : out[t][s]) {
+          bool ins;
+          uint32_t &c = k1[s].get(KmerKey<u128>{x}, &ins);
+          if (c < 0xFFFFu) ++c;
+        }
+        std::vector<u128>().swap(out[t][s]);
+      }
+      if (erase)
+        for (size_t i = 0; i < k1[s].keys.size(); ++i)
+          if (k1[s].state[i] == 1 && (k1[s].vals[i] < lo || k1[s].vals[i] >= hi)) k1[s].erase_slot(i);
+    });
+  }
+
+  /* the read-orientation (k+1)-mer at codes[p..p+k] kept by the counter? */
+  bool k1_exists(const std::vector<int> &codes, uint32_t p) const {
+    const KOps<u128> k1o(ko.k + 1);
+    u128 x = 0;
+    for (int i = 0; i <= ko.k; ++i) x = (x << 2) | (u128)codes[p + i];
+    const u128 y = k1o.rc(x), c = x < y ? x : y;
+    return const_cast<OAMap<KmerKey<u128>, uint32_t> &>(k1[shard1(c)]).find(KmerKey<u128>{c}) != nullptr;
+  }
+
   bool parse_and_count(const char *buf, size_t n) {
     double t0 = now();
     std::vector<ReadSpan> seqs;
@@ -341,6 +404,7 @@ struct Run {
     if (!split_fastq(buf, n, seqs, records)) return false;
     res->n_reads = records;
     const int k = ko.k;
+    if (cfg.edge_filter) count_k1mers(buf, seqs);
     std::vector<std::vector<std::vector<std::pair<W, uint8_t>>>> out(T, std::vector<std::vector<std::pair<W, uint8_t>>>(T));
     std::vector<uint64_t> used(T, 0), inst(T, 0);
     parallel(T, [&](int t) {
@@ -361,10 +425,20 @@ struct Run {
           km = ((km << 2) | W(codes[p + k - 1])) & ko.mask;
           unsigned in = p > 0 ? (1u << codes[p - 1]) : 0u;
           unsigned o = (p + k < L) ? (1u << codes[p + k]) : 0u;
+          ++inst[t];
+          if (cfg.edge_filter) {
+            /* transform_biedges_by_frequency (debruijn_biedge_filters.hpp:331-423): an edge
+             * whose (k+1)-mer the counter lost is cleared; filter_isolated_nodes (:66-75)
+             * drops a pair left without edges.  (The reference checks a k-mer's in edge
+             * through the out edge of the k-mer before it in parse order: the same
+             * (k+1)-mer within a read, and an empty edge at a read's start either way.) */
+            if (in && !k1_exists(codes, p - 1)) in = 0;
+            if (o && !k1_exists(codes, p)) o = 0;
+            if (!in && !o) continue;
+          }
           W ck = km; uint8_t e2 = (uint8_t)((in << 4) | o);
           canonical(ck, e2);
           out[t][shard(ck)].emplace_back(ck, e2);
-          ++inst[t];
         }
       }
     });
@@ -1038,7 +1112,13 @@ extern "C" int oracle_run(const char *fastq, size_t nbytes, const oracle_cfg *cf
    * compare directly; k = 32 still computes in one 64-bit word, as Kmer<32> does */
   r->words = cfg->k <= 31 ? 1 : 2;
   oracle_cfg c = *cfg;
-  if (!c.thresholding) {
+  if (c.edge_filter && !c.thresholding) c.edge_filter = 0;   /* build_index: no filter at all */
+  if (c.edge_filter) {
+    /* the (k+1)-mer bounds stay in thresh[2..3]; the node insert is build_index's */
+    c.thresholding = 0;
+    c.thresh[0] = c.thresh[4] = 0;
+    c.thresh[1] = c.thresh[5] = ~0ULL;
+  } else if (!c.thresholding) {
     /* build_index: no flags (every entry kept with both edges) */
     c.thresh[0] = c.thresh[2] = c.thresh[4] = 0;
     c.thresh[1] = c.thresh[3] = c.thresh[5] = ~0ULL;

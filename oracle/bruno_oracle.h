@@ -34,6 +34,10 @@ typedef struct oracle_cfg {
   int32_t threads;          /* host threads = hash shards (stand-in for MPI ranks); 0 = 1 */
   int32_t keep_k2;          /* 1: keep the unfiltered (k+2)-mer count table for output */
   int32_t keep_filtered;    /* 1: keep the filtered (k+2)-mer entries for output */
+  int32_t edge_filter;      /* 1 (with thresholding): the blocked driver's build_index_thresholded
+                               (compact_debruijn_graph_block_construct.cpp:417-470): (k+1)-mers
+                               counted and kept in [thresh[2], thresh[3]), biedges losing the
+                               edges whose (k+1)-mer is gone, then the unthresholded insert */
 } oracle_cfg;
 
 /* Phase timers, seconds, named after the reference's BL_BENCH phases. */

@@ -20,7 +20,7 @@ PHASES = ("parse", "count_k2mers", "filter_insert", "chainmap", "list_rank", "co
 class _Cfg(ctypes.Structure):
     _fields_ = [("k", ctypes.c_int32), ("thresholding", ctypes.c_int32), ("thresh", ctypes.c_uint64 * 6),
                 ("min_update", ctypes.c_int32), ("threads", ctypes.c_int32), ("keep_k2", ctypes.c_int32),
-                ("keep_filtered", ctypes.c_int32)]
+                ("keep_filtered", ctypes.c_int32), ("edge_filter", ctypes.c_int32)]
 
 
 _U64P = ctypes.POINTER(ctypes.c_uint64)
@@ -99,7 +99,7 @@ def _arr(ptr, n, dtype, shape=None):
 
 def run(fastq, k: int = 31, thresholding: bool = True, thresh=None, min_update: bool = True, threads: int = 1,
         keep_k2: bool = False, keep_filtered: bool = False, write_prefix: str | None = None,
-        benchmark: bool = False) -> dict:
+        benchmark: bool = False, edge_filter: bool = False) -> dict:
     """Runs the oracle on FASTQ bytes (or a uint8 array); returns numpy results."""
     lib = _load()
     buf = np.ascontiguousarray(np.frombuffer(fastq, np.uint8) if isinstance(fastq, (bytes, bytearray)) else fastq,
@@ -109,7 +109,7 @@ def run(fastq, k: int = 31, thresholding: bool = True, thresh=None, min_update: 
     t = thresh if thresh is not None else [65536] * 6
     for i in range(6):
         c.thresh[i] = int(min(t[i], 2**64 - 1))
-    c.keep_k2, c.keep_filtered = int(keep_k2), int(keep_filtered)
+    c.keep_k2, c.keep_filtered, c.edge_filter = int(keep_k2), int(keep_filtered), int(edge_filter)
     rp = ctypes.POINTER(_Res)()
     rc = lib.oracle_run(buf.ctypes.data_as(ctypes.c_void_p), buf.nbytes, ctypes.byref(c), ctypes.byref(rp))
     try:

@@ -20,6 +20,8 @@ CASES = [
     ("debruijn.bubble.fastq", ["-T", "-L", "1", "-L", "2", "-L", "1", "-R"]),
     ("natural.withN.fastq", []),
     ("debruijn.palindrome_chr14.fastq", ["-T", "-L", "2", "-L", "2", "-L", "2", "-R"]),
+    ("debruijn.bubble.fastq", ["-T", "-E", "-L", "2", "-R"]),
+    ("test.medium.fastq", ["-T", "-E", "-L", "3"]),
 ]
 OUTPUTS = [".chain.fasta", ".chain.components", ".chain.edges", ".chain.summary", ".branch.fasta", ".branch.edges",
            ".graph.all"]

@@ -253,3 +253,31 @@ def test_inconsistent_chain_pointers_emission(seed, mu, k):
     ref = oracle.run(fq, k=k, thresh=thr, min_update=mu, keep_k2=True, keep_filtered=True)
     assert_same(sort_nodes(*a["nodes"]), ref["nodes"], "graph nodes")
     assert a["sizes"]["n_chain_nodes"] == ref["n_chain_nodes"]
+
+
+@pytest.mark.parametrize("lo", [1, 2, 3])
+@pytest.mark.parametrize("fname", FASTQS)
+def test_edge_filter_parity(fname, lo):
+    """the blocked driver's (k+1)-mer edge-filter build: every output equals the oracle's,
+    step by step and in one call"""
+    thr = bg.thresholds([lo])
+    data = fixture_bytes(fname)
+    ref = oracle.run(data, k=31, thresh=thr, min_update=True, keep_k2=True, keep_filtered=True, edge_filter=True)
+    compare(gpu_run(data, 31, True, thr, True, edge_filter=True), ref)
+    compare_one_call(one_call_run(data, 31, True, thr, True, edge_filter=True), ref)
+
+
+def test_edge_filter_workload_parity():
+    """the 1 Mbp / 100k x 100 bp / 1% workload through the (k+1)-mer edge filter, both rankings"""
+    w = synth.WORKLOADS["plain-small"]
+    fq = synth.make_fastq(w)
+    thr = bg.thresholds(w.lower)
+    for mu in (True, False):
+        ref = oracle.run(fq, k=31, thresh=thr, min_update=mu, threads=16, keep_k2=True, keep_filtered=True,
+                         edge_filter=True)
+        compare(gpu_run(fq, 31, True, thr, mu, edge_filter=True), ref)
+
+
+def test_edge_filter_rejects_large_k():
+    with pytest.raises(bg.BrunoError):
+        bg.Graph(k=33, thresh=bg.thresholds([2]), edge_filter=True)

@@ -213,6 +213,71 @@ def test_compress_ranked_restatement(seed, k):
     assert chain_set(*r["chains"]) == compress_ranked(*r["ranked"], k)
 
 
+def _edge_filter_nodes(fq: bytes, k: int, lo: int, hi: int = 65536):
+    """the blocked driver's build_index_thresholded restated in Python: canonical (k+1)-mer
+    counts (saturating at 65535), those outside [lo, hi) erased; per read position the biedge
+    loses each edge whose (k+1)-mer is gone; pairs without edges are dropped; the rest update
+    their canonical node: self count and one count per present edge"""
+    lines = fq.decode().split("\n")
+    reads = [lines[i + 1].upper() for i in range(0, len(lines) - 3, 4) if lines[i].startswith("@")]
+    reads = [r for r in reads if set(r) <= set("ACGT")]
+    k1 = {}
+    for r in reads:
+        for p in range(len(r) - k):
+            x = r[p:p + k + 1]
+            c = min(x, _rc(x))
+            k1[c] = min(65535, k1.get(c, 0) + 1)
+    keep = {x for x, c in k1.items() if lo <= c < hi}
+    nodes = {}
+    comp = {"A": "T", "C": "G", "G": "C", "T": "A"}
+    for r in reads:
+        if len(r) < k + 2:
+            continue
+        for p in range(len(r) - k + 1):
+            x = r[p:p + k]
+            i = r[p - 1] if p > 0 else None
+            o = r[p + k] if p + k < len(r) else None
+            if i and min(i + x, _rc(i + x)) not in keep:
+                i = None
+            if o and min(x + o, _rc(x + o)) not in keep:
+                o = None
+            if i is None and o is None:
+                continue
+            if x > _rc(x) or x == _rc(x):          # lex_less keeps x only when x < rc(x)
+                x, i, o = _rc(x), (comp[o] if o else None), (comp[i] if i else None)
+            c = nodes.setdefault(x, [0] * 9)
+            if o:
+                c["ACGT".index(o)] = min(65535, c["ACGT".index(o)] + 1)
+            if i:
+                c[4 + "ACGT".index(i)] = min(65535, c[4 + "ACGT".index(i)] + 1)
+            c[8] = min(65535, c[8] + 1)
+    return nodes
+
+
+@pytest.mark.parametrize("fname,lo", [("debruijn.palindrome_chr14.fastq", 2), ("debruijn.bubble.fastq", 3),
+                                      ("test.star.unitiqs.fastq", 1), ("debruijn.shifted_cycle_chr14.fastq", 2)])
+def test_edge_filter_nodes_restated(fname, lo):
+    """the oracle's (k+1)-mer edge-filter build (compact_debruijn_graph_block_construct.cpp:
+    417-470, debruijn_biedge_filters.hpp:66-75, 128-177, 331-423) against a second restatement
+    of it: the same graph nodes with the same nine counters"""
+    k = 31
+    fq = fixture_bytes(fname)
+    r = oracle.run(fq, k=k, thresh=bg.thresholds([lo]), edge_filter=True)
+    keys, counts, _ = r["nodes"]
+    got = {_ascii(keys[i], k): list(map(int, counts[i])) for i in range(len(keys))}
+    want = _edge_filter_nodes(fq, k, lo)
+    assert got == want
+    assert len(got) > 0
+
+
+def test_edge_filter_without_bounds_is_build_index():
+    """with no (k+1)-mer erased the edge filter changes nothing: the unthresholded build"""
+    fq = fixture_bytes("debruijn.bubble.fastq")
+    a = oracle.run(fq, k=31, thresh=bg.thresholds([0]), edge_filter=True)
+    b = oracle.run(fq, k=31, thresholding=False)
+    assert MG.digest(a) == MG.digest(b)
+
+
 def test_malformed_fastq_rejected():
     r = oracle.run(fixture_bytes("test.medium.fastq").replace(b"\n+\n", b"\n-\n", 1), k=31)
     assert r["status"] == 2
