@@ -1018,8 +1018,7 @@ __device__ __forceinline__ bool filter_quick(uint64_t *s, const uint32_t *w, int
     const uint32_t c16 = min(cmax32, entry_count(w[q]));
     t.hist.add(fk | ((c16 < a.t[4] || c16 >= a.t[5]) ? 4u : 0u));
   }
-  if (KWD == 1) s[0] = KEY_TOMB; else { s[0] = KEY_TOMB; s[1] = KEY_TOMB; }
-  return true;
+  return true;   /* the slot keeps its bare key: not a node */
 }
 
 template <class KT, int CAP, bool QUICK = true>
@@ -1103,10 +1102,7 @@ __device__ __forceinline__ void filter_kmer(uint64_t *s, uint64_t slot_index, KT
       }
     }
   }
-  if (!any) {  /* no kept entry: the k-mer never enters the graph */
-    if (KWD == 1) s[0] = KEY_TOMB; else { s[0] = KEY_TOMB; s[1] = KEY_TOMB; }
-    return;
-  }
+  if (!any) return;  /* no kept entry: the k-mer never enters the graph (its key stays bare) */
   uint16_t c16[9];
   #pragma unroll
   for (int q = 0; q < 9; ++q) c16[q] = (uint16_t)min(cmax32, nc[q]);
@@ -1129,6 +1125,7 @@ __device__ __forceinline__ void filter_kmer(uint64_t *s, uint64_t slot_index, KT
   pw[0] = (uint64_t)c16[0] | ((uint64_t)c16[1] << 16) | ((uint64_t)c16[2] << 32) | ((uint64_t)c16[3] << 48);
   pw[1] = (uint64_t)c16[4] | ((uint64_t)c16[5] << 16) | ((uint64_t)c16[6] << 32) | ((uint64_t)c16[7] << 48);
   pw[2] = (uint64_t)c16[8] | ((uint64_t)flags << 16) | (0xFFFFFFFFull << 32);
+  KOps<KT>::store(s, as_node(tkey));   /* the key we hold, marked: no reload of the slot */
 }
 
 /* A k-mer with more biedges than one slot holds: gather the entries of its continuation
@@ -1546,10 +1543,10 @@ __global__ void __launch_bounds__(TPB) k_dump_nodes(const uint64_t *table, uint6
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t *s = table + i * SU;
     KT key = KOps<KT>::load(s);
-    if (key_dead(key)) continue;
+    if (!key_is_node(key)) continue;
     unsigned long long o = atomicAdd(n, 1ull);
     if (o >= cap) continue;
-    KOps<KT>::store(keys + o * KWD, key_kmer(key));
+    KOps<KT>::store(keys + o * KWD, key_kmer(node_key(key)));
     const uint64_t *pw = s + KWD;
     for (int q = 0; q < 4; ++q) {
       counts[o * 9 + q] = (uint16_t)(pw[0] >> (16 * q));

@@ -85,10 +85,6 @@ __device__ __forceinline__ unsigned long long warp_append(bool want, unsigned lo
 }
 
 template <class KT>
-__device__ __forceinline__ bool slot_dead(const uint64_t *s) {
-  return (s[Slot<KT>::KEYW - 1] & KEY_DEAD_BIT) != 0;
-}
-template <class KT>
 __device__ __forceinline__ uint32_t slot_flags(const uint64_t *s) {
   return (uint32_t)(s[Slot<KT>::KEYW + 2] >> 16) & 0xFFFFu;
 }
@@ -102,8 +98,8 @@ template <class KT>
 __device__ __forceinline__ long long table_find(const uint64_t *table, const TableGeom &g, uint32_t max_probe,
                                                 KT kmer) {
   constexpr int SU = Slot<KT>::U64;
-  const KT x = table_key(kmer);
-  Probe pr(g, table_home(g, x));
+  const KT bare = table_key(kmer), x = as_node(bare);
+  Probe pr(g, table_home(g, bare));
   for (uint32_t p = 0; p < max_probe; ++p, pr.next()) {
     const uint64_t *s = table + pr.i * SU;
     KT key = KOps<KT>::load(s);
@@ -128,8 +124,9 @@ __device__ __forceinline__ void table_find2(const uint64_t *table, const TableGe
   for (int q = 0; q < 2; ++q) {
     found[q] = -1;
     done[q] = !has[q];
-    x[q] = table_key(want[q]);
-    const Probe pr(g, table_home(g, x[q]));
+    const KT bare = table_key(want[q]);
+    x[q] = as_node(bare);
+    const Probe pr(g, table_home(g, bare));
     pos[q] = pr.i; lo[q] = pr.lo; hi[q] = pr.hi;
   }
   for (uint32_t p = 0; p < max_probe && !(done[0] && done[1]); ++p) {
@@ -164,7 +161,7 @@ __global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, uint6
     }
     uint64_t own[SU];
     ld_slot<SU>(table + sl * SU, own);
-    const KT K = key_kmer(KOps<KT>::load(own));
+    const KT K = key_kmer(node_key(KOps<KT>::load(own)));
     KOps<KT>::store(ckey + i * KWD, K);
     const uint64_t *pw = own + KWD;
     int inc = -1, outc = -1;
@@ -213,7 +210,7 @@ __global__ void __launch_bounds__(TPB) k_termini(const uint64_t *table, TableGeo
   constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
   for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nb; q += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t *s = table + (uint64_t)branch_list[q] * SU;
-    const KT K = key_kmer(KOps<KT>::load(s));
+    const KT K = key_kmer(node_key(KOps<KT>::load(s)));
     const uint64_t *pw = s + KWD;
     for (int c = 0; c < 4; ++c) {
       if ((pw[0] >> (16 * c)) & 0xFFFFu) {  /* out neighbour receives (branch, IN) */

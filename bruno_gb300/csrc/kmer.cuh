@@ -279,4 +279,16 @@ __device__ __forceinline__ bool key_dead(KW2 k) { return (k.hi & KEY_DEAD_BIT) !
 __device__ __forceinline__ bool key_cont(KW1 k) { return (k.v & KEY_CONT) != 0; }
 __device__ __forceinline__ bool key_cont(KW2 k) { return (k.hi & KEY_CONT) != 0; }
 
+/* After the filter a graph node's key carries KEY_NODE -- the continuation bit, free by then
+ * because the filter folds every continuation slot into its k-mer's first slot -- and a k-mer
+ * the filter dropped keeps its bare key, so dropping one costs no write.  Homes are always
+ * computed from the bare key. */
+constexpr uint64_t KEY_NODE = KEY_CONT;
+__device__ __forceinline__ bool key_is_node(KW1 k) { return (k.v & (KEY_DEAD_BIT | KEY_NODE)) == KEY_NODE; }
+__device__ __forceinline__ bool key_is_node(KW2 k) { return (k.hi & (KEY_DEAD_BIT | KEY_NODE)) == KEY_NODE; }
+__device__ __forceinline__ KW1 node_key(KW1 k) { return {k.v & ~KEY_NODE}; }
+__device__ __forceinline__ KW2 node_key(KW2 k) { return {k.lo, k.hi & ~KEY_NODE}; }
+__device__ __forceinline__ KW1 as_node(KW1 k) { return {k.v | KEY_NODE}; }
+__device__ __forceinline__ KW2 as_node(KW2 k) { return {k.lo, k.hi | KEY_NODE}; }
+
 }  // namespace bg
