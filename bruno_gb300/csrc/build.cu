@@ -93,19 +93,30 @@ __global__ void __launch_bounds__(TPB) k_tile_stats(const unsigned char *buf, ui
   const uint64_t t1 = (n < t0 + TILE ? n : t0 + TILE);
   unsigned long long cnt = 0;
   long long lastnw = -1;
-  for (uint64_t p = t0 + 16ull * threadIdx.x; p < t1; p += 16ull * TPB) {
-    const uint4 v = load16(buf, p, t1, aligned);
-    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+  /* four 16-byte loads in flight per thread, then their bytes */
+  for (uint64_t p0 = t0 + 16ull * threadIdx.x; p0 < t1; p0 += 64ull * TPB) {
+    uint4 v[4];
     #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const uint32_t nl = bytes_eq(w[q], 0x0A0A0A0Au), cr = bytes_eq(w[q], 0x0D0D0D0Du);
-      cnt += __popc(nl) >> 3;
-      uint32_t keep = ~(nl | cr);
-      /* bytes beyond the tile end are zero padding, not data */
-      const uint64_t base = p + 4 * q;
-      if (base >= t1) keep = 0;
-      else if (base + 4 > t1) keep &= (1u << (8 * (t1 - base))) - 1u;
-      if (keep) lastnw = max(lastnw, (long long)(base + ((31 - __clz(keep)) >> 3)));
+    for (int u = 0; u < 4; ++u) {
+      const uint64_t p = p0 + 16ull * TPB * u;
+      v[u] = p < t1 ? load16(buf, p, t1, aligned) : make_uint4(0u, 0u, 0u, 0u);
+    }
+    #pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint64_t p = p0 + 16ull * TPB * u;
+      if (p >= t1) continue;
+      const uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+      #pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t nl = bytes_eq(w[q], 0x0A0A0A0Au), cr = bytes_eq(w[q], 0x0D0D0D0Du);
+        cnt += __popc(nl) >> 3;
+        uint32_t keep = ~(nl | cr);
+        /* bytes beyond the tile end are zero padding, not data */
+        const uint64_t base = p + 4 * q;
+        if (base >= t1) keep = 0;
+        else if (base + 4 > t1) keep &= (1u << (8 * (t1 - base))) - 1u;
+        if (keep) lastnw = max(lastnw, (long long)(base + ((31 - __clz(keep)) >> 3)));
+      }
     }
   }
   __shared__ unsigned long long sc[TPB / 32];
@@ -134,25 +145,32 @@ __global__ void __launch_bounds__(TPB) k_index_lines(const unsigned char *buf, u
   uint64_t base = tile_base[blockIdx.x];
   unsigned long long nl_eff = 0;  /* newlines ending lines before E, max over this thread */
   if (blockIdx.x == 0 && threadIdx.x == 0 && E > 0 && buf[0] != '@') atomicMin(&ctr->bad_line, 0ull);
-  /* stripes of TPB*16 bytes, 16 consecutive bytes per thread, in byte order */
-  for (uint64_t s0 = t0; s0 < t1; s0 += (uint64_t)TPB * 16) {
-    const uint64_t g0 = s0 + (uint64_t)threadIdx.x * 16;
-    uint32_t m = 0;
-    if (g0 < t1) {
-      const uint4 v = load16(buf, g0, t1, aligned);
-      const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+  /* stripes of TPB*64 bytes, 64 consecutive bytes per thread (four 16-byte loads in flight),
+   * in byte order: one block scan per stripe */
+  for (uint64_t s0 = t0; s0 < t1; s0 += (uint64_t)TPB * 64) {
+    const uint64_t g0 = s0 + (uint64_t)threadIdx.x * 64;
+    uint64_t m = 0;
+    uint4 v[4];
+    #pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint64_t p = g0 + 16ull * u;
+      v[u] = p < t1 ? load16(buf, p, t1, aligned) : make_uint4(0u, 0u, 0u, 0u);
+    }
+    #pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
       #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const uint32_t nl = bytes_eq(w[q], 0x0A0A0A0Au);   /* 0xFF per newline byte */
         #pragma unroll
-        for (int b = 0; b < 4; ++b) m |= ((nl >> (8 * b + 7)) & 1u) << (4 * q + b);
+        for (int b = 0; b < 4; ++b) m |= (uint64_t)((nl >> (8 * b + 7)) & 1u) << (16 * u + 4 * q + b);
       }
     }
     uint32_t total;
-    const uint32_t rank = block_exscan(__popc(m), total);
+    const uint32_t rank = block_exscan((uint32_t)__popcll(m), total);
     uint64_t j = base + rank;
     while (m) {
-      int i = __ffs(m) - 1;
+      int i = __ffsll((long long)m) - 1;
       m &= m - 1;
       const uint64_t p = g0 + i;
       if ((long long)p < E) {
