@@ -1398,7 +1398,7 @@ __global__ void __launch_bounds__(PTPB) k_count_local(const uint64_t *recs, cons
   const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(sm);
   for (uint32_t v = tid; v < region * 2u; v += PTPB) dst[v] = src[v];
   slots = warp_sum(slots); entries = warp_sum(entries);
-  if ((tid & 31) == 0) {
+  if ((tid & 31) == 0) {   /* reductions without a returned value: nothing waits on them */
     if (slots) atomicAdd(&ctr->n_slots_claimed, slots);
     if (entries) atomicAdd(&ctr->n_entries, entries);
   }

@@ -84,6 +84,19 @@ __device__ __forceinline__ unsigned long long warp_append(bool want, unsigned lo
   return base + __popc(m & ((1u << lane) - 1));
 }
 
+/* block-aggregated append: one atomic on `counter` per block and call (all threads of the
+ * block must call it together); returns this thread's slot if `want` */
+__device__ __forceinline__ unsigned long long block_append(bool want, unsigned long long *counter) {
+  __shared__ unsigned long long s_base;
+  uint32_t total;
+  const uint32_t r = block_exscan(want ? 1u : 0u, total);
+  if (threadIdx.x == 0) s_base = total ? atomicAdd(counter, (unsigned long long)total) : 0ull;
+  __syncthreads();
+  const unsigned long long b = s_base;
+  __syncthreads();   /* everyone has read s_base before a next call writes it */
+  return b + r;
+}
+
 template <class KT>
 __device__ __forceinline__ uint32_t slot_flags(const uint64_t *s) {
   return (uint32_t)(s[Slot<KT>::KEYW + 2] >> 16) & 0xFFFFu;
@@ -389,7 +402,7 @@ __global__ void __launch_bounds__(TPB) k_fast_check(ChainState *cs, uint64_t M, 
       }
       ruler = term_side || (mix64(v * 0x9e3779b97f4a7c15ull + 0x632be59bd9b4e019ull) % RULER_SAMPLE) == 0;
     }
-    const unsigned long long o = warp_append(ruler, &ctr->lr_remaining);
+    const unsigned long long o = block_append(ruler, &ctr->lr_remaining);
     if (v < M) cs[v].pad = ruler ? o : (uint64_t)NONE32;
     if (ruler) rnode[o] = (uint32_t)v;
   }
@@ -453,7 +466,12 @@ __global__ void __launch_bounds__(TPB) k_fast_jump(const Jump *E, Jump *F, uint6
     F[q] = e;
   }
   undone = warp_sum(undone);
-  if ((threadIdx.x & 31) == 0 && undone) atomicAdd(&ctr->lr_applied, undone);
+  __shared__ unsigned long long s_undone;
+  if (threadIdx.x == 0) s_undone = 0;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0 && undone) atomicAdd(&s_undone, undone);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_undone) atomicAdd(&ctr->lr_applied, s_undone);
 }
 
 /* final state of one side: the path end in that direction, its flip, the distance */
@@ -548,11 +566,22 @@ __global__ void __launch_bounds__(TPB) k_fast_mark(const ChainState *cs, const C
   }
   ncy = warp_sum(ncy); niso = warp_sum(niso); bad = warp_sum(bad);
   for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_down_sync(~0u, mx, o));
+  /* one global atomic per counter and block: per-warp ones on the same words serialised */
+  __shared__ unsigned long long s_ncy, s_niso, s_bad, s_mx;
+  if (threadIdx.x == 0) { s_ncy = 0; s_niso = 0; s_bad = 0; s_mx = 0; }
+  __syncthreads();
   if ((threadIdx.x & 31) == 0) {
-    if (bad) atomicAdd(&ctr->lr_multi, bad);
-    if (ncy) atomicAdd(&ctr->n_cycle, ncy);
-    if (niso) atomicAdd(&ctr->n_isolated, niso);
-    if (mx) atomicMax(nmax, mx);
+    if (bad) atomicAdd(&s_bad, bad);
+    if (ncy) atomicAdd(&s_ncy, ncy);
+    if (niso) atomicAdd(&s_niso, niso);
+    if (mx) atomicMax(&s_mx, mx);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (s_bad) atomicAdd(&ctr->lr_multi, s_bad);
+    if (s_ncy) atomicAdd(&ctr->n_cycle, s_ncy);
+    if (s_niso) atomicAdd(&ctr->n_isolated, s_niso);
+    if (s_mx) atomicMax(nmax, s_mx);
   }
 }
 
@@ -629,7 +658,7 @@ __global__ void __launch_bounds__(TPB) k_ranked(EmitArgs a) {
       a.dist_of[i] = dist;
       head = dist == 0;
     }
-    const unsigned long long o = warp_append(live, &a.ctr->n_ranked);
+    const unsigned long long o = block_append(live, &a.ctr->n_ranked);
     if (live) {
       KOps<KT>::store(a.rK + o * KWD, K);
       KOps<KT>::store(a.rrep + o * KWD, rep);
