@@ -676,7 +676,7 @@ __global__ void __launch_bounds__(TPB) k_ranked(EmitArgs a) {
 }
 
 template <class KT>
-__global__ void __launch_bounds__(TPB) k_fill(EmitArgs a, const uint64_t *ch_off, char *chars, uint32_t *seen) {
+__global__ void __launch_bounds__(TPB) k_fill(EmitArgs a, const uint64_t *ch_off, char *chars) {
   constexpr int KWD = KOps<KT>::WORDS;
   const char ACGT[4] = {'A', 'C', 'G', 'T'};
   bool bad = false;
@@ -693,7 +693,6 @@ __global__ void __launch_bounds__(TPB) k_fill(EmitArgs a, const uint64_t *ch_off
     const KT R = KOps<KT>::rc(term(st.outD) ? key : ptr_kmer<KT>(st.outP, a.ckey, a.cedge, a.k), a.k);
     const bool sense = KOps<KT>::le(L, R);
     const KT K = sense ? key : KOps<KT>::rc(key, a.k);
-    atomicAdd(&seen[h], 1u);
     if (d == 0) {   /* the representative itself: all k bases */
       for (int q = 0; q < a.k; ++q) chars[off + q] = ACGT[KOps<KT>::base_lsb(K, a.k - 1 - q)];
     } else {        /* one base per node: the last base of K on the representative's strand */
@@ -705,17 +704,16 @@ __global__ void __launch_bounds__(TPB) k_fill(EmitArgs a, const uint64_t *ch_off
   if (bad) atomicOr(&a.ctr->err, (unsigned long long)DERR_UNCLEAN_CHAINS);
 }
 
-/* every chain got one node per position after the representative's k bases: node counts
- * match the lengths, and no character stayed unwritten (the buffer starts zeroed), so no two
- * nodes shared a position */
-__global__ void k_check_chains(const uint64_t *ch_off, const uint32_t *seen, uint64_t nh, int k, const char *chars,
-                               uint64_t nchars, DevCounters *ctr) {
+/* every chain position was written: no character stayed zero (the buffer starts zeroed).
+ * With every write inside its chain (k_fill checks that), the positions are then covered, and
+ * they are covered once exactly when the live nodes are as many as the positions -- one per
+ * chain for the representative's k bases plus one per further base -- which the host checks:
+ * n_ranked == n_chain_chars - n_chains * (k - 1). */
+__global__ void k_check_chains(const char *chars, uint64_t nchars, DevCounters *ctr) {
   bool bad = false;
-  for (uint64_t h = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (uint64_t)gridDim.x * blockDim.x)
-    if ((uint64_t)seen[h] + (uint64_t)(k - 1) != ch_off[h + 1] - ch_off[h]) bad = true;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nchars; i += (uint64_t)gridDim.x * blockDim.x)
     if (chars[i] == 0) bad = true;
-  if (bad) atomicOr(&ctr->err, (unsigned long long)DERR_UNCLEAN_CHAINS);
+  if (__any_sync(~0u, bad) && (threadIdx.x & 31) == 0) atomicOr(&ctr->err, (unsigned long long)DERR_UNCLEAN_CHAINS);
 }
 
 /* ================================================================ general emission
@@ -1137,7 +1135,7 @@ bruno_status compress_typed(Ctx *c) {
   if ((st = ensure(c, c->head_len, (Mb + 1) * 8)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->head_off, (Mb + 1) * 8)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->ch_rep, Mb * 8 * KWD)) != BRUNO_OK) return st;
-  if ((st = ensure(c, c->pay, Mb * 8)) != BRUNO_OK) return st;   /* reused: dist_of + seen */
+  if ((st = ensure(c, c->pay, Mb * 8)) != BRUNO_OK) return st;   /* reused: dist_of */
   cudaMemsetAsync(&c->dctr->n_ranked, 0, 8, c->stream);
   cudaMemsetAsync(&c->dctr->n_heads, 0, 8, c->stream);
   cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
@@ -1161,14 +1159,12 @@ bruno_status compress_typed(Ctx *c) {
   c->n_chain_chars = c->hctr->n_chain_chars;
   if ((st = ensure(c, c->ch_chars, std::max<uint64_t>(1, c->n_chain_chars))) != BRUNO_OK) return st;
   cudaMemsetAsync(c->ch_chars.p, 0, c->n_chain_chars, c->stream);
-  uint32_t *seen = (uint32_t *)((int32_t *)c->pay.p + Mb);
-  cudaMemsetAsync(seen, 0, Mb * 4, c->stream);
-  k_fill<KT><<<sms * 8, TPB, 0, c->stream>>>(a, (const uint64_t *)c->head_off.p, (char *)c->ch_chars.p, seen);
-  c->launches += 5;  /* k_ranked, scan, k_fill, k_check_chains, scan of heads */
-  k_check_chains<<<sms * 2, TPB, 0, c->stream>>>((const uint64_t *)c->head_off.p, seen, nh, c->cfg.k,
-                                                 (const char *)c->ch_chars.p, c->n_chain_chars, c->dctr);
+  k_fill<KT><<<sms * 8, TPB, 0, c->stream>>>(a, (const uint64_t *)c->head_off.p, (char *)c->ch_chars.p);
+  c->launches += 4;  /* k_ranked, scan, k_fill, k_check_chains */
+  k_check_chains<<<sms * 4, TPB, 0, c->stream>>>((const char *)c->ch_chars.p, c->n_chain_chars, c->dctr);
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
-  c->chains_clean = !(c->hctr->err & DERR_UNCLEAN_CHAINS);
+  c->chains_clean = !(c->hctr->err & DERR_UNCLEAN_CHAINS) &&
+                    c->n_ranked + nh * (uint64_t)(c->cfg.k - 1) == c->n_chain_chars;
   if (!c->chains_clean) return general_emission<KT>(c, a);
   return BRUNO_OK;
 }
