@@ -611,7 +611,10 @@ struct ExtractSmem {
   uint64_t q[NBUCKET][XQ];
   unsigned int hll[HLL_M];
   unsigned int cnt[NBUCKET];
-  unsigned long long base[NBUCKET];
+  unsigned long long base[NBUCKET];   /* this flush: first `rem` records from base, the rest from base2 */
+  unsigned long long base2[NBUCKET];
+  unsigned int rem[NBUCKET];
+  unsigned long long cpos[NBUCKET], cend[NBUCKET];   /* the block's current chunk of each bucket */
   int overflow;
 };
 
@@ -782,12 +785,13 @@ template <bool EF>
 __global__ void __launch_bounds__(XTPB, 2) k_extract(const uint64_t *rstart, const uint64_t *rend, uint64_t nreads,
                                                       int k, uint64_t *records, uint64_t cap,
                                                       unsigned long long *bucket_cnt, uint8_t *hll_partial,
-                                                      const uint64_t *k1tab, uint64_t k1slots, DevCounters *ctr) {
+                                                      const uint64_t *k1tab, uint64_t k1slots, uint32_t chunk,
+                                                      DevCounters *ctr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ExtractSmem &S = *reinterpret_cast<ExtractSmem *>(smem_raw);
   const int tid = threadIdx.x;
   for (int i = tid; i < HLL_M; i += XTPB) S.hll[i] = 0;
-  for (int i = tid; i < NBUCKET; i += XTPB) S.cnt[i] = 0;
+  for (int i = tid; i < NBUCKET; i += XTPB) { S.cnt[i] = 0; S.cpos[i] = 0; S.cend[i] = 0; }
   if (tid == 0) S.overflow = 0;
   __syncthreads();
   const uint64_t stride = (uint64_t)gridDim.x * XTPB;
@@ -866,25 +870,45 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract(const uint64_t *rstart, con
       }
     }
     __syncthreads();
+    /* each block fills chunks of `chunk` records per bucket, claimed with one atomic each, so
+     * most flushes need no global atomic; a chunk's unused tail is zeroed at the end (0 is no
+     * record: a biedge code is never 0) */
     if (tid < NBUCKET) {
       const unsigned f = min(S.cnt[tid], (unsigned)XQ);
       if (f) {
-        const unsigned long long old = atomicAdd(&bucket_cnt[tid], (unsigned long long)f);
-        if (old + f > cap) S.overflow = 1;
-        S.base[tid] = (unsigned long long)tid * cap + old;
+        const unsigned long long p = S.cpos[tid], avail = S.cend[tid] - p;
+        S.base[tid] = p;
+        if (avail >= f) {
+          S.rem[tid] = f;
+          S.cpos[tid] = p + f;
+        } else {
+          const unsigned long long need = f - avail, ch = max(need, (unsigned long long)chunk);
+          const unsigned long long old = atomicAdd(&bucket_cnt[tid], ch);
+          if (old + ch > cap) S.overflow = 1;
+          const unsigned long long nb = (unsigned long long)tid * cap + old;
+          S.rem[tid] = (unsigned)avail;
+          S.base2[tid] = nb;
+          S.cpos[tid] = nb + need;
+          S.cend[tid] = nb + ch;
+        }
       }
     }
     __syncthreads();
     for (int x = tid; x < NBUCKET * XQ; x += XTPB) {
       const int b = x / XQ, j = x % XQ;
       if ((unsigned)j < min(S.cnt[b], (unsigned)XQ)) {
-        const unsigned long long dst = S.base[b] + j;
+        const unsigned long long dst = (unsigned)j < S.rem[b] ? S.base[b] + j : S.base2[b] + (j - S.rem[b]);
         if (dst < (unsigned long long)(b + 1) * cap) records[dst] = S.q[b][j];
       }
     }
     __syncthreads();
     if (tid < NBUCKET) S.cnt[tid] = 0;
     if (!__syncthreads_or(active)) break;
+  }
+  /* the unused tails of the block's chunks hold no records */
+  for (int b = tid >> 5; b < NBUCKET; b += XTPB / 32) {
+    const unsigned long long e = min(S.cend[b], (unsigned long long)(b + 1) * cap);
+    for (unsigned long long p = S.cpos[b] + (tid & 31); p < e; p += 32) records[p] = 0ull;
   }
   inst = warp_sum(inst); used = warp_sum(used);
   if ((tid & 31) == 0) {
@@ -928,7 +952,7 @@ __global__ void __launch_bounds__(TPB) k_insert(const uint64_t *records, const u
   #pragma unroll
   for (int q = 0; q < INS_BATCH; ++q) {
     const uint64_t j = i + q * stride;
-    nxt[q] = j < n ? __ldcs(rb + j) : ~0ull;
+    nxt[q] = j < n ? __ldcs(rb + j) : 0ull;   /* 0: no record (past the end, or a chunk tail) */
   }
   for (; i < n; i += INS_BATCH * stride) {
     uint64_t rec[INS_BATCH], home[INS_BATCH], raw[INS_BATCH][SU];
@@ -936,18 +960,18 @@ __global__ void __launch_bounds__(TPB) k_insert(const uint64_t *records, const u
     for (int q = 0; q < INS_BATCH; ++q) {
       rec[q] = nxt[q];
       const uint64_t j = i + (INS_BATCH + q) * stride;
-      nxt[q] = j < n ? __ldcs(rb + j) : ~0ull;
+      nxt[q] = j < n ? __ldcs(rb + j) : 0ull;
     }
     #pragma unroll
     for (int q = 0; q < INS_BATCH; ++q) {
-      if (rec[q] == ~0ull) continue;
+      if (rec[q] == 0ull) continue;
       const uint64_t h = ((uint64_t)b << LOW_BITS) | (rec[q] >> 5);
       home[q] = lo + __umul64hi(h << (2 + g.pbits), g.region);
       ld_slot<SU>(table + home[q] * SU, raw[q]);
     }
     #pragma unroll
     for (int q = 0; q < INS_BATCH; ++q) {
-      if (rec[q] == ~0ull) continue;
+      if (rec[q] == 0ull) continue;
       const uint64_t h = ((uint64_t)b << LOW_BITS) | (rec[q] >> 5);
       if (!table_count<KW1>(table, g, max_probe, KW1{h}, (unsigned)(rec[q] & 31), home[q], raw[q], slots, entries,
                             lo))
@@ -1192,6 +1216,7 @@ struct SplitSmem {
   unsigned int start[1 << MAX_SPLIT_BITS];        /* their first position in buf */
   unsigned long long base[1 << MAX_SPLIT_BITS];   /* their first position in the output */
   unsigned int wsum[XTPB / 32];
+  unsigned int wsum_total;
   int overflow;
 };
 
@@ -1227,7 +1252,7 @@ __global__ void __launch_bounds__(XTPB, 2) k_split(const uint64_t *records, cons
     for (int j = 0; j < SPLIT_ROUND; ++j) {
       const uint64_t i = r0 + (uint64_t)j * XTPB + tid;
       pos[j] = ~0u;
-      if (i < hi) {
+      if (i < hi && recs[j] != 0ull) {   /* 0: an unused chunk tail */
         const unsigned sq = (unsigned)(recs[j] >> shift) & (unsigned)(nq - 1);
         pos[j] = (sq << 16) | atomicAdd(&S.cnt[sq], 1u);
       }
@@ -1256,6 +1281,7 @@ __global__ void __launch_bounds__(XTPB, 2) k_split(const uint64_t *records, cons
         if (lane >= o) z += y;
       }
       if (lane < XTPB / 32) S.wsum[lane] = z - w;
+      if (lane == XTPB / 32 - 1) S.wsum_total = z;
     }
     __syncthreads();
     const unsigned ex = S.wsum[wid] + x - v;
@@ -1278,7 +1304,7 @@ __global__ void __launch_bounds__(XTPB, 2) k_split(const uint64_t *records, cons
     for (int j = 0; j < SPLIT_ROUND; ++j)
       if (pos[j] != ~0u) S.buf[S.start[pos[j] >> 16] + (pos[j] & 0xFFFFu)] = recs[j];
     __syncthreads();
-    const unsigned nr = (unsigned)min((uint64_t)SPLIT_REC, hi - r0);
+    const unsigned nr = S.wsum_total;   /* the round's records, holes left out */
     for (unsigned y = tid; y < nr; y += XTPB) {
       const uint64_t rec = S.buf[y];
       const unsigned q = (unsigned)(rec >> shift) & (unsigned)(nq - 1);
@@ -1389,6 +1415,7 @@ __global__ void __launch_bounds__(PTPB) k_count_local(const uint64_t *recs, cons
   for (uint64_t i = tid; i < n; i += PTPB) {
     const uint64_t rec = nxt;
     nxt = i + PTPB < n ? __ldcs(rp + i + PTPB) : 0ull;
+    if (rec == 0ull) continue;   /* an unused chunk tail, when the buckets are the partitions */
     const uint64_t h = bucket_hi | (rec >> 5);
     const uint32_t home = (uint32_t)__umul64hi(h << (2 + g.pbits), g.region);
     if (!sm_count(sm, sm_base, region, h, (unsigned)(rec & 31), home, slots, entries)) full = true;
@@ -1760,15 +1787,18 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
   }();
   (void)attr;
   cudaEventRecord(c->kev[0], c->stream);
+  /* chunk tails waste at most eb * chunk records a bucket: keep that within half the margin */
+  const uint64_t margin = cap - upper / NBUCKET;
+  const uint32_t chunk = (uint32_t)std::max<uint64_t>(XQ, std::min<uint64_t>(512, margin / (2ull * eb)));
   if (c->cfg.edge_filter)
     k_extract<true><<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
         (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k, (uint64_t *)c->records.p, cap,
         (unsigned long long *)c->bucket_cnt.p, (uint8_t *)c->blk_cnt.p, (const uint64_t *)c->k1tab.p, c->k1slots,
-        c->dctr);
+        chunk, c->dctr);
   else
     k_extract<false><<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
         (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k, (uint64_t *)c->records.p, cap,
-        (unsigned long long *)c->bucket_cnt.p, (uint8_t *)c->blk_cnt.p, nullptr, 0, c->dctr);
+        (unsigned long long *)c->bucket_cnt.p, (uint8_t *)c->blk_cnt.p, nullptr, 0, chunk, c->dctr);
   k_hll_merge<<<HLL_M / 256, 256, 0, c->stream>>>((const uint8_t *)c->blk_cnt.p, eb, c->dctr);
   c->launches += 2;
   cudaEventRecord(c->kev[1], c->stream);
