@@ -1789,7 +1789,7 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
   cudaEventRecord(c->kev[0], c->stream);
   /* chunk tails waste at most eb * chunk records a bucket: keep that within half the margin */
   const uint64_t margin = cap - upper / NBUCKET;
-  const uint32_t chunk = (uint32_t)std::max<uint64_t>(XQ, std::min<uint64_t>(512, margin / (2ull * eb)));
+  const uint32_t chunk = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(512, margin / (2ull * eb)));
   if (c->cfg.edge_filter)
     k_extract<true><<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
         (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k, (uint64_t *)c->records.p, cap,
