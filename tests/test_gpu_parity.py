@@ -143,7 +143,10 @@ def test_plain_small_workload_parity():
     fq = synth.make_fastq(w)
     thr = bg.thresholds(w.lower)
     ref = oracle.run(fq, k=31, thresh=thr, min_update=True, threads=16, keep_k2=True, keep_filtered=True)
-    compare(gpu_run(fq, 31, True, thr, True), ref)
+    gpu = gpu_run(fq, 31, True, thr, True)
+    compare(gpu, ref)
+    # the shared-memory partition path ran (no fallback to whole-table or L2 counting)
+    assert gpu["sizes"]["table_partitions"] >= 256
 
 
 def test_repeat_rich_workload_parity():
