@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstddef>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 
@@ -33,7 +34,7 @@ bruno_status ensure(Ctx *c, Buf &b, size_t bytes, bool preserve) {
   if (bytes <= b.bytes && b.p) return BRUNO_OK;
   void *p = nullptr;
   size_t want = std::max(bytes + bytes / 8, (size_t)256);
-  cudaError_t e = cudaMallocAsync(&p, want, c->stream);
+  cudaError_t e = cudaMallocFromPoolAsync(&p, want, c->pool, c->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return set_err(c, BRUNO_ERR_OOM, "device allocation of " + std::to_string(want) + " bytes failed");
@@ -43,6 +44,29 @@ bruno_status ensure(Ctx *c, Buf &b, size_t bytes, bool preserve) {
   b.p = p;
   b.bytes = want;
   return BRUNO_OK;
+}
+
+/* The library's own stream-ordered pool on a device (created once, kept for the process): it
+ * keeps what is freed instead of returning it at every synchronisation, so a context that
+ * rebuilds with the same sizes never waits for memory to be mapped again; the device's default
+ * pool, which other code in the process may use, is left as it is. */
+cudaMemPool_t library_pool(int device) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  if (device < 0 || device >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!pools[device]) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaMemPool_t p = nullptr;
+    if (cudaMemPoolCreate(&p, &props) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[device] = p;
+  }
+  return pools[device];
 }
 
 static void release(Buf &b) {
@@ -87,6 +111,8 @@ bruno_status bruno_ctx_create(const bruno_cfg *cfg, bruno_ctx **out) {
   c->exact_ranking = cfg->exact_ranking != 0;
   c->force_direct_count = cfg->direct_count;
   bruno_status st = cuda_check(c, cudaSetDevice(cfg->device), "cudaSetDevice");
+  if (st == BRUNO_OK && !(c->pool = library_pool(cfg->device)))
+    st = set_err(c, BRUNO_ERR_CUDA, "stream-ordered memory pool");
   if (st == BRUNO_OK) st = cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
   c->own_stream = true;
   /* The k-mer table is read at random, one 32-byte slot per probe: ask L2 to fetch only

@@ -58,6 +58,7 @@ struct Ctx {
   int W = 1;                     /* key words */
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  cudaMemPool_t pool = nullptr;  /* the library's stream-ordered pool on this device */
   std::string err;
   int stage = 0;                 /* 0 empty, 1 loaded, 2 counted, 3 filtered, 4 chains, 5 ranked, 6 compressed */
 
@@ -123,6 +124,7 @@ struct Ctx {
 bruno_status set_err(Ctx *c, bruno_status s, const std::string &msg);
 bruno_status cuda_check(Ctx *c, cudaError_t e, const char *what);
 bruno_status ensure(Ctx *c, Buf &b, size_t bytes, bool preserve = false);
+cudaMemPool_t library_pool(int device);
 bruno_status sync_counters(Ctx *c, bool with_hll = false);
 
 /* exclusive scan of n uint64 values (in may equal out); writes the total to *total_dev */
