@@ -1647,20 +1647,45 @@ void scan_u64(const uint64_t *in, uint64_t *out, uint64_t n, unsigned long long 
 }
 
 /* ------------------------------------------------------------ read index */
+namespace {
+bruno_status extract_begin(Ctx *c, uint64_t upper, int max_blocks);
+void extract_reads(Ctx *c, uint64_t r0, uint64_t r1);
+}  // namespace
+
+/* Indexes every FASTQ segment.  A segment copied from the host in pieces (load_fastq) is
+ * indexed as soon as its piece has landed, and on the partitioned path its reads are extracted
+ * right away, so parsing and extraction run under the remaining copies. */
 bruno_status run_index_reads(Ctx *c) {
   bruno_status st;
   /* first pass: sizes for every segment */
-  uint64_t total_tiles = 0;
-  for (auto &sg : c->segs) total_tiles = std::max<uint64_t>(total_tiles, (sg.n + TILE - 1) / TILE);
+  uint64_t total_tiles = 0, total_bytes = 0;
+  for (auto &sg : c->segs) {
+    total_tiles = std::max<uint64_t>(total_tiles, (sg.n + TILE - 1) / TILE);
+    total_bytes += sg.n;
+  }
   if ((st = ensure(c, c->tile_cnt, std::max<uint64_t>(1, total_tiles) * 8)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->tile_base, std::max<uint64_t>(1, total_tiles) * 8)) != BRUNO_OK) return st;
+  bool piped = false;
+  for (auto &sg : c->segs) piped |= sg.ev >= 0;
+  c->pre_extracted = piped && c->W == 1 && !c->cfg.edge_filter && c->force_direct_count != 1;
+  cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
+  if (c->pre_extracted) {
+    /* every record holds its sequence and an equally long quality line, so the k-mer
+     * positions of all reads are at most half the bytes */
+    int blocks = 0;   /* one launch a segment: at most 2 per SM, at most one per XTPB reads (8 bytes a read at least) */
+    for (auto &sg : c->segs)
+      blocks += (int)std::min<uint64_t>(num_sms() * 2, (sg.n / 8 + XTPB) / XTPB);
+    if ((st = extract_begin(c, total_bytes / 2 + 1, std::max(1, blocks))) != BRUNO_OK) return st;
+    cudaEventRecord(c->kev[0], c->stream);
+  }
   /* the read arrays need the record count first; newline counts give an upper bound */
   uint64_t rcap = 0;
   for (size_t si = 0; si < c->segs.size(); ++si) {
     const Segment &sg = c->segs[si];
     if (sg.n == 0) continue;
+    if (sg.ev >= 0) cudaStreamWaitEvent(c->stream, c->seg_ev[sg.ev], 0);
     const uint64_t tiles = (sg.n + TILE - 1) / TILE;
-    cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
+    cudaMemsetAsync(&c->dctr->n_newlines_eff, 0, 8, c->stream);   /* the extraction's tallies stay */
     long long neg = -1;
     unsigned long long nb = ~0ull;
     cudaMemcpyAsync(&c->dctr->last_nonws, &neg, sizeof(neg), cudaMemcpyHostToDevice, c->stream);
@@ -1672,8 +1697,11 @@ bruno_status run_index_reads(Ctx *c) {
     scan_u64((const uint64_t *)c->tile_cnt.p, (uint64_t *)c->tile_base.p, tiles, &c->dctr->n_records, c->stream);
     if ((st = sync_counters(c)) != BRUNO_OK) return st;
     /* n_records temporarily holds the total newline count: records <= newlines / 4 + 1 */
-    const uint64_t upper = c->hctr->n_records / 4 + 1;
-    /* grow keeping the spans of earlier files */
+    uint64_t upper = c->hctr->n_records / 4 + 1;
+    /* grow keeping the spans of earlier files; pieces of one input grow once, for all pieces
+     * at the first piece's records per byte */
+    if (c->pre_extracted && si == 0 && sg.n > 0)
+      upper = std::max<uint64_t>(upper, (uint64_t)((double)upper * (double)total_bytes / (double)sg.n * 1.05) + 1);
     if ((st = ensure(c, c->rstart, (rcap + upper) * 8, true)) != BRUNO_OK) return st;
     if ((st = ensure(c, c->rend, (rcap + upper) * 8, true)) != BRUNO_OK) return st;
     k_index_lines<<<(unsigned)tiles, TPB, 0, c->stream>>>((const unsigned char *)sg.ptr, sg.n,
@@ -1687,6 +1715,7 @@ bruno_status run_index_reads(Ctx *c) {
     if (h.bad_line != ~0ull || (lines & 3) != 0)
       return set_err(c, BRUNO_ERR_BAD_INPUT, "malformed FASTQ in file " + std::to_string(si) + " near line " +
                                                  std::to_string(h.bad_line != ~0ull ? h.bad_line : lines));
+    if (c->pre_extracted) extract_reads(c, rcap, rcap + lines / 4);
     rcap += lines / 4;
   }
   c->n_reads = rcap;
@@ -1763,44 +1792,68 @@ bruno_status count_direct(Ctx *c) {
 }
 
 /* the partitioned count (k <= 31); returns with used = false if a bucket overflowed */
-bruno_status count_partitioned(Ctx *c, bool &used) {
+/* Extraction into the hash buckets, in one launch over all reads or in one launch per FASTQ
+ * segment as segments arrive: `upper` bounds the k-mer positions of all launches together and
+ * `max_blocks` their blocks together; every block claims bucket chunks of its own, so chunk
+ * tails waste at most max_blocks * chunk records a bucket, kept within half the margin. */
+bruno_status extract_begin(Ctx *c, uint64_t upper, int max_blocks) {
   bruno_status st;
-  used = false;
-  const int sms = num_sms();
-  const uint64_t nreads = c->n_reads;
-  cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
-  k_kmer_upper<<<sms * 4, TPB, 0, c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads,
-                                               c->cfg.k, c->dctr);
-  c->launches += 1;
-  if ((st = sync_counters(c)) != BRUNO_OK) return st;
-  const uint64_t upper = c->hctr->n_upper;
   const uint64_t cap = upper / NBUCKET + upper / (NBUCKET * 12) + 4096;  /* hashing spreads buckets within ~0.1% */
   if ((st = ensure(c, c->records, (size_t)NBUCKET * cap * 8)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->bucket_cnt, NBUCKET * 8)) != BRUNO_OK) return st;
   cudaMemsetAsync(c->bucket_cnt.p, 0, NBUCKET * 8, c->stream);
-  const int eb = std::max(1, std::min<int>(sms * 2, (int)((nreads + XTPB - 1) / XTPB)));
-  if ((st = ensure(c, c->blk_cnt, (size_t)eb * HLL_M)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->blk_cnt, (size_t)max_blocks * HLL_M)) != BRUNO_OK) return st;
   static const bool attr = [] {
     cudaFuncSetAttribute(k_extract<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
     cudaFuncSetAttribute(k_extract<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
     return true;
   }();
   (void)attr;
-  cudaEventRecord(c->kev[0], c->stream);
-  /* chunk tails waste at most eb * chunk records a bucket: keep that within half the margin */
   const uint64_t margin = cap - upper / NBUCKET;
-  const uint32_t chunk = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(512, margin / (2ull * eb)));
+  c->xcap = cap;
+  c->xchunk = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(512, margin / (2ull * max_blocks)));
+  c->xblk = 0;
+  c->xblk_max = max_blocks;
+  return BRUNO_OK;
+}
+
+/* one extraction launch over reads [r0, r1) */
+void extract_reads(Ctx *c, uint64_t r0, uint64_t r1) {
+  const uint64_t nr = r1 - r0;
+  if (nr == 0) return;
+  const int eb = std::max(1, std::min<int>({num_sms() * 2, (int)((nr + XTPB - 1) / XTPB), c->xblk_max - c->xblk}));
+  const uint64_t *rs = (const uint64_t *)c->rstart.p + r0, *re = (const uint64_t *)c->rend.p + r0;
+  uint8_t *part = (uint8_t *)c->blk_cnt.p + (uint64_t)c->xblk * HLL_M;
   if (c->cfg.edge_filter)
     k_extract<true><<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
-        (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k, (uint64_t *)c->records.p, cap,
-        (unsigned long long *)c->bucket_cnt.p, (uint8_t *)c->blk_cnt.p, (const uint64_t *)c->k1tab.p, c->k1slots,
-        chunk, c->dctr);
+        rs, re, nr, c->cfg.k, (uint64_t *)c->records.p, c->xcap, (unsigned long long *)c->bucket_cnt.p, part,
+        (const uint64_t *)c->k1tab.p, c->k1slots, c->xchunk, c->dctr);
   else
     k_extract<false><<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
-        (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k, (uint64_t *)c->records.p, cap,
-        (unsigned long long *)c->bucket_cnt.p, (uint8_t *)c->blk_cnt.p, nullptr, 0, chunk, c->dctr);
-  k_hll_merge<<<HLL_M / 256, 256, 0, c->stream>>>((const uint8_t *)c->blk_cnt.p, eb, c->dctr);
-  c->launches += 2;
+        rs, re, nr, c->cfg.k, (uint64_t *)c->records.p, c->xcap, (unsigned long long *)c->bucket_cnt.p, part, nullptr,
+        0, c->xchunk, c->dctr);
+  c->xblk += eb;
+  c->launches += 1;
+}
+
+bruno_status count_partitioned(Ctx *c, bool &used) {
+  bruno_status st;
+  used = false;
+  const int sms = num_sms();
+  const uint64_t nreads = c->n_reads;
+  if (!c->pre_extracted) {   /* the read index ran alone: one extraction launch over all reads */
+    cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
+    k_kmer_upper<<<sms * 4, TPB, 0, c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads,
+                                                 c->cfg.k, c->dctr);
+    c->launches += 1;
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    if ((st = extract_begin(c, c->hctr->n_upper, sms * 2)) != BRUNO_OK) return st;
+    cudaEventRecord(c->kev[0], c->stream);
+    extract_reads(c, 0, nreads);
+  }
+  const uint64_t cap = c->xcap;
+  k_hll_merge<<<HLL_M / 256, 256, 0, c->stream>>>((const uint8_t *)c->blk_cnt.p, c->xblk, c->dctr);
+  c->launches += 1;
   cudaEventRecord(c->kev[1], c->stream);
   if ((st = sync_counters(c, true)) != BRUNO_OK) return st;
   if (c->hctr->err & DERR_TABLE_FULL) return BRUNO_OK;   /* a bucket overflowed: count directly */

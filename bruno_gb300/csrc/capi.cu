@@ -11,6 +11,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "internal.cuh"
 
@@ -84,6 +85,32 @@ bruno_status sync_counters(Ctx *c, bool with_hll) {
 }
 
 static void record(Ctx *c, int i) { cudaEventRecord(c->ev[i], c->stream); }
+
+/* Record starts that cut a host FASTQ buffer into pieces of about `piece` bytes; {0} alone when
+ * the buffer is under two pieces.  A cut is the start of a line that begins with '@' and whose
+ * second-next line begins with '+': a quality line may begin with '@' as well, but two lines
+ * after a quality line comes a sequence, which holds no '+'.  A target with no such line in the
+ * MiB after it gets no cut. */
+static std::vector<uint64_t> piece_cuts(const char *buf, uint64_t n, uint64_t piece) {
+  std::vector<uint64_t> cuts{0};
+  if (piece == 0 || n < 2 * piece) return cuts;
+  auto line_end = [&](uint64_t from) -> uint64_t {   /* the newline ending the line at `from`, or n */
+    if (from >= n) return n;
+    const void *e = std::memchr(buf + from, '\n', n - from);
+    return e ? (uint64_t)((const char *)e - buf) : n;
+  };
+  for (uint64_t target = piece; target + piece / 2 < n; target += piece) {
+    const uint64_t limit = std::min<uint64_t>(n, target + (1ull << 20));
+    for (uint64_t q = line_end(target) + 1; q < limit; q = line_end(q) + 1) {
+      if (buf[q] != '@' || q <= cuts.back()) continue;
+      const uint64_t e1 = line_end(q);
+      if (e1 >= n) break;
+      const uint64_t e2 = line_end(e1 + 1);
+      if (e2 + 1 < n && buf[e2 + 1] == '+') { cuts.push_back(q); break; }
+    }
+  }
+  return cuts;
+}
 static double elapsed(Ctx *c, int a, int b) {
   float ms = 0;
   if (cudaEventElapsedTime(&ms, c->ev[a], c->ev[b]) != cudaSuccess) { cudaGetLastError(); return 0; }
@@ -122,6 +149,9 @@ bruno_status bruno_ctx_create(const bruno_cfg *cfg, bruno_ctx **out) {
   if (st == BRUNO_OK) st = cuda_check(c, cudaMallocHost(&c->hctr, sizeof(DevCounters)), "pinned counters");
   for (int i = 0; i < 8 && st == BRUNO_OK; ++i) st = cuda_check(c, cudaEventCreate(&c->ev[i]), "event");
   for (int i = 0; i < 5 && st == BRUNO_OK; ++i) st = cuda_check(c, cudaEventCreate(&c->kev[i]), "event");
+  if (st == BRUNO_OK) st = cuda_check(c, cudaEventCreate(&c->h2d_end), "event");
+  if (st == BRUNO_OK) st = cuda_check(c, cudaEventCreateWithFlags(&c->order_ev, cudaEventDisableTiming), "event");
+  if (st == BRUNO_OK) st = cuda_check(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking), "stream");
   if (st != BRUNO_OK) { bruno_ctx_destroy(c); return st; }
   cudaMemsetAsync(c->dctr, 0, sizeof(DevCounters), c->stream);
   *out = c;
@@ -130,6 +160,7 @@ bruno_status bruno_ctx_create(const bruno_cfg *cfg, bruno_ctx **out) {
 
 bruno_status bruno_ctx_destroy(bruno_ctx *c) {
   if (!c) return BRUNO_ERR_ARG;
+  if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
   if (c->stream) cudaStreamSynchronize(c->stream);
   Buf *bufs[] = {&c->rstart, &c->rend, &c->tile_cnt, &c->tile_base, &c->table, &c->k2_keys, &c->k2_edges, &c->k2_counts,
                  &c->f_keys, &c->f_edges, &c->f_counts, &c->blk_cnt, &c->blk_base, &c->ckey, &c->cedge,
@@ -142,6 +173,10 @@ bruno_status bruno_ctx_destroy(bruno_ctx *c) {
   if (c->hctr) cudaFreeHost(c->hctr);
   for (int i = 0; i < 8; ++i) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   for (int i = 0; i < 5; ++i) if (c->kev[i]) cudaEventDestroy(c->kev[i]);
+  for (cudaEvent_t e : c->seg_ev) cudaEventDestroy(e);
+  if (c->h2d_end) cudaEventDestroy(c->h2d_end);
+  if (c->order_ev) cudaEventDestroy(c->order_ev);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return BRUNO_OK;
@@ -172,6 +207,15 @@ bruno_status bruno_reset(bruno_ctx *c) {
   c->n_k2 = c->n_filtered = 0;
   c->k2_dumped = false;
   c->h2d_pending = false;
+  c->h2d_piped = false;
+  c->host_loads = 0;
+  c->seg_ev_used = 0;
+  /* copies still queued on the copy stream finish before the context's stream frees or reuses
+   * their buffers */
+  if (c->copy_stream) {
+    cudaEventRecord(c->order_ev, c->copy_stream);
+    cudaStreamWaitEvent(c->stream, c->order_ev, 0);
+  }
   c->n_nodes = c->n_branch = c->n_chain = 0;
   c->iterations = c->n_cycle = c->n_isolated = c->multi = 0;
   c->n_ranked = c->n_heads = c->n_chain_chars = 0;
@@ -194,14 +238,45 @@ bruno_status bruno_load_fastq(bruno_ctx *c, const char *buf, size_t nbytes, int3
   if (is_device) {
     c->segs.push_back({buf, nbytes});
   } else {
-    const size_t i = c->segs.size();
+    const size_t i = c->host_loads++;
     if (c->seg_bufs.size() <= i) c->seg_bufs.resize(i + 1);
-    bruno_status st = ensure(c, c->seg_bufs[i], nbytes + 1);
+    const std::vector<uint64_t> cuts = piece_cuts(buf, nbytes, c->cfg.h2d_chunk ? c->cfg.h2d_chunk : (256ull << 20));
+    /* each piece starts on a 16-byte boundary of the device copy, for the parser's vector loads */
+    bruno_status st = ensure(c, c->seg_bufs[i], nbytes + 16 * cuts.size() + 1);
     if (st != BRUNO_OK) return st;
-    if (!c->h2d_pending) { record(c, 7); c->h2d_pending = true; }   /* before the first host copy */
-    st = cuda_check(c, cudaMemcpyAsync(c->seg_bufs[i].p, buf, nbytes, cudaMemcpyHostToDevice, c->stream), "H2D FASTQ");
-    if (st != BRUNO_OK) return st;
-    c->segs.push_back({(const char *)c->seg_bufs[i].p, nbytes});
+    char *dst = (char *)c->seg_bufs[i].p;
+    if (cuts.size() < 2 && !c->h2d_piped) {   /* one piece: copied on the context's stream */
+      if (!c->h2d_pending) { record(c, 7); c->h2d_pending = true; }   /* before the first host copy */
+      st = cuda_check(c, cudaMemcpyAsync(dst, buf, nbytes, cudaMemcpyHostToDevice, c->stream), "H2D FASTQ");
+      if (st != BRUNO_OK) return st;
+      c->segs.push_back({dst, nbytes});
+    } else {
+      /* pieces on the copy stream, after whatever the context's stream has queued (the buffer's
+       * allocation, an earlier copy); each piece is a segment with its own event, so that the
+       * read index parses a piece while the next one is still in flight */
+      cudaEventRecord(c->order_ev, c->stream);
+      cudaStreamWaitEvent(c->copy_stream, c->order_ev, 0);
+      if (!c->h2d_pending) { cudaEventRecord(c->ev[7], c->copy_stream); c->h2d_pending = true; }
+      uint64_t at = 0;   /* where the piece goes in the device copy */
+      for (size_t j = 0; j < cuts.size(); ++j) {
+        const uint64_t off = cuts[j], len = (j + 1 < cuts.size() ? cuts[j + 1] : nbytes) - off;
+        st = cuda_check(c, cudaMemcpyAsync(dst + at, buf + off, len, cudaMemcpyHostToDevice, c->copy_stream),
+                        "H2D FASTQ");
+        if (st != BRUNO_OK) return st;
+        if (c->seg_ev_used == c->seg_ev.size()) {
+          cudaEvent_t e;
+          st = cuda_check(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+          if (st != BRUNO_OK) return st;
+          c->seg_ev.push_back(e);
+        }
+        const int ev = (int)c->seg_ev_used++;
+        cudaEventRecord(c->seg_ev[ev], c->copy_stream);
+        c->segs.push_back({dst + at, len, ev});
+        at = (at + len + 15) & ~15ull;
+      }
+      cudaEventRecord(c->h2d_end, c->copy_stream);
+      c->h2d_piped = true;
+    }
   }
   c->stage = 1;
   return BRUNO_OK;
@@ -220,8 +295,15 @@ bruno_status bruno_compute_biedge_freqencies(bruno_ctx *c) {
   if (c->cfg.keep_k2 && (st = run_dump_k2(c)) != BRUNO_OK) return st;
   cudaEventSynchronize(c->ev[2]);
   c->phase_ms[0] = elapsed(c, 0, 1);
-  if (c->h2d_pending) {   /* the copies run back to back, right before this call's start event */
-    c->phase_ms[10] = elapsed(c, 7, 0);
+  if (c->h2d_pending) {   /* the copies: back to back right before this call's start event, or
+                            on the copy stream beneath the read index */
+    if (c->h2d_piped) {
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, c->ev[7], c->h2d_end) != cudaSuccess) { cudaGetLastError(); ms = 0; }
+      c->phase_ms[10] = ms;
+    } else {
+      c->phase_ms[10] = elapsed(c, 7, 0);
+    }
     c->h2d_pending = false;
   }
   c->phase_ms[1] = elapsed(c, 1, 2);

@@ -38,7 +38,7 @@ struct DevCounters {
   unsigned int hll[1 << 12];           /* HyperLogLog registers, p = 12 */
 };
 
-struct Segment { const char *ptr; uint64_t n; };
+struct Segment { const char *ptr; uint64_t n; int ev = -1; };   /* ev: copy-done event, -1 if none */
 
 /* chain state of one chain node, 32 B: pointers encode a chain index (bits 0..31) plus
  * PF_FLIP (the target k-mer, on this node's strand, is the reverse complement of the
@@ -59,6 +59,17 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cudaMemPool_t pool = nullptr;  /* the library's stream-ordered pool on this device */
+  cudaStream_t copy_stream = nullptr;   /* host FASTQ pieces are copied here, one event each */
+  std::vector<cudaEvent_t> seg_ev;
+  cudaEvent_t h2d_end = nullptr;
+  cudaEvent_t order_ev = nullptr; /* orders the copy stream after the context's stream */
+  size_t seg_ev_used = 0;
+  size_t host_loads = 0;         /* host buffers loaded since the reset (one device buffer each) */
+  bool h2d_piped = false;        /* this build's copies ran on the copy stream, ending at h2d_end */
+  bool pre_extracted = false;    /* the read index already extracted every segment's reads */
+  uint64_t xcap = 0;             /* extraction: bucket capacity, chunk, HLL partial blocks */
+  uint32_t xchunk = 1;
+  int xblk = 0, xblk_max = 0;
   std::string err;
   int stage = 0;                 /* 0 empty, 1 loaded, 2 counted, 3 filtered, 4 chains, 5 ranked, 6 compressed */
 

@@ -69,6 +69,11 @@ typedef struct bruno_cfg {
                                cleared, pairs left without edges dropped, the rest inserted
                                unthresholded; k <= 31, not with direct_count = 1.  0 = the
                                (k+2)-mer count filter (local_insert_by_freqencies). */
+  uint64_t h2d_chunk;       /* FASTQ from host memory is copied in pieces of about this many bytes,
+                               cut at record starts, and each piece is parsed (and on the k <= 31
+                               counting path its k-mers extracted) as soon as it lands, while the
+                               rest is still copying; inputs under two pieces are copied whole.
+                               0 = 256 MiB. */
 } bruno_cfg;
 
 typedef struct bruno_sizes {

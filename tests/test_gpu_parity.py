@@ -176,6 +176,41 @@ def test_small_table_regrows():
     compare(out, ref)
 
 
+def at_quality(fq: bytes) -> bytes:
+    """every quality line made to start with '@' (a valid quality character): a piece boundary
+    must still fall on a header, not on a quality line"""
+    lines = bytes(fq).split(b"\n")
+    for i in range(3, len(lines), 4):
+        if lines[i]:
+            lines[i] = b"@" + lines[i][1:]
+    return b"\n".join(lines)
+
+
+@pytest.mark.parametrize("kw", [{}, {"direct_count": 1}, {"direct_count": 2}, {"exact_ranking": True}])
+def test_host_pieces_parity(kw):
+    """host FASTQ copied and indexed in 64 KiB pieces (extraction under the later copies),
+    one and two files, equal to the oracle"""
+    w = synth.WORKLOADS["plain-small"]
+    fq = at_quality(synth.make_fastq(w))
+    thr = bg.thresholds(w.lower)
+    ref = oracle.run(fq, k=31, thresh=thr, min_update=True, threads=16, keep_k2=True, keep_filtered=True)
+    compare(gpu_run(fq, 31, True, thr, True, h2d_chunk=1 << 16, **kw), ref)
+    lines = fq.split(b"\n")
+    cut = sum(len(l) + 1 for l in lines[:len(lines) // 12 * 4])   # a record start, a third of the way in
+    compare(gpu_run(None, 31, True, thr, True, files=[fq[:cut], fq[cut:]], h2d_chunk=1 << 16, **kw), ref)
+
+
+@pytest.mark.parametrize("fname", ["test.unitiqs.fastq", "natural.withN.fastq", "debruijn.palindrome_chr14.fastq"])
+def test_host_pieces_fixture_parity(fname):
+    """pieces of about 1 KiB: dozens of segments, each waited on by the index"""
+    data = at_quality(fixture_bytes(fname))
+    for k, kw in ((31, {}), (45, {}), (31, {"edge_filter": True})):
+        thr = bg.thresholds([2])
+        ref = oracle.run(data, k=k, thresh=thr, min_update=True, keep_k2=True, keep_filtered=True,
+                         edge_filter=kw.get("edge_filter", False))
+        compare(gpu_run(data, k, True, thr, True, h2d_chunk=1024, **kw), ref)
+
+
 def test_malformed_fastq_is_bad_input():
     data = fixture_bytes("test.medium.fastq").replace(b"\n+\n", b"\n-\n", 1)
     with pytest.raises(bg.BrunoError) as e:
