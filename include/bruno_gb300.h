@@ -116,7 +116,9 @@ bruno_status bruno_reset(bruno_ctx *ctx);
 /* Adds one FASTQ file's bytes.  Replaces partitioned_file::read_file + parse_file_data
  * (compact_dbg_io.hpp:165-195, compact_dbg_freq_construct_clean.cpp:321-323).  If
  * is_device != 0, `buf` is a device pointer that must stay valid until
- * bruno_compute_biedge_freqencies returns; otherwise the bytes are copied to the device. */
+ * bruno_compute_biedge_freqencies returns; otherwise the bytes are copied to the device,
+ * asynchronously (in cfg.h2d_chunk pieces on the context's copy stream when the buffer holds
+ * at least two), so the host buffer too must stay valid until that call returns. */
 bruno_status bruno_load_fastq(bruno_ctx *ctx, const char *buf, size_t nbytes, int32_t is_device);
 
 /* Parses every loaded file into canonical (k-mer, biedge) pairs and counts each distinct
