@@ -255,8 +255,11 @@ struct Run {
   std::vector<OAMap<KmerKey<W>, ChainNode<W>>> chain; /* debruijn_chain_graph map per shard */
   std::vector<std::vector<std::pair<K2Key<W>, uint32_t>>> filtered;
 
-  Run(const oracle_cfg &c, oracle_result *r)
-      : cfg(c), T(c.threads > 0 ? c.threads : 1), ko(c.k), res(r) {}
+  const uint64_t clean_k1_lo;   /* threshes[2] as the driver passed it, whatever the filter used */
+  std::vector<W> cycle_kmers;   /* get_cycle_node_kmers after the last list ranking */
+
+  Run(const oracle_cfg &c, oracle_result *r, uint64_t k1_lo)
+      : cfg(c), T(c.threads > 0 ? c.threads : 1), ko(c.k), res(r), clean_k1_lo(k1_lo) {}
 
   /* owning shard: the high hash bits, independent of the low bits that pick map slots */
   int shard(W kmer) const { return (int)((hash_word(kmer) >> 40) % (uint64_t)T); }
@@ -767,11 +770,16 @@ struct Run {
       for (size_t i = 0; i < chain[s].keys.size(); ++i)
         if (chain[s].state[i] == 1 && unfinished(chain[s].vals[i])) any_unfinished = true;
     std::vector<uint64_t> ncy(T, 0), niso(T, 0);
+    std::vector<std::vector<W>> cyk(T);
     const uint32_t maxd = 0x1u << iterations;
     parallel(T, [&](int s) {
       for (size_t i = 0; i < chain[s].keys.size(); ++i) {
         if (chain[s].state[i] != 1) continue;
-        if (any_unfinished && is_cycle(chain[s].vals[i], maxd)) { chain[s].erase_slot(i); ++ncy[s]; }
+        if (any_unfinished && is_cycle(chain[s].vals[i], maxd)) {
+          cyk[s].push_back(chain[s].keys[i].v);
+          chain[s].erase_slot(i);
+          ++ncy[s];
+        }
       }
       for (size_t i = 0; i < chain[s].keys.size(); ++i) {
         if (chain[s].state[i] != 1) continue;
@@ -780,6 +788,8 @@ struct Run {
       }
     });
     for (int s = 0; s < T; ++s) { res->n_cycle_nodes += ncy[s]; res->n_isolated += niso[s]; }
+    cycle_kmers.clear();
+    for (int s = 0; s < T; ++s) cycle_kmers.insert(cycle_kmers.end(), cyk[s].begin(), cyk[s].end());
     res->seconds[ORACLE_T_LIST_RANK] = now() - t0;
   }
 
@@ -861,7 +871,7 @@ struct Run {
   struct FreqSum { uint64_t count = 0, sum = 0; uint16_t mn = 0xFFFF, mx = 0; };
   struct EdgeRec { W L, R; uint16_t f[11]; };
 
-  const Node *node_of(W canon) { return nodes[shard(canon)].find(KmerKey<W>{canon}); }
+  Node *node_of(W canon) { return nodes[shard(canon)].find(KmerKey<W>{canon}); }
   W canon_of(W x) const { W y = ko.rc(x); return x < y ? x : y; }
 
   void chain_edges() {
@@ -1021,17 +1031,303 @@ struct Run {
     }
   }
 
+
+  /* ================================================== graph cleaning
+   * clean_deadend_and_bubbles_naive (compact_dbg_clean.hpp:575-890), the cleaning of the
+   * _freq_clean driver (compact_dbg_freq_construct_clean.cpp:633-700), on one rank. */
+  static bool single16(unsigned n) { return n != 0 && (n & (n - 1)) == 0; }
+  static uint16_t in_total(const Node &n) {   /* get_in_edge_total_frequency (debruijn_graph_node.hpp:307-313) */
+    uint16_t t = 0;
+    for (int c = 4; c < 8; ++c) t = sat_add(t, n.c[c]);
+    return t;
+  }
+  static uint16_t out_total(const Node &n) {  /* get_out_edge_total_frequency (:299-305) */
+    uint16_t t = 0;
+    for (int c = 0; c < 4; ++c) t = sat_add(t, n.c[c]);
+    return t;
+  }
+  static bool no_edges(const Node &n) {     /* graph::IsIsolated (debruijn_graph_filters.hpp:163-172) */
+    for (int c = 0; c < 8; ++c) if (n.c[c]) return false;
+    return true;
+  }
+
+  /* idx.erase_if(IsIsolated): nodes without any edge leave the graph */
+  void erase_isolated() {
+    parallel(T, [&](int s) {
+      for (size_t i = 0; i < nodes[s].keys.size(); ++i)
+        if (nodes[s].state[i] == 1 && no_edges(nodes[s].vals[i])) nodes[s].erase_slot(i);
+    });
+  }
+
+  /* erase_simple_biedges (debruijn_graph_map.hpp:600-608): each (k-mer, DNA16 biedge) put on
+   * the canonical strand (transform_input), then compact_multi_biedge::erase (debruijn_graph_node.hpp
+   * :223-226) zeroes the count of each single-character nibble; the self count stays. */
+  void erase_simple(const std::vector<std::pair<W, uint8_t>> &q) {
+    for (auto e : q) {
+      W x = e.first; uint8_t ed = e.second;
+      canonical(x, ed);
+      Node *n = node_of(x);
+      if (!n) continue;
+      const unsigned out = from_dna16(ed & 0xFu), in = from_dna16(ed >> 4);
+      if (out < 4) n->c[out] = 0;
+      if (in < 4) n->c[4 + in] = 0;
+    }
+  }
+
+  /* get_remote_edges for simple biedges (:475-510): the same edge seen from the other end.
+   * An in-nibble c of x is the edge from c.x[0..k-2] whose out-nibble is x's last character;
+   * an out-nibble c is the edge to x[1..k-1].c whose in-nibble is x's first character. */
+  std::vector<std::pair<W, uint8_t>> remote_simple(const std::vector<std::pair<W, uint8_t>> &q) const {
+    std::vector<std::pair<W, uint8_t>> r;
+    for (auto e : q) {
+      const unsigned in = e.second >> 4, out = e.second & 0xFu;
+      if (single16(in))
+        r.emplace_back(ko.next_reverse_from_char(e.first, from_dna16(in)), (uint8_t)(1u << ko.last(e.first)));
+      if (single16(out))
+        r.emplace_back(ko.next_from_char(e.first, from_dna16(out)), (uint8_t)((1u << ko.first(e.first)) << 4));
+    }
+    return r;
+  }
+
+  /* get_remote_edges for whole nodes (:440-471): every in- and out-neighbour's edge back */
+  void remote_multi(W x, const Node &n, std::vector<std::pair<W, uint8_t>> &r) const {
+    for (unsigned c = 0; c < 4; ++c)
+      if (n.c[4 + c] > 0) r.emplace_back(ko.next_reverse_from_char(x, c), (uint8_t)(1u << ko.last(x)));
+    for (unsigned c = 0; c < 4; ++c)
+      if (n.c[c] > 0) r.emplace_back(ko.next_from_char(x, c), (uint8_t)((1u << ko.first(x)) << 4));
+  }
+
+  /* erase_nodes(kmers) (:833-836 -> erase_nodes_and_edges :811-827): the nodes found leave
+   * the graph, then their neighbours lose the edges back to them */
+  void erase_graph_nodes(const std::vector<W> &kmers) {
+    std::vector<std::pair<W, Node>> found;
+    for (W x : kmers) {
+      W y = ko.rc(x), key = x < y ? x : y;
+      OAMap<KmerKey<W>, Node> &m = nodes[shard(key)];
+      Node *n = m.find(KmerKey<W>{key});
+      if (n) found.emplace_back(key, *n);
+    }
+    for (auto &f : found) {
+      OAMap<KmerKey<W>, Node> &m = nodes[shard(f.first)];
+      Node *n = m.find(KmerKey<W>{f.first});
+      if (n) m.erase_slot((size_t)(n - m.vals.data()));
+    }
+    std::vector<std::pair<W, uint8_t>> rev;
+    for (auto &f : found) remote_multi(f.first, f.second, rev);
+    erase_simple(rev);
+  }
+
+  /* erase_edges(query, edge_freq_filter) (:770-775): find_edges with the predicate (:615-660)
+   * keeps, per query, the single-character nibbles whose edge exists with a count below
+   * min_freq (compact_multi_biedge::select, debruijn_graph_node.hpp:240-247), all looked up
+   * before anything is erased; then the reverse edges and the edges themselves are erased
+   * (erase_edges_internal, :737-747).  Returns the number of query edges kept. */
+  uint64_t erase_low_edges(std::vector<std::pair<W, uint8_t>> q, uint32_t min_freq) {
+    std::vector<std::pair<W, uint8_t>> found;
+    for (auto &e : q) {
+      W x = e.first; uint8_t ed = e.second;
+      canonical(x, ed);
+      const Node *n = node_of(x);
+      if (!n) continue;
+      const unsigned in = ed >> 4, out = ed & 0xFu;
+      auto sel = [&](uint16_t v) { return (uint32_t)v < min_freq ? v : (uint16_t)0; };
+      if (single16(in) && sel(n->c[4 + from_dna16(in)]) == 0) ed &= 0x0Fu;
+      if (single16(out) && sel(n->c[from_dna16(out)]) == 0) ed &= 0xF0u;
+      if (ed > 0) found.emplace_back(x, ed);
+    }
+    erase_simple(remote_simple(found));
+    erase_simple(found);
+    return found.size();
+  }
+
+  /* summarized_chain<K, uint16> (debruijn_chain_node.hpp:174): prev at 5', 5' terminus (the
+   * chain representative), 3' terminus, next at 3', distance between the termini, and the
+   * 5' / 3' end-edge frequencies */
+  struct FSum { W k0, k1, k2, k3; uint32_t len; uint16_t f5, f6; };
+
+  FSum rc_sum(const FSum &x) const {   /* transform::reverse_complement (debruijn_chain_node.hpp:257-268) */
+    return FSum{ko.rc(x.k3), ko.rc(x.k2), ko.rc(x.k1), ko.rc(x.k0), x.len, x.f6, x.f5};
+  }
+
+  /* to_summarized_chains(dbg) (debruijn_chain_graph.hpp:2044-2130) over the chain map's
+   * termini (IsTerminusOrIsolated): one summary per terminus oriented so that the 5' terminus
+   * is the representative, the end edge's frequency the terminus node's total in- or out-edge
+   * frequency; sorted by (5' terminus, next at 3'), a unit chain kept as is and two
+   * consecutive termini of one chain merged (merge_summarized_chains, debruijn_chain_node.hpp
+   * :176-197).  On one rank the left and right shifts deliver value-initialised summaries, so a
+   * last summary whose 5' terminus is the all-A k-mer is dropped and a first one with that
+   * terminus merges with the empty summary.  False where the reference throws. */
+  bool freq_summaries(std::vector<FSum> &out) {
+    std::vector<FSum> r;
+    for (int s = 0; s < T; ++s)
+      for (size_t i = 0; i < chain[s].keys.size(); ++i) {
+        if (chain[s].state[i] != 1) continue;
+        const ChainNode<W> &x = chain[s].vals[i];
+        const W K = chain[s].keys[i].v;
+        const bool t5 = is_chain_terminal(x.inD), t3 = is_chain_terminal(x.outD);
+        if (!t5 && !t3) continue;
+        const Node *n = node_of(K);
+        if (!n) return false;
+        const uint32_t d = get_chain_dist(x.inD) + get_chain_dist(x.outD);
+        if (t5 && t3) {
+          r.push_back(FSum{x.inK, K, K, x.outK, d, in_total(*n), out_total(*n)});
+        } else if (t5) {
+          const W o = ko.rc(x.outK);
+          if (K < o) r.push_back(FSum{x.inK, K, x.outK, W(0), d, in_total(*n), 0});
+          else if (o < K) r.push_back(FSum{W(0), o, ko.rc(K), ko.rc(x.inK), d, 0, in_total(*n)});
+          else return false;
+        } else {
+          const W o = ko.rc(K);
+          if (x.inK < o) r.push_back(FSum{W(0), x.inK, K, x.outK, d, 0, out_total(*n)});
+          else if (o < x.inK) r.push_back(FSum{ko.rc(x.outK), o, ko.rc(x.inK), W(0), d, out_total(*n), 0});
+          else return false;
+        }
+      }
+    /* the reference's sort compares (5' terminus, next at 3') only; the rest of the record
+     * breaks ties here, where merging is order-independent anyway */
+    std::sort(r.begin(), r.end(), [](const FSum &a, const FSum &b) {
+      if (a.k1 != b.k1) return a.k1 < b.k1;
+      if (a.k3 != b.k3) return a.k3 < b.k3;
+      if (a.k0 != b.k0) return a.k0 < b.k0;
+      if (a.k2 != b.k2) return a.k2 < b.k2;
+      if (a.f5 != b.f5) return a.f5 < b.f5;
+      return a.f6 < b.f6;
+    });
+    out.clear();
+    if (r.empty()) return true;
+    size_t max_pos = r.size();
+    if (r.back().k1 == W(0)) --max_pos;
+    FSum last{W(0), W(0), W(0), W(0), 0, 0, 0};
+    for (size_t pos = 0; pos < max_pos; ++pos) {
+      if (r[pos].len == 0) {
+        out.push_back(r[pos]);
+      } else if (r[pos].k1 == last.k1) {
+        FSum m = r[pos];
+        if (m.f5 < last.f5) { m.k0 = last.k0; m.f5 = last.f5; }
+        if (m.f6 < last.f6) { m.k3 = last.k3; m.f6 = last.f6; }
+        out.push_back(m);
+      }
+      last = r[pos];
+    }
+    return true;
+  }
+
+  /* find_deadends (debruijn_topo_operations.hpp:146-175) with deadend_filter
+   * (compact_dbg_clean.hpp:63-80): shorter than max_len, both end-edge frequencies below
+   * min_freq, exactly one end without an edge */
+  std::vector<FSum> find_deadends(const std::vector<FSum> &sums, uint32_t max_len, uint32_t min_freq) const {
+    std::vector<FSum> r;
+    for (const FSum &x : sums)
+      if (x.len < max_len && x.f5 < min_freq && x.f6 < min_freq && ((x.f5 == 0) != (x.f6 == 0))) r.push_back(x);
+    return r;
+  }
+
+  /* find_bubbles (debruijn_topo_operations.hpp:285-395) with bubble_filter
+   * (compact_dbg_clean.hpp:84-112): chains with both ends on branches (find_normal_chains,
+   * :251-272) put on the strand where the 5' branch is not above rc(3' branch), sorted by
+   * (5' branch, 3' branch, length), then every run of two or more consecutive chains between
+   * the same two branches whose neighbours differ in length by at most 1 and have some end
+   * edge below min_freq.  On one rank the redistribution by 5' branch (:320-345) moves nothing
+   * that could join or split a run.  Ties of the reference's sort are broken by the termini. */
+  std::vector<FSum> find_bubbles(const std::vector<FSum> &sums, uint32_t min_freq) const {
+    std::vector<FSum> t;
+    for (const FSum &x : sums)
+      if (x.len > 0 && x.f5 > 0 && x.f6 > 0) t.push_back(x.k0 > ko.rc(x.k3) ? rc_sum(x) : x);
+    std::sort(t.begin(), t.end(), [](const FSum &a, const FSum &b) {
+      if (a.k0 != b.k0) return a.k0 < b.k0;
+      if (a.k3 != b.k3) return a.k3 < b.k3;
+      if (a.len != b.len) return a.len < b.len;
+      if (a.k1 != b.k1) return a.k1 < b.k1;
+      return a.k2 < b.k2;
+    });
+    std::vector<FSum> out;
+    if (t.empty()) return out;
+    auto pred = [&](const FSum &l, const FSum &r) {
+      const uint32_t d = l.len > r.len ? l.len - r.len : r.len - l.len;
+      return d <= 1 && (l.f5 < min_freq || l.f6 < min_freq || r.f5 < min_freq || r.f6 < min_freq);
+    };
+    size_t first_i = 0, i = 1;
+    FSum prev = t[0];
+    for (; i < t.size(); ++i) {
+      if (prev.k0 == t[i].k0 && prev.k3 == t[i].k3 && pred(prev, t[i])) { prev = t[i]; continue; }
+      if (i - first_i > 1) out.insert(out.end(), t.begin() + first_i, t.begin() + i);
+      prev = t[i];
+      first_i = i;
+    }
+    if (i - first_i > 1) out.insert(out.end(), t.begin() + first_i, t.begin() + i);
+    return out;
+  }
+
+  /* the edges to sever (compact_dbg_clean.hpp:619-640, 687-699): the 5' branch's out-edge to the
+   * 5' terminus (its last character) and the 3' branch's in-edge from the 3' terminus (its first
+   * character), as DNA16 biedges; a dead end contributes only the end that has an edge */
+  void end_edges(const FSum &x, bool only_present, std::vector<std::pair<W, uint8_t>> &q) const {
+    if (!only_present || x.f5 > 0) q.emplace_back(x.k0, (uint8_t)(1u << ko.last(x.k1)));
+    if (!only_present || x.f6 > 0) q.emplace_back(x.k3, (uint8_t)((1u << ko.first(x.k2)) << 4));
+  }
+
+  void reset_graph_counters(oracle_result *r) {
+    r->n_branch = r->n_chain_nodes = r->iterations = r->collisions = r->n_cycle_nodes = r->n_isolated = 0;
+  }
+
+  void clean() {
+    oracle_result *top = res;
+    oracle_result *cr = (oracle_result *)calloc(1, sizeof(oracle_result));
+    cr->words = top->words;
+    top->clean = cr;
+    const uint32_t min_freq = (uint32_t)(clean_k1_lo + 1);   /* edge_freq_filter(threshes[2] + 1) */
+    const uint32_t max_len = 2u * (uint32_t)ko.k - 1u;       /* deadend_filter(2 * k - 1, ...) */
+    /* the driver removes cycle nodes and then edge-less nodes from the graph right after the
+     * first list ranking (compact_dbg_freq_construct_clean.cpp:599-604) */
+    erase_graph_nodes(cycle_kmers);
+    erase_isolated();
+    std::vector<FSum> sums;
+    if (!freq_summaries(sums)) { top->clean_status = 2; res = top; return; }
+    std::vector<FSum> dead = find_deadends(sums, max_len, min_freq), bub = find_bubbles(sums, min_freq);
+    res = cr;
+    reset_graph_counters(cr);
+    while (!dead.empty() || !bub.empty()) {
+      top->clean_deadends += dead.size();
+      top->clean_bubbles += bub.size();
+      std::vector<std::pair<W, uint8_t>> q;
+      for (const FSum &x : dead) end_edges(x, true, q);
+      uint64_t erased = erase_low_edges(q, min_freq);
+      erase_isolated();
+      q.clear();
+      for (const FSum &x : bub) end_edges(x, false, q);
+      erased += erase_low_edges(q, min_freq);
+      erase_isolated();
+      top->clean_edges += erased;
+      ++top->clean_rounds;
+      if (erased == 0) { top->clean_status = 1; break; }
+      /* recompact: a new chain map from the graph, ranked, cycles and edge-less nodes out */
+      reset_graph_counters(cr);
+      extract_chains();
+      list_rank();
+      erase_graph_nodes(cycle_kmers);
+      erase_isolated();
+      if (!freq_summaries(sums)) { top->clean_status = 2; break; }
+      dead = find_deadends(sums, max_len, min_freq);
+      bub = find_bubbles(sums, min_freq);
+    }
+    /* the cleaned graph's outputs */
+    emit();
+    chain_edges();
+    export_tables(true);
+    res = top;
+  }
+
   /* ====================================================== table outputs */
-  void export_tables() {
+  void export_tables(bool graph_only = false) {
     const int w = res->words;
-    if (cfg.keep_k2) {
+    if (cfg.keep_k2 && !graph_only) {
       std::vector<std::pair<K2Key<W>, uint32_t>> v;
       for (int s = 0; s < T; ++s)
         for (size_t i = 0; i < k2[s].keys.size(); ++i)
           if (k2[s].state[i] == 1) v.emplace_back(k2[s].keys[i], k2[s].vals[i]);
       export_k2(v, &res->n_k2, &res->k2_keys, &res->k2_edges, &res->k2_counts, w);
     }
-    if (cfg.keep_filtered) {
+    if (cfg.keep_filtered && !graph_only) {
       std::vector<std::pair<K2Key<W>, uint32_t>> v;
       for (int s = 0; s < T; ++s) v.insert(v.end(), filtered[s].begin(), filtered[s].end());
       export_k2(v, &res->n_filtered, &res->filt_keys, &res->filt_edges, &res->filt_counts, w);
@@ -1081,13 +1377,14 @@ struct Run {
     chain_edges();
     chain_summaries();
     export_tables();
+    if (cfg.clean) clean();
     return 0;
   }
 };
 
 template <typename W>
-int run_typed(const char *buf, size_t n, const oracle_cfg &cfg, oracle_result *r) {
-  Run<W> run(cfg, r);
+int run_typed(const char *buf, size_t n, const oracle_cfg &cfg, oracle_result *r, uint64_t k1_lo) {
+  Run<W> run(cfg, r, k1_lo);
   return run.run(buf, n);
 }
 
@@ -1112,6 +1409,7 @@ extern "C" int oracle_run(const char *fastq, size_t nbytes, const oracle_cfg *cf
    * compare directly; k = 32 still computes in one 64-bit word, as Kmer<32> does */
   r->words = cfg->k <= 31 ? 1 : 2;
   oracle_cfg c = *cfg;
+  const uint64_t k1_lo = cfg->thresh[2];   /* cleaning reads threshes[2] whatever the build */
   if (c.edge_filter && !c.thresholding) c.edge_filter = 0;   /* build_index: no filter at all */
   if (c.edge_filter) {
     /* the (k+1)-mer bounds stay in thresh[2..3]; the node insert is build_index's */
@@ -1123,7 +1421,8 @@ extern "C" int oracle_run(const char *fastq, size_t nbytes, const oracle_cfg *cf
     c.thresh[0] = c.thresh[2] = c.thresh[4] = 0;
     c.thresh[1] = c.thresh[3] = c.thresh[5] = ~0ULL;
   }
-  int rc = (cfg->k <= 32) ? run_typed<uint64_t>(fastq, nbytes, c, r) : run_typed<u128>(fastq, nbytes, c, r);
+  int rc = (cfg->k <= 32) ? run_typed<uint64_t>(fastq, nbytes, c, r, k1_lo)
+                               : run_typed<u128>(fastq, nbytes, c, r, k1_lo);
   r->status = rc;
   *out = r;
   return rc;
@@ -1138,13 +1437,15 @@ extern "C" void oracle_free(oracle_result *r) {
   free(r->chain_rep); free(r->chain_offsets); free(r->chain_chars);
   free(r->edge_L); free(r->edge_R); free(r->edge_freqs);
   free(r->sum_kmers); free(r->sum_dist); free(r->sum_flags);
+  oracle_free(r->clean);
   free(r);
 }
 
-extern "C" int oracle_write_outputs(const oracle_result *r, int32_t k, const char *prefix, int32_t benchmark) {
-  if (!r || r->status != 0) return 1;
+namespace {
+enum { W_CHAINS = 1, W_EDGES = 2, W_SUMMARY = 4, W_NODES = 8, W_GRAPH_ALL = 16 };
+
+int write_parts(const oracle_result *r, int32_t k, const std::string &p, int32_t benchmark, int parts) {
   const int w = r->words;
-  std::string p(prefix);
   auto canon = [&](const uint64_t *x) {
     /* lex_less on a k-mer word: min(x, rc(x)) */
     if (w == 1) { KOps<uint64_t> ko(k); uint64_t v = x[0], y = ko.rc(v); return v < y ? v : y; }
@@ -1167,7 +1468,7 @@ extern "C" int oracle_write_outputs(const oracle_result *r, int32_t k, const cha
   };
   /* .chain.fasta: print_chain_string (compact_dbg_io.hpp:323-363), sorted by chain_rep_less;
    * the leading newline of the first record is dropped. */
-  {
+  if (parts & W_CHAINS) {
     std::vector<size_t> idx(r->n_ranked);
     for (size_t i = 0; i < idx.size(); ++i) idx[i] = i;
     std::sort(idx.begin(), idx.end(), [&](size_t a, size_t b) {
@@ -1194,7 +1495,7 @@ extern "C" int oracle_write_outputs(const oracle_result *r, int32_t k, const cha
   }
   /* .chain.components: print_chain_nodes (compact_dbg_io.hpp:463-498) sorted by K,
    * print_chain_node (debruijn_chain_operations.hpp:434-441). */
-  if (!benchmark) {
+  if ((parts & W_CHAINS) && !benchmark) {
     std::string s;
     for (size_t i = 0; i < r->n_ranked; ++i) {
       const uint64_t *K = r->ranked_K + i * w;
@@ -1208,7 +1509,7 @@ extern "C" int oracle_write_outputs(const oracle_result *r, int32_t k, const cha
   }
   /* .chain.edges: print_chain_frequencies (compact_dbg_stats.hpp:1034-1057), each value
    * followed by a tab, records already sorted by L. */
-  if (!benchmark) {
+  if ((parts & W_EDGES) && !benchmark) {
     std::string s;
     for (size_t i = 0; i < r->n_chain_edges; ++i) {
       s += ascii_words(r->edge_L + i * w, k, w); s += "\t";
@@ -1224,7 +1525,7 @@ extern "C" int oracle_write_outputs(const oracle_result *r, int32_t k, const cha
   /* .chain.summary: print_chain_summaries (compact_dbg_io.hpp:528-556), space separated.
    * The reference prints the four k-mers with kmerind's Kmer stream operator, which is not part
    * of the reference sources; they are printed here as their bases. */
-  if (!benchmark && r->summaries_ok) {
+  if ((parts & W_SUMMARY) && !benchmark && r->summaries_ok) {
     std::string s;
     for (size_t i = 0; i < r->n_summaries; ++i) {
       for (int j = 0; j < 4; ++j) { s += ascii_words(r->sum_kmers + (i * 4 + j) * w, k, w); s += " "; }
@@ -1239,7 +1540,7 @@ extern "C" int oracle_write_outputs(const oracle_result *r, int32_t k, const cha
   /* .branch.fasta (compact_dbg_io.hpp:254-299), .branch.edges (compact_dbg_stats.hpp:219-262)
    * and .graph.all, all sorted by k-mer; node lines follow print_graph_node
    * (debruijn_graph_operations.hpp:57-78): k-mer, in A C G T, out A C G T, self. */
-  {
+  if (parts & W_NODES) {
     std::string fa, be, ga;
     for (size_t i = 0; i < r->n_nodes; ++i) {
       const uint64_t *x = r->node_keys + i * w;
@@ -1260,10 +1561,26 @@ extern "C" int oracle_write_outputs(const oracle_result *r, int32_t k, const cha
       f = fopen((p + ".branch.edges").c_str(), "wb");
       if (!f) return 1;
       fwrite(be.data(), 1, be.size(), f); fclose(f);
-      f = fopen((p + ".graph.all").c_str(), "wb");
-      if (!f) return 1;
-      fwrite(ga.data(), 1, ga.size(), f); fclose(f);
+      if (parts & W_GRAPH_ALL) {
+        f = fopen((p + ".graph.all").c_str(), "wb");
+        if (!f) return 1;
+        fwrite(ga.data(), 1, ga.size(), f); fclose(f);
+      }
     }
   }
   return 0;
+}
+}  // namespace
+
+/* Without cleaning, the _freq driver's files.  With cleaning, the _freq_clean driver's: the
+ * first compaction's .graph.all, .branch.*, .chain.summary, .chain.fasta and .chain.components
+ * (printed inside the clean block, compact_dbg_freq_construct_clean.cpp:636-660), then, under
+ * the prefix with ".clean" appended (:677), the cleaned graph's .branch.* (:680-697) and its
+ * .chain.fasta, .chain.components and .chain.edges (:733-790). */
+extern "C" int oracle_write_outputs(const oracle_result *r, int32_t k, const char *prefix, int32_t benchmark) {
+  if (!r || r->status != 0) return 1;
+  const std::string p(prefix);
+  if (!r->clean) return write_parts(r, k, p, benchmark, W_CHAINS | W_EDGES | W_SUMMARY | W_NODES | W_GRAPH_ALL);
+  if (write_parts(r, k, p, benchmark, W_CHAINS | W_SUMMARY | W_NODES | W_GRAPH_ALL)) return 1;
+  return write_parts(r->clean, k, p + ".clean", benchmark, W_CHAINS | W_EDGES | W_NODES);
 }

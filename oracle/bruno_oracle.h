@@ -38,6 +38,11 @@ typedef struct oracle_cfg {
                                (compact_debruijn_graph_block_construct.cpp:417-470): (k+1)-mers
                                counted and kept in [thresh[2], thresh[3]), biedges losing the
                                edges whose (k+1)-mer is gone, then the unthresholded insert */
+  int32_t clean;            /* 1: the _freq_clean driver's graph cleaning after the first
+                               compaction (clean_deadend_and_bubbles_naive,
+                               compact_dbg_clean.hpp:575-890): dead ends shorter than 2k-1 and
+                               bubbles lose their end edges of frequency <= thresh[2], the graph
+                               is recompacted, until no dead end or bubble is left */
 } oracle_cfg;
 
 /* Phase timers, seconds, named after the reference's BL_BENCH phases. */
@@ -94,6 +99,17 @@ typedef struct oracle_result {
   int32_t summaries_ok;     /* 0 when the pairing met a case the reference throws on */
 
   double seconds[ORACLE_T_NUM];
+
+  /* graph cleaning (cfg.clean) */
+  uint64_t clean_rounds;    /* iterations of the cleaning loop */
+  uint64_t clean_deadends;  /* dead-end summaries found, over all iterations */
+  uint64_t clean_bubbles;   /* bubble summaries found, over all iterations */
+  uint64_t clean_edges;     /* low-frequency end edges found and erased (with their reverse edges) */
+  int32_t clean_status;     /* 0 done; 1 stopped after an iteration that erased nothing (the
+                               reference repeats such an iteration forever); 2 a terminus case the
+                               reference throws on */
+  struct oracle_result *clean;  /* the cleaned graph: node table (cycles and isolated nodes
+                                   removed), ranked chain nodes, chains and chain edges */
 } oracle_result;
 
 /* Runs the whole path on an in-memory FASTQ buffer.  Returns 0 on success. */
@@ -103,7 +119,10 @@ void oracle_free(oracle_result *r);
 /* Writes the reference driver's text outputs for a finished run:
  * <prefix>.chain.fasta, <prefix>.chain.components, <prefix>.branch.fasta and, unless
  * benchmark != 0, <prefix>.chain.edges, <prefix>.chain.summary (when summaries_ok),
- * <prefix>.branch.edges and <prefix>.graph.all. */
+ * <prefix>.branch.edges and <prefix>.graph.all.  After cleaning, as the _freq_clean driver:
+ * the same first-compaction files except .chain.edges, then <prefix>.clean.branch.edges,
+ * .clean.branch.fasta, .clean.chain.fasta, .clean.chain.components and .clean.chain.edges of
+ * the cleaned graph. */
 int oracle_write_outputs(const oracle_result *r, int32_t k, const char *prefix, int32_t benchmark);
 
 #ifdef __cplusplus

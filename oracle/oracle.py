@@ -20,14 +20,17 @@ PHASES = ("parse", "count_k2mers", "filter_insert", "chainmap", "list_rank", "co
 class _Cfg(ctypes.Structure):
     _fields_ = [("k", ctypes.c_int32), ("thresholding", ctypes.c_int32), ("thresh", ctypes.c_uint64 * 6),
                 ("min_update", ctypes.c_int32), ("threads", ctypes.c_int32), ("keep_k2", ctypes.c_int32),
-                ("keep_filtered", ctypes.c_int32), ("edge_filter", ctypes.c_int32)]
+                ("keep_filtered", ctypes.c_int32), ("edge_filter", ctypes.c_int32), ("clean", ctypes.c_int32)]
 
 
 _U64P = ctypes.POINTER(ctypes.c_uint64)
 
 
 class _Res(ctypes.Structure):
-    _fields_ = [
+    pass
+
+
+_Res._fields_ = [
         ("status", ctypes.c_int32), ("words", ctypes.c_int32), ("n_reads", ctypes.c_uint64),
         ("n_reads_used", ctypes.c_uint64), ("n_instances", ctypes.c_uint64),
         ("n_k2", ctypes.c_uint64), ("k2_keys", _U64P), ("k2_edges", ctypes.POINTER(ctypes.c_uint8)),
@@ -47,6 +50,8 @@ class _Res(ctypes.Structure):
         ("n_summaries", ctypes.c_uint64), ("sum_kmers", _U64P), ("sum_dist", ctypes.POINTER(ctypes.c_uint32)),
         ("sum_flags", ctypes.POINTER(ctypes.c_uint8)), ("summaries_ok", ctypes.c_int32),
         ("seconds", ctypes.c_double * 6),
+        ("clean_rounds", ctypes.c_uint64), ("clean_deadends", ctypes.c_uint64), ("clean_bubbles", ctypes.c_uint64),
+        ("clean_edges", ctypes.c_uint64), ("clean_status", ctypes.c_int32), ("clean", ctypes.POINTER(_Res)),
     ]
 
 
@@ -97,10 +102,45 @@ def _arr(ptr, n, dtype, shape=None):
     return a.reshape(shape) if shape else a
 
 
+def _graph(r, keep_k2: bool = False, keep_filtered: bool = False) -> dict:
+    """the arrays and counters of one result (the first compaction, or the cleaned graph)"""
+    out = {}
+    w = r.words
+    for n in ("n_reads", "n_reads_used", "n_instances", "n_k2", "n_filtered", "n_nodes", "n_branch",
+              "n_chain_nodes", "iterations", "collisions", "n_cycle_nodes", "n_isolated", "n_ranked", "n_chains"):
+        out[n] = int(getattr(r, n))
+    out["filter_flag_hist"] = list(r.filter_flag_hist)
+    out["seconds"] = dict(zip(PHASES, list(r.seconds)))
+    out["k2"] = (_arr(r.k2_keys, r.n_k2 * w, np.uint64, (r.n_k2, w)), _arr(r.k2_edges, r.n_k2, np.uint8),
+                 _arr(r.k2_counts, r.n_k2, np.uint32)) if keep_k2 else None
+    out["filtered"] = (_arr(r.filt_keys, r.n_filtered * w, np.uint64, (r.n_filtered, w)),
+                       _arr(r.filt_edges, r.n_filtered, np.uint8),
+                       _arr(r.filt_counts, r.n_filtered, np.uint32)) if keep_filtered else None
+    out["nodes"] = (_arr(r.node_keys, r.n_nodes * w, np.uint64, (r.n_nodes, w)),
+                    _arr(r.node_counts, r.n_nodes * 9, np.uint16, (r.n_nodes, 9)),
+                    _arr(r.node_flags, r.n_nodes, np.uint8))
+    out["ranked"] = (_arr(r.ranked_K, r.n_ranked * w, np.uint64, (r.n_ranked, w)),
+                     _arr(r.ranked_rep, r.n_ranked * w, np.uint64, (r.n_ranked, w)),
+                     _arr(r.ranked_dist, r.n_ranked, np.int32))
+    offs = _arr(r.chain_offsets, r.n_chains + 1, np.uint64) if r.n_chains else np.zeros(1, np.uint64)
+    nchars = int(offs[-1])
+    chars = ctypes.string_at(r.chain_chars, nchars) if nchars else b""
+    out["chains"] = (_arr(r.chain_rep, r.n_chains * w, np.uint64, (r.n_chains, w)), offs, chars)
+    ns = r.n_summaries
+    out["summaries"] = (_arr(r.sum_kmers, ns * 4 * w, np.uint64, (ns, 4, w)), _arr(r.sum_dist, ns, np.uint32),
+                        _arr(r.sum_flags, ns * 2, np.uint8, (ns, 2))) if r.summaries_ok else None
+    ne = r.n_chain_edges
+    out["chain_edges"] = (_arr(r.edge_L, ne * w, np.uint64, (ne, w)), _arr(r.edge_R, ne * w, np.uint64, (ne, w)),
+                          _arr(r.edge_freqs, ne * 11, np.uint16, (ne, 11)))
+    return out
+
+
 def run(fastq, k: int = 31, thresholding: bool = True, thresh=None, min_update: bool = True, threads: int = 1,
         keep_k2: bool = False, keep_filtered: bool = False, write_prefix: str | None = None,
-        benchmark: bool = False, edge_filter: bool = False) -> dict:
-    """Runs the oracle on FASTQ bytes (or a uint8 array); returns numpy results."""
+        benchmark: bool = False, edge_filter: bool = False, clean: bool = False) -> dict:
+    """Runs the oracle on FASTQ bytes (or a uint8 array); returns numpy results.  With clean,
+    out["clean"] holds the cleaned graph (nodes, ranked, chains, chain_edges and the ranking
+    counters of the last recompaction) and out["clean_stats"] the loop's tallies."""
     lib = _load()
     buf = np.ascontiguousarray(np.frombuffer(fastq, np.uint8) if isinstance(fastq, (bytes, bytearray)) else fastq,
                                dtype=np.uint8)
@@ -110,40 +150,18 @@ def run(fastq, k: int = 31, thresholding: bool = True, thresh=None, min_update: 
     for i in range(6):
         c.thresh[i] = int(min(t[i], 2**64 - 1))
     c.keep_k2, c.keep_filtered, c.edge_filter = int(keep_k2), int(keep_filtered), int(edge_filter)
+    c.clean = int(clean)
     rp = ctypes.POINTER(_Res)()
     rc = lib.oracle_run(buf.ctypes.data_as(ctypes.c_void_p), buf.nbytes, ctypes.byref(c), ctypes.byref(rp))
     try:
         r = rp.contents
-        out = {"status": rc}
         if rc != 0:
-            return out
-        w = r.words
-        for n in ("n_reads", "n_reads_used", "n_instances", "n_k2", "n_filtered", "n_nodes", "n_branch",
-                  "n_chain_nodes", "iterations", "collisions", "n_cycle_nodes", "n_isolated", "n_ranked", "n_chains"):
-            out[n] = int(getattr(r, n))
-        out["filter_flag_hist"] = list(r.filter_flag_hist)
-        out["seconds"] = dict(zip(PHASES, list(r.seconds)))
-        out["k2"] = (_arr(r.k2_keys, r.n_k2 * w, np.uint64, (r.n_k2, w)), _arr(r.k2_edges, r.n_k2, np.uint8),
-                     _arr(r.k2_counts, r.n_k2, np.uint32)) if keep_k2 else None
-        out["filtered"] = (_arr(r.filt_keys, r.n_filtered * w, np.uint64, (r.n_filtered, w)),
-                           _arr(r.filt_edges, r.n_filtered, np.uint8),
-                           _arr(r.filt_counts, r.n_filtered, np.uint32)) if keep_filtered else None
-        out["nodes"] = (_arr(r.node_keys, r.n_nodes * w, np.uint64, (r.n_nodes, w)),
-                        _arr(r.node_counts, r.n_nodes * 9, np.uint16, (r.n_nodes, 9)),
-                        _arr(r.node_flags, r.n_nodes, np.uint8))
-        out["ranked"] = (_arr(r.ranked_K, r.n_ranked * w, np.uint64, (r.n_ranked, w)),
-                         _arr(r.ranked_rep, r.n_ranked * w, np.uint64, (r.n_ranked, w)),
-                         _arr(r.ranked_dist, r.n_ranked, np.int32))
-        offs = _arr(r.chain_offsets, r.n_chains + 1, np.uint64) if r.n_chains else np.zeros(1, np.uint64)
-        nchars = int(offs[-1])
-        chars = ctypes.string_at(r.chain_chars, nchars) if nchars else b""
-        out["chains"] = (_arr(r.chain_rep, r.n_chains * w, np.uint64, (r.n_chains, w)), offs, chars)
-        ns = r.n_summaries
-        out["summaries"] = (_arr(r.sum_kmers, ns * 4 * w, np.uint64, (ns, 4, w)), _arr(r.sum_dist, ns, np.uint32),
-                            _arr(r.sum_flags, ns * 2, np.uint8, (ns, 2))) if r.summaries_ok else None
-        ne = r.n_chain_edges
-        out["chain_edges"] = (_arr(r.edge_L, ne * w, np.uint64, (ne, w)), _arr(r.edge_R, ne * w, np.uint64, (ne, w)),
-                              _arr(r.edge_freqs, ne * 11, np.uint16, (ne, 11)))
+            return {"status": rc}
+        out = {"status": rc, **_graph(r, keep_k2, keep_filtered)}
+        if clean:
+            out["clean_stats"] = {n: int(getattr(r, "clean_" + n))
+                                  for n in ("rounds", "deadends", "bubbles", "edges", "status")}
+            out["clean"] = _graph(r.clean.contents) if r.clean else None
         if write_prefix:
             lib.oracle_write_outputs(rp, k, write_prefix.encode(), int(benchmark))
         return out

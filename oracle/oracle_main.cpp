@@ -5,8 +5,9 @@
  * (main :848-1030): -T thresholding, -L/-U lower/upper thresholds (one value = (k+1)-mer,
  * three values = k, k+1, k+2; :937-961), -E the (k+1)-mer edge filter of the blocked driver
  * compact_debruijn_graph_block_construct.cpp, -R list_rank_min_update, -B benchmark, -O output
- * prefix; plus -k (k-mer length, a compile-time constant in the reference) and -t (host
- * threads = hash shards).  FASTQ files are concatenated into one k2 counter, as the
+ * prefix; plus -k (k-mer length, a compile-time constant in the reference), -t (host
+ * threads = hash shards) and --clean (the _freq_clean build of the same driver, which cleans
+ * dead ends and bubbles after the first compaction; the _freq build defines NCLEAN).  FASTQ files are concatenated into one k2 counter, as the
  * reference counts all files before filtering (build_index_thresholded :295-348).
  */
 #include "bruno_oracle.h"
@@ -43,6 +44,7 @@ int main(int argc, char **argv) {
     else if (a == "-R") cfg.min_update = 1;
     else if (a == "-B") benchmark = 1;
     else if (a == "-E") cfg.edge_filter = 1;   /* the blocked driver's (k+1)-mer filter build */
+    else if (a == "--clean") cfg.clean = 1;
     else if (a == "-L" && i + 1 < argc) lo.push_back(strtoull(argv[++i], 0, 10));
     else if (a == "-U" && i + 1 < argc) hi.push_back(strtoull(argv[++i], 0, 10));
     else if (a == "-O" && i + 1 < argc) prefix = argv[++i];
@@ -63,7 +65,7 @@ int main(int argc, char **argv) {
     cfg.thresh[3] = std::min<uint64_t>(hi[1], cfg.thresh[3]);
     cfg.thresh[5] = std::min<uint64_t>(hi[2], cfg.thresh[5]);
   }
-  if (files.empty()) { fprintf(stderr, "usage: %s [-T] [-E] [-L n].. [-U n].. [-R] [-B] [-O prefix] [-k K] [-t T] reads.fastq..\n", argv[0]); return 1; }
+  if (files.empty()) { fprintf(stderr, "usage: %s [-T] [-E] [--clean] [-L n].. [-U n].. [-R] [-B] [-O prefix] [-k K] [-t T] reads.fastq..\n", argv[0]); return 1; }
   std::string data;
   for (const char *f : files) {
     if (!read_file(f, data)) { fprintf(stderr, "cannot read %s\n", f); return 1; }

@@ -4,7 +4,8 @@
    into tests/golden/data, so tests never read the reference tree at run time.
 2. Runs the CPU oracle on every fixture with every option set of the reference's
    integration scripts (unthresholded, -T -L 1/2/3, -R on/off, the 3-value form) and
-   records a digest of each output in expected.json.
+   records a digest of each output in expected.json; with ":clean", the same for the graph
+   after the _freq_clean driver's dead-end and bubble cleaning.
 
 Usage: python tests/golden/make_golden.py [path/to/reference]
 """
@@ -25,7 +26,8 @@ FIXTURES = [
     "test.star2.unitiqs.fastq", "test.star2.unitiqs.fasta", "test.short.unitiqs.fastq", "test.short.unitiqs.fasta",
     "test.debruijn.small.fastq", "test.medium.fastq", "debruijn.palindrome.fastq", "debruijn.palindrome2.fastq",
     "debruijn.palindrome_chr14.fastq", "debruijn.shifted_cycle_chr14.fastq", "debruijn.bubble.fastq",
-    "debruijn.bubble2.fastq", "natural.fastq", "natural.withN.fastq",
+    "debruijn.bubble2.fastq", "natural.fastq", "natural.withN.fastq", "debruijn.clean1.fastq",
+    "debruijn.clean2.fastq",
 ]
 FASTQ = [f for f in FIXTURES if f.endswith(".fastq")]
 # (name, thresholding, lower thresholds, upper thresholds, min_update)
@@ -66,8 +68,10 @@ def main() -> None:
     for f in FASTQ:
         fq = open(os.path.join(data, f), "rb").read()
         for name, thr_on, lo, hi, mu in OPTIONS:
-            r = oracle.run(fq, k=31, thresholding=thr_on, thresh=bg.thresholds(lo, hi), min_update=mu)
+            r = oracle.run(fq, k=31, thresholding=thr_on, thresh=bg.thresholds(lo, hi), min_update=mu, clean=True)
             expected[f"{f}:{name}"] = digest(r) if r["status"] == 0 else {"status": r["status"]}
+            if r["status"] == 0:
+                expected[f"{f}:{name}:clean"] = dict(digest(r["clean"]), **r["clean_stats"])
     with open(os.path.join(HERE, "expected.json"), "w") as fh:
         json.dump(expected, fh, indent=1, sort_keys=True)
     print(f"{len(expected)} golden entries")

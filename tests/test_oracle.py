@@ -60,14 +60,15 @@ def _digest(result):
 
 @pytest.mark.parametrize("key", sorted(EXPECTED))
 def test_oracle_matches_golden(key):
-    fname, opt = key.split(":")
+    fname, opt, *clean = key.split(":")
     name, thr_on, lo, hi, mu = OPTIONS[opt]
-    r = oracle.run(fixture_bytes(fname), k=31, thresholding=thr_on, thresh=bg.thresholds(lo, hi), min_update=mu)
+    r = oracle.run(fixture_bytes(fname), k=31, thresholding=thr_on, thresh=bg.thresholds(lo, hi), min_update=mu,
+                   clean=bool(clean))
     exp = EXPECTED[key]
     if "status" in exp and len(exp) == 1:
         assert r["status"] == exp["status"]
         return
-    assert _digest(r) == exp
+    assert (dict(_digest(r["clean"]), **r["clean_stats"]) if clean else _digest(r)) == exp
 
 
 @pytest.mark.parametrize("fname", ["test.star.unitiqs.fastq", "debruijn.palindrome_chr14.fastq",
@@ -286,3 +287,111 @@ def test_malformed_fastq_rejected():
 def test_reads_with_n_are_dropped():
     a = oracle.run(fixture_bytes("natural.withN.fastq"), k=31, thresholding=False)
     assert a["n_reads_used"] < a["n_reads"]
+
+
+# ---------------------------------------------------------------- graph cleaning
+# clean_deadend_and_bubbles_naive (compact_dbg_clean.hpp:575-890).  The reference ships no
+# cleaned outputs, so these cases pin the restatement by construction: reads tiling a random
+# genome at 20x, plus reads that add a low-coverage tip or bubble whose fate is known.
+
+def _fastq(reads) -> bytes:
+    return b"".join(b"@r%d\n%s\n+\n%s\n" % (i, r.encode(), b"I" * len(r)) for i, r in enumerate(reads))
+
+
+def _genome(n, seed):
+    rng = np.random.default_rng(seed)
+    return "".join("ACGT"[x] for x in rng.integers(0, 4, n))
+
+
+def _tiling(g, L=100, step=5):
+    return [g[i:i + L] for i in range(0, len(g) - L + 1, step)]
+
+
+def _canon_strings(strings):
+    return sorted(min(x, _rc(x)) for x in strings)
+
+
+def _subst(c):
+    return "ACGT"[("ACGT".index(c) + 1) % 4]
+
+
+def test_clean_severs_short_low_coverage_tip():
+    """one read with an error 10 bases before its end: a 10-node tip (shorter than 2k-1) off a
+    20x genome.  Cleaning severs the tip's edge of frequency 1 (below -L 1's 2): the genome
+    becomes one chain again and the tip stays as a chain of its own."""
+    k, g = 31, _genome(400, 11)
+    bad = list(g[150:250]); bad[90] = _subst(bad[90]); bad = "".join(bad)
+    r = oracle.run(_fastq(_tiling(g) + [bad]), k=k, thresh=bg.thresholds([1]), clean=True)
+    assert r["clean_stats"] == {"rounds": 1, "deadends": 1, "bubbles": 0, "edges": 1, "status": 0}
+    # before: the genome's chains on either side of the branch k-mer g[209:240], and the tip
+    assert _canon_strings(chain_strings(r)) == _canon_strings([g[:239], g[210:], bad[60:]])
+    assert _canon_strings(chain_strings(r["clean"])) == _canon_strings([g, bad[60:]])
+
+
+def test_clean_keeps_long_tip():
+    """a tip of 2k-1 nodes or more is not a dead end to clean: nothing changes.  Four errors in
+    one 150-base read make every k-mer from the first error's on new: a 110-node tip."""
+    k, g = 31, _genome(400, 12)
+    bad = list(g[100:250])
+    for p in (40, 70, 100, 130):
+        bad[p] = _subst(bad[p])
+    bad = "".join(bad)
+    r = oracle.run(_fastq(_tiling(g) + [bad]), k=k, thresh=bg.thresholds([1]), clean=True)
+    assert r["clean_stats"]["rounds"] == 0
+    assert _canon_strings(chain_strings(r["clean"])) == _canon_strings(chain_strings(r))
+    assert len(chain_strings(r)) == 3
+
+
+def test_clean_severs_low_coverage_bubble_path():
+    """one read with a substitution mid-read: a k-node bubble path beside the 20x genome's.  The
+    two paths between the same branches have equal lengths and a low-frequency end, so both
+    lose their end edges below frequency 2: only the error path's go, the genome re-joins."""
+    k, g = 31, _genome(400, 13)
+    bad = list(g[150:250]); bad[50] = _subst(bad[50]); bad = "".join(bad)
+    r = oracle.run(_fastq(_tiling(g) + [bad]), k=k, thresh=bg.thresholds([1]), clean=True)
+    assert r["clean_stats"] == {"rounds": 1, "deadends": 0, "bubbles": 2, "edges": 2, "status": 0}
+    assert _canon_strings(chain_strings(r["clean"])) == _canon_strings([g, bad[50 - k + 1:50 + k]])
+
+
+def _node_map(nodes, k):
+    keys, counts, _ = nodes
+    return {_ascii(keys[i], k): counts[i].astype(int) for i in range(len(keys))}
+
+
+def _edge_neighbour(x, i):
+    """the node at the other end of count index i (out A C G T, in A C G T) of canonical k-mer x,
+    as stored (canonical), and the count index of the same edge there"""
+    code = "ACGT".index
+    if i < 4:    # out-edge to y = x[1:] + c: on y an in-edge from x's first character
+        y, j = x[1:] + "ACGT"[i], 4 + code(x[0])
+    else:        # in-edge from y = c + x[:-1]: on y an out-edge to x's last character
+        y, j = "ACGT"[i - 4] + x[:-1], code(x[-1])
+    if _rc(y) < y:   # stored on the other strand: in <-> out, character complemented
+        y, j = _rc(y), (4 + 3 - j) if j < 4 else 3 - (j - 4)
+    return y, j
+
+
+@pytest.mark.parametrize("fname,lo", [("debruijn.palindrome_chr14.fastq", ()), ("debruijn.bubble.fastq", (1,)),
+                                      ("debruijn.clean2.fastq", ()), ("debruijn.clean1.fastq", (1,))])
+def test_clean_only_erases_edges_in_pairs(fname, lo):
+    """cleaning removes edges and edge-less nodes, never adds or changes a count, and every edge
+    it removes is removed on both of its nodes (erase_edges_internal, debruijn_graph_map.hpp
+    :737-747); cycle nodes and nodes left without edges leave the graph"""
+    k = 31
+    r = oracle.run(fixture_bytes(fname), k=k, thresholding=bool(lo), thresh=bg.thresholds(lo), clean=True)
+    assert r["clean_stats"]["status"] == 0 and r["clean_stats"]["rounds"] > 0
+    before, after = _node_map(r["nodes"], k), _node_map(r["clean"]["nodes"], k)
+    assert set(after) <= set(before)
+    removed = 0
+    for x, a in after.items():
+        b = before[x]
+        assert a[8] == b[8]                                  # self count kept
+        assert all(a[i] in (0, b[i]) for i in range(8))      # an edge is kept or erased
+        assert any(a[:8])                                    # no edge-less node stays
+        for i in range(8):
+            if b[i] and not a[i]:
+                removed += 1
+                y, j = _edge_neighbour(x, i)
+                if y in after and y in before and before[y][j]:
+                    assert after[y][j] == 0, (x, i, y, j)
+    assert removed > 0
