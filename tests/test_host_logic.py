@@ -89,3 +89,75 @@ def test_partition_mix_is_a_bijection():
         v = rnd.getrandbits(62)
         h = fwd(v)
         assert h <= m and back(h) == v
+
+
+# ----------------------------------------------------- host FASTQ piece boundaries
+PIECE_HARNESS = r'''
+#include "piece_cuts.h"
+#include <cstdio>
+#include <string>
+int main(int argc, char **argv) {
+  FILE *f = fopen(argv[1], "rb");
+  std::string b;
+  char buf[1 << 16];
+  size_t n;
+  while ((n = fread(buf, 1, sizeof(buf), f)) > 0) b.append(buf, n);
+  fclose(f);
+  for (uint64_t c : piece_cuts(b.data(), b.size(), strtoull(argv[2], 0, 10))) printf("%llu\n", (unsigned long long)c);
+}
+'''
+
+
+@pytest.fixture(scope="module")
+def piece_cuts_cli(tmp_path_factory):
+    import os
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("no host C++ compiler")
+    d = tmp_path_factory.mktemp("pc")
+    src, exe = d / "pc.cpp", d / "pc"
+    src.write_text(PIECE_HARNESS)
+    subprocess.run([gxx, "-O2", "-std=c++17", "-I", os.path.join(os.path.dirname(bg.__file__), "csrc"), str(src),
+                    "-o", str(exe)], check=True)
+
+    def run(data: bytes, piece: int):
+        f = d / "in.fq"
+        f.write_bytes(data)
+        return [int(x) for x in subprocess.check_output([str(exe), str(f), str(piece)]).split()]
+    return run
+
+
+def _record_starts(fq: bytes):
+    starts, pos = set(), 0
+    for i, line in enumerate(fq.split(b"\n")):
+        if i % 4 == 0:
+            starts.add(pos)
+        pos += len(line) + 1
+    return starts
+
+
+@pytest.mark.parametrize("piece", [1024, 4096, 1 << 16])
+def test_piece_cuts_fall_on_record_starts(piece_cuts_cli, piece):
+    """bruno_load_fastq cuts host FASTQ only at record starts, even where every quality line
+    begins with '@', and about every `piece` bytes"""
+    w = synth.Workload("pc", 50_000, 100, 2_000, 0.01, 31, (2,), 0.0, (1000, 2000), (2, 2), (0.01, 0.01), 5)
+    lines = bytes(synth.make_fastq(w)).split(b"\n")
+    for i in range(3, len(lines), 4):
+        if lines[i]:
+            lines[i] = b"@" + lines[i][1:]
+    fq = b"\n".join(lines)
+    cuts = piece_cuts_cli(fq, piece)
+    assert cuts[0] == 0 and cuts == sorted(set(cuts))
+    assert set(cuts) <= _record_starts(fq)
+    assert len(cuts) >= len(fq) // piece - 2
+    assert all(b - a < 2 * piece + 1024 for a, b in zip(cuts, cuts[1:] + [len(fq)]))
+
+
+def test_piece_cuts_small_or_unsplittable_inputs(piece_cuts_cli):
+    rec = b"@r\nACGT\n+\nIIII\n"
+    assert piece_cuts_cli(rec * 10, 1 << 20) == [0]          # under two pieces: one copy
+    assert piece_cuts_cli(rec * 10, 0) == [0]
+    one = b"@r\n" + b"A" * 5000 + b"\n+\n" + b"I" * 5000 + b"\n"
+    assert piece_cuts_cli(one, 1024) == [0]                  # one record: nowhere to cut
