@@ -62,6 +62,11 @@ class _PoolResult(ctypes.Structure):
                 ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double)]
 
 
+class _CleanStats(ctypes.Structure):
+    _fields_ = [("rounds", ctypes.c_uint64), ("deadends", ctypes.c_uint64), ("bubbles", ctypes.c_uint64),
+                ("edges", ctypes.c_uint64), ("status", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 _lib: Optional[ctypes.CDLL] = None
 
 # every entry point of include/bruno_gb300.h
@@ -72,7 +77,7 @@ EXPORTS = (
     "bruno_get_sizes", "bruno_copy_k2", "bruno_copy_filtered", "bruno_copy_nodes", "bruno_copy_ranked",
     "bruno_copy_chains", "bruno_copy_chain_edges", "bruno_copy_chain_summaries", "bruno_host_alloc", "bruno_host_free", "bruno_phase_ms",
     "bruno_count_biedges_noalloc", "bruno_pool_create", "bruno_pool_submit", "bruno_pool_wait",
-    "bruno_pool_result_free", "bruno_pool_destroy",
+    "bruno_pool_result_free", "bruno_pool_destroy", "bruno_clean_deadend_and_bubbles_naive",
 )
 
 
@@ -105,6 +110,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "bruno_pool_submit": [P, P, SZ, ctypes.POINTER(U64)],
         "bruno_pool_wait": [P, U64, ctypes.POINTER(_PoolResult)], "bruno_pool_result_free": [ctypes.POINTER(_PoolResult)],
         "bruno_pool_destroy": [P],
+        "bruno_clean_deadend_and_bubbles_naive": [P, ctypes.POINTER(_CleanStats)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -269,6 +275,15 @@ class Graph:
 
     def to_compressed_chains(self) -> None:
         self._check(self.lib.bruno_to_compressed_chains(self.ctx), "to_compressed_chains")
+
+    def clean_deadend_and_bubbles_naive(self) -> dict:
+        """The _freq_clean driver's graph cleaning (compact_dbg_clean.hpp:575-890) on the ranked
+        graph; afterwards every copy returns the cleaned graph.  Returns the loop's tallies."""
+        s = _CleanStats()
+        st = self.lib.bruno_clean_deadend_and_bubbles_naive(self.ctx, ctypes.byref(s))
+        out = {n: int(getattr(s, n)) for n in ("rounds", "deadends", "bubbles", "edges", "status")}
+        self._check(st, "clean_deadend_and_bubbles_naive")
+        return out
 
     def build_and_compact(self, data, nbytes: Optional[int] = None, is_device: bool = False) -> None:
         """The whole plain path; host bytes are copied in, device bytes are read in place."""

@@ -142,6 +142,7 @@ bruno_status bruno_ctx_destroy(bruno_ctx *c) {
                  &c->f_keys, &c->f_edges, &c->f_counts, &c->blk_cnt, &c->blk_base, &c->ckey, &c->cedge,
                  &c->cstate, &c->cstate2, &c->pend, &c->pay, &c->unf0, &c->unf1, &c->removed, &c->r_K, &c->r_rep, &c->r_dist,
                  &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list, &c->e_ends, &c->e_freqs, &c->s_kmers, &c->s_dist, &c->s_flags, &c->k1tab,
+                 &c->cl_trec, &c->cl_tslot, &c->cl_sums, &c->cl_norm, &c->cl_htab, &c->cl_q, &c->cl_found,
                  &c->records, &c->bucket_cnt, &c->records2, &c->sub_cnt};
   for (Buf *b : bufs) release(*b);
   for (Buf &b : c->seg_bufs) release(b);
@@ -201,6 +202,7 @@ bruno_status bruno_reset(bruno_ctx *c) {
   c->n_summaries = 0;
   c->summaries_done = false;
   c->general_emission = false;
+  c->cleaned = false;
   c->launches = 0;
   std::memset(c->flag_hist, 0, sizeof(c->flag_hist));
   std::memset(c->phase_ms, 0, sizeof(c->phase_ms));
@@ -291,7 +293,8 @@ bruno_status bruno_local_insert_by_freqencies(bruno_ctx *c, const uint64_t *thre
   if (!c) return BRUNO_ERR_ARG;
   if (c->stage != 2) return set_err(c, BRUNO_ERR_ARG, "local_insert_by_freqencies needs counted (k+2)-mers");
   record(c, 2);
-  bruno_status st = run_filter(c, thresh ? thresh : c->cfg.thresh);
+  std::memcpy(c->thr_used, thresh ? thresh : c->cfg.thresh, sizeof(c->thr_used));
+  bruno_status st = run_filter(c, c->thr_used);
   if (st != BRUNO_OK) return st;
   record(c, 3);
   cudaEventSynchronize(c->ev[3]);
@@ -336,6 +339,27 @@ bruno_status bruno_to_compressed_chains(bruno_ctx *c) {
   record(c, 6);
   cudaEventSynchronize(c->ev[6]);
   c->phase_ms[5] = elapsed(c, 5, 6);
+  c->stage = 6;
+  if (!c->chains_clean)
+    return set_err(c, BRUNO_ERR_INVARIANT,
+                   "chain pointers are not mutually consistent (asymmetric edge filtering); the listranked "
+                   "nodes are valid, the compacted sequences are not");
+  return BRUNO_OK;
+}
+
+bruno_status bruno_clean_deadend_and_bubbles_naive(bruno_ctx *c, bruno_clean_stats *stats) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (c->stage < 5) return set_err(c, BRUNO_ERR_ARG, "cleaning needs ranked chains");
+  if (c->cleaned) return set_err(c, BRUNO_ERR_ARG, "the graph is cleaned already; call bruno_reset first");
+  bruno_clean_stats s{};
+  record(c, 5);
+  bruno_status st = run_clean(c, &s.rounds, &s.deadends, &s.bubbles, &s.edges, &s.status);
+  if (stats) *stats = s;
+  if (st != BRUNO_OK) return st;
+  record(c, 6);
+  cudaEventSynchronize(c->ev[6]);
+  c->phase_ms[5] = elapsed(c, 5, 6);
+  c->cleaned = true;
   c->stage = 6;
   if (!c->chains_clean)
     return set_err(c, BRUNO_ERR_INVARIANT,

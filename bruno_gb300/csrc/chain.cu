@@ -1233,6 +1233,591 @@ bruno_status chain_edges_typed(Ctx *c) {
   return BRUNO_OK;
 }
 
+
+/* ================================================================ graph cleaning
+ * clean_deadend_and_bubbles_naive (compact_dbg_clean.hpp:575-890) on the device, one rank:
+ * dead ends and bubbles are read off summaries weighted by the node table, their low-frequency
+ * end edges are erased on both nodes, edge-less nodes leave the graph, the nodes are classified
+ * again and the chain map is rebuilt and ranked, until no dead end or bubble is left. */
+
+/* summarized_chain<K, uint16> (debruijn_chain_node.hpp:174): prev at 5', 5' terminus (the
+ * chain representative), 3' terminus, next at 3', distance between the termini, the 5' and 3'
+ * end-edge frequencies; plus the chain node the record was made from */
+template <class KT>
+struct FSum { KT k0, k1, k2, k3; uint32_t len; uint16_t f5, f6; uint32_t node, pad; };
+
+/* an erase query or a found edge: k-mer (low word first) and a DNA16 biedge */
+struct EraseQ { uint64_t w[2]; uint32_t edge, pad; };
+
+/* the bubble grouping table: chains with one 5' branch k-mer (key + 1; 0 = empty) */
+struct BubbleEnt { unsigned long long key; unsigned int cnt; unsigned int idx[8]; unsigned int pad; };
+
+template <class KT>
+__device__ __forceinline__ int kcmp(KT a, KT b) { return KOps<KT>::lt(a, b) ? -1 : (KOps<KT>::eq(a, b) ? 0 : 1); }
+
+/* the summaries' order: the reference's sort keys (5' terminus, next at 3'), then the rest of
+ * the record, as the oracle breaks the reference's ties */
+template <class KT>
+__device__ __forceinline__ int sum_cmp(const FSum<KT> &a, const FSum<KT> &b) {
+  int c;
+  if ((c = kcmp(a.k1, b.k1)) != 0) return c;
+  if ((c = kcmp(a.k3, b.k3)) != 0) return c;
+  if ((c = kcmp(a.k0, b.k0)) != 0) return c;
+  if ((c = kcmp(a.k2, b.k2)) != 0) return c;
+  if (a.f5 != b.f5) return a.f5 < b.f5 ? -1 : 1;
+  if (a.f6 != b.f6) return a.f6 < b.f6 ? -1 : 1;
+  return 0;
+}
+
+/* the bubbles' order: (5' branch, 3' branch, length), then the termini */
+template <class KT>
+__device__ __forceinline__ bool bubble_less(const FSum<KT> &a, const FSum<KT> &b) {
+  int c;
+  if ((c = kcmp(a.k0, b.k0)) != 0) return c < 0;
+  if ((c = kcmp(a.k3, b.k3)) != 0) return c < 0;
+  if (a.len != b.len) return a.len < b.len;
+  if ((c = kcmp(a.k1, b.k1)) != 0) return c < 0;
+  return kcmp(a.k2, b.k2) < 0;
+}
+
+__device__ __forceinline__ uint16_t count_at(uint64_t w, unsigned c) { return (uint16_t)(w >> (16 * c)); }
+/* get_{in,out}_edge_total_frequency (debruijn_graph_node.hpp:299-313): saturating sum */
+__device__ __forceinline__ uint16_t total_of(uint64_t w) {
+  uint32_t t = 0;
+  #pragma unroll
+  for (unsigned c = 0; c < 4; ++c) t = min(0xFFFFu, t + count_at(w, c));
+  return (uint16_t)t;
+}
+__device__ __forceinline__ bool single16(unsigned n) { return n != 0 && (n & (n - 1)) == 0; }
+__device__ __forceinline__ unsigned rc_biedge16(unsigned e) { return (comp16(e & 0xFu) << 4) | comp16((e >> 4) & 0xFu); }
+
+template <class KT>
+__device__ __forceinline__ void canon_edge(KT &x, unsigned &e, int k) {   /* lex_less on (k-mer, biedge) */
+  const KT y = KOps<KT>::rc(x, k);
+  if (!KOps<KT>::lt(x, y)) { x = y; e = rc_biedge16(e); }
+}
+
+/* zero the counts that the single-character nibbles of e name, on the node of canonical x */
+template <class KT>
+__device__ __forceinline__ void zero_edges(uint64_t *table, const TableGeom &g, KT x, unsigned e) {
+  constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
+  const long long s = table_find<KT>(table, g, 4096u, x);
+  if (s < 0) return;
+  unsigned long long *pw = (unsigned long long *)(table + (uint64_t)s * SU + KWD);
+  const unsigned out = e & 0xFu, in = (e >> 4) & 0xFu;
+  if (single16(out)) atomicAnd(&pw[0], ~(0xFFFFull << (16 * (__ffs(out) - 1))));
+  if (single16(in)) atomicAnd(&pw[1], ~(0xFFFFull << (16 * (__ffs(in) - 1))));
+}
+
+template <class KT>
+__device__ __forceinline__ void clear_node(uint64_t *slot) {   /* the slot stops being a graph node */
+  atomicAnd((unsigned long long *)&slot[Slot<KT>::KEYW - 1], ~(unsigned long long)KEY_NODE);
+}
+
+/* erase_nodes(get_cycle_node_kmers()) (debruijn_graph_map.hpp:833-836, 811-827): every cycle
+ * node leaves the graph and its neighbours lose the edges back to it (get_remote_edges, :440-471) */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_cl_cycles(const uint64_t *ckey, const uint8_t *removed, uint64_t M,
+                                                    uint64_t *table, TableGeom g, int k) {
+  constexpr int KWD = KOps<KT>::WORDS, SU = Slot<KT>::U64;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (removed[i] != 1) continue;
+    const KT K = KOps<KT>::load(ckey + i * KWD);
+    const long long s = table_find<KT>(table, g, 4096u, K);
+    if (s < 0) continue;
+    uint64_t *slot = table + (uint64_t)s * SU;
+    const uint64_t out = slot[KWD], in = slot[KWD + 1];
+    for (unsigned c = 0; c < 4; ++c) {
+      if (count_at(out, c)) {   /* K.c: its in-edge from K's first base */
+        KT y = KOps<KT>::append(K, c, k);
+        unsigned e = (1u << KOps<KT>::first(K, k)) << 4;
+        canon_edge(y, e, k);
+        zero_edges<KT>(table, g, y, e);
+      }
+      if (count_at(in, c)) {    /* c.K: its out-edge to K's last base */
+        KT y = KOps<KT>::prepend(c, K, k);
+        unsigned e = 1u << KOps<KT>::last(K);
+        canon_edge(y, e, k);
+        zero_edges<KT>(table, g, y, e);
+      }
+    }
+    clear_node<KT>(slot);
+  }
+}
+
+/* idx.erase_if(IsIsolated) (debruijn_graph_filters.hpp:163-172): nodes without an edge leave
+ * the graph; counts the nodes and branch nodes that stay */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_cl_isolated(uint64_t *table, uint64_t nslots, DevCounters *ctr) {
+  constexpr int KWD = Slot<KT>::KEYW, SU = Slot<KT>::U64;
+  unsigned long long live = 0, br = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t *s = table + i * SU;
+    if (!key_is_node(KOps<KT>::load(s))) continue;
+    if (s[KWD] == 0 && s[KWD + 1] == 0) { clear_node<KT>(s); continue; }
+    ++live;
+    br += (slot_flags<KT>(s) & NF_BRANCH) ? 1 : 0;
+  }
+  live = warp_sum(live); br = warp_sum(br);
+  if ((threadIdx.x & 31) == 0) {
+    if (live) atomicAdd(&ctr->cl_live, live);
+    if (br) atomicAdd(&ctr->cl_live_branch, br);
+  }
+}
+
+/* IsBranchPoint / IsChainNode again for every node (the filter's rule, debruijn_graph_filters.hpp
+ * :57-220), with the chain and branch lists and each chain node's index rebuilt */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_cl_classify(uint64_t *table, uint64_t nslots, int k, uint32_t *chain_list,
+                                                      uint32_t *branch_list, uint64_t cap, DevCounters *ctr) {
+  constexpr int KWD = Slot<KT>::KEYW, SU = Slot<KT>::U64;
+  bool over = false;
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < nslots; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    uint64_t *s = table + (i < nslots ? i : 0) * SU;
+    const bool node = i < nslots && key_is_node(KOps<KT>::load(s));
+    bool branch = false;
+    if (node) {
+      const KT key = key_kmer(node_key(KOps<KT>::load(s)));
+      const bool kpal = k_palindrome(key, k);
+      const bool high = km1_high_palindrome(key, k), low = km1_low_palindrome(key, k);
+      const unsigned first = KOps<KT>::first(key, k), last = KOps<KT>::last(key);
+      const bool oddk = (k & 1) != 0;
+      unsigned din = 0, dout = 0;
+      bool k1pal = false;
+      #pragma unroll
+      for (unsigned c = 0; c < 4; ++c) {
+        const bool o = count_at(s[KWD], c) > 0, n = count_at(s[KWD + 1], c) > 0;
+        dout += o; din += n;
+        if (oddk && o && low && (first == 3u - c || first == c)) k1pal = true;
+        if (oddk && n && high && (last == 3u - c || last == c)) k1pal = true;
+      }
+      branch = din >= 2 || dout >= 2 || kpal || k1pal;
+    }
+    const unsigned long long oc = block_append(node && !branch, &ctr->n_chain);
+    const unsigned long long ob = block_append(node && branch, &ctr->n_branch);
+    if (node) {
+      const unsigned long long o = branch ? ob : oc;
+      if (o >= cap) { over = true; continue; }
+      const uint64_t aux = branch ? 0xFFFFFFFFull : o;
+      s[KWD + 2] = (s[KWD + 2] & 0xFFFFull) | ((uint64_t)(branch ? NF_BRANCH : NF_CHAIN) << 16) | (aux << 32);
+      (branch ? branch_list : chain_list)[o] = (uint32_t)i;
+    }
+  }
+  if (over) atomicOr(&ctr->err, (unsigned long long)DERR_INVARIANT);
+}
+
+/* to_summarized_chains(dbg) (debruijn_chain_graph.hpp:2044-2105), first half: one record per
+ * chain end (IsTerminusOrIsolated), oriented so that the 5' terminus is the representative,
+ * with the end node's total in- or out-edge frequency.  tslot: record index per chain node. */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_cl_termini(EmitArgs a, const uint64_t *table, TableGeom g, FSum<KT> *trec,
+                                                     uint32_t *tslot, DevCounters *ctr) {
+  constexpr int KWD = KOps<KT>::WORDS, SU = Slot<KT>::U64;
+  unsigned long long nz = 0;
+  bool bad = false, missing = false;
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < a.M; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    bool want = false;
+    FSum<KT> r{};
+    if (i < a.M && a.removed[i] == 0) {
+      const ChainState st = a.cs[i];
+      const bool t5 = term(st.inD), t3 = term(st.outD);
+      if (t5 || t3) {
+        want = true;
+        const KT K = KOps<KT>::load(a.ckey + i * KWD);
+        const KT inK = side_kmer<KT>(st.inP, a), outK = side_kmer<KT>(st.outP, a);
+        uint16_t fin = 0, fout = 0;
+        const long long s = table_find<KT>(table, g, 4096u, K);
+        if (s < 0) missing = true;
+        else { fout = total_of(table[(uint64_t)s * SU + KWD]); fin = total_of(table[(uint64_t)s * SU + KWD + 1]); }
+        const KT Z{};
+        r.len = (st.inD & DM) + (st.outD & DM);
+        r.node = (uint32_t)i;
+        if (t5 && t3) {   /* unit or isolated chain */
+          r.k0 = inK; r.k1 = K; r.k2 = K; r.k3 = outK; r.f5 = fin; r.f6 = fout;
+        } else if (t5) {
+          const KT o = KOps<KT>::rc(outK, a.k);
+          if (KOps<KT>::lt(K, o)) { r.k0 = inK; r.k1 = K; r.k2 = outK; r.k3 = Z; r.f5 = fin; }
+          else if (KOps<KT>::lt(o, K)) { r.k0 = Z; r.k1 = o; r.k2 = KOps<KT>::rc(K, a.k); r.k3 = KOps<KT>::rc(inK, a.k); r.f6 = fin; }
+          else bad = true;   /* the reference throws: a palindrome or a mobius strip */
+        } else {
+          const KT o = KOps<KT>::rc(K, a.k);
+          if (KOps<KT>::lt(inK, o)) { r.k0 = Z; r.k1 = inK; r.k2 = K; r.k3 = outK; r.f6 = fout; }
+          else if (KOps<KT>::lt(o, inK)) { r.k0 = KOps<KT>::rc(outK, a.k); r.k1 = o; r.k2 = KOps<KT>::rc(inK, a.k); r.k3 = Z; r.f5 = fout; }
+          else bad = true;
+        }
+        nz += KOps<KT>::eq(r.k1, Z) ? 0 : 1;
+      }
+    }
+    const unsigned long long o = block_append(want, &ctr->cl_term);
+    if (want) { trec[o] = r; tslot[i] = (uint32_t)o; }
+  }
+  nz = warp_sum(nz);
+  if ((threadIdx.x & 31) == 0 && nz) atomicAdd(&ctr->cl_nonzero, nz);
+  if (bad) atomicOr(&ctr->err, (unsigned long long)DERR_UNCLEAN_CHAINS);
+  if (missing) atomicOr(&ctr->err, (unsigned long long)DERR_INVARIANT);
+}
+
+/* second half (:2107-2128): sorted by (5' terminus, next at 3'), a unit chain's record is kept
+ * and the two ends of a chain merge (merge_summarized_chains, debruijn_chain_node.hpp:176-197:
+ * the later record in that order keeps its fields unless the earlier one has the larger end
+ * frequency).  Each end finds its partner through its ranked pointer; the later one emits.  On
+ * one rank the shifts deliver value-initialised records: a first record on the all-A k-mer is
+ * also emitted alone, and a last one on it is dropped. */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_cl_pair(EmitArgs a, const FSum<KT> *trec, const uint32_t *tslot, uint64_t nt,
+                                                  FSum<KT> *sums, DevCounters *ctr) {
+  const bool all_polya = *(volatile unsigned long long *)&ctr->cl_nonzero == 0;
+  bool bad = false;
+  for (uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x; t0 < nt; t0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t t = t0 + threadIdx.x;
+    bool emit = false;
+    FSum<KT> m{};
+    if (t < nt) {
+      const FSum<KT> r = trec[t];
+      const bool polya = KOps<KT>::eq(r.k1, KT{});
+      if (r.len == 0) {
+        m = r;
+        emit = !(polya && all_polya);
+      } else {
+        const ChainState st = a.cs[r.node];
+        const uint64_t P = term(st.inD) ? st.outP : st.inP;
+        const uint32_t j = (uint32_t)P;
+        if ((P & (PF_EXT | PF_BLANK)) || j >= a.M || j == r.node || a.removed[j] != 0 ||
+            !(term(a.cs[j].inD) || term(a.cs[j].outD))) {
+          bad = true;
+        } else {
+          const FSum<KT> q = trec[tslot[j]];
+          if (q.node != j || q.len != r.len || !KOps<KT>::eq(q.k1, r.k1) || !KOps<KT>::eq(q.k2, r.k2)) {
+            bad = true;
+          } else {
+            const int c = sum_cmp<KT>(r, q);
+            if (c > 0 || (c == 0 && r.node > j)) {
+              m = r;
+              if (m.f5 < q.f5) { m.k0 = q.k0; m.f5 = q.f5; }
+              if (m.f6 < q.f6) { m.k3 = q.k3; m.f6 = q.f6; }
+              emit = !(polya && all_polya);
+            } else if (polya) {
+              m = r;
+              emit = true;
+            }
+          }
+        }
+      }
+    }
+    const unsigned long long o = block_append(emit, &ctr->cl_sum);
+    if (emit) sums[o] = m;
+  }
+  if (bad) atomicOr(&ctr->err, (unsigned long long)DERR_UNCLEAN_CHAINS);
+}
+
+template <class KT>
+__device__ __forceinline__ void put_query(EraseQ *q, unsigned long long o, KT x, unsigned e) {
+  EraseQ v{};
+  KOps<KT>::store(v.w, x);
+  v.edge = e;
+  q[o] = v;
+}
+
+/* find_deadends (debruijn_topo_operations.hpp:146-175) with deadend_filter
+ * (compact_dbg_clean.hpp:63-80) and the end edges to sever (:619-640): the 5' branch's
+ * out-edge to the 5' terminus, the 3' branch's in-edge from the 3' terminus; and the chains
+ * with both ends on branches (find_normal_chains, :251-272), put on the strand where the 5'
+ * branch is not above the reverse complement of the 3' branch (find_bubbles, :310-316) */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_cl_select(const FSum<KT> *sums, uint64_t ns, int k, uint32_t min_freq,
+                                                    uint32_t max_len, EraseQ *q, FSum<KT> *norm, DevCounters *ctr) {
+  unsigned long long nd = 0;
+  for (uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x; t0 < ns; t0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t t = t0 + threadIdx.x;
+    FSum<KT> r{};
+    if (t < ns) r = sums[t];
+    const bool valid = t < ns;
+    const bool dead = valid && r.len < max_len && r.f5 < min_freq && r.f6 < min_freq && ((r.f5 == 0) != (r.f6 == 0));
+    const bool d5 = dead && r.f5 > 0, d3 = dead && r.f6 > 0;
+    const bool normal = valid && r.len > 0 && r.f5 > 0 && r.f6 > 0;
+    nd += dead ? 1 : 0;
+    unsigned long long o = block_append(d5, &ctr->cl_q);
+    if (d5) put_query<KT>(q, o, r.k0, 1u << KOps<KT>::last(r.k1));
+    o = block_append(d3, &ctr->cl_q);
+    if (d3) put_query<KT>(q, o, r.k3, (1u << KOps<KT>::first(r.k2, k)) << 4);
+    if (normal && KOps<KT>::lt(KOps<KT>::rc(r.k3, k), r.k0)) {   /* transform::reverse_complement(summary) */
+      FSum<KT> x = r;
+      x.k0 = KOps<KT>::rc(r.k3, k); x.k1 = KOps<KT>::rc(r.k2, k);
+      x.k2 = KOps<KT>::rc(r.k1, k); x.k3 = KOps<KT>::rc(r.k0, k);
+      x.f5 = r.f6; x.f6 = r.f5;
+      r = x;
+    }
+    o = block_append(normal, &ctr->cl_norm);
+    if (normal) norm[o] = r;
+  }
+  nd = warp_sum(nd);
+  if ((threadIdx.x & 31) == 0 && nd) atomicAdd(&ctr->cl_dead, nd);
+}
+
+__device__ __forceinline__ unsigned long long bubble_key(KW1 x) { return x.v + 1; }   /* k-mers fit 62 bits */
+__device__ __forceinline__ unsigned long long bubble_key(KW2 x) {
+  return (mix64(x.lo ^ mix64(x.hi + 0x9e3779b97f4a7c15ull)) >> 1) + 1;
+}
+
+/* chains grouped by their 5' branch k-mer (at most four leave one k-mer's out side; eight
+ * places allow for hash collisions of 128-bit k-mers, told apart in k_cl_bubbles) */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_cl_group(const FSum<KT> *norm, uint64_t nn, BubbleEnt *tab, uint64_t hcap,
+                                                   DevCounters *ctr) {
+  bool over = false;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += (uint64_t)gridDim.x * blockDim.x) {
+    const unsigned long long key = bubble_key(norm[i].k0);
+    uint64_t h = mix64(key) & (hcap - 1);
+    bool placed = false;
+    for (uint64_t p = 0; p < hcap && !placed; ++p, h = (h + 1) & (hcap - 1)) {
+      const unsigned long long prev = atomicCAS(&tab[h].key, 0ull, key);
+      if (prev != 0ull && prev != key) continue;
+      const unsigned int c = atomicAdd(&tab[h].cnt, 1u);
+      if (c < 8) tab[h].idx[c] = (unsigned int)i; else over = true;
+      placed = true;
+    }
+    if (!placed) over = true;
+  }
+  if (over) atomicOr(&ctr->err, (unsigned long long)DERR_INVARIANT);
+}
+
+/* find_bubbles' scan (:348-392) per group: sorted by (5' branch, 3' branch, length), every run
+ * of two or more chains between the same two branches whose neighbours pass bubble_filter
+ * (compact_dbg_clean.hpp:84-112: lengths within one, an end edge below min_freq) gives both
+ * end edges of each of its chains to sever (:687-699) */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_cl_bubbles(const FSum<KT> *norm, const BubbleEnt *tab, uint64_t hcap, int k,
+                                                     uint32_t min_freq, EraseQ *q, DevCounters *ctr) {
+  bool over = false;
+  unsigned long long nb = 0;
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < hcap; e += (uint64_t)gridDim.x * blockDim.x) {
+    if (tab[e].key == 0ull) continue;
+    const unsigned int n = tab[e].cnt;
+    if (n > 8) { over = true; continue; }
+    if (n < 2) continue;
+    unsigned int m[8];
+    for (unsigned int x = 0; x < n; ++x) m[x] = tab[e].idx[x];
+    for (unsigned int x = 1; x < n; ++x)   /* insertion sort, at most eight */
+      for (unsigned int y = x; y > 0 && bubble_less<KT>(norm[m[y]], norm[m[y - 1]]); --y) {
+        const unsigned int t = m[y]; m[y] = m[y - 1]; m[y - 1] = t;
+      }
+    unsigned int first = 0, x = 1;
+    for (; x <= n; ++x) {
+      bool same = false;
+      if (x < n) {
+        const FSum<KT> &l = norm[m[x - 1]], &r = norm[m[x]];
+        const uint32_t d = l.len > r.len ? l.len - r.len : r.len - l.len;
+        same = KOps<KT>::eq(l.k0, r.k0) && KOps<KT>::eq(l.k3, r.k3) && d <= 1 &&
+               (l.f5 < min_freq || l.f6 < min_freq || r.f5 < min_freq || r.f6 < min_freq);
+      }
+      if (same) continue;
+      if (x - first > 1) {
+        const unsigned long long o = atomicAdd(&ctr->cl_q, 2ull * (x - first));
+        for (unsigned int y = first; y < x; ++y) {
+          const FSum<KT> &c = norm[m[y]];
+          put_query<KT>(q, o + 2ull * (y - first), c.k0, 1u << KOps<KT>::last(c.k1));
+          put_query<KT>(q, o + 2ull * (y - first) + 1, c.k3, (1u << KOps<KT>::first(c.k2, k)) << 4);
+        }
+        nb += x - first;
+      }
+      first = x;
+    }
+  }
+  if (nb) atomicAdd(&ctr->cl_bub, nb);
+  if (over) atomicOr(&ctr->err, (unsigned long long)DERR_INVARIANT);
+}
+
+/* erase_edges(query, edge_freq_filter) (debruijn_graph_map.hpp:770-775), first step
+ * (find_edges with the predicate, :615-660): per query on the canonical strand, the nibbles
+ * whose edge exists with a count below min_freq (compact_multi_biedge::select) */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_cl_find(const EraseQ *q, uint64_t q0, uint64_t q1, const uint64_t *table,
+                                                  TableGeom g, int k, uint32_t min_freq, EraseQ *found,
+                                                  DevCounters *ctr) {
+  constexpr int KWD = Slot<KT>::KEYW, SU = Slot<KT>::U64;
+  for (uint64_t t0 = q0 + (uint64_t)blockIdx.x * blockDim.x; t0 < q1; t0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t t = t0 + threadIdx.x;
+    bool want = false;
+    KT x{};
+    unsigned e = 0;
+    if (t < q1) {
+      x = KOps<KT>::load(q[t].w);
+      e = q[t].edge;
+      canon_edge(x, e, k);
+      const long long s = table_find<KT>(table, g, 4096u, x);
+      if (s >= 0) {
+        const uint64_t *pw = table + (uint64_t)s * SU + KWD;
+        const unsigned in = (e >> 4) & 0xFu, out = e & 0xFu;
+        if (single16(in)) {
+          const uint16_t v = count_at(pw[1], __ffs(in) - 1);
+          if (!(v > 0 && v < min_freq)) e &= 0x0Fu;
+        }
+        if (single16(out)) {
+          const uint16_t v = count_at(pw[0], __ffs(out) - 1);
+          if (!(v > 0 && v < min_freq)) e &= 0xF0u;
+        }
+        want = e != 0;
+      }
+    }
+    const unsigned long long o = block_append(want, &ctr->cl_found);
+    if (want) put_query<KT>(found, o, x, e);
+  }
+}
+
+/* second step (erase_edges_internal, :737-747): the edges found and, on the neighbours, the
+ * same edges seen from there (get_remote_edges for simple biedges, :475-510) */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_cl_erase(const EraseQ *f, uint64_t nf, uint64_t *table, TableGeom g, int k) {
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += (uint64_t)gridDim.x * blockDim.x) {
+    const KT x = KOps<KT>::load(f[t].w);
+    const unsigned e = f[t].edge, in = (e >> 4) & 0xFu, out = e & 0xFu;
+    zero_edges<KT>(table, g, x, e);
+    if (single16(in)) {
+      KT y = KOps<KT>::prepend((unsigned)(__ffs(in) - 1), x, k);
+      unsigned r = 1u << KOps<KT>::last(x);
+      canon_edge(y, r, k);
+      zero_edges<KT>(table, g, y, r);
+    }
+    if (single16(out)) {
+      KT y = KOps<KT>::append(x, (unsigned)(__ffs(out) - 1), k);
+      unsigned r = (1u << KOps<KT>::first(x, k)) << 4;
+      canon_edge(y, r, k);
+      zero_edges<KT>(table, g, y, r);
+    }
+  }
+}
+
+template <class KT>
+bruno_status clean_typed(Ctx *c, uint64_t *rounds, uint64_t *deadends, uint64_t *bubbles, uint64_t *edges,
+                         int32_t *status) {
+  bruno_status st;
+  const int sms = sms_count(), k = c->cfg.k;
+  const uint32_t min_freq = (uint32_t)(c->thr_used[2] + 1);     /* edge_freq_filter(threshes[2] + 1) */
+  const uint32_t max_len = 2u * (uint32_t)k - 1u;               /* deadend_filter(2 * k - 1, ...) */
+  uint64_t *table = (uint64_t *)c->table.p;
+  const int KWD = Slot<KT>::KEYW;
+  *rounds = *deadends = *bubbles = *edges = 0;
+  *status = 0;
+  auto isolated = [&]() -> bruno_status {
+    cudaMemsetAsync(&c->dctr->cl_live, 0, 16, c->stream);
+    k_cl_isolated<KT><<<sms * 8, TPB, 0, c->stream>>>(table, c->nslots, c->dctr);
+    c->launches += 1;
+    bruno_status s2 = sync_counters(c);
+    if (s2 != BRUNO_OK) return s2;
+    c->n_nodes = c->hctr->cl_live;
+    c->n_branch = c->hctr->cl_live_branch;
+    return BRUNO_OK;
+  };
+  auto cycles = [&]() -> bruno_status {
+    if (c->n_cycle && c->n_chain)
+      k_cl_cycles<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->ckey.p, (const uint8_t *)c->removed.p,
+                                                      c->n_chain, table, c->geom, k);
+    c->launches += 1;
+    return isolated();
+  };
+  /* the driver takes cycle nodes and then edge-less nodes out right after the first ranking
+   * (compact_dbg_freq_construct_clean.cpp:599-604) */
+  if ((st = cycles()) != BRUNO_OK) return st;
+  for (uint64_t iter = 0;; ++iter) {
+    const uint64_t M = c->n_chain, Mb = std::max<uint64_t>(1, M);
+    if ((st = ensure(c, c->cl_trec, Mb * sizeof(FSum<KT>))) != BRUNO_OK) return st;
+    if ((st = ensure(c, c->cl_tslot, Mb * 4)) != BRUNO_OK) return st;
+    EmitArgs a{};
+    a.ckey = (const uint64_t *)c->ckey.p; a.cedge = (const uint8_t *)c->cedge.p; a.cs = (const ChainState *)c->cstate.p;
+    a.removed = (const uint8_t *)c->removed.p; a.M = M; a.k = k;
+    FSum<KT> *trec = (FSum<KT> *)c->cl_trec.p;
+    cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
+    cudaMemsetAsync(&c->dctr->cl_term, 0, 8 * 8, c->stream);   /* cl_term .. cl_bub */
+    if (M) k_cl_termini<KT><<<sms * 8, TPB, 0, c->stream>>>(a, table, c->geom, trec, (uint32_t *)c->cl_tslot.p, c->dctr);
+    c->launches += 1;
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    const uint64_t nt = c->hctr->cl_term, ntb = std::max<uint64_t>(1, nt);
+    if ((st = ensure(c, c->cl_sums, ntb * sizeof(FSum<KT>))) != BRUNO_OK) return st;
+    if ((st = ensure(c, c->cl_norm, ntb * sizeof(FSum<KT>))) != BRUNO_OK) return st;
+    if ((st = ensure(c, c->cl_q, 4 * ntb * sizeof(EraseQ))) != BRUNO_OK) return st;
+    if ((st = ensure(c, c->cl_found, 4 * ntb * sizeof(EraseQ))) != BRUNO_OK) return st;
+    FSum<KT> *sums = (FSum<KT> *)c->cl_sums.p, *norm = (FSum<KT> *)c->cl_norm.p;
+    EraseQ *q = (EraseQ *)c->cl_q.p, *found = (EraseQ *)c->cl_found.p;
+    const int gt = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 8, (nt + TPB - 1) / TPB));
+    if (nt) k_cl_pair<KT><<<gt, TPB, 0, c->stream>>>(a, trec, (const uint32_t *)c->cl_tslot.p, nt, sums, c->dctr);
+    c->launches += 1;
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    if (c->hctr->err & DERR_INVARIANT) return set_err(c, BRUNO_ERR_INVARIANT, "cleaning: a chain end has no node");
+    if (c->hctr->err & DERR_UNCLEAN_CHAINS) {
+      *status = 2;
+      return set_err(c, BRUNO_ERR_INVARIANT, "cleaning needs mutually consistent chain pointers");
+    }
+    const uint64_t ns = c->hctr->cl_sum;
+    if (ns) k_cl_select<KT><<<gt, TPB, 0, c->stream>>>(sums, ns, k, min_freq, max_len, q, norm, c->dctr);
+    c->launches += 1;
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    const uint64_t nq_dead = c->hctr->cl_q, nn = c->hctr->cl_norm, n_dead = c->hctr->cl_dead;
+    uint64_t hcap = 64;
+    while (hcap < 2 * nn) hcap <<= 1;
+    if ((st = ensure(c, c->cl_htab, hcap * sizeof(BubbleEnt))) != BRUNO_OK) return st;
+    BubbleEnt *tab = (BubbleEnt *)c->cl_htab.p;
+    cudaMemsetAsync(tab, 0, hcap * sizeof(BubbleEnt), c->stream);
+    const int gn = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 8, (nn + TPB - 1) / TPB));
+    const int gh = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 8, (hcap + TPB - 1) / TPB));
+    if (nn) {
+      k_cl_group<KT><<<gn, TPB, 0, c->stream>>>(norm, nn, tab, hcap, c->dctr);
+      k_cl_bubbles<KT><<<gh, TPB, 0, c->stream>>>(norm, tab, hcap, k, min_freq, q, c->dctr);
+    }
+    c->launches += 2;
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    if (c->hctr->err & DERR_INVARIANT) return set_err(c, BRUNO_ERR_INVARIANT, "cleaning: bubble grouping overflowed");
+    const uint64_t nq = c->hctr->cl_q, n_bub = c->hctr->cl_bub;
+    if (n_dead == 0 && n_bub == 0) break;
+    *deadends += n_dead;
+    *bubbles += n_bub;
+    /* dead ends first, then bubbles, each followed by the removal of edge-less nodes */
+    uint64_t erased = 0;
+    const uint64_t ranges[2][2] = {{0, nq_dead}, {nq_dead, nq}};
+    for (int b = 0; b < 2; ++b) {
+      const uint64_t q0 = ranges[b][0], q1 = ranges[b][1];
+      cudaMemsetAsync(&c->dctr->cl_found, 0, 8, c->stream);
+      const int gq = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 8, (q1 - q0 + TPB - 1) / TPB));
+      if (q1 > q0) k_cl_find<KT><<<gq, TPB, 0, c->stream>>>(q, q0, q1, table, c->geom, k, min_freq, found, c->dctr);
+      c->launches += 1;
+      if ((st = sync_counters(c)) != BRUNO_OK) return st;
+      const uint64_t nf = c->hctr->cl_found;
+      const int gf = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 8, (nf + TPB - 1) / TPB));
+      if (nf) k_cl_erase<KT><<<gf, TPB, 0, c->stream>>>(found, nf, table, c->geom, k);
+      c->launches += 1;
+      erased += nf;
+      if ((st = isolated()) != BRUNO_OK) return st;
+    }
+    *edges += erased;
+    ++*rounds;
+    if (erased == 0) { *status = 1; break; }   /* the reference would find the same again, forever */
+    /* recompaction: classify, rebuild the chain map, rank, take cycles and edge-less nodes out */
+    const uint64_t cap = std::max<uint64_t>(1, c->n_slots_claimed);
+    cudaMemsetAsync(&c->dctr->n_chain, 0, 8, c->stream);
+    cudaMemsetAsync(&c->dctr->n_branch, 0, 8, c->stream);
+    cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
+    k_cl_classify<KT><<<sms * 8, TPB, 0, c->stream>>>(table, c->nslots, k, (uint32_t *)c->chain_list.p,
+                                                      (uint32_t *)c->branch_list.p, cap, c->dctr);
+    c->launches += 1;
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    if (c->hctr->err & DERR_INVARIANT) return set_err(c, BRUNO_ERR_INVARIANT, "cleaning: node lists overflowed");
+    c->n_chain = c->hctr->n_chain;
+    c->n_branch = c->hctr->n_branch;
+    c->n_nodes = c->n_chain + c->n_branch;
+    if ((st = extract_typed<KT>(c)) != BRUNO_OK) return st;
+    if ((st = run_list_rank(c, c->cfg.min_update)) != BRUNO_OK) return st;
+    if ((st = cycles()) != BRUNO_OK) return st;
+    (void)iter;
+  }
+  (void)KWD;
+  /* the cleaned graph, compacted; on-demand outputs are rebuilt from it */
+  c->general_emission = false;
+  c->chain_edges_done = false;
+  c->summaries_done = false;
+  return compress_typed<KT>(c);
+}
+
 }  // namespace
 
 bruno_status run_extract_chains(Ctx *c) { return c->W == 1 ? extract_typed<KW1>(c) : extract_typed<KW2>(c); }
@@ -1365,6 +1950,12 @@ bruno_status run_compress(Ctx *c) { return c->W == 1 ? compress_typed<KW1>(c) : 
 bruno_status run_chain_edges(Ctx *c) { return c->W == 1 ? chain_edges_typed<KW1>(c) : chain_edges_typed<KW2>(c); }
 bruno_status run_chain_summaries(Ctx *c) {
   return c->W == 1 ? chain_summaries_typed<KW1>(c) : chain_summaries_typed<KW2>(c);
+}
+
+bruno_status run_clean(Ctx *c, uint64_t *rounds, uint64_t *deadends, uint64_t *bubbles, uint64_t *edges,
+                       int32_t *status) {
+  return c->W == 1 ? clean_typed<KW1>(c, rounds, deadends, bubbles, edges, status)
+                   : clean_typed<KW2>(c, rounds, deadends, bubbles, edges, status);
 }
 
 }  // namespace bg

@@ -35,6 +35,10 @@ struct DevCounters {
   unsigned long long n_upper;          /* k-mer positions of all reads long enough */
   unsigned long long n_chain_edges;    /* chain-end records appended */
   unsigned long long n_groups, n_hist; /* general emission: representative groups, histogram bins */
+  /* graph cleaning: terminus records, those not on the all-A k-mer, merged summaries, chains
+   * with both ends on branches, erase queries, edges found, dead ends, bubble chains, live
+   * nodes and live branch nodes after an erasure pass */
+  unsigned long long cl_term, cl_nonzero, cl_sum, cl_norm, cl_q, cl_found, cl_dead, cl_bub, cl_live, cl_live_branch;
   unsigned int hll[1 << 12];           /* HyperLogLog registers, p = 12 */
 };
 
@@ -123,6 +127,11 @@ struct Ctx {
   Buf s_kmers, s_dist, s_flags;  /* chain summaries, built on demand */
   uint64_t n_summaries = 0;
   bool summaries_done = false;
+  /* graph cleaning: terminus records and their index per chain node, merged summaries,
+   * chains between two branches, the bubble grouping table, erase queries, edges found */
+  Buf cl_trec, cl_tslot, cl_sums, cl_norm, cl_htab, cl_q, cl_found;
+  bool cleaned = false;
+  uint64_t thr_used[6] = {0, 0, 0, 0, 0, 0};   /* the thresholds local_insert_by_freqencies used */
 
   cudaEvent_t ev[8] = {nullptr};
   cudaEvent_t kev[5] = {nullptr};  /* counting sub-steps */
@@ -151,6 +160,10 @@ bruno_status run_list_rank(Ctx *c, int min_update);
 bruno_status run_compress(Ctx *c);
 bruno_status run_chain_edges(Ctx *c);
 bruno_status run_chain_summaries(Ctx *c);
+/* clean_deadend_and_bubbles_naive on the ranked chain map and the node table; leaves the
+ * cleaned graph compacted (as run_compress does) */
+bruno_status run_clean(Ctx *c, uint64_t *rounds, uint64_t *deadends, uint64_t *bubbles, uint64_t *edges,
+                       int32_t *status);
 bruno_status run_copy_nodes(Ctx *c, uint64_t *keys, uint16_t *counts, uint8_t *flags, size_t cap, size_t *n);
 
 }  // namespace bg

@@ -148,6 +148,29 @@ bruno_status bruno_list_rank(bruno_ctx *ctx, int32_t min_update, uint64_t *itera
  * (:1778-1856). */
 bruno_status bruno_to_compressed_chains(bruno_ctx *ctx);
 
+/* Graph cleaning of the reference driver's _freq_clean build (the _freq build defines
+ * NCLEAN): clean_deadend_and_bubbles_naive (test/common/compact_dbg_clean.hpp:575-890) after
+ * the first compaction (compact_dbg_freq_construct_clean.cpp:633-700).  Cycle nodes and then
+ * edge-less nodes leave the graph; then, until none is found, chains shorter than 2k-1 with
+ * exactly one end on a branch (dead ends, find_deadends, debruijn_topo_operations.hpp:146-175)
+ * and runs of chains between the same two branches with lengths within one (bubbles,
+ * find_bubbles, :285-395) lose their end edges of frequency at most thresh[2] (the thresholds
+ * local_insert_by_freqencies used) on both nodes, edge-less nodes go, and the graph is
+ * compacted again.  Needs ranked chains (the first compaction's outputs are to be copied out
+ * before); leaves the cleaned graph compacted, so that every copy call returns the cleaned
+ * graph.  BRUNO_ERR_INVARIANT with stats->status = 2 when the chain pointers are not mutually
+ * consistent; stats->status = 1 when an iteration erased nothing (the reference would repeat it
+ * forever), 0 otherwise.  stats may be NULL. */
+typedef struct bruno_clean_stats {
+  uint64_t rounds;          /* iterations of the cleaning loop */
+  uint64_t deadends;        /* dead-end chains found, over all iterations */
+  uint64_t bubbles;         /* bubble chains found, over all iterations */
+  uint64_t edges;           /* low-frequency end edges erased (with their reverse edges) */
+  int32_t status;
+  int32_t reserved;
+} bruno_clean_stats;
+bruno_status bruno_clean_deadend_and_bubbles_naive(bruno_ctx *ctx, bruno_clean_stats *stats);
+
 /* The whole plain path in one call: load (host or device bytes), count, filter, extract,
  * rank, compress.  Equivalent to the reference driver's build_index_thresholded ->
  * extract_chains -> list_rank[_min_update] -> to_ranked_chain_nodes sequence

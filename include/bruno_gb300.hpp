@@ -187,6 +187,14 @@ class debruijn_chain_graph {
           "copy_chain_summaries");
     return n;
   }
+  /* clean_deadend_and_bubbles_naive (test/common/compact_dbg_clean.hpp:575-890) on this chain
+   * graph and its de Bruijn graph; afterwards both describe the cleaned graph */
+  bruno_clean_stats clean_deadend_and_bubbles_naive() {
+    bruno_clean_stats s{};
+    check(bruno_clean_deadend_and_bubbles_naive(c_.get(), &s), c_.get(), "clean_deadend_and_bubbles_naive");
+    ranked_ = true;
+    return s;
+  }
 
  private:
   size_t rank(int min_update) {
