@@ -395,3 +395,36 @@ def test_clean_only_erases_edges_in_pairs(fname, lo):
                 if y in after and y in before and before[y][j]:
                     assert after[y][j] == 0, (x, i, y, j)
     assert removed > 0
+
+
+@pytest.mark.parametrize("fname,lo", [("debruijn.palindrome_chr14.fastq", ()), ("debruijn.bubble.fastq", (1,)),
+                                      ("debruijn.clean1.fastq", ()), ("debruijn.clean2.fastq", (1,))])
+def test_clean_shard_invariance(fname, lo):
+    """cleaning gives the same graph for any number of host shards (the reference's rank-count
+    invariance, as its bubble-clean script checks across -np)"""
+    fq = fixture_bytes(fname)
+    kw = dict(k=31, thresholding=bool(lo), thresh=bg.thresholds(lo), clean=True)
+    base = oracle.run(fq, threads=1, **kw)
+    assert base["clean_stats"]["rounds"] > 0
+    for t in (2, 5, 16):
+        r = oracle.run(fq, threads=t, **kw)
+        assert r["clean_stats"] == base["clean_stats"], t
+        assert _digest(r["clean"]) == _digest(base["clean"]), t
+
+
+def test_clean_files_match_arrays(tmp_path):
+    """the --clean file set: first-compaction files without .chain.edges, then the .clean.*
+    files of the cleaned graph, whose chains are the cleaned arrays' chains"""
+    fq = fixture_bytes("debruijn.bubble.fastq")
+    prefix = str(tmp_path / "o")
+    r = oracle.run(fq, k=31, thresh=bg.thresholds([1]), clean=True, write_prefix=prefix)
+    names = sorted(p.name[2:] for p in tmp_path.iterdir())
+    assert names == sorted(["branch.edges", "branch.fasta", "chain.components", "chain.fasta", "chain.summary",
+                            "graph.all", "clean.branch.edges", "clean.branch.fasta", "clean.chain.components",
+                            "clean.chain.fasta", "clean.chain.edges"])
+    with open(prefix + ".clean.chain.fasta") as f:
+        assert sorted(fasta_records(f.read())) == sorted(chain_strings(r["clean"]))
+    with open(prefix + ".chain.fasta") as f:
+        assert sorted(fasta_records(f.read())) == sorted(chain_strings(r))
+    with open(prefix + ".clean.branch.edges") as f:
+        assert len(f.read().splitlines()) == int((r["clean"]["nodes"][2] & 1).sum())
