@@ -50,6 +50,8 @@ def parse_args():
     ap.add_argument("--rates", type=float, nargs="+", default=[10, 50, 100, 200, 500], help="served: requests/s")
     ap.add_argument("--requests", type=int, default=200, help="served: most requests per rate")
     ap.add_argument("--seconds", type=float, default=4.0, help="served: target seconds per rate")
+    ap.add_argument("--h2d-streams", type=int, default=1, help="copy streams for the host FASTQ pieces (1..4)")
+    ap.add_argument("--h2d-chunk", type=int, default=0, help="host FASTQ piece size in bytes (0 = the library's)")
     ap.add_argument("--api", default="build", choices=["build", "steps"],
                     help="build: bruno_build_and_compact (one call); steps: the reference's call sequence "
                          "(load, compute_biedge_freqencies, local_insert_by_freqencies, extract_chains, "
@@ -358,7 +360,8 @@ def main():
     dev.copy_(torch.from_numpy(host.array[:n]), non_blocking=False)
     torch.cuda.synchronize()
 
-    g = bg.Graph(k=w.k, thresh=bg.thresholds(w.lower), min_update=True, device=local)
+    g = bg.Graph(k=w.k, thresh=bg.thresholds(w.lower), min_update=True, device=local,
+                 h2d_streams=args.h2d_streams, h2d_chunk=args.h2d_chunk)
     g.set_stream(stream.cuda_stream)
 
     def step_device():
@@ -468,7 +471,8 @@ def main():
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded generator, " + w.name + ")",
                 "config": dict(workload_config(w), api="bruno_build_and_compact" if args.api == "build"
-                               else "step calls"),
+                               else "step calls", h2d_streams=args.h2d_streams,
+                               h2d_chunk=args.h2d_chunk or 256 << 20),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n, "d2h_bytes_per_step": d2h,
                         "ms_per_step": ems / args.steps,
                         "h2d_ms": statistics.mean(p["h2d"] for p in e2e_phases),

@@ -128,6 +128,11 @@ bruno_status bruno_ctx_create(const bruno_cfg *cfg, bruno_ctx **out) {
   if (st == BRUNO_OK) st = cuda_check(c, cudaEventCreate(&c->h2d_end), "event");
   if (st == BRUNO_OK) st = cuda_check(c, cudaEventCreateWithFlags(&c->order_ev, cudaEventDisableTiming), "event");
   if (st == BRUNO_OK) st = cuda_check(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking), "stream");
+  c->n_copy = std::max(1, std::min(4, (int)c->cfg.h2d_streams));
+  for (int i = 0; i + 1 < c->n_copy && st == BRUNO_OK; ++i) {
+    st = cuda_check(c, cudaStreamCreateWithFlags(&c->copy_more[i], cudaStreamNonBlocking), "stream");
+    if (st == BRUNO_OK) st = cuda_check(c, cudaEventCreateWithFlags(&c->copy_tail[i], cudaEventDisableTiming), "event");
+  }
   if (st != BRUNO_OK) { bruno_ctx_destroy(c); return st; }
   cudaMemsetAsync(c->dctr, 0, sizeof(DevCounters), c->stream);
   *out = c;
@@ -137,6 +142,7 @@ bruno_status bruno_ctx_create(const bruno_cfg *cfg, bruno_ctx **out) {
 bruno_status bruno_ctx_destroy(bruno_ctx *c) {
   if (!c) return BRUNO_ERR_ARG;
   if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+  for (cudaStream_t s : c->copy_more) if (s) cudaStreamSynchronize(s);
   if (c->stream) cudaStreamSynchronize(c->stream);
   Buf *bufs[] = {&c->rstart, &c->rend, &c->tile_cnt, &c->tile_base, &c->table, &c->k2_keys, &c->k2_edges, &c->k2_counts,
                  &c->f_keys, &c->f_edges, &c->f_counts, &c->blk_cnt, &c->blk_base, &c->ckey, &c->cedge,
@@ -154,6 +160,10 @@ bruno_status bruno_ctx_destroy(bruno_ctx *c) {
   if (c->h2d_end) cudaEventDestroy(c->h2d_end);
   if (c->order_ev) cudaEventDestroy(c->order_ev);
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  for (int i = 0; i < 3; ++i) {
+    if (c->copy_more[i]) cudaStreamDestroy(c->copy_more[i]);
+    if (c->copy_tail[i]) cudaEventDestroy(c->copy_tail[i]);
+  }
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return BRUNO_OK;
@@ -192,6 +202,10 @@ bruno_status bruno_reset(bruno_ctx *c) {
   if (c->copy_stream) {
     cudaEventRecord(c->order_ev, c->copy_stream);
     cudaStreamWaitEvent(c->stream, c->order_ev, 0);
+    for (int i = 0; i + 1 < c->n_copy; ++i) {
+      cudaEventRecord(c->order_ev, c->copy_more[i]);
+      cudaStreamWaitEvent(c->stream, c->order_ev, 0);
+    }
   }
   c->n_nodes = c->n_branch = c->n_chain = 0;
   c->iterations = c->n_cycle = c->n_isolated = c->multi = 0;
@@ -234,12 +248,14 @@ bruno_status bruno_load_fastq(bruno_ctx *c, const char *buf, size_t nbytes, int3
        * read index parses a piece while the next one is still in flight */
       cudaEventRecord(c->order_ev, c->stream);
       cudaStreamWaitEvent(c->copy_stream, c->order_ev, 0);
+      for (int i = 0; i + 1 < c->n_copy; ++i) cudaStreamWaitEvent(c->copy_more[i], c->order_ev, 0);
       if (!c->h2d_pending) { cudaEventRecord(c->ev[7], c->copy_stream); c->h2d_pending = true; }
       uint64_t at = 0;   /* where the piece goes in the device copy */
       for (size_t j = 0; j < cuts.size(); ++j) {
         const uint64_t off = cuts[j], len = (j + 1 < cuts.size() ? cuts[j + 1] : nbytes) - off;
-        st = cuda_check(c, cudaMemcpyAsync(dst + at, buf + off, len, cudaMemcpyHostToDevice, c->copy_stream),
-                        "H2D FASTQ");
+        const int sj = (int)(j % (size_t)c->n_copy);   /* pieces go round robin over the copy streams */
+        cudaStream_t cs = sj == 0 ? c->copy_stream : c->copy_more[sj - 1];
+        st = cuda_check(c, cudaMemcpyAsync(dst + at, buf + off, len, cudaMemcpyHostToDevice, cs), "H2D FASTQ");
         if (st != BRUNO_OK) return st;
         if (c->seg_ev_used == c->seg_ev.size()) {
           cudaEvent_t e;
@@ -248,9 +264,13 @@ bruno_status bruno_load_fastq(bruno_ctx *c, const char *buf, size_t nbytes, int3
           c->seg_ev.push_back(e);
         }
         const int ev = (int)c->seg_ev_used++;
-        cudaEventRecord(c->seg_ev[ev], c->copy_stream);
+        cudaEventRecord(c->seg_ev[ev], cs);
         c->segs.push_back({dst + at, len, ev});
         at = (at + len + 15) & ~15ull;
+      }
+      for (int i = 0; i + 1 < c->n_copy; ++i) {   /* h2d_end after the last copy of every stream */
+        cudaEventRecord(c->copy_tail[i], c->copy_more[i]);
+        cudaStreamWaitEvent(c->copy_stream, c->copy_tail[i], 0);
       }
       cudaEventRecord(c->h2d_end, c->copy_stream);
       c->h2d_piped = true;

@@ -64,6 +64,9 @@ struct Ctx {
   bool own_stream = false;
   cudaMemPool_t pool = nullptr;  /* the library's stream-ordered pool on this device */
   cudaStream_t copy_stream = nullptr;   /* host FASTQ pieces are copied here, one event each */
+  cudaStream_t copy_more[3] = {nullptr, nullptr, nullptr};   /* further copy streams (cfg.h2d_streams) */
+  cudaEvent_t copy_tail[3] = {nullptr, nullptr, nullptr};    /* their last copy, joined before h2d_end */
+  int n_copy = 1;
   std::vector<cudaEvent_t> seg_ev;
   cudaEvent_t h2d_end = nullptr;
   cudaEvent_t order_ev = nullptr; /* orders the copy stream after the context's stream */

@@ -74,6 +74,8 @@ typedef struct bruno_cfg {
                                counting path its k-mers extracted) as soon as it lands, while the
                                rest is still copying; inputs under two pieces are copied whole.
                                0 = 256 MiB. */
+  int32_t h2d_streams;      /* copy streams the pieces are spread over, round robin (1..4; 0 = 1) */
+  int32_t reserved0;
 } bruno_cfg;
 
 typedef struct bruno_sizes {
