@@ -284,7 +284,11 @@ class Graph:
         s = _CleanStats()
         st = self.lib.bruno_clean_deadend_and_bubbles_naive(self.ctx, ctypes.byref(s))
         out = {n: int(getattr(s, n)) for n in ("rounds", "deadends", "bubbles", "edges", "status")}
-        self._check(st, "clean_deadend_and_bubbles_naive")
+        try:
+            self._check(st, "clean_deadend_and_bubbles_naive")
+        except BrunoError as e:
+            e.stats = out      # status 2: declined (chain pointers not mutually consistent)
+            raise
         return out
 
     def build_and_compact(self, data, nbytes: Optional[int] = None, is_device: bool = False) -> None:
