@@ -102,3 +102,22 @@ def test_missing_library_fails_loudly(tmp_path):
             bg.load_library(str(tmp_path / "absent.so"))
         finally:
             bg._lib = bg._lib_backup
+
+
+def test_clean_stats_layout_matches_header(tmp_path):
+    src = tmp_path / "layout3.c"
+    src.write_text(f'''
+#include <stdio.h>
+#include <stddef.h>
+#include "{HEADER}"
+int main(void) {{
+  printf("%zu %zu %zu\\n", sizeof(bruno_clean_stats), offsetof(bruno_clean_stats, edges),
+         offsetof(bruno_clean_stats, status));
+  printf("%zu %zu\\n", offsetof(bruno_cfg, h2d_chunk), offsetof(bruno_cfg, h2d_streams));
+  return 0;
+}}''')
+    exe = tmp_path / "layout3"
+    subprocess.run(["gcc", "-std=c99", "-o", str(exe), str(src)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    S, C = bg._CleanStats, bg._Cfg
+    assert got == [ctypes.sizeof(S), S.edges.offset, S.status.offset, C.h2d_chunk.offset, C.h2d_streams.offset]
