@@ -62,14 +62,14 @@ def compare_clean(gpu, ref):
 
 
 def _constructed(case: str) -> bytes:
-    """the oracle tests' constructions: a 10-node tip, a 110-node tip, a one-read SNP bubble"""
+    """the oracle tests' constructions: a 10-node tip, a 100-node tip, a one-read SNP bubble"""
     if case == "tip":
         g = _genome(400, 11)
         bad = list(g[150:250]); bad[90] = _subst(bad[90])
     elif case == "long_tip":
         g = _genome(400, 12)
         bad = list(g[100:250])
-        for p in (40, 70, 100, 130):
+        for p in (50, 80, 110, 140):
             bad[p] = _subst(bad[p])
     else:
         g = _genome(400, 13)

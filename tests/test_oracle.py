@@ -315,25 +315,29 @@ def _subst(c):
     return "ACGT"[("ACGT".index(c) + 1) % 4]
 
 
-def test_clean_severs_short_low_coverage_tip():
+@pytest.mark.parametrize("k", [31, 45])
+def test_clean_severs_short_low_coverage_tip(k):
     """one read with an error 10 bases before its end: a 10-node tip (shorter than 2k-1) off a
     20x genome.  Cleaning severs the tip's edge of frequency 1 (below -L 1's 2): the genome
     becomes one chain again and the tip stays as a chain of its own."""
-    k, g = 31, _genome(400, 11)
+    g = _genome(400, 11)
     bad = list(g[150:250]); bad[90] = _subst(bad[90]); bad = "".join(bad)
     r = oracle.run(_fastq(_tiling(g) + [bad]), k=k, thresh=bg.thresholds([1]), clean=True)
     assert r["clean_stats"] == {"rounds": 1, "deadends": 1, "bubbles": 0, "edges": 1, "status": 0}
-    # before: the genome's chains on either side of the branch k-mer g[209:240], and the tip
-    assert _canon_strings(chain_strings(r)) == _canon_strings([g[:239], g[210:], bad[60:]])
-    assert _canon_strings(chain_strings(r["clean"])) == _canon_strings([g, bad[60:]])
+    # before: the genome's chains on either side of the branch k-mer g[240-k:240], and the tip
+    tip = bad[90 - k + 1:]
+    assert _canon_strings(chain_strings(r)) == _canon_strings([g[:239], g[241 - k:], tip])
+    assert _canon_strings(chain_strings(r["clean"])) == _canon_strings([g, tip])
 
 
-def test_clean_keeps_long_tip():
+@pytest.mark.parametrize("k", [31, 45])
+def test_clean_keeps_long_tip(k):
     """a tip of 2k-1 nodes or more is not a dead end to clean: nothing changes.  Four errors in
-    one 150-base read make every k-mer from the first error's on new: a 110-node tip."""
-    k, g = 31, _genome(400, 12)
+    one 150-base read, the first past the read's first k-mer, make every k-mer from the first
+    error's on new: a 100-node tip off the genome (2k-1 is 61 at k = 31, 89 at k = 45)."""
+    g = _genome(400, 12)
     bad = list(g[100:250])
-    for p in (40, 70, 100, 130):
+    for p in (50, 80, 110, 140):
         bad[p] = _subst(bad[p])
     bad = "".join(bad)
     r = oracle.run(_fastq(_tiling(g) + [bad]), k=k, thresh=bg.thresholds([1]), clean=True)
@@ -342,11 +346,12 @@ def test_clean_keeps_long_tip():
     assert len(chain_strings(r)) == 3
 
 
-def test_clean_severs_low_coverage_bubble_path():
+@pytest.mark.parametrize("k", [31, 45])
+def test_clean_severs_low_coverage_bubble_path(k):
     """one read with a substitution mid-read: a k-node bubble path beside the 20x genome's.  The
     two paths between the same branches have equal lengths and a low-frequency end, so both
     lose their end edges below frequency 2: only the error path's go, the genome re-joins."""
-    k, g = 31, _genome(400, 13)
+    g = _genome(400, 13)
     bad = list(g[150:250]); bad[50] = _subst(bad[50]); bad = "".join(bad)
     r = oracle.run(_fastq(_tiling(g) + [bad]), k=k, thresh=bg.thresholds([1]), clean=True)
     assert r["clean_stats"] == {"rounds": 1, "deadends": 0, "bubbles": 2, "edges": 2, "status": 0}
