@@ -52,6 +52,8 @@ def parse_args():
     ap.add_argument("--seconds", type=float, default=4.0, help="served: target seconds per rate")
     ap.add_argument("--h2d-streams", type=int, default=1, help="copy streams for the host FASTQ pieces (1..4)")
     ap.add_argument("--h2d-chunk", type=int, default=0, help="host FASTQ piece size in bytes (0 = the library's)")
+    ap.add_argument("--rank-fill", type=int, default=0, choices=[0, 1],
+                    help="ranking's final states: 0 = second walk, 1 = one pass over the nodes")
     ap.add_argument("--api", default="build", choices=["build", "steps"],
                     help="build: bruno_build_and_compact (one call); steps: the reference's call sequence "
                          "(load, compute_biedge_freqencies, local_insert_by_freqencies, extract_chains, "
@@ -361,7 +363,7 @@ def main():
     torch.cuda.synchronize()
 
     g = bg.Graph(k=w.k, thresh=bg.thresholds(w.lower), min_update=True, device=local,
-                 h2d_streams=args.h2d_streams, h2d_chunk=args.h2d_chunk)
+                 h2d_streams=args.h2d_streams, h2d_chunk=args.h2d_chunk, rank_fill=args.rank_fill)
     g.set_stream(stream.cuda_stream)
 
     def step_device():
@@ -472,7 +474,7 @@ def main():
                 "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded generator, " + w.name + ")",
                 "config": dict(workload_config(w), api="bruno_build_and_compact" if args.api == "build"
                                else "step calls", h2d_streams=args.h2d_streams,
-                               h2d_chunk=args.h2d_chunk or 256 << 20),
+                               h2d_chunk=args.h2d_chunk or 256 << 20, rank_fill=args.rank_fill),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n, "d2h_bytes_per_step": d2h,
                         "ms_per_step": ems / args.steps,
                         "h2d_ms": statistics.mean(p["h2d"] for p in e2e_phases),

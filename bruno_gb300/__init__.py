@@ -41,7 +41,7 @@ class _Cfg(ctypes.Structure):
         ("min_update", ctypes.c_int32), ("device", ctypes.c_int32), ("table_slots", ctypes.c_uint64),
         ("max_load", ctypes.c_double), ("keep_k2", ctypes.c_int32), ("keep_filtered", ctypes.c_int32),
         ("exact_ranking", ctypes.c_int32), ("direct_count", ctypes.c_int32), ("edge_filter", ctypes.c_int32),
-        ("h2d_chunk", ctypes.c_uint64), ("h2d_streams", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+        ("h2d_chunk", ctypes.c_uint64), ("h2d_streams", ctypes.c_int32), ("rank_fill", ctypes.c_int32),
     ]
 
 
@@ -174,6 +174,7 @@ class GraphConfig:
     edge_filter: bool = False      # the blocked driver's (k+1)-mer filter build (k <= 31)
     h2d_chunk: int = 0             # host FASTQ copied and parsed in pieces of this many bytes (0 = 256 MiB)
     h2d_streams: int = 1           # copy streams the pieces are spread over (1..4)
+    rank_fill: int = 0             # ranking's final states: 0 = second walk, 1 = one pass over the nodes
 
     def to_c(self) -> _Cfg:
         c = _Cfg()
@@ -187,6 +188,7 @@ class GraphConfig:
         c.edge_filter = int(self.edge_filter)
         c.h2d_chunk = int(self.h2d_chunk)
         c.h2d_streams = int(self.h2d_streams)
+        c.rank_fill = int(self.rank_fill)
         return c
 
 

@@ -424,7 +424,7 @@ __device__ __forceinline__ bool answers(const ChainState &t, int facing, uint32_
  * grid is one resident wave, so each thread walks several sides and the geometric walk
  * lengths average out. */
 __global__ void __launch_bounds__(TPB) k_fast_walk(const ChainState *cs, const uint32_t *rnode, uint64_t R, uint64_t M,
-                                                    Jump *E0, DevCounters *ctr) {
+                                                    Jump *E0, uint64_t *place, DevCounters *ctr) {
   unsigned long long bad = 0;
   for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 2 * R; q += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t ord = (uint32_t)(q >> 1), r = rnode[ord];
@@ -444,6 +444,8 @@ __global__ void __launch_bounds__(TPB) k_fast_walk(const ChainState *cs, const u
       if (!answers(st, 1 - dir, cur, f)) { ++bad; break; }
       cur = nxt;
       if ((uint32_t)st.pad != NONE32) { out = Jump{(uint32_t)st.pad, flip, dist}; break; }
+      /* the node's place on the segment, in the slot of the direction this walk crosses it */
+      if (place) place[2ull * nxt + dir] = ((uint64_t)q << 32) | (dist << 1) | flip;
     }
     E0[q] = out;
   }
@@ -532,6 +534,34 @@ __global__ void __launch_bounds__(TPB) k_fast_fill(const ChainState *cs, ChainSt
       else { w.outP = Pb; w.outD = Db; w.inP = Pf; w.inD = Df; }
       cs2[v] = w;
     }
+  }
+}
+
+/* The final states in one pass over the nodes (rank_fill = 1): a node between two rulers has
+ * its place recorded by both walkers of its segment (walker, steps from its ruler, flip so
+ * far), in the slot of the direction each crossed it; either record gives the state k_fast_fill
+ * would write (the two walkers' path ends and distances are the same ones, seen from the two
+ * sides).  Rulers, nodes on ruler cycles and nodes on cycles without a ruler are left as they
+ * are, as k_fast_fill leaves them. */
+__global__ void __launch_bounds__(TPB) k_fast_place(const ChainState *cs, ChainState *cs2, const uint32_t *rnode,
+                                                     uint64_t M, const Jump *E, const uint64_t *place) {
+  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < M; v += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t p0 = place[2 * v], p1 = place[2 * v + 1];
+    if (p0 == ~0ull && p1 == ~0ull) continue;
+    const int dir = p0 != ~0ull ? 0 : 1;
+    const uint64_t p = dir ? p1 : p0;
+    const uint64_t q = p >> 32, j = (p >> 1) & 0x7FFFFFFFull;
+    const uint32_t flip = (uint32_t)(p & 1u);
+    const Jump ef = E[q], eb = E[q ^ 1];
+    if (!(ef.fd & 2u) || !(eb.fd & 2u)) continue;                 /* a ruler cycle */
+    ChainState w;
+    w.pad = cs[v].pad;
+    const uint64_t Pb = (uint64_t)rnode[eb.t] | (((flip ^ (eb.fd & 1u)) != 0) ? PF_FLIP : 0ull);
+    const uint64_t Pf = (uint64_t)rnode[ef.t] | (((flip ^ (ef.fd & 1u)) != 0) ? PF_FLIP : 0ull);
+    const uint32_t Db = (uint32_t)(j + eb.d) | TM, Df = (uint32_t)(ef.d - j) | TM;
+    if (dir) { w.inP = Pb; w.inD = Db; w.outP = Pf; w.outD = Df; }
+    else { w.outP = Pb; w.outD = Db; w.inP = Pf; w.inD = Df; }
+    cs2[v] = w;
   }
 }
 
@@ -1847,7 +1877,18 @@ static bruno_status fast_list_rank(Ctx *c, bool &used) {
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_fast_walk, TPB, 0) == cudaSuccess && o > 0 ? o : 4;
   }();
   const int gw = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * walk_occ, (2 * R + TPB - 1) / TPB));
-  k_fast_walk<<<gw, TPB, 0, c->stream>>>(cs, rnode, R, M, E0, c->dctr);
+  uint64_t *place = nullptr;
+  Buf place_buf;
+  struct FreeOnExit {   /* the places go back to the pool on every way out */
+    Buf &b; cudaStream_t s;
+    ~FreeOnExit() { if (b.p) cudaFreeAsync(b.p, s); }
+  } place_guard{place_buf, c->stream};
+  if (c->cfg.rank_fill == 1) {   /* two 8-byte places per node, all ones = not on a walked segment */
+    if ((st = ensure(c, place_buf, Mb * 16)) != BRUNO_OK) return st;
+    place = (uint64_t *)place_buf.p;
+    cudaMemsetAsync(place, 0xFF, M * 16, c->stream);
+  }
+  k_fast_walk<<<gw, TPB, 0, c->stream>>>(cs, rnode, R, M, E0, place, c->dctr);
   c->launches += 1;
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   if (c->hctr->lr_multi != 0) return BRUNO_OK;                /* a pointer not answered by its target */
@@ -1869,7 +1910,11 @@ static bruno_status fast_list_rank(Ctx *c, bool &used) {
   if ((st = ensure(c, c->cstate2, Mb * sizeof(ChainState))) != BRUNO_OK) return st;
   ChainState *cs2 = (ChainState *)c->cstate2.p;
   cudaMemsetAsync(cs2, 0xFF, M * sizeof(ChainState), c->stream);
-  k_fast_fill<<<gw, TPB, 0, c->stream>>>(cs, cs2, rnode, R, E0, src);
+  if (place) {
+    k_fast_place<<<sms * 8, TPB, 0, c->stream>>>(cs, cs2, rnode, M, src, place);
+  } else {
+    k_fast_fill<<<gw, TPB, 0, c->stream>>>(cs, cs2, rnode, R, E0, src);
+  }
   k_fast_rulers<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 8, (R + TPB - 1) / TPB)), TPB, 0,
                   c->stream>>>(cs, cs2, rnode, R, src);
   cudaMemsetAsync(&c->dctr->n_cycle, 0, 16, c->stream);

@@ -75,7 +75,9 @@ typedef struct bruno_cfg {
                                rest is still copying; inputs under two pieces are copied whole.
                                0 = 256 MiB. */
   int32_t h2d_streams;      /* copy streams the pieces are spread over, round robin (1..4; 0 = 1) */
-  int32_t reserved0;
+  int32_t rank_fill;        /* the O(M) ranking's final states: 0 = a second walk of every segment
+                               between rulers; 1 = the first walk records each node's place on its
+                               segment and one pass over the nodes sets the final states */
 } bruno_cfg;
 
 typedef struct bruno_sizes {
