@@ -49,7 +49,7 @@ def build_library(force: bool = False) -> str:
     """Compiles the CUDA library; returns the path of the shared object."""
     os.makedirs(os.path.join(LIB, "obj"), exist_ok=True)
     out = os.path.join(LIB, "libbruno_gb300.so")
-    headers = [os.path.join(CSRC, h) for h in ("kmer.cuh", "internal.cuh", "piece_cuts.h")] + [os.path.join(INCLUDE, "bruno_gb300.h")]
+    headers = [os.path.join(CSRC, h) for h in ("kmer.cuh", "internal.cuh", "piece_cuts.h", "pool_admission.h")] + [os.path.join(INCLUDE, "bruno_gb300.h")]
     srcs = [os.path.join(CSRC, s) for s in CUDA_SOURCES]
     if not force and _newer(out, srcs + headers):
         return out

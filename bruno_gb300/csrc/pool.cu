@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "../../include/bruno_gb300.h"
+#include "pool_admission.h"
 
 namespace {
 
@@ -71,26 +72,18 @@ struct bruno_pool {
 
 namespace {
 
-uint64_t estimate(size_t n) { return 20ull * n + (64ull << 20); }
+using bruno_pool_rules::estimate;
 
 /* may worker w take request q now?  (called with the lock held) */
 bool admits(const bruno_pool *p, int w, const Request &q) {
-  uint64_t sum = 0;
-  bool others_busy = false;
-  for (size_t i = 0; i < p->held.size(); ++i) {
-    sum += (int)i == w ? std::max(p->held[i], q.est) : p->held[i];
-    if ((int)i != w && p->busy[i]) others_busy = true;
-  }
-  if (q.solo) return !others_busy;
-  return sum <= p->budget || !others_busy;
+  return bruno_pool_rules::admits(p->held, p->busy, p->budget, w, q.est, q.solo);
 }
 
 /* should idle worker w free its buffers so that the queue head fits?  (lock held) */
 bool should_trim(const bruno_pool *p, int w) {
-  if (p->queue.empty() || p->busy[w] || p->held[w] == 0) return false;
-  for (size_t i = 0; i < p->held.size(); ++i)
-    if (!p->busy[i] && admits(p, (int)i, p->queue.front())) return false;   /* someone can take it */
-  return true;
+  if (p->queue.empty()) return false;
+  const Request &q = p->queue.front();
+  return bruno_pool_rules::should_trim(p->held, p->busy, p->budget, w, q.est, q.solo);
 }
 
 void run_one(bruno_ctx *ctx, int words, const Request &q, bruno_pool_result &r) {

@@ -161,3 +161,81 @@ def test_piece_cuts_small_or_unsplittable_inputs(piece_cuts_cli):
     assert piece_cuts_cli(rec * 10, 0) == [0]
     one = b"@r\n" + b"A" * 5000 + b"\n+\n" + b"I" * 5000 + b"\n"
     assert piece_cuts_cli(one, 1024) == [0]                  # one record: nowhere to cut
+
+
+# ----------------------------------------------------------------- pool admission rules
+RULES_HARNESS = r'''
+#include "pool_admission.h"
+#include <cstdio>
+#include <iostream>
+#include <sstream>
+#include <string>
+/* each line: op budget w est solo n held... busy...  ->  prints 0 or 1 (E n -> the estimate) */
+int main() {
+  std::string line;
+  while (std::getline(std::cin, line)) {
+    std::istringstream in(line);
+    std::string op;
+    in >> op;
+    if (op == "E") { unsigned long long n; in >> n; printf("%llu\n", (unsigned long long)bruno_pool_rules::estimate(n)); continue; }
+    unsigned long long budget, est; int w, solo, n;
+    in >> budget >> w >> est >> solo >> n;
+    std::vector<uint64_t> held(n);
+    std::vector<bool> busy(n);
+    for (auto &h : held) { unsigned long long x; in >> x; h = x; }
+    for (int i = 0; i < n; ++i) { int b; in >> b; busy[i] = b != 0; }
+    const bool r = op == "A" ? bruno_pool_rules::admits(held, busy, budget, w, est, solo != 0)
+                             : bruno_pool_rules::should_trim(held, busy, budget, w, est, solo != 0);
+    printf("%d\n", r ? 1 : 0);
+  }
+}
+'''
+
+
+@pytest.fixture(scope="module")
+def pool_rules(tmp_path_factory):
+    import os
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("no host C++ compiler")
+    d = tmp_path_factory.mktemp("rules")
+    src, exe = d / "rules.cpp", d / "rules"
+    src.write_text(RULES_HARNESS)
+    subprocess.run([gxx, "-O1", "-std=c++17", "-I", os.path.join(os.path.dirname(bg.__file__), "csrc"), str(src),
+                    "-o", str(exe)], check=True)
+
+    def run(lines):
+        out = subprocess.run([str(exe)], input="\n".join(lines) + "\n", capture_output=True, text=True, check=True)
+        return [int(x) for x in out.stdout.split()]
+    return run
+
+
+def _q(op, budget, w, est, solo, held, busy):
+    return " ".join(str(x) for x in [op, budget, w, est, int(solo), len(held), *held, *[int(b) for b in busy]])
+
+
+def test_pool_estimate(pool_rules):
+    assert pool_rules(["E 0", "E 1000"]) == [64 << 20, 20_000 + (64 << 20)]
+
+
+def test_pool_admission_rules(pool_rules):
+    cases = [
+        # (expected, query)
+        (1, _q("A", 1000, 0, 500, False, [0, 0], [False, False])),      # fits
+        (1, _q("A", 1000, 0, 2000, False, [0, 0], [False, False])),     # too large, but nothing else runs
+        (0, _q("A", 1000, 1, 500, False, [600, 0], [True, False])),     # 600 + 500 over budget beside a busy one
+        (1, _q("A", 1000, 1, 300, False, [600, 0], [True, False])),     # 600 + 300 fits
+        (1, _q("A", 1000, 1, 500, False, [600, 0], [False, False])),    # over budget, but the other is idle
+        (1, _q("A", 1000, 0, 500, False, [800, 0], [False, False])),    # a worker counts at max(held, est)
+        (0, _q("A", 1000, 0, 100, True, [0, 0], [False, True])),        # solo: waits for the busy one
+        (1, _q("A", 1000, 0, 100, True, [0, 900], [False, False])),     # solo: nothing busy, budget ignored
+        # trimming: only an idle worker holding buffers, only when no free worker can take the head
+        (1, _q("T", 1000, 0, 600, False, [600, 500], [False, True])),
+        (0, _q("T", 1000, 0, 300, False, [600, 0], [False, True])),     # worker 0 can take it
+        (0, _q("T", 1000, 1, 600, False, [600, 500], [False, True])),   # worker 1 is busy
+        (0, _q("T", 1000, 0, 600, False, [0, 500], [False, True])),     # holds nothing
+        (1, _q("T", 1000, 0, 600, False, [400, 700, 0], [False, True, False])),
+    ]
+    assert pool_rules([q for _, q in cases]) == [e for e, _ in cases]
