@@ -239,3 +239,47 @@ def test_pool_admission_rules(pool_rules):
         (1, _q("T", 1000, 0, 600, False, [400, 700, 0], [False, True, False])),
     ]
     assert pool_rules([q for _, q in cases]) == [e for e, _ in cases]
+
+
+# ---------------------------------------------------- the C++ facade's -L/-U mapping
+THRESH_HARNESS = r'''
+#include "bruno_gb300.hpp"
+#include <cstdio>
+#include <iostream>
+#include <sstream>
+#include <string>
+/* each line: nlo lo... nhi hi...  ->  the six thresholds */
+int main() {
+  std::string line;
+  while (std::getline(std::cin, line)) {
+    std::istringstream in(line);
+    size_t n;
+    std::vector<uint64_t> lo, hi;
+    in >> n; lo.resize(n); for (auto &x : lo) in >> x;
+    in >> n; hi.resize(n); for (auto &x : hi) in >> x;
+    for (uint64_t t : bruno_gb300::thresholds(lo, hi)) printf("%llu ", (unsigned long long)t);
+    printf("\n");
+  }
+}
+'''
+
+
+def test_cpp_thresholds_match_python(tmp_path):
+    """the driver's -L/-U handling in the C++ facade equals bruno_gb300.thresholds (and so the
+    reference driver's, compact_dbg_freq_construct_clean.cpp:937-961)"""
+    import os
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("no host C++ compiler")
+    src, exe = tmp_path / "t.cpp", tmp_path / "t"
+    src.write_text(THRESH_HARNESS)
+    inc = os.path.join(os.path.dirname(os.path.dirname(bg.__file__)), "include")
+    subprocess.run([gxx, "-O1", "-std=c++17", "-I", inc, str(src), "-o", str(exe)], check=True)
+    cases = [((), ()), ((2,), ()), ((3,), (50,)), ((1, 2, 3), ()), ((1, 2, 3), (10, 20, 30)), ((70000,), ()),
+             ((), (5,)), ((0,), (65536,))]
+    lines = [" ".join(str(x) for x in [len(lo), *lo, len(hi), *hi]) for lo, hi in cases]
+    out = subprocess.run([str(exe)], input="\n".join(lines) + "\n", capture_output=True, text=True, check=True)
+    got = [[int(x) for x in l.split()] for l in out.stdout.splitlines()]
+    assert got == [bg.thresholds(lo, hi) for lo, hi in cases]
