@@ -67,6 +67,13 @@ class _CleanStats(ctypes.Structure):
                 ("edges", ctypes.c_uint64), ("status", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
+class _DeviceView(ctypes.Structure):
+    _fields_ = [("ranked_K", ctypes.c_void_p), ("ranked_rep", ctypes.c_void_p), ("ranked_dist", ctypes.c_void_p),
+                ("chain_reps", ctypes.c_void_p), ("chain_offsets", ctypes.c_void_p), ("chain_chars", ctypes.c_void_p),
+                ("n_ranked", ctypes.c_uint64), ("n_chains", ctypes.c_uint64), ("n_chain_chars", ctypes.c_uint64),
+                ("words", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 _lib: Optional[ctypes.CDLL] = None
 
 # every entry point of include/bruno_gb300.h
@@ -78,6 +85,7 @@ EXPORTS = (
     "bruno_copy_chains", "bruno_copy_chain_edges", "bruno_copy_chain_summaries", "bruno_host_alloc", "bruno_host_free", "bruno_phase_ms",
     "bruno_count_biedges_noalloc", "bruno_pool_create", "bruno_pool_submit", "bruno_pool_wait",
     "bruno_pool_result_free", "bruno_pool_destroy", "bruno_clean_deadend_and_bubbles_naive",
+    "bruno_device_results",
 )
 
 
@@ -111,6 +119,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "bruno_pool_wait": [P, U64, ctypes.POINTER(_PoolResult)], "bruno_pool_result_free": [ctypes.POINTER(_PoolResult)],
         "bruno_pool_destroy": [P],
         "bruno_clean_deadend_and_bubbles_naive": [P, ctypes.POINTER(_CleanStats)],
+        "bruno_device_results": [P, ctypes.POINTER(_DeviceView)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -279,6 +288,13 @@ class Graph:
 
     def to_compressed_chains(self) -> None:
         self._check(self.lib.bruno_to_compressed_chains(self.ctx), "to_compressed_chains")
+
+    def device_results(self) -> dict:
+        """device addresses (ints) and sizes of the listranked nodes and compacted chains, read-only,
+        valid until the context is rebuilt or changed"""
+        v = _DeviceView()
+        self._check(self.lib.bruno_device_results(self.ctx, ctypes.byref(v)), "device_results")
+        return {n: (int(getattr(v, n) or 0)) for n, _ in _DeviceView._fields_ if n != "reserved"}
 
     def clean_deadend_and_bubbles_naive(self) -> dict:
         """The _freq_clean driver's graph cleaning (compact_dbg_clean.hpp:575-890) on the ranked

@@ -490,6 +490,25 @@ bruno_status bruno_copy_chains(bruno_ctx *c, uint64_t *reps, uint64_t *offsets, 
   return st;
 }
 
+bruno_status bruno_device_results(bruno_ctx *c, bruno_device_view *o) {
+  if (!c || !o) return BRUNO_ERR_ARG;
+  if (c->stage < 6) return set_err(c, BRUNO_ERR_ARG, "results exist after to_compressed_chains");
+  bruno_status st = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  if (st != BRUNO_OK) return st;
+  std::memset(o, 0, sizeof(*o));
+  o->ranked_K = (const uint64_t *)c->r_K.p;
+  o->ranked_rep = (const uint64_t *)c->r_rep.p;
+  o->ranked_dist = (const int32_t *)c->r_dist.p;
+  o->chain_reps = (const uint64_t *)c->ch_rep.p;
+  o->chain_offsets = (const uint64_t *)c->head_off.p;
+  o->chain_chars = (const char *)c->ch_chars.p;
+  o->n_ranked = c->n_ranked;
+  o->n_chains = c->n_heads;
+  o->n_chain_chars = c->n_chain_chars;
+  o->words = c->W;
+  return BRUNO_OK;
+}
+
 bruno_status bruno_copy_chain_edges(bruno_ctx *c, uint64_t *ends, uint16_t *freqs, size_t cap, size_t *n) {
   if (!c) return BRUNO_ERR_ARG;
   if (c->stage < 6) return set_err(c, BRUNO_ERR_ARG, "chain edges exist after to_compressed_chains");

@@ -212,6 +212,24 @@ bruno_status bruno_copy_chains(bruno_ctx *ctx, uint64_t *reps, uint64_t *offsets
  * truncated), min and max of the self frequencies of the chain's nodes.  Records come in no
  * particular order (the reference sorts them by L before printing).  Computed on the device at
  * the first call after bruno_to_compressed_chains, which may pass NULL buffers to query n. */
+/* Device addresses of the results, for a consumer on the same device that reads them in place
+ * (zero copy): the listranked nodes as bruno_copy_ranked gives them and the compacted chains as
+ * bruno_copy_chains gives them.  Read-only; valid until the next call that rebuilds or changes
+ * the context (bruno_reset, a load, a build, the cleaning, bruno_ctx_destroy).  Read them on the
+ * context's stream or after it has been synchronised (this call synchronises it). */
+typedef struct bruno_device_view {
+  const uint64_t *ranked_K;       /* n_ranked k-mers (words each) */
+  const uint64_t *ranked_rep;     /* n_ranked representatives (words each) */
+  const int32_t *ranked_dist;     /* n_ranked distances */
+  const uint64_t *chain_reps;     /* n_chains representatives (words each) */
+  const uint64_t *chain_offsets;  /* n_chains + 1 offsets into chain_chars */
+  const char *chain_chars;        /* n_chain_chars bases */
+  uint64_t n_ranked, n_chains, n_chain_chars;
+  int32_t words;
+  int32_t reserved;
+} bruno_device_view;
+bruno_status bruno_device_results(bruno_ctx *ctx, bruno_device_view *out);
+
 bruno_status bruno_copy_chain_edges(bruno_ctx *ctx, uint64_t *ends, uint16_t *freqs, size_t cap, size_t *n);
 /* Chain summaries: debruijn_chain_graph::to_summarized_chains()
  * (src/debruijn/debruijn_chain_graph.hpp:1876-2005), the records print_chain_summaries

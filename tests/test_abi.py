@@ -121,3 +121,22 @@ int main(void) {{
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
     S, C = bg._CleanStats, bg._Cfg
     assert got == [ctypes.sizeof(S), S.edges.offset, S.status.offset, C.h2d_chunk.offset, C.h2d_streams.offset]
+
+
+def test_device_view_layout_matches_header(tmp_path):
+    src = tmp_path / "layout4.c"
+    src.write_text(f'''
+#include <stdio.h>
+#include <stddef.h>
+#include "{HEADER}"
+int main(void) {{
+  printf("%zu %zu %zu %zu\\n", sizeof(bruno_device_view), offsetof(bruno_device_view, chain_chars),
+         offsetof(bruno_device_view, n_ranked), offsetof(bruno_device_view, words));
+  printf("%zu\\n", offsetof(bruno_cfg, rank_fill));
+  return 0;
+}}''')
+    exe = tmp_path / "layout4"
+    subprocess.run(["gcc", "-std=c99", "-o", str(exe), str(src)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    V, C = bg._DeviceView, bg._Cfg
+    assert got == [ctypes.sizeof(V), V.chain_chars.offset, V.n_ranked.offset, V.words.offset, C.rank_fill.offset]

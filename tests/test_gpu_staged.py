@@ -33,3 +33,35 @@ def test_rank_fill_workload_parity(k):
     thr = bg.thresholds(w.lower)
     ref = oracle.run(fq, k=k, thresh=thr, min_update=True, threads=16, keep_k2=True, keep_filtered=True)
     compare(gpu_run(fq, k, True, thr, True, rank_fill=1), ref)
+
+
+class _DevArray:
+    """a read-only device array for torch.as_tensor (the CUDA array interface)"""
+
+    def __init__(self, ptr, n, typestr):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, True), "version": 2}
+
+
+def test_device_results_zero_copy():
+    """bruno_device_results: the device arrays read in place equal what the copy calls return"""
+    torch = pytest.importorskip("torch")
+    data = fixture_bytes("debruijn.palindrome_chr14.fastq")
+    g = bg.Graph(k=31, thresh=bg.thresholds([2]))
+    try:
+        g.build_and_compact(data)
+        v = g.device_results()
+        K, rep, dist = g.ranked()
+        reps, offs, chars = g.chains()
+        w = v["words"]
+        assert v["n_ranked"] == len(dist) and v["n_chains"] == len(reps) and v["n_chain_chars"] == len(chars)
+
+        def read(ptr, n, typestr):
+            return torch.as_tensor(_DevArray(ptr, n, typestr), device="cuda").cpu().numpy()
+        assert (read(v["ranked_K"], v["n_ranked"] * w, "<u8").reshape(-1, w) == K).all()
+        assert (read(v["ranked_rep"], v["n_ranked"] * w, "<u8").reshape(-1, w) == rep).all()
+        assert (read(v["ranked_dist"], v["n_ranked"], "<i4") == dist).all()
+        assert (read(v["chain_reps"], v["n_chains"] * w, "<u8").reshape(-1, w) == reps).all()
+        assert (read(v["chain_offsets"], v["n_chains"] + 1, "<u8") == offs).all()
+        assert read(v["chain_chars"], v["n_chain_chars"], "|u1").tobytes() == bytes(chars)
+    finally:
+        g.close()
