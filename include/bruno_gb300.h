@@ -40,7 +40,7 @@ typedef enum bruno_status {
   BRUNO_ERR_TABLE_FULL = 4,       /* hash table probe limit hit even after regrowth */
   BRUNO_ERR_RANK_NOT_CONVERGED = 5,/* not returned: the round-synchronous ranking stops at the
                                      reference's 30-round cap without an error, as the reference
-                                     does (debruijn_chain_graph.hpp list_rank*); sizes.iterations
+                                     does (debruijn_chain_graph.hpp:923-926, 1249-1252); sizes.iterations
                                      = 30 shows it */
   BRUNO_ERR_INVARIANT = 6,        /* an internal invariant failed (reported, never trapped) */
   BRUNO_ERR_CUDA = 7,             /* a CUDA runtime call failed */
