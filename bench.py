@@ -52,6 +52,9 @@ def parse_args():
     ap.add_argument("--seconds", type=float, default=4.0, help="served: target seconds per rate")
     ap.add_argument("--h2d-streams", type=int, default=1, help="copy streams for the host FASTQ pieces (1..4)")
     ap.add_argument("--h2d-chunk", type=int, default=0, help="host FASTQ piece size in bytes (0 = the library's)")
+    ap.add_argument("--e2e-workers", type=int, default=0,
+                    help="e2e through a pool of this many contexts (bruno_pool_*), so that one step's host "
+                         "copy overlaps the previous step's device work; 0 = one context, steps in turn")
     ap.add_argument("--rank-fill", type=int, default=0, choices=[0, 1],
                     help="ranking's final states: 0 = second walk, 1 = one pass over the nodes")
     ap.add_argument("--api", default="build", choices=["build", "steps"],
@@ -415,17 +418,36 @@ def main():
         g._check(g.lib.bruno_copy_chains(g.ctx, ctypes.c_void_p(out_reps.ptr), ctypes.c_void_p(out_offs.ptr),
                                          ctypes.c_void_p(out_chars.ptr), nc, max(1, nch), ctypes.byref(ncs),
                                          ctypes.byref(nchs)), "copy_chains")
-    step_e2e()
-    barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e2e_phases = []
-    e0.record(stream)
-    for _ in range(args.steps):
+    if args.e2e_workers > 0:
+        # steps streamed through a pool of contexts: each step still copies its FASTQ in and its
+        # chains out, but one step's copy runs under the previous step's device work; host clock
+        # between device synchronisations (the pool's workers run on streams of their own)
+        pool = bg.Pool(workers=args.e2e_workers, k=w.k, thresh=bg.thresholds(w.lower), min_update=True,
+                       device=local, h2d_streams=args.h2d_streams, h2d_chunk=args.h2d_chunk,
+                       rank_fill=args.rank_fill)
+        for t in [pool.submit(host.array[:n]) for _ in range(args.e2e_workers)]:
+            assert pool.wait(t)["status"] == 0
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        tickets = [pool.submit(host.array[:n]) for _ in range(args.steps)]
+        res = [pool.wait(t) for t in tickets]
+        torch.cuda.synchronize()
+        ems = max_over_ranks((time.perf_counter() - t0) * 1e3, world)
+        pool.close()
+        assert all(r["status"] == 0 and r["sizes"]["n_instances"] == inst_step for r in res)
+    else:
         step_e2e()
-        e2e_phases.append(g.phase_ms())
-    e1.record(stream)
-    barrier()
-    ems = max_over_ranks(e0.elapsed_time(e1), world)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step_e2e()
+            e2e_phases.append(g.phase_ms())
+        e1.record(stream)
+        barrier()
+        ems = max_over_ranks(e0.elapsed_time(e1), world)
     e2e_value = inst_step * args.steps * world / (ems / 1e3)
     d2h = nch + 8 * (nc + 1) + 8 * g.words * nc
 
@@ -477,10 +499,11 @@ def main():
                                h2d_chunk=args.h2d_chunk or 256 << 20, rank_fill=args.rank_fill),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n, "d2h_bytes_per_step": d2h,
                         "ms_per_step": ems / args.steps,
-                        "h2d_ms": statistics.mean(p["h2d"] for p in e2e_phases),
+                        "h2d_ms": statistics.mean(p["h2d"] for p in e2e_phases) if e2e_phases else None,
                         "device_ms": statistics.mean(sum(p[k] for k in ("parse", "count_k2mers", "filter_insert",
                                                                         "chainmap", "list_rank", "compress"))
-                                                     for p in e2e_phases)},
+                                                     for p in e2e_phases) if e2e_phases else None,
+                        "contexts": max(1, args.e2e_workers)},
                 "roofline": {"bound": "hbm", "kernel": top, "achieved": kernels[top]["achieved"], "peak": peak,
                              "unit": "GB/s", "frac": kernels[top]["frac"], "peak_source": peak_src,
                              "traffic": traffic, "alg_bytes_per_launch": kernels[top]["alg_bytes_per_launch"],
