@@ -433,3 +433,35 @@ def test_clean_files_match_arrays(tmp_path):
         assert sorted(fasta_records(f.read())) == sorted(chain_strings(r))
     with open(prefix + ".clean.branch.edges") as f:
         assert len(f.read().splitlines()) == int((r["clean"]["nodes"][2] & 1).sum())
+
+
+@pytest.mark.parametrize("fname,lo", [("debruijn.bubble.fastq", (1,)), ("debruijn.palindrome_chr14.fastq", ()),
+                                      ("debruijn.clean1.fastq", ()), ("debruijn.clean2.fastq", (1,))])
+def test_cleaned_chains_are_a_compaction_of_the_cleaned_graph(fname, lo):
+    """check_compacted_files.sh's idea on the cleaned outputs: every k-mer of every cleaned chain
+    is a chain node of the cleaned node table, consecutive k-mers are joined by an edge that both
+    nodes hold, and every chain node of the table lies on exactly one chain (cycles created by the
+    cleaning leave the graph, as compact_dbg_clean.hpp:797-806 takes them out)"""
+    k = 31
+    r = oracle.run(fixture_bytes(fname), k=k, thresholding=bool(lo), thresh=bg.thresholds(lo), clean=True)
+    c = r["clean"]
+    nodes = _node_map(c["nodes"], k)
+    flags = {_ascii(c["nodes"][0][i], k): int(c["nodes"][2][i]) for i in range(len(c["nodes"][2]))}
+    canon = lambda x: min(x, _rc(x))
+    seen = set()
+    for s in chain_strings(c):
+        kmers = [s[i:i + k] for i in range(len(s) - k + 1)]
+        for x in kmers:
+            assert canon(x) in nodes and flags[canon(x)] & 2, x
+            assert canon(x) not in seen, x
+            seen.add(canon(x))
+        for a, b in zip(kmers, kmers[1:]):
+            # a -> b: a's out-edge to b's last base, b's in-edge from a's first base, each on its
+            # stored strand
+            ca, cb = canon(a), canon(b)
+            out_i = "ACGT".index(b[-1]) if ca == a else 4 + 3 - "ACGT".index(b[-1])
+            in_i = 4 + "ACGT".index(a[0]) if cb == b else 3 - "ACGT".index(a[0])
+            assert nodes[ca][out_i] > 0 and nodes[cb][in_i] > 0, (a, b)
+    # the loop takes the cycle nodes of each recompaction out of the graph, and edge-less nodes
+    # go too, so every chain node left is on exactly one chain
+    assert seen == {x for x, f in flags.items() if f & 2}
