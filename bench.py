@@ -165,7 +165,8 @@ def cpu_baseline(w, frac, threads):
     dt = time.perf_counter() - t0
     return {"value": r["n_instances"] / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"first {ws.n_reads} of {w.n_reads} reads ({frac * 100:g}%), {r['n_instances']} k-mers, "
-                      f"{dt:.2f} s", "seconds": dt, "instances": r["n_instances"]}
+                      f"{dt:.2f} s", "seconds": dt, "instances": r["n_instances"],
+            "phases_s": {p: round(t, 4) for p, t in r["seconds"].items()}}
 
 
 def run_reference(args, w):
@@ -186,7 +187,8 @@ def run_reference(args, w):
             "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(secs), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded generator)",
             "config": workload_config(w), "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": b["sample"]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": b["sample"],
+                             "phases_s": b["phases_s"]},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -516,7 +518,7 @@ def main():
                                                 "table_partitions")}}
         if not args.no_cpu_baseline:
             b = cpu_baseline(w, args.cpu_sample, os.cpu_count() or 1)
-            line["cpu_baseline"] = {k: b[k] for k in ("value", "unit", "cores", "kind", "sample")}
+            line["cpu_baseline"] = {k: b[k] for k in ("value", "unit", "cores", "kind", "sample", "phases_s")}
         print(json.dumps(line), flush=True)
     g.close()
     host.free()
