@@ -1,6 +1,7 @@
 """GPU parity of code paths that have not yet run on a GPU: the ranking's one-pass final states
-(cfg.rank_fill = 1).  Staged like tests/test_gpu_clean.py: marker `gpu_staged`, selected only by
-`-m gpu_staged`, skipped without a GPU; moved to `gpu` once it has passed on a GB300."""
+(cfg.rank_fill = 1), the zero-copy result view, and host pieces over several copy streams.
+Staged like tests/test_gpu_clean.py: marker `gpu_staged`, selected only by `-m gpu_staged`,
+skipped without a GPU; moved to `gpu` once it has passed on a GB300."""
 import pytest
 
 import bruno_gb300 as bg
@@ -65,3 +66,19 @@ def test_device_results_zero_copy():
         assert read(v["chain_chars"], v["n_chain_chars"], "|u1").tobytes() == bytes(chars)
     finally:
         g.close()
+
+
+@pytest.mark.parametrize("streams", [2, 3, 4])
+def test_host_pieces_over_copy_streams(streams):
+    """host FASTQ pieces spread round robin over several copy streams (cfg.h2d_streams), each
+    piece waited on by its own event, with extraction under the later copies: equal to the oracle"""
+    from test_gpu_parity import at_quality
+    w = synth.WORKLOADS["plain-small"]
+    fq = at_quality(synth.make_fastq(w))
+    thr = bg.thresholds(w.lower)
+    ref = oracle.run(fq, k=31, thresh=thr, min_update=True, threads=16, keep_k2=True, keep_filtered=True)
+    compare(gpu_run(fq, 31, True, thr, True, h2d_chunk=1 << 16, h2d_streams=streams), ref)
+    data = at_quality(fixture_bytes("natural.withN.fastq"))
+    thr2 = bg.thresholds([2])
+    ref2 = oracle.run(data, k=45, thresh=thr2, min_update=True, keep_k2=True, keep_filtered=True)
+    compare(gpu_run(data, 45, True, thr2, True, h2d_chunk=1024, h2d_streams=streams), ref2)
