@@ -145,3 +145,18 @@ def test_clean_driver_outputs_identical(tmp_path, fname, flags):
         b = open(tmp_path / ("ref" + ext), "rb").read()
         assert a == b, f"{fname} {' '.join(flags)}: {ext} differs"
     assert not os.path.exists(tmp_path / "gpu.chain.edges")
+
+
+@pytest.mark.parametrize("case", ["empty", "one_read", "circle"])
+def test_clean_edge_cases(case):
+    g = _genome(200, 21)
+    if case == "empty":
+        fq = b""
+    elif case == "one_read":
+        fq = _fastq([g[:150]])
+    else:
+        circ = g + g[:60]
+        fq = _fastq([circ[i:i + 100] for i in range(0, len(g), 5)])
+    thr = bg.thresholds([1])
+    ref = oracle.run(fq, k=31, thresh=thr, clean=True)
+    compare_clean(gpu_clean(fq, 31, True, thr), ref)

@@ -465,3 +465,21 @@ def test_cleaned_chains_are_a_compaction_of_the_cleaned_graph(fname, lo):
     # the loop takes the cycle nodes of each recompaction out of the graph, and edge-less nodes
     # go too, so every chain node left is on exactly one chain
     assert seen == {x for x, f in flags.items() if f & 2}
+
+
+def test_clean_edge_cases():
+    """no input; one read (a chain whose both ends lack edges is no dead end); a circular genome
+    (one cycle, which the driver takes out before cleaning, leaving nothing to clean)"""
+    thr = bg.thresholds([1])
+    r = oracle.run(b"", k=31, thresh=thr, clean=True)
+    assert r["clean_stats"] == {"rounds": 0, "deadends": 0, "bubbles": 0, "edges": 0, "status": 0}
+    assert r["clean"]["n_nodes"] == 0 and r["clean"]["n_chains"] == 0
+    g = _genome(200, 21)
+    r = oracle.run(_fastq([g[:150]]), k=31, thresh=thr, clean=True)
+    assert r["clean_stats"]["rounds"] == 0
+    assert chain_strings(r["clean"]) == chain_strings(r) and len(chain_strings(r)) == 1
+    circ = g + g[:60]   # reads around a circle: every k-mer has one successor and one predecessor
+    reads = [circ[i:i + 100] for i in range(0, len(g), 5)]
+    r = oracle.run(_fastq(reads), k=31, thresh=thr, clean=True)
+    assert r["n_cycle_nodes"] == len(g) and r["n_chains"] == 0
+    assert r["clean_stats"]["rounds"] == 0 and r["clean"]["n_nodes"] == 0
