@@ -483,3 +483,31 @@ def test_clean_edge_cases():
     r = oracle.run(_fastq(reads), k=31, thresh=thr, clean=True)
     assert r["n_cycle_nodes"] == len(g) and r["n_chains"] == 0
     assert r["clean_stats"]["rounds"] == 0 and r["clean"]["n_nodes"] == 0
+
+
+@pytest.mark.parametrize("fname,lo", [("debruijn.bubble.fastq", (1,)), ("debruijn.palindrome_chr14.fastq", ()),
+                                      ("debruijn.clean2.fastq", (1,))])
+def test_cleaned_chain_edges_follow_chain_strings(tmp_path, fname, lo):
+    """the same second derivation of .chain.edges, on the cleaned graph's .clean.chain.edges"""
+    k = 31
+    r = oracle.run(fixture_bytes(fname), k=k, thresholding=bool(lo), thresh=bg.thresholds(lo), clean=True,
+                   write_prefix=str(tmp_path / "p"))
+    c = r["clean"]
+    assert r["clean_stats"]["rounds"] > 0
+    keys, counts, _ = c["nodes"]
+    node = {_ascii(keys[i], k): counts[i] for i in range(len(keys))}
+    K, rep, _ = c["ranked"]
+    selfs = {}
+    for i in range(len(K)):
+        selfs.setdefault(_ascii(rep[i], k), []).append(int(node[min(_ascii(K[i], k), _rc(_ascii(K[i], k)))][8]))
+    lines = []
+    for s in chain_strings(c):
+        L, R = s[:k], s[-k:]
+        cl, cr = node[min(L, _rc(L))], node[min(R, _rc(R))]
+        lin = list(cl[4:8]) if L <= _rc(L) else [cl[3], cl[2], cl[1], cl[0]]
+        rout = list(cr[0:4]) if R <= _rc(R) else [cr[7], cr[6], cr[5], cr[4]]
+        f = selfs[L]
+        mean = int(np.float32(sum(f)) / np.float32(len(f)))
+        lines.append(f"{L}\t{R}\t" + "".join(f"{int(v)}\t" for v in lin + rout + [mean, min(f), max(f)]) + "\n")
+    assert open(tmp_path / "p.clean.chain.edges").read() == "".join(sorted(lines))
+    assert len(lines) == c["n_chains"] > 0
