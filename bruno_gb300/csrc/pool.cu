@@ -19,7 +19,8 @@
  * budget -- or when no other worker is busy, so that a request larger than the budget still
  * runs alone.  The estimate is 20 bytes of device memory per FASTQ byte plus 64 MiB.  When the
  * request at the head of the queue fits nowhere, idle workers free their buffers; a request
- * that still runs out of device memory is queued again, once, to run with no other build busy.
+ * that still runs out of device memory is queued again, once, to run with no other build busy,
+ * and no other request starts until it has finished.
  */
 #include <cuda_runtime.h>
 
@@ -30,6 +31,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <set>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -66,6 +68,8 @@ struct bruno_pool {
   std::vector<std::thread> threads;
   std::vector<uint64_t> held;    /* per worker: largest estimate run so far */
   std::vector<bool> busy;
+  bool solo_running = false;     /* a retried request is running and must stay alone */
+  std::set<uint64_t> collected;  /* tickets whose results were already handed out */
   uint64_t next_ticket = 1;
   bool stop = false;
 };
@@ -76,14 +80,14 @@ using bruno_pool_rules::estimate;
 
 /* may worker w take request q now?  (called with the lock held) */
 bool admits(const bruno_pool *p, int w, const Request &q) {
-  return bruno_pool_rules::admits(p->held, p->busy, p->budget, w, q.est, q.solo);
+  return bruno_pool_rules::admits(p->held, p->busy, p->budget, w, q.est, q.solo, p->solo_running);
 }
 
 /* should idle worker w free its buffers so that the queue head fits?  (lock held) */
 bool should_trim(const bruno_pool *p, int w) {
   if (p->queue.empty()) return false;
   const Request &q = p->queue.front();
-  return bruno_pool_rules::should_trim(p->held, p->busy, p->budget, w, q.est, q.solo);
+  return bruno_pool_rules::should_trim(p->held, p->busy, p->budget, w, q.est, q.solo, p->solo_running);
 }
 
 void run_one(bruno_ctx *ctx, int words, const Request &q, bruno_pool_result &r) {
@@ -127,6 +131,7 @@ void worker_main(bruno_pool *p, int w) {
       p->queue.pop_front();
       p->busy[w] = true;
       p->held[w] = std::max(p->held[w], q.est);
+      if (q.solo) p->solo_running = true;
     }
     const clk::time_point t0 = clk::now();
     Done d;
@@ -143,7 +148,7 @@ void worker_main(bruno_pool *p, int w) {
         std::lock_guard<std::mutex> lk(p->mu);
         p->busy[w] = false;
         p->held[w] = 0;
-        q.solo = true;
+        q.solo = true;   /* solo_running is still false: this request was not solo */
         p->queue.push_front(q);
       }
       p->cv_work.notify_all();
@@ -156,6 +161,7 @@ void worker_main(bruno_pool *p, int w) {
     {
       std::lock_guard<std::mutex> lk(p->mu);
       p->busy[w] = false;
+      if (q.solo) p->solo_running = false;
       if (trim) p->held[w] = 0;
       p->done[q.ticket] = d;
     }
@@ -199,7 +205,8 @@ extern "C" bruno_status bruno_pool_submit(bruno_pool *p, const char *buf, size_t
 extern "C" bruno_status bruno_pool_wait(bruno_pool *p, uint64_t ticket, bruno_pool_result *out) {
   if (!p || !out) return BRUNO_ERR_ARG;
   std::unique_lock<std::mutex> lk(p->mu);
-  if (ticket == 0 || ticket >= p->next_ticket) return BRUNO_ERR_ARG;
+  if (ticket == 0 || ticket >= p->next_ticket || p->collected.count(ticket)) return BRUNO_ERR_ARG;
+  p->collected.insert(ticket);   /* a second wait on this ticket is an error, not a hang */
   p->cv_done.wait(lk, [&] { return p->done.count(ticket) != 0; });
   *out = p->done[ticket].r;
   p->done.erase(ticket);

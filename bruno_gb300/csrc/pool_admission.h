@@ -7,7 +7,8 @@
  * to free worker w while the sum over workers -- w counted at the larger of what it holds and
  * the request's estimate -- stays within the budget, or when no other worker is busy (a request
  * larger than the budget then runs alone).  A request that ran out of memory beside others once
- * (`solo`) waits until no other worker is busy.
+ * (`solo`) waits until no other worker is busy, and while it runs (`solo_running`) no other
+ * request is admitted, so that it really runs alone.
  */
 #ifndef BRUNO_POOL_ADMISSION_H_
 #define BRUNO_POOL_ADMISSION_H_
@@ -24,7 +25,8 @@ inline uint64_t estimate(size_t n) { return 20ull * n + (64ull << 20); }
 
 /* may worker w take a request of estimate `est` now? */
 inline bool admits(const std::vector<uint64_t> &held, const std::vector<bool> &busy, uint64_t budget, int w,
-                   uint64_t est, bool solo) {
+                   uint64_t est, bool solo, bool solo_running = false) {
+  if (solo_running) return false;
   uint64_t sum = 0;
   bool others_busy = false;
   for (size_t i = 0; i < held.size(); ++i) {
@@ -38,8 +40,8 @@ inline bool admits(const std::vector<uint64_t> &held, const std::vector<bool> &b
 /* should idle worker w free its buffers so that the queue head (estimate est) fits?  Only
  * when no free worker could take it as things stand. */
 inline bool should_trim(const std::vector<uint64_t> &held, const std::vector<bool> &busy, uint64_t budget, int w,
-                        uint64_t est, bool solo) {
-  if (busy[w] || held[w] == 0) return false;
+                        uint64_t est, bool solo, bool solo_running = false) {
+  if (solo_running || busy[w] || held[w] == 0) return false;
   for (size_t i = 0; i < held.size(); ++i)
     if (!busy[i] && admits(held, busy, budget, (int)i, est, solo)) return false;
   return true;

@@ -302,10 +302,14 @@ bruno_status bruno_pool_destroy(bruno_pool *pool);
  * latency-sensitive loop that must not stop for an allocator.  Every other entry point
  * allocates through its context, so such callers cannot use them.
  *
- * It counts the n (k-mer, biedge) pairs kmers[i], edges[i] -- the pairs the reference's
- * parser emits and debruijn_graph_map::compute_biedge_freqencies (debruijn_graph_map.hpp:
- * 1085-1141) counts: k-mers in the packing above (`words` uint64 each, bits above 2k zero),
- * biedges as DNA16 bytes -- and writes every distinct pair once with its count to out_kmers,
+ * It counts the n (k-mer, biedge) pairs kmers[i], edges[i] and writes every distinct pair once
+ * with its count to out_kmers, out_edges, out_counts.  A k-mer is in the packing above (`words`
+ * uint64 each, bits above 2k zero) and a biedge is a DNA16 byte (base before the k-mer in the
+ * high nibble, base after it in the low nibble, 0 = none).  Pairs are counted exactly as given,
+ * never canonicalised: pass each k-mer as the smaller of itself and its reverse complement,
+ * with its biedge oriented to match (on a flip the two nibbles swap and each is complemented);
+ * a pair and its reverse complement passed as they come are counted as two different pairs.
+ * The outputs go to out_kmers,
  * out_edges, out_counts (capacity out_cap pairs, in no particular order).  *n_out receives
  * the number of distinct pairs.  All five arrays are DEVICE pointers; passing NULL for all
  * three outputs only counts.  The working hash table lives in one fixed device array of

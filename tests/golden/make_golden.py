@@ -7,7 +7,7 @@
    records a digest of each output in expected.json; with ":clean", the same for the graph
    after the _freq_clean driver's dead-end and bubble cleaning.
 
-Usage: python tests/golden/make_golden.py [path/to/reference]
+Usage: python tests/golden/make_golden.py <path of the ParBLiSS/bruno source tree>
 """
 from __future__ import annotations
 
@@ -56,7 +56,9 @@ def digest(result: dict) -> dict:
 
 
 def main() -> None:
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the ParBLiSS/bruno source tree>")
+    ref = sys.argv[1]
     data = os.path.join(HERE, "data")
     os.makedirs(data, exist_ok=True)
     for f in FIXTURES:

@@ -170,7 +170,7 @@ RULES_HARNESS = r'''
 #include <iostream>
 #include <sstream>
 #include <string>
-/* each line: op budget w est solo n held... busy...  ->  prints 0 or 1 (E n -> the estimate) */
+/* each line: op budget w est solo running n held... busy...  ->  prints 0 or 1 (E n -> the estimate) */
 int main() {
   std::string line;
   while (std::getline(std::cin, line)) {
@@ -178,14 +178,14 @@ int main() {
     std::string op;
     in >> op;
     if (op == "E") { unsigned long long n; in >> n; printf("%llu\n", (unsigned long long)bruno_pool_rules::estimate(n)); continue; }
-    unsigned long long budget, est; int w, solo, n;
-    in >> budget >> w >> est >> solo >> n;
+    unsigned long long budget, est; int w, solo, running, n;
+    in >> budget >> w >> est >> solo >> running >> n;
     std::vector<uint64_t> held(n);
     std::vector<bool> busy(n);
     for (auto &h : held) { unsigned long long x; in >> x; h = x; }
     for (int i = 0; i < n; ++i) { int b; in >> b; busy[i] = b != 0; }
-    const bool r = op == "A" ? bruno_pool_rules::admits(held, busy, budget, w, est, solo != 0)
-                             : bruno_pool_rules::should_trim(held, busy, budget, w, est, solo != 0);
+    const bool r = op == "A" ? bruno_pool_rules::admits(held, busy, budget, w, est, solo != 0, running != 0)
+                             : bruno_pool_rules::should_trim(held, busy, budget, w, est, solo != 0, running != 0);
     printf("%d\n", r ? 1 : 0);
   }
 }
@@ -212,8 +212,9 @@ def pool_rules(tmp_path_factory):
     return run
 
 
-def _q(op, budget, w, est, solo, held, busy):
-    return " ".join(str(x) for x in [op, budget, w, est, int(solo), len(held), *held, *[int(b) for b in busy]])
+def _q(op, budget, w, est, solo, held, busy, running=False):
+    return " ".join(str(x) for x in [op, budget, w, est, int(solo), int(running), len(held), *held,
+                                     *[int(b) for b in busy]])
 
 
 def test_pool_estimate(pool_rules):
@@ -237,6 +238,12 @@ def test_pool_admission_rules(pool_rules):
         (0, _q("T", 1000, 1, 600, False, [600, 500], [False, True])),   # worker 1 is busy
         (0, _q("T", 1000, 0, 600, False, [0, 500], [False, True])),     # holds nothing
         (1, _q("T", 1000, 0, 600, False, [400, 700, 0], [False, True, False])),
+        # a retried (solo) request is running: nothing else starts beside it, however small,
+        # and no idle worker trims for a head that cannot start anyway
+        (0, _q("A", 1000, 0, 10, False, [0, 900], [False, True], running=True)),
+        (0, _q("A", 1000, 0, 10, False, [0, 0, 0], [False, True, False], running=True)),
+        (0, _q("T", 1000, 0, 600, False, [600, 500], [False, True], running=True)),
+        (1, _q("A", 1000, 0, 10, False, [0, 900], [False, True], running=False)),
     ]
     assert pool_rules([q for _, q in cases]) == [e for e, _ in cases]
 
