@@ -210,6 +210,56 @@ void parallel(int T, F f) {
   for (auto &x : th) x.join();
 }
 
+/* Sorts v with T threads: T contiguous chunks are sorted at once, then T threads merge them,
+ * each thread the output range between two splitters taken from the sorted chunks.  The
+ * result is the order std::sort gives for a strict weak order (equal elements may come in
+ * any order, as with std::sort). */
+template <typename V, typename C>
+void par_sort(std::vector<V> &v, C less, int T) {
+  const size_t n = v.size();
+  if (T <= 1 || n < (size_t)(1 << 16)) { std::sort(v.begin(), v.end(), less); return; }
+  std::vector<size_t> lo(T + 1);
+  for (int t = 0; t <= T; ++t) lo[t] = n * (size_t)t / (size_t)T;
+  parallel(T, [&](int t) { std::sort(v.begin() + lo[t], v.begin() + lo[t + 1], less); });
+  /* splitters: every chunk's elements at its T quantiles, sorted; thread t merges the
+   * elements in [split[t-1], split[t]) of every chunk (by lower_bound on each side) */
+  std::vector<V> sample;
+  for (int t = 0; t < T; ++t)
+    for (int q = 1; q < T; ++q) sample.push_back(v[lo[t] + (lo[t + 1] - lo[t]) * (size_t)q / (size_t)T]);
+  std::sort(sample.begin(), sample.end(), less);
+  std::vector<V> split;
+  for (int q = 1; q < T; ++q) split.push_back(sample[sample.size() * (size_t)q / (size_t)T]);
+  std::vector<std::vector<size_t>> cut(T, std::vector<size_t>(T + 1));   /* cut[chunk][range] */
+  parallel(T, [&](int c) {
+    cut[c][0] = lo[c];
+    cut[c][T] = lo[c + 1];
+    for (int q = 1; q < T; ++q)
+      cut[c][q] = (size_t)(std::lower_bound(v.begin() + lo[c], v.begin() + lo[c + 1], split[q - 1], less) - v.begin());
+  });
+  std::vector<size_t> out0(T + 1, 0);
+  for (int q = 0; q < T; ++q) {
+    size_t m = 0;
+    for (int c = 0; c < T; ++c) m += cut[c][q + 1] - cut[c][q];
+    out0[q + 1] = out0[q] + m;
+  }
+  std::vector<V> out(n);
+  parallel(T, [&](int q) {
+    /* T-way merge of the chunk pieces of range q */
+    std::vector<std::pair<size_t, size_t>> runs;
+    for (int c = 0; c < T; ++c)
+      if (cut[c][q] < cut[c][q + 1]) runs.emplace_back(cut[c][q], cut[c][q + 1]);
+    size_t o = out0[q];
+    while (!runs.empty()) {
+      size_t best = 0;
+      for (size_t r = 1; r < runs.size(); ++r)
+        if (less(v[runs[r].first], v[runs[best].first])) best = r;
+      out[o++] = v[runs[best].first];
+      if (++runs[best].first == runs[best].second) runs.erase(runs.begin() + (long)best);
+    }
+  });
+  v.swap(out);
+}
+
 double now() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -802,8 +852,8 @@ struct Run {
    * print_chain_as_fasta(chain_only) (:359-384). */
   void emit() {
     double t0 = now();
-    std::vector<Ranked> rk;
-    for (int s = 0; s < T; ++s)
+    std::vector<std::vector<Ranked>> part(T);
+    parallel(T, [&](int s) {
       for (size_t i = 0; i < chain[s].keys.size(); ++i) {
         if (chain[s].state[i] != 1) continue;
         W key = chain[s].keys[i].v;
@@ -811,15 +861,18 @@ struct Run {
         W L = is_chain_terminal(x.inD) ? key : x.inK;
         W R = is_chain_terminal(x.outD) ? ko.rc(key) : ko.rc(x.outK);
         bool sense = L <= R;
-        rk.push_back({sense ? key : ko.rc(key), sense ? L : R,
-                      (int32_t)(sense ? get_chain_dist(x.inD) : get_chain_dist(x.outD))});
+        part[s].push_back({sense ? key : ko.rc(key), sense ? L : R,
+                           (int32_t)(sense ? get_chain_dist(x.inD) : get_chain_dist(x.outD))});
       }
+    });
+    std::vector<Ranked> rk;
+    for (int s = 0; s < T; ++s) { rk.insert(rk.end(), part[s].begin(), part[s].end()); std::vector<Ranked>().swap(part[s]); }
     std::vector<Ranked> byrep(rk);
-    std::sort(byrep.begin(), byrep.end(), [](const Ranked &a, const Ranked &b) {
+    par_sort(byrep, [](const Ranked &a, const Ranked &b) {
       if (a.rep != b.rep) return a.rep < b.rep;
       if (std::abs(a.dist) != std::abs(b.dist)) return std::abs(a.dist) < std::abs(b.dist);
       return a.K < b.K;
-    });
+    }, T);
     std::string chars;
     std::vector<W> reps;
     std::vector<uint64_t> offs;
@@ -829,7 +882,7 @@ struct Run {
       else chars += "ACGT"[ko.last(byrep[i].K)];
     }
     offs.push_back(chars.size());
-    std::sort(rk.begin(), rk.end(), [](const Ranked &a, const Ranked &b) { return a.K < b.K; });
+    par_sort(rk, [](const Ranked &a, const Ranked &b) { return a.K < b.K; }, T);
 
     const int w = res->words;
     res->n_ranked = rk.size();
@@ -1336,7 +1389,7 @@ struct Run {
     for (int s = 0; s < T; ++s)
       for (size_t i = 0; i < nodes[s].keys.size(); ++i)
         if (nodes[s].state[i] == 1) nv.emplace_back(nodes[s].keys[i].v, nodes[s].vals[i]);
-    std::sort(nv.begin(), nv.end(), [](const std::pair<W, Node> &a, const std::pair<W, Node> &b) { return a.first < b.first; });
+    par_sort(nv, [](const std::pair<W, Node> &a, const std::pair<W, Node> &b) { return a.first < b.first; }, T);
     res->n_nodes = nv.size();
     res->node_keys = (uint64_t *)calloc(nv.size() * w + 1, 8);
     res->node_counts = (uint16_t *)calloc(nv.size() * 9 + 1, 2);
@@ -1348,11 +1401,11 @@ struct Run {
                                      (is_chain(nv[i].first, nv[i].second) ? 2 : 0));
     }
   }
-  static void export_k2(std::vector<std::pair<K2Key<W>, uint32_t>> &v, uint64_t *n, uint64_t **keys,
-                        uint8_t **edges, uint32_t **counts, int w) {
-    std::sort(v.begin(), v.end(), [](const std::pair<K2Key<W>, uint32_t> &a, const std::pair<K2Key<W>, uint32_t> &b) {
+  void export_k2(std::vector<std::pair<K2Key<W>, uint32_t>> &v, uint64_t *n, uint64_t **keys,
+                 uint8_t **edges, uint32_t **counts, int w) {
+    par_sort(v, [](const std::pair<K2Key<W>, uint32_t> &a, const std::pair<K2Key<W>, uint32_t> &b) {
       return a.first.kmer < b.first.kmer || (a.first.kmer == b.first.kmer && a.first.edge < b.first.edge);
-    });
+    }, T);
     *n = v.size();
     *keys = (uint64_t *)calloc(v.size() * w + 1, 8);
     *edges = (uint8_t *)calloc(v.size() + 1, 1);

@@ -13,8 +13,6 @@ DATA = os.path.join(GOLDEN, "data")
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (parity of the CUDA library against the oracle)")
-    config.addinivalue_line("markers", "gpu_staged: GPU parity tests of code that has not yet run on a GPU; "
-                                       "selected only by -m gpu_staged, skipped without a GPU")
 
 
 @pytest.fixture(scope="session", autouse=True)

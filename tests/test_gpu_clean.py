@@ -1,10 +1,6 @@
 """Graph cleaning on the GPU (bruno_clean_deadend_and_bubbles_naive; the _freq_clean driver's
 clean_deadend_and_bubbles_naive, compact_dbg_clean.hpp:575-890) against the oracle's
-restatement, bit-exact after sorting.
-
-Staged: these tests carry the `gpu_staged` marker, not `gpu`, until they have passed on a
-GB300 (`python -m pytest tests -m gpu_staged`); then they move to `gpu`.  Without a GPU they
-are skipped."""
+restatement, bit-exact after sorting.  Without a GPU they are skipped."""
 import os
 import subprocess
 
@@ -26,7 +22,7 @@ def _has_cuda() -> bool:
         return False
 
 
-pytestmark = [pytest.mark.gpu_staged, pytest.mark.skipif(not _has_cuda(), reason="needs a CUDA GPU")]
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not _has_cuda(), reason="needs a CUDA GPU")]
 
 
 def gpu_clean(data, k, thr_on, thresh, mu=True, **kw):

@@ -1,7 +1,5 @@
-"""GPU parity of code paths that have not yet run on a GPU: the ranking's one-pass final states
-(cfg.rank_fill = 1), the zero-copy result view, and host pieces over several copy streams.
-Staged like tests/test_gpu_clean.py: marker `gpu_staged`, selected only by `-m gpu_staged`,
-skipped without a GPU; moved to `gpu` once it has passed on a GB300."""
+"""GPU parity of the optional paths: the ranking's one-pass final states (cfg.rank_fill = 1),
+the zero-copy result view, and host pieces over several copy streams."""
 import pytest
 
 import bruno_gb300 as bg
@@ -11,7 +9,7 @@ from conftest import fixture_bytes
 from test_gpu_clean import _has_cuda
 from test_gpu_parity import compare, gpu_run
 
-pytestmark = [pytest.mark.gpu_staged, pytest.mark.skipif(not _has_cuda(), reason="needs a CUDA GPU")]
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not _has_cuda(), reason="needs a CUDA GPU")]
 
 
 @pytest.mark.parametrize("fname", ["debruijn.palindrome_chr14.fastq", "debruijn.shifted_cycle_chr14.fastq",
@@ -40,7 +38,7 @@ class _DevArray:
     """a read-only device array for torch.as_tensor (the CUDA array interface)"""
 
     def __init__(self, ptr, n, typestr):
-        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, True), "version": 2}
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 2}
 
 
 def test_device_results_zero_copy():
