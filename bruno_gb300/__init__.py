@@ -85,8 +85,17 @@ EXPORTS = (
     "bruno_copy_chains", "bruno_copy_chain_edges", "bruno_copy_chain_summaries", "bruno_host_alloc", "bruno_host_free", "bruno_phase_ms",
     "bruno_count_biedges_noalloc", "bruno_pool_create", "bruno_pool_submit", "bruno_pool_wait",
     "bruno_pool_result_free", "bruno_pool_destroy", "bruno_clean_deadend_and_bubbles_naive",
-    "bruno_device_results",
+    "bruno_device_results", "bruno_graph_find_if", "bruno_graph_erase_if", "bruno_graph_erase_nodes",
+    "bruno_chain_find_if", "bruno_get_cycle_node_kmers", "bruno_get_isolated",
 )
+
+# node predicates (bliss::debruijn::filter::graph) and chain predicates
+# (bliss::debruijn::filter::chain) as the C ABI numbers them
+NODE_FILTERS = {"all": 0, "IsKPalindrome": 1, "IsKplus1Palindrome": 2, "IsBranchPoint": 3, "IsIsolated": 4,
+                "IsChainInternalNode": 5, "IsChainNode": 6}
+CHAIN_FILTERS = {"all": 0, "IsUnitLength": 1, "IsIsolated": 2, "IsTerminus": 3, "IsInternal": 4,
+                 "IsTerminusOrIsolated": 5, "IsCanonicalTerminus": 6, "IsCanonicalTerminusOrIsolated": 7,
+                 "PointsToTermini": 8, "PointsToInternalNode": 9}
 
 
 def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
@@ -120,6 +129,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "bruno_pool_destroy": [P],
         "bruno_clean_deadend_and_bubbles_naive": [P, ctypes.POINTER(_CleanStats)],
         "bruno_device_results": [P, ctypes.POINTER(_DeviceView)],
+        "bruno_graph_find_if": [P, I32, P, P, P, SZ, PSZ], "bruno_graph_erase_if": [P, I32, PSZ],
+        "bruno_graph_erase_nodes": [P, P, SZ],
+        "bruno_chain_find_if": [P, I32, P, P, P, P, P, SZ, PSZ],
+        "bruno_get_cycle_node_kmers": [P, P, SZ, PSZ], "bruno_get_isolated": [P, P, P, P, P, P, SZ, PSZ],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -381,6 +394,62 @@ class Graph:
             self._check(self.lib.bruno_copy_nodes(self.ctx, self._ptr(keys), self._ptr(counts), self._ptr(flags),
                                                   n.value, ctypes.byref(n)), "copy_nodes")
         return keys, counts, flags
+
+    # ------------------------------------------------- graph and chain-map queries
+    def find_if(self, pred: str):
+        """debruijn_graph::find_if(pred): the matching nodes as nodes() gives them"""
+        f = NODE_FILTERS[pred]
+        n = ctypes.c_size_t()
+        self._check(self.lib.bruno_graph_find_if(self.ctx, f, None, None, None, 0, ctypes.byref(n)), "graph_find_if")
+        keys = np.zeros((n.value, self.words), np.uint64)
+        counts = np.zeros((n.value, 9), np.uint16)
+        flags = np.zeros(n.value, np.uint8)
+        if n.value:
+            self._check(self.lib.bruno_graph_find_if(self.ctx, f, self._ptr(keys), self._ptr(counts), self._ptr(flags),
+                                                     n.value, ctypes.byref(n)), "graph_find_if")
+        return keys, counts, flags
+
+    def erase_if(self, pred: str) -> int:
+        """debruijn_graph::erase_if(pred); returns the number of nodes erased"""
+        n = ctypes.c_size_t()
+        self._check(self.lib.bruno_graph_erase_if(self.ctx, NODE_FILTERS[pred], ctypes.byref(n)), "graph_erase_if")
+        return n.value
+
+    def erase_nodes(self, kmers) -> None:
+        """debruijn_graph_map::erase_nodes(query): k-mers (n, words), either strand"""
+        q = np.ascontiguousarray(np.asarray(kmers, np.uint64).reshape(-1, self.words))
+        self._check(self.lib.bruno_graph_erase_nodes(self.ctx, self._ptr(q), len(q)), "graph_erase_nodes")
+
+    def _chain_records(self, fn, what, *lead):
+        n = ctypes.c_size_t()
+        self._check(fn(self.ctx, *lead, None, None, None, None, None, 0, ctypes.byref(n)), what)
+        K = np.zeros((n.value, self.words), np.uint64)
+        inK = np.zeros((n.value, self.words), np.uint64)
+        outK = np.zeros((n.value, self.words), np.uint64)
+        inD = np.zeros(n.value, np.uint32)
+        outD = np.zeros(n.value, np.uint32)
+        if n.value:
+            self._check(fn(self.ctx, *lead, self._ptr(K), self._ptr(inK), self._ptr(outK), self._ptr(inD),
+                           self._ptr(outD), n.value, ctypes.byref(n)), what)
+        return K, inK, outK, inD, outD
+
+    def chain_find_if(self, pred: str):
+        """debruijn_chain_graph::find_if(pred): records (K, inK, outK, inDist, outDist)"""
+        return self._chain_records(self.lib.bruno_chain_find_if, "chain_find_if", CHAIN_FILTERS[pred])
+
+    def get_isolated(self):
+        """debruijn_chain_graph::get_isolated(): records as chain_find_if gives them"""
+        return self._chain_records(self.lib.bruno_get_isolated, "get_isolated")
+
+    def get_cycle_node_kmers(self):
+        """debruijn_chain_graph::get_cycle_node_kmers(): k-mers (n, words)"""
+        n = ctypes.c_size_t()
+        self._check(self.lib.bruno_get_cycle_node_kmers(self.ctx, None, 0, ctypes.byref(n)), "get_cycle_node_kmers")
+        K = np.zeros((n.value, self.words), np.uint64)
+        if n.value:
+            self._check(self.lib.bruno_get_cycle_node_kmers(self.ctx, self._ptr(K), n.value, ctypes.byref(n)),
+                        "get_cycle_node_kmers")
+        return K
 
     def ranked(self):
         """listranked chain nodes: K (n, words), rep (n, words), dist"""

@@ -371,15 +371,61 @@ __device__ __forceinline__ uint64_t ld_cg(const uint64_t *p) { return __ldcg((co
 /* one slot (4 or 8 words) with 256-bit relaxed loads: a single L2 request per 32 bytes */
 __device__ __forceinline__ uint32_t ld_cg32(const uint32_t *p) { return __ldcg(p); }
 
+/* One more occurrence of the entry whose word lives at `key` (its address), in the exact
+ * side table of counts past 2^24.  Every such entry needs 2^24 occurrences, so at most
+ * n_instances / 2^24 of them exist: the table cannot fill below 2^34 instances. */
+__device__ __forceinline__ void big_add(DevCounters *ctr, unsigned long long key) {
+  unsigned h = (unsigned)mix64(key) & (BIG_SLOTS - 1);
+  for (int p = 0; p < BIG_SLOTS; ++p, h = (h + 1) & (BIG_SLOTS - 1)) {
+    const unsigned long long prev = atomicCAS(&ctr->big_key[h], 0ull, key);
+    if (prev == 0ull) atomicAdd(&ctr->n_big, 1ull);
+    if (prev == 0ull || prev == key) { atomicAdd(&ctr->big_cnt[h], 1ull); return; }
+  }
+  atomicOr(&ctr->err, (unsigned long long)DERR_INVARIANT);
+}
+__device__ __forceinline__ unsigned long long big_get(const DevCounters *ctr, unsigned long long key) {
+  unsigned h = (unsigned)mix64(key) & (BIG_SLOTS - 1);
+  for (int p = 0; p < BIG_SLOTS; ++p, h = (h + 1) & (BIG_SLOTS - 1)) {
+    const unsigned long long k = ctr->big_key[h];
+    if (k == key) return ctr->big_cnt[h];
+    if (k == 0ull) return 0;
+  }
+  return 0;
+}
+
+/* after counting: every side-table entry resolved to (table key, biedge code, exact count) */
+template <class KT>
+__global__ void k_big_resolve(const uint64_t *table, const DevCounters *ctr, BigRes *out,
+                              unsigned long long *n_out) {
+  constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
+  for (int h = threadIdx.x; h < BIG_SLOTS; h += blockDim.x) {
+    const unsigned long long key = ctr->big_key[h];
+    if (key == 0ull) continue;
+    const uint64_t off = (uint64_t)(key - (unsigned long long)(uintptr_t)table);   /* bytes into the table */
+    const uint64_t *slot = table + (off / (SU * 8)) * SU;
+    const uint32_t w = *(const uint32_t *)(uintptr_t)key;
+    BigRes r;
+    r.k0 = slot[0];
+    r.k1 = KWD == 2 ? slot[1] : 0ull;
+    if (KWD == 1) r.k0 &= ~KEY_CONT; else r.k1 &= ~KEY_CONT;
+    r.code = entry_code(w);
+    r.pad = 0;
+    r.count = (unsigned long long)(w >> E_COUNT_SHIFT) + ctr->big_cnt[h];
+    out[atomicAdd(n_out, 1ull)] = r;
+  }
+}
+
 /* One count into the entry words e[0..n) of a slot whose current contents were read into
  * `seen`.  Returns true when counted, false when every entry holds another biedge (slot
  * full).  A free entry is claimed with CAS; a stale free entry (claimed since the read)
  * shows up as a failed CAS returning the claimer's word.  Increments are fire-and-forget
- * while the count is below 2^24; above that the returned value is checked so that the
- * `big` bit is set before the 26-bit count can wrap. */
+ * while the count seen is below 2^24; from there on the entry word keeps its count (at most
+ * 2^24 plus the increments in flight, far below the 26-bit field's limit), carries E_BIG, and
+ * every further occurrence is counted exactly in the side table, so that the raw (k+2)-mer
+ * counts stay exact to 32 bits like the reference's uint32 K2FreqType. */
 template <int NE>
 __device__ __forceinline__ bool count_in_entries(uint32_t *e, const uint32_t *seen, unsigned code,
-                                                 unsigned long long &claims) {
+                                                 unsigned long long &claims, DevCounters *ctr) {
   #pragma unroll
   for (int i = 0; i < NE; ++i) {
     uint32_t w = seen[i];
@@ -393,8 +439,8 @@ __device__ __forceinline__ bool count_in_entries(uint32_t *e, const uint32_t *se
       if ((w >> E_COUNT_SHIFT) < (1u << 24) && !(w & E_BIG)) {
         atomicAdd(e + i, 1u << E_COUNT_SHIFT);          /* result unused: a reduction */
       } else {
-        const uint32_t old = atomicAdd(e + i, 1u << E_COUNT_SHIFT);
-        if (old >> 31) atomicOr(e + i, E_BIG);
+        if (!(w & E_BIG)) atomicOr(e + i, E_BIG);
+        big_add(ctr, (unsigned long long)(uintptr_t)(e + i));
       }
       return true;
     }
@@ -450,7 +496,7 @@ template <class KT>
 __device__ __forceinline__ bool table_count(uint64_t *table, const TableGeom &g, uint32_t max_probe, KT x,
                                             unsigned code, uint64_t home, uint64_t *raw,
                                             unsigned long long &slot_claims, unsigned long long &entry_claims,
-                                            uint64_t part_lo = ~0ull) {
+                                            DevCounters *ctr, uint64_t part_lo = ~0ull) {
   constexpr int SU = Slot<KT>::U64, NE = Slot<KT>::ENTRIES, KWD = Slot<KT>::KEYW;
   bool seen_primary = false;
   Probe pr(g, home, part_lo);
@@ -481,7 +527,7 @@ __device__ __forceinline__ bool table_count(uint64_t *table, const TableGeom &g,
     }
     if (key_matches(key, x, seen_primary)) {
       seen_primary = true;
-      if (count_in_entries<NE>((uint32_t *)(slot + KWD), seen, code, entry_claims)) return true;
+      if (count_in_entries<NE>((uint32_t *)(slot + KWD), seen, code, entry_claims, ctr)) return true;
     }
   }
   return false;
@@ -555,11 +601,11 @@ __global__ void __launch_bounds__(TPB, 4) k_count(CountArgs a) {
         }
         if (pa < pend) {
           ++inst;
-          if (!table_count<KT>(a.table, a.g, a.max_probe, xa, ca, ia, ra, slots, entries)) full = true;
+          if (!table_count<KT>(a.table, a.g, a.max_probe, xa, ca, ia, ra, slots, entries, a.ctr)) full = true;
         }
         if (pc < pend) {
           ++inst;
-          if (!table_count<KT>(a.table, a.g, a.max_probe, xc, cc, ic, rc, slots, entries)) full = true;
+          if (!table_count<KT>(a.table, a.g, a.max_probe, xc, cc, ic, rc, slots, entries, a.ctr)) full = true;
         }
       }
     }
@@ -974,7 +1020,7 @@ __global__ void __launch_bounds__(TPB) k_insert(const uint64_t *records, const u
       if (rec[q] == 0ull) continue;
       const uint64_t h = ((uint64_t)b << LOW_BITS) | (rec[q] >> 5);
       if (!table_count<KW1>(table, g, max_probe, KW1{h}, (unsigned)(rec[q] & 31), home[q], raw[q], slots, entries,
-                            lo))
+                            ctr, lo))
         full = true;
     }
   }
@@ -997,6 +1043,7 @@ struct FilterArgs {
   int thresholding;
   uint32_t max_probe;
   uint64_t *f_keys; uint8_t *f_edges; uint32_t *f_counts; uint64_t f_cap;
+  const BigRes *big; uint64_t n_big;   /* entries counted past 2^24, for exact filtered counts */
   DevCounters *ctr;
 };
 
@@ -1140,7 +1187,13 @@ __device__ __forceinline__ void filter_kmer(uint64_t *s, uint64_t slot_index, KT
       if (o < a.f_cap) {
         KOps<KT>::store(a.f_keys + o * KWD, key);
         a.f_edges[o] = code_biedge(biedge_code(in5, out5));
-        a.f_counts[o] = cnt;
+        uint32_t exact = cnt;
+        if (w[q] & E_BIG)   /* counted past 2^24: the exact count, to 32 bits like the reference's */
+          for (uint64_t b = 0; b < a.n_big; ++b)
+            if (a.big[b].code == code && a.big[b].k0 == ((const uint64_t *)&tkey)[0] &&
+                (KWD == 1 || a.big[b].k1 == ((const uint64_t *)&tkey)[KWD - 1]))
+              exact = (uint32_t)a.big[b].count;
+        a.f_counts[o] = exact;
       }
     }
   }
@@ -1351,8 +1404,8 @@ __device__ __forceinline__ bool sm_count_entries(uint32_t *e, const uint32_t *se
     }
     if (entry_code(w) == code) {
       if ((w >> E_COUNT_SHIFT) < (1u << 24) && !(w & E_BIG)) {
-        atomicAdd(e + i, 1u << E_COUNT_SHIFT);   /* result unused: a partition holds far fewer
-                                                    than 2^24 records, so this cannot reach E_BIG */
+        atomicAdd(e + i, 1u << E_COUNT_SHIFT);   /* result unused: a partition counted here holds
+                                                    fewer than 2^24 records, so this never reaches E_BIG */
       } else {
         const uint32_t old = atomicAdd(e + i, 1u << E_COUNT_SHIFT);
         if (old >> 31) atomicOr(e + i, E_BIG);
@@ -1460,7 +1513,10 @@ __global__ void __launch_bounds__(TPB) k_dump_k2(const uint64_t *table, uint64_t
       if (o < cap) {
         KOps<KT>::store(keys + o * KWD, key);
         edges[o] = code_biedge(entry_code(e[j]));
-        counts[o] = entry_count(e[j]);
+        /* past 2^24 the exact count is the word's plus the side table's, kept to 32 bits as the
+         * reference's uint32 counter keeps it */
+        counts[o] = (e[j] & E_BIG) ? (uint32_t)((e[j] >> E_COUNT_SHIFT) + big_get(ctr, (unsigned long long)(uintptr_t)(e + j)))
+                                   : entry_count(e[j]);
       }
     }
   }
@@ -1766,6 +1822,8 @@ bruno_status count_direct(Ctx *c) {
     cudaEventRecord(c->kev[1], c->stream);
     k_table_init<KT><<<sms * 8, TPB, 0, c->stream>>>((uint64_t *)c->table.p, slots);
     cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
+    cudaMemsetAsync(c->dctr->big_key, 0, sizeof(c->dctr->big_key) + sizeof(c->dctr->big_cnt), c->stream);
+    cudaMemsetAsync(&c->dctr->n_big, 0, 8, c->stream);
     cudaEventRecord(c->kev[2], c->stream);
     CountArgs a{(const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k, (uint64_t *)c->table.p,
                 c->geom, 4096u, c->dctr};
@@ -1874,6 +1932,8 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
     bool counted = false, counted_local = false;
     cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
     cudaMemsetAsync(&c->dctr->n_slots_claimed, 0, 16, c->stream);
+    cudaMemsetAsync(c->dctr->big_key, 0, sizeof(c->dctr->big_key) + sizeof(c->dctr->big_cnt), c->stream);
+    cudaMemsetAsync(&c->dctr->n_big, 0, 8, c->stream);
     if (region_c <= (uint64_t)PART_SLOTS && c->force_direct_count != 2) {
       c->geom = TableGeom{region_c << pb, region_c, pb};
       c->nslots = c->geom.nslots;
@@ -1904,7 +1964,9 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
         cnts = (const unsigned long long *)c->sub_cnt.p;
         rcap = cap2;
       }
-      if (split_ok) {
+      /* a partition counts in shared memory only while no entry can pass 2^24 occurrences
+       * (beyond that the L2 path keeps exact counts in the side table) */
+      if (split_ok && rcap < (1ull << 24)) {
         k_count_local<<<(unsigned)nparts, PTPB, (unsigned)(region_c * 32), c->stream>>>(
             recs, cnts, rcap, sbits, (uint64_t *)c->table.p, c->geom, c->dctr);
         c->launches += 1;
@@ -2000,7 +2062,7 @@ bruno_status build_k1_table(Ctx *c) {
 }
 
 template <class KT>
-bruno_status count_typed(Ctx *c) {
+bruno_status count_paths(Ctx *c) {
   if (c->cfg.edge_filter) {   /* the (k+1)-mer filter works on the partitioned path (k <= 31) */
     bruno_status st = build_k1_table(c);
     if (st != BRUNO_OK) return st;
@@ -2014,6 +2076,23 @@ bruno_status count_typed(Ctx *c) {
     if (st != BRUNO_OK || used) return st;
   }
   return count_direct<KT>(c);
+}
+
+/* counting, then the entries counted past 2^24 (if any) resolved for the filter */
+template <class KT>
+bruno_status count_typed(Ctx *c) {
+  bruno_status st = count_paths<KT>(c);
+  if (st != BRUNO_OK) return st;
+  c->n_big = c->hctr->n_big;
+  if (c->n_big == 0) return BRUNO_OK;
+  if ((st = ensure(c, c->bigres, BIG_SLOTS * sizeof(BigRes))) != BRUNO_OK) return st;
+  cudaMemsetAsync(&c->dctr->n_big_res, 0, 8, c->stream);
+  k_big_resolve<KT><<<1, 1024, 0, c->stream>>>((const uint64_t *)c->table.p, c->dctr, (BigRes *)c->bigres.p,
+                                               &c->dctr->n_big_res);
+  c->launches += 1;
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  c->n_big = std::min<uint64_t>(c->hctr->n_big_res, BIG_SLOTS);
+  return BRUNO_OK;
 }
 
 template <class KT>
@@ -2052,6 +2131,8 @@ bruno_status filter_typed(Ctx *c, const uint64_t *thr) {
   a.chain_list = (uint32_t *)c->chain_list.p;
   a.branch_list = (uint32_t *)c->branch_list.p;
   a.list_cap = cap;
+  a.big = (const BigRes *)c->bigres.p;
+  a.n_big = c->n_big;
   if (c->cfg.keep_filtered) {
     const uint64_t n = std::max<uint64_t>(1, c->n_entries);
     if ((st = ensure(c, c->f_keys, n * 8 * Slot<KT>::KEYW)) != BRUNO_OK) return st;
@@ -2147,7 +2228,7 @@ __global__ void __launch_bounds__(TPB) k_count_pairs(const uint64_t *kmers, cons
     const uint64_t home = table_home(g, key);
     uint64_t raw[SU];
     ld_slot<SU>(table + home * SU, raw);
-    if (!table_count<KT>(table, g, max_probe, key, biedge_code(in5, out5), home, raw, slots, entries)) full = true;
+    if (!table_count<KT>(table, g, max_probe, key, biedge_code(in5, out5), home, raw, slots, entries, ctr)) full = true;
   }
   slots = warp_sum(slots); entries = warp_sum(entries);
   if ((threadIdx.x & 31) == 0) {

@@ -78,7 +78,7 @@ static void release(Buf &b) {
 }
 
 bruno_status sync_counters(Ctx *c, bool with_hll) {
-  const size_t n = with_hll ? sizeof(DevCounters) : offsetof(DevCounters, hll);
+  const size_t n = with_hll ? offsetof(DevCounters, big_key) : offsetof(DevCounters, hll);
   cudaError_t e = cudaMemcpyAsync(c->hctr, c->dctr, n, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e == cudaSuccess) e = cudaGetLastError();
@@ -537,6 +537,52 @@ bruno_status bruno_copy_chain_summaries(bruno_ctx *c, uint64_t *kmers, uint32_t 
   if (st == BRUNO_OK) st = copy_d2h(c, flags, c->s_flags.p, c->n_summaries * 2);
   if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
   return st;
+}
+
+bruno_status bruno_graph_find_if(bruno_ctx *c, int32_t filter, uint64_t *keys, uint16_t *counts, uint8_t *flags,
+                                 size_t cap, size_t *n) {
+  if (!c || !n) return BRUNO_ERR_ARG;
+  if (filter < BRUNO_NODES_ALL || filter > BRUNO_IS_CHAIN_NODE) return set_err(c, BRUNO_ERR_ARG, "unknown node filter");
+  if (c->stage < 3) return set_err(c, BRUNO_ERR_ARG, "nodes exist after local_insert_by_freqencies");
+  return run_node_query(c, filter, false, keys, counts, flags, cap, n);
+}
+
+bruno_status bruno_graph_erase_if(bruno_ctx *c, int32_t filter, size_t *n_erased) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (filter < BRUNO_NODES_ALL || filter > BRUNO_IS_CHAIN_NODE) return set_err(c, BRUNO_ERR_ARG, "unknown node filter");
+  if (c->stage < 3) return set_err(c, BRUNO_ERR_ARG, "nodes exist after local_insert_by_freqencies");
+  size_t n = 0;
+  const bruno_status st = run_node_query(c, filter, true, nullptr, nullptr, nullptr, 0, &n);
+  if (n_erased) *n_erased = n;
+  return st;
+}
+
+bruno_status bruno_graph_erase_nodes(bruno_ctx *c, const uint64_t *kmers, size_t n) {
+  if (!c || (!kmers && n)) return BRUNO_ERR_ARG;
+  if (c->stage < 3) return set_err(c, BRUNO_ERR_ARG, "nodes exist after local_insert_by_freqencies");
+  return run_erase_nodes(c, kmers, n);
+}
+
+bruno_status bruno_chain_find_if(bruno_ctx *c, int32_t filter, uint64_t *kmers, uint64_t *in_kmers,
+                                 uint64_t *out_kmers, uint32_t *in_dist, uint32_t *out_dist, size_t cap, size_t *n) {
+  if (!c || !n) return BRUNO_ERR_ARG;
+  if (filter < BRUNO_CHAIN_ALL || filter > BRUNO_CHAIN_POINTS_TO_INTERNAL_NODE)
+    return set_err(c, BRUNO_ERR_ARG, "unknown chain filter");
+  if (c->stage < 4) return set_err(c, BRUNO_ERR_ARG, "the chain map exists after extract_chains");
+  return run_chain_query(c, filter, 0, kmers, in_kmers, out_kmers, in_dist, out_dist, cap, n);
+}
+
+bruno_status bruno_get_cycle_node_kmers(bruno_ctx *c, uint64_t *kmers, size_t cap, size_t *n) {
+  if (!c || !n) return BRUNO_ERR_ARG;
+  if (c->stage < 5) return set_err(c, BRUNO_ERR_ARG, "cycle nodes are known after list_rank");
+  return run_chain_query(c, BRUNO_CHAIN_ALL, 1, kmers, nullptr, nullptr, nullptr, nullptr, cap, n);
+}
+
+bruno_status bruno_get_isolated(bruno_ctx *c, uint64_t *kmers, uint64_t *in_kmers, uint64_t *out_kmers,
+                                uint32_t *in_dist, uint32_t *out_dist, size_t cap, size_t *n) {
+  if (!c || !n) return BRUNO_ERR_ARG;
+  if (c->stage < 5) return set_err(c, BRUNO_ERR_ARG, "isolated nodes are known after list_rank");
+  return run_chain_query(c, BRUNO_CHAIN_ALL, 2, kmers, in_kmers, out_kmers, in_dist, out_dist, cap, n);
 }
 
 bruno_status bruno_host_alloc(size_t bytes, void **out) {

@@ -1719,6 +1719,293 @@ __global__ void __launch_bounds__(TPB) k_cl_erase(const EraseQ *f, uint64_t nf, 
   }
 }
 
+/* ================================================================ graph and chain queries
+ * The graph and chain-map operations the reference driver calls between the phases:
+ * debruijn_graph::find_if / erase_if (debruijn_graph.hpp:188-252) with the node predicates of
+ * bliss::debruijn::filter::graph, debruijn_graph_map::erase_nodes (debruijn_graph_map.hpp:
+ * 833-836: the nodes and, on their neighbours, the edges back to them), and
+ * debruijn_chain_graph::find_if (debruijn_chain_graph.hpp:306-311) with the chain predicates of
+ * bliss::debruijn::filter::chain, get_cycle_node_kmers and get_isolated (:440-470). */
+
+/* the node predicates (debruijn_graph_filters.hpp:38-220), on a node's canonical k-mer and its
+ * out / in count words; the (k+1)-mer palindrome test is is_k1_k1pair_rc_palindrome
+ * (kmer_traits.hpp:108-125) over the present edges */
+template <class KT>
+__device__ __forceinline__ bool node_matches(int f, KT key, uint64_t out, uint64_t in, int k) {
+  const bool kpal = k_palindrome(key, k), oddk = (k & 1) != 0;
+  const bool high = oddk && km1_high_palindrome(key, k), low = oddk && km1_low_palindrome(key, k);
+  const unsigned first = KOps<KT>::first(key, k), last = KOps<KT>::last(key);
+  unsigned din = 0, dout = 0;
+  bool k1pal = false;
+  #pragma unroll
+  for (unsigned c = 0; c < 4; ++c) {
+    const bool o = count_at(out, c) > 0, n = count_at(in, c) > 0;
+    dout += o; din += n;
+    if (o && low && (first == 3u - c || first == c)) k1pal = true;
+    if (n && high && (last == 3u - c || last == c)) k1pal = true;
+  }
+  switch (f) {
+    case BRUNO_NODES_ALL: return true;
+    case BRUNO_IS_K_PALINDROME: return kpal;
+    case BRUNO_IS_KPLUS1_PALINDROME: return k1pal;
+    case BRUNO_IS_BRANCH_POINT: return din >= 2 || dout >= 2 || kpal || k1pal;
+    case BRUNO_IS_ISOLATED_NODE: return din == 0 && dout == 0;
+    case BRUNO_IS_CHAIN_INTERNAL_NODE: return din == 1 && dout == 1 && !kpal && !k1pal;
+    case BRUNO_IS_CHAIN_NODE: return din < 2 && dout < 2 && !kpal && !k1pal;
+    default: return false;
+  }
+}
+
+/* find_if(pred) over the node table: (k-mer, counts[9], flags) of every matching node, flags
+ * evaluated on the current counts; erase (erase_if) instead clears the matching nodes */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_node_query(uint64_t *table, uint64_t nslots, int k, int f, bool erase,
+                                                     uint64_t *keys, uint16_t *counts, uint8_t *flags, uint64_t cap,
+                                                     DevCounters *ctr) {
+  constexpr int KWD = Slot<KT>::KEYW, SU = Slot<KT>::U64;
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < nslots; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    uint64_t *s = table + (i < nslots ? i : 0) * SU;
+    bool hit = false;
+    KT key{};
+    if (i < nslots && key_is_node(KOps<KT>::load(s))) {
+      key = key_kmer(node_key(KOps<KT>::load(s)));
+      hit = node_matches<KT>(f, key, s[KWD], s[KWD + 1], k);
+    }
+    const unsigned long long o = block_append(hit, &ctr->n_k2_dump);
+    if (!hit) continue;
+    if (erase) { clear_node<KT>(s); continue; }
+    if (o >= cap) continue;
+    if (keys) KOps<KT>::store(keys + o * KWD, key);
+    if (counts)
+      for (int q = 0; q < 4; ++q) {
+        counts[o * 9 + q] = count_at(s[KWD], (unsigned)q);
+        counts[o * 9 + 4 + q] = count_at(s[KWD + 1], (unsigned)q);
+      }
+    if (counts) counts[o * 9 + 8] = (uint16_t)s[KWD + 2];
+    if (flags)
+      flags[o] = (uint8_t)((node_matches<KT>(BRUNO_IS_BRANCH_POINT, key, s[KWD], s[KWD + 1], k) ? NF_BRANCH : 0u) |
+                           (node_matches<KT>(BRUNO_IS_CHAIN_NODE, key, s[KWD], s[KWD + 1], k) ? NF_CHAIN : 0u));
+  }
+}
+
+/* erase_nodes(query) (debruijn_graph_map.hpp:833-836, erase_nodes_and_edges :811-827): each
+ * queried k-mer (either strand) that is a node leaves the graph, and its neighbours lose the
+ * edges back to it (get_remote_edges, :440-471).  A node erased here has no edge left on a
+ * surviving neighbour whatever the order of the threads: only a neighbour erased in the same
+ * call can clear an edge of the node before its thread reads it. */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_erase_nodes(const uint64_t *q, uint64_t n, uint64_t *table, TableGeom g,
+                                                      int k) {
+  constexpr int KWD = KOps<KT>::WORDS, SW = Slot<KT>::KEYW, SU = Slot<KT>::U64;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    KT K = KOps<KT>::load(q + i * KWD);
+    const KT R = KOps<KT>::rc(K, k);
+    if (!KOps<KT>::lt(K, R)) K = R;
+    const long long sl = table_find<KT>(table, g, 4096u, K);
+    if (sl < 0) continue;
+    uint64_t *slot = table + (uint64_t)sl * SU;
+    const uint64_t out = slot[SW], in = slot[SW + 1];
+    for (unsigned c = 0; c < 4; ++c) {
+      if (count_at(out, c)) {   /* K.c: its in-edge from K's first base */
+        KT y = KOps<KT>::append(K, c, k);
+        unsigned e = (1u << KOps<KT>::first(K, k)) << 4;
+        canon_edge(y, e, k);
+        zero_edges<KT>(table, g, y, e);
+      }
+      if (count_at(in, c)) {    /* c.K: its out-edge to K's last base */
+        KT y = KOps<KT>::prepend(c, K, k);
+        unsigned e = 1u << KOps<KT>::last(K);
+        canon_edge(y, e, k);
+        zero_edges<KT>(table, g, y, e);
+      }
+    }
+    clear_node<KT>(slot);
+  }
+}
+
+/* live nodes after an erasure, with the classification of each stored again from its counts
+ * (the filter's IsBranchPoint / IsChainNode), so that the node copy-out stays current */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_node_recount(uint64_t *table, uint64_t nslots, int k, DevCounters *ctr) {
+  constexpr int KWD = Slot<KT>::KEYW, SU = Slot<KT>::U64;
+  unsigned long long live = 0, br = 0, ch = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t *s = table + i * SU;
+    if (!key_is_node(KOps<KT>::load(s))) continue;
+    const KT key = key_kmer(node_key(KOps<KT>::load(s)));
+    const bool b = node_matches<KT>(BRUNO_IS_BRANCH_POINT, key, s[KWD], s[KWD + 1], k);
+    const bool cn = node_matches<KT>(BRUNO_IS_CHAIN_NODE, key, s[KWD], s[KWD + 1], k);
+    const uint64_t fl = (b ? NF_BRANCH : 0u) | (cn ? NF_CHAIN : 0u);
+    s[KWD + 2] = (s[KWD + 2] & ~(0xFFFFull << 16)) | (fl << 16);
+    ++live; br += b; ch += cn;
+  }
+  live = warp_sum(live); br = warp_sum(br); ch = warp_sum(ch);
+  if ((threadIdx.x & 31) == 0) {
+    if (live) atomicAdd(&ctr->n_nodes, live);
+    if (br) atomicAdd(&ctr->n_branch, br);
+    if (ch) atomicAdd(&ctr->n_chain, ch);
+  }
+}
+
+/* the chain predicates (debruijn_chain_filters.hpp:37-186) on a chain-map record */
+template <class KT>
+__device__ __forceinline__ bool chain_matches(int f, KT K, KT inK, KT outK, uint32_t inD, uint32_t outD, int k) {
+  const bool ti = term(inD), to = term(outD);
+  switch (f) {
+    case BRUNO_CHAIN_ALL: return true;
+    case BRUNO_CHAIN_IS_UNIT_LENGTH: return ti && to;
+    case BRUNO_CHAIN_IS_ISOLATED: return inD == TM && outD == TM;
+    case BRUNO_CHAIN_IS_TERMINUS: return ti != to;
+    case BRUNO_CHAIN_IS_INTERNAL: return (inD & DM) > 0 && (outD & DM) > 0;
+    case BRUNO_CHAIN_IS_TERMINUS_OR_ISOLATED: return ti || to;
+    case BRUNO_CHAIN_IS_CANONICAL_TERMINUS:
+    case BRUNO_CHAIN_IS_CANONICAL_TERMINUS_OR_ISOLATED:
+      if (ti && to) return f == BRUNO_CHAIN_IS_CANONICAL_TERMINUS_OR_ISOLATED;
+      if (ti) return KOps<KT>::le(K, KOps<KT>::rc(outK, k));
+      if (to) return KOps<KT>::lt(KOps<KT>::rc(K, k), inK);
+      return false;
+    case BRUNO_CHAIN_POINTS_TO_TERMINI: return !ptcn(inD) && !ptcn(outD);
+    case BRUNO_CHAIN_POINTS_TO_INTERNAL_NODE: return ptcn(inD) || ptcn(outD);
+    default: return false;
+  }
+}
+
+/* chain-map records (K, inK, outK, inD, outD) of the nodes whose removed[] mark is `which`
+ * (0: in the chain map, 1: cycle nodes, 2: isolated nodes) that match f */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_chain_query(EmitArgs a, int f, uint8_t which, uint64_t *kmers, uint64_t *inK,
+                                                      uint64_t *outK, uint32_t *inD, uint32_t *outD, uint64_t cap) {
+  constexpr int KWD = KOps<KT>::WORDS;
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < a.M; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    bool hit = false;
+    KT K{}, L{}, R{};
+    ChainState st{};
+    if (i < a.M && (a.removed ? a.removed[i] : 0) == which) {
+      st = a.cs[i];
+      K = KOps<KT>::load(a.ckey + i * KWD);
+      L = side_kmer<KT>(st.inP, a);
+      R = side_kmer<KT>(st.outP, a);
+      hit = chain_matches<KT>(f, K, L, R, st.inD, st.outD, a.k);
+    }
+    const unsigned long long o = block_append(hit, &a.ctr->n_k2_dump);
+    if (!hit || o >= cap) continue;
+    if (kmers) KOps<KT>::store(kmers + o * KWD, K);
+    if (inK) KOps<KT>::store(inK + o * KWD, L);
+    if (outK) KOps<KT>::store(outK + o * KWD, R);
+    if (inD) inD[o] = st.inD;
+    if (outD) outD[o] = st.outD;
+  }
+}
+
+template <class KT>
+bruno_status node_query_typed(Ctx *c, int f, bool erase, uint64_t *keys, uint16_t *counts, uint8_t *flags, size_t cap,
+                              size_t *n) {
+  bruno_status st;
+  const bool copy = !erase && (keys || counts || flags);
+  const uint64_t nb = std::max<uint64_t>(1, c->n_nodes);
+  Buf dk, dc, df;
+  if (copy) {
+    if ((st = ensure(c, dk, nb * 8 * c->W)) != BRUNO_OK) return st;
+    if ((st = ensure(c, dc, nb * 18)) != BRUNO_OK) return st;
+    if ((st = ensure(c, df, nb)) != BRUNO_OK) return st;
+  }
+  cudaMemsetAsync(&c->dctr->n_k2_dump, 0, 8, c->stream);
+  k_node_query<KT><<<sms_count() * 8, TPB, 0, c->stream>>>((uint64_t *)c->table.p, c->nslots, c->cfg.k, f, erase,
+                                                          (uint64_t *)dk.p, (uint16_t *)dc.p, (uint8_t *)df.p,
+                                                          copy ? nb : 0, c->dctr);
+  c->launches += 1;
+  bruno_status r = sync_counters(c);
+  const uint64_t hits = c->hctr->n_k2_dump;
+  if (n) *n = hits;
+  if (r == BRUNO_OK && copy) {
+    if (cap < hits) r = set_err(c, BRUNO_ERR_CAPACITY, "find_if buffers too small");
+    if (r == BRUNO_OK && keys) r = cuda_check(c, cudaMemcpyAsync(keys, dk.p, hits * 8 * c->W, cudaMemcpyDeviceToHost, c->stream), "copy");
+    if (r == BRUNO_OK && counts) r = cuda_check(c, cudaMemcpyAsync(counts, dc.p, hits * 18, cudaMemcpyDeviceToHost, c->stream), "copy");
+    if (r == BRUNO_OK && flags) r = cuda_check(c, cudaMemcpyAsync(flags, df.p, hits, cudaMemcpyDeviceToHost, c->stream), "copy");
+    if (r == BRUNO_OK) r = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  }
+  if (copy) { cudaFreeAsync(dk.p, c->stream); cudaFreeAsync(dc.p, c->stream); cudaFreeAsync(df.p, c->stream); }
+  return r;
+}
+
+template <class KT>
+bruno_status node_recount_typed(Ctx *c) {
+  cudaMemsetAsync(&c->dctr->n_nodes, 0, 8, c->stream);
+  cudaMemsetAsync(&c->dctr->n_branch, 0, 8, c->stream);
+  cudaMemsetAsync(&c->dctr->n_chain, 0, 8, c->stream);
+  k_node_recount<KT><<<sms_count() * 8, TPB, 0, c->stream>>>((uint64_t *)c->table.p, c->nslots, c->cfg.k, c->dctr);
+  c->launches += 1;
+  bruno_status st = sync_counters(c);
+  if (st != BRUNO_OK) return st;
+  c->n_nodes = c->hctr->n_nodes;
+  c->n_branch = c->hctr->n_branch;
+  c->chain_edges_done = false;   /* the chain ends' edge counts come from the node table */
+  return BRUNO_OK;
+}
+
+template <class KT>
+bruno_status erase_nodes_typed(Ctx *c, const uint64_t *kmers, size_t n) {
+  bruno_status st;
+  if (n) {
+    Buf dq;
+    if ((st = ensure(c, dq, n * 8 * c->W)) != BRUNO_OK) return st;
+    if ((st = cuda_check(c, cudaMemcpyAsync(dq.p, kmers, n * 8 * c->W, cudaMemcpyHostToDevice, c->stream), "copy")) !=
+        BRUNO_OK)
+      return st;
+    const int g = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms_count() * 8, (n + TPB - 1) / TPB));
+    k_erase_nodes<KT><<<g, TPB, 0, c->stream>>>((const uint64_t *)dq.p, n, (uint64_t *)c->table.p, c->geom, c->cfg.k);
+    c->launches += 1;
+    cudaFreeAsync(dq.p, c->stream);
+  }
+  return node_recount_typed<KT>(c);
+}
+
+template <class KT>
+bruno_status chain_query_typed(Ctx *c, int f, int which, uint64_t *kmers, uint64_t *inK, uint64_t *outK, uint32_t *inD,
+                               uint32_t *outD, size_t cap, size_t *n) {
+  bruno_status st;
+  const uint64_t M = c->n_chain, Mb = std::max<uint64_t>(1, M);
+  const bool copy = kmers || inK || outK || inD || outD;
+  Buf b0, b1, b2, b3, b4;
+  if (copy) {
+    if ((st = ensure(c, b0, Mb * 8 * c->W)) != BRUNO_OK) return st;
+    if ((st = ensure(c, b1, Mb * 8 * c->W)) != BRUNO_OK) return st;
+    if ((st = ensure(c, b2, Mb * 8 * c->W)) != BRUNO_OK) return st;
+    if ((st = ensure(c, b3, Mb * 4)) != BRUNO_OK) return st;
+    if ((st = ensure(c, b4, Mb * 4)) != BRUNO_OK) return st;
+  }
+  EmitArgs a{};
+  a.ckey = (const uint64_t *)c->ckey.p; a.cedge = (const uint8_t *)c->cedge.p; a.cs = (const ChainState *)c->cstate.p;
+  a.removed = c->stage >= 5 ? (const uint8_t *)c->removed.p : nullptr;
+  a.M = M; a.k = c->cfg.k; a.ctr = c->dctr;
+  cudaMemsetAsync(&c->dctr->n_k2_dump, 0, 8, c->stream);
+  if (M)
+    k_chain_query<KT><<<sms_count() * 8, TPB, 0, c->stream>>>(a, f, (uint8_t)which, (uint64_t *)b0.p, (uint64_t *)b1.p,
+                                                             (uint64_t *)b2.p, (uint32_t *)b3.p, (uint32_t *)b4.p,
+                                                             copy ? Mb : 0);
+  c->launches += 1;
+  bruno_status r = sync_counters(c);
+  const uint64_t hits = c->hctr->n_k2_dump;
+  if (n) *n = hits;
+  if (r == BRUNO_OK && copy) {
+    if (cap < hits) r = set_err(c, BRUNO_ERR_CAPACITY, "chain find_if buffers too small");
+    const size_t kb = hits * 8 * c->W;
+    if (r == BRUNO_OK && kmers) r = cuda_check(c, cudaMemcpyAsync(kmers, b0.p, kb, cudaMemcpyDeviceToHost, c->stream), "copy");
+    if (r == BRUNO_OK && inK) r = cuda_check(c, cudaMemcpyAsync(inK, b1.p, kb, cudaMemcpyDeviceToHost, c->stream), "copy");
+    if (r == BRUNO_OK && outK) r = cuda_check(c, cudaMemcpyAsync(outK, b2.p, kb, cudaMemcpyDeviceToHost, c->stream), "copy");
+    if (r == BRUNO_OK && inD) r = cuda_check(c, cudaMemcpyAsync(inD, b3.p, hits * 4, cudaMemcpyDeviceToHost, c->stream), "copy");
+    if (r == BRUNO_OK && outD) r = cuda_check(c, cudaMemcpyAsync(outD, b4.p, hits * 4, cudaMemcpyDeviceToHost, c->stream), "copy");
+    if (r == BRUNO_OK) r = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  }
+  if (copy) {
+    cudaFreeAsync(b0.p, c->stream); cudaFreeAsync(b1.p, c->stream); cudaFreeAsync(b2.p, c->stream);
+    cudaFreeAsync(b3.p, c->stream); cudaFreeAsync(b4.p, c->stream);
+  }
+  return r;
+}
+
 template <class KT>
 bruno_status clean_typed(Ctx *c, uint64_t *rounds, uint64_t *deadends, uint64_t *bubbles, uint64_t *edges,
                          int32_t *status) {
@@ -1997,6 +2284,21 @@ bruno_status run_chain_summaries(Ctx *c) {
   return c->W == 1 ? chain_summaries_typed<KW1>(c) : chain_summaries_typed<KW2>(c);
 }
 
+bruno_status run_node_query(Ctx *c, int filter, bool erase, uint64_t *keys, uint16_t *counts, uint8_t *flags,
+                            size_t cap, size_t *n) {
+  bruno_status st = c->W == 1 ? node_query_typed<KW1>(c, filter, erase, keys, counts, flags, cap, n)
+                              : node_query_typed<KW2>(c, filter, erase, keys, counts, flags, cap, n);
+  if (st != BRUNO_OK || !erase) return st;
+  return c->W == 1 ? node_recount_typed<KW1>(c) : node_recount_typed<KW2>(c);
+}
+bruno_status run_erase_nodes(Ctx *c, const uint64_t *kmers, size_t n) {
+  return c->W == 1 ? erase_nodes_typed<KW1>(c, kmers, n) : erase_nodes_typed<KW2>(c, kmers, n);
+}
+bruno_status run_chain_query(Ctx *c, int filter, int which, uint64_t *kmers, uint64_t *inK, uint64_t *outK,
+                             uint32_t *inD, uint32_t *outD, size_t cap, size_t *n) {
+  return c->W == 1 ? chain_query_typed<KW1>(c, filter, which, kmers, inK, outK, inD, outD, cap, n)
+                   : chain_query_typed<KW2>(c, filter, which, kmers, inK, outK, inD, outD, cap, n);
+}
 bruno_status run_clean(Ctx *c, uint64_t *rounds, uint64_t *deadends, uint64_t *bubbles, uint64_t *edges,
                        int32_t *status) {
   return c->W == 1 ? clean_typed<KW1>(c, rounds, deadends, bubbles, edges, status)

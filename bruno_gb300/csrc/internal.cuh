@@ -39,8 +39,18 @@ struct DevCounters {
    * with both ends on branches, erase queries, edges found, dead ends, bubble chains, live
    * nodes and live branch nodes after an erasure pass */
   unsigned long long cl_term, cl_nonzero, cl_sum, cl_norm, cl_q, cl_found, cl_dead, cl_bub, cl_live, cl_live_branch;
+  unsigned long long n_big, n_big_res; /* entries counted past 2^24 (keys in big_key), resolved */
   unsigned int hll[1 << 12];           /* HyperLogLog registers, p = 12 */
+  /* exact counts of (k-mer, biedge) entries past 2^24 occurrences: an entry word's count stops
+   * there and sets E_BIG, and every later occurrence adds 1 here, under the entry word's
+   * address (open addressing, key 0 = free); cleared before every counting pass */
+  unsigned long long big_key[1024];
+  unsigned long long big_cnt[1024];
 };
+constexpr int BIG_SLOTS = 1024;
+/* an entry counted past 2^24, resolved after counting: its table key (continuation mark
+ * cleared), its biedge code and its exact count (for the filtered-entry copy-out) */
+struct BigRes { uint64_t k0, k1; uint32_t code, pad; unsigned long long count; };
 
 struct Segment { const char *ptr; uint64_t n; int ev = -1; };   /* ev: copy-done event, -1 if none */
 
@@ -99,6 +109,8 @@ struct Ctx {
   bool h2d_pending = false;      /* ev[7] marks the start of this build's host-to-device copies */
   int force_direct_count = 0;    /* cfg.direct_count: 0 automatic, 1 whole table, 2 L2 partitions */
   Buf chain_list, branch_list;   /* slot indices, filled by the filter */
+  Buf bigres;                    /* BigRes per entry counted past 2^24 (n_big of them) */
+  uint64_t n_big = 0;
   Buf k1tab;                     /* the (k+1)-mer edge filter's (key, count) table */
   uint64_t k1slots = 0;
 
@@ -168,5 +180,15 @@ bruno_status run_chain_summaries(Ctx *c);
 bruno_status run_clean(Ctx *c, uint64_t *rounds, uint64_t *deadends, uint64_t *bubbles, uint64_t *edges,
                        int32_t *status);
 bruno_status run_copy_nodes(Ctx *c, uint64_t *keys, uint16_t *counts, uint8_t *flags, size_t cap, size_t *n);
+/* debruijn_graph::find_if / erase_if over the node table (filter: a bruno_node_filter); after an
+ * erasure the node counts and stored classifications are brought up to date */
+bruno_status run_node_query(Ctx *c, int filter, bool erase, uint64_t *keys, uint16_t *counts, uint8_t *flags,
+                            size_t cap, size_t *n);
+/* debruijn_graph_map::erase_nodes: host k-mers (either strand), with the edges back to them */
+bruno_status run_erase_nodes(Ctx *c, const uint64_t *kmers, size_t n);
+/* chain-map records of the nodes whose removed[] mark is `which` (0 chain map, 1 cycle, 2 isolated)
+ * matching a bruno_chain_filter */
+bruno_status run_chain_query(Ctx *c, int filter, int which, uint64_t *kmers, uint64_t *inK, uint64_t *outK,
+                             uint32_t *inD, uint32_t *outD, size_t cap, size_t *n);
 
 }  // namespace bg

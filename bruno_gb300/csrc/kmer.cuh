@@ -12,8 +12,9 @@
  *   KW1: 32 B = key u64 | 6 x u32 entry words
  *   KW2: 64 B = key lo u64 | key hi u64 | 12 x u32 entry words
  * During counting an entry word is [count:26 | biedge code:5 | big:1]: the code numbers the
- * canonical (in, out) pair 1..25 (0 = free entry) and `big` is set once the count passed
- * 2^25, after which the exact value is irrelevant (every consumer caps at 65535).  A k-mer
+ * canonical (in, out) pair 1..25 (0 = free entry) and `big` is set once the count reached
+ * 2^24: the word's count then stops and the rest is counted exactly in a side table (read only
+ * by the raw-count copy-out; every other consumer caps at 65535).  A k-mer
  * with more distinct biedges than one slot holds continues in later slots of its probe
  * sequence, keyed k-mer | CONT.  After the filter the slot holds the graph node instead:
  *   word after the key: counts[0..3] (u16: out A C G T), then counts[4..7] (in A C G T),
@@ -251,7 +252,7 @@ __device__ __forceinline__ uint8_t code_biedge(unsigned code) {
 constexpr uint32_t E_BIG = 1u;
 constexpr int E_CODE_SHIFT = 1;
 constexpr int E_COUNT_SHIFT = 6;
-constexpr uint32_t E_COUNT_BIG = 1u << 26;  /* stands for any count >= 2^25 */
+constexpr uint32_t E_COUNT_BIG = 1u << 26;  /* stands for any count >= 2^24 where only a cap matters */
 __device__ __forceinline__ unsigned entry_code(uint32_t e) { return (e >> E_CODE_SHIFT) & 31u; }
 __device__ __forceinline__ uint32_t entry_count(uint32_t e) {
   return (e & E_BIG) ? E_COUNT_BIG : (e >> E_COUNT_SHIFT);

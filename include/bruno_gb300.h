@@ -248,6 +248,67 @@ bruno_status bruno_copy_chain_edges(bruno_ctx *ctx, uint64_t *ends, uint16_t *fr
 bruno_status bruno_copy_chain_summaries(bruno_ctx *ctx, uint64_t *kmers, uint32_t *dist, uint8_t *flags, size_t cap,
                                         size_t *n);
 
+/* ---------------------------------------------------------------------------------------
+ * Graph and chain-map queries between the phases, as the reference driver makes them
+ * (compact_dbg_freq_construct_clean.cpp:599-610, 794-807).  Predicates are tag values. */
+
+/* Node predicates of bliss::debruijn::filter::graph (src/debruijn/debruijn_graph_filters.hpp),
+ * evaluated on a node's canonical k-mer and its current edge counts. */
+typedef enum bruno_node_filter {
+  BRUNO_NODES_ALL = 0,              /* every node */
+  BRUNO_IS_K_PALINDROME = 1,        /* IsKPalindrome (:38-55) */
+  BRUNO_IS_KPLUS1_PALINDROME = 2,   /* IsKplus1Palindrome (:57-140) */
+  BRUNO_IS_BRANCH_POINT = 3,        /* IsBranchPoint (:142-160) */
+  BRUNO_IS_ISOLATED_NODE = 4,       /* IsIsolated (:163-172): no in and no out edge */
+  BRUNO_IS_CHAIN_INTERNAL_NODE = 5, /* IsChainInternalNode (:189-203) */
+  BRUNO_IS_CHAIN_NODE = 6           /* IsChainNode (:206-220) */
+} bruno_node_filter;
+
+/* debruijn_graph::find_if(pred) (debruijn_graph.hpp:193-196): the matching nodes, in the format of
+ * bruno_copy_nodes (flags evaluated on the current counts).  Size-query pattern.  After
+ * bruno_local_insert_by_freqencies. */
+bruno_status bruno_graph_find_if(bruno_ctx *ctx, int32_t filter, uint64_t *keys, uint16_t *counts, uint8_t *flags,
+                                 size_t cap, size_t *n);
+/* debruijn_graph::erase_if(pred) (:247-250): the matching nodes leave the graph (their neighbours'
+ * edges stay, as the reference's plain erase leaves them).  *n_erased may be NULL. */
+bruno_status bruno_graph_erase_if(bruno_ctx *ctx, int32_t filter, size_t *n_erased);
+/* debruijn_graph_map::erase_nodes(query) (debruijn_graph_map.hpp:833-836): each k-mer of the host
+ * array (n of them, either strand, `words` uint64 each) that is a node leaves the graph, and its
+ * neighbours lose their edges to it (erase_nodes_and_edges, :811-827). */
+bruno_status bruno_graph_erase_nodes(bruno_ctx *ctx, const uint64_t *kmers, size_t n);
+
+/* Chain-map predicates of bliss::debruijn::filter::chain (src/debruijn/debruijn_chain_filters.hpp),
+ * evaluated on a chain-map record (k-mer, in k-mer, out k-mer, in distance, out distance). */
+typedef enum bruno_chain_filter {
+  BRUNO_CHAIN_ALL = 0,                              /* every record */
+  BRUNO_CHAIN_IS_UNIT_LENGTH = 1,                   /* IsUnitLength (:37-46) */
+  BRUNO_CHAIN_IS_ISOLATED = 2,                      /* IsIsolated (:49-58) */
+  BRUNO_CHAIN_IS_TERMINUS = 3,                      /* IsTerminus (:60-69) */
+  BRUNO_CHAIN_IS_INTERNAL = 4,                      /* IsInternal (:71-82) */
+  BRUNO_CHAIN_IS_TERMINUS_OR_ISOLATED = 5,          /* IsTerminusOrIsolated (:84-97) */
+  BRUNO_CHAIN_IS_CANONICAL_TERMINUS = 6,            /* IsCanonicalTerminus (:100-122) */
+  BRUNO_CHAIN_IS_CANONICAL_TERMINUS_OR_ISOLATED = 7,/* IsCanonicalTerminusOrIsolated (:125-147) */
+  BRUNO_CHAIN_POINTS_TO_TERMINI = 8,                /* PointsToTermini (:153-165) */
+  BRUNO_CHAIN_POINTS_TO_INTERNAL_NODE = 9           /* PointsToInternalNode (:169-186) */
+} bruno_chain_filter;
+
+/* debruijn_chain_graph::find_if(pred) (debruijn_chain_graph.hpp:306-311): the chain-map records
+ * simple_biedge<K> = (inK, outK, inDist, outDist) (debruijn_chain_node.hpp:49-50) of the matching
+ * nodes, keyed by the canonical k-mer; inK / outK are on the key's strand, the all-A k-mer where
+ * the node has no neighbour; distances carry the terminal mark in their top bit.  After
+ * bruno_extract_chains (the records before ranking) or after bruno_list_rank (the ranked
+ * records; cycle and isolated nodes have left the chain map by then).  Size-query pattern; any
+ * output may be NULL. */
+bruno_status bruno_chain_find_if(bruno_ctx *ctx, int32_t filter, uint64_t *kmers, uint64_t *in_kmers,
+                                 uint64_t *out_kmers, uint32_t *in_dist, uint32_t *out_dist, size_t cap, size_t *n);
+/* get_cycle_node_kmers (debruijn_chain_graph.hpp:448-460): the k-mers separate_cycles took out of
+ * the chain map in the last ranking.  Size-query pattern. */
+bruno_status bruno_get_cycle_node_kmers(bruno_ctx *ctx, uint64_t *kmers, size_t cap, size_t *n);
+/* get_isolated (:462-468): the chain-map records separate_isolated took out, as bruno_chain_find_if
+ * gives records.  Size-query pattern. */
+bruno_status bruno_get_isolated(bruno_ctx *ctx, uint64_t *kmers, uint64_t *in_kmers, uint64_t *out_kmers,
+                                uint32_t *in_dist, uint32_t *out_dist, size_t cap, size_t *n);
+
 /* Page-locked host memory, for fast host<->device copies of FASTQ input and results. */
 bruno_status bruno_host_alloc(size_t bytes, void **out);
 bruno_status bruno_host_free(void *p);

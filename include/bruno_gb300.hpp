@@ -7,10 +7,16 @@
  *   bliss::debruijn::graph::debruijn_graph<K,uint16_t>     bruno_gb300::debruijn_graph
  *     .get_map().compute_biedge_freqencies(nodes, k2)        .get_map().compute_biedge_freqencies()
  *     .get_map().local_insert_by_freqencies(k2, threshes)    .get_map().local_insert_by_freqencies(threshes)
+ *     .find_if(pred) / .erase_if(pred)                       same, pred a tag of bruno_gb300::filter::graph
+ *     .get_map().erase_nodes(kmers)                          same
  *   bliss::debruijn::graph::debruijn_chain_graph<K>        bruno_gb300::debruijn_chain_graph
  *     .extract_chains(idx)                                   .extract_chains(idx)
  *     .list_rank_min_update() / .list_rank()                 same
  *     .to_ranked_chain_nodes() / .to_compressed_chains()     same
+ *     .find_if(pred)                                         same, pred a tag of bruno_gb300::filter::chain
+ *     .get_cycle_node_kmers() / .get_isolated()              same
+ *     .get_internal_node_kmers()                             same
+ *   bliss::debruijn::filter::graph::IsBranchPoint, ...     bruno_gb300::filter::graph::IsBranchPoint, ...
  *
  * The reference's (k-mer, biedge) vector and k2 counter are not materialised on the host:
  * they live in device memory inside the context.  Errors become bruno_gb300::error
@@ -56,6 +62,44 @@ inline std::vector<uint64_t> thresholds(const std::vector<uint64_t> &lower, cons
   return t;
 }
 
+/* The reference's predicate structs as tag types: each names the C ABI's predicate number. */
+namespace filter {
+namespace graph {   /* bliss::debruijn::filter::graph (src/debruijn/debruijn_graph_filters.hpp) */
+struct IsKPalindrome { static constexpr int32_t value = BRUNO_IS_K_PALINDROME; };
+struct IsKplus1Palindrome { static constexpr int32_t value = BRUNO_IS_KPLUS1_PALINDROME; };
+struct IsBranchPoint { static constexpr int32_t value = BRUNO_IS_BRANCH_POINT; };
+struct IsIsolated { static constexpr int32_t value = BRUNO_IS_ISOLATED_NODE; };
+struct IsChainInternalNode { static constexpr int32_t value = BRUNO_IS_CHAIN_INTERNAL_NODE; };
+struct IsChainNode { static constexpr int32_t value = BRUNO_IS_CHAIN_NODE; };
+}  // namespace graph
+namespace chain {   /* bliss::debruijn::filter::chain (src/debruijn/debruijn_chain_filters.hpp) */
+struct IsUnitLength { static constexpr int32_t value = BRUNO_CHAIN_IS_UNIT_LENGTH; };
+struct IsIsolated { static constexpr int32_t value = BRUNO_CHAIN_IS_ISOLATED; };
+struct IsTerminus { static constexpr int32_t value = BRUNO_CHAIN_IS_TERMINUS; };
+struct IsInternal { static constexpr int32_t value = BRUNO_CHAIN_IS_INTERNAL; };
+struct IsTerminusOrIsolated { static constexpr int32_t value = BRUNO_CHAIN_IS_TERMINUS_OR_ISOLATED; };
+struct IsCanonicalTerminus { static constexpr int32_t value = BRUNO_CHAIN_IS_CANONICAL_TERMINUS; };
+struct IsCanonicalTerminusOrIsolated { static constexpr int32_t value = BRUNO_CHAIN_IS_CANONICAL_TERMINUS_OR_ISOLATED; };
+struct PointsToTermini { static constexpr int32_t value = BRUNO_CHAIN_POINTS_TO_TERMINI; };
+struct PointsToInternalNode { static constexpr int32_t value = BRUNO_CHAIN_POINTS_TO_INTERNAL_NODE; };
+}  // namespace chain
+}  // namespace filter
+
+/* (k-mer, compact_multi_biedge) records of find_if: keys (words each), counts (9 each), flags */
+struct node_records {
+  std::vector<uint64_t> keys;
+  std::vector<uint16_t> counts;
+  std::vector<uint8_t> flags;
+  size_t size() const { return flags.size(); }
+};
+
+/* (k-mer, simple_biedge<K>) records of the chain map: K, inK, outK (words each), inDist, outDist */
+struct chain_records {
+  std::vector<uint64_t> K, inK, outK;
+  std::vector<uint32_t> inD, outD;
+  size_t size() const { return inD.size(); }
+};
+
 /* one graph build on one GPU; the graph map and the chain graph share it */
 class context {
  public:
@@ -97,6 +141,11 @@ class debruijn_graph_map {
     return c_.sizes().n_nodes;
   }
   size_t local_size() const { return c_.sizes().n_nodes; }
+  /* erase_nodes(query) (:833-836): the nodes (k-mers of either strand, words each) and, on their
+   * neighbours, the edges back to them */
+  void erase_nodes(const std::vector<uint64_t> &query) {
+    check(bruno_graph_erase_nodes(c_.get(), query.data(), query.size() / c_.words()), c_.get(), "erase_nodes");
+  }
   /* the node table: k-mers (words per node) and counts[9] (out ACGT, in ACGT, self) */
   void to_vector(std::vector<uint64_t> &keys, std::vector<uint16_t> &counts, std::vector<uint8_t> &flags) const {
     size_t n = 0;
@@ -115,7 +164,26 @@ class debruijn_graph {
   explicit debruijn_graph(context &c) : c_(c), map_(c) {}
   debruijn_graph_map &get_map() { return map_; }
   size_t size() const { return map_.local_size(); }
+  size_t local_size() const { return map_.local_size(); }
   context &ctx() { return c_; }
+  /* find_if(pred) (debruijn_graph.hpp:193-196) */
+  template <typename Pred>
+  node_records find_if(const Pred &) const {
+    node_records r;
+    size_t n = 0;
+    check(bruno_graph_find_if(c_.get(), Pred::value, nullptr, nullptr, nullptr, 0, &n), c_.get(), "find_if");
+    r.keys.resize(n * c_.words()); r.counts.resize(n * 9); r.flags.resize(n);
+    check(bruno_graph_find_if(c_.get(), Pred::value, r.keys.data(), r.counts.data(), r.flags.data(), n, &n), c_.get(),
+          "find_if");
+    return r;
+  }
+  /* erase_if(pred) (:247-250): the matching nodes; returns how many */
+  template <typename Pred>
+  size_t erase_if(const Pred &) {
+    size_t n = 0;
+    check(bruno_graph_erase_if(c_.get(), Pred::value, &n), c_.get(), "erase_if");
+    return n;
+  }
 
  private:
   context &c_;
@@ -137,6 +205,21 @@ class debruijn_chain_graph {
   size_t list_rank_min_update() { return rank(1); }
   size_t list_rank() { return rank(0); }
   size_t size() const { return c_.sizes().n_ranked; }
+  /* find_if(pred) (debruijn_chain_graph.hpp:306-311) over the chain map */
+  template <typename Pred>
+  chain_records find_if(const Pred &) const { return records(Pred::value, 0); }
+  /* get_cycle_node_kmers (:448-460): words per k-mer */
+  std::vector<uint64_t> get_cycle_node_kmers() const {
+    size_t n = 0;
+    check(bruno_get_cycle_node_kmers(c_.get(), nullptr, 0, &n), c_.get(), "get_cycle_node_kmers");
+    std::vector<uint64_t> k(n * c_.words());
+    check(bruno_get_cycle_node_kmers(c_.get(), k.data(), n, &n), c_.get(), "get_cycle_node_kmers");
+    return k;
+  }
+  /* get_isolated (:462-468) */
+  chain_records get_isolated() const { return records(-1, 2); }
+  /* get_internal_node_kmers (:410-415): the k-mers of IsInternal records */
+  std::vector<uint64_t> get_internal_node_kmers() const { return find_if(filter::chain::IsInternal()).K; }
   listranked_chain_nodes to_ranked_chain_nodes() {
     compress();
     listranked_chain_nodes r;
@@ -202,6 +285,19 @@ class debruijn_chain_graph {
     check(bruno_list_rank(c_.get(), min_update, &it), c_.get(), "list_rank");
     ranked_ = false;
     return it;
+  }
+  chain_records records(int32_t filter, int which) const {
+    chain_records r;
+    size_t n = 0;
+    auto call = [&](uint64_t *K, uint64_t *inK, uint64_t *outK, uint32_t *inD, uint32_t *outD, size_t cap) {
+      return which == 2 ? bruno_get_isolated(c_.get(), K, inK, outK, inD, outD, cap, &n)
+                        : bruno_chain_find_if(c_.get(), filter, K, inK, outK, inD, outD, cap, &n);
+    };
+    check(call(nullptr, nullptr, nullptr, nullptr, nullptr, 0), c_.get(), "chain find_if");
+    const size_t w = c_.words();
+    r.K.resize(n * w); r.inK.resize(n * w); r.outK.resize(n * w); r.inD.resize(n); r.outD.resize(n);
+    check(call(r.K.data(), r.inK.data(), r.outK.data(), r.inD.data(), r.outD.data(), n), c_.get(), "chain find_if");
+    return r;
   }
   void compress() {
     if (!ranked_) {

@@ -307,6 +307,7 @@ struct Run {
 
   const uint64_t clean_k1_lo;   /* threshes[2] as the driver passed it, whatever the filter used */
   std::vector<W> cycle_kmers;   /* get_cycle_node_kmers after the last list ranking */
+  std::vector<std::pair<W, ChainNode<W>>> isolated_recs;   /* get_isolated after the last ranking */
 
   Run(const oracle_cfg &c, oracle_result *r, uint64_t k1_lo)
       : cfg(c), T(c.threads > 0 ? c.threads : 1), ko(c.k), res(r), clean_k1_lo(k1_lo) {}
@@ -821,6 +822,7 @@ struct Run {
         if (chain[s].state[i] == 1 && unfinished(chain[s].vals[i])) any_unfinished = true;
     std::vector<uint64_t> ncy(T, 0), niso(T, 0);
     std::vector<std::vector<W>> cyk(T);
+    std::vector<std::vector<std::pair<W, ChainNode<W>>>> isok(T);
     const uint32_t maxd = 0x1u << iterations;
     parallel(T, [&](int s) {
       for (size_t i = 0; i < chain[s].keys.size(); ++i) {
@@ -834,12 +836,18 @@ struct Run {
       for (size_t i = 0; i < chain[s].keys.size(); ++i) {
         if (chain[s].state[i] != 1) continue;
         const ChainNode<W> &x = chain[s].vals[i];
-        if (points_to_self(x.inD) && points_to_self(x.outD)) { chain[s].erase_slot(i); ++niso[s]; }
+        if (points_to_self(x.inD) && points_to_self(x.outD)) {
+          isok[s].push_back({chain[s].keys[i].v, x});
+          chain[s].erase_slot(i);
+          ++niso[s];
+        }
       }
     });
     for (int s = 0; s < T; ++s) { res->n_cycle_nodes += ncy[s]; res->n_isolated += niso[s]; }
     cycle_kmers.clear();
     for (int s = 0; s < T; ++s) cycle_kmers.insert(cycle_kmers.end(), cyk[s].begin(), cyk[s].end());
+    isolated_recs.clear();
+    for (int s = 0; s < T; ++s) isolated_recs.insert(isolated_recs.end(), isok[s].begin(), isok[s].end());
     res->seconds[ORACLE_T_LIST_RANK] = now() - t0;
   }
 
@@ -1370,6 +1378,44 @@ struct Run {
     res = top;
   }
 
+  /* ====================================================== chain-map outputs */
+  static void put_records(std::vector<std::pair<W, ChainNode<W>>> &v, int w, uint64_t *n, uint64_t **keys,
+                          uint64_t **in, uint64_t **out, uint32_t **ind, uint32_t **outd) {
+    std::sort(v.begin(), v.end(), [](const std::pair<W, ChainNode<W>> &a, const std::pair<W, ChainNode<W>> &b) {
+      return a.first < b.first;
+    });
+    *n = v.size();
+    *keys = (uint64_t *)calloc(v.size() * w + 1, 8);
+    *in = (uint64_t *)calloc(v.size() * w + 1, 8);
+    *out = (uint64_t *)calloc(v.size() * w + 1, 8);
+    *ind = (uint32_t *)calloc(v.size() + 1, 4);
+    *outd = (uint32_t *)calloc(v.size() + 1, 4);
+    for (size_t i = 0; i < v.size(); ++i) {
+      store_word(*keys + i * w, v[i].first, w);
+      store_word(*in + i * w, v[i].second.inK, w);
+      store_word(*out + i * w, v[i].second.outK, w);
+      (*ind)[i] = v[i].second.inD;
+      (*outd)[i] = v[i].second.outD;
+    }
+  }
+  void export_chain_map() {
+    const int w = res->words;
+    std::vector<std::pair<W, ChainNode<W>>> v;
+    for (int s = 0; s < T; ++s)
+      for (size_t i = 0; i < chain[s].keys.size(); ++i)
+        if (chain[s].state[i] == 1) v.emplace_back(chain[s].keys[i].v, chain[s].vals[i]);
+    put_records(v, w, &res->n_chain_map, &res->cm_keys, &res->cm_in, &res->cm_out, &res->cm_in_dist,
+                &res->cm_out_dist);
+    std::vector<std::pair<W, ChainNode<W>>> iso(isolated_recs);
+    put_records(iso, w, &res->n_isolated_recs, &res->iso_keys, &res->iso_in, &res->iso_out, &res->iso_in_dist,
+                &res->iso_out_dist);
+    std::vector<W> cyc(cycle_kmers);
+    std::sort(cyc.begin(), cyc.end());
+    res->n_cycle_kmers = cyc.size();
+    res->cycle_keys = (uint64_t *)calloc(cyc.size() * w + 1, 8);
+    for (size_t i = 0; i < cyc.size(); ++i) store_word(res->cycle_keys + i * w, cyc[i], w);
+  }
+
   /* ====================================================== table outputs */
   void export_tables(bool graph_only = false) {
     const int w = res->words;
@@ -1430,6 +1476,7 @@ struct Run {
     chain_edges();
     chain_summaries();
     export_tables();
+    export_chain_map();
     if (cfg.clean) clean();
     return 0;
   }
@@ -1491,6 +1538,9 @@ extern "C" void oracle_free(oracle_result *r) {
   free(r->edge_L); free(r->edge_R); free(r->edge_freqs);
   free(r->sum_kmers); free(r->sum_dist); free(r->sum_flags);
   oracle_free(r->clean);
+  free(r->cm_keys); free(r->cm_in); free(r->cm_out); free(r->cm_in_dist); free(r->cm_out_dist);
+  free(r->iso_keys); free(r->iso_in); free(r->iso_out); free(r->iso_in_dist); free(r->iso_out_dist);
+  free(r->cycle_keys);
   free(r);
 }
 

@@ -110,6 +110,18 @@ typedef struct oracle_result {
                                reference throws on */
   struct oracle_result *clean;  /* the cleaned graph: node table (cycles and isolated nodes
                                    removed), ranked chain nodes, chains and chain edges */
+
+  /* the chain map after list ranking (separate_cycles and separate_isolated have taken their
+   * nodes out), sorted by k-mer: per node simple_biedge<K> = (inK, outK, inDist, outDist)
+   * (debruijn_chain_node.hpp:49-50); then the records separate_isolated took out (get_isolated,
+   * debruijn_chain_graph.hpp:462-468), and the k-mers separate_cycles took out
+   * (get_cycle_node_kmers, :448-460), both sorted by k-mer */
+  uint64_t n_chain_map;
+  uint64_t *cm_keys, *cm_in, *cm_out; uint32_t *cm_in_dist, *cm_out_dist;
+  uint64_t n_isolated_recs;
+  uint64_t *iso_keys, *iso_in, *iso_out; uint32_t *iso_in_dist, *iso_out_dist;
+  uint64_t n_cycle_kmers;
+  uint64_t *cycle_keys;
 } oracle_result;
 
 /* Runs the whole path on an in-memory FASTQ buffer.  Returns 0 on success. */

@@ -52,6 +52,11 @@ _Res._fields_ = [
         ("seconds", ctypes.c_double * 6),
         ("clean_rounds", ctypes.c_uint64), ("clean_deadends", ctypes.c_uint64), ("clean_bubbles", ctypes.c_uint64),
         ("clean_edges", ctypes.c_uint64), ("clean_status", ctypes.c_int32), ("clean", ctypes.POINTER(_Res)),
+        ("n_chain_map", ctypes.c_uint64), ("cm_keys", _U64P), ("cm_in", _U64P), ("cm_out", _U64P),
+        ("cm_in_dist", ctypes.POINTER(ctypes.c_uint32)), ("cm_out_dist", ctypes.POINTER(ctypes.c_uint32)),
+        ("n_isolated_recs", ctypes.c_uint64), ("iso_keys", _U64P), ("iso_in", _U64P), ("iso_out", _U64P),
+        ("iso_in_dist", ctypes.POINTER(ctypes.c_uint32)), ("iso_out_dist", ctypes.POINTER(ctypes.c_uint32)),
+        ("n_cycle_kmers", ctypes.c_uint64), ("cycle_keys", _U64P),
     ]
 
 
@@ -132,6 +137,14 @@ def _graph(r, keep_k2: bool = False, keep_filtered: bool = False) -> dict:
     ne = r.n_chain_edges
     out["chain_edges"] = (_arr(r.edge_L, ne * w, np.uint64, (ne, w)), _arr(r.edge_R, ne * w, np.uint64, (ne, w)),
                           _arr(r.edge_freqs, ne * 11, np.uint16, (ne, 11)))
+
+    def records(n, keys, inK, outK, inD, outD):
+        return (_arr(keys, n * w, np.uint64, (n, w)), _arr(inK, n * w, np.uint64, (n, w)),
+                _arr(outK, n * w, np.uint64, (n, w)), _arr(inD, n, np.uint32), _arr(outD, n, np.uint32))
+    # the chain map after ranking, the isolated records and the cycle k-mers, each sorted by k-mer
+    out["chain_map"] = records(r.n_chain_map, r.cm_keys, r.cm_in, r.cm_out, r.cm_in_dist, r.cm_out_dist)
+    out["isolated"] = records(r.n_isolated_recs, r.iso_keys, r.iso_in, r.iso_out, r.iso_in_dist, r.iso_out_dist)
+    out["cycle_kmers"] = _arr(r.cycle_keys, r.n_cycle_kmers * w, np.uint64, (r.n_cycle_kmers, w))
     return out
 
 
