@@ -74,6 +74,11 @@ class _DeviceView(ctypes.Structure):
                 ("words", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
+class _IndexCheck(ctypes.Structure):
+    _fields_ = [("n_query", ctypes.c_uint64), ("n_absent", ctypes.c_uint64), ("n_unreferenced", ctypes.c_uint64),
+                ("n_unanswered", ctypes.c_uint64), ("edge_hist", ctypes.c_uint64 * 25)]
+
+
 _lib: Optional[ctypes.CDLL] = None
 
 # every entry point of include/bruno_gb300.h
@@ -86,7 +91,7 @@ EXPORTS = (
     "bruno_count_biedges_noalloc", "bruno_pool_create", "bruno_pool_submit", "bruno_pool_wait",
     "bruno_pool_result_free", "bruno_pool_destroy", "bruno_clean_deadend_and_bubbles_naive",
     "bruno_device_results", "bruno_graph_find_if", "bruno_graph_erase_if", "bruno_graph_erase_nodes",
-    "bruno_chain_find_if", "bruno_get_cycle_node_kmers", "bruno_get_isolated",
+    "bruno_chain_find_if", "bruno_get_cycle_node_kmers", "bruno_get_isolated", "bruno_check_index",
 )
 
 # node predicates (bliss::debruijn::filter::graph) and chain predicates
@@ -133,6 +138,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "bruno_graph_erase_nodes": [P, P, SZ],
         "bruno_chain_find_if": [P, I32, P, P, P, P, P, SZ, PSZ],
         "bruno_get_cycle_node_kmers": [P, P, SZ, PSZ], "bruno_get_isolated": [P, P, P, P, P, P, SZ, PSZ],
+        "bruno_check_index": [P, ctypes.POINTER(_IndexCheck)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -396,6 +402,18 @@ class Graph:
         return keys, counts, flags
 
     # ------------------------------------------------- graph and chain-map queries
+    def check_index(self) -> dict:
+        """check_index (compact_dbg_stats.hpp:45-119) and the edge-count histogram; "ok" is False
+        where the reference's debug build would assert (the library returns BRUNO_ERR_INVARIANT)"""
+        r = _IndexCheck()
+        st = self.lib.bruno_check_index(self.ctx, ctypes.byref(r))
+        if st not in (0, 6):
+            self._check(st, "check_index")
+        d = {n: int(getattr(r, n)) for n, _ in _IndexCheck._fields_ if n != "edge_hist"}
+        d["edge_hist"] = list(r.edge_hist)
+        d["ok"] = st == 0
+        return d
+
     def find_if(self, pred: str):
         """debruijn_graph::find_if(pred): the matching nodes as nodes() gives them"""
         f = NODE_FILTERS[pred]

@@ -149,7 +149,7 @@ bruno_status bruno_ctx_destroy(bruno_ctx *c) {
                  &c->cstate, &c->cstate2, &c->pend, &c->pay, &c->unf0, &c->unf1, &c->removed, &c->r_K, &c->r_rep, &c->r_dist,
                  &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list, &c->e_ends, &c->e_freqs, &c->s_kmers, &c->s_dist, &c->s_flags, &c->k1tab,
                  &c->cl_trec, &c->cl_tslot, &c->cl_sums, &c->cl_norm, &c->cl_htab, &c->cl_q, &c->cl_found,
-                 &c->records, &c->bucket_cnt, &c->records2, &c->sub_cnt};
+                 &c->records, &c->bucket_cnt, &c->records2, &c->sub_cnt, &c->bigres};
   for (Buf *b : bufs) release(*b);
   for (Buf &b : c->seg_bufs) release(b);
   if (c->dctr) cudaFree(c->dctr);
@@ -555,6 +555,16 @@ bruno_status bruno_graph_erase_if(bruno_ctx *c, int32_t filter, size_t *n_erased
   const bruno_status st = run_node_query(c, filter, true, nullptr, nullptr, nullptr, 0, &n);
   if (n_erased) *n_erased = n;
   return st;
+}
+
+bruno_status bruno_check_index(bruno_ctx *c, bruno_index_check *out) {
+  if (!c || !out) return BRUNO_ERR_ARG;
+  if (c->stage < 3) return set_err(c, BRUNO_ERR_ARG, "nodes exist after local_insert_by_freqencies");
+  const bruno_status st = run_check_index(c, out);
+  if (st != BRUNO_OK) return st;
+  if (out->n_absent || out->n_unreferenced)
+    return set_err(c, BRUNO_ERR_INVARIANT, "check_index: the graph names absent neighbours or holds unnamed nodes");
+  return BRUNO_OK;
 }
 
 bruno_status bruno_graph_erase_nodes(bruno_ctx *c, const uint64_t *kmers, size_t n) {

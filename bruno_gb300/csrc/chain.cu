@@ -1899,6 +1899,107 @@ __global__ void __launch_bounds__(TPB) k_chain_query(EmitArgs a, int f, uint8_t 
   }
 }
 
+/* check_index (test/common/compact_dbg_stats.hpp:45-119): every neighbour k-mer that a node's
+ * edges name (get_out_neighbors / get_in_neighbors, canonical) must be a node, and every node
+ * with an edge must be named by some node; also counted: edges whose neighbour lacks the edge
+ * back, and the in x out edge-count histogram of print_compact_multi_biedge_histogram
+ * (debruijn_stats.hpp:39-74).  `ref` gets one bit per table slot named as a neighbour. */
+struct IndexCheck { unsigned long long query, absent, unreferenced, unanswered, hist[25]; };
+
+template <class KT>
+__device__ __forceinline__ bool has_edge(const uint64_t *table, long long sl, unsigned e) {
+  constexpr int KWD = Slot<KT>::KEYW, SU = Slot<KT>::U64;
+  const uint64_t *pw = table + (uint64_t)sl * SU + KWD;
+  const unsigned out = e & 0xFu, in = (e >> 4) & 0xFu;
+  if (single16(out) && !count_at(pw[0], __ffs(out) - 1)) return false;
+  if (single16(in) && !count_at(pw[1], __ffs(in) - 1)) return false;
+  return true;
+}
+
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_check_refs(const uint64_t *table, uint64_t nslots, TableGeom g, int k,
+                                                     uint32_t *ref, IndexCheck *out) {
+  constexpr int KWD = Slot<KT>::KEYW, SU = Slot<KT>::U64;
+  __shared__ unsigned long long s_hist[25];
+  for (int i = threadIdx.x; i < 25; i += blockDim.x) s_hist[i] = 0;
+  __syncthreads();
+  unsigned long long q = 0, absent = 0, unanswered = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t *s = table + i * SU;
+    if (!key_is_node(KOps<KT>::load(s))) continue;
+    const KT K = key_kmer(node_key(KOps<KT>::load(s)));
+    const uint64_t ow = s[KWD], iw = s[KWD + 1];
+    unsigned din = 0, dout = 0;
+    for (unsigned c = 0; c < 4; ++c) {
+      for (int side = 0; side < 2; ++side) {
+        if (!count_at(side ? iw : ow, c)) continue;
+        ++q;
+        side ? ++din : ++dout;
+        /* the neighbour and the edge it should have back: K.c has an in edge from first(K);
+         * c.K has an out edge to last(K) */
+        KT y = side ? KOps<KT>::prepend(c, K, k) : KOps<KT>::append(K, c, k);
+        unsigned e = side ? (1u << KOps<KT>::last(K)) : ((1u << KOps<KT>::first(K, k)) << 4);
+        canon_edge(y, e, k);
+        const long long sl = table_find<KT>(table, g, 4096u, y);
+        if (sl < 0) { ++absent; continue; }
+        atomicOr(&ref[(uint64_t)sl >> 5], 1u << ((uint64_t)sl & 31));
+        if (!has_edge<KT>(table, sl, e)) ++unanswered;
+      }
+    }
+    atomicAdd(&s_hist[din * 5 + dout], 1ull);
+  }
+  q = warp_sum(q); absent = warp_sum(absent); unanswered = warp_sum(unanswered);
+  if ((threadIdx.x & 31) == 0) {
+    if (q) atomicAdd(&out->query, q);
+    if (absent) atomicAdd(&out->absent, absent);
+    if (unanswered) atomicAdd(&out->unanswered, unanswered);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 25; i += blockDim.x)
+    if (s_hist[i]) atomicAdd(&out->hist[i], s_hist[i]);
+}
+
+/* the second check: nodes with an edge that no node named */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_check_unreferenced(const uint64_t *table, uint64_t nslots,
+                                                             const uint32_t *ref, IndexCheck *out) {
+  constexpr int KWD = Slot<KT>::KEYW, SU = Slot<KT>::U64;
+  unsigned long long n = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t *s = table + i * SU;
+    if (!key_is_node(KOps<KT>::load(s))) continue;
+    if (s[KWD] == 0 && s[KWD + 1] == 0) continue;   /* IsIsolated: erased before the check */
+    if (!(ref[i >> 5] & (1u << (i & 31)))) ++n;
+  }
+  n = warp_sum(n);
+  if ((threadIdx.x & 31) == 0 && n) atomicAdd(&out->unreferenced, n);
+}
+
+template <class KT>
+bruno_status check_index_typed(Ctx *c, bruno_index_check *o) {
+  bruno_status st;
+  Buf ref, res;
+  const uint64_t words = (c->nslots + 31) / 32 + 1;
+  if ((st = ensure(c, ref, words * 4)) != BRUNO_OK) return st;
+  if ((st = ensure(c, res, sizeof(IndexCheck))) != BRUNO_OK) return st;
+  cudaMemsetAsync(ref.p, 0, words * 4, c->stream);
+  cudaMemsetAsync(res.p, 0, sizeof(IndexCheck), c->stream);
+  k_check_refs<KT><<<sms_count() * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, c->geom, c->cfg.k,
+                                                          (uint32_t *)ref.p, (IndexCheck *)res.p);
+  k_check_unreferenced<KT><<<sms_count() * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots,
+                                                                  (const uint32_t *)ref.p, (IndexCheck *)res.p);
+  c->launches += 2;
+  IndexCheck h{};
+  st = cuda_check(c, cudaMemcpyAsync(&h, res.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "copy");
+  if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "check_index");
+  cudaFreeAsync(ref.p, c->stream);
+  cudaFreeAsync(res.p, c->stream);
+  if (st != BRUNO_OK) return st;
+  o->n_query = h.query; o->n_absent = h.absent; o->n_unreferenced = h.unreferenced; o->n_unanswered = h.unanswered;
+  for (int i = 0; i < 25; ++i) o->edge_hist[i] = h.hist[i];
+  return BRUNO_OK;
+}
+
 template <class KT>
 bruno_status node_query_typed(Ctx *c, int f, bool erase, uint64_t *keys, uint16_t *counts, uint8_t *flags, size_t cap,
                               size_t *n) {
@@ -2290,6 +2391,9 @@ bruno_status run_node_query(Ctx *c, int filter, bool erase, uint64_t *keys, uint
                               : node_query_typed<KW2>(c, filter, erase, keys, counts, flags, cap, n);
   if (st != BRUNO_OK || !erase) return st;
   return c->W == 1 ? node_recount_typed<KW1>(c) : node_recount_typed<KW2>(c);
+}
+bruno_status run_check_index(Ctx *c, bruno_index_check *out) {
+  return c->W == 1 ? check_index_typed<KW1>(c, out) : check_index_typed<KW2>(c, out);
 }
 bruno_status run_erase_nodes(Ctx *c, const uint64_t *kmers, size_t n) {
   return c->W == 1 ? erase_nodes_typed<KW1>(c, kmers, n) : erase_nodes_typed<KW2>(c, kmers, n);

@@ -184,6 +184,8 @@ bruno_status run_copy_nodes(Ctx *c, uint64_t *keys, uint16_t *counts, uint8_t *f
  * erasure the node counts and stored classifications are brought up to date */
 bruno_status run_node_query(Ctx *c, int filter, bool erase, uint64_t *keys, uint16_t *counts, uint8_t *flags,
                             size_t cap, size_t *n);
+/* check_index (compact_dbg_stats.hpp:45-119) and the edge-count histogram over the node table */
+bruno_status run_check_index(Ctx *c, bruno_index_check *out);
 /* debruijn_graph_map::erase_nodes: host k-mers (either strand), with the edges back to them */
 bruno_status run_erase_nodes(Ctx *c, const uint64_t *kmers, size_t n);
 /* chain-map records of the nodes whose removed[] mark is `which` (0 chain map, 1 cycle, 2 isolated)

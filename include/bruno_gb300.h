@@ -277,6 +277,23 @@ bruno_status bruno_graph_erase_if(bruno_ctx *ctx, int32_t filter, size_t *n_eras
  * neighbours lose their edges to it (erase_nodes_and_edges, :811-827). */
 bruno_status bruno_graph_erase_nodes(bruno_ctx *ctx, const uint64_t *kmers, size_t n);
 
+/* The reference driver's debug check of the graph, check_index (test/common/compact_dbg_stats.hpp:
+ * 45-119): every neighbour k-mer that a node's edges name must be a node (n_absent = 0), and every
+ * node with an edge must be named as a neighbour by some node (n_unreferenced = 0).  Also reported:
+ * edges whose neighbour node lacks the edge back (n_unanswered), and the in-edge count x out-edge
+ * count histogram of print_edge_histogram (compact_dbg_stats.hpp:121-135, debruijn_stats.hpp:
+ * 39-74), edge_hist[in * 5 + out].  Returns BRUNO_ERR_INVARIANT, with *out filled, when either of
+ * the reference's two checks fails (where the reference's debug build asserts).  After
+ * bruno_local_insert_by_freqencies. */
+typedef struct bruno_index_check {
+  uint64_t n_query;         /* neighbour k-mers named: one per edge of every node */
+  uint64_t n_absent;        /* of them, k-mers that are not nodes */
+  uint64_t n_unreferenced;  /* nodes with an edge that no node names */
+  uint64_t n_unanswered;    /* edges whose neighbour node has no edge back */
+  uint64_t edge_hist[25];
+} bruno_index_check;
+bruno_status bruno_check_index(bruno_ctx *ctx, bruno_index_check *out);
+
 /* Chain-map predicates of bliss::debruijn::filter::chain (src/debruijn/debruijn_chain_filters.hpp),
  * evaluated on a chain-map record (k-mer, in k-mer, out k-mer, in distance, out distance). */
 typedef enum bruno_chain_filter {

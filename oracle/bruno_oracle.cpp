@@ -514,6 +514,8 @@ struct Run {
         std::vector<std::pair<W, uint8_t>>().swap(out[t][s]);
       }
     });
+    res->n_k2 = 0;   /* the distinct (k+2)-mer entries, whether or not the table is kept */
+    for (int s = 0; s < T; ++s) res->n_k2 += k2[s].live;
     res->seconds[ORACLE_T_COUNT_K2] = now() - t1;
     return true;
   }
@@ -1378,6 +1380,73 @@ struct Run {
     res = top;
   }
 
+  /* ====================================================== check_index
+   * test/common/compact_dbg_stats.hpp:45-119, run where the driver runs it after the build
+   * (compact_dbg_freq_construct_clean.cpp:515): the neighbours every node's edges name
+   * (get_out_neighbors / get_in_neighbors, debruijn_graph_node.hpp:316-381) are counted in the
+   * canonical index -- absent ones fail the first check; the index minus every named k-mer minus
+   * IsIsolated nodes must be empty -- the second.  Also the edges whose neighbour lacks the edge
+   * back, and print_compact_multi_biedge_histogram's in x out histogram (debruijn_stats.hpp:39-74). */
+  void check_index() {
+    std::vector<uint64_t> q(T, 0), absent(T, 0), unanswered(T, 0);
+    std::vector<std::array<uint64_t, 25>> hist(T);
+    std::vector<std::vector<W>> named(T);
+    parallel(T, [&](int s) {
+      hist[s].fill(0);
+      for (size_t i = 0; i < nodes[s].keys.size(); ++i) {
+        if (nodes[s].state[i] != 1) continue;
+        const W K = nodes[s].keys[i].v;
+        const Node &n = nodes[s].vals[i];
+        unsigned din = 0, dout = 0;
+        for (unsigned c = 0; c < 4; ++c) {
+          for (int side = 0; side < 2; ++side) {
+            if (!n.c[side ? 4 + c : c]) continue;
+            ++q[s];
+            side ? ++din : ++dout;
+            /* K.c answers with its in edge from first(K); c.K with its out edge to last(K) */
+            W y = side ? ((K >> 2) | (W(c) << (2 * (ko.k - 1)))) : (((K << 2) | W(c)) & ko.mask);
+            unsigned want_in = side ? 4 : ko.first(K), want_out = side ? ko.last(K) : 4;
+            const W r = ko.rc(y);
+            if (!(y < r)) {   /* lex_less flips the pair: in and out swap, complemented */
+              y = r;
+              const unsigned wi = want_out < 4 ? 3 - want_out : 4, wo = want_in < 4 ? 3 - want_in : 4;
+              want_in = wi; want_out = wo;
+            }
+            named[s].push_back(y);
+            const Node *m = node_of(y);
+            if (!m) { ++absent[s]; continue; }
+            if ((want_out < 4 && !m->c[want_out]) || (want_in < 4 && !m->c[4 + want_in])) ++unanswered[s];
+          }
+        }
+        ++hist[s][din * 5 + dout];
+      }
+    });
+    std::vector<std::vector<uint8_t>> marks(T);
+    for (int s = 0; s < T; ++s) marks[s].assign(nodes[s].keys.size(), 0);
+    for (int s = 0; s < T; ++s)
+      for (W y : named[s]) {
+        OAMap<KmerKey<W>, Node> &m = nodes[shard(y)];
+        Node *x = m.find(KmerKey<W>{y});
+        if (x) marks[shard(y)][(size_t)(x - m.vals.data())] = 1;
+      }
+    uint64_t unref = 0;
+    for (int s = 0; s < T; ++s)
+      for (size_t i = 0; i < nodes[s].keys.size(); ++i) {
+        if (nodes[s].state[i] != 1 || marks[s][i]) continue;
+        const Node &n = nodes[s].vals[i];
+        bool any = false;
+        for (int c = 0; c < 8; ++c) any |= n.c[c] != 0;
+        unref += any;   /* IsIsolated nodes are erased before the check */
+      }
+    res->check_query = res->check_absent = res->check_unanswered = 0;
+    for (int i = 0; i < 25; ++i) res->edge_hist[i] = 0;
+    for (int s = 0; s < T; ++s) {
+      res->check_query += q[s]; res->check_absent += absent[s]; res->check_unanswered += unanswered[s];
+      for (int i = 0; i < 25; ++i) res->edge_hist[i] += hist[s][i];
+    }
+    res->check_unreferenced = unref;
+  }
+
   /* ====================================================== chain-map outputs */
   static void put_records(std::vector<std::pair<W, ChainNode<W>>> &v, int w, uint64_t *n, uint64_t **keys,
                           uint64_t **in, uint64_t **out, uint32_t **ind, uint32_t **outd) {
@@ -1470,6 +1539,7 @@ struct Run {
      * :187-198).  A sum of saturating increments equals the saturating add of the pair's
      * count, so the same insert step serves both builds; it just sets no flags. */
     filter_insert();
+    check_index();
     extract_chains();
     list_rank();
     emit();

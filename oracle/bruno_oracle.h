@@ -122,6 +122,12 @@ typedef struct oracle_result {
   uint64_t *iso_keys, *iso_in, *iso_out; uint32_t *iso_in_dist, *iso_out_dist;
   uint64_t n_cycle_kmers;
   uint64_t *cycle_keys;
+
+  /* check_index (test/common/compact_dbg_stats.hpp:45-119) on the graph after the build:
+   * neighbour k-mers named, of them absent, nodes with an edge that no node names, edges whose
+   * neighbour lacks the edge back; and the in x out edge-count histogram (in * 5 + out) */
+  uint64_t check_query, check_absent, check_unreferenced, check_unanswered;
+  uint64_t edge_hist[25];
 } oracle_result;
 
 /* Runs the whole path on an in-memory FASTQ buffer.  Returns 0 on success. */

@@ -57,6 +57,8 @@ _Res._fields_ = [
         ("n_isolated_recs", ctypes.c_uint64), ("iso_keys", _U64P), ("iso_in", _U64P), ("iso_out", _U64P),
         ("iso_in_dist", ctypes.POINTER(ctypes.c_uint32)), ("iso_out_dist", ctypes.POINTER(ctypes.c_uint32)),
         ("n_cycle_kmers", ctypes.c_uint64), ("cycle_keys", _U64P),
+        ("check_query", ctypes.c_uint64), ("check_absent", ctypes.c_uint64), ("check_unreferenced", ctypes.c_uint64),
+        ("check_unanswered", ctypes.c_uint64), ("edge_hist", ctypes.c_uint64 * 25),
     ]
 
 
@@ -145,6 +147,9 @@ def _graph(r, keep_k2: bool = False, keep_filtered: bool = False) -> dict:
     out["chain_map"] = records(r.n_chain_map, r.cm_keys, r.cm_in, r.cm_out, r.cm_in_dist, r.cm_out_dist)
     out["isolated"] = records(r.n_isolated_recs, r.iso_keys, r.iso_in, r.iso_out, r.iso_in_dist, r.iso_out_dist)
     out["cycle_kmers"] = _arr(r.cycle_keys, r.n_cycle_kmers * w, np.uint64, (r.n_cycle_kmers, w))
+    out["check_index"] = {"n_query": int(r.check_query), "n_absent": int(r.check_absent),
+                          "n_unreferenced": int(r.check_unreferenced), "n_unanswered": int(r.check_unanswered),
+                          "edge_hist": list(r.edge_hist)}
     return out
 
 

@@ -29,11 +29,13 @@ def gpu_run(data, k, thr_on, thresh, mu, files=None, **kw):
     g.compute_biedge_freqencies()
     k2 = g.k2()
     g.local_insert_by_freqencies()
+    check = g.check_index()
     g.extract_chains()
     it = g.list_rank_min_update() if mu else g.list_rank()
     g.to_compressed_chains()
     out = dict(sizes=g.sizes(), k2=k2, filtered=g.filtered(), nodes=g.nodes(), ranked=g.ranked(),
-               chains=g.chains(), chain_edges=g.chain_edges(), summaries=summaries_or_none(g), iterations=it)
+               chains=g.chains(), chain_edges=g.chain_edges(), summaries=summaries_or_none(g), iterations=it,
+               check=check)
     g.close()
     return out
 
@@ -72,6 +74,12 @@ def compare(gpu, ref):
     assert chain_set(*gpu["chains"]) == chain_set(*ref["chains"]), "compacted chains"
     assert_same(gpu["chain_edges"], ref["chain_edges"], "chain end edges")
     compare_summaries(gpu, ref)
+    # check_index on the built graph: the same counts and histogram as the oracle's, and the
+    # library's verdict is the reference's assertion
+    chk = dict(gpu["check"])
+    ok = chk.pop("ok")
+    assert chk == ref["check_index"], (chk, ref["check_index"])
+    assert ok == (chk["n_absent"] == 0 and chk["n_unreferenced"] == 0)
 
 
 PATHS = {"fast": {}, "round_sync": {"exact_ranking": True}, "direct_count": {"direct_count": 1},

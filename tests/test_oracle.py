@@ -511,3 +511,26 @@ def test_cleaned_chain_edges_follow_chain_strings(tmp_path, fname, lo):
         lines.append(f"{L}\t{R}\t" + "".join(f"{int(v)}\t" for v in lin + rout + [mean, min(f), max(f)]) + "\n")
     assert open(tmp_path / "p.clean.chain.edges").read() == "".join(sorted(lines))
     assert len(lines) == c["n_chains"] > 0
+
+
+def test_check_index_holds_on_consistent_builds():
+    """check_index (compact_dbg_stats.hpp:45-119) holds on every fixture built unthresholded or
+    with -L alone (the filter trims both sides of an edge alike); it can fail only where
+    separate k and k+2 bounds trim an edge on one side (the reference's debug build would
+    assert there), and the edge histogram covers every node"""
+    import os
+    from conftest import DATA, fixture_bytes
+    failed_222 = 0
+    for f in sorted(os.listdir(DATA)):
+        if not f.endswith(".fastq"):
+            continue
+        for lo in ([], [1], [2], [3], [2, 2, 2]):
+            r = oracle.run(fixture_bytes(f), k=31, thresholding=bool(lo), thresh=bg.thresholds(lo))
+            c = r["check_index"]
+            assert sum(c["edge_hist"]) == r["n_nodes"]
+            assert c["n_query"] == sum(((i // 5) + (i % 5)) * v for i, v in enumerate(c["edge_hist"]))
+            if len(lo) == 3:
+                failed_222 += c["n_absent"] > 0
+            else:
+                assert c["n_absent"] == 0 and c["n_unreferenced"] == 0 and c["n_unanswered"] == 0, (f, lo, c)
+    assert failed_222 > 0
