@@ -43,6 +43,9 @@ def parse_args():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="plain-scale")
     ap.add_argument("--cpu-sample", type=float, default=0.2, help="fraction of reads in the CPU baseline sample")
+    ap.add_argument("--ref-sample", type=float, default=0.05,
+                    help="fraction of reads in each step of the reference arm (a bounded sample of the workload, "
+                         "so that every step of --steps/--warmup takes a few seconds)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--samples", type=int, default=None,
                     help="batched / served: number of distinct samples (256 / 48)")
@@ -174,7 +177,7 @@ def run_reference(args, w):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    sample = max(args.cpu_sample, 1e-4)
+    sample = max(args.ref_sample, 1e-4)
     for _ in range(args.warmup):
         cpu_baseline(w, sample, threads)
     vals, secs = [], []
@@ -496,9 +499,10 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded generator, " + w.name + ")",
-                "config": dict(workload_config(w), api="bruno_build_and_compact" if args.api == "build"
-                               else "step calls", h2d_streams=args.h2d_streams,
-                               h2d_chunk=args.h2d_chunk or 256 << 20, rank_fill=args.rank_fill),
+                "config": workload_config(w),
+                "run": {"api": "bruno_build_and_compact" if args.api == "build" else "step calls",
+                        "h2d_streams": args.h2d_streams, "h2d_chunk": args.h2d_chunk or 256 << 20,
+                        "rank_fill": args.rank_fill},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n, "d2h_bytes_per_step": d2h,
                         "ms_per_step": ems / args.steps,
                         "h2d_ms": statistics.mean(p["h2d"] for p in e2e_phases) if e2e_phases else None,

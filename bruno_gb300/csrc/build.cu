@@ -966,6 +966,269 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract(const uint64_t *rstart, con
   for (int x = tid; x < HLL_M; x += XTPB) dst[x] = (uint8_t)S.hll[x];
 }
 
+/* ------------------------------------------------ warp-per-read extraction
+ * Phase A of the partitioned count, one warp per read: the warp stages up to WX_SUB k-mer
+ * positions of its read as 2-bit words with coalesced byte loads and ballots (stage_chunk),
+ * every lane then rolls a contiguous run of canonical (k-mer, biedge) pairs
+ * (for_each_kmer_run), and each pair becomes the same 8-byte record as in k_extract.  The
+ * records of a round go to a block-wide stage in shared memory (one reservation per warp and
+ * round); when the stage is full the block sorts it by bucket (histogram, scan, scatter) and
+ * appends each bucket's run to chunks of `chunk` records the block claims per bucket, one
+ * global atomic per claim, so the bucket files grow by contiguous runs without a global
+ * atomic per flush.  Work comes as items of consecutive reads of one sample (the batched form
+ * counts many samples at once, each in buckets of its own); a block takes a contiguous range of
+ * items, so it changes sample rarely, and zeroes the unused tails of its chunks when it does.
+ * The distinct-count estimate is a HyperLogLog per sample, fed with the k-mers whose mix has
+ * its HLL_SAMPLE low bits zero (1 in 8; the estimate is scaled back). */
+constexpr int WX_TPB = 256, WX_WARPS = WX_TPB / 32;
+constexpr int WX_SUB = 128;                             /* positions a warp emits per round */
+constexpr int WX_STAGE = 3072;                          /* records staged per block between flushes */
+constexpr int WX_FLUSH = WX_STAGE - WX_WARPS * WX_SUB;  /* flush when another round might not fit */
+constexpr int WX_WORDS = 12;                            /* staged words per warp: 32 + 128 + k + 1 bases + 3 spare */
+constexpr int HLL_SAMPLE = 3;
+
+/* bucket b of sample s holds records[rec_base + b * cap, + cap); chunk = records a block claims at once */
+struct XSample { unsigned long long rec_base, cap; unsigned int chunk, pad; };
+/* reads [a, b) of sample s */
+struct XItem { unsigned long long a, b; unsigned int s, pad; };
+
+static_assert(WX_TPB == NBUCKET, "one bucket a thread in the flush");
+
+struct WXSmem {
+  uint64_t stage[WX_STAGE];
+  uint64_t sorted[WX_STAGE];
+  uint8_t stage_b[WX_STAGE];
+  uint8_t sorted_b[WX_STAGE];
+  uint64_t words[WX_WARPS][WX_WORDS];
+  unsigned long long cpos[NBUCKET], cend[NBUCKET];   /* the block's open chunk per bucket */
+  unsigned long long base1[NBUCKET], base2[NBUCKET];
+  unsigned int cnt[NBUCKET], start[NBUCKET], rem[NBUCKET];
+  unsigned int wsum[WX_WARPS + 1];
+  unsigned int n, item_next;
+  unsigned long long inst, used;
+  int overflow;
+};
+
+/* the stage's records into their buckets' chunks (every thread of the block calls it) */
+__device__ __forceinline__ void wx_flush(WXSmem &S, const XSample &xs, unsigned s, uint64_t *records,
+                                         unsigned long long *bucket_cnt) {
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const unsigned n = S.n;
+  S.cnt[tid] = 0;   /* WX_TPB == NBUCKET: one bucket a thread */
+  __syncthreads();
+  uint16_t rank[WX_STAGE / WX_TPB];
+  #pragma unroll
+  for (int j = 0; j < WX_STAGE / WX_TPB; ++j) {
+    const unsigned i = tid + j * WX_TPB;
+    if (i < n) rank[j] = (uint16_t)atomicAdd(&S.cnt[S.stage_b[i]], 1u);
+  }
+  __syncthreads();
+  /* exclusive scan of the 256 counts */
+  const unsigned v = S.cnt[tid];
+  unsigned x = v;
+  #pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(~0u, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) S.wsum[wid] = x;
+  __syncthreads();
+  if (tid == 0) {
+    unsigned run = 0;
+    for (int w = 0; w < WX_WARPS; ++w) { const unsigned t = S.wsum[w]; S.wsum[w] = run; run += t; }
+  }
+  __syncthreads();
+  S.start[tid] = S.wsum[wid] + x - v;
+  /* reservations: the open chunk first, then a new chunk of max(need, chunk) records */
+  if (v) {
+    const unsigned long long p = S.cpos[tid], avail = S.cend[tid] - p;
+    S.base1[tid] = p;
+    if (avail >= v) {
+      S.rem[tid] = v;
+      S.cpos[tid] = p + v;
+    } else {
+      const unsigned long long need = v - avail, ch = max(need, (unsigned long long)xs.chunk);
+      const unsigned long long old = atomicAdd(&bucket_cnt[(uint64_t)s * NBUCKET + tid], ch);
+      if (old + ch > xs.cap) S.overflow = 1;
+      const unsigned long long nb = xs.rec_base + (uint64_t)tid * xs.cap + old;
+      S.rem[tid] = (unsigned)avail;
+      S.base2[tid] = nb;
+      S.cpos[tid] = nb + need;
+      S.cend[tid] = nb + ch;
+    }
+  }
+  __syncthreads();
+  #pragma unroll
+  for (int j = 0; j < WX_STAGE / WX_TPB; ++j) {
+    const unsigned i = tid + j * WX_TPB;
+    if (i < n) {
+      const unsigned b = S.stage_b[i], y = S.start[b] + rank[j];
+      S.sorted[y] = S.stage[i];
+      S.sorted_b[y] = (uint8_t)b;
+    }
+  }
+  __syncthreads();
+  for (unsigned y = tid; y < n; y += WX_TPB) {
+    const unsigned b = S.sorted_b[y], j = y - S.start[b];
+    const unsigned long long dst = j < S.rem[b] ? S.base1[b] + j : S.base2[b] + (j - S.rem[b]);
+    if (dst < xs.rec_base + (unsigned long long)(b + 1) * xs.cap) records[dst] = S.sorted[y];
+  }
+  __syncthreads();
+  if (tid == 0) S.n = 0;
+  __syncthreads();
+}
+
+/* the unused tails of the block's chunks hold no records (0 is never a record) */
+__device__ __forceinline__ void wx_close(WXSmem &S, const XSample &xs, uint64_t *records) {
+  const int tid = threadIdx.x;
+  for (int b = tid >> 5; b < NBUCKET; b += WX_WARPS) {
+    const unsigned long long e = min(S.cend[b], xs.rec_base + (unsigned long long)(b + 1) * xs.cap);
+    for (unsigned long long p = S.cpos[b] + (tid & 31); p < e; p += 32) records[p] = 0ull;
+  }
+  __syncthreads();
+  S.cpos[tid] = 0;
+  S.cend[tid] = 0;
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(WX_TPB, 3) k_extract_w(const uint64_t *rstart, const uint64_t *rend, uint64_t r0,
+                                                         uint64_t r1, const XItem *items, uint64_t n_items,
+                                                         uint32_t item_reads, int k, const XSample *xsamp,
+                                                         uint64_t *records, unsigned long long *bucket_cnt,
+                                                         unsigned int *hll, unsigned long long *s_inst,
+                                                         unsigned long long *s_used, DevCounters *ctr) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  WXSmem &S = *reinterpret_cast<WXSmem *>(smem_raw);
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  S.cpos[tid] = 0;
+  S.cend[tid] = 0;
+  if (tid == 0) { S.n = 0; S.overflow = 0; }
+  const uint64_t nit = items ? n_items : (r1 - r0 + item_reads - 1) / item_reads;
+  /* a contiguous range of items per block */
+  const uint64_t per = (nit + gridDim.x - 1) / gridDim.x;
+  const uint64_t it0 = min(nit, (uint64_t)blockIdx.x * per), it1 = min(nit, it0 + per);
+  unsigned cur_s = ~0u;
+  XSample xs{};
+  __syncthreads();
+  for (uint64_t it = it0; it < it1; ++it) {
+    uint64_t a, b;
+    unsigned s;
+    if (items) { a = items[it].a; b = items[it].b; s = items[it].s; }
+    else { a = r0 + it * item_reads; b = min(r1, a + item_reads); s = 0; }
+    if (s != cur_s) {   /* a new sample: flush what is staged, close the old sample's chunks */
+      if (cur_s != ~0u) {
+        if (S.n) wx_flush(S, xs, cur_s, records, bucket_cnt);
+        wx_close(S, xs, records);
+      }
+      cur_s = s;
+      xs = xsamp[s];
+    }
+    if (tid == 0) { S.item_next = 0; S.inst = 0; S.used = 0; }
+    __syncthreads();
+    unsigned int *hreg = hll + (uint64_t)s * HLL_M;
+    const unsigned char *sp = nullptr;
+    uint32_t L = 0, npos = 0, p0 = 0;
+    bool have = false;
+    unsigned long long inst = 0, used = 0;
+    for (;;) {
+      while (!have) {   /* this warp's next usable read of the item */
+        unsigned idx = 0;
+        if (lane == 0) idx = atomicAdd(&S.item_next, 1u);
+        idx = __shfl_sync(~0u, idx, 0);
+        if (a + idx >= b) break;
+        const uint64_t r = a + idx;
+        sp = (const unsigned char *)rstart[r];
+        L = (uint32_t)(rend[r] - rstart[r]);
+        if (L < (uint32_t)k + 2) continue;           /* shorter than the k+2 window */
+        npos = L - k + 1;
+        if (npos > (uint32_t)WX_SUB) {                /* long read: the N filter before any record */
+          bool bad = false;
+          for (uint32_t i = lane; i < L; i += 32) bad |= base_code(sp[i]) < 0;
+          if (__any_sync(~0u, bad)) continue;
+        }
+        p0 = 0;
+        have = true;
+      }
+      if (!__syncthreads_or(have)) break;             /* the item is done */
+      if (have) {
+        const uint32_t pend = min(npos, p0 + WX_SUB);
+        __syncwarp();
+        const bool bad = stage_chunk(ReadView{sp, L}, p0, pend, k, S.words[wid], lane);
+        if (bad) {
+          have = false;                                /* a short read with N: dropped whole */
+        } else {
+          if (p0 == 0) used += (lane == 0);
+          for_each_kmer_run<KW1>(S.words[wid], p0, pend, p0, L, k, lane, [&](bool valid, KW1 x, unsigned code) {
+            uint64_t rec = 0;
+            unsigned bk = 0;
+            if (valid) {
+              ++inst;
+              const uint64_t h = bj_fwd(x.v);
+              bk = (unsigned)(h >> LOW_BITS);
+              rec = ((h & ((1ull << LOW_BITS) - 1)) << 5) | code;
+              if ((h & ((1u << HLL_SAMPLE) - 1)) == 0) {
+                const unsigned idx = (unsigned)(h >> (62 - HLL_P));
+                const unsigned rho = (unsigned)__clzll((h << (2 + HLL_P)) | (1ull << (1 + HLL_P))) + 1u;
+                if (rho > hreg[idx]) atomicMax(&hreg[idx], rho);
+              }
+            }
+            const unsigned m = __ballot_sync(~0u, valid);
+            if (m) {
+              unsigned base = 0;
+              if (lane == 0) base = atomicAdd(&S.n, (unsigned)__popc(m));
+              base = __shfl_sync(~0u, base, 0);
+              if (valid) {
+                const unsigned o = base + __popc(m & ((1u << lane) - 1));
+                S.stage[o] = rec;
+                S.stage_b[o] = (uint8_t)bk;
+              }
+            }
+          });
+          p0 = pend;
+          if (p0 >= npos) have = false;
+        }
+      }
+      __syncthreads();
+      if (S.n > (unsigned)WX_FLUSH) wx_flush(S, xs, cur_s, records, bucket_cnt);
+    }
+    /* the item's tallies */
+    inst = warp_sum(inst); used = warp_sum(used);
+    if (lane == 0) {
+      if (inst) atomicAdd(&S.inst, inst);
+      if (used) atomicAdd(&S.used, used);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      if (S.inst) { atomicAdd(&ctr->n_instances, S.inst); if (s_inst) atomicAdd(&s_inst[s], S.inst); }
+      if (S.used) { atomicAdd(&ctr->n_reads_used, S.used); if (s_used) atomicAdd(&s_used[s], S.used); }
+    }
+    __syncthreads();
+  }
+  if (cur_s != ~0u) {
+    if (S.n) wx_flush(S, xs, cur_s, records, bucket_cnt);
+    wx_close(S, xs, records);
+  }
+  if (tid == 0 && S.overflow) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
+}
+
+/* per-sample distinct estimate inputs: sum of 2^-register and the number of zero registers
+ * (one block per sample; the host finishes the HyperLogLog estimate) */
+__global__ void k_hll_sums(const unsigned int *hll, double *sum, unsigned int *zeros) {
+  __shared__ double ss[256];
+  __shared__ unsigned int zz[256];
+  const unsigned int *reg = hll + (uint64_t)blockIdx.x * HLL_M;
+  double t = 0;
+  unsigned z = 0;
+  for (int i = threadIdx.x; i < HLL_M; i += blockDim.x) { t += ldexp(1.0, -(int)reg[i]); z += reg[i] == 0; }
+  ss[threadIdx.x] = t; zz[threadIdx.x] = z;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) { ss[threadIdx.x] += ss[threadIdx.x + o]; zz[threadIdx.x] += zz[threadIdx.x + o]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { sum[blockIdx.x] = ss[0]; zeros[blockIdx.x] = zz[0]; }
+}
+
 /* one table partition: keys EMPTY, entries 0 (stays in L2 for the inserts that follow) */
 template <class KT>
 __global__ void k_part_init(uint64_t *table, uint64_t first_slot, uint64_t nslots) {
@@ -1706,6 +1969,7 @@ void scan_u64(const uint64_t *in, uint64_t *out, uint64_t n, unsigned long long 
 namespace {
 bruno_status extract_begin(Ctx *c, uint64_t upper, int max_blocks);
 void extract_reads(Ctx *c, uint64_t r0, uint64_t r1);
+int wx_blocks(uint64_t nr);
 }  // namespace
 
 /* Indexes every FASTQ segment.  A segment copied from the host in pieces (load_fastq) is
@@ -1728,9 +1992,8 @@ bruno_status run_index_reads(Ctx *c) {
   if (c->pre_extracted) {
     /* every record holds its sequence and an equally long quality line, so the k-mer
      * positions of all reads are at most half the bytes */
-    int blocks = 0;   /* one launch a segment: at most 2 per SM, at most one per XTPB reads (8 bytes a read at least) */
-    for (auto &sg : c->segs)
-      blocks += (int)std::min<uint64_t>(num_sms() * 2, (sg.n / 8 + XTPB) / XTPB);
+    int blocks = 0;   /* one launch a segment, bounded as extract_reads bounds it (8 bytes a read at least) */
+    for (auto &sg : c->segs) blocks += wx_blocks(sg.n / 8 + 1);
     if ((st = extract_begin(c, total_bytes / 2 + 1, std::max(1, blocks))) != BRUNO_OK) return st;
     cudaEventRecord(c->kev[0], c->stream);
   }
@@ -1787,6 +2050,14 @@ double hll_estimate(const unsigned int *reg) {
   double est = alpha * m * m / sum;
   if (est <= 2.5 * m && zeros > 0) est = m * std::log(m / zeros);
   return est;
+}
+
+/* the HyperLogLog estimate of the k-mers sampled into it (1 in 2^HLL_SAMPLE), scaled back to all */
+double hll_sampled_estimate(double sum, unsigned zeros) {
+  const double m = HLL_M, alpha = 0.7213 / (1.0 + 1.079 / m);
+  double est = alpha * m * m / sum;
+  if (est <= 2.5 * m && zeros > 0) est = m * std::log(m / zeros);
+  return est * (double)(1u << HLL_SAMPLE);
 }
 
 uint64_t slots_for(const Ctx *c, double distinct) {
@@ -1872,13 +2143,44 @@ bruno_status extract_begin(Ctx *c, uint64_t upper, int max_blocks) {
   c->xchunk = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(512, margin / (2ull * max_blocks)));
   c->xblk = 0;
   c->xblk_max = max_blocks;
+  if (!c->cfg.edge_filter) {   /* the warp-per-read extraction: one sample, its HyperLogLog */
+    static const bool wattr = [] {
+      cudaFuncSetAttribute(k_extract_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(WXSmem));
+      return true;
+    }();
+    (void)wattr;
+    if ((st = ensure(c, c->xsamp, sizeof(XSample))) != BRUNO_OK) return st;
+    if ((st = ensure(c, c->hllreg, HLL_M * 4)) != BRUNO_OK) return st;
+    const XSample xs{0ull, cap, c->xchunk, 0u};
+    if ((st = cuda_check(c, cudaMemcpyAsync(c->xsamp.p, &xs, sizeof(xs), cudaMemcpyHostToDevice, c->stream),
+                         "extraction layout")) != BRUNO_OK)
+      return st;
+    cudaMemsetAsync(c->hllreg.p, 0, HLL_M * 4, c->stream);
+  }
   return BRUNO_OK;
+}
+
+/* blocks of one warp-per-read extraction launch over nr reads (at most 3 per SM, at least one
+ * item of WX_ITEM reads each) */
+constexpr uint32_t WX_ITEM = 64;
+int wx_blocks(uint64_t nr) {
+  return (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)num_sms() * 3, (nr + WX_ITEM - 1) / WX_ITEM));
 }
 
 /* one extraction launch over reads [r0, r1) */
 void extract_reads(Ctx *c, uint64_t r0, uint64_t r1) {
   const uint64_t nr = r1 - r0;
   if (nr == 0) return;
+  if (!c->cfg.edge_filter) {
+    const int eb = std::max(1, std::min(wx_blocks(nr), c->xblk_max - c->xblk));
+    k_extract_w<<<eb, WX_TPB, sizeof(WXSmem), c->stream>>>(
+        (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, r0, r1, nullptr, 0, WX_ITEM, c->cfg.k,
+        (const XSample *)c->xsamp.p, (uint64_t *)c->records.p, (unsigned long long *)c->bucket_cnt.p,
+        (unsigned int *)c->hllreg.p, nullptr, nullptr, c->dctr);
+    c->xblk += eb;
+    c->launches += 1;
+    return;
+  }
   const int eb = std::max(1, std::min<int>({num_sms() * 2, (int)((nr + XTPB - 1) / XTPB), c->xblk_max - c->xblk}));
   const uint64_t *rs = (const uint64_t *)c->rstart.p + r0, *re = (const uint64_t *)c->rend.p + r0;
   uint8_t *part = (uint8_t *)c->blk_cnt.p + (uint64_t)c->xblk * HLL_M;
@@ -1905,19 +2207,34 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
                                                  c->cfg.k, c->dctr);
     c->launches += 1;
     if ((st = sync_counters(c)) != BRUNO_OK) return st;
-    if ((st = extract_begin(c, c->hctr->n_upper, sms * 2)) != BRUNO_OK) return st;
+    if ((st = extract_begin(c, c->hctr->n_upper, c->cfg.edge_filter ? sms * 2 : wx_blocks(nreads))) != BRUNO_OK)
+      return st;
     cudaEventRecord(c->kev[0], c->stream);
     extract_reads(c, 0, nreads);
   }
   const uint64_t cap = c->xcap;
-  k_hll_merge<<<HLL_M / 256, 256, 0, c->stream>>>((const uint8_t *)c->blk_cnt.p, c->xblk, c->dctr);
-  c->launches += 1;
-  cudaEventRecord(c->kev[1], c->stream);
-  if ((st = sync_counters(c, true)) != BRUNO_OK) return st;
+  double distinct = 0;
+  if (c->cfg.edge_filter) {
+    k_hll_merge<<<HLL_M / 256, 256, 0, c->stream>>>((const uint8_t *)c->blk_cnt.p, c->xblk, c->dctr);
+    c->launches += 1;
+    cudaEventRecord(c->kev[1], c->stream);
+    if ((st = sync_counters(c, true)) != BRUNO_OK) return st;
+    distinct = hll_estimate(c->hctr->hll);
+  } else {
+    if ((st = ensure(c, c->hsum, 16)) != BRUNO_OK) return st;
+    k_hll_sums<<<1, 256, 0, c->stream>>>((const unsigned int *)c->hllreg.p, (double *)c->hsum.p,
+                                         (unsigned int *)((double *)c->hsum.p + 1));
+    c->launches += 1;
+    cudaEventRecord(c->kev[1], c->stream);
+    double hs[2] = {0, 0};
+    cudaMemcpyAsync(hs, c->hsum.p, 16, cudaMemcpyDeviceToHost, c->stream);
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    distinct = hll_sampled_estimate(hs[0], *(const unsigned int *)&hs[1]);
+  }
   if (c->hctr->err & DERR_TABLE_FULL) return BRUNO_OK;   /* a bucket overflowed: count directly */
   c->n_instances = c->hctr->n_instances;
   c->n_reads_used = c->hctr->n_reads_used;
-  uint64_t slots = c->cfg.table_slots ? c->cfg.table_slots : slots_for(c, hll_estimate(c->hctr->hll));
+  uint64_t slots = c->cfg.table_slots ? c->cfg.table_slots : slots_for(c, distinct);
   static const bool part_attr = [] {
     cudaFuncSetAttribute(k_count_local, cudaFuncAttributeMaxDynamicSharedMemorySize, PART_SLOTS * 32);
     cudaFuncSetAttribute(k_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SplitSmem));

@@ -105,6 +105,7 @@ struct Ctx {
   TableGeom geom{0, 0, 0};
   uint64_t nslots = 0, n_entries = 0, n_slots_claimed = 0;
   Buf records, bucket_cnt;       /* partitioned counting: 8-byte records per hash bucket */
+  Buf xsamp, hllreg, hsum;       /* the extraction's bucket layout, HyperLogLog registers, their sums */
   Buf records2, sub_cnt;         /* the same records split per table partition */
   bool h2d_pending = false;      /* ev[7] marks the start of this build's host-to-device copies */
   int force_direct_count = 0;    /* cfg.direct_count: 0 automatic, 1 whole table, 2 L2 partitions */

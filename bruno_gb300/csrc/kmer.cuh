@@ -195,6 +195,7 @@ struct TableGeom {
   uint64_t nslots;   /* region << pbits */
   uint64_t region;
   int pbits;
+  uint64_t base;     /* first slot: a sample's table in a batch of samples starts here (0 otherwise) */
 };
 
 /* The table stores a key derived from the canonical k-mer: for k <= 31 the 62-bit mix
@@ -208,17 +209,17 @@ __device__ __forceinline__ KW2 key_kmer(KW2 t) { return t; }
 __device__ __forceinline__ uint64_t table_home(const TableGeom &g, KW1 t) {
   const uint64_t h = t.v;
   const uint64_t q = g.pbits ? (h >> (62 - g.pbits)) : 0;
-  return q * g.region + __umul64hi(h << (2 + g.pbits), g.region);
+  return g.base + q * g.region + __umul64hi(h << (2 + g.pbits), g.region);
 }
 __device__ __forceinline__ uint64_t table_home(const TableGeom &g, KW2 t) {
-  return __umul64hi(KOps<KW2>::hash(t), g.region);   /* pbits == 0 */
+  return g.base + __umul64hi(KOps<KW2>::hash(t), g.region);   /* pbits == 0 */
 }
 /* linear probing inside one partition */
 struct Probe {
   uint64_t i, lo, hi;
   /* part_lo: the first slot of the partition if the caller knows it (saves a division) */
   __device__ __forceinline__ Probe(const TableGeom &g, uint64_t start, uint64_t part_lo = ~0ull) : i(start) {
-    lo = part_lo != ~0ull ? part_lo : (g.pbits ? (start / g.region) * g.region : 0);
+    lo = part_lo != ~0ull ? part_lo : (g.pbits ? g.base + ((start - g.base) / g.region) * g.region : g.base);
     hi = lo + g.region;
   }
   __device__ __forceinline__ void next() { if (++i == hi) i = lo; }
