@@ -42,6 +42,7 @@ class _Cfg(ctypes.Structure):
         ("max_load", ctypes.c_double), ("keep_k2", ctypes.c_int32), ("keep_filtered", ctypes.c_int32),
         ("exact_ranking", ctypes.c_int32), ("direct_count", ctypes.c_int32), ("edge_filter", ctypes.c_int32),
         ("h2d_chunk", ctypes.c_uint64), ("h2d_streams", ctypes.c_int32), ("rank_fill", ctypes.c_int32),
+        ("part_slots", ctypes.c_int32), ("count_threads", ctypes.c_int32),
     ]
 
 
@@ -92,6 +93,8 @@ EXPORTS = (
     "bruno_pool_result_free", "bruno_pool_destroy", "bruno_clean_deadend_and_bubbles_naive",
     "bruno_device_results", "bruno_graph_find_if", "bruno_graph_erase_if", "bruno_graph_erase_nodes",
     "bruno_chain_find_if", "bruno_get_cycle_node_kmers", "bruno_get_isolated", "bruno_check_index",
+    "bruno_build_samples", "bruno_sample_count", "bruno_sample_sizes", "bruno_sample_copy_ranked",
+    "bruno_sample_copy_chains", "bruno_sample_copy_nodes", "bruno_pool_create_batched",
 )
 
 # node predicates (bliss::debruijn::filter::graph) and chain predicates
@@ -139,6 +142,12 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "bruno_chain_find_if": [P, I32, P, P, P, P, P, SZ, PSZ],
         "bruno_get_cycle_node_kmers": [P, P, SZ, PSZ], "bruno_get_isolated": [P, P, P, P, P, P, SZ, PSZ],
         "bruno_check_index": [P, ctypes.POINTER(_IndexCheck)],
+        "bruno_build_samples": [P, ctypes.POINTER(P), ctypes.POINTER(SZ), SZ, I32],
+        "bruno_sample_count": [P, PSZ], "bruno_sample_sizes": [P, SZ, ctypes.POINTER(_Sizes)],
+        "bruno_sample_copy_ranked": [P, SZ, P, P, P, SZ, PSZ],
+        "bruno_sample_copy_chains": [P, SZ, P, P, P, SZ, SZ, PSZ, PSZ],
+        "bruno_sample_copy_nodes": [P, SZ, P, P, P, SZ, PSZ],
+        "bruno_pool_create_batched": [ctypes.POINTER(_Cfg), ctypes.c_uint32, U64, ctypes.POINTER(P)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -203,6 +212,8 @@ class GraphConfig:
     h2d_chunk: int = 0             # host FASTQ copied and parsed in pieces of this many bytes (0 = 256 MiB)
     h2d_streams: int = 1           # copy streams the pieces are spread over (1..4)
     rank_fill: int = 0             # ranking's final states: 0 = second walk, 1 = one pass over the nodes
+    part_slots: int = 0            # most slots of one shared-memory table partition (256..3072; 0 = 3072)
+    count_threads: int = 0         # threads of a partition's counting block (256, 512, 1024; 0 = 512)
 
     def to_c(self) -> _Cfg:
         c = _Cfg()
@@ -217,6 +228,8 @@ class GraphConfig:
         c.h2d_chunk = int(self.h2d_chunk)
         c.h2d_streams = int(self.h2d_streams)
         c.rank_fill = int(self.rank_fill)
+        c.part_slots = int(self.part_slots)
+        c.count_threads = int(self.count_threads)
         return c
 
 
@@ -339,6 +352,74 @@ class Graph:
         self._keep = [arr]
         self._check(self.lib.bruno_build_and_compact(self.ctx, arr.ctypes.data_as(ctypes.c_void_p), arr.nbytes, 0),
                     "build_and_compact")
+
+    # ------------------------------------------------------------------ batched form
+    def build_samples(self, samples, is_device: bool = False, nbytes=None) -> None:
+        """The batched form: every sample (bytes / uint8 arrays, or device addresses with their
+        sizes in nbytes) built in one pass; each sample's results are those of its plain build."""
+        n = len(samples)
+        ptrs = (ctypes.c_void_p * max(1, n))()
+        sizes = (ctypes.c_size_t * max(1, n))()
+        keep = []
+        for i, x in enumerate(samples):
+            if is_device:
+                ptrs[i], sizes[i] = int(x), int(nbytes[i])
+                continue
+            arr = np.ascontiguousarray(np.frombuffer(x, dtype=np.uint8) if isinstance(x, (bytes, bytearray)) else x,
+                                       dtype=np.uint8)
+            keep.append(arr)
+            ptrs[i], sizes[i] = arr.ctypes.data, arr.nbytes
+        self._keep = keep
+        self._check(self.lib.bruno_build_samples(self.ctx, ptrs, sizes, n, int(is_device)), "build_samples")
+
+    def sample_count(self) -> int:
+        n = ctypes.c_size_t()
+        self._check(self.lib.bruno_sample_count(self.ctx, ctypes.byref(n)), "sample_count")
+        return n.value
+
+    def sample_sizes(self, sample: int) -> dict:
+        s = _Sizes()
+        self._check(self.lib.bruno_sample_sizes(self.ctx, sample, ctypes.byref(s)), "sample_sizes")
+        d = {n: getattr(s, n) for n, _ in _Sizes._fields_ if n != "filter_flag_hist"}
+        d["filter_flag_hist"] = list(s.filter_flag_hist)
+        return d
+
+    def sample_ranked(self, sample: int):
+        n = ctypes.c_size_t()
+        fn = self.lib.bruno_sample_copy_ranked
+        self._check(fn(self.ctx, sample, None, None, None, 0, ctypes.byref(n)), "sample_copy_ranked")
+        K = np.zeros((n.value, self.words), np.uint64)
+        rep = np.zeros((n.value, self.words), np.uint64)
+        dist = np.zeros(n.value, np.int32)
+        if n.value:
+            self._check(fn(self.ctx, sample, self._ptr(K), self._ptr(rep), self._ptr(dist), n.value, ctypes.byref(n)),
+                        "sample_copy_ranked")
+        return K, rep, dist
+
+    def sample_chains(self, sample: int):
+        nc, nch = ctypes.c_size_t(), ctypes.c_size_t()
+        fn = self.lib.bruno_sample_copy_chains
+        self._check(fn(self.ctx, sample, None, None, None, 0, 0, ctypes.byref(nc), ctypes.byref(nch)),
+                    "sample_copy_chains")
+        reps = np.zeros((nc.value, self.words), np.uint64)
+        offs = np.zeros(nc.value + 1, np.uint64)
+        chars = np.zeros(max(1, nch.value), np.uint8)
+        if nc.value:
+            self._check(fn(self.ctx, sample, self._ptr(reps), self._ptr(offs), self._ptr(chars), nc.value, chars.size,
+                           ctypes.byref(nc), ctypes.byref(nch)), "sample_copy_chains")
+        return reps, offs, chars[:nch.value]
+
+    def sample_nodes(self, sample: int):
+        n = ctypes.c_size_t()
+        fn = self.lib.bruno_sample_copy_nodes
+        self._check(fn(self.ctx, sample, None, None, None, 0, ctypes.byref(n)), "sample_copy_nodes")
+        keys = np.zeros((n.value, self.words), np.uint64)
+        counts = np.zeros((n.value, 9), np.uint16)
+        flags = np.zeros(n.value, np.uint8)
+        if n.value:
+            self._check(fn(self.ctx, sample, self._ptr(keys), self._ptr(counts), self._ptr(flags), n.value,
+                           ctypes.byref(n)), "sample_copy_nodes")
+        return keys, counts, flags
 
     def run(self, *files) -> "Graph":
         """load every file, then count, filter, extract, rank and compress"""
@@ -556,12 +637,18 @@ class Pool:
     equals the plain path's for that input alone.  Submit a batch and wait for each ticket, or
     submit requests as they arrive and wait for them when needed."""
 
-    def __init__(self, config: Optional[GraphConfig] = None, workers: int = 8, mem_budget: int = 0, **kw):
+    def __init__(self, config: Optional[GraphConfig] = None, workers: int = 8, mem_budget: int = 0,
+                 batched: bool = False, max_samples: int = 256, **kw):
+        """batched: continuous batching over the fused form (one scheduler, passes of up to
+        max_samples requests that fit mem_budget) instead of `workers` side-by-side builds"""
         self.lib = load_library()
         self.config = config or GraphConfig(**kw)
         c = self.config.to_c()
         self.pool = ctypes.c_void_p()
-        st = self.lib.bruno_pool_create(ctypes.byref(c), workers, mem_budget, ctypes.byref(self.pool))
+        if batched:
+            st = self.lib.bruno_pool_create_batched(ctypes.byref(c), max_samples, mem_budget, ctypes.byref(self.pool))
+        else:
+            st = self.lib.bruno_pool_create(ctypes.byref(c), workers, mem_budget, ctypes.byref(self.pool))
         if st != 0:
             raise BrunoError(st, "pool_create")
         self._bufs = {}

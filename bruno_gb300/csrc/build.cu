@@ -1007,7 +1007,39 @@ struct WXSmem {
   unsigned int n, item_next;
   unsigned long long inst, used;
   int overflow;
+  unsigned int hll[HLL_M / 4];   /* the block's HyperLogLog registers for its current sample, a byte each */
 };
+
+/* register idx = max(register, v), a byte in a 32-bit word of shared memory; a CAS that loses to
+ * another update retries (at most 64 times: a register left low only lowers the estimate, which
+ * the table's regrowth absorbs) */
+__device__ __forceinline__ void hll_max_u8(unsigned int *reg, unsigned idx, unsigned v) {
+  unsigned int *w = reg + (idx >> 2);
+  const unsigned sh = 8 * (idx & 3);
+  unsigned old = *w;
+  for (int t = 0; t < 64 && ((old >> sh) & 0xFFu) < v; ++t) {
+    const unsigned prev = atomicCAS(w, old, (old & ~(0xFFu << sh)) | (v << sh));
+    if (prev == old) break;
+    old = prev;
+  }
+}
+
+/* the block's registers into the sample's (atomic max), then cleared */
+__device__ __forceinline__ void hll_flush(WXSmem &S, unsigned int *hreg) {
+  __syncthreads();
+  for (int i = threadIdx.x; i < HLL_M / 4; i += WX_TPB) {
+    const unsigned w = S.hll[i];
+    if (w) {
+      #pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const unsigned v = (w >> (8 * b)) & 0xFFu;
+        if (v) atomicMax(&hreg[4 * i + b], v);
+      }
+      S.hll[i] = 0;
+    }
+  }
+  __syncthreads();
+}
 
 /* the stage's records into their buckets' chunks (every thread of the block calls it) */
 __device__ __forceinline__ void wx_flush(WXSmem &S, const XSample &xs, unsigned s, uint64_t *records,
@@ -1091,6 +1123,49 @@ __device__ __forceinline__ void wx_close(WXSmem &S, const XSample &xs, uint64_t 
   __syncthreads();
 }
 
+/* Stages bases [c0, c0 + 256) of a read (c0 = p0 - 32; bases outside [0, L) read as A) as 2-bit
+ * words in the layout of stage_chunk, in one round of loads: lane j covers bases [c0 + 8j,
+ * c0 + 8j + 8) with at most two aligned 8-byte loads, each holding a byte of the read (nothing
+ * outside the read's own bytes is touched beyond the words that hold them).  Returns true if a
+ * base of the read in the window is not A/C/G/T. */
+__device__ __forceinline__ bool stage_window(const unsigned char *s, uint32_t L, long long c0, uint64_t *words,
+                                             int lane) {
+  const long long lo = c0 + 8 * lane;
+  unsigned code16 = 0;
+  bool bad = false;
+  if (lo + 8 > 0 && lo < (long long)L) {
+    const uintptr_t sa = (uintptr_t)s, ea = sa + L;
+    const uintptr_t a = sa + (uintptr_t)lo;   /* wraps for lo < 0: compared below as a signed offset */
+    const long long first = lo > 0 ? lo : 0, last = (lo + 8 < (long long)L ? lo + 8 : (long long)L) - 1;
+    const uintptr_t w0 = (sa + (uintptr_t)first) & ~(uintptr_t)7, w1 = (sa + (uintptr_t)last) & ~(uintptr_t)7;
+    const uint64_t x0 = __ldg((const unsigned long long *)w0);
+    const uint64_t x1 = w1 != w0 ? __ldg((const unsigned long long *)w1) : 0ull;
+    (void)ea;
+    #pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const long long off = lo + i;
+      unsigned c = 0;
+      if (off >= 0 && off < (long long)L) {
+        const uintptr_t ad = a + (uintptr_t)i;
+        const uint64_t x = (ad & ~(uintptr_t)7) == w0 ? x0 : x1;
+        const unsigned b = (unsigned)(x >> (8 * (ad & 7))) & 0xFFu;
+        const unsigned l = b | 0x20u;
+        bad |= !(l == 'a' || l == 'c' || l == 'g' || l == 't');
+        c = ((b >> 1) ^ (b >> 2)) & 3u;   /* A0 C1 G2 T3, either case */
+      }
+      code16 |= c << (14 - 2 * i);
+    }
+  }
+  /* word q = bases [c0 + 32q, +32): lanes 4q .. 4q+3, 16 bits each, first base highest */
+  const unsigned n1 = __shfl_down_sync(~0u, code16, 1), n2 = __shfl_down_sync(~0u, code16, 2),
+                 n3 = __shfl_down_sync(~0u, code16, 3);
+  if ((lane & 3) == 0)
+    words[lane >> 2] = ((uint64_t)code16 << 48) | ((uint64_t)n1 << 32) | ((uint64_t)n2 << 16) | (uint64_t)n3;
+  if (lane < 3) words[8 + lane] = 0;
+  __syncwarp();
+  return __any_sync(~0u, bad);
+}
+
 __global__ void __launch_bounds__(WX_TPB, 3) k_extract_w(const uint64_t *rstart, const uint64_t *rend, uint64_t r0,
                                                          uint64_t r1, const XItem *items, uint64_t n_items,
                                                          uint32_t item_reads, int k, const XSample *xsamp,
@@ -1102,6 +1177,7 @@ __global__ void __launch_bounds__(WX_TPB, 3) k_extract_w(const uint64_t *rstart,
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   S.cpos[tid] = 0;
   S.cend[tid] = 0;
+  for (int i = tid; i < HLL_M / 4; i += WX_TPB) S.hll[i] = 0;
   if (tid == 0) { S.n = 0; S.overflow = 0; }
   const uint64_t nit = items ? n_items : (r1 - r0 + item_reads - 1) / item_reads;
   /* a contiguous range of items per block */
@@ -1119,26 +1195,33 @@ __global__ void __launch_bounds__(WX_TPB, 3) k_extract_w(const uint64_t *rstart,
       if (cur_s != ~0u) {
         if (S.n) wx_flush(S, xs, cur_s, records, bucket_cnt);
         wx_close(S, xs, records);
+        hll_flush(S, hll + (uint64_t)cur_s * HLL_M);
       }
       cur_s = s;
       xs = xsamp[s];
     }
     if (tid == 0) { S.item_next = 0; S.inst = 0; S.used = 0; }
     __syncthreads();
-    unsigned int *hreg = hll + (uint64_t)s * HLL_M;
     const unsigned char *sp = nullptr;
     uint32_t L = 0, npos = 0, p0 = 0;
     bool have = false;
     unsigned long long inst = 0, used = 0;
+    /* the warp's next read, its span loaded ahead while the current one is processed */
+    uint64_t nr = ~0ull, ns = 0, ne = 0;
+    auto grab = [&]() {
+      unsigned idx = 0;
+      if (lane == 0) idx = atomicAdd(&S.item_next, 1u);
+      idx = __shfl_sync(~0u, idx, 0);
+      nr = a + idx < b ? a + idx : ~0ull;
+      if (nr != ~0ull) { ns = rstart[nr]; ne = rend[nr]; }
+    };
+    grab();
     for (;;) {
       while (!have) {   /* this warp's next usable read of the item */
-        unsigned idx = 0;
-        if (lane == 0) idx = atomicAdd(&S.item_next, 1u);
-        idx = __shfl_sync(~0u, idx, 0);
-        if (a + idx >= b) break;
-        const uint64_t r = a + idx;
-        sp = (const unsigned char *)rstart[r];
-        L = (uint32_t)(rend[r] - rstart[r]);
+        if (nr == ~0ull) break;
+        sp = (const unsigned char *)ns;
+        L = (uint32_t)(ne - ns);
+        grab();
         if (L < (uint32_t)k + 2) continue;           /* shorter than the k+2 window */
         npos = L - k + 1;
         if (npos > (uint32_t)WX_SUB) {                /* long read: the N filter before any record */
@@ -1153,7 +1236,7 @@ __global__ void __launch_bounds__(WX_TPB, 3) k_extract_w(const uint64_t *rstart,
       if (have) {
         const uint32_t pend = min(npos, p0 + WX_SUB);
         __syncwarp();
-        const bool bad = stage_chunk(ReadView{sp, L}, p0, pend, k, S.words[wid], lane);
+        const bool bad = stage_window(sp, L, (long long)p0 - 32, S.words[wid], lane);
         if (bad) {
           have = false;                                /* a short read with N: dropped whole */
         } else {
@@ -1169,7 +1252,7 @@ __global__ void __launch_bounds__(WX_TPB, 3) k_extract_w(const uint64_t *rstart,
               if ((h & ((1u << HLL_SAMPLE) - 1)) == 0) {
                 const unsigned idx = (unsigned)(h >> (62 - HLL_P));
                 const unsigned rho = (unsigned)__clzll((h << (2 + HLL_P)) | (1ull << (1 + HLL_P))) + 1u;
-                if (rho > hreg[idx]) atomicMax(&hreg[idx], rho);
+                if (rho > ((S.hll[idx >> 2] >> (8 * (idx & 3))) & 0xFFu)) hll_max_u8(S.hll, idx, rho);
               }
             }
             const unsigned m = __ballot_sync(~0u, valid);
@@ -1207,6 +1290,7 @@ __global__ void __launch_bounds__(WX_TPB, 3) k_extract_w(const uint64_t *rstart,
   if (cur_s != ~0u) {
     if (S.n) wx_flush(S, xs, cur_s, records, bucket_cnt);
     wx_close(S, xs, records);
+    hll_flush(S, hll + (uint64_t)cur_s * HLL_M);
   }
   if (tid == 0 && S.overflow) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
 }
@@ -1307,6 +1391,8 @@ struct FilterArgs {
   uint32_t max_probe;
   uint64_t *f_keys; uint8_t *f_edges; uint32_t *f_counts; uint64_t f_cap;
   const BigRes *big; uint64_t n_big;   /* entries counted past 2^24, for exact filtered counts */
+  const SGeom *sg; uint32_t S;         /* a batch of S samples (S = 1: the plain build) */
+  unsigned long long *s_tally;         /* per-sample tallies (batch only) */
   DevCounters *ctr;
 };
 
@@ -1335,6 +1421,7 @@ struct FilterTally {
   unsigned long long nodes = 0, branch = 0, chain = 0;
   FlagHist hist;
   int kind = 0;          /* the last k-mer: 0 not a node, 1 chain node, 2 branch node */
+  uint32_t sample = 0;   /* the sample of the k-mer being filtered (batch) */
 };
 
 /* v[c] for a run-time c in 0..3, as selects */
@@ -1475,7 +1562,7 @@ __device__ __forceinline__ void filter_kmer(uint64_t *s, uint64_t slot_index, KT
     if (oddk && c16[4 + c] > 0 && high && (last == 3u - c || last == (unsigned)c)) k1pal = true;
   }
   const bool is_branch = din >= 2 || dout >= 2 || kpal || k1pal;
-  const uint32_t flags = is_branch ? NF_BRANCH : NF_CHAIN;
+  const uint32_t flags = (is_branch ? NF_BRANCH : NF_CHAIN) | (t.sample << NF_SAMPLE_SHIFT);
   ++t.nodes; t.branch += is_branch; t.chain += !is_branch;
   /* chain nodes get their chain index (slot aux) when the block flushes its node list */
   t.kind = is_branch ? 2 : 1;
@@ -1496,7 +1583,7 @@ __device__ __noinline__ void filter_wide_global(uint64_t *s, uint64_t i, KT key,
   uint32_t all[25];
   int ne = NE;
   for (int q = 0; q < NE; ++q) all[q] = w[q];
-  Probe pr(a.g, i);
+  Probe pr(a.S > 1 ? a.sg[t.sample].g : a.g, i);   /* inside the k-mer's own partition */
   for (uint32_t probe = 1; probe < a.max_probe; ++probe) {
     pr.next();
     uint64_t *s2 = a.table + pr.i * SU;
@@ -1520,8 +1607,18 @@ __device__ __noinline__ void filter_wide_global(uint64_t *s, uint64_t i, KT key,
  * bits of the mix); k_count_local then gives each partition to one CTA, which counts the
  * partition's records into shared memory with shared-memory atomics and writes the finished
  * slot region to the table once, in coalesced 16-byte stores. */
-constexpr int PART_SLOTS = 3072;           /* 96 KB of slots */
-constexpr int PTPB = 512;
+constexpr int PART_SLOTS = 3072;           /* 96 KB of slots: the largest region */
+constexpr int PTPB = 512;                  /* k_count_local threads unless cfg.count_threads says otherwise */
+/* the tunables of the shared-memory count: the largest partition region (which bounds every
+ * probe run; cfg.part_slots, 256..3072) and the counting block's threads (cfg.count_threads) */
+uint64_t part_slots(const Ctx *c) {
+  const int v = c->cfg.part_slots;
+  return v <= 0 ? (uint64_t)PART_SLOTS : (uint64_t)std::max(256, std::min(PART_SLOTS, v));
+}
+int count_threads(const Ctx *c) {
+  const int v = c->cfg.count_threads;
+  return (v == 256 || v == 512 || v == 1024) ? v : PTPB;
+}
 constexpr int MAX_SPLIT_BITS = 10;
 constexpr int SPLIT_ROUND = 16;            /* records per thread per round */
 constexpr int SPLIT_REC = XTPB * SPLIT_ROUND;   /* 8192 records a round */
@@ -1536,99 +1633,105 @@ struct SplitSmem {
   int overflow;
 };
 
-/* bucket blockIdx.y -> its 2^sbits partitions; every block takes one contiguous share and
- * moves it in rounds of SPLIT_REC records, a counting sort each: the records stay in
- * registers while a shared-memory histogram gives each its rank in its partition, a block
- * scan turns the histogram into offsets, one reservation per partition and round claims the
- * output run, and the records, scattered into partition order in shared memory, go out in
- * one coalesced pass. */
-__global__ void __launch_bounds__(XTPB, 2) k_split(const uint64_t *records, const unsigned long long *bucket_cnt,
-                                                 uint64_t cap, int sbits, uint64_t *out, uint64_t cap2,
+/* A bucket of sample s -> its 2^sbits partitions (sbits = the sample's partition bits - 8): work
+ * items are pieces [lo, hi) of one bucket, and a block moves its items in rounds of SPLIT_REC
+ * records, a counting sort each: the records stay in registers while a shared-memory histogram
+ * gives each its rank in its partition, a block scan turns the histogram into offsets, one
+ * reservation per partition and round claims the output run, and the records, scattered into
+ * partition order in shared memory, go out in one coalesced pass. */
+struct SplitItem { unsigned long long lo, hi; unsigned int gb, pad; };   /* gb = sample * 256 + bucket */
+
+__global__ void __launch_bounds__(XTPB, 2) k_split(const uint64_t *records, const XSample *xs, const SGeom *sg,
+                                                 const SplitItem *items, uint64_t n_items, uint64_t *out,
                                                  unsigned long long *sub_cnt, DevCounters *ctr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SplitSmem &S = *reinterpret_cast<SplitSmem *>(smem_raw);
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nq = 1 << sbits, b = blockIdx.y;
-  for (int i = tid; i < nq; i += XTPB) S.cnt[i] = 0;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int i = tid; i < (1 << MAX_SPLIT_BITS); i += XTPB) S.cnt[i] = 0;   /* every round re-zeroes what it used */
   if (tid == 0) S.overflow = 0;
   __syncthreads();
-  const uint64_t n = min((unsigned long long)cap, bucket_cnt[b]);
-  const uint64_t per = (n + gridDim.x - 1) / gridDim.x;
-  const uint64_t lo = min(n, (uint64_t)blockIdx.x * per), hi = min(n, lo + per);
-  const uint64_t *rb = records + (uint64_t)b * cap;
-  const int shift = 5 + LOW_BITS - sbits;
-  for (uint64_t r0 = lo; r0 < hi; r0 += SPLIT_REC) {
-    uint64_t recs[SPLIT_ROUND];   /* every load of the round is in flight before the first use */
-    uint32_t pos[SPLIT_ROUND];    /* partition << 16 | rank in it; ~0 past the end */
-    #pragma unroll
-    for (int j = 0; j < SPLIT_ROUND; ++j) {
-      const uint64_t i = r0 + (uint64_t)j * XTPB + tid;
-      recs[j] = i < hi ? __ldcs(rb + i) : 0ull;
-    }
-    #pragma unroll
-    for (int j = 0; j < SPLIT_ROUND; ++j) {
-      const uint64_t i = r0 + (uint64_t)j * XTPB + tid;
-      pos[j] = ~0u;
-      if (i < hi && recs[j] != 0ull) {   /* 0: an unused chunk tail */
-        const unsigned sq = (unsigned)(recs[j] >> shift) & (unsigned)(nq - 1);
-        pos[j] = (sq << 16) | atomicAdd(&S.cnt[sq], 1u);
-      }
-    }
-    __syncthreads();
-    /* exclusive scan of the histogram (two partitions a thread) and the reservations */
-    const int q0 = 2 * tid;
-    const unsigned c0 = q0 < nq ? S.cnt[q0] : 0u, c1 = q0 + 1 < nq ? S.cnt[q0 + 1] : 0u;
-    if (q0 < nq) S.cnt[q0] = 0;
-    if (q0 + 1 < nq) S.cnt[q0 + 1] = 0;
-    const unsigned v = c0 + c1;
-    unsigned x = v;
-    #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned y = __shfl_up_sync(~0u, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) S.wsum[wid] = x;
-    __syncthreads();
-    if (wid == 0) {
-      const unsigned w = lane < XTPB / 32 ? S.wsum[lane] : 0u;
-      unsigned z = w;
+  for (uint64_t it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const SplitItem item = items[it];
+    const unsigned smp = item.gb >> NBUCKET_BITS, b = item.gb & (NBUCKET - 1);
+    const XSample X = xs[smp];
+    const SGeom G = sg[smp];
+    const int sbits = G.g.pbits - NBUCKET_BITS, nq = 1 << sbits;
+    const uint64_t *rb = records + X.rec_base + (uint64_t)b * X.cap;
+    const int shift = 5 + LOW_BITS - sbits;
+    for (uint64_t r0 = item.lo; r0 < item.hi; r0 += SPLIT_REC) {
+      uint64_t recs[SPLIT_ROUND];   /* every load of the round is in flight before the first use */
+      uint32_t pos[SPLIT_ROUND];    /* partition << 16 | rank in it; ~0 past the end */
       #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(~0u, z, o);
-        if (lane >= o) z += y;
+      for (int j = 0; j < SPLIT_ROUND; ++j) {
+        const uint64_t i = r0 + (uint64_t)j * XTPB + tid;
+        recs[j] = i < item.hi ? __ldcs(rb + i) : 0ull;
       }
-      if (lane < XTPB / 32) S.wsum[lane] = z - w;
-      if (lane == XTPB / 32 - 1) S.wsum_total = z;
-    }
-    __syncthreads();
-    const unsigned ex = S.wsum[wid] + x - v;
-    #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int q = q0 + h;
-      const unsigned c = h ? c1 : c0;
-      if (q < nq) {
-        S.start[q] = h ? ex + c0 : ex;
-        if (c) {
-          const uint64_t part = ((uint64_t)b << sbits) | (unsigned)q;
-          const unsigned long long old = atomicAdd(&sub_cnt[part], (unsigned long long)c);
-          if (old + c > cap2) S.overflow = 1;
-          S.base[q] = part * cap2 + old;
+      #pragma unroll
+      for (int j = 0; j < SPLIT_ROUND; ++j) {
+        const uint64_t i = r0 + (uint64_t)j * XTPB + tid;
+        pos[j] = ~0u;
+        if (i < item.hi && recs[j] != 0ull) {   /* 0: an unused chunk tail */
+          const unsigned sq = (unsigned)(recs[j] >> shift) & (unsigned)(nq - 1);
+          pos[j] = (sq << 16) | atomicAdd(&S.cnt[sq], 1u);
         }
       }
+      __syncthreads();
+      /* exclusive scan of the histogram (two partitions a thread) and the reservations */
+      const int q0 = 2 * tid;
+      const unsigned c0 = q0 < nq ? S.cnt[q0] : 0u, c1 = q0 + 1 < nq ? S.cnt[q0 + 1] : 0u;
+      if (q0 < nq) S.cnt[q0] = 0;
+      if (q0 + 1 < nq) S.cnt[q0 + 1] = 0;
+      const unsigned v = c0 + c1;
+      unsigned x = v;
+      #pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(~0u, x, o);
+        if (lane >= o) x += y;
+      }
+      if (lane == 31) S.wsum[wid] = x;
+      __syncthreads();
+      if (wid == 0) {
+        const unsigned w = lane < XTPB / 32 ? S.wsum[lane] : 0u;
+        unsigned z = w;
+        #pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const unsigned y = __shfl_up_sync(~0u, z, o);
+          if (lane >= o) z += y;
+        }
+        if (lane < XTPB / 32) S.wsum[lane] = z - w;
+        if (lane == XTPB / 32 - 1) S.wsum_total = z;
+      }
+      __syncthreads();
+      const unsigned ex = S.wsum[wid] + x - v;
+      #pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int q = q0 + h;
+        const unsigned c = h ? c1 : c0;
+        if (q < nq) {
+          S.start[q] = h ? ex + c0 : ex;
+          if (c) {
+            const uint64_t j = ((uint64_t)b << sbits) | (unsigned)q;   /* the sample's partition */
+            const unsigned long long old = atomicAdd(&sub_cnt[G.pbase + j], (unsigned long long)c);
+            if (old + c > G.cap2) S.overflow = 1;
+            S.base[q] = G.rec2_base + j * G.cap2 + old;
+          }
+        }
+      }
+      __syncthreads();
+      #pragma unroll
+      for (int j = 0; j < SPLIT_ROUND; ++j)
+        if (pos[j] != ~0u) S.buf[S.start[pos[j] >> 16] + (pos[j] & 0xFFFFu)] = recs[j];
+      __syncthreads();
+      const unsigned nr = S.wsum_total;   /* the round's records, holes left out */
+      for (unsigned y = tid; y < nr; y += XTPB) {
+        const uint64_t rec = S.buf[y];
+        const unsigned q = (unsigned)(rec >> shift) & (unsigned)(nq - 1);
+        const uint64_t j = ((uint64_t)b << sbits) | q;
+        const unsigned long long dst = S.base[q] + (y - S.start[q]);
+        if (dst < G.rec2_base + (j + 1) * G.cap2) out[dst] = rec;
+      }
+      __syncthreads();   /* the next round writes buf, start and base */
     }
-    __syncthreads();
-    #pragma unroll
-    for (int j = 0; j < SPLIT_ROUND; ++j)
-      if (pos[j] != ~0u) S.buf[S.start[pos[j] >> 16] + (pos[j] & 0xFFFFu)] = recs[j];
-    __syncthreads();
-    const unsigned nr = S.wsum_total;   /* the round's records, holes left out */
-    for (unsigned y = tid; y < nr; y += XTPB) {
-      const uint64_t rec = S.buf[y];
-      const unsigned q = (unsigned)(rec >> shift) & (unsigned)(nq - 1);
-      const uint64_t part = ((uint64_t)b << sbits) | q;
-      const unsigned long long dst = S.base[q] + (y - S.start[q]);
-      if (dst < (part + 1) * cap2) out[dst] = rec;
-    }
-    /* the next round writes buf, start and base only after its first two barriers */
   }
   if (tid == 0 && S.overflow) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
 }
@@ -1711,39 +1814,49 @@ __device__ __forceinline__ bool sm_count(uint64_t *sm, uint32_t sm_base, uint32_
   return false;
 }
 
-/* one CTA per partition: clear the slots, count the partition's records, write back */
-__global__ void __launch_bounds__(PTPB) k_count_local(const uint64_t *recs, const unsigned long long *rec_cnt,
-                                                       uint64_t rcap, int sbits, uint64_t *table, TableGeom g,
-                                                       DevCounters *ctr) {
+/* One CTA per partition (blockIdx.x counts the partitions of all samples): clear the slots, count
+ * the partition's records into them, write the region back.  Partition j of sample s holds the
+ * records whose mix has j in its top pbits bits: the bucket (top 8) and the split bits. */
+__global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, const unsigned long long *rec_cnt,
+                                                       const SGeom *sg, uint32_t nsamples, uint64_t *table,
+                                                       unsigned long long *s_tally, DevCounters *ctr) {
   extern __shared__ __align__(16) uint64_t sm[];
   const uint64_t part = blockIdx.x;
-  const uint32_t region = (uint32_t)g.region;
+  const uint32_t smp = sample_of_part(sg, nsamples, part);
+  const SGeom G = sg[smp];
+  const uint64_t j = part - G.pbase;
+  const int sbits = G.g.pbits - NBUCKET_BITS;
+  const uint32_t region = (uint32_t)G.g.region;
   const int tid = threadIdx.x;
-  for (uint32_t w = tid; w < region * 4u; w += PTPB) sm[w] = (w & 3u) == 0 ? KEY_EMPTY : 0ull;
+  const uint32_t nt = blockDim.x;   /* the block shape is a tunable (cfg.count_threads) */
+  for (uint32_t w = tid; w < region * 4u; w += nt) sm[w] = (w & 3u) == 0 ? KEY_EMPTY : 0ull;
   __syncthreads();
   const uint32_t sm_base = (uint32_t)__cvta_generic_to_shared(sm);
-  const uint64_t n = min((unsigned long long)rcap, rec_cnt[part]);
-  const uint64_t *rp = recs + part * rcap;
-  const uint64_t bucket_hi = (part >> sbits) << LOW_BITS;   /* bucket bits of the mix */
+  const uint64_t n = min((unsigned long long)G.cap2, rec_cnt[part]);
+  const uint64_t *rp = recs + G.rec2_base + j * G.cap2;
+  const uint64_t bucket_hi = (j >> sbits) << LOW_BITS;   /* bucket bits of the mix */
   unsigned long long slots = 0, entries = 0;
   bool full = false;
   uint64_t nxt = tid < n ? __ldcs(rp + tid) : 0ull;
-  for (uint64_t i = tid; i < n; i += PTPB) {
+  for (uint64_t i = tid; i < n; i += nt) {
     const uint64_t rec = nxt;
-    nxt = i + PTPB < n ? __ldcs(rp + i + PTPB) : 0ull;
+    nxt = i + nt < n ? __ldcs(rp + i + nt) : 0ull;
     if (rec == 0ull) continue;   /* an unused chunk tail, when the buckets are the partitions */
     const uint64_t h = bucket_hi | (rec >> 5);
-    const uint32_t home = (uint32_t)__umul64hi(h << (2 + g.pbits), g.region);
+    const uint32_t home = (uint32_t)__umul64hi(h << (2 + G.g.pbits), G.g.region);
     if (!sm_count(sm, sm_base, region, h, (unsigned)(rec & 31), home, slots, entries)) full = true;
   }
   __syncthreads();
-  ulonglong2 *dst = reinterpret_cast<ulonglong2 *>(table + part * g.region * 4);
+  ulonglong2 *dst = reinterpret_cast<ulonglong2 *>(table + (G.g.base + j * G.g.region) * 4);
   const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(sm);
-  for (uint32_t v = tid; v < region * 2u; v += PTPB) dst[v] = src[v];
+  for (uint32_t v = tid; v < region * 2u; v += nt) dst[v] = src[v];
   slots = warp_sum(slots); entries = warp_sum(entries);
   if ((tid & 31) == 0) {   /* reductions without a returned value: nothing waits on them */
     if (slots) atomicAdd(&ctr->n_slots_claimed, slots);
-    if (entries) atomicAdd(&ctr->n_entries, entries);
+    if (entries) {
+      atomicAdd(&ctr->n_entries, entries);
+      if (s_tally) atomicAdd(&s_tally[(uint64_t)smp * T_NUM + T_ENTRIES], entries);
+    }
   }
   if (full) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
 }
@@ -1807,6 +1920,14 @@ __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
   t.hist.clear();
   for (uint64_t c0 = (uint64_t)blockIdx.x * FCHUNK; c0 < a.nslots; c0 += (uint64_t)gridDim.x * FCHUNK) {
     if (tid == 0) { s_nc = 0; s_nb = 0; s_ncand = 0; }
+    /* a batch: the chunk's slots belong to sample s0 up to `bound` and to s0 + 1 after it (a
+     * sample has at least 256 partitions of 64 slots, more than a chunk) */
+    uint32_t s0 = 0;
+    uint64_t bound = ~0ull;
+    if (a.S > 1) {
+      s0 = sample_of_slot(a.sg, a.S, c0);
+      if (s0 + 1 < a.S) bound = a.sg[s0 + 1].g.base;
+    }
     __syncthreads();
     if (t.hist.n >= FlagHist::DRAIN) {   /* drain the 16-bit bins long before they could wrap */
       #pragma unroll
@@ -1862,6 +1983,7 @@ __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
         ne += w[q] != 0;
       }
       t.kind = 0;
+      t.sample = i < bound ? s0 : s0 + 1;
       if (ne < NE) filter_kmer<KT, NE, false>(s, i, key, w, ne, a, t);
       else filter_wide_global<KT>(s, i, key, w, a, t);   /* continuation slots */
       if (t.kind == 1) s_chain[atomicAdd(&s_nc, 1u)] = (uint32_t)i;
@@ -1884,6 +2006,19 @@ __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
     }
     for (unsigned x = tid; x < s_nb; x += TPB)
       if (s_base_b + x < a.list_cap) a.branch_list[s_base_b + x] = s_branch[x];
+    if (a.s_tally) {   /* per-sample node tallies: the chunk's nodes past `bound` are s0 + 1's */
+      unsigned hc = 0, hb = 0;
+      for (unsigned x = tid; x < s_nc; x += TPB) hc += s_chain[x] >= bound;
+      for (unsigned x = tid; x < s_nb; x += TPB) hb += s_branch[x] >= bound;
+      hc = (unsigned)warp_sum(hc); hb = (unsigned)warp_sum(hb);
+      if (lane == 0 && hc) atomicAdd(&a.s_tally[(uint64_t)(s0 + 1) * T_NUM + T_CHAIN], (unsigned long long)hc);
+      if (lane == 0 && hb) atomicAdd(&a.s_tally[(uint64_t)(s0 + 1) * T_NUM + T_BRANCH], (unsigned long long)hb);
+      if (tid == 0 && s_nc) atomicAdd(&a.s_tally[(uint64_t)s0 * T_NUM + T_CHAIN], (unsigned long long)s_nc);
+      if (tid == 0 && s_nb) atomicAdd(&a.s_tally[(uint64_t)s0 * T_NUM + T_BRANCH], (unsigned long long)s_nb);
+      /* s0 got every node of the chunk: take back those past `bound` */
+      if (lane == 0 && hc) atomicAdd(&a.s_tally[(uint64_t)s0 * T_NUM + T_CHAIN], (unsigned long long)(0 - (unsigned long long)hc));
+      if (lane == 0 && hb) atomicAdd(&a.s_tally[(uint64_t)s0 * T_NUM + T_BRANCH], (unsigned long long)(0 - (unsigned long long)hb));
+    }
     __syncthreads();   /* every thread has read s_nc / s_nb before the next chunk resets them */
   }
   unsigned long long nodes = warp_sum(t.nodes);
@@ -1917,7 +2052,7 @@ __global__ void __launch_bounds__(TPB) k_dump_nodes(const uint64_t *table, uint6
       counts[o * 9 + 4 + q] = (uint16_t)(pw[1] >> (16 * q));
     }
     counts[o * 9 + 8] = (uint16_t)pw[2];
-    if (flags) flags[o] = (uint8_t)(pw[2] >> 16);
+    if (flags) flags[o] = (uint8_t)((pw[2] >> 16) & (NF_BRANCH | NF_CHAIN));
   }
 }
 
@@ -2143,20 +2278,97 @@ bruno_status extract_begin(Ctx *c, uint64_t upper, int max_blocks) {
   c->xchunk = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(512, margin / (2ull * max_blocks)));
   c->xblk = 0;
   c->xblk_max = max_blocks;
-  if (!c->cfg.edge_filter) {   /* the warp-per-read extraction: one sample, its HyperLogLog */
+  /* the bucket layout of the one sample (the split reads it too) */
+  if ((st = ensure(c, c->xsamp, sizeof(XSample))) != BRUNO_OK) return st;
+  const XSample xs{0ull, cap, c->xchunk, 0u};
+  if ((st = cuda_check(c, cudaMemcpyAsync(c->xsamp.p, &xs, sizeof(xs), cudaMemcpyHostToDevice, c->stream),
+                       "extraction layout")) != BRUNO_OK)
+    return st;
+  if (!c->cfg.edge_filter) {   /* the warp-per-read extraction and its HyperLogLog */
     static const bool wattr = [] {
       cudaFuncSetAttribute(k_extract_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(WXSmem));
       return true;
     }();
     (void)wattr;
-    if ((st = ensure(c, c->xsamp, sizeof(XSample))) != BRUNO_OK) return st;
     if ((st = ensure(c, c->hllreg, HLL_M * 4)) != BRUNO_OK) return st;
-    const XSample xs{0ull, cap, c->xchunk, 0u};
-    if ((st = cuda_check(c, cudaMemcpyAsync(c->xsamp.p, &xs, sizeof(xs), cudaMemcpyHostToDevice, c->stream),
-                         "extraction layout")) != BRUNO_OK)
-      return st;
     cudaMemsetAsync(c->hllreg.p, 0, HLL_M * 4, c->stream);
   }
+  return BRUNO_OK;
+}
+
+/* The shared-memory count of every partition of every sample (sg: per sample its table
+ * geometry and first partition; caps: its bucket capacity).  Buckets are split into their
+ * partitions first unless the one sample has no split bits (its buckets are the partitions).
+ * ok = false when a skewed input overflowed a partition's split capacity or an entry could pass
+ * 2^24 occurrences in shared memory: nothing was counted and the caller falls back. */
+bruno_status split_and_count(Ctx *c, std::vector<SGeom> &sg, const std::vector<uint64_t> &caps, bool &ok,
+                             unsigned long long *s_tally) {
+  bruno_status st;
+  ok = false;
+  const uint32_t S = (uint32_t)sg.size();
+  bool split = S > 1;
+  for (uint32_t q = 0; q < S; ++q) split |= sg[q].g.pbits > NBUCKET_BITS;
+  uint64_t r2 = 0, cap2_max = 0, region_max = 0;
+  for (uint32_t q = 0; q < S; ++q) {
+    const int sbits = sg[q].g.pbits - NBUCKET_BITS;
+    sg[q].rec2_base = split ? r2 : 0;
+    sg[q].cap2 = split ? (caps[q] >> sbits) + (caps[q] >> sbits) / 8 + 1024 : caps[q];
+    r2 += (uint64_t)sg[q].cap2 << sg[q].g.pbits;
+    cap2_max = std::max(cap2_max, sg[q].cap2);
+    region_max = std::max<uint64_t>(region_max, sg[q].g.region);
+  }
+  if (cap2_max >= (1ull << 24)) return BRUNO_OK;   /* counts could pass 2^24 in shared memory */
+  const uint64_t nparts = sg.back().pbase + (1ull << sg.back().g.pbits);
+  if ((st = ensure(c, c->sgeom, S * sizeof(SGeom))) != BRUNO_OK) return st;
+  if ((st = cuda_check(c, cudaMemcpyAsync(c->sgeom.p, sg.data(), S * sizeof(SGeom), cudaMemcpyHostToDevice, c->stream),
+                       "sample geometry")) != BRUNO_OK)
+    return st;
+  const uint64_t *recs = (const uint64_t *)c->records.p;
+  const unsigned long long *cnts = (const unsigned long long *)c->bucket_cnt.p;
+  cudaEventRecord(c->kev[4], c->stream);
+  if (split) {
+    if ((st = ensure(c, c->records2, (size_t)(r2 * 8))) != BRUNO_OK) return st;
+    if ((st = ensure(c, c->sub_cnt, (size_t)(nparts * 8))) != BRUNO_OK) return st;
+    cudaMemsetAsync(c->sub_cnt.p, 0, nparts * 8, c->stream);
+    /* items: pieces of every bucket, from the bucket counts */
+    std::vector<unsigned long long> bc((size_t)S * NBUCKET);
+    if ((st = cuda_check(c, cudaMemcpyAsync(bc.data(), c->bucket_cnt.p, bc.size() * 8, cudaMemcpyDeviceToHost,
+                                            c->stream), "bucket counts")) != BRUNO_OK)
+      return st;
+    if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "bucket counts")) != BRUNO_OK) return st;
+    constexpr uint64_t PIECE = 16ull * SPLIT_REC;
+    std::vector<SplitItem> items;
+    for (uint32_t gb = 0; gb < S * NBUCKET; ++gb) {
+      const uint64_t n = std::min<uint64_t>(caps[gb / NBUCKET], bc[gb]);
+      for (uint64_t lo = 0; lo < n; lo += PIECE) items.push_back(SplitItem{lo, std::min(n, lo + PIECE), gb, 0u});
+    }
+    if (!items.empty()) {
+      if ((st = ensure(c, c->split_items, items.size() * sizeof(SplitItem))) != BRUNO_OK) return st;
+      if ((st = cuda_check(c, cudaMemcpyAsync(c->split_items.p, items.data(), items.size() * sizeof(SplitItem),
+                                              cudaMemcpyHostToDevice, c->stream), "split items")) != BRUNO_OK)
+        return st;
+      const int grid = (int)std::min<uint64_t>(items.size(), (uint64_t)num_sms() * 2);
+      k_split<<<grid, XTPB, sizeof(SplitSmem), c->stream>>>((const uint64_t *)c->records.p,
+                                                             (const XSample *)c->xsamp.p, (const SGeom *)c->sgeom.p,
+                                                             (const SplitItem *)c->split_items.p, items.size(),
+                                                             (uint64_t *)c->records2.p,
+                                                             (unsigned long long *)c->sub_cnt.p, c->dctr);
+      c->launches += 1;
+    }
+    cudaEventRecord(c->kev[4], c->stream);
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    if (c->hctr->err & DERR_TABLE_FULL) {   /* a skewed bucket: the caller falls back */
+      cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
+      return BRUNO_OK;
+    }
+    recs = (const uint64_t *)c->records2.p;
+    cnts = (const unsigned long long *)c->sub_cnt.p;
+  }
+  k_count_local<<<(unsigned)nparts, count_threads(c), (unsigned)(region_max * 32), c->stream>>>(
+      recs, cnts, (const SGeom *)c->sgeom.p, S, (uint64_t *)c->table.p, s_tally, c->dctr);
+  c->launches += 1;
+  if ((st = cuda_check(c, cudaGetLastError(), "k_count_local")) != BRUNO_OK) return st;
+  ok = true;
   return BRUNO_OK;
 }
 
@@ -2244,54 +2456,24 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
   for (int attempt = 0; attempt < 4; ++attempt) {
     /* shared-memory path: 2^pb partitions (pb >= 8) small enough for one CTA's shared memory */
     int pb = NBUCKET_BITS;
-    while (pb < NBUCKET_BITS + MAX_SPLIT_BITS && (slots + (1ull << pb) - 1) >> pb > (uint64_t)PART_SLOTS) ++pb;
+    while (pb < NBUCKET_BITS + MAX_SPLIT_BITS && (slots + (1ull << pb) - 1) >> pb > part_slots(c)) ++pb;
     const uint64_t region_c = std::max<uint64_t>(64, (slots + (1ull << pb) - 1) >> pb);
     bool counted = false, counted_local = false;
     cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
     cudaMemsetAsync(&c->dctr->n_slots_claimed, 0, 16, c->stream);
     cudaMemsetAsync(c->dctr->big_key, 0, sizeof(c->dctr->big_key) + sizeof(c->dctr->big_cnt), c->stream);
     cudaMemsetAsync(&c->dctr->n_big, 0, 8, c->stream);
-    if (region_c <= (uint64_t)PART_SLOTS && c->force_direct_count != 2) {
+    if (region_c <= part_slots(c) && c->force_direct_count != 2) {
       c->geom = TableGeom{region_c << pb, region_c, pb};
       c->nslots = c->geom.nslots;
       if ((st = ensure(c, c->table, c->nslots * 32)) != BRUNO_OK) return st;
-      const int sbits = pb - NBUCKET_BITS;
-      const uint64_t nparts = 1ull << pb;
-      const uint64_t *recs = (const uint64_t *)c->records.p;
-      const unsigned long long *cnts = (const unsigned long long *)c->bucket_cnt.p;
-      uint64_t rcap = cap;
       cudaEventRecord(c->kev[2], c->stream);
-      bool split_ok = true;
-      cudaEventRecord(c->kev[4], c->stream);
-      if (sbits > 0) {
-        const uint64_t cap2 = (cap >> sbits) + (cap >> sbits) / 8 + 1024;
-        if ((st = ensure(c, c->records2, (size_t)(nparts * cap2 * 8))) != BRUNO_OK) return st;
-        if ((st = ensure(c, c->sub_cnt, (size_t)(nparts * 8))) != BRUNO_OK) return st;
-        cudaMemsetAsync(c->sub_cnt.p, 0, nparts * 8, c->stream);
-        const int gx = std::max(1, (sms * 16 + NBUCKET - 1) / NBUCKET);
-        k_split<<<dim3(gx, NBUCKET), XTPB, sizeof(SplitSmem), c->stream>>>((const uint64_t *)c->records.p,
-                                                          (const unsigned long long *)c->bucket_cnt.p, cap, sbits,
-                                                          (uint64_t *)c->records2.p, cap2,
-                                                          (unsigned long long *)c->sub_cnt.p, c->dctr);
-        c->launches += 1;
-        cudaEventRecord(c->kev[4], c->stream);
-        if ((st = sync_counters(c)) != BRUNO_OK) return st;
-        split_ok = !(c->hctr->err & DERR_TABLE_FULL);   /* a skewed bucket: use the L2 path below */
-        recs = (const uint64_t *)c->records2.p;
-        cnts = (const unsigned long long *)c->sub_cnt.p;
-        rcap = cap2;
-      }
-      /* a partition counts in shared memory only while no entry can pass 2^24 occurrences
-       * (beyond that the L2 path keeps exact counts in the side table) */
-      if (split_ok && rcap < (1ull << 24)) {
-        k_count_local<<<(unsigned)nparts, PTPB, (unsigned)(region_c * 32), c->stream>>>(
-            recs, cnts, rcap, sbits, (uint64_t *)c->table.p, c->geom, c->dctr);
-        c->launches += 1;
+      std::vector<SGeom> sg{SGeom{c->geom, 0, 0, 0}};
+      bool ok = false;
+      if ((st = split_and_count(c, sg, std::vector<uint64_t>{cap}, ok, nullptr)) != BRUNO_OK) return st;
+      if (ok) {
         cudaEventRecord(c->kev[3], c->stream);
-        if ((st = cuda_check(c, cudaGetLastError(), "k_count_local")) != BRUNO_OK) return st;
         counted = counted_local = true;
-      } else {
-        cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
       }
     }
     if (!counted) {
@@ -2450,6 +2632,9 @@ bruno_status filter_typed(Ctx *c, const uint64_t *thr) {
   a.list_cap = cap;
   a.big = (const BigRes *)c->bigres.p;
   a.n_big = c->n_big;
+  a.S = c->S;
+  a.sg = (const SGeom *)c->sgeom.p;
+  a.s_tally = c->S > 1 ? (unsigned long long *)c->s_tally.p : nullptr;
   if (c->cfg.keep_filtered) {
     const uint64_t n = std::max<uint64_t>(1, c->n_entries);
     if ((st = ensure(c, c->f_keys, n * 8 * Slot<KT>::KEYW)) != BRUNO_OK) return st;
@@ -2470,6 +2655,167 @@ bruno_status filter_typed(Ctx *c, const uint64_t *thr) {
 }
 }  // namespace
 
+namespace {
+/* first read of each sample: the first read whose sequence starts at or after the sample's
+ * first byte (reads are indexed in byte order) */
+__global__ void k_sample_first_read(const uint64_t *rstart, uint64_t nreads, const uint64_t *samp_addr, uint32_t n,
+                                    uint64_t *r0) {
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const uint64_t a = samp_addr[q];
+    uint64_t lo = 0, hi = nreads;
+    while (lo < hi) { const uint64_t m = (lo + hi) >> 1; if (rstart[m] < a) lo = m + 1; else hi = m; }
+    r0[q] = lo;
+  }
+}
+
+}  // namespace
+
+/* The batched form's count: S samples, concatenated in one device copy, each counted into
+ * partitions of its own in one pass of every counting kernel (the plain path's kernels; the
+ * plain build is a batch of one).  Needs k <= 31 and the shared-memory partitions. */
+bruno_status run_count_samples(Ctx *c) {
+  bruno_status st;
+  const uint32_t S = c->S;
+  const int sms = num_sms();
+  if ((st = run_index_reads(c)) != BRUNO_OK) return st;
+  const uint64_t nreads = c->n_reads;
+  /* per sample: its first read */
+  {
+    std::vector<uint64_t> addr(S + 1);
+    const uint64_t base = (uint64_t)(uintptr_t)c->segs[0].ptr;
+    for (uint32_t q = 0; q <= S; ++q) addr[q] = base + c->samp_off[q];
+    Buf da;
+    if ((st = ensure(c, da, (S + 1) * 16)) != BRUNO_OK) return st;
+    cudaMemcpyAsync(da.p, addr.data(), (S + 1) * 8, cudaMemcpyHostToDevice, c->stream);
+    k_sample_first_read<<<(S + 1 + 255) / 256, 256, 0, c->stream>>>((const uint64_t *)c->rstart.p, nreads,
+                                                                    (const uint64_t *)da.p, S + 1,
+                                                                    (uint64_t *)da.p + (S + 1));
+    c->samp_r0.assign(S + 1, 0);
+    cudaMemcpyAsync(c->samp_r0.data(), (uint64_t *)da.p + (S + 1), (S + 1) * 8, cudaMemcpyDeviceToHost, c->stream);
+    st = cuda_check(c, cudaStreamSynchronize(c->stream), "sample reads");
+    cudaFreeAsync(da.p, c->stream);
+    if (st != BRUNO_OK) return st;
+    c->samp_r0[S] = nreads;
+    c->launches += 1;
+  }
+  /* extraction: items of WX_ITEM reads of one sample; per sample its buckets */
+  std::vector<XItem> items;
+  std::vector<uint64_t> items_of(S, 0);
+  for (uint32_t q = 0; q < S; ++q)
+    for (uint64_t a = c->samp_r0[q]; a < c->samp_r0[q + 1]; a += WX_ITEM) {
+      items.push_back(XItem{a, std::min<uint64_t>(c->samp_r0[q + 1], a + WX_ITEM), q, 0u});
+      ++items_of[q];
+    }
+  const int eb = wx_blocks(nreads);
+  const uint64_t per = std::max<uint64_t>(1, (items.size() + eb - 1) / eb);
+  std::vector<XSample> xs(S);
+  std::vector<uint64_t> caps(S);
+  uint64_t rec_total = 0;
+  for (uint32_t q = 0; q < S; ++q) {
+    const uint64_t upper = (c->samp_off[q + 1] - c->samp_off[q]) / 2 + 1;   /* k-mer positions <= bytes / 2 */
+    const uint64_t cap = upper / NBUCKET + upper / (NBUCKET * 12) + 4096;
+    const uint64_t touching = (items_of[q] + per - 1) / per + 1;   /* blocks whose chunks can hold its records */
+    const uint64_t margin = cap - upper / NBUCKET;
+    xs[q] = XSample{rec_total, cap, (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(512, margin / (2 * touching))), 0u};
+    caps[q] = cap;
+    rec_total += cap * NBUCKET;
+  }
+  if ((st = ensure(c, c->records, rec_total * 8)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->bucket_cnt, (size_t)S * NBUCKET * 8)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->xsamp, S * sizeof(XSample))) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->hllreg, (size_t)S * HLL_M * 4)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->s_inst, (size_t)S * 8)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->s_used, (size_t)S * 8)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->s_tally, (size_t)S * T_NUM * 8)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->hsum, (size_t)S * 16)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->xitems, std::max<size_t>(1, items.size()) * sizeof(XItem))) != BRUNO_OK) return st;
+  cudaMemsetAsync(c->bucket_cnt.p, 0, (size_t)S * NBUCKET * 8, c->stream);
+  cudaMemsetAsync(c->hllreg.p, 0, (size_t)S * HLL_M * 4, c->stream);
+  cudaMemsetAsync(c->s_inst.p, 0, (size_t)S * 8, c->stream);
+  cudaMemsetAsync(c->s_used.p, 0, (size_t)S * 8, c->stream);
+  cudaMemsetAsync(c->s_tally.p, 0, (size_t)S * T_NUM * 8, c->stream);
+  cudaMemcpyAsync(c->xsamp.p, xs.data(), S * sizeof(XSample), cudaMemcpyHostToDevice, c->stream);
+  if (!items.empty())
+    cudaMemcpyAsync(c->xitems.p, items.data(), items.size() * sizeof(XItem), cudaMemcpyHostToDevice, c->stream);
+  static const bool wattr = [] {
+    cudaFuncSetAttribute(k_extract_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(WXSmem));
+    cudaFuncSetAttribute(k_count_local, cudaFuncAttributeMaxDynamicSharedMemorySize, PART_SLOTS * 32);
+    cudaFuncSetAttribute(k_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SplitSmem));
+    return true;
+  }();
+  (void)wattr;
+  cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
+  cudaEventRecord(c->kev[0], c->stream);
+  if (!items.empty())
+    k_extract_w<<<eb, WX_TPB, sizeof(WXSmem), c->stream>>>(
+        (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, 0, 0, (const XItem *)c->xitems.p, items.size(),
+        WX_ITEM, c->cfg.k, (const XSample *)c->xsamp.p, (uint64_t *)c->records.p,
+        (unsigned long long *)c->bucket_cnt.p, (unsigned int *)c->hllreg.p, (unsigned long long *)c->s_inst.p,
+        (unsigned long long *)c->s_used.p, c->dctr);
+  k_hll_sums<<<S, 256, 0, c->stream>>>((const unsigned int *)c->hllreg.p, (double *)c->hsum.p,
+                                       (unsigned int *)((double *)c->hsum.p + S));
+  c->launches += 2;
+  cudaEventRecord(c->kev[1], c->stream);
+  std::vector<double> hs(2 * S);
+  cudaMemcpyAsync(hs.data(), c->hsum.p, (size_t)S * 16, cudaMemcpyDeviceToHost, c->stream);
+  c->h_inst.assign(S, 0);
+  c->h_used.assign(S, 0);
+  cudaMemcpyAsync(c->h_inst.data(), c->s_inst.p, (size_t)S * 8, cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(c->h_used.data(), c->s_used.p, (size_t)S * 8, cudaMemcpyDeviceToHost, c->stream);
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  if (c->hctr->err & DERR_TABLE_FULL)
+    return set_err(c, BRUNO_ERR_TABLE_FULL, "batch: a sample's hash bucket overflowed (a skewed sample)");
+  c->n_instances = c->hctr->n_instances;
+  c->n_reads_used = c->hctr->n_reads_used;
+  const unsigned int *zeros = (const unsigned int *)(hs.data() + S);
+  std::vector<uint64_t> slots(S);
+  for (uint32_t q = 0; q < S; ++q) slots[q] = slots_for(c, hll_sampled_estimate(hs[q], zeros[q]));
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    std::vector<SGeom> sg(S);
+    uint64_t base = 0, pbase = 0;
+    for (uint32_t q = 0; q < S; ++q) {
+      int pb = NBUCKET_BITS;
+      while (pb < NBUCKET_BITS + MAX_SPLIT_BITS && (slots[q] + (1ull << pb) - 1) >> pb > part_slots(c)) ++pb;
+      const uint64_t region = std::max<uint64_t>(64, (slots[q] + (1ull << pb) - 1) >> pb);
+      if (region > part_slots(c))
+        return set_err(c, BRUNO_ERR_ARG, "batch: sample " + std::to_string(q) + " is too large for one batch");
+      sg[q].g = TableGeom{region << pb, region, pb, base};
+      sg[q].pbase = pbase;
+      base += region << pb;
+      pbase += 1ull << pb;
+    }
+    c->nslots = base;
+    c->geom = TableGeom{base, sg[0].g.region, sg[0].g.pbits, 0};
+    if ((st = ensure(c, c->table, c->nslots * 32)) != BRUNO_OK) return st;
+    cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
+    cudaMemsetAsync(&c->dctr->n_slots_claimed, 0, 16, c->stream);
+    cudaMemsetAsync(c->s_tally.p, 0, (size_t)S * T_NUM * 8, c->stream);
+    cudaEventRecord(c->kev[2], c->stream);
+    bool ok = false;
+    if ((st = split_and_count(c, sg, caps, ok, (unsigned long long *)c->s_tally.p)) != BRUNO_OK) return st;
+    if (!ok) return set_err(c, BRUNO_ERR_TABLE_FULL, "batch: a partition of a skewed sample overflowed");
+    cudaEventRecord(c->kev[3], c->stream);
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    if (!(c->hctr->err & DERR_TABLE_FULL)) {
+      c->h_sgeom = sg;
+      c->n_entries = c->hctr->n_entries;
+      c->n_slots_claimed = c->hctr->n_slots_claimed;
+      c->n_big = 0;
+      float ms[3] = {0, 0, 0};
+      cudaEventElapsedTime(&ms[0], c->kev[0], c->kev[1]);
+      cudaEventElapsedTime(&ms[1], c->kev[2], c->kev[4]);
+      cudaEventElapsedTime(&ms[2], c->kev[2], c->kev[3]);
+      c->phase_ms[6] = ms[0];
+      c->phase_ms[7] = 0;
+      c->phase_ms[8] = ms[2];
+      c->phase_ms[9] = ms[1];
+      return BRUNO_OK;
+    }
+    for (auto &x : slots) x *= 2;   /* an estimate was too low: every sample grows, all count again */
+  }
+  return set_err(c, BRUNO_ERR_TABLE_FULL, "batch: k-mer table full after regrowth");
+}
+
 bruno_status run_count(Ctx *c) { return c->W == 1 ? count_typed<KW1>(c) : count_typed<KW2>(c); }
 bruno_status run_dump_k2(Ctx *c) { return c->W == 1 ? dump_k2_typed<KW1>(c) : dump_k2_typed<KW2>(c); }
 bruno_status run_filter(Ctx *c, const uint64_t *thresh) {
@@ -2477,28 +2823,35 @@ bruno_status run_filter(Ctx *c, const uint64_t *thresh) {
 }
 
 bruno_status run_copy_nodes(Ctx *c, uint64_t *keys, uint16_t *counts, uint8_t *flags, size_t cap, size_t *n) {
+  return run_copy_nodes_range(c, 0, c->nslots, c->n_nodes, keys, counts, flags, cap, n);
+}
+
+bruno_status run_copy_nodes_range(Ctx *c, uint64_t base, uint64_t nslots, uint64_t nnodes, uint64_t *keys,
+                                  uint16_t *counts, uint8_t *flags, size_t cap, size_t *n) {
   bruno_status st;
-  *n = c->n_nodes;
+  *n = nnodes;
   if (!keys && !counts && !flags) return BRUNO_OK;
-  if (cap < c->n_nodes) return set_err(c, BRUNO_ERR_CAPACITY, "node buffers too small");
-  const uint64_t nn = std::max<uint64_t>(1, c->n_nodes);
+  if (cap < nnodes) return set_err(c, BRUNO_ERR_CAPACITY, "node buffers too small");
+  const uint64_t nn = std::max<uint64_t>(1, nnodes);
   Buf dk, dc, df;
   if ((st = ensure(c, dk, nn * 8 * c->W)) != BRUNO_OK) return st;
   if ((st = ensure(c, dc, nn * 18)) != BRUNO_OK) return st;
   if ((st = ensure(c, df, nn)) != BRUNO_OK) return st;
   cudaMemsetAsync(&c->dctr->n_k2_dump, 0, 8, c->stream);
   if (c->W == 1)
-    k_dump_nodes<KW1><<<num_sms() * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, (uint64_t *)dk.p,
-                                                            (uint16_t *)dc.p, (uint8_t *)df.p, nn, &c->dctr->n_k2_dump);
+    k_dump_nodes<KW1><<<num_sms() * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p + base * Slot<KW1>::U64, nslots,
+                                                            (uint64_t *)dk.p, (uint16_t *)dc.p, (uint8_t *)df.p, nn,
+                                                            &c->dctr->n_k2_dump);
   else
-    k_dump_nodes<KW2><<<num_sms() * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, (uint64_t *)dk.p,
-                                                            (uint16_t *)dc.p, (uint8_t *)df.p, nn, &c->dctr->n_k2_dump);
+    k_dump_nodes<KW2><<<num_sms() * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p + base * Slot<KW2>::U64, nslots,
+                                                            (uint64_t *)dk.p, (uint16_t *)dc.p, (uint8_t *)df.p, nn,
+                                                            &c->dctr->n_k2_dump);
   bruno_status r = BRUNO_OK;
-  if (keys) r = cuda_check(c, cudaMemcpyAsync(keys, dk.p, c->n_nodes * 8 * c->W, cudaMemcpyDeviceToHost, c->stream), "copy");
+  if (keys) r = cuda_check(c, cudaMemcpyAsync(keys, dk.p, nnodes * 8 * c->W, cudaMemcpyDeviceToHost, c->stream), "copy");
   if (r == BRUNO_OK && counts)
-    r = cuda_check(c, cudaMemcpyAsync(counts, dc.p, c->n_nodes * 18, cudaMemcpyDeviceToHost, c->stream), "copy");
+    r = cuda_check(c, cudaMemcpyAsync(counts, dc.p, nnodes * 18, cudaMemcpyDeviceToHost, c->stream), "copy");
   if (r == BRUNO_OK && flags)
-    r = cuda_check(c, cudaMemcpyAsync(flags, df.p, c->n_nodes, cudaMemcpyDeviceToHost, c->stream), "copy");
+    r = cuda_check(c, cudaMemcpyAsync(flags, df.p, nnodes, cudaMemcpyDeviceToHost, c->stream), "copy");
   if (r == BRUNO_OK) r = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
   cudaFreeAsync(dk.p, c->stream); cudaFreeAsync(dc.p, c->stream); cudaFreeAsync(df.p, c->stream);
   return r;

@@ -150,7 +150,8 @@ bruno_status bruno_ctx_destroy(bruno_ctx *c) {
                  &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list, &c->e_ends, &c->e_freqs, &c->s_kmers, &c->s_dist, &c->s_flags, &c->k1tab,
                  &c->cl_trec, &c->cl_tslot, &c->cl_sums, &c->cl_norm, &c->cl_htab, &c->cl_q, &c->cl_found,
                  &c->records, &c->bucket_cnt, &c->records2, &c->sub_cnt, &c->bigres,
-                 &c->xsamp, &c->hllreg, &c->hsum};
+                 &c->xsamp, &c->hllreg, &c->hsum, &c->sgeom, &c->s_tally, &c->s_inst, &c->s_used, &c->xitems,
+                 &c->split_items, &c->csample, &c->r_samp, &c->h_samp, &c->grp_tmp};
   for (Buf *b : bufs) release(*b);
   for (Buf &b : c->seg_bufs) release(b);
   if (c->dctr) cudaFree(c->dctr);
@@ -191,6 +192,9 @@ bruno_status bruno_reset(bruno_ctx *c) {
   if (!c) return BRUNO_ERR_ARG;
   c->segs.clear();
   c->stage = 0;
+  c->S = 1;   /* the plain build; bruno_build_samples sets a batch */
+  c->samp_off.clear();
+  c->samp_r0.clear();
   c->n_reads = c->n_reads_used = c->n_instances = c->n_entries = 0;
   c->n_k2 = c->n_filtered = 0;
   c->k2_dumped = false;
@@ -370,6 +374,7 @@ bruno_status bruno_to_compressed_chains(bruno_ctx *c) {
 
 bruno_status bruno_clean_deadend_and_bubbles_naive(bruno_ctx *c, bruno_clean_stats *stats) {
   if (!c) return BRUNO_ERR_ARG;
+  if (c->S > 1) return set_err(c, BRUNO_ERR_ARG, "graph cleaning works on one graph; build it with bruno_build_and_compact");
   if (c->stage < 5) return set_err(c, BRUNO_ERR_ARG, "cleaning needs ranked chains");
   if (c->cleaned) return set_err(c, BRUNO_ERR_ARG, "the graph is cleaned already; call bruno_reset first");
   bruno_clean_stats s{};
@@ -594,6 +599,181 @@ bruno_status bruno_get_isolated(bruno_ctx *c, uint64_t *kmers, uint64_t *in_kmer
   if (!c || !n) return BRUNO_ERR_ARG;
   if (c->stage < 5) return set_err(c, BRUNO_ERR_ARG, "isolated nodes are known after list_rank");
   return run_chain_query(c, BRUNO_CHAIN_ALL, 2, kmers, in_kmers, out_kmers, in_dist, out_dist, cap, n);
+}
+
+/* ------------------------------------------------------------------ batched form */
+bruno_status bruno_build_samples(bruno_ctx *c, const char *const *bufs, const size_t *nbytes, size_t n_samples,
+                                 int32_t is_device) {
+  if (!c || !bufs || !nbytes || n_samples == 0) return BRUNO_ERR_ARG;
+  if (n_samples > MAX_SAMPLES) return set_err(c, BRUNO_ERR_ARG, "batch: at most 16384 samples in one batch");
+  for (size_t q = 0; q < n_samples; ++q)
+    if (!bufs[q] && nbytes[q]) return BRUNO_ERR_ARG;
+  if (c->W != 1 || c->cfg.edge_filter || c->cfg.keep_k2 || c->cfg.keep_filtered || c->force_direct_count)
+    return set_err(c, BRUNO_ERR_ARG, "batch: k <= 31, the (k+2)-mer filter, no raw or filtered count copies, "
+                                     "automatic counting path");
+  if (c->cfg.thresholding && (c->cfg.thresh[0] != 0 || c->cfg.thresh[1] < 65536 || c->cfg.thresh[4] != 0 ||
+                              c->cfg.thresh[5] < 65536))
+    return set_err(c, BRUNO_ERR_ARG, "batch: only the (k+1)-mer bounds may be set (one -L / -U value)");
+  bruno_status st = bruno_reset(c);
+  if (st != BRUNO_OK) return st;
+  /* one device copy of all samples, one after another; a sample whose last byte is not a newline
+   * gets one, so that no record runs into the next sample */
+  std::vector<unsigned char> last(n_samples, '\n');
+  if (is_device) {
+    for (size_t q = 0; q < n_samples; ++q)
+      if (nbytes[q]) cudaMemcpyAsync(&last[q], bufs[q] + nbytes[q] - 1, 1, cudaMemcpyDeviceToHost, c->stream);
+    if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "sample ends")) != BRUNO_OK) return st;
+  } else {
+    for (size_t q = 0; q < n_samples; ++q) if (nbytes[q]) last[q] = (unsigned char)bufs[q][nbytes[q] - 1];
+  }
+  c->samp_off.assign(n_samples + 1, 0);
+  for (size_t q = 0; q < n_samples; ++q)
+    c->samp_off[q + 1] = c->samp_off[q] + nbytes[q] + (nbytes[q] && last[q] != '\n' ? 1 : 0);
+  const uint64_t total = c->samp_off[n_samples];
+  if (c->seg_bufs.empty()) c->seg_bufs.resize(1);
+  if ((st = ensure(c, c->seg_bufs[0], total + 16)) != BRUNO_OK) return st;
+  char *dst = (char *)c->seg_bufs[0].p;
+  static const char nl = '\n';
+  record(c, 7);
+  for (size_t q = 0; q < n_samples && st == BRUNO_OK; ++q) {
+    if (!nbytes[q]) continue;
+    st = cuda_check(c, cudaMemcpyAsync(dst + c->samp_off[q], bufs[q], nbytes[q],
+                                       is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream),
+                    "sample copy");
+    if (st == BRUNO_OK && last[q] != '\n')
+      st = cuda_check(c, cudaMemcpyAsync(dst + c->samp_off[q] + nbytes[q], &nl, 1, cudaMemcpyHostToDevice, c->stream),
+                      "sample end");
+  }
+  if (st != BRUNO_OK) return st;
+  c->segs.push_back({dst, total});
+  c->S = (uint32_t)n_samples;
+  c->stage = 1;
+  record(c, 0);
+  if ((st = run_count_samples(c)) != BRUNO_OK) return st;
+  record(c, 1);
+  cudaEventSynchronize(c->ev[1]);
+  c->phase_ms[10] = elapsed(c, 7, 0);
+  c->phase_ms[1] = elapsed(c, 0, 1);
+  c->stage = 2;
+  if ((st = bruno_local_insert_by_freqencies(c, nullptr)) != BRUNO_OK) return st;
+  if ((st = bruno_extract_chains(c)) != BRUNO_OK) return st;
+  if ((st = bruno_list_rank(c, c->cfg.min_update, nullptr)) != BRUNO_OK) return st;
+  if (!c->fast_ranked)
+    return set_err(c, BRUNO_ERR_INVARIANT, "batch: the chain maps are not mutually consistent");
+  if ((st = bruno_to_compressed_chains(c)) != BRUNO_OK) return st;
+  /* per-sample tallies and ranges */
+  const uint32_t S = c->S;
+  c->h_tally.assign((size_t)S * T_NUM, 0);
+  st = cuda_check(c, cudaMemcpyAsync(c->h_tally.data(), c->s_tally.p, (size_t)S * T_NUM * 8, cudaMemcpyDeviceToHost,
+                                     c->stream), "tallies");
+  std::vector<uint64_t> off(c->n_heads + 1, 0);
+  if (st == BRUNO_OK)
+    st = cuda_check(c, cudaMemcpyAsync(off.data(), c->head_off.p, (c->n_heads + 1) * 8, cudaMemcpyDeviceToHost,
+                                       c->stream), "chain offsets");
+  if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "tallies");
+  if (st != BRUNO_OK) return st;
+  c->h_iter.assign(S, 0);
+  for (uint32_t q = 0; q < S; ++q) {
+    uint64_t *t = &c->h_tally[(size_t)q * T_NUM];
+    const uint64_t nmax = t[T_NMAX];
+    uint64_t it = 0;
+    if (nmax >= 2) { uint64_t x = nmax - 1; while (x >>= 1) ++it; ++it; }   /* floor(log2(nmax-1)) + 1 */
+    else if (t[T_CYCLE] > 0) it = 1;
+    c->h_iter[q] = it;
+    t[T_RANKED] = c->h_rank0[q + 1] - c->h_rank0[q];
+    t[T_HEADS] = c->h_head0[q + 1] - c->h_head0[q];
+    t[T_CHARS] = off[c->h_head0[q + 1]] - off[c->h_head0[q]];
+  }
+  return BRUNO_OK;
+}
+
+static bruno_status batch_sample(bruno_ctx *c, size_t sample) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (c->S <= 1 || c->stage < 6 || c->h_tally.empty()) return set_err(c, BRUNO_ERR_ARG, "no batch built");
+  if (sample >= c->S) return set_err(c, BRUNO_ERR_ARG, "sample index out of range");
+  return BRUNO_OK;
+}
+
+bruno_status bruno_sample_count(bruno_ctx *c, size_t *n_samples) {
+  if (!c || !n_samples) return BRUNO_ERR_ARG;
+  *n_samples = c->stage >= 6 ? c->S : 0;
+  return BRUNO_OK;
+}
+
+bruno_status bruno_sample_sizes(bruno_ctx *c, size_t sample, bruno_sizes *o) {
+  bruno_status st = batch_sample(c, sample);
+  if (st != BRUNO_OK) return st;
+  if (!o) return BRUNO_ERR_ARG;
+  std::memset(o, 0, sizeof(*o));
+  const uint64_t *t = &c->h_tally[sample * T_NUM];
+  const SGeom &g = c->h_sgeom[sample];
+  o->n_reads = c->samp_r0[sample + 1] - c->samp_r0[sample];
+  o->n_reads_used = c->h_used[sample];
+  o->n_instances = c->h_inst[sample];
+  o->n_k2 = t[T_ENTRIES];
+  o->n_nodes = t[T_CHAIN] + t[T_BRANCH];
+  o->n_branch = t[T_BRANCH];
+  o->n_chain_nodes = t[T_CHAIN];
+  o->iterations = c->h_iter[sample];
+  o->n_cycle_nodes = t[T_CYCLE];
+  o->n_isolated = t[T_ISOLATED];
+  o->n_ranked = t[T_RANKED];
+  o->n_chains = t[T_HEADS];
+  o->n_chain_chars = t[T_CHARS];
+  o->table_slots = g.g.nslots;
+  o->table_partitions = 1ull << g.g.pbits;
+  o->launches = c->launches;
+  return BRUNO_OK;
+}
+
+bruno_status bruno_sample_copy_ranked(bruno_ctx *c, size_t sample, uint64_t *K, uint64_t *rep, int32_t *dist,
+                                      size_t cap, size_t *n) {
+  bruno_status st = batch_sample(c, sample);
+  if (st != BRUNO_OK) return st;
+  const uint64_t a = c->h_rank0[sample], cnt = c->h_rank0[sample + 1] - a;
+  if (n) *n = cnt;
+  if (!K && !rep && !dist) return BRUNO_OK;
+  if (cap < cnt) return set_err(c, BRUNO_ERR_CAPACITY, "copy buffer too small");
+  const size_t w = 8 * c->W;
+  if (K) st = copy_d2h(c, K, (const char *)c->r_K.p + a * w, cnt * w);
+  if (st == BRUNO_OK && rep) st = copy_d2h(c, rep, (const char *)c->r_rep.p + a * w, cnt * w);
+  if (st == BRUNO_OK && dist) st = copy_d2h(c, dist, (const char *)c->r_dist.p + a * 4, cnt * 4);
+  if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  return st;
+}
+
+bruno_status bruno_sample_copy_chains(bruno_ctx *c, size_t sample, uint64_t *reps, uint64_t *offsets, char *chars,
+                                      size_t cap_chains, size_t cap_chars, size_t *n_chains, size_t *n_chars) {
+  bruno_status st = batch_sample(c, sample);
+  if (st != BRUNO_OK) return st;
+  const uint64_t h0 = c->h_head0[sample], h1 = c->h_head0[sample + 1], nc = h1 - h0;
+  const uint64_t nch = c->h_tally[sample * T_NUM + T_CHARS];
+  if (n_chains) *n_chains = nc;
+  if (n_chars) *n_chars = nch;
+  if (!reps && !offsets && !chars) return BRUNO_OK;
+  if ((reps || offsets) && cap_chains < nc) return set_err(c, BRUNO_ERR_CAPACITY, "chain buffer too small");
+  if (chars && cap_chars < nch) return set_err(c, BRUNO_ERR_CAPACITY, "char buffer too small");
+  uint64_t off0 = 0;
+  st = cuda_check(c, cudaMemcpyAsync(&off0, (const uint64_t *)c->head_off.p + h0, 8, cudaMemcpyDeviceToHost, c->stream),
+                  "offset");
+  if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "offset");
+  const size_t w = 8 * c->W;
+  if (st == BRUNO_OK && reps) st = copy_d2h(c, reps, (const char *)c->ch_rep.p + h0 * w, nc * w);
+  if (st == BRUNO_OK && offsets) st = copy_d2h(c, offsets, (const uint64_t *)c->head_off.p + h0, (nc + 1) * 8);
+  if (st == BRUNO_OK && chars) st = copy_d2h(c, chars, (const char *)c->ch_chars.p + off0, nch);
+  if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  if (st == BRUNO_OK && offsets)
+    for (uint64_t i = 0; i <= nc; ++i) offsets[i] -= off0;   /* offsets into this sample's chars */
+  return st;
+}
+
+bruno_status bruno_sample_copy_nodes(bruno_ctx *c, size_t sample, uint64_t *keys, uint16_t *counts, uint8_t *flags,
+                                     size_t cap, size_t *n) {
+  bruno_status st = batch_sample(c, sample);
+  if (st != BRUNO_OK) return st;
+  const uint64_t *t = &c->h_tally[sample * T_NUM];
+  return run_copy_nodes_range(c, c->h_sgeom[sample].g.base, c->h_sgeom[sample].g.nslots, t[T_CHAIN] + t[T_BRANCH],
+                              keys, counts, flags, cap, n);
 }
 
 bruno_status bruno_host_alloc(size_t bytes, void **out) {

@@ -161,10 +161,11 @@ __device__ __forceinline__ void table_find2(const uint64_t *table, const TableGe
 /* chain index i (listed by the filter, which also stored i in the slot) -> its k-mer, its
  * chain-map record and its edge byte; one read of its own slot gives key and counters */
 template <class KT>
-__global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, uint64_t nslots, TableGeom g, int k,
+__global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, uint64_t nslots, TableGeom g0,
+                                                     const SGeom *sg, uint32_t nsamples, int k,
                                                      const uint32_t *chain_list, uint64_t M, uint64_t *ckey,
-                                                     ChainState *cs, uint8_t *cedge, uint32_t max_probe,
-                                                     DevCounters *ctr) {
+                                                     ChainState *cs, uint8_t *cedge, uint32_t *csample,
+                                                     uint32_t max_probe, DevCounters *ctr) {
   constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t sl = chain_list[i];
@@ -174,6 +175,12 @@ __global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, uint6
     }
     uint64_t own[SU];
     ld_slot<SU>(table + sl * SU, own);
+    TableGeom g = g0;
+    if (nsamples > 1) {   /* a batch: the node's sample (in its flags) has its own partitions */
+      const uint32_t smp = (uint32_t)(own[KWD + 2] >> (16 + NF_SAMPLE_SHIFT)) & (MAX_SAMPLES - 1);
+      g = sg[smp < nsamples ? smp : 0].g;
+      csample[i] = smp;
+    }
     const KT K = key_kmer(node_key(KOps<KT>::load(own)));
     KOps<KT>::store(ckey + i * KWD, K);
     const uint64_t *pw = own + KWD;
@@ -218,13 +225,19 @@ __global__ void __launch_bounds__(TPB) k_chain_init(const uint64_t *table, uint6
 
 /* neighbours of branch nodes get their facing side set to branch_neighbor (0) */
 template <class KT>
-__global__ void __launch_bounds__(TPB) k_termini(const uint64_t *table, TableGeom g, int k, ChainState *cs, uint64_t M,
+__global__ void __launch_bounds__(TPB) k_termini(const uint64_t *table, TableGeom g0, const SGeom *sg,
+                                                  uint32_t nsamples, int k, ChainState *cs, uint64_t M,
                                                   uint32_t max_probe, const uint32_t *branch_list, uint64_t nb) {
   constexpr int SU = Slot<KT>::U64, KWD = Slot<KT>::KEYW;
   for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nb; q += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t *s = table + (uint64_t)branch_list[q] * SU;
     const KT K = key_kmer(node_key(KOps<KT>::load(s)));
     const uint64_t *pw = s + KWD;
+    TableGeom g = g0;
+    if (nsamples > 1) {
+      const uint32_t smp = (uint32_t)(pw[2] >> (16 + NF_SAMPLE_SHIFT)) & (MAX_SAMPLES - 1);
+      g = sg[smp < nsamples ? smp : 0].g;
+    }
     for (int c = 0; c < 4; ++c) {
       if ((pw[0] >> (16 * c)) & 0xFFFFu) {  /* out neighbour receives (branch, IN) */
         KT n = KOps<KT>::append(K, (unsigned)c, k), y = KOps<KT>::rc(n, k);
@@ -569,30 +582,48 @@ __global__ void __launch_bounds__(TPB) k_fast_place(const ChainState *cs, ChainS
  * counts, and the longest path in nodes.  cs2 starts as all ones, which no final state is. */
 constexpr uint32_t CS2_UNSET = 0xFFFFFFFFu;
 __global__ void __launch_bounds__(TPB) k_fast_mark(const ChainState *cs, const ChainState *cs2, uint64_t M,
-                                                    uint8_t *removed, unsigned long long *nmax, DevCounters *ctr) {
+                                                    uint8_t *removed, unsigned long long *nmax,
+                                                    const uint32_t *csample, unsigned long long *s_tally,
+                                                    DevCounters *ctr) {
   unsigned long long ncy = 0, niso = 0, mx = 0, bad = 0;
-  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < M; v += (uint64_t)gridDim.x * blockDim.x) {
-    const ChainState st = cs2[v];
-    const bool cyc = st.inD == CS2_UNSET;
-    uint8_t r = 0;
-    if (cyc) {
-      r = 1; ++ncy;
-      /* no walk reached this node: check its pointers here (consistent only on a cycle) */
-      const ChainState o = cs[v];
-      for (int s = 0; s < 2; ++s) {
-        const uint32_t D = side_dist(o, s);
-        const uint64_t P = side_ptr(o, s);
-        if (side_terminal(D)) continue;
-        if (D != 1 || (P & (PF_EXT | PF_BLANK))) { ++bad; continue; }
-        const uint32_t f = (P & PF_FLIP) ? 1u : 0u;
-        if (!answers(cs[(uint32_t)P], f ? s : 1 - s, (uint32_t)v, f)) ++bad;
+  const int lane = threadIdx.x & 31;
+  for (uint64_t v0 = (uint64_t)blockIdx.x * blockDim.x; v0 < M; v0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t v = v0 + threadIdx.x;
+    uint32_t cyc_v = 0, iso_v = 0, mx_v = 0;
+    if (v < M) {
+      const ChainState st = cs2[v];
+      const bool cyc = st.inD == CS2_UNSET;
+      uint8_t r = 0;
+      if (cyc) {
+        r = 1; cyc_v = 1;
+        /* no walk reached this node: check its pointers here (consistent only on a cycle) */
+        const ChainState o = cs[v];
+        for (int s = 0; s < 2; ++s) {
+          const uint32_t D = side_dist(o, s);
+          const uint64_t P = side_ptr(o, s);
+          if (side_terminal(D)) continue;
+          if (D != 1 || (P & (PF_EXT | PF_BLANK))) { ++bad; continue; }
+          const uint32_t f = (P & PF_FLIP) ? 1u : 0u;
+          if (!answers(cs[(uint32_t)P], f ? s : 1 - s, (uint32_t)v, f)) ++bad;
+        }
+      } else {
+        mx_v = 1u + (st.inD & DM) + (st.outD & DM);
+        if (st.inD == TM && st.outD == TM) { r = 2; iso_v = 1; }
+      }
+      removed[v] = r;
+      ncy += cyc_v; niso += iso_v; mx = max(mx, (unsigned long long)mx_v);
+    }
+    if (s_tally) {   /* a batch: the same tallies per sample, summed over the lanes of one sample */
+      const uint32_t smp = v < M ? csample[v] : ~0u;
+      const unsigned peers = __match_any_sync(~0u, smp);
+      const uint32_t sc = __reduce_add_sync(peers, cyc_v), si = __reduce_add_sync(peers, iso_v);
+      const uint32_t sm = __reduce_max_sync(peers, mx_v);
+      if (v < M && lane == __ffs(peers) - 1) {
+        if (sc) atomicAdd(&s_tally[(uint64_t)smp * T_NUM + T_CYCLE], (unsigned long long)sc);
+        if (si) atomicAdd(&s_tally[(uint64_t)smp * T_NUM + T_ISOLATED], (unsigned long long)si);
+        if (sm) atomicMax(&s_tally[(uint64_t)smp * T_NUM + T_NMAX], (unsigned long long)sm);
       }
     }
-    else {
-      mx = max(mx, 1ull + (st.inD & DM) + (st.outD & DM));
-      if (st.inD == TM && st.outD == TM) { r = 2; ++niso; }
-    }
-    removed[v] = r;
   }
   ncy = warp_sum(ncy); niso = warp_sum(niso); bad = warp_sum(bad);
   for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_down_sync(~0u, mx, o));
@@ -661,6 +692,8 @@ struct EmitArgs {
   uint32_t *heads;     /* per chain ordinal: head node */
   uint64_t *head_len;  /* per chain ordinal: k - 1 + nodes */
   uint64_t *ch_rep;
+  const uint32_t *csample;   /* a batch: per chain node its sample; then per listranked node and */
+  uint32_t *r_samp, *h_samp; /* per chain (head) their sample */
   DevCounters *ctr;
 };
 
@@ -693,6 +726,7 @@ __global__ void __launch_bounds__(TPB) k_ranked(EmitArgs a) {
       KOps<KT>::store(a.rK + o * KWD, K);
       KOps<KT>::store(a.rrep + o * KWD, rep);
       a.rdist[o] = dist;
+      if (a.csample) a.r_samp[o] = a.csample[i];
     }
     const unsigned long long h = warp_append(head, &a.ctr->n_heads);
     if (i < a.M) a.head_of[i] = head ? (uint32_t)h : NONE32;
@@ -701,6 +735,7 @@ __global__ void __launch_bounds__(TPB) k_ranked(EmitArgs a) {
       a.heads[h] = (uint32_t)i;
       a.head_len[h] = (uint64_t)(a.k - 1) + (st.inD & DM) + (st.outD & DM) + 1;
       KOps<KT>::store(a.ch_rep + h * KWD, rep);
+      if (a.csample) a.h_samp[h] = a.csample[i];
     }
   }
 }
@@ -1068,13 +1103,16 @@ bruno_status extract_typed(Ctx *c) {
   if ((st = ensure(c, c->cstate, Mb * sizeof(ChainState))) != BRUNO_OK) return st;
   const int sms = sms_count();
   cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
-  k_chain_init<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, c->geom, c->cfg.k,
+  if (c->S > 1 && (st = ensure(c, c->csample, Mb * 4)) != BRUNO_OK) return st;
+  k_chain_init<KT><<<sms * 8, TPB, 0, c->stream>>>((const uint64_t *)c->table.p, c->nslots, c->geom,
+                                                   (const SGeom *)c->sgeom.p, c->S, c->cfg.k,
                                                    (const uint32_t *)c->chain_list.p, M, (uint64_t *)c->ckey.p,
-                                                   (ChainState *)c->cstate.p, (uint8_t *)c->cedge.p, 4096u, c->dctr);
+                                                   (ChainState *)c->cstate.p, (uint8_t *)c->cedge.p,
+                                                   (uint32_t *)c->csample.p, 4096u, c->dctr);
   if (c->n_branch)
     k_termini<KT><<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>(sms * 8, (c->n_branch + TPB - 1) / TPB)), TPB, 0,
-                    c->stream>>>((const uint64_t *)c->table.p, c->geom, c->cfg.k, (ChainState *)c->cstate.p, M, 4096u,
-                                 (const uint32_t *)c->branch_list.p, c->n_branch);
+                    c->stream>>>((const uint64_t *)c->table.p, c->geom, (const SGeom *)c->sgeom.p, c->S, c->cfg.k,
+                                 (ChainState *)c->cstate.p, M, 4096u, (const uint32_t *)c->branch_list.p, c->n_branch);
   c->launches += 2;
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   if (c->hctr->err & DERR_INVARIANT) return set_err(c, BRUNO_ERR_INVARIANT, "chain list incomplete");
@@ -1151,6 +1189,111 @@ bruno_status general_emission(Ctx *c, EmitArgs a) {
   return BRUNO_OK;
 }
 
+/* ================================================================ batch grouping
+ * A batch's listranked nodes and chains are grouped by sample (a counting sort on the sample
+ * of each), so that each sample's results are one contiguous range; the order inside a sample
+ * is arbitrary, as the table order is in the plain build. */
+__global__ void __launch_bounds__(TPB) k_samp_hist(const uint32_t *samp, uint64_t n, unsigned long long *hist) {
+  const int lane = threadIdx.x & 31;
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    const uint32_t s = i < n ? samp[i] : ~0u;
+    const unsigned peers = __match_any_sync(~0u, s);
+    if (i < n && lane == __ffs(peers) - 1) atomicAdd(&hist[s], (unsigned long long)__popc(peers));
+  }
+}
+
+/* listranked nodes to their sample's range (cursor: the range starts, advanced as they fill) */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_group_ranked(const uint32_t *samp, uint64_t n, unsigned long long *cursor,
+                                                       const uint64_t *K, const uint64_t *rep, const int32_t *dist,
+                                                       uint64_t *K2, uint64_t *rep2, int32_t *dist2) {
+  constexpr int KWD = KOps<KT>::WORDS;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const unsigned long long o = atomicAdd(&cursor[samp[i]], 1ull);
+    KOps<KT>::store(K2 + o * KWD, KOps<KT>::load(K + i * KWD));
+    KOps<KT>::store(rep2 + o * KWD, KOps<KT>::load(rep + i * KWD));
+    dist2[o] = dist[i];
+  }
+}
+
+/* chains (heads) to their sample's range; head_of follows its head to the new ordinal */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_group_heads(const uint32_t *samp, uint64_t nh, unsigned long long *cursor,
+                                                      const uint32_t *heads, const uint64_t *len, const uint64_t *rep,
+                                                      uint32_t *heads2, uint64_t *len2, uint64_t *rep2,
+                                                      uint32_t *head_of) {
+  constexpr int KWD = KOps<KT>::WORDS;
+  for (uint64_t h = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (uint64_t)gridDim.x * blockDim.x) {
+    const unsigned long long o = atomicAdd(&cursor[samp[h]], 1ull);
+    heads2[o] = heads[h];
+    len2[o] = len[h];
+    KOps<KT>::store(rep2 + o * KWD, KOps<KT>::load(rep + h * KWD));
+    head_of[heads[h]] = (uint32_t)o;
+  }
+}
+
+/* the counting sort's ranges: per sample the count, and the exclusive scan as start (host) */
+bruno_status sample_ranges(Ctx *c, const uint32_t *samp, uint64_t n, std::vector<uint64_t> &start,
+                           unsigned long long **cursor) {
+  bruno_status st;
+  const uint32_t S = c->S;
+  if ((st = ensure(c, c->grp_tmp, (size_t)S * 8)) != BRUNO_OK) return st;
+  cudaMemsetAsync(c->grp_tmp.p, 0, (size_t)S * 8, c->stream);
+  if (n)
+    k_samp_hist<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms_count() * 8, (n + TPB - 1) / TPB)), TPB,
+                  0, c->stream>>>(samp, n, (unsigned long long *)c->grp_tmp.p);
+  std::vector<unsigned long long> hist(S);
+  st = cuda_check(c, cudaMemcpyAsync(hist.data(), c->grp_tmp.p, (size_t)S * 8, cudaMemcpyDeviceToHost, c->stream), "hist");
+  if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "hist");
+  if (st != BRUNO_OK) return st;
+  start.assign(S + 1, 0);
+  for (uint32_t q = 0; q < S; ++q) start[q + 1] = start[q] + hist[q];
+  st = cuda_check(c, cudaMemcpyAsync(c->grp_tmp.p, start.data(), (size_t)S * 8, cudaMemcpyHostToDevice, c->stream),
+                  "cursors");
+  *cursor = (unsigned long long *)c->grp_tmp.p;
+  c->launches += 1;
+  return st;
+}
+
+/* both groupings, between k_ranked and the chain offsets */
+template <class KT>
+bruno_status group_by_sample(Ctx *c) {
+  bruno_status st;
+  const uint64_t n = c->n_ranked, nh = c->n_heads, nb = std::max<uint64_t>(1, n), hb = std::max<uint64_t>(1, nh);
+  const int KWD = KOps<KT>::WORDS;
+  const unsigned g = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms_count() * 8, (n + TPB - 1) / TPB));
+  unsigned long long *cursor = nullptr;
+  /* listranked nodes */
+  if ((st = sample_ranges(c, (const uint32_t *)c->r_samp.p, n, c->h_rank0, &cursor)) != BRUNO_OK) return st;
+  Buf K2, R2, D2;
+  if ((st = ensure(c, K2, nb * 8 * KWD)) != BRUNO_OK) return st;
+  if ((st = ensure(c, R2, nb * 8 * KWD)) != BRUNO_OK) return st;
+  if ((st = ensure(c, D2, nb * 4)) != BRUNO_OK) return st;
+  if (n)
+    k_group_ranked<KT><<<g, TPB, 0, c->stream>>>((const uint32_t *)c->r_samp.p, n, cursor, (const uint64_t *)c->r_K.p,
+                                                 (const uint64_t *)c->r_rep.p, (const int32_t *)c->r_dist.p,
+                                                 (uint64_t *)K2.p, (uint64_t *)R2.p, (int32_t *)D2.p);
+  std::swap(c->r_K, K2); std::swap(c->r_rep, R2); std::swap(c->r_dist, D2);
+  cudaFreeAsync(K2.p, c->stream); cudaFreeAsync(R2.p, c->stream); cudaFreeAsync(D2.p, c->stream);
+  /* chains */
+  if ((st = sample_ranges(c, (const uint32_t *)c->h_samp.p, nh, c->h_head0, &cursor)) != BRUNO_OK) return st;
+  Buf H2, L2, P2;
+  if ((st = ensure(c, H2, hb * 4)) != BRUNO_OK) return st;
+  if ((st = ensure(c, L2, (hb + 1) * 8)) != BRUNO_OK) return st;
+  if ((st = ensure(c, P2, hb * 8 * KWD)) != BRUNO_OK) return st;
+  const unsigned gh = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms_count() * 8, (nh + TPB - 1) / TPB));
+  if (nh)
+    k_group_heads<KT><<<gh, TPB, 0, c->stream>>>((const uint32_t *)c->h_samp.p, nh, cursor, (const uint32_t *)c->heads.p,
+                                                 (const uint64_t *)c->head_len.p, (const uint64_t *)c->ch_rep.p,
+                                                 (uint32_t *)H2.p, (uint64_t *)L2.p, (uint64_t *)P2.p,
+                                                 (uint32_t *)c->head_of.p);
+  std::swap(c->heads, H2); std::swap(c->head_len, L2); std::swap(c->ch_rep, P2);
+  cudaFreeAsync(H2.p, c->stream); cudaFreeAsync(L2.p, c->stream); cudaFreeAsync(P2.p, c->stream);
+  c->launches += 2;
+  return BRUNO_OK;
+}
+
 template <class KT>
 bruno_status compress_typed(Ctx *c) {
   bruno_status st;
@@ -1176,12 +1319,24 @@ bruno_status compress_typed(Ctx *c) {
   a.rep_idx = (uint32_t *)c->rep_idx.p; a.dist_of = (int32_t *)c->pay.p; a.head_of = (uint32_t *)c->head_of.p;
   a.heads = (uint32_t *)c->heads.p; a.head_len = (uint64_t *)c->head_len.p; a.ch_rep = (uint64_t *)c->ch_rep.p;
   a.ctr = c->dctr;
+  if (c->S > 1) {   /* a batch: the sample of every listranked node and chain */
+    if ((st = ensure(c, c->r_samp, Mb * 4)) != BRUNO_OK) return st;
+    if ((st = ensure(c, c->h_samp, Mb * 4)) != BRUNO_OK) return st;
+    a.csample = (const uint32_t *)c->csample.p;
+    a.r_samp = (uint32_t *)c->r_samp.p;
+    a.h_samp = (uint32_t *)c->h_samp.p;
+  }
   const int sms = sms_count();
   k_ranked<KT><<<sms * 8, TPB, 0, c->stream>>>(a);
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   c->n_ranked = c->hctr->n_ranked;
   c->n_heads = c->hctr->n_heads;
   const uint64_t nh = c->n_heads;
+  if (c->S > 1) {
+    if ((st = group_by_sample<KT>(c)) != BRUNO_OK) return st;
+    a.rK = (uint64_t *)c->r_K.p; a.rrep = (uint64_t *)c->r_rep.p; a.rdist = (int32_t *)c->r_dist.p;
+    a.heads = (uint32_t *)c->heads.p; a.head_len = (uint64_t *)c->head_len.p; a.ch_rep = (uint64_t *)c->ch_rep.p;
+  }
   /* offsets: exclusive scan of per-chain lengths, total into n_chain_chars */
   cudaMemsetAsync((uint64_t *)c->head_len.p + nh, 0, 8, c->stream);
   scan_u64((const uint64_t *)c->head_len.p, (uint64_t *)c->head_off.p, nh + 1, &c->dctr->n_chain_chars, c->stream);
@@ -2307,7 +2462,9 @@ static bruno_status fast_list_rank(Ctx *c, bool &used) {
                   c->stream>>>(cs, cs2, rnode, R, src);
   cudaMemsetAsync(&c->dctr->n_cycle, 0, 16, c->stream);
   cudaMemsetAsync(&c->dctr->n_heads, 0, 8, c->stream);        /* longest path, in nodes */
-  k_fast_mark<<<sms * 8, TPB, 0, c->stream>>>(cs, cs2, M, (uint8_t *)c->removed.p, &c->dctr->n_heads, c->dctr);
+  k_fast_mark<<<sms * 8, TPB, 0, c->stream>>>(cs, cs2, M, (uint8_t *)c->removed.p, &c->dctr->n_heads,
+                                               c->S > 1 ? (const uint32_t *)c->csample.p : nullptr,
+                                               c->S > 1 ? (unsigned long long *)c->s_tally.p : nullptr, c->dctr);
   c->launches += 3;
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   if (c->hctr->lr_multi != 0) return BRUNO_OK;   /* an unreached node is not on a consistent cycle */
@@ -2326,9 +2483,11 @@ static bruno_status fast_list_rank(Ctx *c, bool &used) {
 
 bruno_status run_list_rank(Ctx *c, int min_update) {
   bruno_status st;
+  c->fast_ranked = false;
   if (!c->exact_ranking) {
     bool used = false;
     if ((st = fast_list_rank(c, used)) != BRUNO_OK) return st;
+    c->fast_ranked = used;
     if (used) return BRUNO_OK;
   }
   const uint64_t M = c->n_chain, Mb = std::max<uint64_t>(1, M);

@@ -54,6 +54,33 @@ struct BigRes { uint64_t k0, k1; uint32_t code, pad; unsigned long long count; }
 
 struct Segment { const char *ptr; uint64_t n; int ev = -1; };   /* ev: copy-done event, -1 if none */
 
+/* One sample's share of the k-mer table when the table is cut into shared-memory partitions;
+ * a batch of samples (the batched form) gives every sample partitions of its own, and the
+ * plain build is a batch of one.  Partition j of sample s is global partition pbase + j: its
+ * slots are g.base + j * g.region onwards, its split records rec2_base + j * cap2 onwards. */
+struct SGeom {
+  TableGeom g;
+  uint64_t pbase, rec2_base, cap2;
+};
+/* per-sample tallies of a batch (u64 each, T_NUM per sample) */
+enum {
+  T_ENTRIES = 0, T_CHAIN, T_BRANCH, T_CYCLE, T_ISOLATED, T_NMAX, T_RANKED, T_HEADS, T_CHARS, T_NUM
+};
+/* the largest s with sg[s].pbase <= P (partition -> sample), and likewise for a table slot */
+__device__ __forceinline__ uint32_t sample_of_part(const SGeom *sg, uint32_t S, uint64_t P) {
+  uint32_t lo = 0, hi = S;
+  while (hi - lo > 1) { const uint32_t m = (lo + hi) >> 1; if (sg[m].pbase <= P) lo = m; else hi = m; }
+  return lo;
+}
+__device__ __forceinline__ uint32_t sample_of_slot(const SGeom *sg, uint32_t S, uint64_t slot) {
+  uint32_t lo = 0, hi = S;
+  while (hi - lo > 1) { const uint32_t m = (lo + hi) >> 1; if (sg[m].g.base <= slot) lo = m; else hi = m; }
+  return lo;
+}
+/* node flags bits 2..15 hold the node's sample in a batch */
+constexpr int NF_SAMPLE_SHIFT = 2;
+constexpr uint32_t MAX_SAMPLES = 1u << 14;
+
 /* chain state of one chain node, 32 B: pointers encode a chain index (bits 0..31) plus
  * PF_FLIP (the target k-mer, on this node's strand, is the reverse complement of the
  * target's canonical key), PF_EXT (the target is the non-chain in- (PF_EXTOUT clear) or
@@ -106,6 +133,16 @@ struct Ctx {
   uint64_t nslots = 0, n_entries = 0, n_slots_claimed = 0;
   Buf records, bucket_cnt;       /* partitioned counting: 8-byte records per hash bucket */
   Buf xsamp, hllreg, hsum;       /* the extraction's bucket layout, HyperLogLog registers, their sums */
+  /* batched form: S samples, one after another in the FASTQ; per sample its byte offset in the
+   * device copy (S + 1 values), first read (S + 1), table geometry and tallies */
+  uint32_t S = 1;
+  std::vector<uint64_t> samp_off, samp_r0;
+  std::vector<SGeom> h_sgeom;
+  Buf sgeom, s_tally, s_inst, s_used, xitems, split_items, csample, r_samp, h_samp, grp_tmp;
+  std::vector<uint64_t> h_tally;           /* T_NUM per sample, after the build */
+  std::vector<uint64_t> h_inst, h_used;    /* instances and reads used per sample */
+  std::vector<uint64_t> h_rank0, h_head0;  /* first listranked node / chain of each sample (S + 1) */
+  std::vector<uint64_t> h_iter;            /* ranking rounds per sample */
   Buf records2, sub_cnt;         /* the same records split per table partition */
   bool h2d_pending = false;      /* ev[7] marks the start of this build's host-to-device copies */
   int force_direct_count = 0;    /* cfg.direct_count: 0 automatic, 1 whole table, 2 L2 partitions */
@@ -131,6 +168,7 @@ struct Ctx {
   Buf ckey, cedge, cstate, cstate2, pend, pay, unf0, unf1, removed;
   uint64_t iterations = 0, n_cycle = 0, n_isolated = 0, multi = 0;
   bool exact_ranking = false;    /* force the round-synchronous ranking (tests) */
+  bool fast_ranked = false;      /* the last ranking took the O(M) path (a batch needs it) */
 
   /* emission */
   Buf r_K, r_rep, r_dist, rep_idx, head_of, heads, head_len, head_off, ch_rep, ch_off, ch_chars;
@@ -169,6 +207,7 @@ void scan_u64(const uint64_t *in, uint64_t *out, uint64_t n, unsigned long long 
 /* -------------------------------------------------------------- phase launchers */
 bruno_status run_index_reads(Ctx *c);        /* FASTQ line structure -> read spans */
 bruno_status run_count(Ctx *c);              /* distinct-count estimate, table, counting */
+bruno_status run_count_samples(Ctx *c);      /* the same for a batch of c->S samples (read index included) */
 bruno_status run_dump_k2(Ctx *c);            /* optional raw (k+2)-mer copy */
 bruno_status run_filter(Ctx *c, const uint64_t *thresh);
 bruno_status run_extract_chains(Ctx *c);
@@ -181,6 +220,9 @@ bruno_status run_chain_summaries(Ctx *c);
 bruno_status run_clean(Ctx *c, uint64_t *rounds, uint64_t *deadends, uint64_t *bubbles, uint64_t *edges,
                        int32_t *status);
 bruno_status run_copy_nodes(Ctx *c, uint64_t *keys, uint16_t *counts, uint8_t *flags, size_t cap, size_t *n);
+/* the nodes of table slots [base, base + nslots), of which there are nn */
+bruno_status run_copy_nodes_range(Ctx *c, uint64_t base, uint64_t nslots, uint64_t nn, uint64_t *keys, uint16_t *counts,
+                                  uint8_t *flags, size_t cap, size_t *n);
 /* debruijn_graph::find_if / erase_if over the node table (filter: a bruno_node_filter); after an
  * erasure the node counts and stored classifications are brought up to date */
 bruno_status run_node_query(Ctx *c, int filter, bool erase, uint64_t *keys, uint16_t *counts, uint8_t *flags,

@@ -21,6 +21,10 @@
  * request at the head of the queue fits nowhere, idle workers free their buffers; a request
  * that still runs out of device memory is queued again, once, to run with no other build busy,
  * and no other request starts until it has finished.
+ *
+ * The batched mode (bruno_pool_create_batched) replaces the workers by one scheduler that runs
+ * continuous batching over the fused form: every pass takes the queued requests that fit the
+ * budget and builds them together in one pass of every kernel (bruno_build_samples).
  */
 #include <cuda_runtime.h>
 
@@ -61,6 +65,8 @@ struct Done {
 struct bruno_pool {
   bruno_cfg cfg{};
   uint64_t budget = 0;
+  bool batched = false;          /* continuous batching: one scheduler thread, fused passes */
+  uint32_t max_samples = 0;      /* requests in one fused pass at most */
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Request> queue;
@@ -171,7 +177,102 @@ void worker_main(bruno_pool *p, int w) {
   if (ctx) bruno_ctx_destroy(ctx);
 }
 
+/* copies one sample's results of a fused pass into a result record */
+void take_sample(bruno_ctx *ctx, size_t i, int words, bruno_pool_result &r) {
+  r.words = words;
+  r.status = bruno_sample_sizes(ctx, i, &r.sizes);
+  if (r.status != BRUNO_OK) return;
+  size_t nc = 0, nch = 0;
+  r.status = bruno_sample_copy_chains(ctx, i, nullptr, nullptr, nullptr, 0, 0, &nc, &nch);
+  if (r.status != BRUNO_OK) return;
+  r.reps = (uint64_t *)std::malloc(std::max<size_t>(1, nc) * 8 * words);
+  r.offsets = (uint64_t *)std::malloc((nc + 1) * 8);
+  r.chars = (char *)std::malloc(std::max<size_t>(1, nch));
+  if (!r.reps || !r.offsets || !r.chars) { r.status = BRUNO_ERR_OOM; return; }
+  r.status = bruno_sample_copy_chains(ctx, i, r.reps, r.offsets, r.chars, nc, nch, &nc, &nch);
+  r.n_chains = nc;
+  r.n_chars = nch;
+}
+
+/* Continuous batching: the scheduler takes every queued request that fits the memory budget
+ * (at least one, at most max_samples), builds them in one fused pass (bruno_build_samples), and
+ * hands out each request's results; requests that arrive during a pass wait for the next one.
+ * Where the fused pass cannot run (a configuration the batched form refuses, or an error), each
+ * request of the pass is built on its own with the plain path, so every result is always the
+ * plain path's. */
+void batch_main(bruno_pool *p) {
+  bruno_ctx *ctx = nullptr;
+  const int words = p->cfg.k <= 31 ? 1 : 2;
+  for (;;) {
+    std::vector<Request> take;
+    {
+      std::unique_lock<std::mutex> lk(p->mu);
+      p->cv_work.wait(lk, [&] { return p->stop || !p->queue.empty(); });
+      if (p->stop && p->queue.empty()) break;
+      uint64_t sum = 0;
+      while (!p->queue.empty() && take.size() < p->max_samples) {
+        const Request &q = p->queue.front();
+        if (!take.empty() && sum + q.est > p->budget) break;
+        sum += q.est;
+        take.push_back(q);
+        p->queue.pop_front();
+      }
+      p->busy[0] = true;
+      p->held[0] = std::max(p->held[0], sum);
+    }
+    const clk::time_point t0 = clk::now();
+    std::vector<Done> out(take.size());
+    for (auto &d : out) std::memset(&d.r, 0, sizeof(d.r));
+    bruno_status st = ctx ? BRUNO_OK : bruno_ctx_create(&p->cfg, &ctx);
+    if (st == BRUNO_OK) {
+      std::vector<const char *> bufs(take.size());
+      std::vector<size_t> ns(take.size());
+      for (size_t i = 0; i < take.size(); ++i) { bufs[i] = take[i].buf; ns[i] = take[i].n; }
+      st = take.size() > 1 ? bruno_build_samples(ctx, bufs.data(), ns.data(), take.size(), 0) : BRUNO_ERR_ARG;
+      if (st == BRUNO_OK) {
+        for (size_t i = 0; i < take.size(); ++i) take_sample(ctx, i, words, out[i].r);
+      } else {   /* one request, or a pass the batched form cannot take: the plain path, one by one */
+        for (size_t i = 0; i < take.size(); ++i) run_one(ctx, words, take[i], out[i].r);
+      }
+    } else {
+      for (auto &d : out) d.r.status = st;
+    }
+    const clk::time_point t1 = clk::now();
+    {
+      std::lock_guard<std::mutex> lk(p->mu);
+      for (size_t i = 0; i < take.size(); ++i) {
+        out[i].r.queue_ms = std::chrono::duration<double, std::milli>(t0 - take[i].submitted).count();
+        out[i].r.run_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        out[i].r.worker = 0;
+        p->done[take[i].ticket] = out[i];
+      }
+      p->busy[0] = false;
+    }
+    p->cv_done.notify_all();
+  }
+  if (ctx) bruno_ctx_destroy(ctx);
+}
+
 }  // namespace
+
+extern "C" bruno_status bruno_pool_create_batched(const bruno_cfg *cfg, uint32_t max_samples, uint64_t mem_budget,
+                                                  bruno_pool **out) {
+  if (!cfg || !out || max_samples < 1 || max_samples > 16384) return BRUNO_ERR_ARG;
+  *out = nullptr;
+  if (cudaSetDevice(cfg->device) != cudaSuccess) { cudaGetLastError(); return BRUNO_ERR_CUDA; }
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { cudaGetLastError(); return BRUNO_ERR_CUDA; }
+  bruno_pool *p = new bruno_pool();
+  p->cfg = *cfg;
+  p->batched = true;
+  p->max_samples = max_samples;
+  p->budget = mem_budget ? mem_budget : (uint64_t)(0.8 * (double)free_b);
+  p->held.assign(1, 0);
+  p->busy.assign(1, false);
+  p->threads.emplace_back(batch_main, p);
+  *out = p;
+  return BRUNO_OK;
+}
 
 extern "C" bruno_status bruno_pool_create(const bruno_cfg *cfg, int32_t workers, uint64_t mem_budget,
                                           bruno_pool **out) {

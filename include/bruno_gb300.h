@@ -81,6 +81,9 @@ typedef struct bruno_cfg {
   int32_t rank_fill;        /* the O(M) ranking's final states: 0 = a second walk of every segment
                                between rulers; 1 = the first walk records each node's place on its
                                segment and one pass over the nodes sets the final states */
+  int32_t part_slots;       /* k <= 31 counting in shared memory: the most slots of one table
+                               partition, which also bounds every probe run (256..3072; 0 = 3072) */
+  int32_t count_threads;    /* threads of a partition's counting block (256, 512 or 1024; 0 = 512) */
 } bruno_cfg;
 
 typedef struct bruno_sizes {
@@ -340,6 +343,36 @@ bruno_status bruno_host_free(void *p);
 bruno_status bruno_phase_ms(bruno_ctx *ctx, double *ms, size_t n);
 
 /* ---------------------------------------------------------------------------------------
+ * Batched form: many samples built in one pass.  No counterpart in the reference (one graph per
+ * MPI job there).  The n_samples FASTQ buffers (host memory, or device memory with is_device)
+ * are copied one after another into one device buffer, and every kernel of the path runs once
+ * over all of them: each sample counts into hash-table partitions of its own (sized from its own
+ * distinct-count estimate), is filtered, chained and ranked, so that each sample's graph, chains
+ * and counts are exactly what bruno_build_and_compact gives for that sample alone.  The whole
+ * path of one sample is the reference driver's build_index_thresholded -> extract_chains ->
+ * list_rank[_min_update] -> to_ranked_chain_nodes (compact_dbg_freq_construct_clean.cpp:
+ * 295-348, 549-737).  Needs k <= 31, no edge filter, no raw or filtered count copies, and
+ * thresholds on the (k+1)-mer counts only (one -L / -U value: the chain maps are then mutually
+ * consistent); at most 16384 samples.  The results stay in the context, grouped by sample, until
+ * the next build or reset; bruno_copy_ranked / bruno_copy_chains return all samples' results
+ * (sample after sample), the calls below one sample's. */
+bruno_status bruno_build_samples(bruno_ctx *ctx, const char *const *bufs, const size_t *nbytes, size_t n_samples,
+                                 int32_t is_device);
+/* Samples of the last batch (0 if none was built). */
+bruno_status bruno_sample_count(bruno_ctx *ctx, size_t *n_samples);
+/* One sample's sizes, as bruno_get_sizes gives them for a plain build of the sample alone
+ * (n_filtered and filter_flag_hist are not kept per sample and read 0). */
+bruno_status bruno_sample_sizes(bruno_ctx *ctx, size_t sample, bruno_sizes *out);
+/* One sample's listranked nodes, compacted chains (offsets into the sample's own chars) and graph
+ * nodes, in the formats of bruno_copy_ranked / bruno_copy_chains / bruno_copy_nodes. */
+bruno_status bruno_sample_copy_ranked(bruno_ctx *ctx, size_t sample, uint64_t *K, uint64_t *rep, int32_t *dist,
+                                      size_t cap, size_t *n);
+bruno_status bruno_sample_copy_chains(bruno_ctx *ctx, size_t sample, uint64_t *reps, uint64_t *offsets, char *chars,
+                                      size_t cap_chains, size_t cap_chars, size_t *n_chains, size_t *n_chars);
+bruno_status bruno_sample_copy_nodes(bruno_ctx *ctx, size_t sample, uint64_t *keys, uint16_t *counts, uint8_t *flags,
+                                     size_t cap, size_t *n);
+
+/* ---------------------------------------------------------------------------------------
  * Many builds at once.  No counterpart in the reference (one graph per MPI job there): a pool
  * of `workers` host threads, each with its own context and stream, runs
  * bruno_build_and_compact for submitted FASTQ buffers, so several small graphs share the GPU.
@@ -365,6 +398,14 @@ typedef struct bruno_pool_result {
   double run_ms;            /* start -> result on the host */
 } bruno_pool_result;
 bruno_status bruno_pool_create(const bruno_cfg *cfg, int32_t workers, uint64_t mem_budget, bruno_pool **out);
+/* The same pool over the batched form (continuous batching): one scheduler thread repeatedly
+ * takes every queued request whose estimates fit mem_budget together (at least one, at most
+ * max_samples, 1..16384) and builds them in one fused pass (bruno_build_samples); requests that
+ * arrive during a pass join the next one.  Results, submit / wait / free / destroy as above (run_ms
+ * is the pass that built the request).  Where the batched form refuses the configuration, each
+ * request is built with the plain path instead; every result equals the plain path's. */
+bruno_status bruno_pool_create_batched(const bruno_cfg *cfg, uint32_t max_samples, uint64_t mem_budget,
+                                       bruno_pool **out);
 bruno_status bruno_pool_submit(bruno_pool *pool, const char *buf, size_t nbytes, uint64_t *ticket);
 /* Blocks until the request is done; the result's arrays belong to the caller. */
 bruno_status bruno_pool_wait(bruno_pool *pool, uint64_t ticket, bruno_pool_result *out);

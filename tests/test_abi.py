@@ -140,3 +140,25 @@ int main(void) {{
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
     V, C = bg._DeviceView, bg._Cfg
     assert got == [ctypes.sizeof(V), V.chain_chars.offset, V.n_ranked.offset, V.words.offset, C.rank_fill.offset]
+
+
+def test_check_and_tunable_layouts_match_header(tmp_path):
+    src = tmp_path / "layout5.c"
+    src.write_text(f'''
+#include <stdio.h>
+#include <stddef.h>
+#include "{HEADER}"
+int main(void) {{
+  printf("%zu %zu %zu\\n", sizeof(bruno_index_check), offsetof(bruno_index_check, n_unanswered),
+         offsetof(bruno_index_check, edge_hist));
+  printf("%zu %zu %zu\\n", offsetof(bruno_cfg, part_slots), offsetof(bruno_cfg, count_threads), sizeof(bruno_cfg));
+  printf("%d %d %d\\n", (int)BRUNO_IS_CHAIN_NODE, (int)BRUNO_CHAIN_POINTS_TO_INTERNAL_NODE, (int)BRUNO_IS_BRANCH_POINT);
+  return 0;
+}}''')
+    exe = tmp_path / "layout5"
+    subprocess.run(["gcc", "-std=c99", "-o", str(exe), str(src)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    X, C = bg._IndexCheck, bg._Cfg
+    assert got == [ctypes.sizeof(X), X.n_unanswered.offset, X.edge_hist.offset, C.part_slots.offset,
+                   C.count_threads.offset, ctypes.sizeof(C), bg.NODE_FILTERS["IsChainNode"],
+                   bg.CHAIN_FILTERS["PointsToInternalNode"], bg.NODE_FILTERS["IsBranchPoint"]]

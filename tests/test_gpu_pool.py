@@ -99,3 +99,67 @@ def test_bad_request_reports_its_status():
         _same(pool.wait(t_good), _alone(good))
     finally:
         pool.close()
+
+
+# ------------------------------------------------------- continuous batching (the served form)
+def test_batched_pool_equals_plain_path():
+    """requests queued together are built in fused passes; each result is its plain build's"""
+    fqs = _samples(24, 21)
+    pool = bg.Pool(batched=True, max_samples=16, thresh=bg.thresholds([2]), min_update=True)
+    try:
+        results = [pool.wait(t) for t in [pool.submit(fq) for fq in fqs]]
+    finally:
+        pool.close()
+    # requests of one pass share its run time: the 24 requests went in at most a few passes
+    assert len({round(r["run_ms"], 6) for r in results}) < len(fqs)
+    for fq, r in zip(fqs, results):
+        _same(r, _alone(fq))
+
+
+def test_batched_pool_requests_join_later_passes():
+    """requests from several threads arrive while passes run and join the next pass"""
+    fqs = _samples(16, 22)
+    alone = [_alone(fq) for fq in fqs]
+    pool = bg.Pool(batched=True, max_samples=64, thresh=bg.thresholds([2]), min_update=True)
+    got = {}
+
+    def client(idx):
+        for i in idx:
+            time.sleep(0.003 * (i % 3))
+            got[i] = pool.wait(pool.submit(fqs[i]))
+
+    try:
+        threads = [threading.Thread(target=client, args=(list(range(c, 16, 4)),)) for c in range(4)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+    finally:
+        pool.close()
+    for i in range(16):
+        _same(got[i], alone[i])
+
+
+def test_batched_pool_bad_request_falls_back_per_request():
+    """a malformed request fails its pass; each request of that pass is then built alone"""
+    pool = bg.Pool(batched=True, max_samples=8, thresh=bg.thresholds([2]))
+    try:
+        good = _samples(2, 23)
+        tickets = [pool.submit(good[0]), pool.submit(b"@r\nACGT\n-\nIIII\n"), pool.submit(good[1])]
+        res = [pool.wait(t) for t in tickets]
+    finally:
+        pool.close()
+    assert res[1]["status"] == 2
+    _same(res[0], _alone(good[0]))
+    _same(res[2], _alone(good[1]))
+
+
+def test_batched_pool_small_budget_one_request_a_pass():
+    fqs = _samples(5, 24)
+    pool = bg.Pool(batched=True, max_samples=8, mem_budget=1 << 20, thresh=bg.thresholds([2]), min_update=True)
+    try:
+        results = [pool.wait(t) for t in [pool.submit(fq) for fq in fqs]]
+    finally:
+        pool.close()
+    for fq, r in zip(fqs, results):
+        _same(r, _alone(fq))
