@@ -94,7 +94,7 @@ EXPORTS = (
     "bruno_device_results", "bruno_graph_find_if", "bruno_graph_erase_if", "bruno_graph_erase_nodes",
     "bruno_chain_find_if", "bruno_get_cycle_node_kmers", "bruno_get_isolated", "bruno_check_index",
     "bruno_build_samples", "bruno_sample_count", "bruno_sample_sizes", "bruno_sample_copy_ranked",
-    "bruno_sample_copy_chains", "bruno_sample_copy_nodes", "bruno_pool_create_batched",
+    "bruno_sample_copy_chains", "bruno_sample_copy_nodes", "bruno_pool_create_batched", "bruno_sample_ranges",
 )
 
 # node predicates (bliss::debruijn::filter::graph) and chain predicates
@@ -148,6 +148,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "bruno_sample_copy_chains": [P, SZ, P, P, P, SZ, SZ, PSZ, PSZ],
         "bruno_sample_copy_nodes": [P, SZ, P, P, P, SZ, PSZ],
         "bruno_pool_create_batched": [ctypes.POINTER(_Cfg), ctypes.c_uint32, U64, ctypes.POINTER(P)],
+        "bruno_sample_ranges": [P, P, P, P],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -383,6 +384,20 @@ class Graph:
         d = {n: getattr(s, n) for n, _ in _Sizes._fields_ if n != "filter_flag_hist"}
         d["filter_flag_hist"] = list(s.filter_flag_hist)
         return d
+
+    def batch_chains(self) -> list:
+        """every sample's compacted chains (reps, offsets, chars) from one copy of the batch's chains"""
+        n = self.sample_count()
+        c0 = np.zeros(n + 1, np.uint64)
+        ch0 = np.zeros(n + 1, np.uint64)
+        self._check(self.lib.bruno_sample_ranges(self.ctx, None, self._ptr(c0), self._ptr(ch0)), "sample_ranges")
+        reps, offs, chars = self.chains()
+        out = []
+        for i in range(n):
+            a, b = int(c0[i]), int(c0[i + 1])
+            base = int(ch0[i])
+            out.append((reps[a:b], offs[a:b + 1] - np.uint64(base), chars[base:int(ch0[i + 1])]))
+        return out
 
     def sample_ranked(self, sample: int):
         n = ctypes.c_size_t()

@@ -966,25 +966,13 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract(const uint64_t *rstart, con
   for (int x = tid; x < HLL_M; x += XTPB) dst[x] = (uint8_t)S.hll[x];
 }
 
-/* ------------------------------------------------ warp-per-read extraction
- * Phase A of the partitioned count, one warp per read: the warp stages up to WX_SUB k-mer
- * positions of its read as 2-bit words with coalesced byte loads and ballots (stage_chunk),
- * every lane then rolls a contiguous run of canonical (k-mer, biedge) pairs
- * (for_each_kmer_run), and each pair becomes the same 8-byte record as in k_extract.  The
- * records of a round go to a block-wide stage in shared memory (one reservation per warp and
- * round); when the stage is full the block sorts it by bucket (histogram, scan, scatter) and
- * appends each bucket's run to chunks of `chunk` records the block claims per bucket, one
- * global atomic per claim, so the bucket files grow by contiguous runs without a global
- * atomic per flush.  Work comes as items of consecutive reads of one sample (the batched form
- * counts many samples at once, each in buckets of its own); a block takes a contiguous range of
- * items, so it changes sample rarely, and zeroes the unused tails of its chunks when it does.
- * The distinct-count estimate is a HyperLogLog per sample, fed with the k-mers whose mix has
- * its HLL_SAMPLE low bits zero (1 in 8; the estimate is scaled back). */
-constexpr int WX_TPB = 256, WX_WARPS = WX_TPB / 32;
-constexpr int WX_SUB = 128;                             /* positions a warp emits per round */
-constexpr int WX_STAGE = 3072;                          /* records staged per block between flushes */
-constexpr int WX_FLUSH = WX_STAGE - WX_WARPS * WX_SUB;  /* flush when another round might not fit */
-constexpr int WX_WORDS = 12;                            /* staged words per warp: 32 + 128 + k + 1 bases + 3 spare */
+/* ------------------------------------------------ extraction by samples
+ * k_extract_s is k_extract (one thread per read, per-bucket queues in shared memory, chunk
+ * claims) over work items of one sample's reads: every sample has buckets of its own (the
+ * batched form counts many samples at once; the plain build is one sample).  A block takes a
+ * contiguous range of items, so it changes sample rarely; when it does, it zeroes the unused
+ * tails of its chunks and folds its HyperLogLog registers into the sample's.  The estimate is
+ * fed with the k-mers whose mix has its HLL_SAMPLE low bits zero (1 in 8; scaled back). */
 constexpr int HLL_SAMPLE = 3;
 
 /* bucket b of sample s holds records[rec_base + b * cap, + cap); chunk = records a block claims at once */
@@ -992,305 +980,166 @@ struct XSample { unsigned long long rec_base, cap; unsigned int chunk, pad; };
 /* reads [a, b) of sample s */
 struct XItem { unsigned long long a, b; unsigned int s, pad; };
 
-static_assert(WX_TPB == NBUCKET, "one bucket a thread in the flush");
-
-struct WXSmem {
-  uint64_t stage[WX_STAGE];
-  uint64_t sorted[WX_STAGE];
-  uint8_t stage_b[WX_STAGE];
-  uint8_t sorted_b[WX_STAGE];
-  uint64_t words[WX_WARPS][WX_WORDS];
-  unsigned long long cpos[NBUCKET], cend[NBUCKET];   /* the block's open chunk per bucket */
-  unsigned long long base1[NBUCKET], base2[NBUCKET];
-  unsigned int cnt[NBUCKET], start[NBUCKET], rem[NBUCKET];
-  unsigned int wsum[WX_WARPS + 1];
-  unsigned int n, item_next;
-  unsigned long long inst, used;
-  int overflow;
-  unsigned int hll[HLL_M / 4];   /* the block's HyperLogLog registers for its current sample, a byte each */
-};
-
-/* register idx = max(register, v), a byte in a 32-bit word of shared memory; a CAS that loses to
- * another update retries (at most 64 times: a register left low only lowers the estimate, which
- * the table's regrowth absorbs) */
-__device__ __forceinline__ void hll_max_u8(unsigned int *reg, unsigned idx, unsigned v) {
-  unsigned int *w = reg + (idx >> 2);
-  const unsigned sh = 8 * (idx & 3);
-  unsigned old = *w;
-  for (int t = 0; t < 64 && ((old >> sh) & 0xFFu) < v; ++t) {
-    const unsigned prev = atomicCAS(w, old, (old & ~(0xFFu << sh)) | (v << sh));
-    if (prev == old) break;
-    old = prev;
-  }
-}
-
-/* the block's registers into the sample's (atomic max), then cleared */
-__device__ __forceinline__ void hll_flush(WXSmem &S, unsigned int *hreg) {
-  __syncthreads();
-  for (int i = threadIdx.x; i < HLL_M / 4; i += WX_TPB) {
-    const unsigned w = S.hll[i];
-    if (w) {
-      #pragma unroll
-      for (int b = 0; b < 4; ++b) {
-        const unsigned v = (w >> (8 * b)) & 0xFFu;
-        if (v) atomicMax(&hreg[4 * i + b], v);
-      }
-      S.hll[i] = 0;
-    }
-  }
-  __syncthreads();
-}
-
-/* the stage's records into their buckets' chunks (every thread of the block calls it) */
-__device__ __forceinline__ void wx_flush(WXSmem &S, const XSample &xs, unsigned s, uint64_t *records,
-                                         unsigned long long *bucket_cnt) {
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const unsigned n = S.n;
-  S.cnt[tid] = 0;   /* WX_TPB == NBUCKET: one bucket a thread */
-  __syncthreads();
-  uint16_t rank[WX_STAGE / WX_TPB];
-  #pragma unroll
-  for (int j = 0; j < WX_STAGE / WX_TPB; ++j) {
-    const unsigned i = tid + j * WX_TPB;
-    if (i < n) rank[j] = (uint16_t)atomicAdd(&S.cnt[S.stage_b[i]], 1u);
-  }
-  __syncthreads();
-  /* exclusive scan of the 256 counts */
-  const unsigned v = S.cnt[tid];
-  unsigned x = v;
-  #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const unsigned y = __shfl_up_sync(~0u, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) S.wsum[wid] = x;
-  __syncthreads();
-  if (tid == 0) {
-    unsigned run = 0;
-    for (int w = 0; w < WX_WARPS; ++w) { const unsigned t = S.wsum[w]; S.wsum[w] = run; run += t; }
-  }
-  __syncthreads();
-  S.start[tid] = S.wsum[wid] + x - v;
-  /* reservations: the open chunk first, then a new chunk of max(need, chunk) records */
-  if (v) {
-    const unsigned long long p = S.cpos[tid], avail = S.cend[tid] - p;
-    S.base1[tid] = p;
-    if (avail >= v) {
-      S.rem[tid] = v;
-      S.cpos[tid] = p + v;
-    } else {
-      const unsigned long long need = v - avail, ch = max(need, (unsigned long long)xs.chunk);
-      const unsigned long long old = atomicAdd(&bucket_cnt[(uint64_t)s * NBUCKET + tid], ch);
-      if (old + ch > xs.cap) S.overflow = 1;
-      const unsigned long long nb = xs.rec_base + (uint64_t)tid * xs.cap + old;
-      S.rem[tid] = (unsigned)avail;
-      S.base2[tid] = nb;
-      S.cpos[tid] = nb + need;
-      S.cend[tid] = nb + ch;
-    }
-  }
-  __syncthreads();
-  #pragma unroll
-  for (int j = 0; j < WX_STAGE / WX_TPB; ++j) {
-    const unsigned i = tid + j * WX_TPB;
-    if (i < n) {
-      const unsigned b = S.stage_b[i], y = S.start[b] + rank[j];
-      S.sorted[y] = S.stage[i];
-      S.sorted_b[y] = (uint8_t)b;
-    }
-  }
-  __syncthreads();
-  for (unsigned y = tid; y < n; y += WX_TPB) {
-    const unsigned b = S.sorted_b[y], j = y - S.start[b];
-    const unsigned long long dst = j < S.rem[b] ? S.base1[b] + j : S.base2[b] + (j - S.rem[b]);
-    if (dst < xs.rec_base + (unsigned long long)(b + 1) * xs.cap) records[dst] = S.sorted[y];
-  }
-  __syncthreads();
-  if (tid == 0) S.n = 0;
-  __syncthreads();
-}
-
-/* the unused tails of the block's chunks hold no records (0 is never a record) */
-__device__ __forceinline__ void wx_close(WXSmem &S, const XSample &xs, uint64_t *records) {
+/* the block's open chunks of sample xs closed (tails zeroed) and its registers folded into the
+ * sample's (every thread of the block calls it) */
+__device__ __forceinline__ void xs_close(ExtractSmem &S, const XSample &xs, uint64_t *records, unsigned int *hreg) {
   const int tid = threadIdx.x;
-  for (int b = tid >> 5; b < NBUCKET; b += WX_WARPS) {
+  __syncthreads();
+  for (int b = tid >> 5; b < NBUCKET; b += XTPB / 32) {
     const unsigned long long e = min(S.cend[b], xs.rec_base + (unsigned long long)(b + 1) * xs.cap);
     for (unsigned long long p = S.cpos[b] + (tid & 31); p < e; p += 32) records[p] = 0ull;
   }
-  __syncthreads();
-  S.cpos[tid] = 0;
-  S.cend[tid] = 0;
-  __syncthreads();
-}
-
-/* Stages bases [c0, c0 + 256) of a read (c0 = p0 - 32; bases outside [0, L) read as A) as 2-bit
- * words in the layout of stage_chunk, in one round of loads: lane j covers bases [c0 + 8j,
- * c0 + 8j + 8) with at most two aligned 8-byte loads, each holding a byte of the read (nothing
- * outside the read's own bytes is touched beyond the words that hold them).  Returns true if a
- * base of the read in the window is not A/C/G/T. */
-__device__ __forceinline__ bool stage_window(const unsigned char *s, uint32_t L, long long c0, uint64_t *words,
-                                             int lane) {
-  const long long lo = c0 + 8 * lane;
-  unsigned code16 = 0;
-  bool bad = false;
-  if (lo + 8 > 0 && lo < (long long)L) {
-    const uintptr_t sa = (uintptr_t)s, ea = sa + L;
-    const uintptr_t a = sa + (uintptr_t)lo;   /* wraps for lo < 0: compared below as a signed offset */
-    const long long first = lo > 0 ? lo : 0, last = (lo + 8 < (long long)L ? lo + 8 : (long long)L) - 1;
-    const uintptr_t w0 = (sa + (uintptr_t)first) & ~(uintptr_t)7, w1 = (sa + (uintptr_t)last) & ~(uintptr_t)7;
-    const uint64_t x0 = __ldg((const unsigned long long *)w0);
-    const uint64_t x1 = w1 != w0 ? __ldg((const unsigned long long *)w1) : 0ull;
-    (void)ea;
-    #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const long long off = lo + i;
-      unsigned c = 0;
-      if (off >= 0 && off < (long long)L) {
-        const uintptr_t ad = a + (uintptr_t)i;
-        const uint64_t x = (ad & ~(uintptr_t)7) == w0 ? x0 : x1;
-        const unsigned b = (unsigned)(x >> (8 * (ad & 7))) & 0xFFu;
-        const unsigned l = b | 0x20u;
-        bad |= !(l == 'a' || l == 'c' || l == 'g' || l == 't');
-        c = ((b >> 1) ^ (b >> 2)) & 3u;   /* A0 C1 G2 T3, either case */
-      }
-      code16 |= c << (14 - 2 * i);
-    }
+  for (int i = tid; i < HLL_M; i += XTPB) {
+    if (S.hll[i]) atomicMax(&hreg[i], S.hll[i]);
+    S.hll[i] = 0;
   }
-  /* word q = bases [c0 + 32q, +32): lanes 4q .. 4q+3, 16 bits each, first base highest */
-  const unsigned n1 = __shfl_down_sync(~0u, code16, 1), n2 = __shfl_down_sync(~0u, code16, 2),
-                 n3 = __shfl_down_sync(~0u, code16, 3);
-  if ((lane & 3) == 0)
-    words[lane >> 2] = ((uint64_t)code16 << 48) | ((uint64_t)n1 << 32) | ((uint64_t)n2 << 16) | (uint64_t)n3;
-  if (lane < 3) words[8 + lane] = 0;
-  __syncwarp();
-  return __any_sync(~0u, bad);
+  __syncthreads();
+  for (int b = tid; b < NBUCKET; b += XTPB) { S.cpos[b] = 0; S.cend[b] = 0; }
+  __syncthreads();
 }
 
-__global__ void __launch_bounds__(WX_TPB, 3) k_extract_w(const uint64_t *rstart, const uint64_t *rend, uint64_t r0,
-                                                         uint64_t r1, const XItem *items, uint64_t n_items,
-                                                         uint32_t item_reads, int k, const XSample *xsamp,
-                                                         uint64_t *records, unsigned long long *bucket_cnt,
-                                                         unsigned int *hll, unsigned long long *s_inst,
-                                                         unsigned long long *s_used, DevCounters *ctr) {
+__global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, const uint64_t *rend, uint64_t r0,
+                                                        uint64_t r1, const XItem *items, uint64_t n_items,
+                                                        uint32_t item_reads, int k, const XSample *xsamp,
+                                                        uint64_t *records, unsigned long long *bucket_cnt,
+                                                        unsigned int *hll, unsigned long long *s_inst,
+                                                        unsigned long long *s_used, DevCounters *ctr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  WXSmem &S = *reinterpret_cast<WXSmem *>(smem_raw);
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  S.cpos[tid] = 0;
-  S.cend[tid] = 0;
-  for (int i = tid; i < HLL_M / 4; i += WX_TPB) S.hll[i] = 0;
-  if (tid == 0) { S.n = 0; S.overflow = 0; }
+  ExtractSmem &S = *reinterpret_cast<ExtractSmem *>(smem_raw);
+  const int tid = threadIdx.x;
+  for (int i = tid; i < HLL_M; i += XTPB) S.hll[i] = 0;
+  for (int i = tid; i < NBUCKET; i += XTPB) { S.cnt[i] = 0; S.cpos[i] = 0; S.cend[i] = 0; }
+  if (tid == 0) S.overflow = 0;
+  __syncthreads();
+  const uint64_t kmask = (k == 32) ? ~0ull : ((1ull << (2 * k)) - 1);
+  const int top = 2 * k - 2;
   const uint64_t nit = items ? n_items : (r1 - r0 + item_reads - 1) / item_reads;
-  /* a contiguous range of items per block */
   const uint64_t per = (nit + gridDim.x - 1) / gridDim.x;
   const uint64_t it0 = min(nit, (uint64_t)blockIdx.x * per), it1 = min(nit, it0 + per);
   unsigned cur_s = ~0u;
   XSample xs{};
-  __syncthreads();
+  unsigned long long inst_all = 0, used_all = 0;
   for (uint64_t it = it0; it < it1; ++it) {
     uint64_t a, b;
-    unsigned s;
-    if (items) { a = items[it].a; b = items[it].b; s = items[it].s; }
-    else { a = r0 + it * item_reads; b = min(r1, a + item_reads); s = 0; }
-    if (s != cur_s) {   /* a new sample: flush what is staged, close the old sample's chunks */
-      if (cur_s != ~0u) {
-        if (S.n) wx_flush(S, xs, cur_s, records, bucket_cnt);
-        wx_close(S, xs, records);
-        hll_flush(S, hll + (uint64_t)cur_s * HLL_M);
-      }
-      cur_s = s;
-      xs = xsamp[s];
+    unsigned smp;
+    if (items) { a = items[it].a; b = items[it].b; smp = items[it].s; }
+    else { a = r0 + it * item_reads; b = min(r1, a + item_reads); smp = 0; }
+    if (smp != cur_s) {
+      if (cur_s != ~0u) xs_close(S, xs, records, hll + (uint64_t)cur_s * HLL_M);
+      cur_s = smp;
+      xs = xsamp[smp];
     }
-    if (tid == 0) { S.item_next = 0; S.inst = 0; S.used = 0; }
-    __syncthreads();
-    const unsigned char *sp = nullptr;
-    uint32_t L = 0, npos = 0, p0 = 0;
-    bool have = false;
+    uint64_t r = a + tid;
     unsigned long long inst = 0, used = 0;
-    /* the warp's next read, its span loaded ahead while the current one is processed */
-    uint64_t nr = ~0ull, ns = 0, ne = 0;
-    auto grab = [&]() {
-      unsigned idx = 0;
-      if (lane == 0) idx = atomicAdd(&S.item_next, 1u);
-      idx = __shfl_sync(~0u, idx, 0);
-      nr = a + idx < b ? a + idx : ~0ull;
-      if (nr != ~0ull) { ns = rstart[nr]; ne = rend[nr]; }
-    };
-    grab();
-    for (;;) {
-      while (!have) {   /* this warp's next usable read of the item */
-        if (nr == ~0ull) break;
-        sp = (const unsigned char *)ns;
-        L = (uint32_t)(ne - ns);
-        grab();
-        if (L < (uint32_t)k + 2) continue;           /* shorter than the k+2 window */
-        npos = L - k + 1;
-        if (npos > (uint32_t)WX_SUB) {                /* long read: the N filter before any record */
-          bool bad = false;
-          for (uint32_t i = lane; i < L; i += 32) bad |= base_code(sp[i]) < 0;
-          if (__any_sync(~0u, bad)) continue;
-        }
-        p0 = 0;
-        have = true;
+    SeqCursor sc;
+    uint32_t L = 0, i = 0;
+    uint64_t fwd = 0, rev = 0;
+    unsigned left = 0;
+    /* advance to the next usable read of this thread in the item */
+    auto next_read = [&]() -> bool {
+      for (; r < b; r += XTPB) {
+        const unsigned char *sp = (const unsigned char *)rstart[r], *ep = (const unsigned char *)rend[r];
+        const uint32_t len = (uint32_t)(ep - sp);
+        if (len < (uint32_t)k + 2 || !seq_valid(sp, ep)) continue;
+        ++used;
+        sc.init(sp, ep);
+        L = len; i = 0; fwd = 0; rev = 0; left = 0;
+        return true;
       }
-      if (!__syncthreads_or(have)) break;             /* the item is done */
-      if (have) {
-        const uint32_t pend = min(npos, p0 + WX_SUB);
-        __syncwarp();
-        const bool bad = stage_window(sp, L, (long long)p0 - 32, S.words[wid], lane);
-        if (bad) {
-          have = false;                                /* a short read with N: dropped whole */
-        } else {
-          if (p0 == 0) used += (lane == 0);
-          for_each_kmer_run<KW1>(S.words[wid], p0, pend, p0, L, k, lane, [&](bool valid, KW1 x, unsigned code) {
-            uint64_t rec = 0;
-            unsigned bk = 0;
-            if (valid) {
-              ++inst;
-              const uint64_t h = bj_fwd(x.v);
-              bk = (unsigned)(h >> LOW_BITS);
-              rec = ((h & ((1ull << LOW_BITS) - 1)) << 5) | code;
-              if ((h & ((1u << HLL_SAMPLE) - 1)) == 0) {
-                const unsigned idx = (unsigned)(h >> (62 - HLL_P));
-                const unsigned rho = (unsigned)__clzll((h << (2 + HLL_P)) | (1ull << (1 + HLL_P))) + 1u;
-                if (rho > ((S.hll[idx >> 2] >> (8 * (idx & 3))) & 0xFFu)) hll_max_u8(S.hll, idx, rho);
-              }
-            }
-            const unsigned m = __ballot_sync(~0u, valid);
-            if (m) {
-              unsigned base = 0;
-              if (lane == 0) base = atomicAdd(&S.n, (unsigned)__popc(m));
-              base = __shfl_sync(~0u, base, 0);
-              if (valid) {
-                const unsigned o = base + __popc(m & ((1u << lane) - 1));
-                S.stage[o] = rec;
-                S.stage_b[o] = (uint8_t)bk;
-              }
-            }
-          });
-          p0 = pend;
-          if (p0 >= npos) have = false;
+      return false;
+    };
+    auto emit = [&](unsigned in5, unsigned out5) {
+      uint64_t x = fwd;
+      if (!(fwd < rev)) {   /* lex_less: flip the k-mer and reverse-complement the biedge */
+        x = rev;
+        const unsigned ni = out5 ? 5u - out5 : 0u, no = in5 ? 5u - in5 : 0u;
+        in5 = ni; out5 = no;
+      }
+      const uint64_t h = bj_fwd(x);
+      const unsigned bucket = (unsigned)(h >> LOW_BITS);
+      const uint64_t rec = ((h & ((1ull << LOW_BITS) - 1)) << 5) | biedge_code(in5, out5);
+      if ((h & ((1u << HLL_SAMPLE) - 1)) == 0) {
+        const unsigned idx = (unsigned)(h >> (62 - HLL_P));
+        const unsigned rho = (unsigned)__clzll((h << (2 + HLL_P)) | (1ull << (1 + HLL_P))) + 1u;
+        if (rho > S.hll[idx]) atomicMax(&S.hll[idx], rho);
+      }
+      ++inst;
+      const unsigned pos = atomicAdd(&S.cnt[bucket], 1u);
+      if (pos < (unsigned)XQ) {
+        S.q[bucket][pos] = rec;
+      } else {   /* queue full this round: append straight to the bucket */
+        const unsigned long long o = atomicAdd(&bucket_cnt[(uint64_t)cur_s * NBUCKET + bucket], 1ull);
+        if (o < xs.cap) records[xs.rec_base + (uint64_t)bucket * xs.cap + o] = rec;
+        else S.overflow = 1;
+      }
+    };
+    bool active = next_read();
+    for (;;) {
+      int emitted = 0;
+      while (active && emitted < XROUND) {
+        const unsigned byte = sc.next();
+        const unsigned c = ((byte >> 1) ^ (byte >> 2)) & 3u;   /* A0 C1 G2 T3, either case */
+        if (i >= (uint32_t)k) {   /* the k-mer ending before base i, its out-base is base i */
+          emit(i > (uint32_t)k ? left + 1u : 0u, c + 1u);
+          ++emitted;
+        }
+        left = (unsigned)(fwd >> top) & 3u;
+        fwd = ((fwd << 2) | c) & kmask;
+        rev = (rev >> 2) | ((uint64_t)(3u - c) << top);
+        if (++i == L) {   /* the last k-mer has no out-base */
+          emit(left + 1u, 0u);
+          ++emitted;
+          r += XTPB;
+          active = next_read();
         }
       }
       __syncthreads();
-      if (S.n > (unsigned)WX_FLUSH) wx_flush(S, xs, cur_s, records, bucket_cnt);
+      /* each block fills chunks of `chunk` records per bucket, claimed with one atomic each, so
+       * most flushes need no global atomic; a chunk's unused tail is zeroed when the block
+       * leaves the sample (0 is no record: a biedge code is never 0) */
+      if (tid < NBUCKET) {
+        const unsigned f = min(S.cnt[tid], (unsigned)XQ);
+        if (f) {
+          const unsigned long long p = S.cpos[tid], avail = S.cend[tid] - p;
+          S.base[tid] = p;
+          if (avail >= f) {
+            S.rem[tid] = f;
+            S.cpos[tid] = p + f;
+          } else {
+            const unsigned long long need = f - avail, ch = max(need, (unsigned long long)xs.chunk);
+            const unsigned long long old = atomicAdd(&bucket_cnt[(uint64_t)cur_s * NBUCKET + tid], ch);
+            if (old + ch > xs.cap) S.overflow = 1;
+            const unsigned long long nb = xs.rec_base + (unsigned long long)tid * xs.cap + old;
+            S.rem[tid] = (unsigned)avail;
+            S.base2[tid] = nb;
+            S.cpos[tid] = nb + need;
+            S.cend[tid] = nb + ch;
+          }
+        }
+      }
+      __syncthreads();
+      for (int x = tid; x < NBUCKET * XQ; x += XTPB) {
+        const int bk = x / XQ, j = x % XQ;
+        if ((unsigned)j < min(S.cnt[bk], (unsigned)XQ)) {
+          const unsigned long long dst = (unsigned)j < S.rem[bk] ? S.base[bk] + j : S.base2[bk] + (j - S.rem[bk]);
+          if (dst < xs.rec_base + (unsigned long long)(bk + 1) * xs.cap) records[dst] = S.q[bk][j];
+        }
+      }
+      __syncthreads();
+      if (tid < NBUCKET) S.cnt[tid] = 0;
+      if (!__syncthreads_or(active)) break;
     }
-    /* the item's tallies */
     inst = warp_sum(inst); used = warp_sum(used);
-    if (lane == 0) {
-      if (inst) atomicAdd(&S.inst, inst);
-      if (used) atomicAdd(&S.used, used);
+    if ((tid & 31) == 0) {
+      inst_all += inst; used_all += used;
+      if (s_inst && inst) atomicAdd(&s_inst[smp], inst);
+      if (s_used && used) atomicAdd(&s_used[smp], used);
     }
-    __syncthreads();
-    if (tid == 0) {
-      if (S.inst) { atomicAdd(&ctr->n_instances, S.inst); if (s_inst) atomicAdd(&s_inst[s], S.inst); }
-      if (S.used) { atomicAdd(&ctr->n_reads_used, S.used); if (s_used) atomicAdd(&s_used[s], S.used); }
-    }
-    __syncthreads();
   }
-  if (cur_s != ~0u) {
-    if (S.n) wx_flush(S, xs, cur_s, records, bucket_cnt);
-    wx_close(S, xs, records);
-    hll_flush(S, hll + (uint64_t)cur_s * HLL_M);
+  if (cur_s != ~0u) xs_close(S, xs, records, hll + (uint64_t)cur_s * HLL_M);
+  if ((tid & 31) == 0) {
+    if (inst_all) atomicAdd(&ctr->n_instances, inst_all);
+    if (used_all) atomicAdd(&ctr->n_reads_used, used_all);
   }
   if (tid == 0 && S.overflow) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
 }
@@ -1818,10 +1667,13 @@ __device__ __forceinline__ bool sm_count(uint64_t *sm, uint32_t sm_base, uint32_
  * the partition's records into them, write the region back.  Partition j of sample s holds the
  * records whose mix has j in its top pbits bits: the bucket (top 8) and the split bits. */
 __global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, const unsigned long long *rec_cnt,
-                                                       const SGeom *sg, uint32_t nsamples, uint64_t *table,
-                                                       unsigned long long *s_tally, DevCounters *ctr) {
+                                                       const SGeom *sg, uint32_t nsamples, const uint32_t *plist,
+                                                       uint64_t *table, unsigned long long *s_tally,
+                                                       DevCounters *ctr) {
   extern __shared__ __align__(16) uint64_t sm[];
-  const uint64_t part = blockIdx.x;
+  /* plist: the partitions of one launch (a batch launches its partitions by region size, each
+   * launch with the shared memory its largest region needs); NULL = partition blockIdx.x */
+  const uint64_t part = plist ? plist[blockIdx.x] : blockIdx.x;
   const uint32_t smp = sample_of_part(sg, nsamples, part);
   const SGeom G = sg[smp];
   const uint64_t j = part - G.pbase;
@@ -2268,7 +2120,6 @@ bruno_status extract_begin(Ctx *c, uint64_t upper, int max_blocks) {
   cudaMemsetAsync(c->bucket_cnt.p, 0, NBUCKET * 8, c->stream);
   if ((st = ensure(c, c->blk_cnt, (size_t)max_blocks * HLL_M)) != BRUNO_OK) return st;
   static const bool attr = [] {
-    cudaFuncSetAttribute(k_extract<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
     cudaFuncSetAttribute(k_extract<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
     return true;
   }();
@@ -2284,12 +2135,12 @@ bruno_status extract_begin(Ctx *c, uint64_t upper, int max_blocks) {
   if ((st = cuda_check(c, cudaMemcpyAsync(c->xsamp.p, &xs, sizeof(xs), cudaMemcpyHostToDevice, c->stream),
                        "extraction layout")) != BRUNO_OK)
     return st;
-  if (!c->cfg.edge_filter) {   /* the warp-per-read extraction and its HyperLogLog */
-    static const bool wattr = [] {
-      cudaFuncSetAttribute(k_extract_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(WXSmem));
+  if (!c->cfg.edge_filter) {   /* the extraction by samples and its HyperLogLog */
+    static const bool sattr = [] {
+      cudaFuncSetAttribute(k_extract_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
       return true;
     }();
-    (void)wattr;
+    (void)sattr;
     if ((st = ensure(c, c->hllreg, HLL_M * 4)) != BRUNO_OK) return st;
     cudaMemsetAsync(c->hllreg.p, 0, HLL_M * 4, c->stream);
   }
@@ -2364,19 +2215,50 @@ bruno_status split_and_count(Ctx *c, std::vector<SGeom> &sg, const std::vector<u
     recs = (const uint64_t *)c->records2.p;
     cnts = (const unsigned long long *)c->sub_cnt.p;
   }
-  k_count_local<<<(unsigned)nparts, count_threads(c), (unsigned)(region_max * 32), c->stream>>>(
-      recs, cnts, (const SGeom *)c->sgeom.p, S, (uint64_t *)c->table.p, s_tally, c->dctr);
-  c->launches += 1;
+  if (S == 1) {
+    k_count_local<<<(unsigned)nparts, count_threads(c), (unsigned)(region_max * 32), c->stream>>>(
+        recs, cnts, (const SGeom *)c->sgeom.p, S, nullptr, (uint64_t *)c->table.p, s_tally, c->dctr);
+    c->launches += 1;
+  } else {
+    /* partitions grouped by region size: a launch per group, with shared memory for its largest */
+    static const uint64_t bound[4] = {256, 768, 1536, ~0ull};
+    std::vector<uint32_t> plist;
+    std::vector<size_t> at{0};
+    std::vector<uint64_t> rmax;
+    for (int cl = 0; cl < 4; ++cl) {
+      uint64_t m = 0;
+      for (uint32_t q = 0; q < S; ++q) {
+        const uint64_t r = sg[q].g.region;
+        if (r > bound[cl] || (cl > 0 && r <= bound[cl - 1])) continue;
+        for (uint64_t j = 0; j < (1ull << sg[q].g.pbits); ++j) plist.push_back((uint32_t)(sg[q].pbase + j));
+        m = std::max(m, r);
+      }
+      at.push_back(plist.size());
+      rmax.push_back(m);
+    }
+    if ((st = ensure(c, c->grp_tmp, plist.size() * 4 + 16)) != BRUNO_OK) return st;
+    if ((st = cuda_check(c, cudaMemcpyAsync(c->grp_tmp.p, plist.data(), plist.size() * 4, cudaMemcpyHostToDevice,
+                                            c->stream), "partition lists")) != BRUNO_OK)
+      return st;
+    for (int cl = 0; cl < 4; ++cl) {
+      const size_t n = at[cl + 1] - at[cl];
+      if (!n) continue;
+      k_count_local<<<(unsigned)n, count_threads(c), (unsigned)(rmax[cl] * 32), c->stream>>>(
+          recs, cnts, (const SGeom *)c->sgeom.p, S, (const uint32_t *)c->grp_tmp.p + at[cl], (uint64_t *)c->table.p,
+          s_tally, c->dctr);
+      c->launches += 1;
+    }
+  }
   if ((st = cuda_check(c, cudaGetLastError(), "k_count_local")) != BRUNO_OK) return st;
   ok = true;
   return BRUNO_OK;
 }
 
-/* blocks of one warp-per-read extraction launch over nr reads (at most 3 per SM, at least one
- * item of WX_ITEM reads each) */
-constexpr uint32_t WX_ITEM = 64;
+/* blocks of one extraction launch over nr reads (at most 2 per SM, at least one item of WX_ITEM
+ * reads each) */
+constexpr uint32_t WX_ITEM = XTPB * 4;
 int wx_blocks(uint64_t nr) {
-  return (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)num_sms() * 3, (nr + WX_ITEM - 1) / WX_ITEM));
+  return (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)num_sms() * 2, (nr + WX_ITEM - 1) / WX_ITEM));
 }
 
 /* one extraction launch over reads [r0, r1) */
@@ -2385,7 +2267,7 @@ void extract_reads(Ctx *c, uint64_t r0, uint64_t r1) {
   if (nr == 0) return;
   if (!c->cfg.edge_filter) {
     const int eb = std::max(1, std::min(wx_blocks(nr), c->xblk_max - c->xblk));
-    k_extract_w<<<eb, WX_TPB, sizeof(WXSmem), c->stream>>>(
+    k_extract_s<<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
         (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, r0, r1, nullptr, 0, WX_ITEM, c->cfg.k,
         (const XSample *)c->xsamp.p, (uint64_t *)c->records.p, (unsigned long long *)c->bucket_cnt.p,
         (unsigned int *)c->hllreg.p, nullptr, nullptr, c->dctr);
@@ -2396,14 +2278,10 @@ void extract_reads(Ctx *c, uint64_t r0, uint64_t r1) {
   const int eb = std::max(1, std::min<int>({num_sms() * 2, (int)((nr + XTPB - 1) / XTPB), c->xblk_max - c->xblk}));
   const uint64_t *rs = (const uint64_t *)c->rstart.p + r0, *re = (const uint64_t *)c->rend.p + r0;
   uint8_t *part = (uint8_t *)c->blk_cnt.p + (uint64_t)c->xblk * HLL_M;
-  if (c->cfg.edge_filter)
-    k_extract<true><<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
-        rs, re, nr, c->cfg.k, (uint64_t *)c->records.p, c->xcap, (unsigned long long *)c->bucket_cnt.p, part,
-        (const uint64_t *)c->k1tab.p, c->k1slots, c->xchunk, c->dctr);
-  else
-    k_extract<false><<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
-        rs, re, nr, c->cfg.k, (uint64_t *)c->records.p, c->xcap, (unsigned long long *)c->bucket_cnt.p, part, nullptr,
-        0, c->xchunk, c->dctr);
+  /* the (k+1)-mer edge filter's extraction (the rest goes by samples, above) */
+  k_extract<true><<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
+      rs, re, nr, c->cfg.k, (uint64_t *)c->records.p, c->xcap, (unsigned long long *)c->bucket_cnt.p, part,
+      (const uint64_t *)c->k1tab.p, c->k1slots, c->xchunk, c->dctr);
   c->xblk += eb;
   c->launches += 1;
 }
@@ -2738,7 +2616,7 @@ bruno_status run_count_samples(Ctx *c) {
   if (!items.empty())
     cudaMemcpyAsync(c->xitems.p, items.data(), items.size() * sizeof(XItem), cudaMemcpyHostToDevice, c->stream);
   static const bool wattr = [] {
-    cudaFuncSetAttribute(k_extract_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(WXSmem));
+    cudaFuncSetAttribute(k_extract_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
     cudaFuncSetAttribute(k_count_local, cudaFuncAttributeMaxDynamicSharedMemorySize, PART_SLOTS * 32);
     cudaFuncSetAttribute(k_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SplitSmem));
     return true;
@@ -2747,7 +2625,7 @@ bruno_status run_count_samples(Ctx *c) {
   cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
   cudaEventRecord(c->kev[0], c->stream);
   if (!items.empty())
-    k_extract_w<<<eb, WX_TPB, sizeof(WXSmem), c->stream>>>(
+    k_extract_s<<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
         (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, 0, 0, (const XItem *)c->xitems.p, items.size(),
         WX_ITEM, c->cfg.k, (const XSample *)c->xsamp.p, (uint64_t *)c->records.p,
         (unsigned long long *)c->bucket_cnt.p, (unsigned int *)c->hllreg.p, (unsigned long long *)c->s_inst.p,

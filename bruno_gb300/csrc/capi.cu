@@ -700,6 +700,19 @@ bruno_status bruno_sample_count(bruno_ctx *c, size_t *n_samples) {
   return BRUNO_OK;
 }
 
+bruno_status bruno_sample_ranges(bruno_ctx *c, uint64_t *ranked0, uint64_t *chains0, uint64_t *chars0) {
+  if (!c) return BRUNO_ERR_ARG;
+  if (c->S <= 1 || c->stage < 6 || c->h_tally.empty()) return set_err(c, BRUNO_ERR_ARG, "no batch built");
+  uint64_t chars = 0;
+  for (uint32_t q = 0; q <= c->S; ++q) {
+    if (ranked0) ranked0[q] = c->h_rank0[q];
+    if (chains0) chains0[q] = c->h_head0[q];
+    if (chars0) chars0[q] = chars;
+    if (q < c->S) chars += c->h_tally[(size_t)q * T_NUM + T_CHARS];
+  }
+  return BRUNO_OK;
+}
+
 bruno_status bruno_sample_sizes(bruno_ctx *c, size_t sample, bruno_sizes *o) {
   bruno_status st = batch_sample(c, sample);
   if (st != BRUNO_OK) return st;

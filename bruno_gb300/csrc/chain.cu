@@ -1203,14 +1203,30 @@ __global__ void __launch_bounds__(TPB) k_samp_hist(const uint32_t *samp, uint64_
   }
 }
 
+/* a place in its sample's range for every lane: the lanes of one warp with the same sample take
+ * consecutive places with one atomic on the sample's cursor (neighbouring elements mostly share
+ * a sample, and per-element atomics on one cursor serialise) */
+__device__ __forceinline__ unsigned long long group_place(uint32_t s, bool valid, unsigned long long *cursor) {
+  const int lane = threadIdx.x & 31;
+  const unsigned peers = __match_any_sync(~0u, valid ? s : ~0u);
+  const int leader = __ffs(peers) - 1;
+  unsigned long long base = 0;
+  if (valid && lane == leader) base = atomicAdd(&cursor[s], (unsigned long long)__popc(peers));
+  base = __shfl_sync(~0u, base, leader);
+  return base + __popc(peers & ((1u << lane) - 1));
+}
+
 /* listranked nodes to their sample's range (cursor: the range starts, advanced as they fill) */
 template <class KT>
 __global__ void __launch_bounds__(TPB) k_group_ranked(const uint32_t *samp, uint64_t n, unsigned long long *cursor,
                                                        const uint64_t *K, const uint64_t *rep, const int32_t *dist,
                                                        uint64_t *K2, uint64_t *rep2, int32_t *dist2) {
   constexpr int KWD = KOps<KT>::WORDS;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const unsigned long long o = atomicAdd(&cursor[samp[i]], 1ull);
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    const bool valid = i < n;
+    const unsigned long long o = group_place(valid ? samp[i] : 0u, valid, cursor);
+    if (!valid) continue;
     KOps<KT>::store(K2 + o * KWD, KOps<KT>::load(K + i * KWD));
     KOps<KT>::store(rep2 + o * KWD, KOps<KT>::load(rep + i * KWD));
     dist2[o] = dist[i];
@@ -1224,8 +1240,11 @@ __global__ void __launch_bounds__(TPB) k_group_heads(const uint32_t *samp, uint6
                                                       uint32_t *heads2, uint64_t *len2, uint64_t *rep2,
                                                       uint32_t *head_of) {
   constexpr int KWD = KOps<KT>::WORDS;
-  for (uint64_t h = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (uint64_t)gridDim.x * blockDim.x) {
-    const unsigned long long o = atomicAdd(&cursor[samp[h]], 1ull);
+  for (uint64_t h0 = (uint64_t)blockIdx.x * blockDim.x; h0 < nh; h0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t h = h0 + threadIdx.x;
+    const bool valid = h < nh;
+    const unsigned long long o = group_place(valid ? samp[h] : 0u, valid, cursor);
+    if (!valid) continue;
     heads2[o] = heads[h];
     len2[o] = len[h];
     KOps<KT>::store(rep2 + o * KWD, KOps<KT>::load(rep + h * KWD));

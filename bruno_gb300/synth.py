@@ -58,6 +58,10 @@ WORKLOADS = {
     # the plain-scale mix at a fifth of the genome (profiling case: 10 Mbp, 2M x 150 bp, k=31, -L 3)
     "plain-medium": Workload("plain-medium", 10_000_000, 150, 2_000_000, 0.005, 31, (3,), 0.02, (1000, 10000),
                              (2, 8), (0.01, 0.01), 5),
+    # the plain-scale mix at a twelfth of the genome, sized for full ncu captures (a few GB on the
+    # device, inputs still larger than L2): 4 Mbp + 2% repeats, 800k x 150 bp, k=31, -L 3
+    "plain-profile": Workload("plain-profile", 4_000_000, 150, 800_000, 0.005, 31, (3,), 0.02, (1000, 10000),
+                              (2, 8), (0.01, 0.01), 6),
     # 200 Mbp + 5% repeats (1-20 kbp, 2-16 copies, 1-3% divergence), 30x 150 bp, k=63, -L 3
     "large-k": Workload("large-k", 200_000_000, 150, 40_000_000, 0.005, 63, (3,), 0.05, (1000, 20000), (2, 16),
                         (0.01, 0.03)),

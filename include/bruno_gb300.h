@@ -360,6 +360,10 @@ bruno_status bruno_build_samples(bruno_ctx *ctx, const char *const *bufs, const 
                                  int32_t is_device);
 /* Samples of the last batch (0 if none was built). */
 bruno_status bruno_sample_count(bruno_ctx *ctx, size_t *n_samples);
+/* Where each sample's results start in what bruno_copy_ranked / bruno_copy_chains return for the
+ * whole batch (each array n_samples + 1 long, may be NULL): listranked nodes, chains, and chain
+ * characters, so that one copy of everything serves every sample. */
+bruno_status bruno_sample_ranges(bruno_ctx *ctx, uint64_t *ranked0, uint64_t *chains0, uint64_t *chars0);
 /* One sample's sizes, as bruno_get_sizes gives them for a plain build of the sample alone
  * (n_filtered and filter_flag_hist are not kept per sample and read 0). */
 bruno_status bruno_sample_sizes(bruno_ctx *ctx, size_t sample, bruno_sizes *out);

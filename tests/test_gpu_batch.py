@@ -35,6 +35,9 @@ def batch(samples, **cfg):
         out = [dict(sizes=g.sample_sizes(i), nodes=sort_nodes(*g.sample_nodes(i)),
                     ranked=sort_ranked(*g.sample_ranked(i)), chains=chain_set(*g.sample_chains(i)))
                for i in range(len(samples))]
+        # one copy of the whole batch's chains, sliced by bruno_sample_ranges, gives the same
+        for i, ch in enumerate(g.batch_chains()):
+            assert chain_set(*ch) == out[i]["chains"], i
         total = g.sizes()
         return out, total
     finally:

@@ -327,3 +327,15 @@ def test_edge_filter_workload_parity():
 def test_edge_filter_rejects_large_k():
     with pytest.raises(bg.BrunoError):
         bg.Graph(k=33, thresh=bg.thresholds([2]), edge_filter=True)
+
+
+def test_large_k_workload_parity():
+    """the large-k mix (5% repeats of 1-20 kbp in 2-16 copies at 1-3% divergence, 30x 150 bp,
+    0.5% substitutions, k = 63, -L 3) at a hundredth of its genome: 128-bit keys through the
+    whole-table count, every output against the oracle"""
+    w = synth.Workload("large-k-small", 2_000_000, 150, 400_000, 0.005, 63, (3,), 0.05, (1000, 20000), (2, 16),
+                       (0.01, 0.03), 9)
+    fq = synth.make_fastq(w)
+    thr = bg.thresholds(w.lower)
+    ref = oracle.run(fq, k=63, thresh=thr, min_update=True, threads=16, keep_k2=True, keep_filtered=True)
+    compare(gpu_run(fq, 63, True, thr, True, max_load=0.7), ref)
