@@ -49,7 +49,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--samples", type=int, default=None,
                     help="batched / served: number of distinct samples (256 / 48)")
-    ap.add_argument("--workers", type=int, default=8, help="served: pool workers")
+    ap.add_argument("--tune", type=int, default=1, choices=[0, 1],
+                    help="batched: 1 = autotune the table shape on a probe quarter, 0 = the library's defaults")
     ap.add_argument("--rates", type=float, nargs="+", default=[10, 50, 100, 200, 500], help="served: requests/s")
     ap.add_argument("--requests", type=int, default=200, help="served: most requests per rate")
     ap.add_argument("--seconds", type=float, default=4.0, help="served: target seconds per rate")
@@ -249,7 +250,7 @@ def run_batched(args):
     _plain_loop(bg, cfg, bufs[:8], sizes[:8])                 # warm-up
     plain_s, plain = _plain_loop(bg, cfg, bufs, sizes)
     probe = views[::4]
-    best, tune = autotune.tune_batch(cfg, probe)
+    best, tune = autotune.tune_batch(cfg, probe) if args.tune else (cfg, {})
     g = bg.Graph(best)
     g.build_samples(probe)                                    # warm-up of the chosen shape
     passes = []

@@ -1242,6 +1242,7 @@ struct FilterArgs {
   const BigRes *big; uint64_t n_big;   /* entries counted past 2^24, for exact filtered counts */
   const SGeom *sg; uint32_t S;         /* a batch of S samples (S = 1: the plain build) */
   unsigned long long *s_tally;         /* per-sample tallies (batch only) */
+  const uint32_t *cand; uint64_t n_cand; /* the slots the count listed (NULL: every slot) */
   DevCounters *ctr;
 };
 
@@ -1663,12 +1664,23 @@ __device__ __forceinline__ bool sm_count(uint64_t *sm, uint32_t sm_base, uint32_
   return false;
 }
 
+/* The counting kernel's share of the filter, for thresholded builds: a k-mer that the filter's
+ * quick rule drops (its total below the (k+1)-mer lower bound: every entry gets flags 1 and 2 and
+ * the slot keeps its bare key; filter_quick) is tallied here and left as it is; every other
+ * k-mer's first slot is listed, and the filter then reads only the listed slots. */
+struct CandArgs {
+  uint32_t *cand;                      /* NULL: no listing */
+  uint64_t cap;
+  unsigned long long *n_cand, *quick_hist;
+  uint64_t t[6];
+};
+
 /* One CTA per partition (blockIdx.x counts the partitions of all samples): clear the slots, count
  * the partition's records into them, write the region back.  Partition j of sample s holds the
  * records whose mix has j in its top pbits bits: the bucket (top 8) and the split bits. */
 __global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, const unsigned long long *rec_cnt,
                                                        const SGeom *sg, uint32_t nsamples, const uint32_t *plist,
-                                                       uint64_t *table, unsigned long long *s_tally,
+                                                       uint64_t *table, unsigned long long *s_tally, CandArgs ca,
                                                        DevCounters *ctr) {
   extern __shared__ __align__(16) uint64_t sm[];
   /* plist: the partitions of one launch (a batch launches its partitions by region size, each
@@ -1702,6 +1714,68 @@ __global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, cons
   ulonglong2 *dst = reinterpret_cast<ulonglong2 *>(table + (G.g.base + j * G.g.region) * 4);
   const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(sm);
   for (uint32_t v = tid; v < region * 2u; v += nt) dst[v] = src[v];
+  if (ca.cand) {
+    /* the region is written back: each slot's key word now holds its place in the block's list
+     * (~0: not listed), so the listing needs no shared memory of its own */
+    __shared__ unsigned int s_nc, s_qh[16];
+    __shared__ unsigned long long s_base;
+    if (tid < 16) s_qh[tid] = 0;
+    if (tid == 0) s_nc = 0;
+    __syncthreads();
+    const uint32_t cmax32 = 0xFFFFu;
+    FlagHist fh;   /* at most 12 slots of 6 entries a thread: the 16-bit bins cannot wrap */
+    fh.clear();
+    const int lane = tid & 31;
+    for (uint32_t q0 = 0; q0 < region; q0 += nt) {
+      const uint32_t q = q0 + tid;
+      bool listed = false;
+      if (q < region) {
+        const uint64_t key = sm[q * 4];
+        if (key != KEY_EMPTY && !(key & KEY_CONT)) {   /* a continuation belongs to its first slot */
+          uint32_t w[6];
+          int ne = 0;
+          uint32_t kf = 0;
+          #pragma unroll
+          for (int e = 0; e < 6; ++e) {
+            w[e] = (uint32_t)(sm[q * 4 + 1 + e / 2] >> (32 * (e & 1)));
+            ne += w[e] != 0;
+            kf += entry_count(w[e]);
+          }
+          kf = min(cmax32, kf);
+          if (ne == 6 || kf >= ca.t[2]) {
+            listed = true;
+          } else {
+            const unsigned fk = 3u | ((kf < ca.t[0] || kf >= ca.t[1]) ? 8u : 0u);
+            #pragma unroll
+            for (int e = 0; e < 6; ++e) {
+              if (!w[e]) continue;
+              const uint32_t c16 = min(cmax32, entry_count(w[e]));
+              fh.add(fk | ((c16 < ca.t[4] || c16 >= ca.t[5]) ? 4u : 0u));
+            }
+          }
+        }
+      }
+      const unsigned m = __ballot_sync(~0u, listed);   /* the loop bound is the same for every lane */
+      unsigned base = 0;
+      if (m && lane == __ffs(m) - 1) base = atomicAdd(&s_nc, (unsigned)__popc(m));
+      if (m) base = __shfl_sync(~0u, base, __ffs(m) - 1);
+      if (q < region) sm[q * 4] = listed ? (uint64_t)(base + __popc(m & ((1u << lane) - 1))) : ~0ull;
+    }
+    #pragma unroll
+    for (int f = 0; f < 16; ++f) {
+      const unsigned long long h = warp_sum(fh.get(f));
+      if (lane == 0 && h) atomicAdd(&s_qh[f], (unsigned)h);
+    }
+    __syncthreads();
+    if (tid == 0) s_base = s_nc ? atomicAdd(ca.n_cand, (unsigned long long)s_nc) : 0;
+    if (tid < 16 && s_qh[tid]) atomicAdd(&ca.quick_hist[tid], (unsigned long long)s_qh[tid]);
+    __syncthreads();
+    const uint64_t slot0 = G.g.base + j * G.g.region;
+    for (uint32_t q = tid; q < region; q += nt) {
+      const uint64_t o = sm[q * 4];
+      if (o != ~0ull && s_base + o < ca.cap) ca.cand[s_base + o] = (uint32_t)(slot0 + q);
+    }
+  }
   slots = warp_sum(slots); entries = warp_sum(entries);
   if ((tid & 31) == 0) {   /* reductions without a returned value: nothing waits on them */
     if (slots) atomicAdd(&ctr->n_slots_claimed, slots);
@@ -1770,13 +1844,14 @@ __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
   if (tid == 0) s_nodes = 0;
   FilterTally t;
   t.hist.clear();
-  for (uint64_t c0 = (uint64_t)blockIdx.x * FCHUNK; c0 < a.nslots; c0 += (uint64_t)gridDim.x * FCHUNK) {
+  const uint64_t limit = a.cand ? a.n_cand : a.nslots;   /* chunks of listed slots, or of slots */
+  for (uint64_t c0 = (uint64_t)blockIdx.x * FCHUNK; c0 < limit; c0 += (uint64_t)gridDim.x * FCHUNK) {
     if (tid == 0) { s_nc = 0; s_nb = 0; s_ncand = 0; }
     /* a batch: the chunk's slots belong to sample s0 up to `bound` and to s0 + 1 after it (a
      * sample has at least 256 partitions of 64 slots, more than a chunk) */
     uint32_t s0 = 0;
     uint64_t bound = ~0ull;
-    if (a.S > 1) {
+    if (a.S > 1 && !a.cand) {
       s0 = sample_of_slot(a.sg, a.S, c0);
       if (s0 + 1 < a.S) bound = a.sg[s0 + 1].g.base;
     }
@@ -1787,9 +1862,14 @@ __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
         if (t.hist.get(f)) atomicAdd(&s_hist[f], t.hist.get(f));
       t.hist.clear();
     }
-    /* pass 1 */
+    /* pass 1 (listed slots all go to pass 2) */
+    if (a.cand) {
+      const uint32_t nchunk = (uint32_t)min((uint64_t)FCHUNK, limit - c0);
+      for (uint32_t x = tid; x < nchunk; x += TPB) s_cand[x] = (uint16_t)x;
+      if (tid == 0) s_ncand = nchunk;
+    }
     #pragma unroll 2
-    for (int r = 0; r < FCHUNK / TPB; ++r) {
+    for (int r = 0; r < (a.cand ? 0 : FCHUNK / TPB); ++r) {
       const uint32_t off = (uint32_t)(r * TPB + tid);
       const uint64_t i = c0 + off;
       bool full_pass = false;
@@ -1822,7 +1902,7 @@ __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
     /* pass 2 */
     const unsigned ncand = s_ncand;
     for (unsigned x = tid; x < ncand; x += TPB) {
-      const uint64_t i = c0 + s_cand[x];
+      const uint64_t i = a.cand ? (uint64_t)a.cand[c0 + s_cand[x]] : c0 + s_cand[x];
       uint64_t *s = a.table + i * SU;
       uint64_t raw[SU];
       ld_slot<SU>(s, raw);
@@ -1835,7 +1915,7 @@ __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
         ne += w[q] != 0;
       }
       t.kind = 0;
-      t.sample = i < bound ? s0 : s0 + 1;
+      t.sample = a.cand && a.S > 1 ? sample_of_slot(a.sg, a.S, i) : (i < bound ? s0 : s0 + 1);
       if (ne < NE) filter_kmer<KT, NE, false>(s, i, key, w, ne, a, t);
       else filter_wide_global<KT>(s, i, key, w, a, t);   /* continuation slots */
       if (t.kind == 1) s_chain[atomicAdd(&s_nc, 1u)] = (uint32_t)i;
@@ -1858,7 +1938,20 @@ __global__ void __launch_bounds__(TPB) k_filter(FilterArgs a) {
     }
     for (unsigned x = tid; x < s_nb; x += TPB)
       if (s_base_b + x < a.list_cap) a.branch_list[s_base_b + x] = s_branch[x];
-    if (a.s_tally) {   /* per-sample node tallies: the chunk's nodes past `bound` are s0 + 1's */
+    if (a.s_tally && a.cand) {   /* per-sample node tallies of listed slots: each node's own sample */
+      for (int list = 0; list < 2; ++list) {
+        const unsigned cnt = list ? s_nb : s_nc;
+        const uint32_t *sl = list ? s_branch : s_chain;
+        for (unsigned x0 = 0; x0 < cnt; x0 += TPB) {   /* the same bound for every thread */
+          const unsigned x = x0 + tid;
+          const uint32_t smp = x < cnt ? sample_of_slot(a.sg, a.S, sl[x]) : ~0u;
+          const unsigned peers = __match_any_sync(~0u, smp);
+          if (x < cnt && lane == __ffs(peers) - 1)
+            atomicAdd(&a.s_tally[(uint64_t)smp * T_NUM + (list ? T_BRANCH : T_CHAIN)],
+                      (unsigned long long)__popc(peers));
+        }
+      }
+    } else if (a.s_tally) {   /* per-sample node tallies: the chunk's nodes past `bound` are s0 + 1's */
       unsigned hc = 0, hb = 0;
       for (unsigned x = tid; x < s_nc; x += TPB) hc += s_chain[x] >= bound;
       for (unsigned x = tid; x < s_nb; x += TPB) hb += s_branch[x] >= bound;
@@ -2215,9 +2308,21 @@ bruno_status split_and_count(Ctx *c, std::vector<SGeom> &sg, const std::vector<u
     recs = (const uint64_t *)c->records2.p;
     cnts = (const unsigned long long *)c->sub_cnt.p;
   }
+  /* thresholded builds: the count lists the slots the filter must read (at most one per slot) */
+  CandArgs ca{};
+  const uint64_t nslots_all = sg.back().g.base + sg.back().g.nslots;
+  if (c->cfg.thresholding && !c->cfg.edge_filter && nslots_all < (1ull << 32)) {
+    if ((st = ensure(c, c->cand, nslots_all * 4)) != BRUNO_OK) return st;
+    ca.cand = (uint32_t *)c->cand.p;
+    ca.cap = nslots_all;
+    ca.n_cand = &c->dctr->n_cand;
+    ca.quick_hist = c->dctr->quick_hist;
+    for (int i = 0; i < 6; ++i) ca.t[i] = c->cfg.thresh[i];
+    cudaMemsetAsync(&c->dctr->n_cand, 0, sizeof(c->dctr->n_cand) + sizeof(c->dctr->quick_hist), c->stream);
+  }
   if (S == 1) {
     k_count_local<<<(unsigned)nparts, count_threads(c), (unsigned)(region_max * 32), c->stream>>>(
-        recs, cnts, (const SGeom *)c->sgeom.p, S, nullptr, (uint64_t *)c->table.p, s_tally, c->dctr);
+        recs, cnts, (const SGeom *)c->sgeom.p, S, nullptr, (uint64_t *)c->table.p, s_tally, ca, c->dctr);
     c->launches += 1;
   } else {
     /* partitions grouped by region size: a launch per group, with shared memory for its largest */
@@ -2245,13 +2350,21 @@ bruno_status split_and_count(Ctx *c, std::vector<SGeom> &sg, const std::vector<u
       if (!n) continue;
       k_count_local<<<(unsigned)n, count_threads(c), (unsigned)(rmax[cl] * 32), c->stream>>>(
           recs, cnts, (const SGeom *)c->sgeom.p, S, (const uint32_t *)c->grp_tmp.p + at[cl], (uint64_t *)c->table.p,
-          s_tally, c->dctr);
+          s_tally, ca, c->dctr);
       c->launches += 1;
     }
   }
   if ((st = cuda_check(c, cudaGetLastError(), "k_count_local")) != BRUNO_OK) return st;
+  c->have_cand = ca.cand != nullptr;   /* valid once the caller sees no overflow */
   ok = true;
   return BRUNO_OK;
+}
+
+/* after a counting pass without overflow: the listed slots and the quick drops' tallies */
+void take_candidates(Ctx *c) {
+  if (!c->have_cand) return;
+  c->n_cand = c->hctr->n_cand;
+  for (int f = 0; f < 16; ++f) c->quick_hist[f] = c->hctr->quick_hist[f];
 }
 
 /* blocks of one extraction launch over nr reads (at most 2 per SM, at least one item of WX_ITEM
@@ -2395,6 +2508,8 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
       }
       c->n_entries = c->hctr->n_entries;
       c->n_slots_claimed = c->hctr->n_slots_claimed;
+      if (counted_local) take_candidates(c);
+      else c->have_cand = false;
       used = true;
       return BRUNO_OK;
     }
@@ -2452,12 +2567,14 @@ bruno_status count_paths(Ctx *c) {
     bruno_status st = count_partitioned(c, used);
     if (st != BRUNO_OK || used) return st;
   }
+  c->have_cand = false;   /* whatever a partitioned attempt listed is stale */
   return count_direct<KT>(c);
 }
 
 /* counting, then the entries counted past 2^24 (if any) resolved for the filter */
 template <class KT>
 bruno_status count_typed(Ctx *c) {
+  c->have_cand = false;
   bruno_status st = count_paths<KT>(c);
   if (st != BRUNO_OK) return st;
   c->n_big = c->hctr->n_big;
@@ -2521,14 +2638,24 @@ bruno_status filter_typed(Ctx *c, const uint64_t *thr) {
     a.f_keys = (uint64_t *)c->f_keys.p; a.f_edges = (uint8_t *)c->f_edges.p; a.f_counts = (uint32_t *)c->f_counts.p;
     a.f_cap = n;
   }
+  /* the count listed the slots that need the full filter (same thresholds): read only those,
+   * and add the quick drops the count tallied */
+  const bool use_cand = c->have_cand && a.thresholding && std::equal(thr, thr + 6, c->cfg.thresh);
+  if (use_cand) {
+    a.cand = (const uint32_t *)c->cand.p;
+    a.n_cand = c->n_cand;
+  }
   cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
-  k_filter<KT><<<num_sms() * 8, TPB, 0, c->stream>>>(a);
+  const uint64_t chunks = ((use_cand ? c->n_cand : c->nslots) + FCHUNK - 1) / FCHUNK;
+  k_filter<KT><<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)num_sms() * 8, chunks)), TPB, 0,
+                 c->stream>>>(a);
   c->launches += 1;
+  c->have_cand = false;   /* the listed slots are nodes or tombstones now */
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   const DevCounters &h = *c->hctr;
   c->n_nodes = h.n_nodes; c->n_branch = h.n_branch; c->n_chain = h.n_chain;
   c->n_filtered = std::min<uint64_t>(h.n_filtered, a.f_cap);
-  for (int f = 0; f < 16; ++f) c->flag_hist[f] = h.flag_hist[f];
+  for (int f = 0; f < 16; ++f) c->flag_hist[f] = h.flag_hist[f] + (use_cand ? c->quick_hist[f] : 0);
   return BRUNO_OK;
 }
 }  // namespace
@@ -2553,6 +2680,7 @@ __global__ void k_sample_first_read(const uint64_t *rstart, uint64_t nreads, con
  * plain build is a batch of one).  Needs k <= 31 and the shared-memory partitions. */
 bruno_status run_count_samples(Ctx *c) {
   bruno_status st;
+  c->have_cand = false;
   const uint32_t S = c->S;
   const int sms = num_sms();
   if ((st = run_index_reads(c)) != BRUNO_OK) return st;
@@ -2679,6 +2807,7 @@ bruno_status run_count_samples(Ctx *c) {
       c->n_entries = c->hctr->n_entries;
       c->n_slots_claimed = c->hctr->n_slots_claimed;
       c->n_big = 0;
+      take_candidates(c);
       float ms[3] = {0, 0, 0};
       cudaEventElapsedTime(&ms[0], c->kev[0], c->kev[1]);
       cudaEventElapsedTime(&ms[1], c->kev[2], c->kev[4]);

@@ -40,6 +40,8 @@ struct DevCounters {
    * nodes and live branch nodes after an erasure pass */
   unsigned long long cl_term, cl_nonzero, cl_sum, cl_norm, cl_q, cl_found, cl_dead, cl_bub, cl_live, cl_live_branch;
   unsigned long long n_big, n_big_res; /* entries counted past 2^24 (keys in big_key), resolved */
+  unsigned long long n_cand;           /* slots the count listed for the filter */
+  unsigned long long quick_hist[16];   /* the filter flags of the entries the count dropped */
   unsigned int hll[1 << 12];           /* HyperLogLog registers, p = 12 */
   /* exact counts of (k-mer, biedge) entries past 2^24 occurrences: an entry word's count stops
    * there and sets E_BIG, and every later occurrence adds 1 here, under the entry word's
@@ -149,6 +151,11 @@ struct Ctx {
   Buf chain_list, branch_list;   /* slot indices, filled by the filter */
   Buf bigres;                    /* BigRes per entry counted past 2^24 (n_big of them) */
   uint64_t n_big = 0;
+  /* thresholded counts in shared memory list the first slots of the k-mers the filter's quick
+   * rule cannot drop, and tally the flags of those it drops; the filter then reads the list */
+  Buf cand;
+  bool have_cand = false;
+  uint64_t n_cand = 0, quick_hist[16] = {0};
   Buf k1tab;                     /* the (k+1)-mer edge filter's (key, count) table */
   uint64_t k1slots = 0;
 

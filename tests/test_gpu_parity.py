@@ -329,7 +329,7 @@ def test_edge_filter_rejects_large_k():
         bg.Graph(k=33, thresh=bg.thresholds([2]), edge_filter=True)
 
 
-def test_large_k_workload_parity():
+def test_large_k_mix_parity():
     """the large-k mix (5% repeats of 1-20 kbp in 2-16 copies at 1-3% divergence, 30x 150 bp,
     0.5% substitutions, k = 63, -L 3) at a hundredth of its genome: 128-bit keys through the
     whole-table count, every output against the oracle"""
