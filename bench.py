@@ -262,6 +262,7 @@ def run_batched(args):
         res = [{"status": 0, "sizes": g.sample_sizes(i), "chains": chains[i]} for i in range(len(views))]
         passes.append((time.perf_counter() - t0, t1 - t0))
     phases = g.phase_ms()
+    tot = g.sizes()
     g.close()
     dt = statistics.median(p[0] for p in passes)
     exact = all(_same_as_plain(r, p) for r, p in zip(res, plain))
@@ -274,6 +275,8 @@ def run_batched(args):
             "plain_loop_graphs_per_s": len(fqs) / plain_s, "speedup_vs_plain_loop": plain_s / dt,
             "pass_ms": {"with_copy_out": 1e3 * dt, "build_only": 1e3 * statistics.median(p[1] for p in passes)},
             "phase_ms": phases,
+            "sizes": {k: tot[k] for k in ("n_reads", "n_instances", "n_k2", "n_nodes", "n_chain_nodes", "n_chains",
+                                          "n_ranked", "table_slots", "table_partitions")},
             "autotuned": {"max_load": best.max_load, "part_slots": best.part_slots, "count_threads": best.count_threads},
             "autotune_graphs_per_s": tune,
             "latency_ms": {"p50": 1e3 * dt, "p99": 1e3 * dt,

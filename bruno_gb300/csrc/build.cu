@@ -1714,17 +1714,26 @@ __global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, cons
   ulonglong2 *dst = reinterpret_cast<ulonglong2 *>(table + (G.g.base + j * G.g.region) * 4);
   const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(sm);
   for (uint32_t v = tid; v < region * 2u; v += nt) dst[v] = src[v];
+  slots = warp_sum(slots); entries = warp_sum(entries);
+  if ((tid & 31) == 0) {   /* reductions without a returned value: nothing waits on them */
+    if (slots) atomicAdd(&ctr->n_slots_claimed, slots);
+    if (entries) {
+      atomicAdd(&ctr->n_entries, entries);
+      if (s_tally) atomicAdd(&s_tally[(uint64_t)smp * T_NUM + T_ENTRIES], entries);
+    }
+  }
   if (ca.cand) {
     /* the region is written back: each slot's key word now holds its place in the block's list
      * (~0: not listed), so the listing needs no shared memory of its own */
-    __shared__ unsigned int s_nc, s_qh[16];
+    __shared__ unsigned int s_nc, s_qh[4];
     __shared__ unsigned long long s_base;
-    if (tid < 16) s_qh[tid] = 0;
+    if (tid < 4) s_qh[tid] = 0;
     if (tid == 0) s_nc = 0;
     __syncthreads();
-    const uint32_t cmax32 = 0xFFFFu;
-    FlagHist fh;   /* at most 12 slots of 6 entries a thread: the 16-bit bins cannot wrap */
-    fh.clear();
+    /* a quick drop's entries get flags 3 | 8 (k-mer total outside the k bounds) | 4 (entry count
+     * outside the k+2 bounds): four possible values, tallied as 16-bit fields of one word (at
+     * most 12 slots of 6 entries a thread, so no field can wrap) */
+    uint64_t qh = 0;
     const int lane = tid & 31;
     for (uint32_t q0 = 0; q0 < region; q0 += nt) {
       const uint32_t q = q0 + tid;
@@ -1732,25 +1741,23 @@ __global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, cons
       if (q < region) {
         const uint64_t key = sm[q * 4];
         if (key != KEY_EMPTY && !(key & KEY_CONT)) {   /* a continuation belongs to its first slot */
-          uint32_t w[6];
           int ne = 0;
           uint32_t kf = 0;
           #pragma unroll
           for (int e = 0; e < 6; ++e) {
-            w[e] = (uint32_t)(sm[q * 4 + 1 + e / 2] >> (32 * (e & 1)));
-            ne += w[e] != 0;
-            kf += entry_count(w[e]);
+            const uint32_t w = (uint32_t)(sm[q * 4 + 1 + e / 2] >> (32 * (e & 1)));
+            ne += w != 0;
+            kf += entry_count(w);
           }
-          kf = min(cmax32, kf);
-          if (ne == 6 || kf >= ca.t[2]) {
-            listed = true;
-          } else {
-            const unsigned fk = 3u | ((kf < ca.t[0] || kf >= ca.t[1]) ? 8u : 0u);
+          kf = min(0xFFFFu, kf);
+          listed = ne == 6 || kf >= ca.t[2];
+          if (!listed) {
+            const uint32_t kout = (kf < ca.t[0] || kf >= ca.t[1]) ? 2u : 0u;
             #pragma unroll
             for (int e = 0; e < 6; ++e) {
-              if (!w[e]) continue;
-              const uint32_t c16 = min(cmax32, entry_count(w[e]));
-              fh.add(fk | ((c16 < ca.t[4] || c16 >= ca.t[5]) ? 4u : 0u));
+              const uint32_t w = (uint32_t)(sm[q * 4 + 1 + e / 2] >> (32 * (e & 1)));
+              const uint32_t c16 = min(0xFFFFu, entry_count(w));
+              if (w) qh += 1ull << (16 * (kout | ((c16 < ca.t[4] || c16 >= ca.t[5]) ? 1u : 0u)));
             }
           }
         }
@@ -1762,26 +1769,18 @@ __global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, cons
       if (q < region) sm[q * 4] = listed ? (uint64_t)(base + __popc(m & ((1u << lane) - 1))) : ~0ull;
     }
     #pragma unroll
-    for (int f = 0; f < 16; ++f) {
-      const unsigned long long h = warp_sum(fh.get(f));
+    for (int f = 0; f < 4; ++f) {
+      const unsigned long long h = warp_sum((qh >> (16 * f)) & 0xFFFFull);
       if (lane == 0 && h) atomicAdd(&s_qh[f], (unsigned)h);
     }
     __syncthreads();
     if (tid == 0) s_base = s_nc ? atomicAdd(ca.n_cand, (unsigned long long)s_nc) : 0;
-    if (tid < 16 && s_qh[tid]) atomicAdd(&ca.quick_hist[tid], (unsigned long long)s_qh[tid]);
+    if (tid < 4 && s_qh[tid]) atomicAdd(&ca.quick_hist[3 + 4 * tid], (unsigned long long)s_qh[tid]);
     __syncthreads();
     const uint64_t slot0 = G.g.base + j * G.g.region;
     for (uint32_t q = tid; q < region; q += nt) {
       const uint64_t o = sm[q * 4];
       if (o != ~0ull && s_base + o < ca.cap) ca.cand[s_base + o] = (uint32_t)(slot0 + q);
-    }
-  }
-  slots = warp_sum(slots); entries = warp_sum(entries);
-  if ((tid & 31) == 0) {   /* reductions without a returned value: nothing waits on them */
-    if (slots) atomicAdd(&ctr->n_slots_claimed, slots);
-    if (entries) {
-      atomicAdd(&ctr->n_entries, entries);
-      if (s_tally) atomicAdd(&s_tally[(uint64_t)smp * T_NUM + T_ENTRIES], entries);
     }
   }
   if (full) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
@@ -2039,10 +2038,104 @@ bruno_status count_typed(Ctx *c);
 template <class KT>
 bruno_status filter_typed(Ctx *c, const uint64_t *thr);
 
+/* The multi-block scan: block b owns elements [b * chunk, (b + 1) * chunk).  Pass 1 sums each
+ * block's elements, the single-block scan turns the sums into block offsets, pass 2 scans each
+ * block's elements from its offset.  Every access is a coalesced run: a thread takes SCAN_V
+ * consecutive elements of a tile of SCAN_TPB * SCAN_V. */
+constexpr int SCAN_TPB = 1024, SCAN_V = 4;
+constexpr uint64_t SCAN_TILE = (uint64_t)SCAN_TPB * SCAN_V;
+
+__device__ __forceinline__ uint64_t block_sum_u64(uint64_t v, uint64_t *warp_part) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) warp_part[wid] = v;
+  __syncthreads();
+  uint64_t t = lane < (int)(blockDim.x >> 5) ? warp_part[lane] : 0;
+  t = warp_sum(t);
+  __syncthreads();   /* warp_part is reused by the caller's next call */
+  return t;
+}
+
+__global__ void __launch_bounds__(SCAN_TPB) k_scan_reduce(const uint64_t *in, uint64_t n, uint64_t chunk,
+                                                           uint64_t *block_sum) {
+  __shared__ uint64_t wp[32];
+  const uint64_t b0 = (uint64_t)blockIdx.x * chunk, b1 = min(n, b0 + chunk);
+  uint64_t s = 0;
+  for (uint64_t i = b0 + threadIdx.x; i < b1; i += SCAN_TPB) s += in[i];
+  s = block_sum_u64(s, wp);
+  if (threadIdx.x == 0) block_sum[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(SCAN_TPB) k_scan_apply(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t chunk,
+                                                          const uint64_t *block_off) {
+  __shared__ uint64_t wp[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint64_t b0 = (uint64_t)blockIdx.x * chunk, b1 = min(n, b0 + chunk);
+  uint64_t carry = block_off[blockIdx.x];
+  for (uint64_t t0 = b0; t0 < b1; t0 += SCAN_TILE) {
+    const uint64_t i0 = t0 + (uint64_t)threadIdx.x * SCAN_V;
+    uint64_t v[SCAN_V], sum = 0;
+    #pragma unroll
+    for (int q = 0; q < SCAN_V; ++q) {
+      v[q] = i0 + q < b1 ? in[i0 + q] : 0;
+      sum += v[q];
+    }
+    /* exclusive scan of the threads' sums: warp shuffles, then the warps' totals */
+    uint64_t inc = sum;
+    #pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t y = __shfl_up_sync(~0u, inc, o);
+      if (lane >= o) inc += y;
+    }
+    if (lane == 31) wp[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+      uint64_t w = lane < (SCAN_TPB >> 5) ? wp[lane] : 0;
+      #pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_up_sync(~0u, w, o);
+        if (lane >= o) w += y;
+      }
+      wp[lane] = w;   /* inclusive totals of warps 0..lane */
+    }
+    __syncthreads();
+    uint64_t run = carry + (wid ? wp[wid - 1] : 0) + inc - sum;
+    const uint64_t tile_total = wp[(SCAN_TPB >> 5) - 1];
+    #pragma unroll
+    for (int q = 0; q < SCAN_V; ++q) {
+      if (i0 + q < b1) out[i0 + q] = run;
+      run += v[q];
+    }
+    carry += tile_total;
+    __syncthreads();   /* wp is rewritten by the next tile */
+  }
+}
+
 }  // namespace
 
-void scan_u64(const uint64_t *in, uint64_t *out, uint64_t n, unsigned long long *total_dev, cudaStream_t s) {
-  k_scan_single<<<1, 1024, 0, s>>>(in, out, n, total_dev);
+int scan_u64(const uint64_t *in, uint64_t *out, uint64_t n, unsigned long long *total_dev, cudaStream_t s,
+             uint64_t *scratch) {
+  const uint64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+  if (tiles <= 2 || !scratch) {
+    k_scan_single<<<1, 1024, 0, s>>>(in, out, n, total_dev);
+    return 1;
+  }
+  /* blocks of a whole number of tiles, at most 1024 of them (the offsets' scan is one block) */
+  const uint64_t nb_max = std::min<uint64_t>(1024, (uint64_t)num_sms() * 2);
+  const uint64_t tiles_per = (tiles + nb_max - 1) / nb_max;
+  const uint64_t chunk = tiles_per * SCAN_TILE;
+  const unsigned nb = (unsigned)((n + chunk - 1) / chunk);
+  k_scan_reduce<<<nb, SCAN_TPB, 0, s>>>(in, n, chunk, scratch);
+  k_scan_single<<<1, 1024, 0, s>>>(scratch, scratch, nb, total_dev);
+  k_scan_apply<<<nb, SCAN_TPB, 0, s>>>(in, out, n, chunk, scratch);
+  return 3;
+}
+
+bruno_status scan_ctx(Ctx *c, const uint64_t *in, uint64_t *out, uint64_t n, unsigned long long *total_dev) {
+  bruno_status st = ensure(c, c->scan_tmp, 1024 * 8);
+  if (st != BRUNO_OK) return st;
+  c->launches += scan_u64(in, out, n, total_dev, c->stream, (uint64_t *)c->scan_tmp.p);
+  return BRUNO_OK;
 }
 
 /* ------------------------------------------------------------ read index */
@@ -2089,11 +2182,13 @@ bruno_status run_index_reads(Ctx *c) {
     unsigned long long nb = ~0ull;
     cudaMemcpyAsync(&c->dctr->last_nonws, &neg, sizeof(neg), cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(&c->dctr->bad_line, &nb, sizeof(nb), cudaMemcpyHostToDevice, c->stream);
-    c->launches += 3;
+    c->launches += 2;   /* k_tile_stats, k_index_lines; the scan counts its own */
     const bool aligned = ((uintptr_t)sg.ptr & 15) == 0;
     k_tile_stats<<<(unsigned)tiles, TPB, 0, c->stream>>>((const unsigned char *)sg.ptr, sg.n, (uint64_t *)c->tile_cnt.p,
                                                           c->dctr, aligned);
-    scan_u64((const uint64_t *)c->tile_cnt.p, (uint64_t *)c->tile_base.p, tiles, &c->dctr->n_records, c->stream);
+    if ((st = scan_ctx(c, (const uint64_t *)c->tile_cnt.p, (uint64_t *)c->tile_base.p, tiles, &c->dctr->n_records)) !=
+        BRUNO_OK)
+      return st;
     if ((st = sync_counters(c)) != BRUNO_OK) return st;
     /* n_records temporarily holds the total newline count: records <= newlines / 4 + 1 */
     uint64_t upper = c->hctr->n_records / 4 + 1;
@@ -2140,6 +2235,13 @@ double hll_sampled_estimate(double sum, unsigned zeros) {
   return est * (double)(1u << HLL_SAMPLE);
 }
 
+/* node and chain lists hold 32-bit slot indices: a table is at most 2^32 - 1 slots (137 GB of
+ * 32-byte slots, 275 GB of 64-byte ones) */
+bruno_status table_room(Ctx *c, uint64_t slots) {
+  if (slots < (1ull << 32)) return BRUNO_OK;
+  return set_err(c, BRUNO_ERR_TABLE_FULL, "k-mer table would need 2^32 slots or more");
+}
+
 uint64_t slots_for(const Ctx *c, double distinct) {
   const double load = c->cfg.max_load > 0 ? c->cfg.max_load : 0.5;
   /* a k-mer with more than one slot's worth of biedges takes continuation slots */
@@ -2167,6 +2269,7 @@ bruno_status count_direct(Ctx *c) {
   }
   for (int attempt = 0; attempt < 4; ++attempt) {
     const size_t bytes = slots * Slot<KT>::U64 * 8;
+    if ((st = table_room(c, slots)) != BRUNO_OK) return st;
     if ((st = ensure(c, c->table, bytes)) != BRUNO_OK) return st;
     c->nslots = slots;
     c->geom = TableGeom{slots, slots, 0};
@@ -2457,6 +2560,7 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
     if (region_c <= part_slots(c) && c->force_direct_count != 2) {
       c->geom = TableGeom{region_c << pb, region_c, pb};
       c->nslots = c->geom.nslots;
+      if ((st = table_room(c, c->nslots)) != BRUNO_OK) return st;
       if ((st = ensure(c, c->table, c->nslots * 32)) != BRUNO_OK) return st;
       cudaEventRecord(c->kev[2], c->stream);
       std::vector<SGeom> sg{SGeom{c->geom, 0, 0, 0}};
@@ -2475,6 +2579,7 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
       const uint64_t region = std::max<uint64_t>(64, (slots + (1ull << pt) - 1) >> pt);
       c->geom = TableGeom{region << pt, region, pt};
       c->nslots = c->geom.nslots;
+      if ((st = table_room(c, c->nslots)) != BRUNO_OK) return st;
       if ((st = ensure(c, c->table, c->nslots * 32)) != BRUNO_OK) return st;
       cudaEventRecord(c->kev[2], c->stream);
       const int G = 1 << (NBUCKET_BITS - pt);
@@ -2792,6 +2897,7 @@ bruno_status run_count_samples(Ctx *c) {
     }
     c->nslots = base;
     c->geom = TableGeom{base, sg[0].g.region, sg[0].g.pbits, 0};
+    if ((st = table_room(c, c->nslots)) != BRUNO_OK) return st;
     if ((st = ensure(c, c->table, c->nslots * 32)) != BRUNO_OK) return st;
     cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
     cudaMemsetAsync(&c->dctr->n_slots_claimed, 0, 16, c->stream);

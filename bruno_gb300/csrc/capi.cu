@@ -35,7 +35,8 @@ bruno_status cuda_check(Ctx *c, cudaError_t e, const char *what) {
 bruno_status ensure(Ctx *c, Buf &b, size_t bytes, bool preserve) {
   if (bytes <= b.bytes && b.p) return BRUNO_OK;
   void *p = nullptr;
-  size_t want = std::max(bytes + bytes / 8, (size_t)256);
+  /* an eighth more, at most 1 GiB more, so that a slightly larger rebuild keeps the buffer */
+  size_t want = std::max(bytes + std::min(bytes / 8, (size_t)1 << 30), (size_t)256);
   cudaError_t e = cudaMallocFromPoolAsync(&p, want, c->pool, c->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -149,7 +150,7 @@ bruno_status bruno_ctx_destroy(bruno_ctx *c) {
                  &c->cstate, &c->cstate2, &c->pend, &c->pay, &c->unf0, &c->unf1, &c->removed, &c->r_K, &c->r_rep, &c->r_dist,
                  &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list, &c->e_ends, &c->e_freqs, &c->s_kmers, &c->s_dist, &c->s_flags, &c->k1tab,
                  &c->cl_trec, &c->cl_tslot, &c->cl_sums, &c->cl_norm, &c->cl_htab, &c->cl_q, &c->cl_found,
-                 &c->records, &c->bucket_cnt, &c->records2, &c->sub_cnt, &c->bigres, &c->cand,
+                 &c->records, &c->bucket_cnt, &c->records2, &c->sub_cnt, &c->bigres, &c->cand, &c->scan_tmp,
                  &c->xsamp, &c->hllreg, &c->hsum, &c->sgeom, &c->s_tally, &c->s_inst, &c->s_used, &c->xitems,
                  &c->split_items, &c->csample, &c->r_samp, &c->h_samp, &c->grp_tmp};
   for (Buf *b : bufs) release(*b);

@@ -1153,8 +1153,8 @@ bruno_status general_emission(Ctx *c, EmitArgs a) {
   uint64_t *hoff = (uint64_t *)bhoff.p;
   cudaMemsetAsync(hoff + G, 0, 8, c->stream);
   k_gen_binlen<<<sms * 2, TPB, 0, c->stream>>>(gmax, G, hoff);
-  scan_u64(hoff, hoff, G + 1, &c->dctr->n_hist, c->stream);
-  c->launches += 2;
+  c->launches += 1;
+  if ((st = scan_ctx(c, hoff, hoff, G + 1, &c->dctr->n_hist)) != BRUNO_OK) { release(); return st; }
   if ((st = sync_counters(c)) != BRUNO_OK) { release(); return st; }
   const uint64_t H = c->hctr->n_hist;
   if ((st = ensure(c, bn, (H + 1) * 8)) != BRUNO_OK || (st = ensure(c, bw, (H + 1) * 8)) != BRUNO_OK ||
@@ -1167,11 +1167,14 @@ bruno_status general_emission(Ctx *c, EmitArgs a) {
   cudaMemsetAsync(woff, 0, (H + 1) * 8, c->stream);
   cudaMemsetAsync(bcur.p, 0, std::max<uint64_t>(1, H) * 4, c->stream);
   k_gen_hist<<<sms * 8, TPB, 0, c->stream>>>(a.removed, dist_of, M, c->cfg.k, gid, hoff, noff, woff);
-  scan_u64(noff, noff, H + 1, nullptr, c->stream);
-  scan_u64(woff, woff, H + 1, &c->dctr->n_chain_chars, c->stream);
+  if ((st = scan_ctx(c, noff, noff, H + 1, nullptr)) != BRUNO_OK ||
+      (st = scan_ctx(c, woff, woff, H + 1, &c->dctr->n_chain_chars)) != BRUNO_OK) {
+    release();
+    return st;
+  }
   k_gen_place<<<sms * 8, TPB, 0, c->stream>>>(a.removed, dist_of, M, gid, hoff, noff, (uint32_t *)bcur.p,
                                               (uint32_t *)bmem.p);
-  c->launches += 4;
+  c->launches += 2;   /* k_gen_hist, k_gen_place */
   if ((st = sync_counters(c)) != BRUNO_OK) { release(); return st; }
   const uint64_t total = c->hctr->n_chain_chars;
   if ((st = ensure(c, c->ch_chars, std::max<uint64_t>(1, total))) != BRUNO_OK) { release(); return st; }
@@ -1358,13 +1361,15 @@ bruno_status compress_typed(Ctx *c) {
   }
   /* offsets: exclusive scan of per-chain lengths, total into n_chain_chars */
   cudaMemsetAsync((uint64_t *)c->head_len.p + nh, 0, 8, c->stream);
-  scan_u64((const uint64_t *)c->head_len.p, (uint64_t *)c->head_off.p, nh + 1, &c->dctr->n_chain_chars, c->stream);
+  if ((st = scan_ctx(c, (const uint64_t *)c->head_len.p, (uint64_t *)c->head_off.p, nh + 1,
+                     &c->dctr->n_chain_chars)) != BRUNO_OK)
+    return st;
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   c->n_chain_chars = c->hctr->n_chain_chars;
   if ((st = ensure(c, c->ch_chars, std::max<uint64_t>(1, c->n_chain_chars))) != BRUNO_OK) return st;
   cudaMemsetAsync(c->ch_chars.p, 0, c->n_chain_chars, c->stream);
   k_fill<KT><<<sms * 8, TPB, 0, c->stream>>>(a, (const uint64_t *)c->head_off.p, (char *)c->ch_chars.p);
-  c->launches += 4;  /* k_ranked, scan, k_fill, k_check_chains */
+  c->launches += 3;  /* k_ranked, k_fill, k_check_chains (the scan counts its own) */
   k_check_chains<<<sms * 4, TPB, 0, c->stream>>>((const char *)c->ch_chars.p, c->n_chain_chars, c->dctr);
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   c->chains_clean = !(c->hctr->err & DERR_UNCLEAN_CHAINS) &&

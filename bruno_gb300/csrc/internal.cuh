@@ -149,6 +149,7 @@ struct Ctx {
   bool h2d_pending = false;      /* ev[7] marks the start of this build's host-to-device copies */
   int force_direct_count = 0;    /* cfg.direct_count: 0 automatic, 1 whole table, 2 L2 partitions */
   Buf chain_list, branch_list;   /* slot indices, filled by the filter */
+  Buf scan_tmp;                  /* block offsets of the multi-block scan */
   Buf bigres;                    /* BigRes per entry counted past 2^24 (n_big of them) */
   uint64_t n_big = 0;
   /* thresholded counts in shared memory list the first slots of the k-mers the filter's quick
@@ -208,8 +209,13 @@ bruno_status ensure(Ctx *c, Buf &b, size_t bytes, bool preserve = false);
 cudaMemPool_t library_pool(int device);
 bruno_status sync_counters(Ctx *c, bool with_hll = false);
 
-/* exclusive scan of n uint64 values (in may equal out); writes the total to *total_dev */
-void scan_u64(const uint64_t *in, uint64_t *out, uint64_t n, unsigned long long *total_dev, cudaStream_t s);
+/* exclusive scan of n uint64 values (in may equal out); writes the total to *total_dev (may be
+ * NULL).  scratch: 1024 device words for the block offsets (NULL: one block does it all).
+ * Returns the number of kernels launched. */
+int scan_u64(const uint64_t *in, uint64_t *out, uint64_t n, unsigned long long *total_dev, cudaStream_t s,
+             uint64_t *scratch);
+/* the same on the context's stream with the context's scratch; counts its launches */
+bruno_status scan_ctx(Ctx *c, const uint64_t *in, uint64_t *out, uint64_t n, unsigned long long *total_dev);
 
 /* -------------------------------------------------------------- phase launchers */
 bruno_status run_index_reads(Ctx *c);        /* FASTQ line structure -> read spans */
