@@ -2139,6 +2139,7 @@ bruno_status scan_ctx(Ctx *c, const uint64_t *in, uint64_t *out, uint64_t n, uns
 }
 
 /* ------------------------------------------------------------ read index */
+bruno_status batch_segment(Ctx *c, size_t si, uint64_t r0, uint64_t r1);
 namespace {
 bruno_status extract_begin(Ctx *c, uint64_t upper, int max_blocks);
 void extract_reads(Ctx *c, uint64_t r0, uint64_t r1);
@@ -2160,7 +2161,8 @@ bruno_status run_index_reads(Ctx *c) {
   if ((st = ensure(c, c->tile_base, std::max<uint64_t>(1, total_tiles) * 8)) != BRUNO_OK) return st;
   bool piped = false;
   for (auto &sg : c->segs) piped |= sg.ev >= 0;
-  c->pre_extracted = piped && c->W == 1 && !c->cfg.edge_filter && c->force_direct_count != 1;
+  c->pre_extracted = piped && c->S == 1 && c->W == 1 && !c->cfg.edge_filter && c->force_direct_count != 1;
+  const bool batch_hook = piped && c->S > 1 && c->batch_piped;   /* a batch extracts group by group */
   cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
   if (c->pre_extracted) {
     /* every record holds its sequence and an equally long quality line, so the k-mer
@@ -2194,7 +2196,7 @@ bruno_status run_index_reads(Ctx *c) {
     uint64_t upper = c->hctr->n_records / 4 + 1;
     /* grow keeping the spans of earlier files; pieces of one input grow once, for all pieces
      * at the first piece's records per byte */
-    if (c->pre_extracted && si == 0 && sg.n > 0)
+    if ((c->pre_extracted || batch_hook) && si == 0 && sg.n > 0)
       upper = std::max<uint64_t>(upper, (uint64_t)((double)upper * (double)total_bytes / (double)sg.n * 1.05) + 1);
     if ((st = ensure(c, c->rstart, (rcap + upper) * 8, true)) != BRUNO_OK) return st;
     if ((st = ensure(c, c->rend, (rcap + upper) * 8, true)) != BRUNO_OK) return st;
@@ -2210,6 +2212,7 @@ bruno_status run_index_reads(Ctx *c) {
       return set_err(c, BRUNO_ERR_BAD_INPUT, "malformed FASTQ in file " + std::to_string(si) + " near line " +
                                                  std::to_string(h.bad_line != ~0ull ? h.bad_line : lines));
     if (c->pre_extracted) extract_reads(c, rcap, rcap + lines / 4);
+    if (batch_hook && (st = batch_segment(c, si, rcap, rcap + lines / 4)) != BRUNO_OK) return st;
     rcap += lines / 4;
   }
   c->n_reads = rcap;
@@ -2783,53 +2786,91 @@ __global__ void k_sample_first_read(const uint64_t *rstart, uint64_t nreads, con
 /* The batched form's count: S samples, concatenated in one device copy, each counted into
  * partitions of its own in one pass of every counting kernel (the plain path's kernels; the
  * plain build is a batch of one).  Needs k <= 31 and the shared-memory partitions. */
+namespace {
+/* The first read of each sample q in [q0, q1), among reads [r0, r1) (every read before r0 lies
+ * before sample q0, every read of these samples before r1); out gets q1 - q0 + 1 values, the
+ * last r1. */
+bruno_status first_reads(Ctx *c, uint32_t q0, uint32_t q1, uint64_t r0, uint64_t r1, std::vector<uint64_t> &out) {
+  bruno_status st;
+  const uint32_t n = q1 - q0;
+  out.assign(n + 1, r1);
+  if (n == 0) return BRUNO_OK;
+  std::vector<uint64_t> addr(n);
+  const uint64_t base = (uint64_t)(uintptr_t)c->seg_bufs[0].p;
+  for (uint32_t q = 0; q < n; ++q) addr[q] = base + c->samp_off[q0 + q];
+  if ((st = ensure(c, c->fr_tmp, (size_t)n * 16)) != BRUNO_OK) return st;
+  uint64_t *d = (uint64_t *)c->fr_tmp.p;
+  cudaMemcpyAsync(d, addr.data(), (size_t)n * 8, cudaMemcpyHostToDevice, c->stream);
+  k_sample_first_read<<<(n + 255) / 256, 256, 0, c->stream>>>((const uint64_t *)c->rstart.p + r0, r1 - r0, d, n, d + n);
+  c->launches += 1;
+  cudaMemcpyAsync(out.data(), d + n, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream);
+  if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "sample reads")) != BRUNO_OK) return st;
+  for (uint32_t q = 0; q < n; ++q) out[q] += r0;
+  return BRUNO_OK;
+}
+
+/* One extraction launch over samples [q0, q1) whose first reads are f (q1 - q0 + 1 values):
+ * work items of WX_ITEM reads of one sample, each sample's records into its own buckets. */
+bruno_status extract_samples(Ctx *c, uint32_t q0, uint32_t q1, const std::vector<uint64_t> &f) {
+  bruno_status st;
+  std::vector<XItem> items;
+  std::vector<uint64_t> items_of(q1 - q0, 0);
+  for (uint32_t q = q0; q < q1; ++q)
+    for (uint64_t a = f[q - q0]; a < f[q - q0 + 1]; a += WX_ITEM) {
+      items.push_back(XItem{a, std::min<uint64_t>(f[q - q0 + 1], a + WX_ITEM), q, 0u});
+      ++items_of[q - q0];
+    }
+  if (items.empty()) return BRUNO_OK;
+  const int eb = wx_blocks(f.back() - f.front());
+  const uint64_t per = std::max<uint64_t>(1, (items.size() + eb - 1) / eb);
+  std::vector<XSample> xs(q1 - q0);
+  for (uint32_t q = q0; q < q1; ++q) {
+    const uint64_t upper = (c->samp_off[q + 1] - c->samp_off[q]) / 2 + 1;   /* k-mer positions <= bytes / 2 */
+    const uint64_t touching = (items_of[q - q0] + per - 1) / per + 1;   /* blocks whose chunks can hold its records */
+    const uint64_t margin = c->x_cap[q] - upper / NBUCKET;
+    xs[q - q0] = XSample{c->x_base[q], c->x_cap[q],
+                         (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(512, margin / (2 * touching))), 0u};
+  }
+  if ((st = ensure(c, c->xitems, items.size() * sizeof(XItem))) != BRUNO_OK) return st;
+  cudaMemcpyAsync((XSample *)c->xsamp.p + q0, xs.data(), xs.size() * sizeof(XSample), cudaMemcpyHostToDevice,
+                  c->stream);
+  cudaMemcpyAsync(c->xitems.p, items.data(), items.size() * sizeof(XItem), cudaMemcpyHostToDevice, c->stream);
+  k_extract_s<<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
+      (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, 0, 0, (const XItem *)c->xitems.p, items.size(),
+      WX_ITEM, c->cfg.k, (const XSample *)c->xsamp.p, (uint64_t *)c->records.p,
+      (unsigned long long *)c->bucket_cnt.p, (unsigned int *)c->hllreg.p, (unsigned long long *)c->s_inst.p,
+      (unsigned long long *)c->s_used.p, c->dctr);
+  c->launches += 1;
+  return cuda_check(c, cudaGetLastError(), "k_extract_s");
+}
+}  // namespace
+
+/* the read index's hook for a batch copied in groups: segment si (reads [r0, r1)) has landed */
+bruno_status batch_segment(Ctx *c, size_t si, uint64_t r0, uint64_t r1) {
+  std::vector<uint64_t> f;
+  const uint32_t q0 = c->seg_samp[si], q1 = c->seg_samp[si + 1];
+  bruno_status st = first_reads(c, q0, q1, r0, r1, f);
+  return st != BRUNO_OK ? st : extract_samples(c, q0, q1, f);
+}
+
+/* The batched form's count: S samples, concatenated in one device copy, each counted into
+ * partitions of its own in one pass of every counting kernel (the plain path's kernels; the
+ * plain build is a batch of one).  Needs k <= 31 and the shared-memory partitions. */
 bruno_status run_count_samples(Ctx *c) {
   bruno_status st;
   c->have_cand = false;
   const uint32_t S = c->S;
   const int sms = num_sms();
-  if ((st = run_index_reads(c)) != BRUNO_OK) return st;
-  const uint64_t nreads = c->n_reads;
-  /* per sample: its first read */
-  {
-    std::vector<uint64_t> addr(S + 1);
-    const uint64_t base = (uint64_t)(uintptr_t)c->segs[0].ptr;
-    for (uint32_t q = 0; q <= S; ++q) addr[q] = base + c->samp_off[q];
-    Buf da;
-    if ((st = ensure(c, da, (S + 1) * 16)) != BRUNO_OK) return st;
-    cudaMemcpyAsync(da.p, addr.data(), (S + 1) * 8, cudaMemcpyHostToDevice, c->stream);
-    k_sample_first_read<<<(S + 1 + 255) / 256, 256, 0, c->stream>>>((const uint64_t *)c->rstart.p, nreads,
-                                                                    (const uint64_t *)da.p, S + 1,
-                                                                    (uint64_t *)da.p + (S + 1));
-    c->samp_r0.assign(S + 1, 0);
-    cudaMemcpyAsync(c->samp_r0.data(), (uint64_t *)da.p + (S + 1), (S + 1) * 8, cudaMemcpyDeviceToHost, c->stream);
-    st = cuda_check(c, cudaStreamSynchronize(c->stream), "sample reads");
-    cudaFreeAsync(da.p, c->stream);
-    if (st != BRUNO_OK) return st;
-    c->samp_r0[S] = nreads;
-    c->launches += 1;
-  }
-  /* extraction: items of WX_ITEM reads of one sample; per sample its buckets */
-  std::vector<XItem> items;
-  std::vector<uint64_t> items_of(S, 0);
-  for (uint32_t q = 0; q < S; ++q)
-    for (uint64_t a = c->samp_r0[q]; a < c->samp_r0[q + 1]; a += WX_ITEM) {
-      items.push_back(XItem{a, std::min<uint64_t>(c->samp_r0[q + 1], a + WX_ITEM), q, 0u});
-      ++items_of[q];
-    }
-  const int eb = wx_blocks(nreads);
-  const uint64_t per = std::max<uint64_t>(1, (items.size() + eb - 1) / eb);
-  std::vector<XSample> xs(S);
+  /* per sample its buckets: capacities from its bytes, so they are known before any read is */
+  c->x_cap.assign(S, 0);
+  c->x_base.assign(S, 0);
   std::vector<uint64_t> caps(S);
   uint64_t rec_total = 0;
   for (uint32_t q = 0; q < S; ++q) {
     const uint64_t upper = (c->samp_off[q + 1] - c->samp_off[q]) / 2 + 1;   /* k-mer positions <= bytes / 2 */
-    const uint64_t cap = upper / NBUCKET + upper / (NBUCKET * 12) + 4096;
-    const uint64_t touching = (items_of[q] + per - 1) / per + 1;   /* blocks whose chunks can hold its records */
-    const uint64_t margin = cap - upper / NBUCKET;
-    xs[q] = XSample{rec_total, cap, (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(512, margin / (2 * touching))), 0u};
-    caps[q] = cap;
-    rec_total += cap * NBUCKET;
+    caps[q] = c->x_cap[q] = upper / NBUCKET + upper / (NBUCKET * 12) + 4096;
+    c->x_base[q] = rec_total;
+    rec_total += caps[q] * NBUCKET;
   }
   if ((st = ensure(c, c->records, rec_total * 8)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->bucket_cnt, (size_t)S * NBUCKET * 8)) != BRUNO_OK) return st;
@@ -2839,15 +2880,11 @@ bruno_status run_count_samples(Ctx *c) {
   if ((st = ensure(c, c->s_used, (size_t)S * 8)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->s_tally, (size_t)S * T_NUM * 8)) != BRUNO_OK) return st;
   if ((st = ensure(c, c->hsum, (size_t)S * 16)) != BRUNO_OK) return st;
-  if ((st = ensure(c, c->xitems, std::max<size_t>(1, items.size()) * sizeof(XItem))) != BRUNO_OK) return st;
   cudaMemsetAsync(c->bucket_cnt.p, 0, (size_t)S * NBUCKET * 8, c->stream);
   cudaMemsetAsync(c->hllreg.p, 0, (size_t)S * HLL_M * 4, c->stream);
   cudaMemsetAsync(c->s_inst.p, 0, (size_t)S * 8, c->stream);
   cudaMemsetAsync(c->s_used.p, 0, (size_t)S * 8, c->stream);
   cudaMemsetAsync(c->s_tally.p, 0, (size_t)S * T_NUM * 8, c->stream);
-  cudaMemcpyAsync(c->xsamp.p, xs.data(), S * sizeof(XSample), cudaMemcpyHostToDevice, c->stream);
-  if (!items.empty())
-    cudaMemcpyAsync(c->xitems.p, items.data(), items.size() * sizeof(XItem), cudaMemcpyHostToDevice, c->stream);
   static const bool wattr = [] {
     cudaFuncSetAttribute(k_extract_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
     cudaFuncSetAttribute(k_count_local, cudaFuncAttributeMaxDynamicSharedMemorySize, PART_SLOTS * 32);
@@ -2855,17 +2892,19 @@ bruno_status run_count_samples(Ctx *c) {
     return true;
   }();
   (void)wattr;
-  cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
-  cudaEventRecord(c->kev[0], c->stream);
-  if (!items.empty())
-    k_extract_s<<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
-        (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, 0, 0, (const XItem *)c->xitems.p, items.size(),
-        WX_ITEM, c->cfg.k, (const XSample *)c->xsamp.p, (uint64_t *)c->records.p,
-        (unsigned long long *)c->bucket_cnt.p, (unsigned int *)c->hllreg.p, (unsigned long long *)c->s_inst.p,
-        (unsigned long long *)c->s_used.p, c->dctr);
+  /* the read index (its counters reset first); a batch copied in groups extracts each group
+   * as it lands (batch_segment), otherwise one launch over every sample follows */
+  if (c->batch_piped) cudaEventRecord(c->kev[0], c->stream);
+  if ((st = run_index_reads(c)) != BRUNO_OK) return st;
+  const uint64_t nreads = c->n_reads;
+  if ((st = first_reads(c, 0, S, 0, nreads, c->samp_r0)) != BRUNO_OK) return st;
+  if (!c->batch_piped) {
+    cudaEventRecord(c->kev[0], c->stream);
+    if ((st = extract_samples(c, 0, S, c->samp_r0)) != BRUNO_OK) return st;
+  }
   k_hll_sums<<<S, 256, 0, c->stream>>>((const unsigned int *)c->hllreg.p, (double *)c->hsum.p,
                                        (unsigned int *)((double *)c->hsum.p + S));
-  c->launches += 2;
+  c->launches += 1;
   cudaEventRecord(c->kev[1], c->stream);
   std::vector<double> hs(2 * S);
   cudaMemcpyAsync(hs.data(), c->hsum.p, (size_t)S * 16, cudaMemcpyDeviceToHost, c->stream);

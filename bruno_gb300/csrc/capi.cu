@@ -150,7 +150,7 @@ bruno_status bruno_ctx_destroy(bruno_ctx *c) {
                  &c->cstate, &c->cstate2, &c->pend, &c->pay, &c->unf0, &c->unf1, &c->removed, &c->r_K, &c->r_rep, &c->r_dist,
                  &c->rep_idx, &c->head_of, &c->heads, &c->head_len, &c->head_off, &c->ch_rep, &c->ch_off, &c->ch_chars, &c->chain_list, &c->branch_list, &c->e_ends, &c->e_freqs, &c->s_kmers, &c->s_dist, &c->s_flags, &c->k1tab,
                  &c->cl_trec, &c->cl_tslot, &c->cl_sums, &c->cl_norm, &c->cl_htab, &c->cl_q, &c->cl_found,
-                 &c->records, &c->bucket_cnt, &c->records2, &c->sub_cnt, &c->bigres, &c->cand, &c->scan_tmp,
+                 &c->records, &c->bucket_cnt, &c->records2, &c->sub_cnt, &c->bigres, &c->cand, &c->scan_tmp, &c->fr_tmp,
                  &c->xsamp, &c->hllreg, &c->hsum, &c->sgeom, &c->s_tally, &c->s_inst, &c->s_used, &c->xitems,
                  &c->split_items, &c->csample, &c->r_samp, &c->h_samp, &c->grp_tmp};
   for (Buf *b : bufs) release(*b);
@@ -196,6 +196,8 @@ bruno_status bruno_reset(bruno_ctx *c) {
   c->S = 1;   /* the plain build; bruno_build_samples sets a batch */
   c->samp_off.clear();
   c->samp_r0.clear();
+  c->batch_piped = false;
+  c->seg_samp.clear();
   c->n_reads = c->n_reads_used = c->n_instances = c->n_entries = 0;
   c->n_k2 = c->n_filtered = 0;
   c->k2_dumped = false;
@@ -627,33 +629,89 @@ bruno_status bruno_build_samples(bruno_ctx *c, const char *const *bufs, const si
   } else {
     for (size_t q = 0; q < n_samples; ++q) if (nbytes[q]) last[q] = (unsigned char)bufs[q][nbytes[q] - 1];
   }
+  /* host samples travel in groups of whole samples (about cfg.h2d_chunk bytes, each group on a
+   * 16-byte boundary) on the copy stream, one event a group, so that the read index parses and
+   * extracts each group while the next is in flight */
+  const uint64_t group = c->cfg.h2d_chunk ? c->cfg.h2d_chunk : (256ull << 20);
   c->samp_off.assign(n_samples + 1, 0);
-  for (size_t q = 0; q < n_samples; ++q)
-    c->samp_off[q + 1] = c->samp_off[q] + nbytes[q] + (nbytes[q] && last[q] != '\n' ? 1 : 0);
-  const uint64_t total = c->samp_off[n_samples];
+  c->seg_samp.assign(1, 0);
+  uint64_t at = 0, in_group = 0;
+  for (size_t q = 0; q < n_samples; ++q) {
+    if (!is_device && in_group >= group) {
+      at = (at + 15) & ~15ull;
+      c->seg_samp.push_back((uint32_t)q);
+      in_group = 0;
+    }
+    c->samp_off[q] = at;
+    const uint64_t len = nbytes[q] + (nbytes[q] && last[q] != '\n' ? 1 : 0);
+    at += len;
+    in_group += len;
+  }
+  c->samp_off[n_samples] = at;
+  c->seg_samp.push_back((uint32_t)n_samples);
+  const uint64_t total = at;
+  const size_t ngroups = c->seg_samp.size() - 1;
   if (c->seg_bufs.empty()) c->seg_bufs.resize(1);
   if ((st = ensure(c, c->seg_bufs[0], total + 16)) != BRUNO_OK) return st;
   char *dst = (char *)c->seg_bufs[0].p;
   static const char nl = '\n';
-  record(c, 7);
-  for (size_t q = 0; q < n_samples && st == BRUNO_OK; ++q) {
-    if (!nbytes[q]) continue;
-    st = cuda_check(c, cudaMemcpyAsync(dst + c->samp_off[q], bufs[q], nbytes[q],
-                                       is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream),
-                    "sample copy");
-    if (st == BRUNO_OK && last[q] != '\n')
-      st = cuda_check(c, cudaMemcpyAsync(dst + c->samp_off[q] + nbytes[q], &nl, 1, cudaMemcpyHostToDevice, c->stream),
-                      "sample end");
+  c->batch_piped = ngroups > 1;
+  if (!c->batch_piped) {   /* one copy after another on the context's stream, one segment */
+    record(c, 7);
+    for (size_t q = 0; q < n_samples && st == BRUNO_OK; ++q) {
+      if (!nbytes[q]) continue;
+      st = cuda_check(c, cudaMemcpyAsync(dst + c->samp_off[q], bufs[q], nbytes[q],
+                                         is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream),
+                      "sample copy");
+      if (st == BRUNO_OK && last[q] != '\n')
+        st = cuda_check(c, cudaMemcpyAsync(dst + c->samp_off[q] + nbytes[q], &nl, 1, cudaMemcpyHostToDevice,
+                                           c->stream), "sample end");
+    }
+    if (st != BRUNO_OK) return st;
+    c->segs.push_back({dst, total});
+  } else {
+    /* after whatever the context's stream has queued (the buffer's allocation) */
+    cudaEventRecord(c->order_ev, c->stream);
+    cudaStreamWaitEvent(c->copy_stream, c->order_ev, 0);
+    cudaEventRecord(c->ev[7], c->copy_stream);
+    for (size_t gi = 0; gi < ngroups && st == BRUNO_OK; ++gi) {
+      const uint32_t q0 = c->seg_samp[gi], q1 = c->seg_samp[gi + 1];
+      for (uint32_t q = q0; q < q1 && st == BRUNO_OK; ++q) {
+        if (!nbytes[q]) continue;
+        st = cuda_check(c, cudaMemcpyAsync(dst + c->samp_off[q], bufs[q], nbytes[q], cudaMemcpyHostToDevice,
+                                           c->copy_stream), "sample copy");
+        if (st == BRUNO_OK && last[q] != '\n')
+          st = cuda_check(c, cudaMemcpyAsync(dst + c->samp_off[q] + nbytes[q], &nl, 1, cudaMemcpyHostToDevice,
+                                             c->copy_stream), "sample end");
+      }
+      if (st == BRUNO_OK && c->seg_ev_used == c->seg_ev.size()) {
+        cudaEvent_t e;
+        st = cuda_check(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+        if (st == BRUNO_OK) c->seg_ev.push_back(e);
+      }
+      if (st != BRUNO_OK) break;
+      const int ev = (int)c->seg_ev_used++;
+      cudaEventRecord(c->seg_ev[ev], c->copy_stream);
+      uint64_t gend = c->samp_off[q0];   /* the group's last byte: its last sample's end, before any padding */
+      for (uint32_t q = q0; q < q1; ++q) gend = c->samp_off[q] + nbytes[q] + (nbytes[q] && last[q] != '\n' ? 1 : 0);
+      c->segs.push_back({dst + c->samp_off[q0], gend - c->samp_off[q0], ev});
+    }
+    cudaEventRecord(c->h2d_end, c->copy_stream);
+    if (st != BRUNO_OK) return st;
   }
-  if (st != BRUNO_OK) return st;
-  c->segs.push_back({dst, total});
   c->S = (uint32_t)n_samples;
   c->stage = 1;
   record(c, 0);
   if ((st = run_count_samples(c)) != BRUNO_OK) return st;
   record(c, 1);
   cudaEventSynchronize(c->ev[1]);
-  c->phase_ms[10] = elapsed(c, 7, 0);
+  if (c->batch_piped) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, c->ev[7], c->h2d_end) != cudaSuccess) { cudaGetLastError(); ms = 0; }
+    c->phase_ms[10] = ms;
+  } else {
+    c->phase_ms[10] = elapsed(c, 7, 0);
+  }
   c->phase_ms[1] = elapsed(c, 0, 1);
   c->stage = 2;
   if ((st = bruno_local_insert_by_freqencies(c, nullptr)) != BRUNO_OK) return st;

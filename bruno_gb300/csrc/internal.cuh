@@ -139,6 +139,12 @@ struct Ctx {
    * device copy (S + 1 values), first read (S + 1), table geometry and tallies */
   uint32_t S = 1;
   std::vector<uint64_t> samp_off, samp_r0;
+  /* a batch copied from the host in groups of whole samples: segment i holds samples
+   * [seg_samp[i], seg_samp[i + 1]), and the read index extracts each group as it lands */
+  bool batch_piped = false;
+  std::vector<uint32_t> seg_samp;
+  std::vector<uint64_t> x_cap, x_base;     /* per sample: bucket capacity, first record */
+  Buf fr_tmp;                              /* first-read lookups of a group of samples */
   std::vector<SGeom> h_sgeom;
   Buf sgeom, s_tally, s_inst, s_used, xitems, split_items, csample, r_samp, h_samp, grp_tmp;
   std::vector<uint64_t> h_tally;           /* T_NUM per sample, after the build */

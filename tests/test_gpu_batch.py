@@ -77,6 +77,19 @@ def test_batch_equals_plain_per_sample(opt):
     assert total["n_instances"] == n_inst
 
 
+@pytest.mark.parametrize("chunk", [1 << 12, 1 << 16, 1 << 20])
+def test_batch_copied_in_groups(chunk):
+    """host samples copied in groups of whole samples (h2d_chunk bytes each), every group read
+    and extracted while the next is in flight: each sample as its plain build"""
+    thr = bg.thresholds([2])
+    cfg = dict(k=31, thresholding=True, thresh=thr, min_update=True)
+    samples = mixed_samples()
+    got, total = batch(samples, h2d_chunk=chunk, **cfg)
+    for i, data in enumerate(samples):
+        same_as_plain(got[i], plain(data, **cfg), f"sample {i}")
+    assert total["n_reads"] == sum(g["sizes"]["n_reads"] for g in got)
+
+
 def test_batch_equals_oracle():
     samples = mixed_samples()[:6]
     thr = bg.thresholds([2])
