@@ -980,14 +980,96 @@ struct XSample { unsigned long long rec_base, cap; unsigned int chunk, pad; };
 /* reads [a, b) of sample s */
 struct XItem { unsigned long long a, b; unsigned int s, pad; };
 
+/* Records of the extraction, per key width.  k <= 31: 8 bytes, [low 54 bits of bj_fwd(k-mer) |
+ * biedge code:5], the bucket being the mix's top 8 bits.  k > 31: 16 bytes, x = (H << 8) | code
+ * with H = KOps<KW2>::hash(k-mer) (the bucket is H's top 8 bits) and y = the k-mer's high word,
+ * from which the low word follows (kw2_lo).  A zero record is no record (codes are never 0). */
+template <class KT> struct XRec;
+template <> struct XRec<KW1> {
+  using T = uint64_t;
+  static constexpr int ROUND = 8, Q = 32;   /* records a thread between flushes, queue per bucket */
+  __device__ static __forceinline__ T zero() { return 0ull; }
+  __device__ static __forceinline__ bool none(T r) { return r == 0ull; }
+  /* the record of k-mer x with biedge code; its bucket; the HyperLogLog sample (if any) */
+  __device__ static __forceinline__ T make(KW1 x, unsigned code, unsigned &bucket, bool &sampled, unsigned &idx,
+                                           unsigned &rho) {
+    const uint64_t h = bj_fwd(x.v);
+    bucket = (unsigned)(h >> LOW_BITS);
+    sampled = (h & ((1u << HLL_SAMPLE) - 1)) == 0;
+    idx = (unsigned)(h >> (62 - HLL_P));
+    rho = (unsigned)__clzll((h << (2 + HLL_P)) | (1ull << (1 + HLL_P))) + 1u;
+    return ((h & ((1ull << LOW_BITS) - 1)) << 5) | code;
+  }
+};
+template <> struct XRec<KW2> {
+  using T = ulonglong2;
+  static constexpr int ROUND = 4, Q = 16;   /* twice the bytes a record: half the queue */
+  __device__ static __forceinline__ T zero() { return make_ulonglong2(0ull, 0ull); }
+  __device__ static __forceinline__ bool none(T r) { return r.x == 0ull; }
+  __device__ static __forceinline__ T make(KW2 x, unsigned code, unsigned &bucket, bool &sampled, unsigned &idx,
+                                           unsigned &rho) {
+    const uint64_t h = KOps<KW2>::hash(x);
+    bucket = (unsigned)(h >> 56);
+    sampled = (h & ((1u << HLL_SAMPLE) - 1)) == 0;
+    idx = (unsigned)(h >> (64 - HLL_P));
+    rho = (unsigned)__clzll((h << HLL_P) | (1ull << (HLL_P - 1))) + 1u;
+    return make_ulonglong2((h << 8) | code, x.hi);
+  }
+};
+
+template <class KT>
+struct ExtractSmemT {
+  typename XRec<KT>::T q[NBUCKET][XRec<KT>::Q];
+  unsigned int hll[HLL_M];
+  unsigned int cnt[NBUCKET];
+  unsigned long long base[NBUCKET];   /* this flush: first `rem` records from base, the rest from base2 */
+  unsigned long long base2[NBUCKET];
+  unsigned int rem[NBUCKET];
+  unsigned long long cpos[NBUCKET], cend[NBUCKET];   /* the block's current chunk of each bucket */
+  int overflow;
+};
+
+/* the forward k-mer and its reverse complement, rolled base by base */
+template <class KT> struct Roll;
+template <> struct Roll<KW1> {
+  uint64_t fwd, rev, kmask;
+  int top;
+  __device__ __forceinline__ explicit Roll(int k) : fwd(0), rev(0), kmask((1ull << (2 * k)) - 1), top(2 * k - 2) {}
+  __device__ __forceinline__ void reset() { fwd = 0; rev = 0; }
+  __device__ __forceinline__ unsigned first() const { return (unsigned)(fwd >> top) & 3u; }
+  __device__ __forceinline__ void push(unsigned c) {
+    fwd = ((fwd << 2) | c) & kmask;
+    rev = (rev >> 2) | ((uint64_t)(3u - c) << top);
+  }
+  __device__ __forceinline__ bool fwd_canonical() const { return fwd < rev; }
+  __device__ __forceinline__ KW1 f() const { return {fwd}; }
+  __device__ __forceinline__ KW1 r() const { return {rev}; }
+};
+template <> struct Roll<KW2> {
+  KW2 fwd, rev;
+  int k;
+  __device__ __forceinline__ explicit Roll(int k_) : fwd{0, 0}, rev{0, 0}, k(k_) {}
+  __device__ __forceinline__ void reset() { fwd = {0, 0}; rev = {0, 0}; }
+  __device__ __forceinline__ unsigned first() const { return KOps<KW2>::first(fwd, k); }
+  __device__ __forceinline__ void push(unsigned c) {
+    fwd = KOps<KW2>::append(fwd, c, k);
+    rev = KOps<KW2>::prepend(3u - c, rev, k);
+  }
+  __device__ __forceinline__ bool fwd_canonical() const { return KOps<KW2>::lt(fwd, rev); }
+  __device__ __forceinline__ KW2 f() const { return fwd; }
+  __device__ __forceinline__ KW2 r() const { return rev; }
+};
+
 /* the block's open chunks of sample xs closed (tails zeroed) and its registers folded into the
  * sample's (every thread of the block calls it) */
-__device__ __forceinline__ void xs_close(ExtractSmem &S, const XSample &xs, uint64_t *records, unsigned int *hreg) {
+template <class KT>
+__device__ __forceinline__ void xs_close(ExtractSmemT<KT> &S, const XSample &xs, typename XRec<KT>::T *records,
+                                         unsigned int *hreg) {
   const int tid = threadIdx.x;
   __syncthreads();
   for (int b = tid >> 5; b < NBUCKET; b += XTPB / 32) {
     const unsigned long long e = min(S.cend[b], xs.rec_base + (unsigned long long)(b + 1) * xs.cap);
-    for (unsigned long long p = S.cpos[b] + (tid & 31); p < e; p += 32) records[p] = 0ull;
+    for (unsigned long long p = S.cpos[b] + (tid & 31); p < e; p += 32) records[p] = XRec<KT>::zero();
   }
   for (int i = tid; i < HLL_M; i += XTPB) {
     if (S.hll[i]) atomicMax(&hreg[i], S.hll[i]);
@@ -998,21 +1080,22 @@ __device__ __forceinline__ void xs_close(ExtractSmem &S, const XSample &xs, uint
   __syncthreads();
 }
 
+template <class KT>
 __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, const uint64_t *rend, uint64_t r0,
                                                         uint64_t r1, const XItem *items, uint64_t n_items,
                                                         uint32_t item_reads, int k, const XSample *xsamp,
-                                                        uint64_t *records, unsigned long long *bucket_cnt,
+                                                        typename XRec<KT>::T *records, unsigned long long *bucket_cnt,
                                                         unsigned int *hll, unsigned long long *s_inst,
                                                         unsigned long long *s_used, DevCounters *ctr) {
+  using R = XRec<KT>;
+  constexpr int XQT = R::Q, XROUNDT = R::ROUND;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  ExtractSmem &S = *reinterpret_cast<ExtractSmem *>(smem_raw);
+  ExtractSmemT<KT> &S = *reinterpret_cast<ExtractSmemT<KT> *>(smem_raw);
   const int tid = threadIdx.x;
   for (int i = tid; i < HLL_M; i += XTPB) S.hll[i] = 0;
   for (int i = tid; i < NBUCKET; i += XTPB) { S.cnt[i] = 0; S.cpos[i] = 0; S.cend[i] = 0; }
   if (tid == 0) S.overflow = 0;
   __syncthreads();
-  const uint64_t kmask = (k == 32) ? ~0ull : ((1ull << (2 * k)) - 1);
-  const int top = 2 * k - 2;
   const uint64_t nit = items ? n_items : (r1 - r0 + item_reads - 1) / item_reads;
   const uint64_t per = (nit + gridDim.x - 1) / gridDim.x;
   const uint64_t it0 = min(nit, (uint64_t)blockIdx.x * per), it1 = min(nit, it0 + per);
@@ -1025,7 +1108,7 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, c
     if (items) { a = items[it].a; b = items[it].b; smp = items[it].s; }
     else { a = r0 + it * item_reads; b = min(r1, a + item_reads); smp = 0; }
     if (smp != cur_s) {
-      if (cur_s != ~0u) xs_close(S, xs, records, hll + (uint64_t)cur_s * HLL_M);
+      if (cur_s != ~0u) xs_close<KT>(S, xs, records, hll + (uint64_t)cur_s * HLL_M);
       cur_s = smp;
       xs = xsamp[smp];
     }
@@ -1033,7 +1116,7 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, c
     unsigned long long inst = 0, used = 0;
     SeqCursor sc;
     uint32_t L = 0, i = 0;
-    uint64_t fwd = 0, rev = 0;
+    Roll<KT> roll(k);
     unsigned left = 0;
     /* advance to the next usable read of this thread in the item */
     auto next_read = [&]() -> bool {
@@ -1043,29 +1126,25 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, c
         if (len < (uint32_t)k + 2 || !seq_valid(sp, ep)) continue;
         ++used;
         sc.init(sp, ep);
-        L = len; i = 0; fwd = 0; rev = 0; left = 0;
+        L = len; i = 0; roll.reset(); left = 0;
         return true;
       }
       return false;
     };
     auto emit = [&](unsigned in5, unsigned out5) {
-      uint64_t x = fwd;
-      if (!(fwd < rev)) {   /* lex_less: flip the k-mer and reverse-complement the biedge */
-        x = rev;
+      KT x = roll.f();
+      if (!roll.fwd_canonical()) {   /* lex_less: flip the k-mer and reverse-complement the biedge */
+        x = roll.r();
         const unsigned ni = out5 ? 5u - out5 : 0u, no = in5 ? 5u - in5 : 0u;
         in5 = ni; out5 = no;
       }
-      const uint64_t h = bj_fwd(x);
-      const unsigned bucket = (unsigned)(h >> LOW_BITS);
-      const uint64_t rec = ((h & ((1ull << LOW_BITS) - 1)) << 5) | biedge_code(in5, out5);
-      if ((h & ((1u << HLL_SAMPLE) - 1)) == 0) {
-        const unsigned idx = (unsigned)(h >> (62 - HLL_P));
-        const unsigned rho = (unsigned)__clzll((h << (2 + HLL_P)) | (1ull << (1 + HLL_P))) + 1u;
-        if (rho > S.hll[idx]) atomicMax(&S.hll[idx], rho);
-      }
+      unsigned bucket, idx, rho;
+      bool sampled;
+      const typename R::T rec = R::make(x, biedge_code(in5, out5), bucket, sampled, idx, rho);
+      if (sampled && rho > S.hll[idx]) atomicMax(&S.hll[idx], rho);
       ++inst;
       const unsigned pos = atomicAdd(&S.cnt[bucket], 1u);
-      if (pos < (unsigned)XQ) {
+      if (pos < (unsigned)XQT) {
         S.q[bucket][pos] = rec;
       } else {   /* queue full this round: append straight to the bucket */
         const unsigned long long o = atomicAdd(&bucket_cnt[(uint64_t)cur_s * NBUCKET + bucket], 1ull);
@@ -1076,16 +1155,15 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, c
     bool active = next_read();
     for (;;) {
       int emitted = 0;
-      while (active && emitted < XROUND) {
+      while (active && emitted < XROUNDT) {
         const unsigned byte = sc.next();
         const unsigned c = ((byte >> 1) ^ (byte >> 2)) & 3u;   /* A0 C1 G2 T3, either case */
         if (i >= (uint32_t)k) {   /* the k-mer ending before base i, its out-base is base i */
           emit(i > (uint32_t)k ? left + 1u : 0u, c + 1u);
           ++emitted;
         }
-        left = (unsigned)(fwd >> top) & 3u;
-        fwd = ((fwd << 2) | c) & kmask;
-        rev = (rev >> 2) | ((uint64_t)(3u - c) << top);
+        left = roll.first();
+        roll.push(c);
         if (++i == L) {   /* the last k-mer has no out-base */
           emit(left + 1u, 0u);
           ++emitted;
@@ -1098,7 +1176,7 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, c
        * most flushes need no global atomic; a chunk's unused tail is zeroed when the block
        * leaves the sample (0 is no record: a biedge code is never 0) */
       if (tid < NBUCKET) {
-        const unsigned f = min(S.cnt[tid], (unsigned)XQ);
+        const unsigned f = min(S.cnt[tid], (unsigned)XQT);
         if (f) {
           const unsigned long long p = S.cpos[tid], avail = S.cend[tid] - p;
           S.base[tid] = p;
@@ -1118,9 +1196,9 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, c
         }
       }
       __syncthreads();
-      for (int x = tid; x < NBUCKET * XQ; x += XTPB) {
-        const int bk = x / XQ, j = x % XQ;
-        if ((unsigned)j < min(S.cnt[bk], (unsigned)XQ)) {
+      for (int x = tid; x < NBUCKET * XQT; x += XTPB) {
+        const int bk = x / XQT, j = x % XQT;
+        if ((unsigned)j < min(S.cnt[bk], (unsigned)XQT)) {
           const unsigned long long dst = (unsigned)j < S.rem[bk] ? S.base[bk] + j : S.base2[bk] + (j - S.rem[bk]);
           if (dst < xs.rec_base + (unsigned long long)(bk + 1) * xs.cap) records[dst] = S.q[bk][j];
         }
@@ -1136,7 +1214,7 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, c
       if (s_used && used) atomicAdd(&s_used[smp], used);
     }
   }
-  if (cur_s != ~0u) xs_close(S, xs, records, hll + (uint64_t)cur_s * HLL_M);
+  if (cur_s != ~0u) xs_close<KT>(S, xs, records, hll + (uint64_t)cur_s * HLL_M);
   if ((tid & 31) == 0) {
     if (inst_all) atomicAdd(&ctr->n_instances, inst_all);
     if (used_all) atomicAdd(&ctr->n_reads_used, used_all);
@@ -1607,10 +1685,11 @@ __device__ __forceinline__ uint64_t sm_cas128(uint32_t a, uint64_t cmp_lo, uint6
 }
 
 /* count_in_entries on a slot in shared memory */
+template <int NE>
 __device__ __forceinline__ bool sm_count_entries(uint32_t *e, const uint32_t *seen, unsigned code,
                                                  unsigned long long &claims) {
   #pragma unroll
-  for (int i = 0; i < 6; ++i) {
+  for (int i = 0; i < NE; ++i) {
     uint32_t w = seen[i];
     if (w == 0) {
       const uint32_t nw = (code << E_CODE_SHIFT) | (1u << E_COUNT_SHIFT);
@@ -1657,7 +1736,7 @@ __device__ __forceinline__ bool sm_count(uint64_t *sm, uint32_t sm_base, uint32_
     }
     if (key == want) {
       seen_primary = true;
-      if (sm_count_entries((uint32_t *)(sm + (uint64_t)j * 4 + 1), seen, code, entry_claims)) return true;
+      if (sm_count_entries<6>((uint32_t *)(sm + (uint64_t)j * 4 + 1), seen, code, entry_claims)) return true;
     }
     j = (j + 1 == region) ? 0u : j + 1;
   }
@@ -1780,6 +1859,173 @@ __global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, cons
     const uint64_t slot0 = G.g.base + j * G.g.region;
     for (uint32_t q = tid; q < region; q += nt) {
       const uint64_t o = sm[q * 4];
+      if (o != ~0ull && s_base + o < ca.cap) ca.cand[s_base + o] = (uint32_t)(slot0 + q);
+    }
+  }
+  if (full) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
+}
+
+/* ------------------------------------------------ partitioned count, k > 31
+ * The 16-byte records (XRec<KW2>) of the 256 hash buckets are scattered straight into the
+ * table: partition j's records go to the memory of its own slot region (room for four records
+ * a 64-byte slot), and k_count_local2 reads them into shared memory before it writes the
+ * counted region over them, so the records need no second buffer. */
+constexpr int MAX_SPLIT_BITS2 = 16;
+
+__global__ void __launch_bounds__(TPB) k_split_w2(const ulonglong2 *records, const unsigned long long *bucket_cnt,
+                                                   uint64_t cap, TableGeom g, uint64_t *table,
+                                                   unsigned long long *sub_cnt, DevCounters *ctr) {
+  const int sbits = g.pbits - NBUCKET_BITS;
+  const uint64_t room = 4 * g.region;
+  const unsigned b = blockIdx.y;
+  const uint64_t n = min((unsigned long long)cap, bucket_cnt[b]);
+  const ulonglong2 *rb = records + (uint64_t)b * cap;
+  bool over = false;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const ulonglong2 r = __ldcs(rb + i);
+    if (r.x == 0ull) continue;   /* an unused chunk tail */
+    /* the partition: the bucket, then the hash bits right below it (the record's top bits) */
+    const uint64_t j = ((uint64_t)b << sbits) | (sbits ? (r.x >> (64 - sbits)) : 0ull);
+    const unsigned long long o = atomicAdd(&sub_cnt[j], 1ull);
+    if (o < room) __stcs(reinterpret_cast<ulonglong2 *>(table + (g.base + j * g.region) * 8) + o, r);
+    else over = true;
+  }
+  if (over) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
+}
+
+/* one record into a 64-byte slot region in shared memory (key 2 words, 12 entry words);
+ * false if the region is full */
+__device__ __forceinline__ bool sm_count2(uint64_t *sm, uint32_t sm_base, uint32_t region, uint64_t lo, uint64_t hi,
+                                          unsigned code, uint32_t home, unsigned long long &slot_claims,
+                                          unsigned long long &entry_claims) {
+  bool seen_primary = false;
+  uint32_t j = home;
+  for (uint32_t probe = 0; probe < region; ++probe) {
+    const uint32_t a = sm_base + j * 64u;
+    uint64_t k0, k1;
+    asm volatile("ld.volatile.shared.v2.u64 {%0, %1}, [%2];" : "=l"(k0), "=l"(k1) : "r"(a) : "memory");
+    const uint64_t whi = hi | (seen_primary ? KEY_CONT : 0);
+    uint32_t seen[12];
+    bool fresh = false;
+    if (k0 == KEY_EMPTY && k1 == KEY_EMPTY) {
+      uint64_t ohi;
+      const uint64_t olo = sm_cas128(a, KEY_EMPTY, KEY_EMPTY, lo, whi, ohi);
+      if (olo == KEY_EMPTY && ohi == KEY_EMPTY) { ++slot_claims; k0 = lo; k1 = whi; fresh = true; }
+      else { k0 = olo; k1 = ohi; }
+    }
+    if (k0 == lo && k1 == whi) {
+      seen_primary = true;
+      if (fresh) {   /* a slot just claimed has no entries yet */
+        #pragma unroll
+        for (int q = 0; q < 12; ++q) seen[q] = 0;
+      } else {
+        #pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          uint64_t w0, w1;
+          asm volatile("ld.volatile.shared.v2.u64 {%0, %1}, [%2];" : "=l"(w0), "=l"(w1) : "r"(a + 16u + 16u * q)
+                       : "memory");
+          seen[4 * q] = (uint32_t)w0; seen[4 * q + 1] = (uint32_t)(w0 >> 32);
+          seen[4 * q + 2] = (uint32_t)w1; seen[4 * q + 3] = (uint32_t)(w1 >> 32);
+        }
+      }
+      if (sm_count_entries<12>((uint32_t *)(sm + (uint64_t)j * 8 + 2), seen, code, entry_claims)) return true;
+    }
+    j = (j + 1 == region) ? 0u : j + 1;
+  }
+  return false;
+}
+
+/* One CTA per partition j: clear its slots in shared memory, count its records (read from the
+ * region's own memory, where k_split_w2 put them), write the region back over them; with
+ * thresholds, list the slots the filter must read, as k_count_local does. */
+__global__ void __launch_bounds__(1024) k_count_local2(const unsigned long long *sub_cnt, TableGeom g, uint64_t *table,
+                                                        CandArgs ca, DevCounters *ctr) {
+  extern __shared__ __align__(16) uint64_t sm[];
+  const uint64_t j = blockIdx.x;
+  const int sbits = g.pbits - NBUCKET_BITS;
+  const uint32_t region = (uint32_t)g.region;
+  const int tid = threadIdx.x;
+  const uint32_t nt = blockDim.x;
+  for (uint32_t w = tid; w < region * 8u; w += nt) sm[w] = (w & 7u) < 2 ? KEY_EMPTY : 0ull;
+  __syncthreads();
+  const uint32_t sm_base = (uint32_t)__cvta_generic_to_shared(sm);
+  uint64_t *reg = table + (g.base + j * g.region) * 8;
+  const uint64_t n = min((unsigned long long)(4 * g.region), sub_cnt[j]);
+  const ulonglong2 *rp = reinterpret_cast<const ulonglong2 *>(reg);
+  const uint64_t bucket_hi = (j >> sbits) << 56;   /* the bucket: the hash's top 8 bits */
+  unsigned long long slots = 0, entries = 0;
+  bool full = false;
+  ulonglong2 nxt = tid < n ? __ldcs(rp + tid) : make_ulonglong2(0ull, 0ull);
+  for (uint64_t i = tid; i < n; i += nt) {
+    const ulonglong2 r = nxt;
+    nxt = i + nt < n ? __ldcs(rp + i + nt) : make_ulonglong2(0ull, 0ull);
+    const uint64_t h = bucket_hi | (r.x >> 8);
+    const uint64_t hi = r.y, lo = kw2_lo(hi, h);
+    const uint32_t home = (uint32_t)__umul64hi(h << g.pbits, g.region);
+    if (!sm_count2(sm, sm_base, region, lo, hi, (unsigned)(r.x & 31u), home, slots, entries)) full = true;
+  }
+  __syncthreads();   /* every record is read: the region's memory is free for the slots */
+  ulonglong2 *dst = reinterpret_cast<ulonglong2 *>(reg);
+  const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(sm);
+  for (uint32_t v = tid; v < region * 4u; v += nt) dst[v] = src[v];
+  slots = warp_sum(slots); entries = warp_sum(entries);
+  if ((tid & 31) == 0) {
+    if (slots) atomicAdd(&ctr->n_slots_claimed, slots);
+    if (entries) atomicAdd(&ctr->n_entries, entries);
+  }
+  if (ca.cand) {   /* as in k_count_local, with 12 entries a slot */
+    __shared__ unsigned int s_nc, s_qh[4];
+    __shared__ unsigned long long s_base;
+    if (tid < 4) s_qh[tid] = 0;
+    if (tid == 0) s_nc = 0;
+    __syncthreads();
+    uint64_t qh = 0;
+    const int lane = tid & 31;
+    for (uint32_t q0 = 0; q0 < region; q0 += nt) {
+      const uint32_t q = q0 + tid;
+      bool listed = false;
+      if (q < region) {
+        const uint64_t k0 = sm[q * 8], k1 = sm[q * 8 + 1];
+        if (!(k0 == KEY_EMPTY && k1 == KEY_EMPTY) && !(k1 & KEY_CONT)) {
+          int ne = 0;
+          uint32_t kf = 0;
+          #pragma unroll
+          for (int e = 0; e < 12; ++e) {
+            const uint32_t w = (uint32_t)(sm[q * 8 + 2 + e / 2] >> (32 * (e & 1)));
+            ne += w != 0;
+            kf += entry_count(w);
+          }
+          kf = min(0xFFFFu, kf);
+          listed = ne == 12 || kf >= ca.t[2];
+          if (!listed) {
+            const uint32_t kout = (kf < ca.t[0] || kf >= ca.t[1]) ? 2u : 0u;
+            #pragma unroll
+            for (int e = 0; e < 12; ++e) {
+              const uint32_t w = (uint32_t)(sm[q * 8 + 2 + e / 2] >> (32 * (e & 1)));
+              const uint32_t c16 = min(0xFFFFu, entry_count(w));
+              if (w) qh += 1ull << (16 * (kout | ((c16 < ca.t[4] || c16 >= ca.t[5]) ? 1u : 0u)));
+            }
+          }
+        }
+      }
+      const unsigned m = __ballot_sync(~0u, listed);   /* the loop bound is the same for every lane */
+      unsigned base = 0;
+      if (m && lane == __ffs(m) - 1) base = atomicAdd(&s_nc, (unsigned)__popc(m));
+      if (m) base = __shfl_sync(~0u, base, __ffs(m) - 1);
+      if (q < region) sm[q * 8] = listed ? (uint64_t)(base + __popc(m & ((1u << lane) - 1))) : ~0ull;
+    }
+    #pragma unroll
+    for (int f = 0; f < 4; ++f) {
+      const unsigned long long h = warp_sum((qh >> (16 * f)) & 0xFFFFull);
+      if (lane == 0 && h) atomicAdd(&s_qh[f], (unsigned)h);
+    }
+    __syncthreads();
+    if (tid == 0) s_base = s_nc ? atomicAdd(ca.n_cand, (unsigned long long)s_nc) : 0;
+    if (tid < 4 && s_qh[tid]) atomicAdd(&ca.quick_hist[3 + 4 * tid], (unsigned long long)s_qh[tid]);
+    __syncthreads();
+    const uint64_t slot0 = g.base + j * g.region;
+    for (uint32_t q = tid; q < region; q += nt) {
+      const uint64_t o = sm[q * 8];
       if (o != ~0ull && s_base + o < ca.cap) ca.cand[s_base + o] = (uint32_t)(slot0 + q);
     }
   }
@@ -2336,7 +2582,8 @@ bruno_status extract_begin(Ctx *c, uint64_t upper, int max_blocks) {
     return st;
   if (!c->cfg.edge_filter) {   /* the extraction by samples and its HyperLogLog */
     static const bool sattr = [] {
-      cudaFuncSetAttribute(k_extract_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
+      cudaFuncSetAttribute(k_extract_s<KW1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(ExtractSmemT<KW1>));
       return true;
     }();
     (void)sattr;
@@ -2486,7 +2733,7 @@ void extract_reads(Ctx *c, uint64_t r0, uint64_t r1) {
   if (nr == 0) return;
   if (!c->cfg.edge_filter) {
     const int eb = std::max(1, std::min(wx_blocks(nr), c->xblk_max - c->xblk));
-    k_extract_s<<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
+    k_extract_s<KW1><<<eb, XTPB, sizeof(ExtractSmemT<KW1>), c->stream>>>(
         (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, r0, r1, nullptr, 0, WX_ITEM, c->cfg.k,
         (const XSample *)c->xsamp.p, (uint64_t *)c->records.p, (unsigned long long *)c->bucket_cnt.p,
         (unsigned int *)c->hllreg.p, nullptr, nullptr, c->dctr);
@@ -2626,6 +2873,123 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
   return set_err(c, BRUNO_ERR_TABLE_FULL, "k-mer table full after regrowth");
 }
 
+/* The partitioned count for k > 31: exact k-mer positions size 256 buckets of 16-byte records,
+ * one extraction fills them (with the distinct estimate), and per attempt the records are
+ * scattered into the table's partitions and counted in shared memory.  used = false sends the
+ * caller to the direct count: a bucket overflowed, or a partition got more records than its
+ * region holds at every size tried (a heavily skewed input). */
+bruno_status count_partitioned_w2(Ctx *c, bool &used) {
+  bruno_status st;
+  used = false;
+  const int sms = num_sms();
+  const uint64_t nreads = c->n_reads;
+  cudaMemsetAsync(c->dctr, 0, offsetof(DevCounters, hll), c->stream);
+  k_kmer_upper<<<sms * 4, TPB, 0, c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads,
+                                               c->cfg.k, c->dctr);
+  c->launches += 1;
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  const uint64_t upper = c->hctr->n_upper;
+  const uint64_t cap = upper / NBUCKET + upper / (NBUCKET * 12) + 4096;
+  if ((st = ensure(c, c->records, (size_t)NBUCKET * cap * 16)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->bucket_cnt, NBUCKET * 8)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->xsamp, sizeof(XSample))) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->hllreg, HLL_M * 4)) != BRUNO_OK) return st;
+  if ((st = ensure(c, c->hsum, 16)) != BRUNO_OK) return st;
+  cudaMemsetAsync(c->bucket_cnt.p, 0, NBUCKET * 8, c->stream);
+  cudaMemsetAsync(c->hllreg.p, 0, HLL_M * 4, c->stream);
+  const int eb = wx_blocks(nreads);
+  const uint64_t margin = cap - upper / NBUCKET;   /* every block may hold an open chunk of every bucket */
+  const XSample xs{0ull, cap, (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(512, margin / (2ull * eb))), 0u};
+  cudaMemcpyAsync(c->xsamp.p, &xs, sizeof(xs), cudaMemcpyHostToDevice, c->stream);
+  static const bool attr = [] {
+    cudaFuncSetAttribute(k_extract_s<KW2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(ExtractSmemT<KW2>));
+    cudaFuncSetAttribute(k_count_local2, cudaFuncAttributeMaxDynamicSharedMemorySize, PART_SLOTS / 2 * 64);
+    return true;
+  }();
+  (void)attr;
+  cudaEventRecord(c->kev[0], c->stream);
+  k_extract_s<KW2><<<eb, XTPB, sizeof(ExtractSmemT<KW2>), c->stream>>>(
+      (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, 0, nreads, nullptr, 0, WX_ITEM, c->cfg.k,
+      (const XSample *)c->xsamp.p, (ulonglong2 *)c->records.p, (unsigned long long *)c->bucket_cnt.p,
+      (unsigned int *)c->hllreg.p, nullptr, nullptr, c->dctr);
+  k_hll_sums<<<1, 256, 0, c->stream>>>((const unsigned int *)c->hllreg.p, (double *)c->hsum.p,
+                                       (unsigned int *)((double *)c->hsum.p + 1));
+  c->launches += 2;
+  cudaEventRecord(c->kev[1], c->stream);
+  double hs[2] = {0, 0};
+  cudaMemcpyAsync(hs, c->hsum.p, 16, cudaMemcpyDeviceToHost, c->stream);
+  if ((st = sync_counters(c)) != BRUNO_OK) return st;
+  if (c->hctr->err & DERR_TABLE_FULL) {   /* a bucket overflowed: count directly */
+    cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
+    return BRUNO_OK;
+  }
+  c->n_instances = c->hctr->n_instances;
+  c->n_reads_used = c->hctr->n_reads_used;
+  uint64_t slots = c->cfg.table_slots ? c->cfg.table_slots
+                                      : slots_for(c, hll_sampled_estimate(hs[0], *(const unsigned int *)&hs[1]));
+  const uint64_t pmax = part_slots(c) / 2;   /* 64-byte slots: half as many in the same shared memory */
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    int pb = NBUCKET_BITS;
+    while (pb < NBUCKET_BITS + MAX_SPLIT_BITS2 && (slots + (1ull << pb) - 1) >> pb > pmax) ++pb;
+    const uint64_t region = std::max<uint64_t>(64, (slots + (1ull << pb) - 1) >> pb);
+    if (region > pmax) return BRUNO_OK;
+    c->geom = TableGeom{region << pb, region, pb, 0};
+    c->nslots = c->geom.nslots;
+    if ((st = table_room(c, c->nslots)) != BRUNO_OK) return st;
+    if ((st = ensure(c, c->table, c->nslots * 64)) != BRUNO_OK) return st;
+    if ((st = ensure(c, c->sub_cnt, (size_t)8 << pb)) != BRUNO_OK) return st;
+    cudaMemsetAsync(c->sub_cnt.p, 0, (size_t)8 << pb, c->stream);
+    cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
+    cudaMemsetAsync(&c->dctr->n_slots_claimed, 0, 16, c->stream);
+    cudaMemsetAsync(&c->dctr->n_big, 0, 8, c->stream);
+    CandArgs ca{};
+    if (c->cfg.thresholding) {
+      if ((st = ensure(c, c->cand, c->nslots * 4)) != BRUNO_OK) return st;
+      ca.cand = (uint32_t *)c->cand.p;
+      ca.cap = c->nslots;
+      ca.n_cand = &c->dctr->n_cand;
+      ca.quick_hist = c->dctr->quick_hist;
+      for (int i = 0; i < 6; ++i) ca.t[i] = c->cfg.thresh[i];
+      cudaMemsetAsync(&c->dctr->n_cand, 0, sizeof(c->dctr->n_cand) + sizeof(c->dctr->quick_hist), c->stream);
+    }
+    cudaEventRecord(c->kev[2], c->stream);
+    const unsigned gx = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 8, (cap + TPB - 1) / TPB));
+    k_split_w2<<<dim3(gx, NBUCKET), TPB, 0, c->stream>>>((const ulonglong2 *)c->records.p,
+                                                         (const unsigned long long *)c->bucket_cnt.p, cap, c->geom,
+                                                         (uint64_t *)c->table.p, (unsigned long long *)c->sub_cnt.p,
+                                                         c->dctr);
+    cudaEventRecord(c->kev[4], c->stream);
+    k_count_local2<<<(unsigned)(1ull << pb), count_threads(c), (unsigned)(region * 64), c->stream>>>(
+        (const unsigned long long *)c->sub_cnt.p, c->geom, (uint64_t *)c->table.p, ca, c->dctr);
+    c->launches += 2;
+    cudaEventRecord(c->kev[3], c->stream);
+    if ((st = cuda_check(c, cudaGetLastError(), "k_count_local2")) != BRUNO_OK) return st;
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    if (!(c->hctr->err & DERR_TABLE_FULL)) {
+      float ms[3] = {0, 0, 0};
+      cudaEventElapsedTime(&ms[0], c->kev[0], c->kev[1]);
+      cudaEventElapsedTime(&ms[1], c->kev[2], c->kev[4]);
+      cudaEventElapsedTime(&ms[2], c->kev[2], c->kev[3]);
+      c->phase_ms[6] = ms[0];
+      c->phase_ms[7] = 0;
+      c->phase_ms[8] = ms[2];
+      c->phase_ms[9] = ms[1];
+      c->n_entries = c->hctr->n_entries;
+      c->n_slots_claimed = c->hctr->n_slots_claimed;
+      c->have_cand = ca.cand != nullptr;
+      take_candidates(c);
+      used = true;
+      return BRUNO_OK;
+    }
+    /* a partition's records overflowed its region, or its slots filled: larger regions, and
+     * the records scattered again from the buckets */
+    slots = std::max<uint64_t>(slots, c->nslots) * 2;
+  }
+  cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
+  return BRUNO_OK;
+}
+
 /* compute_edge_frequency: the (k+1)-mer table, sized from its own distinct estimate and
  * regrown if a probe run overflows, then thresholded */
 bruno_status build_k1_table(Ctx *c) {
@@ -2673,6 +3037,11 @@ bruno_status count_paths(Ctx *c) {
   if (sizeof(KT) == 8 && c->force_direct_count != 1) {
     bool used = false;
     bruno_status st = count_partitioned(c, used);
+    if (st != BRUNO_OK || used) return st;
+  }
+  if (sizeof(KT) == 16 && c->force_direct_count == 0) {
+    bool used = false;
+    bruno_status st = count_partitioned_w2(c, used);
     if (st != BRUNO_OK || used) return st;
   }
   c->have_cand = false;   /* whatever a partitioned attempt listed is stale */
@@ -2835,7 +3204,7 @@ bruno_status extract_samples(Ctx *c, uint32_t q0, uint32_t q1, const std::vector
   cudaMemcpyAsync((XSample *)c->xsamp.p + q0, xs.data(), xs.size() * sizeof(XSample), cudaMemcpyHostToDevice,
                   c->stream);
   cudaMemcpyAsync(c->xitems.p, items.data(), items.size() * sizeof(XItem), cudaMemcpyHostToDevice, c->stream);
-  k_extract_s<<<eb, XTPB, sizeof(ExtractSmem), c->stream>>>(
+  k_extract_s<KW1><<<eb, XTPB, sizeof(ExtractSmemT<KW1>), c->stream>>>(
       (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, 0, 0, (const XItem *)c->xitems.p, items.size(),
       WX_ITEM, c->cfg.k, (const XSample *)c->xsamp.p, (uint64_t *)c->records.p,
       (unsigned long long *)c->bucket_cnt.p, (unsigned int *)c->hllreg.p, (unsigned long long *)c->s_inst.p,
@@ -2886,7 +3255,8 @@ bruno_status run_count_samples(Ctx *c) {
   cudaMemsetAsync(c->s_used.p, 0, (size_t)S * 8, c->stream);
   cudaMemsetAsync(c->s_tally.p, 0, (size_t)S * T_NUM * 8, c->stream);
   static const bool wattr = [] {
-    cudaFuncSetAttribute(k_extract_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
+    cudaFuncSetAttribute(k_extract_s<KW1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(ExtractSmemT<KW1>));
     cudaFuncSetAttribute(k_count_local, cudaFuncAttributeMaxDynamicSharedMemorySize, PART_SLOTS * 32);
     cudaFuncSetAttribute(k_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SplitSmem));
     return true;

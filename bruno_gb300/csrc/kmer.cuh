@@ -100,6 +100,7 @@ template <> struct KOps<KW2> {
   __device__ static __forceinline__ bool le(KW2 a, KW2 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
   __device__ static __forceinline__ bool eq(KW2 a, KW2 b) { return a.hi == b.hi && a.lo == b.lo; }
   __device__ static __forceinline__ uint64_t hash(KW2 a) { return mix64(a.lo ^ mix64(a.hi + 0x9e3779b97f4a7c15ull)); }
+  /* (KW2_HC below is the same constant: kw2_lo inverts this hash for a given high word) */
   __device__ static __forceinline__ KW2 append(KW2 x, unsigned c, int k) {
     return {(x.lo << 2) | c, ((x.hi << 2) | (x.lo >> 62)) & hmask(k)};
   }
@@ -159,8 +160,10 @@ __device__ __forceinline__ bool k_palindrome(KT x, int k) {
 /* ---------------------------------------------------------------- table layout
  * The table is 2^pbits partitions of `region` slots; a key probes linearly inside its
  * partition.  For k <= 31 the position comes from a bijective mix of the 62-bit k-mer
- * (so an 8-byte record can carry the k-mer as mixed bits: partition bits implicit), for
- * k > 31 from a 64-bit hash with one partition. */
+ * (so an 8-byte record can carry the k-mer as mixed bits: partition bits implicit).  For
+ * k > 31 it comes from H = mix64(lo ^ mix64(hi + c)), which for a given high word is a
+ * bijection of the low word: a 16-byte record carries the high word and H without its top
+ * (bucket) bits, and the low word is mix64_inv(H) ^ mix64(hi + c). */
 constexpr uint64_t M62 = (1ull << 62) - 1;
 constexpr uint64_t BJ_C1 = 0x3C79AC492BA7B653ull & M62;   /* odd */
 constexpr uint64_t BJ_C2 = 0x1C69B3F74AC4AE35ull & M62;   /* odd */
@@ -191,6 +194,22 @@ __host__ __device__ __forceinline__ uint64_t bj_inv(uint64_t h) {
   return xs_inv(x, 31);
 }
 
+/* inverse of mix64: each step of splitmix64's finaliser undone in reverse order */
+__host__ __device__ __forceinline__ uint64_t xs_inv64(uint64_t y, int s) {  /* inverse of y = x ^ (x >> s) */
+  uint64_t x = y;
+  for (int t = s; t < 64; t += s) x = y ^ (x >> s);
+  return x;
+}
+constexpr uint64_t MIX_I1 = inv_odd64(0xbf58476d1ce4e5b9ull), MIX_I2 = inv_odd64(0x94d049bb133111ebull);
+__host__ __device__ __forceinline__ uint64_t mix64_inv(uint64_t x) {
+  x = xs_inv64(x, 31); x *= MIX_I2;
+  x = xs_inv64(x, 27); x *= MIX_I1;
+  return xs_inv64(x, 30);
+}
+constexpr uint64_t KW2_HC = 0x9e3779b97f4a7c15ull;   /* the high word's offset in KOps<KW2>::hash */
+/* the low word of a 128-bit key from its high word and its hash */
+__host__ __device__ __forceinline__ uint64_t kw2_lo(uint64_t hi, uint64_t h) { return mix64_inv(h) ^ mix64(hi + KW2_HC); }
+
 struct TableGeom {
   uint64_t nslots;   /* region << pbits */
   uint64_t region;
@@ -212,7 +231,9 @@ __device__ __forceinline__ uint64_t table_home(const TableGeom &g, KW1 t) {
   return g.base + q * g.region + __umul64hi(h << (2 + g.pbits), g.region);
 }
 __device__ __forceinline__ uint64_t table_home(const TableGeom &g, KW2 t) {
-  return g.base + __umul64hi(KOps<KW2>::hash(t), g.region);   /* pbits == 0 */
+  const uint64_t h = KOps<KW2>::hash(t);
+  if (!g.pbits) return g.base + __umul64hi(h, g.region);
+  return g.base + (h >> (64 - g.pbits)) * g.region + __umul64hi(h << g.pbits, g.region);
 }
 /* linear probing inside one partition */
 struct Probe {
