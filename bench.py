@@ -477,32 +477,46 @@ def main():
     d2h = nch + 8 * (nc + 1) + 8 * g.words * nc
 
     # Roofline of the dominant kernel.  Each candidate's algorithmic bytes per launch (one
-    # launch per step each) and its CUDA-event time on the library's stream:
+    # launch per step each) and its CUDA-event time on the library's stream.  k <= 31:
     #   k_extract      FASTQ bytes + 16 B read span per read read once, 8 B per record written
     #   k_split        8 B per record read and written once
-    #   k_count_local  8 B per record read once + 32 B per table slot written once
-    #   k_filter       32 B per table slot read once + 32 B per graph node written once
+    #   k_count_local  8 B per record read once + 32 B per table slot written once + 4 B per
+    #                  slot it lists for the filter
+    #   k_filter       32 B per slot it reads (the listed ones) + 32 B per graph node written once
     mean = lambda key: statistics.mean(p[key] for p in kms)
     peak, peak_src = measured_peak()
     slots = sizes["table_slots"]
+    listed = sizes["filter_slots_read"]
     if w.k <= 31:
         kern = {
             "k_extract": (n + 16 * sizes["n_reads"] + 8 * inst_step, mean("count_estimate")),
             "k_split": (16 * inst_step, mean("count_split")),
-            "k_count_local": (8 * inst_step + 32 * slots, mean("count_insert") - mean("count_split")),
-            "k_filter": (32 * slots + 32 * sizes["n_nodes"], mean("filter_insert")),
+            "k_count_local": (8 * inst_step + 32 * slots + 4 * listed, mean("count_insert") - mean("count_split")),
+            "k_filter": (32 * listed + 32 * sizes["n_nodes"], mean("filter_insert")),
+        }
+    elif sizes["table_partitions"] > 1:
+        # k > 31, partitioned (128-bit keys, 16-byte records, 64-byte slots):
+        #   k_extract      FASTQ bytes + 16 B read span per read read once, 16 B per record written
+        #   k_split_w2     16 B per record read and written once (into its partition's region)
+        #   k_count_local2 16 B per record read once + 64 B per slot written once + 4 B per listed slot
+        #   k_filter       64 B per slot it reads + 64 B per graph node written once
+        kern = {
+            "k_extract": (n + 16 * sizes["n_reads"] + 16 * inst_step, mean("count_estimate")),
+            "k_split_w2": (32 * inst_step, mean("count_split")),
+            "k_count_local2": (16 * inst_step + 64 * slots + 4 * listed, mean("count_insert") - mean("count_split")),
+            "k_filter": (64 * listed + 64 * sizes["n_nodes"], mean("filter_insert")),
         }
     else:
-        # k > 31 counts straight into the whole table (128-bit keys, 64-byte slots):
+        # k > 31 counted straight into the whole table (the fallback for skewed inputs):
         #   k_hll          FASTQ bytes + 16 B read span per read read once (the distinct estimate)
         #   k_table_init   64 B per slot written once
         #   k_count        FASTQ bytes read once + one random 64-byte read-modify-write per instance
-        #   k_filter       64 B per slot read once + 64 B per graph node written once
+        #   k_filter       64 B per slot it reads + 64 B per graph node written once
         kern = {
             "k_hll": (n + 16 * sizes["n_reads"], mean("count_estimate")),
             "k_table_init": (64 * slots, mean("count_table_init")),
             "k_count": (n + 64 * inst_step, mean("count_insert")),
-            "k_filter": (64 * slots + 64 * sizes["n_nodes"], mean("filter_insert")),
+            "k_filter": (64 * listed + 64 * sizes["n_nodes"], mean("filter_insert")),
         }
     kernels = {k: {"alg_bytes_per_launch": b, "launch_ms": t, "achieved": b / (t / 1e3) / 1e9 if t > 0 else None,
                    "frac": b / (t / 1e3) / 1e9 / peak if t > 0 else None} for k, (b, t) in kern.items()}

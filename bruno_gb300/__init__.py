@@ -53,7 +53,8 @@ class _Sizes(ctypes.Structure):
         "n_chain_chars", "table_slots", "collisions")] + [("filter_flag_hist", ctypes.c_uint64 * 16),
                                                     ("launches", ctypes.c_uint64),
                                                     ("table_partitions", ctypes.c_uint64),
-                                                    ("grouped_chains", ctypes.c_uint64)]
+                                                    ("grouped_chains", ctypes.c_uint64),
+                                                    ("filter_slots_read", ctypes.c_uint64)]
 
 
 class _PoolResult(ctypes.Structure):

@@ -3128,6 +3128,7 @@ bruno_status filter_typed(Ctx *c, const uint64_t *thr) {
                  c->stream>>>(a);
   c->launches += 1;
   c->have_cand = false;   /* the listed slots are nodes or tombstones now */
+  c->filter_read = use_cand ? c->n_cand : c->nslots;
   if ((st = sync_counters(c)) != BRUNO_OK) return st;
   const DevCounters &h = *c->hctr;
   c->n_nodes = h.n_nodes; c->n_branch = h.n_branch; c->n_chain = h.n_chain;

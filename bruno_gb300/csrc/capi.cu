@@ -215,7 +215,7 @@ bruno_status bruno_reset(bruno_ctx *c) {
       cudaStreamWaitEvent(c->stream, c->order_ev, 0);
     }
   }
-  c->n_nodes = c->n_branch = c->n_chain = 0;
+  c->n_nodes = c->n_branch = c->n_chain = c->filter_read = 0;
   c->iterations = c->n_cycle = c->n_isolated = c->multi = 0;
   c->n_ranked = c->n_heads = c->n_chain_chars = 0;
   c->chains_clean = true;
@@ -431,6 +431,7 @@ bruno_status bruno_get_sizes(bruno_ctx *c, bruno_sizes *o) {
   o->launches = c->launches;
   o->table_partitions = 1ull << c->geom.pbits;
   o->grouped_chains = c->general_emission ? 1 : 0;
+  o->filter_slots_read = c->filter_read;
   for (int f = 0; f < 16; ++f) o->filter_flag_hist[f] = c->flag_hist[f];
   return BRUNO_OK;
 }

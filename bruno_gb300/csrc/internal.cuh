@@ -175,6 +175,7 @@ struct Ctx {
 
   /* nodes */
   uint64_t n_nodes = 0, n_branch = 0, n_chain = 0;
+  uint64_t filter_read = 0;      /* slots the filter read */
   uint64_t flag_hist[16] = {0};
   Buf blk_cnt, blk_base;
 

@@ -109,6 +109,8 @@ typedef struct bruno_sizes {
   uint64_t grouped_chains;  /* 1: the chain pointers were not mutually consistent (separate k and
                                k+2 bounds can trim an edge on one side only) and the compaction
                                grouped the nodes by representative */
+  uint64_t filter_slots_read; /* table slots local_insert_by_freqencies read: every slot, or only those
+                                 the count listed (thresholded builds) */
 } bruno_sizes;
 
 typedef struct bruno_ctx bruno_ctx;
