@@ -246,7 +246,7 @@ def run_batched(args):
     sizes = [fq.nbytes for fq in fqs]
     bufs = _pinned_copies(bg, fqs)
     views = [b.array[:n] for b, n in zip(bufs, sizes)]
-    cfg = bg.GraphConfig(k=31, thresh=bg.thresholds([2]), min_update=True)
+    cfg = bg.GraphConfig(k=31, thresh=bg.thresholds([2]), min_update=True, h2d_chunk=args.h2d_chunk)
     _plain_loop(bg, cfg, bufs[:8], sizes[:8])                 # warm-up
     plain_s, plain = _plain_loop(bg, cfg, bufs, sizes)
     probe = views[::4]
@@ -272,6 +272,7 @@ def run_batched(args):
                                    "100-250 bp reads, 0.5-2% substitutions, k=31, -L 2",
                        "fastq_bytes": int(sum(sizes))},
             "form": "one fused pass (bruno_build_samples), host buffers in, chains out",
+            "run": {"h2d_chunk": args.h2d_chunk or 256 << 20, "tune": args.tune},
             "plain_loop_graphs_per_s": len(fqs) / plain_s, "speedup_vs_plain_loop": plain_s / dt,
             "pass_ms": {"with_copy_out": 1e3 * dt, "build_only": 1e3 * statistics.median(p[1] for p in passes)},
             "phase_ms": phases,

@@ -65,6 +65,9 @@ WORKLOADS = {
     # 200 Mbp + 5% repeats (1-20 kbp, 2-16 copies, 1-3% divergence), 30x 150 bp, k=63, -L 3
     "large-k": Workload("large-k", 200_000_000, 150, 40_000_000, 0.005, 63, (3,), 0.05, (1000, 20000), (2, 16),
                         (0.01, 0.03)),
+    # the large-k mix at a fiftieth of the genome, for full ncu captures (4 Mbp, 800k x 150 bp, k=63)
+    "large-k-profile": Workload("large-k-profile", 4_000_000, 150, 800_000, 0.005, 63, (3,), 0.05, (1000, 20000),
+                                (2, 16), (0.01, 0.03), 10),
 }
 
 
