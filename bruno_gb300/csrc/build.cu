@@ -1959,10 +1959,9 @@ __global__ void __launch_bounds__(1024) k_count_local2(const unsigned long long 
   for (uint64_t i = tid; i < n; i += nt) {
     const ulonglong2 r = nxt;
     nxt = i + nt < n ? __ldcs(rp + i + nt) : make_ulonglong2(0ull, 0ull);
-    const uint64_t h = bucket_hi | (r.x >> 8);
-    const uint64_t hi = r.y, lo = kw2_lo(hi, h);
+    const uint64_t h = bucket_hi | (r.x >> 8);   /* the table key is (h, high word) */
     const uint32_t home = (uint32_t)__umul64hi(h << g.pbits, g.region);
-    if (!sm_count2(sm, sm_base, region, lo, hi, (unsigned)(r.x & 31u), home, slots, entries)) full = true;
+    if (!sm_count2(sm, sm_base, region, h, r.y, (unsigned)(r.x & 31u), home, slots, entries)) full = true;
   }
   __syncthreads();   /* every record is read: the region's memory is free for the slots */
   ulonglong2 *dst = reinterpret_cast<ulonglong2 *>(reg);

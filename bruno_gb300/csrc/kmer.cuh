@@ -217,12 +217,14 @@ struct TableGeom {
   uint64_t base;     /* first slot: a sample's table in a batch of samples starts here (0 otherwise) */
 };
 
-/* The table stores a key derived from the canonical k-mer: for k <= 31 the 62-bit mix
- * bj_fwd(k-mer) (so counting records never need inverting), for k > 31 the k-mer itself. */
+/* The table stores a key derived from the canonical k-mer, so that counting records never
+ * need inverting and the key itself gives the position: for k <= 31 the 62-bit mix
+ * bj_fwd(k-mer); for k > 31 the pair (H, high word), H = KOps<KW2>::hash(k-mer) in the low word
+ * (the high word keeps the k-mer's, whose two top bits stay free for the slot marks). */
 __device__ __forceinline__ KW1 table_key(KW1 x) { return {bj_fwd(x.v)}; }
-__device__ __forceinline__ KW2 table_key(KW2 x) { return x; }
+__device__ __forceinline__ KW2 table_key(KW2 x) { return {KOps<KW2>::hash(x), x.hi}; }
 __device__ __forceinline__ KW1 key_kmer(KW1 t) { return {bj_inv(t.v)}; }
-__device__ __forceinline__ KW2 key_kmer(KW2 t) { return t; }
+__device__ __forceinline__ KW2 key_kmer(KW2 t) { return {kw2_lo(t.hi, t.lo), t.hi}; }
 
 /* home slot of a table key */
 __device__ __forceinline__ uint64_t table_home(const TableGeom &g, KW1 t) {
@@ -231,7 +233,7 @@ __device__ __forceinline__ uint64_t table_home(const TableGeom &g, KW1 t) {
   return g.base + q * g.region + __umul64hi(h << (2 + g.pbits), g.region);
 }
 __device__ __forceinline__ uint64_t table_home(const TableGeom &g, KW2 t) {
-  const uint64_t h = KOps<KW2>::hash(t);
+  const uint64_t h = t.lo;   /* the table key's low word is the hash */
   if (!g.pbits) return g.base + __umul64hi(h, g.region);
   return g.base + (h >> (64 - g.pbits)) * g.region + __umul64hi(h << g.pbits, g.region);
 }
