@@ -1937,8 +1937,10 @@ __device__ __forceinline__ bool sm_count2(uint64_t *sm, uint32_t sm_base, uint32
 
 /* One CTA per partition j: clear its slots in shared memory, count its records (read from the
  * region's own memory, where k_split_w2 put them), write the region back over them; with
- * thresholds, list the slots the filter must read, as k_count_local does. */
-__global__ void __launch_bounds__(1024) k_count_local2(const unsigned long long *sub_cnt, TableGeom g, uint64_t *table,
+ * thresholds, list the slots the filter must read, as k_count_local does.  512 threads a CTA,
+ * bounded to 40 registers so that three CTAs share an SM. */
+constexpr int PTPB2 = 512;
+__global__ void __launch_bounds__(PTPB2, 3) k_count_local2(const unsigned long long *sub_cnt, TableGeom g, uint64_t *table,
                                                         CandArgs ca, DevCounters *ctr) {
   extern __shared__ __align__(16) uint64_t sm[];
   const uint64_t j = blockIdx.x;
@@ -2959,7 +2961,7 @@ bruno_status count_partitioned_w2(Ctx *c, bool &used) {
                                                          (uint64_t *)c->table.p, (unsigned long long *)c->sub_cnt.p,
                                                          c->dctr);
     cudaEventRecord(c->kev[4], c->stream);
-    k_count_local2<<<(unsigned)(1ull << pb), count_threads(c), (unsigned)(region * 64), c->stream>>>(
+    k_count_local2<<<(unsigned)(1ull << pb), PTPB2, (unsigned)(region * 64), c->stream>>>(
         (const unsigned long long *)c->sub_cnt.p, c->geom, (uint64_t *)c->table.p, ca, c->dctr);
     c->launches += 2;
     cudaEventRecord(c->kev[3], c->stream);
