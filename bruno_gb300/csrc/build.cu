@@ -1872,23 +1872,45 @@ __global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, cons
  * counted region over them, so the records need no second buffer. */
 constexpr int MAX_SPLIT_BITS2 = 16;
 
+/* Warps take 32-record runs round robin over the buckets (run g is run g / 256 of bucket
+ * g % 256), so that the atomics in flight at any time spread over every bucket's partitions
+ * instead of queueing on one bucket's few cursors; each thread keeps SPLIT2_U records in flight. */
+constexpr int SPLIT2_U = 4;
 __global__ void __launch_bounds__(TPB) k_split_w2(const ulonglong2 *records, const unsigned long long *bucket_cnt,
-                                                   uint64_t cap, TableGeom g, uint64_t *table,
+                                                   uint64_t cap, uint64_t runs_per_bucket, TableGeom g, uint64_t *table,
                                                    unsigned long long *sub_cnt, DevCounters *ctr) {
   const int sbits = g.pbits - NBUCKET_BITS;
   const uint64_t room = 4 * g.region;
-  const unsigned b = blockIdx.y;
-  const uint64_t n = min((unsigned long long)cap, bucket_cnt[b]);
-  const ulonglong2 *rb = records + (uint64_t)b * cap;
+  const int lane = threadIdx.x & 31;
+  const uint64_t nwarps = (uint64_t)gridDim.x * (TPB / 32);
+  const uint64_t total = runs_per_bucket * NBUCKET;
   bool over = false;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const ulonglong2 r = __ldcs(rb + i);
-    if (r.x == 0ull) continue;   /* an unused chunk tail */
-    /* the partition: the bucket, then the hash bits right below it (the record's top bits) */
-    const uint64_t j = ((uint64_t)b << sbits) | (sbits ? (r.x >> (64 - sbits)) : 0ull);
-    const unsigned long long o = atomicAdd(&sub_cnt[j], 1ull);
-    if (o < room) __stcs(reinterpret_cast<ulonglong2 *>(table + (g.base + j * g.region) * 8) + o, r);
-    else over = true;
+  for (uint64_t g0 = (uint64_t)blockIdx.x * (TPB / 32) + (threadIdx.x >> 5); g0 < total; g0 += nwarps * SPLIT2_U) {
+    ulonglong2 r[SPLIT2_U];
+    unsigned bk[SPLIT2_U];
+    #pragma unroll
+    for (int u = 0; u < SPLIT2_U; ++u) {
+      const uint64_t run = g0 + (uint64_t)u * nwarps;
+      bk[u] = (unsigned)(run % NBUCKET);
+      const uint64_t i = (run / NBUCKET) * 32 + lane;
+      r[u] = make_ulonglong2(0ull, 0ull);
+      if (run < total && i < min((unsigned long long)cap, bucket_cnt[bk[u]])) r[u] = __ldcs(records + (uint64_t)bk[u] * cap + i);
+    }
+    unsigned long long o[SPLIT2_U];
+    uint64_t j[SPLIT2_U];
+    #pragma unroll
+    for (int u = 0; u < SPLIT2_U; ++u) {
+      if (r[u].x == 0ull) continue;   /* past the bucket's end, or an unused chunk tail */
+      /* the partition: the bucket, then the hash bits right below it (the record's top bits) */
+      j[u] = ((uint64_t)bk[u] << sbits) | (sbits ? (r[u].x >> (64 - sbits)) : 0ull);
+      o[u] = atomicAdd(&sub_cnt[j[u]], 1ull);
+    }
+    #pragma unroll
+    for (int u = 0; u < SPLIT2_U; ++u) {
+      if (r[u].x == 0ull) continue;
+      if (o[u] < room) __stcs(reinterpret_cast<ulonglong2 *>(table + (g.base + j[u] * g.region) * 8) + o[u], r[u]);
+      else over = true;
+    }
   }
   if (over) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
 }
@@ -2955,11 +2977,12 @@ bruno_status count_partitioned_w2(Ctx *c, bool &used) {
       cudaMemsetAsync(&c->dctr->n_cand, 0, sizeof(c->dctr->n_cand) + sizeof(c->dctr->quick_hist), c->stream);
     }
     cudaEventRecord(c->kev[2], c->stream);
-    const unsigned gx = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 8, (cap + TPB - 1) / TPB));
-    k_split_w2<<<dim3(gx, NBUCKET), TPB, 0, c->stream>>>((const ulonglong2 *)c->records.p,
-                                                         (const unsigned long long *)c->bucket_cnt.p, cap, c->geom,
-                                                         (uint64_t *)c->table.p, (unsigned long long *)c->sub_cnt.p,
-                                                         c->dctr);
+    const uint64_t runs = (cap + 31) / 32;   /* 32-record runs a bucket */
+    const unsigned gx = (unsigned)std::max<uint64_t>(
+        1, std::min<uint64_t>((uint64_t)sms * 8, (runs * NBUCKET + (TPB / 32) * SPLIT2_U - 1) / ((TPB / 32) * SPLIT2_U)));
+    k_split_w2<<<gx, TPB, 0, c->stream>>>((const ulonglong2 *)c->records.p, (const unsigned long long *)c->bucket_cnt.p,
+                                          cap, runs, c->geom, (uint64_t *)c->table.p,
+                                          (unsigned long long *)c->sub_cnt.p, c->dctr);
     cudaEventRecord(c->kev[4], c->stream);
     k_count_local2<<<(unsigned)(1ull << pb), PTPB2, (unsigned)(region * 64), c->stream>>>(
         (const unsigned long long *)c->sub_cnt.p, c->geom, (uint64_t *)c->table.p, ca, c->dctr);
