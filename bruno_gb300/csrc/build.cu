@@ -1871,11 +1871,12 @@ __global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, cons
 constexpr int MAX_SPLIT_BITS2 = 16;
 
 /* Warps take 32-record runs in order; the runs of a window of `win` buckets (a power of two)
- * are interleaved round robin over its buckets.  Within a window the atomics in flight spread
- * over every partition of `win` buckets instead of queueing on one bucket's few cursors, while
- * the scattered stores stay inside the window's share of the table (about 1 GB: a store
- * anywhere in a table of 100 GB measured 2.4 times slower).  Each thread keeps SPLIT2_U
- * records in flight. */
+ * are interleaved round robin over its buckets, so that the atomics in flight spread over at
+ * least 8192 partition cursors (a bucket of a small table has few partitions, and all warps
+ * queueing on them measured 8 times slower), while the scattered stores stay inside as small
+ * a share of the table as that allows (at large k one bucket: spreading them over two buckets'
+ * 0.85 GB measured 1.2 times slower, over the whole 109 GB table 2.4 times).  Each thread keeps
+ * SPLIT2_U records in flight. */
 constexpr int SPLIT2_U = 4;
 __global__ void __launch_bounds__(TPB) k_split_w2(const ulonglong2 *records, const unsigned long long *bucket_cnt,
                                                    uint64_t cap, uint64_t runs_per_bucket, uint32_t win, TableGeom g,
@@ -2982,9 +2983,9 @@ bruno_status count_partitioned_w2(Ctx *c, bool &used) {
     const uint64_t runs = (cap + 31) / 32;   /* 32-record runs a bucket */
     const unsigned gx = (unsigned)std::max<uint64_t>(
         1, std::min<uint64_t>((uint64_t)sms * 8, (runs * NBUCKET + (TPB / 32) * SPLIT2_U - 1) / ((TPB / 32) * SPLIT2_U)));
-    /* the bucket window: about 1 GB of table (a power of two of buckets, at least one) */
+    /* the bucket window: enough buckets for 8192 partition cursors (a power of two) */
     uint32_t win = 1;
-    while (win < NBUCKET && (uint64_t)(2 * win) * (c->nslots / NBUCKET) * 64 <= (1ull << 30)) win *= 2;
+    while (win < NBUCKET && ((uint64_t)win << (pb - NBUCKET_BITS)) < 8192) win *= 2;
     k_split_w2<<<gx, TPB, 0, c->stream>>>((const ulonglong2 *)c->records.p, (const unsigned long long *)c->bucket_cnt.p,
                                           cap, runs, win, c->geom, (uint64_t *)c->table.p,
                                           (unsigned long long *)c->sub_cnt.p, c->dctr);
