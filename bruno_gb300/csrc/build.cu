@@ -1684,29 +1684,31 @@ __device__ __forceinline__ uint64_t sm_cas128(uint32_t a, uint64_t cmp_lo, uint6
   return olo;
 }
 
-/* count_in_entries on a slot in shared memory, without branches per entry: the snapshot gives
- * the entry holding the code (entries fill in order, so it precedes every empty one) and the
- * empty entries; a lost claim reveals what took the entry.  A partition counted in shared
- * memory holds fewer than 2^24 records (the host sizes it so), so no count reaches E_BIG. */
+/* count_in_entries on a slot in shared memory */
 template <int NE>
 __device__ __forceinline__ bool sm_count_entries(uint32_t *e, const uint32_t *seen, unsigned code,
                                                  unsigned long long &claims) {
-  unsigned match = 0, empty = 0;
   #pragma unroll
   for (int i = 0; i < NE; ++i) {
-    match |= (seen[i] != 0 && entry_code(seen[i]) == code) ? (1u << i) : 0u;
-    empty |= seen[i] == 0 ? (1u << i) : 0u;
+    uint32_t w = seen[i];
+    if (w == 0) {
+      const uint32_t nw = (code << E_CODE_SHIFT) | (1u << E_COUNT_SHIFT);
+      const uint32_t old = atomicCAS(e + i, 0u, nw);
+      if (old == 0) { ++claims; return true; }
+      w = old;
+    }
+    if (entry_code(w) == code) {
+      if ((w >> E_COUNT_SHIFT) < (1u << 24) && !(w & E_BIG)) {
+        atomicAdd(e + i, 1u << E_COUNT_SHIFT);   /* result unused: a partition counted here holds
+                                                    fewer than 2^24 records, so this never reaches E_BIG */
+      } else {
+        const uint32_t old = atomicAdd(e + i, 1u << E_COUNT_SHIFT);
+        if (old >> 31) atomicOr(e + i, E_BIG);
+      }
+      return true;
+    }
   }
-  while (!match && empty) {
-    const int i = __ffs(empty) - 1;
-    const uint32_t old = atomicCAS(e + i, 0u, (code << E_CODE_SHIFT) | (1u << E_COUNT_SHIFT));
-    if (old == 0) { ++claims; return true; }
-    if (entry_code(old) == code) match = 1u << i;
-    empty &= ~(1u << i);
-  }
-  if (!match) return false;   /* every entry holds another code: the k-mer continues in a later slot */
-  atomicAdd(e + (__ffs(match) - 1), 1u << E_COUNT_SHIFT);
-  return true;
+  return false;
 }
 
 /* one record into the partition held in shared memory; false if the region is full */

@@ -606,6 +606,11 @@ bruno_status bruno_get_isolated(bruno_ctx *c, uint64_t *kmers, uint64_t *in_kmer
 }
 
 /* ------------------------------------------------------------------ batched form */
+/* dst[i] = src[idx[i]] */
+__global__ void k_gather_u64(const uint64_t *src, const uint64_t *idx, uint32_t n, uint64_t *dst) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[idx[i]];
+}
+
 bruno_status bruno_build_samples(bruno_ctx *c, const char *const *bufs, const size_t *nbytes, size_t n_samples,
                                  int32_t is_device) {
   if (!c || !bufs || !nbytes || n_samples == 0) return BRUNO_ERR_ARG;
@@ -726,10 +731,18 @@ bruno_status bruno_build_samples(bruno_ctx *c, const char *const *bufs, const si
   c->h_tally.assign((size_t)S * T_NUM, 0);
   st = cuda_check(c, cudaMemcpyAsync(c->h_tally.data(), c->s_tally.p, (size_t)S * T_NUM * 8, cudaMemcpyDeviceToHost,
                                      c->stream), "tallies");
-  std::vector<uint64_t> off(c->n_heads + 1, 0);
-  if (st == BRUNO_OK)
-    st = cuda_check(c, cudaMemcpyAsync(off.data(), c->head_off.p, (c->n_heads + 1) * 8, cudaMemcpyDeviceToHost,
-                                       c->stream), "chain offsets");
+  /* each sample's first chain character: the chain offsets at the samples' first chains,
+   * gathered on the device (S + 1 values rather than every chain's offset) */
+  std::vector<uint64_t> off(S + 1, 0);
+  if (st == BRUNO_OK) st = ensure(c, c->fr_tmp, (size_t)(S + 1) * 16);
+  if (st == BRUNO_OK) {
+    uint64_t *d = (uint64_t *)c->fr_tmp.p;
+    cudaMemcpyAsync(d, c->h_head0.data(), (size_t)(S + 1) * 8, cudaMemcpyHostToDevice, c->stream);
+    k_gather_u64<<<(S + 1 + 255) / 256, 256, 0, c->stream>>>((const uint64_t *)c->head_off.p, d, S + 1, d + S + 1);
+    c->launches += 1;
+    st = cuda_check(c, cudaMemcpyAsync(off.data(), d + S + 1, (size_t)(S + 1) * 8, cudaMemcpyDeviceToHost, c->stream),
+                    "chain offsets");
+  }
   if (st == BRUNO_OK) st = cuda_check(c, cudaStreamSynchronize(c->stream), "tallies");
   if (st != BRUNO_OK) return st;
   c->h_iter.assign(S, 0);
@@ -742,7 +755,7 @@ bruno_status bruno_build_samples(bruno_ctx *c, const char *const *bufs, const si
     c->h_iter[q] = it;
     t[T_RANKED] = c->h_rank0[q + 1] - c->h_rank0[q];
     t[T_HEADS] = c->h_head0[q + 1] - c->h_head0[q];
-    t[T_CHARS] = off[c->h_head0[q + 1]] - off[c->h_head0[q]];
+    t[T_CHARS] = off[q + 1] - off[q];
   }
   return BRUNO_OK;
 }
