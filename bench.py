@@ -59,6 +59,10 @@ def parse_args():
     ap.add_argument("--e2e-workers", type=int, default=0,
                     help="e2e through a pool of this many contexts (bruno_pool_*), so that one step's host "
                          "copy overlaps the previous step's device work; 0 = one context, steps in turn")
+    ap.add_argument("--part-slots", type=int, default=0,
+                    help="largest shared-memory partition region in slots (0 = the library's 3072)")
+    ap.add_argument("--count-threads", type=int, default=0, choices=[0, 256, 512, 1024],
+                    help="threads of the shared-memory counting block (0 = the library's 512)")
     ap.add_argument("--max-load", type=float, default=0.0,
                     help="target k-mer table load (0 = the library's 0.5; the large-k workload uses 0.7 so "
                          "its 64-byte slots fit the device)")
@@ -392,7 +396,8 @@ def main():
 
     max_load = args.max_load or (0.7 if w.k > 31 else 0.5)
     g = bg.Graph(k=w.k, thresh=bg.thresholds(w.lower), min_update=True, device=local, max_load=max_load,
-                 h2d_streams=args.h2d_streams, h2d_chunk=args.h2d_chunk, rank_fill=args.rank_fill)
+                 h2d_streams=args.h2d_streams, h2d_chunk=args.h2d_chunk, rank_fill=args.rank_fill,
+                 part_slots=args.part_slots, count_threads=args.count_threads)
     g.set_stream(stream.cuda_stream)
 
     def step_device():
@@ -550,7 +555,8 @@ def main():
                 "config": workload_config(w),
                 "run": {"api": "bruno_build_and_compact" if args.api == "build" else "step calls",
                         "h2d_streams": args.h2d_streams, "h2d_chunk": args.h2d_chunk or 256 << 20,
-                        "rank_fill": args.rank_fill, "max_load": max_load},
+                        "rank_fill": args.rank_fill, "max_load": max_load,
+                        "part_slots": args.part_slots or 3072, "count_threads": args.count_threads or 512},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n, "d2h_bytes_per_step": d2h,
                         "ms_per_step": ems / args.steps,
                         "h2d_ms": statistics.mean(p["h2d"] for p in e2e_phases) if e2e_phases else None,
