@@ -1820,22 +1820,24 @@ __global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, cons
       if (q < region) {
         const uint64_t key = sm[q * 4];
         if (key != KEY_EMPTY && !(key & KEY_CONT)) {   /* a continuation belongs to its first slot */
-          /* one pass: entries, the k-mer's total, and the entries outside the k+2 bounds */
-          int ne = 0, nout = 0;
+          int ne = 0;
           uint32_t kf = 0;
           #pragma unroll
           for (int e = 0; e < 6; ++e) {
             const uint32_t w = (uint32_t)(sm[q * 4 + 1 + e / 2] >> (32 * (e & 1)));
-            const uint32_t c = entry_count(w), c16 = min(0xFFFFu, c);
             ne += w != 0;
-            kf += c;
-            nout += (w != 0 && (c16 < ca.t[4] || c16 >= ca.t[5]));
+            kf += entry_count(w);
           }
           kf = min(0xFFFFu, kf);
           listed = ne == 6 || kf >= ca.t[2];
           if (!listed) {
             const uint32_t kout = (kf < ca.t[0] || kf >= ca.t[1]) ? 2u : 0u;
-            qh += ((uint64_t)(ne - nout) << (16 * kout)) + ((uint64_t)nout << (16 * (kout | 1u)));
+            #pragma unroll
+            for (int e = 0; e < 6; ++e) {
+              const uint32_t w = (uint32_t)(sm[q * 4 + 1 + e / 2] >> (32 * (e & 1)));
+              const uint32_t c16 = min(0xFFFFu, entry_count(w));
+              if (w) qh += 1ull << (16 * (kout | ((c16 < ca.t[4] || c16 >= ca.t[5]) ? 1u : 0u)));
+            }
           }
         }
       }
@@ -2013,21 +2015,24 @@ __global__ void __launch_bounds__(PTPB2, 3) k_count_local2(const unsigned long l
       if (q < region) {
         const uint64_t k0 = sm[q * 8], k1 = sm[q * 8 + 1];
         if (!(k0 == KEY_EMPTY && k1 == KEY_EMPTY) && !(k1 & KEY_CONT)) {
-          int ne = 0, nout = 0;
+          int ne = 0;
           uint32_t kf = 0;
           #pragma unroll
           for (int e = 0; e < 12; ++e) {
             const uint32_t w = (uint32_t)(sm[q * 8 + 2 + e / 2] >> (32 * (e & 1)));
-            const uint32_t c = entry_count(w), c16 = min(0xFFFFu, c);
             ne += w != 0;
-            kf += c;
-            nout += (w != 0 && (c16 < ca.t[4] || c16 >= ca.t[5]));
+            kf += entry_count(w);
           }
           kf = min(0xFFFFu, kf);
           listed = ne == 12 || kf >= ca.t[2];
           if (!listed) {
             const uint32_t kout = (kf < ca.t[0] || kf >= ca.t[1]) ? 2u : 0u;
-            qh += ((uint64_t)(ne - nout) << (16 * kout)) + ((uint64_t)nout << (16 * (kout | 1u)));
+            #pragma unroll
+            for (int e = 0; e < 12; ++e) {
+              const uint32_t w = (uint32_t)(sm[q * 8 + 2 + e / 2] >> (32 * (e & 1)));
+              const uint32_t c16 = min(0xFFFFu, entry_count(w));
+              if (w) qh += 1ull << (16 * (kout | ((c16 < ca.t[4] || c16 >= ca.t[5]) ? 1u : 0u)));
+            }
           }
         }
       }
