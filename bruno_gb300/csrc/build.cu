@@ -1757,14 +1757,24 @@ struct CandArgs {
 /* One CTA per partition (blockIdx.x counts the partitions of all samples): clear the slots, count
  * the partition's records into them, write the region back.  Partition j of sample s holds the
  * records whose mix has j in its top pbits bits: the bucket (top 8) and the split bits. */
+/* the partitions of one launch of k_count_local, as runs of whole samples: the sample whose
+ * partitions start at global partition pbase is the launch's partitions [run, run + 2^pbits) */
+struct ClassRun { uint32_t run, pbase; };
+
 __global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, const unsigned long long *rec_cnt,
-                                                       const SGeom *sg, uint32_t nsamples, const uint32_t *plist,
-                                                       uint64_t *table, unsigned long long *s_tally, CandArgs ca,
-                                                       DevCounters *ctr) {
+                                                       const SGeom *sg, uint32_t nsamples, const ClassRun *cls,
+                                                       uint32_t ncls, uint64_t *table, unsigned long long *s_tally,
+                                                       CandArgs ca, DevCounters *ctr) {
   extern __shared__ __align__(16) uint64_t sm[];
-  /* plist: the partitions of one launch (a batch launches its partitions by region size, each
-   * launch with the shared memory its largest region needs); NULL = partition blockIdx.x */
-  const uint64_t part = plist ? plist[blockIdx.x] : blockIdx.x;
+  /* cls: a batch launches its partitions by region size (each launch with the shared memory its
+   * largest region needs), as runs of samples; NULL = partition blockIdx.x */
+  uint32_t part = blockIdx.x;
+  if (cls) {
+    uint32_t lo = 0, hi = ncls;
+    while (hi - lo > 1) { const uint32_t m = (lo + hi) >> 1; if (__ldg(&cls[m].run) <= blockIdx.x) lo = m; else hi = m; }
+    const ClassRun r = cls[lo];
+    part = r.pbase + (blockIdx.x - r.run);
+  }
   const uint32_t smp = sample_of_part(sg, nsamples, part);
   const SGeom G = sg[smp];
   const uint64_t j = part - G.pbase;
@@ -2703,35 +2713,38 @@ bruno_status split_and_count(Ctx *c, std::vector<SGeom> &sg, const std::vector<u
   }
   if (S == 1) {
     k_count_local<<<(unsigned)nparts, count_threads(c), (unsigned)(region_max * 32), c->stream>>>(
-        recs, cnts, (const SGeom *)c->sgeom.p, S, nullptr, (uint64_t *)c->table.p, s_tally, ca, c->dctr);
+        recs, cnts, (const SGeom *)c->sgeom.p, S, nullptr, 0, (uint64_t *)c->table.p, s_tally, ca, c->dctr);
     c->launches += 1;
   } else {
-    /* partitions grouped by region size: a launch per group, with shared memory for its largest */
-    static const uint64_t bound[4] = {256, 768, 1536, ~0ull};
-    std::vector<uint32_t> plist;
+    /* partitions grouped by region size: a launch per class, with shared memory for its largest
+     * region (classes a factor of about 1.5 apart, so no region reserves much more than it uses) */
+    static const uint64_t bound[] = {128, 192, 256, 384, 512, 768, 1024, 1536, 2048, ~0ull};
+    constexpr int NCL = sizeof(bound) / sizeof(bound[0]);
+    std::vector<ClassRun> runs;
     std::vector<size_t> at{0};
-    std::vector<uint64_t> rmax;
-    for (int cl = 0; cl < 4; ++cl) {
-      uint64_t m = 0;
+    std::vector<uint64_t> rmax, nparts_cl;
+    for (int cl = 0; cl < NCL; ++cl) {
+      uint64_t m = 0, n = 0;
       for (uint32_t q = 0; q < S; ++q) {
         const uint64_t r = sg[q].g.region;
         if (r > bound[cl] || (cl > 0 && r <= bound[cl - 1])) continue;
-        for (uint64_t j = 0; j < (1ull << sg[q].g.pbits); ++j) plist.push_back((uint32_t)(sg[q].pbase + j));
+        runs.push_back(ClassRun{(uint32_t)n, (uint32_t)sg[q].pbase});
+        n += 1ull << sg[q].g.pbits;
         m = std::max(m, r);
       }
-      at.push_back(plist.size());
+      at.push_back(runs.size());
       rmax.push_back(m);
+      nparts_cl.push_back(n);
     }
-    if ((st = ensure(c, c->grp_tmp, plist.size() * 4 + 16)) != BRUNO_OK) return st;
-    if ((st = cuda_check(c, cudaMemcpyAsync(c->grp_tmp.p, plist.data(), plist.size() * 4, cudaMemcpyHostToDevice,
-                                            c->stream), "partition lists")) != BRUNO_OK)
+    if ((st = ensure(c, c->grp_tmp, runs.size() * sizeof(ClassRun) + 16)) != BRUNO_OK) return st;
+    if ((st = cuda_check(c, cudaMemcpyAsync(c->grp_tmp.p, runs.data(), runs.size() * sizeof(ClassRun),
+                                            cudaMemcpyHostToDevice, c->stream), "partition classes")) != BRUNO_OK)
       return st;
-    for (int cl = 0; cl < 4; ++cl) {
-      const size_t n = at[cl + 1] - at[cl];
-      if (!n) continue;
-      k_count_local<<<(unsigned)n, count_threads(c), (unsigned)(rmax[cl] * 32), c->stream>>>(
-          recs, cnts, (const SGeom *)c->sgeom.p, S, (const uint32_t *)c->grp_tmp.p + at[cl], (uint64_t *)c->table.p,
-          s_tally, ca, c->dctr);
+    for (int cl = 0; cl < NCL; ++cl) {
+      if (!nparts_cl[cl]) continue;
+      k_count_local<<<(unsigned)nparts_cl[cl], count_threads(c), (unsigned)(rmax[cl] * 32), c->stream>>>(
+          recs, cnts, (const SGeom *)c->sgeom.p, S, (const ClassRun *)c->grp_tmp.p + at[cl],
+          (uint32_t)(at[cl + 1] - at[cl]), (uint64_t *)c->table.p, s_tally, ca, c->dctr);
       c->launches += 1;
     }
   }
