@@ -503,12 +503,12 @@ def main():
     elif sizes["table_partitions"] > 1:
         # k > 31, partitioned (128-bit keys, 16-byte records, 64-byte slots):
         #   k_extract      FASTQ bytes + 16 B read span per read read once, 16 B per record written
-        #   k_split_w2     16 B per record read and written once (into its partition's region)
+        #   k_split_scatter 16 B per record read and written once (into its partition's region)
         #   k_count_local2 16 B per record read once + 64 B per slot written once + 4 B per listed slot
         #   k_filter       64 B per slot it reads + 64 B per graph node written once
         kern = {
             "k_extract": (n + 16 * sizes["n_reads"] + 16 * inst_step, mean("count_estimate")),
-            "k_split_w2": (32 * inst_step, mean("count_split")),
+            "k_split_scatter": (32 * inst_step, mean("count_split")),
             "k_count_local2": (16 * inst_step + 64 * slots + 4 * listed, mean("count_insert") - mean("count_split")),
             "k_filter": (64 * listed + 64 * sizes["n_nodes"], mean("filter_insert")),
         }

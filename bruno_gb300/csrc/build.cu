@@ -1882,17 +1882,35 @@ __global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, cons
  * counted region over them, so the records need no second buffer. */
 constexpr int MAX_SPLIT_BITS2 = 16;
 
-/* Warps take 32-record runs in order; the runs of a window of `win` buckets (a power of two)
- * are interleaved round robin over its buckets, so that the atomics in flight spread over at
- * least 8192 partition cursors (a bucket of a small table has few partitions, and all warps
- * queueing on them measured 8 times slower), while the scattered stores stay inside as small
- * a share of the table as that allows (at large k one bucket: spreading them over two buckets'
- * 0.85 GB measured 1.2 times slower, over the whole 109 GB table 2.4 times).  Each thread keeps
- * SPLIT2_U records in flight. */
+/* The scatter split (k > 31 always; k <= 31 when a table needs more partitions than k_split's
+ * shared-memory counting sort handles): every record goes straight to the memory of its own
+ * partition's slot region, four records a slot.  Warps take 32-record runs in order; the runs of
+ * a window of `win` buckets (a power of two) are interleaved round robin over its buckets, so
+ * that the atomics in flight spread over at least 8192 partition cursors (a bucket of a small
+ * table has few partitions, and all warps queueing on them measured 8 times slower), while the
+ * scattered stores stay inside as small a share of the table as that allows (at large k one
+ * bucket: spreading them over two buckets' 0.85 GB measured 1.2 times slower, over the whole
+ * 109 GB table 2.4 times).  Each thread keeps SPLIT2_U records in flight. */
+template <class KT> struct ScatterRec;
+template <> struct ScatterRec<KW1> {   /* [low 54 bits of the mix | code:5] */
+  using T = uint64_t;
+  __device__ static __forceinline__ bool none(T r) { return r == 0ull; }
+  __device__ static __forceinline__ uint64_t sub(T r, int sbits) { return sbits ? (r >> (5 + LOW_BITS - sbits)) : 0ull; }
+};
+template <> struct ScatterRec<KW2> {   /* x = (H << 8) | code, y = high word */
+  using T = ulonglong2;
+  __device__ static __forceinline__ bool none(T r) { return r.x == 0ull; }
+  __device__ static __forceinline__ uint64_t sub(T r, int sbits) { return sbits ? (r.x >> (64 - sbits)) : 0ull; }
+};
 constexpr int SPLIT2_U = 4;
-__global__ void __launch_bounds__(TPB) k_split_w2(const ulonglong2 *records, const unsigned long long *bucket_cnt,
-                                                   uint64_t cap, uint64_t runs_per_bucket, uint32_t win, TableGeom g,
-                                                   uint64_t *table, unsigned long long *sub_cnt, DevCounters *ctr) {
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_split_scatter(const typename ScatterRec<KT>::T *records,
+                                                        const unsigned long long *bucket_cnt, uint64_t cap,
+                                                        uint64_t runs_per_bucket, uint32_t win, TableGeom g,
+                                                        uint64_t *table, unsigned long long *sub_cnt, DevCounters *ctr) {
+  using R = ScatterRec<KT>;
+  using T = typename R::T;
+  constexpr int SU = Slot<KT>::U64;
   const int sbits = g.pbits - NBUCKET_BITS;
   const uint64_t room = 4 * g.region;
   const int lane = threadIdx.x & 31;
@@ -1900,7 +1918,7 @@ __global__ void __launch_bounds__(TPB) k_split_w2(const ulonglong2 *records, con
   const uint64_t total = runs_per_bucket * NBUCKET;
   bool over = false;
   for (uint64_t g0 = (uint64_t)blockIdx.x * (TPB / 32) + (threadIdx.x >> 5); g0 < total; g0 += nwarps * SPLIT2_U) {
-    ulonglong2 r[SPLIT2_U];
+    T r[SPLIT2_U];
     unsigned bk[SPLIT2_U];
     #pragma unroll
     for (int u = 0; u < SPLIT2_U; ++u) {
@@ -1908,26 +1926,33 @@ __global__ void __launch_bounds__(TPB) k_split_w2(const ulonglong2 *records, con
       const uint64_t per_win = runs_per_bucket * win, w = run / per_win, rr = run % per_win;
       bk[u] = (unsigned)(w * win + rr % win);
       const uint64_t i = (rr / win) * 32 + lane;
-      r[u] = make_ulonglong2(0ull, 0ull);
+      r[u] = T{};
       if (run < total && i < min((unsigned long long)cap, bucket_cnt[bk[u]])) r[u] = __ldcs(records + (uint64_t)bk[u] * cap + i);
     }
     unsigned long long o[SPLIT2_U];
     uint64_t j[SPLIT2_U];
     #pragma unroll
     for (int u = 0; u < SPLIT2_U; ++u) {
-      if (r[u].x == 0ull) continue;   /* past the bucket's end, or an unused chunk tail */
-      /* the partition: the bucket, then the hash bits right below it (the record's top bits) */
-      j[u] = ((uint64_t)bk[u] << sbits) | (sbits ? (r[u].x >> (64 - sbits)) : 0ull);
+      if (R::none(r[u])) continue;   /* past the bucket's end, or an unused chunk tail */
+      /* the partition: the bucket, then the mix bits right below it */
+      j[u] = ((uint64_t)bk[u] << sbits) | R::sub(r[u], sbits);
       o[u] = atomicAdd(&sub_cnt[j[u]], 1ull);
     }
     #pragma unroll
     for (int u = 0; u < SPLIT2_U; ++u) {
-      if (r[u].x == 0ull) continue;
-      if (o[u] < room) __stcs(reinterpret_cast<ulonglong2 *>(table + (g.base + j[u] * g.region) * 8) + o[u], r[u]);
+      if (R::none(r[u])) continue;
+      if (o[u] < room) __stcs(reinterpret_cast<T *>(table + (g.base + j[u] * g.region) * SU) + o[u], r[u]);
       else over = true;
     }
   }
   if (over) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
+}
+
+/* the bucket window of the scatter split: enough buckets for 8192 partition cursors */
+uint32_t scatter_window(int pbits) {
+  uint32_t win = 1;
+  while (win < NBUCKET && ((uint64_t)win << (pbits - NBUCKET_BITS)) < 8192) win *= 2;
+  return win;
 }
 
 /* one record into a 64-byte slot region in shared memory (key 2 words, 12 entry words);
@@ -1973,7 +1998,7 @@ __device__ __forceinline__ bool sm_count2(uint64_t *sm, uint32_t sm_base, uint32
 }
 
 /* One CTA per partition j: clear its slots in shared memory, count its records (read from the
- * region's own memory, where k_split_w2 put them), write the region back over them; with
+ * region's own memory, where k_split_scatter put them), write the region back over them; with
  * thresholds, list the slots the filter must read, as k_count_local does.  512 threads a CTA,
  * bounded to 40 registers so that three CTAs share an SM. */
 constexpr int PTPB2 = 512;
@@ -2754,6 +2779,46 @@ bruno_status split_and_count(Ctx *c, std::vector<SGeom> &sg, const std::vector<u
   return BRUNO_OK;
 }
 
+/* k <= 31 with more partitions than k_split handles: the bucket records scattered into their
+ * partitions' table regions (k_split_scatter), then k_count_local reads each partition's records
+ * from its own region (the sample's record base 0 and capacity four records a slot, in units of
+ * slots' words) before it writes the counted region over them */
+bruno_status scatter_and_count(Ctx *c, uint64_t cap) {
+  bruno_status st;
+  const int pb = c->geom.pbits;
+  const uint64_t region = c->geom.region;
+  if ((st = ensure(c, c->sub_cnt, (size_t)8 << pb)) != BRUNO_OK) return st;
+  cudaMemsetAsync(c->sub_cnt.p, 0, (size_t)8 << pb, c->stream);
+  const SGeom sg{c->geom, 0, 0, 4 * region};
+  if ((st = ensure(c, c->sgeom, sizeof(SGeom))) != BRUNO_OK) return st;
+  cudaMemcpyAsync(c->sgeom.p, &sg, sizeof(SGeom), cudaMemcpyHostToDevice, c->stream);
+  CandArgs ca{};
+  if (c->cfg.thresholding && !c->cfg.edge_filter) {
+    if ((st = ensure(c, c->cand, c->nslots * 4)) != BRUNO_OK) return st;
+    ca.cand = (uint32_t *)c->cand.p;
+    ca.cap = c->nslots;
+    ca.n_cand = &c->dctr->n_cand;
+    ca.quick_hist = c->dctr->quick_hist;
+    for (int i = 0; i < 6; ++i) ca.t[i] = c->cfg.thresh[i];
+    cudaMemsetAsync(&c->dctr->n_cand, 0, sizeof(c->dctr->n_cand) + sizeof(c->dctr->quick_hist), c->stream);
+  }
+  const int sms = num_sms();
+  const uint64_t runs = (cap + 31) / 32;
+  const unsigned gx = (unsigned)std::max<uint64_t>(
+      1, std::min<uint64_t>((uint64_t)sms * 8, (runs * NBUCKET + (TPB / 32) * SPLIT2_U - 1) / ((TPB / 32) * SPLIT2_U)));
+  k_split_scatter<KW1><<<gx, TPB, 0, c->stream>>>((const uint64_t *)c->records.p,
+                                                  (const unsigned long long *)c->bucket_cnt.p, cap, runs,
+                                                  scatter_window(pb), c->geom, (uint64_t *)c->table.p,
+                                                  (unsigned long long *)c->sub_cnt.p, c->dctr);
+  cudaEventRecord(c->kev[4], c->stream);
+  k_count_local<<<(unsigned)(1ull << pb), count_threads(c), (unsigned)(region * 32), c->stream>>>(
+      (const uint64_t *)c->table.p, (const unsigned long long *)c->sub_cnt.p, (const SGeom *)c->sgeom.p, 1, nullptr, 0,
+      (uint64_t *)c->table.p, nullptr, ca, c->dctr);
+  c->launches += 2;
+  c->have_cand = ca.cand != nullptr;
+  return cuda_check(c, cudaGetLastError(), "k_count_local");
+}
+
 /* after a counting pass without overflow: the listed slots and the quick drops' tallies */
 void take_candidates(Ctx *c) {
   if (!c->have_cand) return;
@@ -2839,9 +2904,10 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
   }();
   (void)part_attr;
   for (int attempt = 0; attempt < 4; ++attempt) {
-    /* shared-memory path: 2^pb partitions (pb >= 8) small enough for one CTA's shared memory */
+    /* shared-memory path: 2^pb partitions (pb >= 8) small enough for one CTA's shared memory;
+     * past k_split's 8 + MAX_SPLIT_BITS bits the records are scattered into the table instead */
     int pb = NBUCKET_BITS;
-    while (pb < NBUCKET_BITS + MAX_SPLIT_BITS && (slots + (1ull << pb) - 1) >> pb > part_slots(c)) ++pb;
+    while (pb < NBUCKET_BITS + MAX_SPLIT_BITS2 && (slots + (1ull << pb) - 1) >> pb > part_slots(c)) ++pb;
     const uint64_t region_c = std::max<uint64_t>(64, (slots + (1ull << pb) - 1) >> pb);
     bool counted = false, counted_local = false;
     cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
@@ -2854,9 +2920,15 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
       if ((st = table_room(c, c->nslots)) != BRUNO_OK) return st;
       if ((st = ensure(c, c->table, c->nslots * 32)) != BRUNO_OK) return st;
       cudaEventRecord(c->kev[2], c->stream);
-      std::vector<SGeom> sg{SGeom{c->geom, 0, 0, 0}};
       bool ok = false;
-      if ((st = split_and_count(c, sg, std::vector<uint64_t>{cap}, ok, nullptr)) != BRUNO_OK) return st;
+      if (pb <= NBUCKET_BITS + MAX_SPLIT_BITS) {
+        std::vector<SGeom> sg{SGeom{c->geom, 0, 0, 0}};
+        if ((st = split_and_count(c, sg, std::vector<uint64_t>{cap}, ok, nullptr)) != BRUNO_OK) return st;
+      } else if ((st = scatter_and_count(c, cap)) != BRUNO_OK) {
+        return st;
+      } else {
+        ok = true;
+      }
       if (ok) {
         cudaEventRecord(c->kev[3], c->stream);
         counted = counted_local = true;
@@ -2998,12 +3070,10 @@ bruno_status count_partitioned_w2(Ctx *c, bool &used) {
     const uint64_t runs = (cap + 31) / 32;   /* 32-record runs a bucket */
     const unsigned gx = (unsigned)std::max<uint64_t>(
         1, std::min<uint64_t>((uint64_t)sms * 8, (runs * NBUCKET + (TPB / 32) * SPLIT2_U - 1) / ((TPB / 32) * SPLIT2_U)));
-    /* the bucket window: enough buckets for 8192 partition cursors (a power of two) */
-    uint32_t win = 1;
-    while (win < NBUCKET && ((uint64_t)win << (pb - NBUCKET_BITS)) < 8192) win *= 2;
-    k_split_w2<<<gx, TPB, 0, c->stream>>>((const ulonglong2 *)c->records.p, (const unsigned long long *)c->bucket_cnt.p,
-                                          cap, runs, win, c->geom, (uint64_t *)c->table.p,
-                                          (unsigned long long *)c->sub_cnt.p, c->dctr);
+    k_split_scatter<KW2><<<gx, TPB, 0, c->stream>>>((const ulonglong2 *)c->records.p,
+                                                    (const unsigned long long *)c->bucket_cnt.p, cap, runs,
+                                                    scatter_window(pb), c->geom, (uint64_t *)c->table.p,
+                                                    (unsigned long long *)c->sub_cnt.p, c->dctr);
     cudaEventRecord(c->kev[4], c->stream);
     k_count_local2<<<(unsigned)(1ull << pb), PTPB2, (unsigned)(region * 64), c->stream>>>(
         (const unsigned long long *)c->sub_cnt.p, c->geom, (uint64_t *)c->table.p, ca, c->dctr);

@@ -324,6 +324,20 @@ def test_edge_filter_workload_parity():
         compare(gpu_run(fq, 31, True, thr, mu, edge_filter=True), ref)
 
 
+@pytest.mark.parametrize("k", [31, 63])
+def test_scatter_split_parity(k):
+    """tables with more partitions than the shared-memory split handles: an explicit 80M-slot
+    table of partitions of at most 256 slots (2^19 of them at k = 31) on a 1 Mbp genome, whose
+    records are scattered straight into their partitions' table regions"""
+    w = synth.WORKLOADS["plain-small"]
+    fq = synth.make_fastq(w)
+    thr = bg.thresholds(w.lower)
+    ref = oracle.run(fq, k=k, thresh=thr, min_update=True, threads=16, keep_k2=True, keep_filtered=True)
+    got = gpu_run(fq, k, True, thr, True, table_slots=80_000_000, part_slots=256)
+    assert got["sizes"]["table_partitions"] > 1 << 18
+    compare(got, ref)
+
+
 def test_edge_filter_rejects_large_k():
     with pytest.raises(bg.BrunoError):
         bg.Graph(k=33, thresh=bg.thresholds([2]), edge_filter=True)
