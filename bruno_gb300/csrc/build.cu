@@ -1097,8 +1097,9 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, c
   if (tid == 0) S.overflow = 0;
   __syncthreads();
   const uint64_t nit = items ? n_items : (r1 - r0 + item_reads - 1) / item_reads;
-  const uint64_t per = (nit + gridDim.x - 1) / gridDim.x;
-  const uint64_t it0 = min(nit, (uint64_t)blockIdx.x * per), it1 = min(nit, it0 + per);
+  /* block b takes items [b * nit / grid, (b + 1) * nit / grid): every block gets the floor or
+   * the ceiling of the mean, so the one wave of blocks ends together */
+  const uint64_t it0 = (uint64_t)blockIdx.x * nit / gridDim.x, it1 = ((uint64_t)blockIdx.x + 1) * nit / gridDim.x;
   unsigned cur_s = ~0u;
   XSample xs{};
   unsigned long long inst_all = 0, used_all = 0;
@@ -2828,7 +2829,7 @@ void take_candidates(Ctx *c) {
 
 /* blocks of one extraction launch over nr reads (at most 2 per SM, at least one item of WX_ITEM
  * reads each) */
-constexpr uint32_t WX_ITEM = XTPB * 4;
+constexpr uint32_t WX_ITEM = XTPB;   /* one read a thread: fine enough to even out the blocks */
 int wx_blocks(uint64_t nr) {
   return (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)num_sms() * 2, (nr + WX_ITEM - 1) / WX_ITEM));
 }
@@ -3307,7 +3308,7 @@ bruno_status extract_samples(Ctx *c, uint32_t q0, uint32_t q1, const std::vector
     }
   if (items.empty()) return BRUNO_OK;
   const int eb = wx_blocks(f.back() - f.front());
-  const uint64_t per = std::max<uint64_t>(1, (items.size() + eb - 1) / eb);
+  const uint64_t per = std::max<uint64_t>(1, items.size() / eb);   /* the fewest items a block takes */
   std::vector<XSample> xs(q1 - q0);
   for (uint32_t q = q0; q < q1; ++q) {
     const uint64_t upper = (c->samp_off[q + 1] - c->samp_off[q]) / 2 + 1;   /* k-mer positions <= bytes / 2 */
