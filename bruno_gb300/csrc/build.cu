@@ -1891,7 +1891,9 @@ constexpr int MAX_SPLIT_BITS2 = 16;
  * table has few partitions, and all warps queueing on them measured 8 times slower), while the
  * scattered stores stay inside as small a share of the table as that allows (at large k one
  * bucket: spreading them over two buckets' 0.85 GB measured 1.2 times slower, over the whole
- * 109 GB table 2.4 times).  Each thread keeps SPLIT2_U records in flight. */
+ * 109 GB table 2.4 times).  Each thread keeps SPLIT2_U records in flight.  A bucket's runs are
+ * counted up to a power of two (2^lg_runs; the padding runs are empty), so that a run's bucket
+ * and place come from shifts, not from 64-bit divisions. */
 template <class KT> struct ScatterRec;
 template <> struct ScatterRec<KW1> {   /* [low 54 bits of the mix | code:5] */
   using T = uint64_t;
@@ -1907,8 +1909,8 @@ constexpr int SPLIT2_U = 4;
 template <class KT>
 __global__ void __launch_bounds__(TPB) k_split_scatter(const typename ScatterRec<KT>::T *records,
                                                         const unsigned long long *bucket_cnt, uint64_t cap,
-                                                        uint64_t runs_per_bucket, uint32_t win, TableGeom g,
-                                                        uint64_t *table, unsigned long long *sub_cnt, DevCounters *ctr) {
+                                                        int lg_runs, int lg_win, TableGeom g, uint64_t *table,
+                                                        unsigned long long *sub_cnt, DevCounters *ctr) {
   using R = ScatterRec<KT>;
   using T = typename R::T;
   constexpr int SU = Slot<KT>::U64;
@@ -1916,7 +1918,9 @@ __global__ void __launch_bounds__(TPB) k_split_scatter(const typename ScatterRec
   const uint64_t room = 4 * g.region;
   const int lane = threadIdx.x & 31;
   const uint64_t nwarps = (uint64_t)gridDim.x * (TPB / 32);
-  const uint64_t total = runs_per_bucket * NBUCKET;
+  const uint64_t total = (uint64_t)NBUCKET << lg_runs;
+  const int lg_per_win = lg_runs + lg_win;
+  const uint64_t win_mask = (1ull << lg_win) - 1, per_win_mask = (1ull << lg_per_win) - 1;
   bool over = false;
   for (uint64_t g0 = (uint64_t)blockIdx.x * (TPB / 32) + (threadIdx.x >> 5); g0 < total; g0 += nwarps * SPLIT2_U) {
     T r[SPLIT2_U];
@@ -1924,9 +1928,9 @@ __global__ void __launch_bounds__(TPB) k_split_scatter(const typename ScatterRec
     #pragma unroll
     for (int u = 0; u < SPLIT2_U; ++u) {
       const uint64_t run = g0 + (uint64_t)u * nwarps;
-      const uint64_t per_win = runs_per_bucket * win, w = run / per_win, rr = run % per_win;
-      bk[u] = (unsigned)(w * win + rr % win);
-      const uint64_t i = (rr / win) * 32 + lane;
+      const uint64_t w = run >> lg_per_win, rr = run & per_win_mask;
+      bk[u] = (unsigned)((w << lg_win) + (rr & win_mask));
+      const uint64_t i = ((rr >> lg_win) << 5) + lane;
       r[u] = T{};
       if (run < total && i < min((unsigned long long)cap, bucket_cnt[bk[u]])) r[u] = __ldcs(records + (uint64_t)bk[u] * cap + i);
     }
@@ -1949,11 +1953,29 @@ __global__ void __launch_bounds__(TPB) k_split_scatter(const typename ScatterRec
   if (over) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
 }
 
-/* the bucket window of the scatter split: enough buckets for 8192 partition cursors */
-uint32_t scatter_window(int pbits) {
-  uint32_t win = 1;
-  while (win < NBUCKET && ((uint64_t)win << (pbits - NBUCKET_BITS)) < 8192) win *= 2;
-  return win;
+/* the bucket window of the scatter split (log2): enough buckets for 8192 partition cursors */
+int scatter_lg_window(int pbits) {
+  int lg = 0;
+  while (lg < NBUCKET_BITS && (1ull << (lg + pbits - NBUCKET_BITS)) < 8192) ++lg;
+  return lg;
+}
+/* log2 of a bucket's 32-record runs, counted up to a power of two */
+int scatter_lg_runs(uint64_t cap) {
+  int lg = 0;
+  while ((1ull << lg) * 32 < cap) ++lg;
+  return lg;
+}
+int num_sms();
+/* blocks of the scatter split: one resident wave (no more than its warps' runs need) */
+template <class KT>
+unsigned scatter_blocks(int lg_runs) {
+  static const int occ = [] {
+    int o = 0;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_split_scatter<KT>, TPB, 0) == cudaSuccess && o > 0 ? o
+                                                                                                                : 4;
+  }();
+  const uint64_t runs = (uint64_t)NBUCKET << lg_runs, per_block = (TPB / 32) * SPLIT2_U;
+  return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)num_sms() * occ, (runs + per_block - 1) / per_block));
 }
 
 /* one record into a 64-byte slot region in shared memory (key 2 words, 12 entry words);
@@ -2803,14 +2825,10 @@ bruno_status scatter_and_count(Ctx *c, uint64_t cap) {
     for (int i = 0; i < 6; ++i) ca.t[i] = c->cfg.thresh[i];
     cudaMemsetAsync(&c->dctr->n_cand, 0, sizeof(c->dctr->n_cand) + sizeof(c->dctr->quick_hist), c->stream);
   }
-  const int sms = num_sms();
-  const uint64_t runs = (cap + 31) / 32;
-  const unsigned gx = (unsigned)std::max<uint64_t>(
-      1, std::min<uint64_t>((uint64_t)sms * 8, (runs * NBUCKET + (TPB / 32) * SPLIT2_U - 1) / ((TPB / 32) * SPLIT2_U)));
-  k_split_scatter<KW1><<<gx, TPB, 0, c->stream>>>((const uint64_t *)c->records.p,
-                                                  (const unsigned long long *)c->bucket_cnt.p, cap, runs,
-                                                  scatter_window(pb), c->geom, (uint64_t *)c->table.p,
-                                                  (unsigned long long *)c->sub_cnt.p, c->dctr);
+  const int lg_runs = scatter_lg_runs(cap);
+  k_split_scatter<KW1><<<scatter_blocks<KW1>(lg_runs), TPB, 0, c->stream>>>(
+      (const uint64_t *)c->records.p, (const unsigned long long *)c->bucket_cnt.p, cap, lg_runs, scatter_lg_window(pb),
+      c->geom, (uint64_t *)c->table.p, (unsigned long long *)c->sub_cnt.p, c->dctr);
   cudaEventRecord(c->kev[4], c->stream);
   k_count_local<<<(unsigned)(1ull << pb), count_threads(c), (unsigned)(region * 32), c->stream>>>(
       (const uint64_t *)c->table.p, (const unsigned long long *)c->sub_cnt.p, (const SGeom *)c->sgeom.p, 1, nullptr, 0,
@@ -3068,13 +3086,10 @@ bruno_status count_partitioned_w2(Ctx *c, bool &used) {
       cudaMemsetAsync(&c->dctr->n_cand, 0, sizeof(c->dctr->n_cand) + sizeof(c->dctr->quick_hist), c->stream);
     }
     cudaEventRecord(c->kev[2], c->stream);
-    const uint64_t runs = (cap + 31) / 32;   /* 32-record runs a bucket */
-    const unsigned gx = (unsigned)std::max<uint64_t>(
-        1, std::min<uint64_t>((uint64_t)sms * 8, (runs * NBUCKET + (TPB / 32) * SPLIT2_U - 1) / ((TPB / 32) * SPLIT2_U)));
-    k_split_scatter<KW2><<<gx, TPB, 0, c->stream>>>((const ulonglong2 *)c->records.p,
-                                                    (const unsigned long long *)c->bucket_cnt.p, cap, runs,
-                                                    scatter_window(pb), c->geom, (uint64_t *)c->table.p,
-                                                    (unsigned long long *)c->sub_cnt.p, c->dctr);
+    const int lg_runs = scatter_lg_runs(cap);
+    k_split_scatter<KW2><<<scatter_blocks<KW2>(lg_runs), TPB, 0, c->stream>>>(
+        (const ulonglong2 *)c->records.p, (const unsigned long long *)c->bucket_cnt.p, cap, lg_runs,
+        scatter_lg_window(pb), c->geom, (uint64_t *)c->table.p, (unsigned long long *)c->sub_cnt.p, c->dctr);
     cudaEventRecord(c->kev[4], c->stream);
     k_count_local2<<<(unsigned)(1ull << pb), PTPB2, (unsigned)(region * 64), c->stream>>>(
         (const unsigned long long *)c->sub_cnt.p, c->geom, (uint64_t *)c->table.p, ca, c->dctr);
