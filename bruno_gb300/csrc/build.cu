@@ -1891,7 +1891,10 @@ constexpr int MAX_SPLIT_BITS2 = 16;
  * table has few partitions, and all warps queueing on them measured 8 times slower), while the
  * scattered stores stay inside as small a share of the table as that allows (at large k one
  * bucket: spreading them over two buckets' 0.85 GB measured 1.2 times slower, over the whole
- * 109 GB table 2.4 times).  Each thread keeps SPLIT2_U records in flight.  A bucket's runs are
+ * 109 GB table 2.4 times).  The atomics on the window's cursors bound it, so it runs as many
+ * threads as an SM holds (24 registers, eight blocks of 256), each with SPLIT2_U records in
+ * flight (four records at 64 registers and half the threads measured 70 against 60 ms at large
+ * k).  A bucket's runs are
  * counted up to a power of two (2^lg_runs; the padding runs are empty), so that a run's bucket
  * and place come from shifts, not from 64-bit divisions. */
 template <class KT> struct ScatterRec;
@@ -1905,9 +1908,9 @@ template <> struct ScatterRec<KW2> {   /* x = (H << 8) | code, y = high word */
   __device__ static __forceinline__ bool none(T r) { return r.x == 0ull; }
   __device__ static __forceinline__ uint64_t sub(T r, int sbits) { return sbits ? (r.x >> (64 - sbits)) : 0ull; }
 };
-constexpr int SPLIT2_U = 4;
+constexpr int SPLIT2_U = 1;
 template <class KT>
-__global__ void __launch_bounds__(TPB) k_split_scatter(const typename ScatterRec<KT>::T *records,
+__global__ void __launch_bounds__(TPB, 8) k_split_scatter(const typename ScatterRec<KT>::T *records,
                                                         const unsigned long long *bucket_cnt, uint64_t cap,
                                                         int lg_runs, int lg_win, TableGeom g, uint64_t *table,
                                                         unsigned long long *sub_cnt, DevCounters *ctr) {
