@@ -1891,10 +1891,7 @@ constexpr int MAX_SPLIT_BITS2 = 16;
  * table has few partitions, and all warps queueing on them measured 8 times slower), while the
  * scattered stores stay inside as small a share of the table as that allows (at large k one
  * bucket: spreading them over two buckets' 0.85 GB measured 1.2 times slower, over the whole
- * 109 GB table 2.4 times).  The atomics on the window's cursors bound it, so it runs as many
- * threads as an SM holds (24 registers, eight blocks of 256), each with SPLIT2_U records in
- * flight (four records at 64 registers and half the threads measured 70 against 60 ms at large
- * k).  A bucket's runs are
+ * 109 GB table 2.4 times).  Each thread keeps SPLIT2_U records in flight.  A bucket's runs are
  * counted up to a power of two (2^lg_runs; the padding runs are empty), so that a run's bucket
  * and place come from shifts, not from 64-bit divisions. */
 template <class KT> struct ScatterRec;
@@ -1908,9 +1905,9 @@ template <> struct ScatterRec<KW2> {   /* x = (H << 8) | code, y = high word */
   __device__ static __forceinline__ bool none(T r) { return r.x == 0ull; }
   __device__ static __forceinline__ uint64_t sub(T r, int sbits) { return sbits ? (r.x >> (64 - sbits)) : 0ull; }
 };
-constexpr int SPLIT2_U = 1;
+constexpr int SPLIT2_U = 4;
 template <class KT>
-__global__ void __launch_bounds__(TPB, 8) k_split_scatter(const typename ScatterRec<KT>::T *records,
+__global__ void __launch_bounds__(TPB) k_split_scatter(const typename ScatterRec<KT>::T *records,
                                                         const unsigned long long *bucket_cnt, uint64_t cap,
                                                         int lg_runs, int lg_win, TableGeom g, uint64_t *table,
                                                         unsigned long long *sub_cnt, DevCounters *ctr) {
@@ -1968,7 +1965,40 @@ int scatter_lg_runs(uint64_t cap) {
   while ((1ull << lg) * 32 < cap) ++lg;
   return lg;
 }
+/* The scatter split bucket after bucket, for tables whose window is one bucket (large tables):
+ * grid row y is bucket y, its blocks stride over the bucket's records, one record a thread
+ * (measured 60 ms at large k against 70-73 for the windowed form above run on one bucket) */
+template <class KT>
+__global__ void __launch_bounds__(TPB) k_split_scatter_rows(const typename ScatterRec<KT>::T *records,
+                                                             const unsigned long long *bucket_cnt, uint64_t cap,
+                                                             TableGeom g, uint64_t *table, unsigned long long *sub_cnt,
+                                                             DevCounters *ctr) {
+  using R = ScatterRec<KT>;
+  using T = typename R::T;
+  constexpr int SU = Slot<KT>::U64;
+  const int sbits = g.pbits - NBUCKET_BITS;
+  const uint64_t room = 4 * g.region;
+  const unsigned b = blockIdx.y;
+  const uint64_t n = min((unsigned long long)cap, bucket_cnt[b]);
+  const T *rb = records + (uint64_t)b * cap;
+  bool over = false;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const T r = __ldcs(rb + i);
+    if (R::none(r)) continue;   /* an unused chunk tail */
+    const uint64_t j = ((uint64_t)b << sbits) | R::sub(r, sbits);
+    const unsigned long long o = atomicAdd(&sub_cnt[j], 1ull);
+    if (o < room) __stcs(reinterpret_cast<T *>(table + (g.base + j * g.region) * SU) + o, r);
+    else over = true;
+  }
+  if (over) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
+}
+
 int num_sms();
+/* the scatter split's launch: bucket after bucket when the window is one bucket, else windows */
+template <class KT>
+void launch_scatter(const typename ScatterRec<KT>::T *records, const unsigned long long *bucket_cnt, uint64_t cap,
+                    int pbits, TableGeom g, uint64_t *table, unsigned long long *sub_cnt, DevCounters *ctr,
+                    cudaStream_t s);
 /* blocks of the scatter split: one resident wave (no more than its warps' runs need) */
 template <class KT>
 unsigned scatter_blocks(int lg_runs) {
@@ -1979,6 +2009,21 @@ unsigned scatter_blocks(int lg_runs) {
   }();
   const uint64_t runs = (uint64_t)NBUCKET << lg_runs, per_block = (TPB / 32) * SPLIT2_U;
   return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)num_sms() * occ, (runs + per_block - 1) / per_block));
+}
+
+template <class KT>
+void launch_scatter(const typename ScatterRec<KT>::T *records, const unsigned long long *bucket_cnt, uint64_t cap,
+                    int pbits, TableGeom g, uint64_t *table, unsigned long long *sub_cnt, DevCounters *ctr,
+                    cudaStream_t s) {
+  const int lg_win = scatter_lg_window(pbits);
+  if (lg_win == 0) {
+    const unsigned gx = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)num_sms() * 8, (cap + TPB - 1) / TPB));
+    k_split_scatter_rows<KT><<<dim3(gx, NBUCKET), TPB, 0, s>>>(records, bucket_cnt, cap, g, table, sub_cnt, ctr);
+  } else {
+    const int lg_runs = scatter_lg_runs(cap);
+    k_split_scatter<KT><<<scatter_blocks<KT>(lg_runs), TPB, 0, s>>>(records, bucket_cnt, cap, lg_runs, lg_win, g, table,
+                                                                    sub_cnt, ctr);
+  }
 }
 
 /* one record into a 64-byte slot region in shared memory (key 2 words, 12 entry words);
@@ -2828,10 +2873,8 @@ bruno_status scatter_and_count(Ctx *c, uint64_t cap) {
     for (int i = 0; i < 6; ++i) ca.t[i] = c->cfg.thresh[i];
     cudaMemsetAsync(&c->dctr->n_cand, 0, sizeof(c->dctr->n_cand) + sizeof(c->dctr->quick_hist), c->stream);
   }
-  const int lg_runs = scatter_lg_runs(cap);
-  k_split_scatter<KW1><<<scatter_blocks<KW1>(lg_runs), TPB, 0, c->stream>>>(
-      (const uint64_t *)c->records.p, (const unsigned long long *)c->bucket_cnt.p, cap, lg_runs, scatter_lg_window(pb),
-      c->geom, (uint64_t *)c->table.p, (unsigned long long *)c->sub_cnt.p, c->dctr);
+  launch_scatter<KW1>((const uint64_t *)c->records.p, (const unsigned long long *)c->bucket_cnt.p, cap, pb, c->geom,
+                      (uint64_t *)c->table.p, (unsigned long long *)c->sub_cnt.p, c->dctr, c->stream);
   cudaEventRecord(c->kev[4], c->stream);
   k_count_local<<<(unsigned)(1ull << pb), count_threads(c), (unsigned)(region * 32), c->stream>>>(
       (const uint64_t *)c->table.p, (const unsigned long long *)c->sub_cnt.p, (const SGeom *)c->sgeom.p, 1, nullptr, 0,
@@ -3089,10 +3132,8 @@ bruno_status count_partitioned_w2(Ctx *c, bool &used) {
       cudaMemsetAsync(&c->dctr->n_cand, 0, sizeof(c->dctr->n_cand) + sizeof(c->dctr->quick_hist), c->stream);
     }
     cudaEventRecord(c->kev[2], c->stream);
-    const int lg_runs = scatter_lg_runs(cap);
-    k_split_scatter<KW2><<<scatter_blocks<KW2>(lg_runs), TPB, 0, c->stream>>>(
-        (const ulonglong2 *)c->records.p, (const unsigned long long *)c->bucket_cnt.p, cap, lg_runs,
-        scatter_lg_window(pb), c->geom, (uint64_t *)c->table.p, (unsigned long long *)c->sub_cnt.p, c->dctr);
+    launch_scatter<KW2>((const ulonglong2 *)c->records.p, (const unsigned long long *)c->bucket_cnt.p, cap, pb,
+                        c->geom, (uint64_t *)c->table.p, (unsigned long long *)c->sub_cnt.p, c->dctr, c->stream);
     cudaEventRecord(c->kev[4], c->stream);
     k_count_local2<<<(unsigned)(1ull << pb), PTPB2, (unsigned)(region * 64), c->stream>>>(
         (const unsigned long long *)c->sub_cnt.p, c->geom, (uint64_t *)c->table.p, ca, c->dctr);

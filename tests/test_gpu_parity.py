@@ -324,17 +324,18 @@ def test_edge_filter_workload_parity():
         compare(gpu_run(fq, 31, True, thr, mu, edge_filter=True), ref)
 
 
-@pytest.mark.parametrize("k", [31, 63])
-def test_scatter_split_parity(k):
-    """tables with more partitions than the shared-memory split handles: an explicit 80M-slot
-    table of partitions of at most 256 slots (2^19 of them at k = 31) on a 1 Mbp genome, whose
-    records are scattered straight into their partitions' table regions"""
+@pytest.mark.parametrize("k,slots,parts", [(31, 80_000_000, 1 << 19), (63, 140_000_000, 1 << 21)])
+def test_scatter_split_parity(k, slots, parts):
+    """tables with more partitions than the shared-memory split handles, on a 1 Mbp genome: an
+    explicit table of partitions of at most 256 slots (k = 31: 2^19 partitions, the records
+    scattered in windows of four buckets) or 128 (k = 63: 2^21 partitions, 8192 a bucket, so
+    the records are scattered bucket after bucket)"""
     w = synth.WORKLOADS["plain-small"]
     fq = synth.make_fastq(w)
     thr = bg.thresholds(w.lower)
     ref = oracle.run(fq, k=k, thresh=thr, min_update=True, threads=16, keep_k2=True, keep_filtered=True)
-    got = gpu_run(fq, k, True, thr, True, table_slots=80_000_000, part_slots=256)
-    assert got["sizes"]["table_partitions"] > 1 << 18
+    got = gpu_run(fq, k, True, thr, True, table_slots=slots, part_slots=256)
+    assert got["sizes"]["table_partitions"] == parts
     compare(got, ref)
 
 
