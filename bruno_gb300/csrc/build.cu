@@ -1712,6 +1712,38 @@ __device__ __forceinline__ bool sm_count_entries(uint32_t *e, const uint32_t *se
   return false;
 }
 
+/* one record into the partition held in shared memory; false if the region is full */
+__device__ __forceinline__ bool sm_count(uint64_t *sm, uint32_t sm_base, uint32_t region, uint64_t h, unsigned code,
+                                         uint32_t home, unsigned long long &slot_claims,
+                                         unsigned long long &entry_claims) {
+  bool seen_primary = false;
+  uint32_t j = home;
+  for (uint32_t probe = 0; probe < region; ++probe) {
+    uint64_t raw[4];
+    sm_ld_slot(sm_base + j * 32u, raw);
+    uint64_t key = raw[0];
+    uint32_t seen[6];
+    #pragma unroll
+    for (int q = 0; q < 6; ++q) seen[q] = (uint32_t)(raw[1 + q / 2] >> (32 * (q & 1)));
+    const uint64_t want = h | (seen_primary ? KEY_CONT : 0);
+    if (key == KEY_EMPTY) {
+      const uint64_t ne0 = (uint64_t)((code << E_CODE_SHIFT) | (1u << E_COUNT_SHIFT));
+      uint64_t ohi;
+      const uint64_t olo = sm_cas128(sm_base + j * 32u, KEY_EMPTY, 0ull, want, ne0, ohi);
+      if (olo == KEY_EMPTY && ohi == 0) { ++slot_claims; ++entry_claims; return true; }
+      key = olo;
+      seen[0] = (uint32_t)ohi;
+      seen[1] = (uint32_t)(ohi >> 32);
+    }
+    if (key == want) {
+      seen_primary = true;
+      if (sm_count_entries<6>((uint32_t *)(sm + (uint64_t)j * 4 + 1), seen, code, entry_claims)) return true;
+    }
+    j = (j + 1 == region) ? 0u : j + 1;
+  }
+  return false;
+}
+
 /* The counting kernel's share of the filter, for thresholded builds: a k-mer that the filter's
  * quick rule drops (its total below the (k+1)-mer lower bound: every entry gets flags 1 and 2 and
  * the slot keeps its bare key; filter_quick) is tallied here and left as it is; every other
@@ -1759,65 +1791,14 @@ __global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, cons
   const uint64_t bucket_hi = (j >> sbits) << LOW_BITS;   /* bucket bits of the mix */
   unsigned long long slots = 0, entries = 0;
   bool full = false;
-  /* Each lane runs its records as a state machine, one probe step a turn: a lane whose record
-   * is counted takes its next one at once instead of idling until the warp's longest probe run
-   * ends, and the warp loops while any lane holds a record. */
-  uint64_t i = tid;
-  uint64_t nxt = i < n ? __ldcs(rp + i) : 0ull;
-  uint64_t h = 0;
-  unsigned code = 0;
-  uint32_t jj = 0, probes = 0;
-  bool prim = false, have = false;
-  auto take = [&]() {   /* the lane's next record, if any */
-    have = false;
-    while (i < n) {
-      const uint64_t rec = nxt;
-      i += nt;
-      nxt = i < n ? __ldcs(rp + i) : 0ull;
-      if (rec == 0ull) continue;   /* an unused chunk tail, when the buckets are the partitions */
-      h = bucket_hi | (rec >> 5);
-      code = (unsigned)(rec & 31);
-      jj = (uint32_t)__umul64hi(h << (2 + G.g.pbits), G.g.region);
-      probes = 0;
-      prim = false;
-      have = true;
-      return;
-    }
-  };
-  take();
-  while (__any_sync(~0u, have)) {
-    if (have) {
-      const uint32_t a = sm_base + jj * 32u;
-      uint64_t raw[4];
-      sm_ld_slot(a, raw);
-      uint64_t key = raw[0];
-      uint32_t seen[6];
-      #pragma unroll
-      for (int q = 0; q < 6; ++q) seen[q] = (uint32_t)(raw[1 + q / 2] >> (32 * (q & 1)));
-      const uint64_t want = h | (prim ? KEY_CONT : 0);
-      bool done = false;
-      if (key == KEY_EMPTY) {
-        const uint64_t ne0 = (uint64_t)((code << E_CODE_SHIFT) | (1u << E_COUNT_SHIFT));
-        uint64_t ohi;
-        const uint64_t olo = sm_cas128(a, KEY_EMPTY, 0ull, want, ne0, ohi);
-        if (olo == KEY_EMPTY && ohi == 0) {
-          ++slots; ++entries; done = true;
-        } else {
-          key = olo;
-          seen[0] = (uint32_t)ohi;
-          seen[1] = (uint32_t)(ohi >> 32);
-        }
-      }
-      if (!done && key == want) {
-        prim = true;
-        done = sm_count_entries<6>((uint32_t *)(sm + (uint64_t)jj * 4 + 1), seen, code, entries);
-      }
-      if (!done) {   /* the next slot of the partition, or the region is full */
-        jj = (jj + 1 == region) ? 0u : jj + 1;
-        if (++probes == region) { full = true; done = true; }
-      }
-      if (done) take();
-    }
+  uint64_t nxt = tid < n ? __ldcs(rp + tid) : 0ull;
+  for (uint64_t i = tid; i < n; i += nt) {
+    const uint64_t rec = nxt;
+    nxt = i + nt < n ? __ldcs(rp + i + nt) : 0ull;
+    if (rec == 0ull) continue;   /* an unused chunk tail, when the buckets are the partitions */
+    const uint64_t h = bucket_hi | (rec >> 5);
+    const uint32_t home = (uint32_t)__umul64hi(h << (2 + G.g.pbits), G.g.region);
+    if (!sm_count(sm, sm_base, region, h, (unsigned)(rec & 31), home, slots, entries)) full = true;
   }
   __syncthreads();
   ulonglong2 *dst = reinterpret_cast<ulonglong2 *>(table + (G.g.base + j * G.g.region) * 4);
