@@ -65,7 +65,7 @@ struct Done {
 struct bruno_pool {
   bruno_cfg cfg{};
   uint64_t budget = 0;
-  bool batched = false;          /* continuous batching: one scheduler thread, fused passes */
+  bool batched = false;          /* continuous batching: scheduler threads running fused passes */
   uint32_t max_samples = 0;      /* requests in one fused pass at most */
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -200,9 +200,13 @@ void take_sample(bruno_ctx *ctx, size_t i, int words, bruno_pool_result &r) {
  * Where the fused pass cannot run (a configuration the batched form refuses, or an error), each
  * request of the pass is built on its own with the plain path, so every result is always the
  * plain path's. */
-void batch_main(bruno_pool *p) {
+/* Scheduler w of the continuous-batching pool: its own context, passes of at most the budget's
+ * share of one scheduler.  With two schedulers one pass's host work (the copies in, every
+ * request's results out) runs beside the other pass's kernels. */
+void batch_main(bruno_pool *p, int w) {
   bruno_ctx *ctx = nullptr;
   const int words = p->cfg.k <= 31 ? 1 : 2;
+  const uint64_t share = p->budget / p->held.size();
   for (;;) {
     std::vector<Request> take;
     {
@@ -212,13 +216,13 @@ void batch_main(bruno_pool *p) {
       uint64_t sum = 0;
       while (!p->queue.empty() && take.size() < p->max_samples) {
         const Request &q = p->queue.front();
-        if (!take.empty() && sum + q.est > p->budget) break;
+        if (!take.empty() && sum + q.est > share) break;
         sum += q.est;
         take.push_back(q);
         p->queue.pop_front();
       }
-      p->busy[0] = true;
-      p->held[0] = std::max(p->held[0], sum);
+      p->busy[w] = true;
+      p->held[w] = std::max(p->held[w], sum);
     }
     const clk::time_point t0 = clk::now();
     std::vector<Done> out(take.size());
@@ -243,10 +247,10 @@ void batch_main(bruno_pool *p) {
       for (size_t i = 0; i < take.size(); ++i) {
         out[i].r.queue_ms = std::chrono::duration<double, std::milli>(t0 - take[i].submitted).count();
         out[i].r.run_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
-        out[i].r.worker = 0;
+        out[i].r.worker = w;
         p->done[take[i].ticket] = out[i];
       }
-      p->busy[0] = false;
+      p->busy[w] = false;
     }
     p->cv_done.notify_all();
   }
@@ -267,9 +271,10 @@ extern "C" bruno_status bruno_pool_create_batched(const bruno_cfg *cfg, uint32_t
   p->batched = true;
   p->max_samples = max_samples;
   p->budget = mem_budget ? mem_budget : (uint64_t)(0.8 * (double)free_b);
-  p->held.assign(1, 0);
-  p->busy.assign(1, false);
-  p->threads.emplace_back(batch_main, p);
+  constexpr int SCHEDULERS = 2;
+  p->held.assign(SCHEDULERS, 0);
+  p->busy.assign(SCHEDULERS, false);
+  for (int w = 0; w < SCHEDULERS; ++w) p->threads.emplace_back(batch_main, p, w);
   *out = p;
   return BRUNO_OK;
 }

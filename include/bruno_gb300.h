@@ -404,10 +404,11 @@ typedef struct bruno_pool_result {
   double run_ms;            /* start -> result on the host */
 } bruno_pool_result;
 bruno_status bruno_pool_create(const bruno_cfg *cfg, int32_t workers, uint64_t mem_budget, bruno_pool **out);
-/* The same pool over the batched form (continuous batching): one scheduler thread repeatedly
- * takes every queued request whose estimates fit mem_budget together (at least one, at most
- * max_samples, 1..16384) and builds them in one fused pass (bruno_build_samples); requests that
- * arrive during a pass join the next one.  Results, submit / wait / free / destroy as above (run_ms
+/* The same pool over the batched form (continuous batching): two scheduler threads, each with
+ * its own context, repeatedly take every queued request whose estimates fit half of mem_budget
+ * together (at least one, at most max_samples, 1..16384) and build them in one fused pass
+ * (bruno_build_samples); requests that arrive during a pass join the next one, and one pass's
+ * copies and result copy-outs run beside the other's kernels.  Results, submit / wait / free / destroy as above (run_ms
  * is the pass that built the request).  Where the batched form refuses the configuration, each
  * request is built with the plain path instead; every result equals the plain path's. */
 bruno_status bruno_pool_create_batched(const bruno_cfg *cfg, uint32_t max_samples, uint64_t mem_budget,
