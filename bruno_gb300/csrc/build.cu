@@ -366,10 +366,7 @@ struct CountArgs {
   DevCounters *ctr;
 };
 
-__device__ __forceinline__ uint64_t ld_cg(const uint64_t *p) { return __ldcg((const unsigned long long *)p); }
 
-/* one slot (4 or 8 words) with 256-bit relaxed loads: a single L2 request per 32 bytes */
-__device__ __forceinline__ uint32_t ld_cg32(const uint32_t *p) { return __ldcg(p); }
 
 /* One more occurrence of the entry whose word lives at `key` (its address), in the exact
  * side table of counts past 2^24.  Every such entry needs 2^24 occurrences, so at most
@@ -448,15 +445,7 @@ __device__ __forceinline__ bool count_in_entries(uint32_t *e, const uint32_t *se
   return false;
 }
 
-/* slot key helpers (KW1: one word; KW2: lo, hi with flags in hi) */
-__device__ __forceinline__ bool key_claim(KW1, uint64_t *slot, KW1 want, bool cont, KW1 &seen, bool &was_empty) {
-  const uint64_t nk = want.v | (cont ? KEY_CONT : 0);
-  const uint64_t old = atomicCAS((unsigned long long *)slot, KEY_EMPTY, nk);
-  was_empty = (old == KEY_EMPTY);
-  seen.v = was_empty ? nk : old;
-  return was_empty;
-}
-
+/* 128-bit CAS on global memory (KW2 keys: lo, hi with the slot marks in hi) */
 __device__ __forceinline__ unsigned long long cas128(uint64_t *addr, uint64_t cmp_lo, uint64_t cmp_hi, uint64_t new_lo,
                                                      uint64_t new_hi, uint64_t &old_hi) {
   unsigned long long olo, ohi;
@@ -473,6 +462,7 @@ __device__ __forceinline__ unsigned long long cas128(uint64_t *addr, uint64_t cm
   return olo;
 }
 
+/* claims a KW2 key (both words in one 128-bit CAS) */
 __device__ __forceinline__ bool key_claim(KW2, uint64_t *slot, KW2 want, bool cont, KW2 &seen, bool &was_empty) {
   const uint64_t nhi = want.hi | (cont ? KEY_CONT : 0);
   uint64_t ohi;
@@ -480,14 +470,6 @@ __device__ __forceinline__ bool key_claim(KW2, uint64_t *slot, KW2 want, bool co
   was_empty = (olo == KEY_EMPTY && ohi == KEY_EMPTY);
   seen = was_empty ? KW2{want.lo, nhi} : KW2{olo, ohi};
   return was_empty;
-}
-
-__device__ __forceinline__ KW1 key_read(KW1, const uint64_t *slot) { return {ld_cg(slot)}; }
-__device__ __forceinline__ KW2 key_read(KW2, const uint64_t *slot) {
-  /* the claim writes both words in one 128-bit atomic, so a 16-byte load sees either
-   * the empty key or the whole claimed key */
-  ulonglong2 v = __ldcg((const ulonglong2 *)slot);
-  return {v.x, v.y};
 }
 
 /* Counts one canonical (k-mer, biedge code) occurrence whose first probe slot `i` was
@@ -1368,7 +1350,6 @@ __device__ __forceinline__ uint32_t pick4(const uint32_t *v, unsigned c) {
 template <class KT, int CAP>
 __device__ __forceinline__ bool filter_quick(uint64_t *s, const uint32_t *w, int ne, const FilterArgs &a,
                                              FilterTally &t) {
-  constexpr int KWD = Slot<KT>::KEYW;
   if (!a.thresholding) return false;
   const uint32_t cmax32 = 0xFFFFu;
   uint32_t kf = 0;
@@ -2610,6 +2591,13 @@ double hll_estimate(const unsigned int *reg) {
   return est;
 }
 
+/* k_hll_sums writes each sample's zero-register count as a 32-bit word after the sums */
+unsigned zeros_word(const void *p) {
+  unsigned z;
+  std::memcpy(&z, p, sizeof z);
+  return z;
+}
+
 /* the HyperLogLog estimate of the k-mers sampled into it (1 in 2^HLL_SAMPLE), scaled back to all */
 double hll_sampled_estimate(double sum, unsigned zeros) {
   const double m = HLL_M, alpha = 0.7213 / (1.0 + 1.079 / m);
@@ -2956,7 +2944,7 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
     double hs[2] = {0, 0};
     cudaMemcpyAsync(hs, c->hsum.p, 16, cudaMemcpyDeviceToHost, c->stream);
     if ((st = sync_counters(c)) != BRUNO_OK) return st;
-    distinct = hll_sampled_estimate(hs[0], *(const unsigned int *)&hs[1]);
+    distinct = hll_sampled_estimate(hs[0], zeros_word(&hs[1]));
   }
   if (c->hctr->err & DERR_TABLE_FULL) return BRUNO_OK;   /* a bucket overflowed: count directly */
   c->n_instances = c->hctr->n_instances;
@@ -3105,7 +3093,7 @@ bruno_status count_partitioned_w2(Ctx *c, bool &used) {
   c->n_instances = c->hctr->n_instances;
   c->n_reads_used = c->hctr->n_reads_used;
   uint64_t slots = c->cfg.table_slots ? c->cfg.table_slots
-                                      : slots_for(c, hll_sampled_estimate(hs[0], *(const unsigned int *)&hs[1]));
+                                      : slots_for(c, hll_sampled_estimate(hs[0], zeros_word(&hs[1])));
   const uint64_t pmax = part_slots(c) / 2;   /* 64-byte slots: half as many in the same shared memory */
   for (int attempt = 0; attempt < 4; ++attempt) {
     int pb = NBUCKET_BITS;
@@ -3463,9 +3451,9 @@ bruno_status run_count_samples(Ctx *c) {
     return set_err(c, BRUNO_ERR_TABLE_FULL, "batch: a sample's hash bucket overflowed (a skewed sample)");
   c->n_instances = c->hctr->n_instances;
   c->n_reads_used = c->hctr->n_reads_used;
-  const unsigned int *zeros = (const unsigned int *)(hs.data() + S);
   std::vector<uint64_t> slots(S);
-  for (uint32_t q = 0; q < S; ++q) slots[q] = slots_for(c, hll_sampled_estimate(hs[q], zeros[q]));
+  const unsigned char *zeros = (const unsigned char *)(hs.data() + S);   /* S 32-bit words after the sums */
+  for (uint32_t q = 0; q < S; ++q) slots[q] = slots_for(c, hll_sampled_estimate(hs[q], zeros_word(zeros + 4 * q)));
   for (int attempt = 0; attempt < 4; ++attempt) {
     std::vector<SGeom> sg(S);
     uint64_t base = 0, pbase = 0;

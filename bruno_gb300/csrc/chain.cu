@@ -38,7 +38,6 @@ namespace bg {
 namespace {
 
 constexpr int TPB = 256;
-constexpr int CHS = TPB * 16;           /* slots per block in the chain-index passes */
 constexpr uint32_t DM = 0x7FFFFFFFu;    /* dist_mask (debruijn_chain_node.hpp:53) */
 constexpr uint32_t TM = 0x80000000u;    /* term_mask */
 constexpr uint32_t NONE32 = 0xFFFFFFFFu;
