@@ -2968,7 +2968,7 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
     cudaMemsetAsync(c->dctr->big_key, 0, sizeof(c->dctr->big_key) + sizeof(c->dctr->big_cnt), c->stream);
     cudaMemsetAsync(&c->dctr->n_big, 0, 8, c->stream);
     if (region_c <= part_slots(c) && c->force_direct_count != 2) {
-      c->geom = TableGeom{region_c << pb, region_c, pb};
+      c->geom = TableGeom{region_c << pb, region_c, pb, 0};
       c->nslots = c->geom.nslots;
       if ((st = table_room(c, c->nslots)) != BRUNO_OK) return st;
       if ((st = ensure(c, c->table, c->nslots * 32)) != BRUNO_OK) return st;
@@ -2993,7 +2993,7 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
       int pt = 0;
       while (pt < NBUCKET_BITS && bytes / (double)(1ull << pt) > 48.0 * 1024 * 1024) ++pt;
       const uint64_t region = std::max<uint64_t>(64, (slots + (1ull << pt) - 1) >> pt);
-      c->geom = TableGeom{region << pt, region, pt};
+      c->geom = TableGeom{region << pt, region, pt, 0};
       c->nslots = c->geom.nslots;
       if ((st = table_room(c, c->nslots)) != BRUNO_OK) return st;
       if ((st = ensure(c, c->table, c->nslots * 32)) != BRUNO_OK) return st;

@@ -131,7 +131,7 @@ struct Ctx {
 
   /* k-mer table */
   Buf table;
-  TableGeom geom{0, 0, 0};
+  TableGeom geom{0, 0, 0, 0};
   uint64_t nslots = 0, n_entries = 0, n_slots_claimed = 0;
   Buf records, bucket_cnt;       /* partitioned counting: 8-byte records per hash bucket */
   Buf xsamp, hllreg, hsum;       /* the extraction's bucket layout, HyperLogLog registers, their sums */
