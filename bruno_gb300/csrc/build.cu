@@ -3281,7 +3281,8 @@ bruno_status filter_typed(Ctx *c, const uint64_t *thr) {
   /* the count listed the slots that need the full filter (same thresholds): read only those,
    * and add the quick drops the count tallied */
   /* (at most one listed slot a slot: a count past the table's slots would mean a lost list) */
-  const bool use_cand = c->have_cand && c->n_cand <= c->nslots && a.thresholding && std::equal(thr, thr + 6, c->cfg.thresh);
+  const bool use_cand = c->have_cand && c->n_cand <= c->nslots && a.thresholding &&
+                        std::equal(thr, thr + 6, c->cfg.thresh);
   if (use_cand) {
     a.cand = (const uint32_t *)c->cand.p;
     a.n_cand = c->n_cand;
