@@ -123,9 +123,7 @@ __device__ __forceinline__ long long table_find(const uint64_t *table, const Tab
 }
 
 /* Two lookups in lockstep: both first probes are in flight together, and each probe reads
- * the whole slot (key, counters, flags, aux) in 32-byte loads; 64-byte slots (k > 31) read
- * only their first half (key, counters) while probing and the second half (flags, aux) once,
- * for the slot found.  found = slot index or -1. */
+ * the whole slot (key, counters, flags, aux) in 32-byte loads.  found = slot index or -1. */
 template <class KT>
 __device__ __forceinline__ void table_find2(const uint64_t *table, const TableGeom &g, uint32_t max_probe,
                                             const KT *want, const bool *has, long long *found,
@@ -143,11 +141,10 @@ __device__ __forceinline__ void table_find2(const uint64_t *table, const TableGe
     const Probe pr(g, table_home(g, bare));
     pos[q] = pr.i; lo[q] = pr.lo; hi[q] = pr.hi;
   }
-  constexpr int PROBE_U64 = SU > 4 ? 4 : SU;   /* the words a probe reads */
   for (uint32_t p = 0; p < max_probe && !(done[0] && done[1]); ++p) {
     #pragma unroll
     for (int q = 0; q < 2; ++q)
-      if (!done[q]) ld_slot<PROBE_U64>(table + pos[q] * SU, raw[q]);
+      if (!done[q]) ld_slot<SU>(table + pos[q] * SU, raw[q]);
     #pragma unroll
     for (int q = 0; q < 2; ++q) {
       if (done[q]) continue;
@@ -156,12 +153,6 @@ __device__ __forceinline__ void table_find2(const uint64_t *table, const TableGe
       else if (key_is_empty(key)) done[q] = true;
       else if (++pos[q] == hi[q]) pos[q] = lo[q];
     }
-  }
-  if constexpr (SU > 4) {   /* the found slots' second halves, both in flight together */
-    #pragma unroll
-    for (int q = 0; q < 2; ++q)
-      if (found[q] >= 0) ld_slot<SU - 4>(table + (uint64_t)found[q] * SU + 4, raw[q] + 4);
-      else for (int w = 4; w < SU; ++w) raw[q][w] = 0;   /* nothing found: no flags */
   }
 }
 
