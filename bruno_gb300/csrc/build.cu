@@ -23,6 +23,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "table_plan.h"
 #include "internal.cuh"
 
 namespace bg {
@@ -1934,18 +1935,9 @@ __global__ void __launch_bounds__(TPB) k_split_scatter(const typename ScatterRec
   if (over) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
 }
 
-/* the bucket window of the scatter split (log2): enough buckets for 8192 partition cursors */
-int scatter_lg_window(int pbits) {
-  int lg = 0;
-  while (lg < NBUCKET_BITS && (1ull << (lg + pbits - NBUCKET_BITS)) < 8192) ++lg;
-  return lg;
-}
-/* log2 of a bucket's 32-record runs, counted up to a power of two */
-int scatter_lg_runs(uint64_t cap) {
-  int lg = 0;
-  while ((1ull << lg) * 32 < cap) ++lg;
-  return lg;
-}
+using bruno_table_plan::scatter_lg_runs;
+using bruno_table_plan::scatter_lg_window;
+
 /* The scatter split bucket after bucket, for tables whose window is one bucket (large tables):
  * grid row y is bucket y, its blocks stride over the bucket's records, one record a thread
  * (measured 60 ms at large k against 70-73 for the windowed form above run on one bucket) */
@@ -2802,8 +2794,7 @@ bruno_status split_and_count(Ctx *c, std::vector<SGeom> &sg, const std::vector<u
   } else {
     /* partitions grouped by region size: a launch per class, with shared memory for its largest
      * region (classes a factor of about 1.5 apart, so no region reserves much more than it uses) */
-    static const uint64_t bound[] = {128, 192, 256, 384, 512, 768, 1024, 1536, 2048, ~0ull};
-    constexpr int NCL = sizeof(bound) / sizeof(bound[0]);
+    constexpr int NCL = bruno_table_plan::REGION_CLASSES;
     std::vector<ClassRun> runs;
     std::vector<size_t> at{0};
     std::vector<uint64_t> rmax, nparts_cl;
@@ -2811,7 +2802,7 @@ bruno_status split_and_count(Ctx *c, std::vector<SGeom> &sg, const std::vector<u
       uint64_t m = 0, n = 0;
       for (uint32_t q = 0; q < S; ++q) {
         const uint64_t r = sg[q].g.region;
-        if (r > bound[cl] || (cl > 0 && r <= bound[cl - 1])) continue;
+        if (bruno_table_plan::region_class(r) != cl) continue;
         runs.push_back(ClassRun{(uint32_t)n, (uint32_t)sg[q].pbase});
         n += 1ull << sg[q].g.pbits;
         m = std::max(m, r);
@@ -2959,9 +2950,9 @@ bruno_status count_partitioned(Ctx *c, bool &used) {
   for (int attempt = 0; attempt < 4; ++attempt) {
     /* shared-memory path: 2^pb partitions (pb >= 8) small enough for one CTA's shared memory;
      * past k_split's 8 + MAX_SPLIT_BITS bits the records are scattered into the table instead */
-    int pb = NBUCKET_BITS;
-    while (pb < NBUCKET_BITS + MAX_SPLIT_BITS2 && (slots + (1ull << pb) - 1) >> pb > part_slots(c)) ++pb;
-    const uint64_t region_c = std::max<uint64_t>(64, (slots + (1ull << pb) - 1) >> pb);
+    const bruno_table_plan::Plan plan = bruno_table_plan::partitions(slots, part_slots(c), MAX_SPLIT_BITS2);
+    const int pb = plan.pbits;
+    const uint64_t region_c = plan.region;
     bool counted = false, counted_local = false;
     cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
     cudaMemsetAsync(&c->dctr->n_slots_claimed, 0, 16, c->stream);
@@ -3096,10 +3087,10 @@ bruno_status count_partitioned_w2(Ctx *c, bool &used) {
                                       : slots_for(c, hll_sampled_estimate(hs[0], zeros_word(&hs[1])));
   const uint64_t pmax = part_slots(c) / 2;   /* 64-byte slots: half as many in the same shared memory */
   for (int attempt = 0; attempt < 4; ++attempt) {
-    int pb = NBUCKET_BITS;
-    while (pb < NBUCKET_BITS + MAX_SPLIT_BITS2 && (slots + (1ull << pb) - 1) >> pb > pmax) ++pb;
-    const uint64_t region = std::max<uint64_t>(64, (slots + (1ull << pb) - 1) >> pb);
-    if (region > pmax) return BRUNO_OK;
+    const bruno_table_plan::Plan plan = bruno_table_plan::partitions(slots, pmax, MAX_SPLIT_BITS2);
+    const int pb = plan.pbits;
+    const uint64_t region = plan.region;
+    if (!plan.fits) return BRUNO_OK;
     c->geom = TableGeom{region << pb, region, pb, 0};
     c->nslots = c->geom.nslots;
     if ((st = table_room(c, c->nslots)) != BRUNO_OK) return st;
@@ -3460,10 +3451,10 @@ bruno_status run_count_samples(Ctx *c) {
     std::vector<SGeom> sg(S);
     uint64_t base = 0, pbase = 0;
     for (uint32_t q = 0; q < S; ++q) {
-      int pb = NBUCKET_BITS;
-      while (pb < NBUCKET_BITS + MAX_SPLIT_BITS && (slots[q] + (1ull << pb) - 1) >> pb > part_slots(c)) ++pb;
-      const uint64_t region = std::max<uint64_t>(64, (slots[q] + (1ull << pb) - 1) >> pb);
-      if (region > part_slots(c))
+      const bruno_table_plan::Plan plan = bruno_table_plan::partitions(slots[q], part_slots(c), MAX_SPLIT_BITS);
+      const int pb = plan.pbits;
+      const uint64_t region = plan.region;
+      if (!plan.fits)
         return set_err(c, BRUNO_ERR_ARG, "batch: sample " + std::to_string(q) + " is too large for one batch");
       sg[q].g = TableGeom{region << pb, region, pb, base};
       sg[q].pbase = pbase;

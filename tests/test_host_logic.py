@@ -290,3 +290,79 @@ def test_cpp_thresholds_match_python(tmp_path):
     out = subprocess.run([str(exe)], input="\n".join(lines) + "\n", capture_output=True, text=True, check=True)
     got = [[int(x) for x in l.split()] for l in out.stdout.splitlines()]
     assert got == [bg.thresholds(lo, hi) for lo, hi in cases]
+
+
+# ----------------------------------------------------- table partitions and the scatter split
+PLAN_HARNESS = r'''
+#include "table_plan.h"
+#include <cstdio>
+#include <cstdlib>
+using namespace bruno_table_plan;
+int main(int argc, char **argv) {
+  const char *what = argv[1];
+  const unsigned long long a = strtoull(argv[2], 0, 10);
+  if (what[0] == 'p') {
+    const Plan p = partitions(a, strtoull(argv[3], 0, 10), atoi(argv[4]));
+    printf("%d %llu %d\n", p.pbits, (unsigned long long)p.region, p.fits ? 1 : 0);
+  } else if (what[0] == 'w') {
+    printf("%d\n", scatter_lg_window((int)a));
+  } else if (what[0] == 'r') {
+    printf("%d\n", scatter_lg_runs(a));
+  } else {
+    printf("%d\n", region_class(a));
+  }
+}
+'''
+
+
+@pytest.fixture(scope="module")
+def plan_cli(tmp_path_factory):
+    import os
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("no host C++ compiler")
+    d = tmp_path_factory.mktemp("plan")
+    src, exe = d / "plan.cpp", d / "plan"
+    src.write_text(PLAN_HARNESS)
+    subprocess.run([gxx, "-O2", "-std=c++17", "-I", os.path.join(os.path.dirname(bg.__file__), "csrc"), str(src),
+                    "-o", str(exe)], check=True)
+    return lambda *args: [int(x) for x in subprocess.check_output([str(exe), *map(str, args)]).split()]
+
+
+def test_partition_plans(plan_cli):
+    # plain scale: 461M slots in 2^18 partitions of 1760 (k_split's 8 + 10 bits suffice)
+    assert plan_cli("p", 461_373_440, 3072, 16) == [18, 1760, 1]
+    # a forced 80M-slot table of regions of at most 256 slots: 2^19 partitions of 153
+    assert plan_cli("p", 80_000_000, 256, 16) == [19, 153, 1]
+    # large k: 1.70B 64-byte slots, regions of at most 1536: 2^21 partitions of 811
+    assert plan_cli("p", 1_700_790_272, 1536, 16) == [21, 811, 1]
+    # small tables keep the 256 buckets as partitions, at least 64 slots each
+    assert plan_cli("p", 1000, 3072, 10) == [8, 64, 1]
+    # too large for the split bits allowed: the caller falls back
+    assert plan_cli("p", 1 << 32, 3072, 10)[2] == 0
+    # every plan covers the slots asked for
+    for slots in (1, 65_536, 3_000_001, 987_654_321):
+        pb, region, fits = plan_cli("p", slots, 3072, 16)
+        assert fits and region << pb >= slots and region <= 3072
+
+
+def test_scatter_window_and_runs(plan_cli):
+    # at least 8192 partition cursors in a window: one bucket once a bucket has 8192 partitions
+    assert plan_cli("w", 21) == [0]
+    assert plan_cli("w", 20) == [1]
+    assert plan_cli("w", 15) == [6]
+    assert plan_cli("w", 8) == [8]
+    # a bucket's 32-record runs counted up to a power of two
+    assert plan_cli("r", 1) == [0]
+    assert plan_cli("r", 32) == [0]
+    assert plan_cli("r", 33) == [1]
+    assert plan_cli("r", 15_000_000) == [19]
+
+
+def test_region_classes(plan_cli):
+    bounds = [128, 192, 256, 384, 512, 768, 1024, 1536, 2048]
+    for c, b in enumerate(bounds):
+        assert plan_cli("c", b) == [c] and plan_cli("c", b + 1) == [c + 1]
+    assert plan_cli("c", 64) == [0] and plan_cli("c", 3072) == [9]
