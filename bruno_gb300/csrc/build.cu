@@ -1530,6 +1530,14 @@ int count_threads(const Ctx *c) {
   const int v = c->cfg.count_threads;
   return (v == 256 || v == 512 || v == 1024) ? v : PTPB;
 }
+/* a counting block for partitions of at most `region` slots: about one thread per two slots
+ * (small samples' partitions hold a few hundred records), at least 128, at most the configured
+ * block */
+int count_threads_for(const Ctx *c, uint64_t region) {
+  int t = 128;
+  while (t < count_threads(c) && (uint64_t)t * 2 < region) t *= 2;
+  return t;
+}
 constexpr int MAX_SPLIT_BITS = 10;
 constexpr int SPLIT_ROUND = 16;            /* records per thread per round */
 constexpr int SPLIT_REC = XTPB * SPLIT_ROUND;   /* 8192 records a round */
@@ -2788,7 +2796,7 @@ bruno_status split_and_count(Ctx *c, std::vector<SGeom> &sg, const std::vector<u
     cudaMemsetAsync(&c->dctr->n_cand, 0, sizeof(c->dctr->n_cand) + sizeof(c->dctr->quick_hist), c->stream);
   }
   if (S == 1) {
-    k_count_local<<<(unsigned)nparts, count_threads(c), (unsigned)(region_max * 32), c->stream>>>(
+    k_count_local<<<(unsigned)nparts, count_threads_for(c, region_max), (unsigned)(region_max * 32), c->stream>>>(
         recs, cnts, (const SGeom *)c->sgeom.p, S, nullptr, 0, (uint64_t *)c->table.p, s_tally, ca, c->dctr);
     c->launches += 1;
   } else {
@@ -2817,7 +2825,8 @@ bruno_status split_and_count(Ctx *c, std::vector<SGeom> &sg, const std::vector<u
       return st;
     for (int cl = 0; cl < NCL; ++cl) {
       if (!nparts_cl[cl]) continue;
-      k_count_local<<<(unsigned)nparts_cl[cl], count_threads(c), (unsigned)(rmax[cl] * 32), c->stream>>>(
+      k_count_local<<<(unsigned)nparts_cl[cl], count_threads_for(c, rmax[cl]), (unsigned)(rmax[cl] * 32),
+                      c->stream>>>(
           recs, cnts, (const SGeom *)c->sgeom.p, S, (const ClassRun *)c->grp_tmp.p + at[cl],
           (uint32_t)(at[cl + 1] - at[cl]), (uint64_t *)c->table.p, s_tally, ca, c->dctr);
       c->launches += 1;
@@ -2855,7 +2864,7 @@ bruno_status scatter_and_count(Ctx *c, uint64_t cap) {
   launch_scatter<KW1>((const uint64_t *)c->records.p, (const unsigned long long *)c->bucket_cnt.p, cap, pb, c->geom,
                       (uint64_t *)c->table.p, (unsigned long long *)c->sub_cnt.p, c->dctr, c->stream);
   cudaEventRecord(c->kev[4], c->stream);
-  k_count_local<<<(unsigned)(1ull << pb), count_threads(c), (unsigned)(region * 32), c->stream>>>(
+  k_count_local<<<(unsigned)(1ull << pb), count_threads_for(c, region), (unsigned)(region * 32), c->stream>>>(
       (const uint64_t *)c->table.p, (const unsigned long long *)c->sub_cnt.p, (const SGeom *)c->sgeom.p, 1, nullptr, 0,
       (uint64_t *)c->table.p, nullptr, ca, c->dctr);
   c->launches += 2;
