@@ -210,7 +210,7 @@ class GraphConfig:
     keep_filtered: bool = False
     exact_ranking: bool = False
     direct_count: int = 0          # 0 automatic, 1 whole-table counting, 2 L2 partitions (k <= 31)
-    edge_filter: bool = False      # the blocked driver's (k+1)-mer filter build (k <= 31)
+    edge_filter: bool = False      # the blocked driver's (k+1)-mer filter build
     h2d_chunk: int = 0             # host FASTQ copied and parsed in pieces of this many bytes (0 = 256 MiB)
     h2d_streams: int = 1           # copy streams the pieces are spread over (1..4)
     rank_fill: int = 0             # ranking's final states: 0 = second walk, 1 = one pass over the nodes

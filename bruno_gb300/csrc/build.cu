@@ -807,6 +807,114 @@ __global__ void __launch_bounds__(TPB) k_k1_threshold(uint64_t *tab, uint64_t ns
   }
 }
 
+/* The same (k+1)-mer table for k > 31: (k+1)-mers of 33..64 bases as 128-bit keys (KW2 packing)
+ * in 32-byte slots [lo, hi, count, 0].  Both words all ones mark an empty slot and (all ones
+ * but the lowest bit, all ones) an erased one: neither is canonical (at 64 bases their reverse
+ * complements are smaller; below, the high word has bits past the k-mer). */
+constexpr uint64_t K1W_TOMB_LO = ~1ull;
+
+struct K1Roll2 {   /* forward and reverse-complement (k+1)-mer of a read, 128-bit */
+  KW2 fw{0, 0}, rv{0, 0};
+  int k1;
+  __device__ __forceinline__ explicit K1Roll2(int k1_) : k1(k1_) {}
+  __device__ __forceinline__ KW2 push(unsigned c) {   /* the canonical (k+1)-mer ending here */
+    fw = KOps<KW2>::append(fw, c, k1);
+    rv = KOps<KW2>::prepend(3u - c, rv, k1);
+    return KOps<KW2>::lt(fw, rv) ? fw : rv;
+  }
+};
+
+__device__ __forceinline__ uint64_t k1w_home(KW2 x, uint64_t nslots) { return __umul64hi(KOps<KW2>::hash(x), nslots); }
+
+/* true if the 128-bit (k+1)-mer x is in the table (erased slots are stepped over) */
+__device__ __forceinline__ bool k1w_exists(const uint64_t *tab, uint64_t nslots, KW2 x) {
+  uint64_t i = k1w_home(x, nslots);
+  for (uint64_t p = 0; p < nslots; ++p) {
+    const ulonglong2 key = __ldg(reinterpret_cast<const ulonglong2 *>(tab + 4 * i));
+    if (key.x == x.lo && key.y == x.hi) return true;
+    if (key.x == KEY_EMPTY && key.y == KEY_EMPTY) return false;
+    if (++i == nslots) i = 0;
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(TPB) k_k1w_hll(const uint64_t *rstart, const uint64_t *rend, uint64_t nreads, int k,
+                                                  uint8_t *partial) {
+  __shared__ unsigned int reg[HLL_M];
+  for (int i = threadIdx.x; i < HLL_M; i += TPB) reg[i] = 0;
+  __syncthreads();
+  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nreads; r += (uint64_t)gridDim.x * blockDim.x) {
+    const unsigned char *s = (const unsigned char *)rstart[r], *e = (const unsigned char *)rend[r];
+    const uint32_t L = (uint32_t)(e - s);
+    if (L < (uint32_t)k + 1 || !seq_valid(s, e)) continue;
+    SeqCursor sc;
+    sc.init(s, e);
+    K1Roll2 roll(k + 1);
+    for (uint32_t i = 0; i < L; ++i) {
+      const unsigned byte = sc.next();
+      const KW2 x = roll.push(((byte >> 1) ^ (byte >> 2)) & 3u);
+      if (i < (uint32_t)k) continue;
+      const uint64_t h = KOps<KW2>::hash(x);
+      const unsigned idx = (unsigned)(h >> (64 - HLL_P));
+      const unsigned rho = (unsigned)__clzll((h << HLL_P) | (1ull << (HLL_P - 1))) + 1u;
+      if (rho > reg[idx]) atomicMax(&reg[idx], rho);
+    }
+  }
+  __syncthreads();
+  uint8_t *dst = partial + (uint64_t)blockIdx.x * HLL_M;
+  for (int i = threadIdx.x; i < HLL_M; i += TPB) dst[i] = (uint8_t)reg[i];
+}
+
+__global__ void __launch_bounds__(TPB) k_k1w_count(const uint64_t *rstart, const uint64_t *rend, uint64_t nreads, int k,
+                                                    uint64_t *tab, uint64_t nslots, uint32_t max_probe,
+                                                    DevCounters *ctr) {
+  bool full = false;
+  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nreads; r += (uint64_t)gridDim.x * blockDim.x) {
+    const unsigned char *s = (const unsigned char *)rstart[r], *e = (const unsigned char *)rend[r];
+    const uint32_t L = (uint32_t)(e - s);
+    if (L < (uint32_t)k + 1 || !seq_valid(s, e)) continue;
+    SeqCursor sc;
+    sc.init(s, e);
+    K1Roll2 roll(k + 1);
+    for (uint32_t i = 0; i < L; ++i) {
+      const unsigned byte = sc.next();
+      const KW2 x = roll.push(((byte >> 1) ^ (byte >> 2)) & 3u);
+      if (i < (uint32_t)k) continue;
+      uint64_t j = k1w_home(x, nslots);
+      bool done = false;
+      for (uint32_t p = 0; p < max_probe && !done; ++p) {
+        uint64_t *slot = tab + 4 * j;
+        /* one 16-byte load: a key is claimed by one 128-bit CAS, so it is seen whole or empty */
+        uint64_t klo, khi;
+        asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(klo), "=l"(khi) : "l"(slot) : "memory");
+        if (klo == KEY_EMPTY && khi == KEY_EMPTY) klo = cas128(slot, KEY_EMPTY, KEY_EMPTY, x.lo, x.hi, khi);
+        if ((klo == KEY_EMPTY && khi == KEY_EMPTY) || (klo == x.lo && khi == x.hi)) {
+          atomicAdd((unsigned long long *)(slot + 2), 1ull);
+          done = true;
+        } else if (++j == nslots) {
+          j = 0;
+        }
+      }
+      full |= !done;
+    }
+  }
+  if (full) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
+}
+
+__global__ void k_k1w_init(uint64_t *tab, uint64_t nslots) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < 4 * nslots; i += (uint64_t)gridDim.x * blockDim.x)
+    tab[i] = (i & 3) < 2 ? KEY_EMPTY : 0ull;
+}
+
+/* erase the 128-bit (k+1)-mers whose saturated count lies outside [lo, hi) */
+__global__ void __launch_bounds__(TPB) k_k1w_threshold(uint64_t *tab, uint64_t nslots, uint64_t lo, uint64_t hi) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (tab[4 * i] == KEY_EMPTY && tab[4 * i + 1] == KEY_EMPTY) continue;
+    const uint64_t c = min(tab[4 * i + 2], (uint64_t)0xFFFFu);
+    if (c < lo || c >= hi) { tab[4 * i] = K1W_TOMB_LO; tab[4 * i + 1] = KEY_EMPTY; }
+  }
+}
+
 /* EF: the (k+1)-mer edge filter above -- each edge whose (k+1)-mer is not in k1tab is cleared
  * and a pair without edges is not emitted; a read's (k+1)-mer at each position is looked up
  * once, as the out edge of one k-mer and the in edge of the next */
@@ -1063,13 +1171,18 @@ __device__ __forceinline__ void xs_close(ExtractSmemT<KT> &S, const XSample &xs,
   __syncthreads();
 }
 
-template <class KT>
+/* EF (k > 31 only): the (k+1)-mer edge filter of the blocked driver, as k_extract<true> applies
+ * it for k <= 31 -- an edge whose (k+1)-mer is not in the 128-bit table k1tab is cleared, and a
+ * pair left without edges is counted as an instance but not emitted (filter_isolated_nodes) */
+template <class KT, bool EF = false>
 __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, const uint64_t *rend, uint64_t r0,
                                                         uint64_t r1, const XItem *items, uint64_t n_items,
                                                         uint32_t item_reads, int k, const XSample *xsamp,
                                                         typename XRec<KT>::T *records, unsigned long long *bucket_cnt,
                                                         unsigned int *hll, unsigned long long *s_inst,
-                                                        unsigned long long *s_used, DevCounters *ctr) {
+                                                        unsigned long long *s_used, const uint64_t *k1tab,
+                                                        uint64_t k1slots, DevCounters *ctr) {
+  static_assert(!EF || sizeof(KT) == 16, "k <= 31 filters edges in k_extract<true>");
   using R = XRec<KT>;
   constexpr int XQT = R::Q, XROUNDT = R::ROUND;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1127,6 +1240,7 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, c
       const typename R::T rec = R::make(x, biedge_code(in5, out5), bucket, sampled, idx, rho);
       if (sampled && rho > S.hll[idx]) atomicMax(&S.hll[idx], rho);
       ++inst;
+      if (EF && in5 == 0 && out5 == 0) return;   /* filter_isolated_nodes */
       const unsigned pos = atomicAdd(&S.cnt[bucket], 1u);
       if (pos < (unsigned)XQT) {
         S.q[bucket][pos] = rec;
@@ -1136,6 +1250,7 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, c
         else S.overflow = 1;
       }
     };
+    bool ef_in_ok = false;   /* EF: the previous position's (k+1)-mer was kept */
     bool active = next_read();
     for (;;) {
       int emitted = 0;
@@ -1143,13 +1258,24 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, c
         const unsigned byte = sc.next();
         const unsigned c = ((byte >> 1) ^ (byte >> 2)) & 3u;   /* A0 C1 G2 T3, either case */
         if (i >= (uint32_t)k) {   /* the k-mer ending before base i, its out-base is base i */
-          emit(i > (uint32_t)k ? left + 1u : 0u, c + 1u);
+          unsigned in5 = i > (uint32_t)k ? left + 1u : 0u, out5 = c + 1u;
+          if constexpr (EF) {   /* the (k+1)-mer k-mer + c, canonical, against the table */
+            const KW2 f1 = KOps<KW2>::append(roll.f(), c, k + 1);
+            KW2 q1 = roll.r();
+            const uint64_t b = (uint64_t)(3u - c);
+            if (2 * k >= 64) q1.hi |= b << (2 * k - 64); else q1.lo |= b << (2 * k);
+            const bool out_ok = k1w_exists(k1tab, k1slots, KOps<KW2>::lt(f1, q1) ? f1 : q1);
+            if (!ef_in_ok) in5 = 0;
+            if (!out_ok) out5 = 0;
+            ef_in_ok = out_ok;
+          }
+          emit(in5, out5);
           ++emitted;
         }
         left = roll.first();
         roll.push(c);
         if (++i == L) {   /* the last k-mer has no out-base */
-          emit(left + 1u, 0u);
+          emit(EF && !ef_in_ok ? 0u : left + 1u, 0u);
           ++emitted;
           r += XTPB;
           active = next_read();
@@ -2895,7 +3021,7 @@ void extract_reads(Ctx *c, uint64_t r0, uint64_t r1) {
     k_extract_s<KW1><<<eb, XTPB, sizeof(ExtractSmemT<KW1>), c->stream>>>(
         (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, r0, r1, nullptr, 0, WX_ITEM, c->cfg.k,
         (const XSample *)c->xsamp.p, (uint64_t *)c->records.p, (unsigned long long *)c->bucket_cnt.p,
-        (unsigned int *)c->hllreg.p, nullptr, nullptr, c->dctr);
+        (unsigned int *)c->hllreg.p, nullptr, nullptr, nullptr, 0, c->dctr);
     c->xblk += eb;
     c->launches += 1;
     return;
@@ -3070,15 +3196,23 @@ bruno_status count_partitioned_w2(Ctx *c, bool &used) {
   static const bool attr = [] {
     cudaFuncSetAttribute(k_extract_s<KW2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)sizeof(ExtractSmemT<KW2>));
+    cudaFuncSetAttribute(k_extract_s<KW2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(ExtractSmemT<KW2>));
     cudaFuncSetAttribute(k_count_local2, cudaFuncAttributeMaxDynamicSharedMemorySize, PART_SLOTS / 2 * 64);
     return true;
   }();
   (void)attr;
   cudaEventRecord(c->kev[0], c->stream);
-  k_extract_s<KW2><<<eb, XTPB, sizeof(ExtractSmemT<KW2>), c->stream>>>(
-      (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, 0, nreads, nullptr, 0, WX_ITEM, c->cfg.k,
-      (const XSample *)c->xsamp.p, (ulonglong2 *)c->records.p, (unsigned long long *)c->bucket_cnt.p,
-      (unsigned int *)c->hllreg.p, nullptr, nullptr, c->dctr);
+  if (c->cfg.edge_filter)   /* the blocked driver's (k+1)-mer filter, table built by build_k1w_table */
+    k_extract_s<KW2, true><<<eb, XTPB, sizeof(ExtractSmemT<KW2>), c->stream>>>(
+        (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, 0, nreads, nullptr, 0, WX_ITEM, c->cfg.k,
+        (const XSample *)c->xsamp.p, (ulonglong2 *)c->records.p, (unsigned long long *)c->bucket_cnt.p,
+        (unsigned int *)c->hllreg.p, nullptr, nullptr, (const uint64_t *)c->k1tab.p, c->k1slots, c->dctr);
+  else
+    k_extract_s<KW2><<<eb, XTPB, sizeof(ExtractSmemT<KW2>), c->stream>>>(
+        (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, 0, nreads, nullptr, 0, WX_ITEM, c->cfg.k,
+        (const XSample *)c->xsamp.p, (ulonglong2 *)c->records.p, (unsigned long long *)c->bucket_cnt.p,
+        (unsigned int *)c->hllreg.p, nullptr, nullptr, nullptr, 0, c->dctr);
   k_hll_sums<<<1, 256, 0, c->stream>>>((const unsigned int *)c->hllreg.p, (double *)c->hsum.p,
                                        (unsigned int *)((double *)c->hsum.p + 1));
   c->launches += 2;
@@ -3110,7 +3244,7 @@ bruno_status count_partitioned_w2(Ctx *c, bool &used) {
     cudaMemsetAsync(&c->dctr->n_slots_claimed, 0, 16, c->stream);
     cudaMemsetAsync(&c->dctr->n_big, 0, 8, c->stream);
     CandArgs ca{};
-    if (c->cfg.thresholding) {
+    if (c->cfg.thresholding && !c->cfg.edge_filter) {   /* the edge filter's insert is unthresholded */
       if ((st = ensure(c, c->cand, c->nslots * 4)) != BRUNO_OK) return st;
       ca.cand = (uint32_t *)c->cand.p;
       ca.cap = c->nslots;
@@ -3188,8 +3322,49 @@ bruno_status build_k1_table(Ctx *c) {
   return set_err(c, BRUNO_ERR_TABLE_FULL, "(k+1)-mer table full after regrowth");
 }
 
+/* build_k1_table for k > 31: (k+1)-mers of 33..64 bases, 32-byte slots */
+bruno_status build_k1w_table(Ctx *c) {
+  bruno_status st;
+  const int sms = num_sms();
+  const uint64_t nreads = c->n_reads;
+  const int hb = std::max(1, std::min<int>(sms * 4, (int)((nreads + TPB - 1) / TPB)));
+  if ((st = ensure(c, c->blk_cnt, (size_t)hb * HLL_M)) != BRUNO_OK) return st;
+  k_k1w_hll<<<hb, TPB, 0, c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads, c->cfg.k,
+                                       (uint8_t *)c->blk_cnt.p);
+  k_hll_merge<<<HLL_M / 256, 256, 0, c->stream>>>((const uint8_t *)c->blk_cnt.p, hb, c->dctr);
+  c->launches += 2;
+  if ((st = sync_counters(c, true)) != BRUNO_OK) return st;
+  uint64_t slots = (uint64_t)(hll_estimate(c->hctr->hll) * 2.2) + 1024;
+  const int gb = std::max(1, std::min<int>(sms * 8, (int)((nreads + TPB - 1) / TPB)));
+  for (int attempt = 0; attempt < 4; ++attempt, slots *= 2) {
+    if ((st = ensure(c, c->k1tab, slots * 32)) != BRUNO_OK) return st;
+    c->k1slots = slots;
+    k_k1w_init<<<sms * 8, TPB, 0, c->stream>>>((uint64_t *)c->k1tab.p, slots);
+    cudaMemsetAsync(&c->dctr->err, 0, 8, c->stream);
+    k_k1w_count<<<gb, TPB, 0, c->stream>>>((const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, nreads,
+                                           c->cfg.k, (uint64_t *)c->k1tab.p, slots, 4096u, c->dctr);
+    c->launches += 2;
+    if ((st = sync_counters(c)) != BRUNO_OK) return st;
+    if (c->hctr->err & DERR_TABLE_FULL) continue;
+    const uint64_t lo = c->cfg.thresh[2], hi = c->cfg.thresh[3];
+    if (lo > 0 || hi < 65536) {
+      k_k1w_threshold<<<sms * 8, TPB, 0, c->stream>>>((uint64_t *)c->k1tab.p, slots, lo, hi);
+      c->launches += 1;
+    }
+    return BRUNO_OK;
+  }
+  return set_err(c, BRUNO_ERR_TABLE_FULL, "(k+1)-mer table full after regrowth");
+}
+
 template <class KT>
 bruno_status count_paths(Ctx *c) {
+  if (c->cfg.edge_filter && sizeof(KT) == 16) {   /* k > 31: the 128-bit (k+1)-mer table, partitioned count */
+    bruno_status st = build_k1w_table(c);
+    if (st != BRUNO_OK) return st;
+    bool used = false;
+    if ((st = count_partitioned_w2(c, used)) != BRUNO_OK) return st;
+    return used ? BRUNO_OK : set_err(c, BRUNO_ERR_TABLE_FULL, "a partition overflowed under the (k+1)-mer filter");
+  }
   if (c->cfg.edge_filter) {   /* the (k+1)-mer filter works on the partitioned path (k <= 31) */
     bruno_status st = build_k1_table(c);
     if (st != BRUNO_OK) return st;
@@ -3374,7 +3549,7 @@ bruno_status extract_samples(Ctx *c, uint32_t q0, uint32_t q1, const std::vector
       (const uint64_t *)c->rstart.p, (const uint64_t *)c->rend.p, 0, 0, (const XItem *)c->xitems.p, items.size(),
       WX_ITEM, c->cfg.k, (const XSample *)c->xsamp.p, (uint64_t *)c->records.p,
       (unsigned long long *)c->bucket_cnt.p, (unsigned int *)c->hllreg.p, (unsigned long long *)c->s_inst.p,
-      (unsigned long long *)c->s_used.p, c->dctr);
+      (unsigned long long *)c->s_used.p, nullptr, 0, c->dctr);
   c->launches += 1;
   return cuda_check(c, cudaGetLastError(), "k_extract_s");
 }

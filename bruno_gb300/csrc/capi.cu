@@ -106,7 +106,7 @@ bruno_status bruno_ctx_create(const bruno_cfg *cfg, bruno_ctx **out) {
   if (!cfg || !out) return BRUNO_ERR_ARG;
   *out = nullptr;
   if (cfg->k < 3 || cfg->k > 63) return BRUNO_ERR_ARG;
-  if (cfg->edge_filter && cfg->thresholding && (cfg->k > 31 || cfg->direct_count == 1)) return BRUNO_ERR_ARG;
+  if (cfg->edge_filter && cfg->thresholding && cfg->direct_count == 1) return BRUNO_ERR_ARG;
   bruno_ctx *c = new (std::nothrow) bruno_ctx();
   if (!c) return BRUNO_ERR_OOM;
   c->cfg = *cfg;

@@ -60,17 +60,18 @@ typedef struct bruno_cfg {
   int32_t keep_filtered;    /* 1: record the filtered (k+2)-mer entries for copy-out */
   int32_t exact_ranking;    /* 1: always run the round-synchronous ranking; 0: use the O(M)
                                ruling-set ranking whenever the chain map is consistent */
-  int32_t direct_count;     /* counting path for k <= 31: 0 = automatic (hash-partitioned records
-                               counted partition by partition in a cluster's shared memory, or
-                               through L2 when a partition is too large for that), 1 = every
+  int32_t direct_count;     /* counting path: 0 = automatic (hash-partitioned records counted
+                               partition by partition in one CTA's shared memory; a skewed input
+                               that overflows a partition falls back to L2-resident partitions at
+                               k <= 31 and to the whole-table count at k > 31), 1 = every
                                instance straight into the whole table, 2 = the L2 partitions
-                               always.  k > 31 always counts straight into the table. */
+                               always (k <= 31; k > 31 then counts into the whole table). */
   int32_t edge_filter;      /* with thresholding: 1 = the blocked driver's build_index_thresholded
                                (test/test/compact_debruijn_graph_block_construct.cpp:417-470):
                                canonical (k+1)-mers counted (saturating uint16) and kept in
                                [thresh[2], thresh[3]), biedge edges whose (k+1)-mer is gone
                                cleared, pairs left without edges dropped, the rest inserted
-                               unthresholded; k <= 31, not with direct_count = 1.  0 = the
+                               unthresholded; not with direct_count = 1.  0 = the
                                (k+2)-mer count filter (local_insert_by_freqencies). */
   uint64_t h2d_chunk;       /* FASTQ from host memory is copied in pieces of about this many bytes,
                                cut at record starts, and each piece is parsed (and on the k <= 31

@@ -88,8 +88,9 @@ def test_bad_config_rejected_without_gpu(lib):
     h = ctypes.c_void_p()
     assert lib.bruno_ctx_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
     assert lib.bruno_ctx_create(None, ctypes.byref(h)) == 1
-    # the (k+1)-mer edge filter keys are 64-bit (k <= 31) and it runs on the partitioned count
-    for bad in (bg.GraphConfig(k=33, edge_filter=True), bg.GraphConfig(k=31, edge_filter=True, direct_count=1)):
+    # the (k+1)-mer edge filter runs on the partitioned count, not the whole-table one
+    for bad in (bg.GraphConfig(k=45, edge_filter=True, direct_count=1),
+                bg.GraphConfig(k=31, edge_filter=True, direct_count=1)):
         cfg = bad.to_c()
         assert lib.bruno_ctx_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
 

@@ -339,9 +339,33 @@ def test_scatter_split_parity(k, slots, parts):
     compare(got, ref)
 
 
-def test_edge_filter_rejects_large_k():
-    with pytest.raises(bg.BrunoError):
-        bg.Graph(k=33, thresh=bg.thresholds([2]), edge_filter=True)
+@pytest.mark.parametrize("k", [32, 33, 63])
+@pytest.mark.parametrize("fname", ["debruijn.palindrome_chr14.fastq", "debruijn.bubble.fastq", "natural.fastq",
+                                   "natural.withN.fastq"])
+def test_edge_filter_large_k_parity(fname, k):
+    """the (k+1)-mer edge filter at k > 31: 128-bit (k+1)-mers (33..64 bases) in their own table,
+    the filter applied in the partitioned count's extraction"""
+    thr = bg.thresholds([2])
+    data = fixture_bytes(fname)
+    ref = oracle.run(data, k=k, thresh=thr, min_update=True, keep_k2=True, keep_filtered=True, edge_filter=True)
+    compare(gpu_run(data, k, True, thr, True, edge_filter=True), ref)
+    compare_one_call(one_call_run(data, k, True, thr, True, edge_filter=True), ref)
+
+
+def test_edge_filter_large_k_workload_parity():
+    """the 1 Mbp / 100k x 100 bp / 1% workload through the edge filter at k = 45"""
+    w = synth.WORKLOADS["plain-small"]
+    fq = synth.make_fastq(w)
+    thr = bg.thresholds(w.lower)
+    ref = oracle.run(fq, k=45, thresh=thr, min_update=True, threads=16, keep_k2=True, keep_filtered=True,
+                     edge_filter=True)
+    compare(gpu_run(fq, 45, True, thr, True, edge_filter=True), ref)
+
+
+def test_edge_filter_rejects_direct_count():
+    for k in (31, 45):
+        with pytest.raises(bg.BrunoError):
+            bg.Graph(k=k, thresh=bg.thresholds([2]), edge_filter=True, direct_count=1)
 
 
 def test_large_k_mix_parity():
