@@ -82,9 +82,11 @@ typedef struct bruno_cfg {
   int32_t rank_fill;        /* the O(M) ranking's final states: 0 = a second walk of every segment
                                between rulers; 1 = the first walk records each node's place on its
                                segment and one pass over the nodes sets the final states */
-  int32_t part_slots;       /* k <= 31 counting in shared memory: the most slots of one table
-                               partition, which also bounds every probe run (256..3072; 0 = 3072) */
-  int32_t count_threads;    /* threads of a partition's counting block (256, 512 or 1024; 0 = 512) */
+  int32_t part_slots;       /* counting in shared memory: the most 32-byte slots of one table
+                               partition, which also bounds every probe run (256..3072; 0 = 3072;
+                               k > 31 partitions hold half as many 64-byte slots) */
+  int32_t count_threads;    /* threads of a k <= 31 partition's counting block at most (256, 512 or
+                               1024; 0 = 512; blocks of small partitions take fewer, at least 128) */
 } bruno_cfg;
 
 typedef struct bruno_sizes {
