@@ -111,7 +111,7 @@ struct Ctx {
   cudaEvent_t order_ev = nullptr; /* orders the copy stream after the context's stream */
   size_t seg_ev_used = 0;
   size_t host_loads = 0;         /* host buffers loaded since the reset (one device buffer each) */
-  bool h2d_piped = false;        /* this build's copies ran on the copy stream, ending at h2d_end */
+  bool h2d_piped = false;        /* the current graph build's copies ran on the copy stream, ending at h2d_end */
   bool pre_extracted = false;    /* the read index already extracted every segment's reads */
   uint64_t xcap = 0;             /* extraction: bucket capacity, chunk, HLL partial blocks */
   uint32_t xchunk = 1;
@@ -152,7 +152,7 @@ struct Ctx {
   std::vector<uint64_t> h_rank0, h_head0;  /* first listranked node / chain of each sample (S + 1) */
   std::vector<uint64_t> h_iter;            /* ranking rounds per sample */
   Buf records2, sub_cnt;         /* the same records split per table partition */
-  bool h2d_pending = false;      /* ev[7] marks the start of this build's host-to-device copies */
+  bool h2d_pending = false;      /* ev[7] marks the start of the current graph build's host-to-device copies */
   int force_direct_count = 0;    /* cfg.direct_count: 0 automatic, 1 whole table, 2 L2 partitions */
   Buf chain_list, branch_list;   /* slot indices, filled by the filter */
   Buf scan_tmp;                  /* block offsets of the multi-block scan */
