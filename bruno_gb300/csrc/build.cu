@@ -1228,19 +1228,22 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, c
       }
       return false;
     };
-    auto emit = [&](unsigned in5, unsigned out5) {
+    /* the record of the k-mer in the roll with edges (in5, out5): canonical form, mix, bucket */
+    auto make_rec = [&](unsigned in5, unsigned out5, unsigned &bucket) -> typename R::T {
       KT x = roll.f();
       if (!roll.fwd_canonical()) {   /* lex_less: flip the k-mer and reverse-complement the biedge */
         x = roll.r();
         const unsigned ni = out5 ? 5u - out5 : 0u, no = in5 ? 5u - in5 : 0u;
         in5 = ni; out5 = no;
       }
-      unsigned bucket, idx, rho;
+      unsigned idx, rho;
       bool sampled;
       const typename R::T rec = R::make(x, biedge_code(in5, out5), bucket, sampled, idx, rho);
       if (sampled && rho > S.hll[idx]) atomicMax(&S.hll[idx], rho);
       ++inst;
-      if (EF && in5 == 0 && out5 == 0) return;   /* filter_isolated_nodes */
+      return rec;
+    };
+    auto enqueue = [&](const typename R::T &rec, unsigned bucket) {
       const unsigned pos = atomicAdd(&S.cnt[bucket], 1u);
       if (pos < (unsigned)XQT) {
         S.q[bucket][pos] = rec;
@@ -1250,11 +1253,35 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, c
         else S.overflow = 1;
       }
     };
+    auto emit = [&](unsigned in5, unsigned out5) {
+      unsigned bucket;
+      const typename R::T rec = make_rec(in5, out5, bucket);
+      if (EF && in5 == 0 && out5 == 0) return;   /* filter_isolated_nodes */
+      enqueue(rec, bucket);
+    };
     bool ef_in_ok = false;   /* EF: the previous position's (k+1)-mer was kept */
     bool active = next_read();
     for (;;) {
       int emitted = 0;
       while (active && emitted < XROUNDT) {
+        if (!EF && i > (uint32_t)k && i + 2 < L && emitted + 2 <= XROUNDT) {
+          /* two interior k-mers a turn: both records are made before either is queued, so
+           * their mixes interleave */
+          const unsigned b1 = sc.next(), b2 = sc.next();
+          const unsigned c1 = ((b1 >> 1) ^ (b1 >> 2)) & 3u, c2 = ((b2 >> 1) ^ (b2 >> 2)) & 3u;
+          unsigned bk1, bk2;
+          const typename R::T rec1 = make_rec(left + 1u, c1 + 1u, bk1);
+          left = roll.first();
+          roll.push(c1);
+          const typename R::T rec2 = make_rec(left + 1u, c2 + 1u, bk2);
+          left = roll.first();
+          roll.push(c2);
+          i += 2;
+          enqueue(rec1, bk1);
+          enqueue(rec2, bk2);
+          emitted += 2;
+          continue;
+        }
         const unsigned byte = sc.next();
         const unsigned c = ((byte >> 1) ^ (byte >> 2)) & 3u;   /* A0 C1 G2 T3, either case */
         if (i >= (uint32_t)k) {   /* the k-mer ending before base i, its out-base is base i */
