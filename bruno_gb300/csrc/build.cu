@@ -1264,9 +1264,10 @@ __global__ void __launch_bounds__(XTPB, 2) k_extract_s(const uint64_t *rstart, c
     for (;;) {
       int emitted = 0;
       while (active && emitted < XROUNDT) {
-        if (!EF && i > (uint32_t)k && i + 2 < L && emitted + 2 <= XROUNDT) {
+        if (!EF && sizeof(KT) == 8 && i > (uint32_t)k && i + 2 < L && emitted + 2 <= XROUNDT) {
           /* two interior k-mers a turn: both records are made before either is queued, so
-           * their mixes interleave */
+           * their mixes interleave (64-bit keys only: with 128-bit keys the second record's
+           * registers spill and the turn measured slower) */
           const unsigned b1 = sc.next(), b2 = sc.next();
           const unsigned c1 = ((b1 >> 1) ^ (b1 >> 2)) & 3u, c2 = ((b2 >> 1) ^ (b2 >> 2)) & 3u;
           unsigned bk1, bk2;
