@@ -1975,23 +1975,18 @@ __global__ void __launch_bounds__(1024) k_count_local(const uint64_t *recs, cons
       if (q < region) {
         const uint64_t key = sm[q * 4];
         if (key != KEY_EMPTY && !(key & KEY_CONT)) {   /* a continuation belongs to its first slot */
+          /* entries fill in order: the first empty one ends them (most slots hold one or two) */
+          const uint32_t *ew = reinterpret_cast<const uint32_t *>(sm + q * 4 + 1);
           int ne = 0;
           uint32_t kf = 0;
-          #pragma unroll
-          for (int e = 0; e < 6; ++e) {
-            const uint32_t w = (uint32_t)(sm[q * 4 + 1 + e / 2] >> (32 * (e & 1)));
-            ne += w != 0;
-            kf += entry_count(w);
-          }
+          while (ne < 6 && ew[ne] != 0) kf += entry_count(ew[ne++]);
           kf = min(0xFFFFu, kf);
           listed = ne == 6 || kf >= ca.t[2];
           if (!listed) {
             const uint32_t kout = (kf < ca.t[0] || kf >= ca.t[1]) ? 2u : 0u;
-            #pragma unroll
-            for (int e = 0; e < 6; ++e) {
-              const uint32_t w = (uint32_t)(sm[q * 4 + 1 + e / 2] >> (32 * (e & 1)));
-              const uint32_t c16 = min(0xFFFFu, entry_count(w));
-              if (w) qh += 1ull << (16 * (kout | ((c16 < ca.t[4] || c16 >= ca.t[5]) ? 1u : 0u)));
+            for (int e = 0; e < ne; ++e) {
+              const uint32_t c16 = min(0xFFFFu, entry_count(ew[e]));
+              qh += 1ull << (16 * (kout | ((c16 < ca.t[4] || c16 >= ca.t[5]) ? 1u : 0u)));
             }
           }
         }
@@ -2256,23 +2251,18 @@ __global__ void __launch_bounds__(PTPB2, 3) k_count_local2(const unsigned long l
       if (q < region) {
         const uint64_t k0 = sm[q * 8], k1 = sm[q * 8 + 1];
         if (!(k0 == KEY_EMPTY && k1 == KEY_EMPTY) && !(k1 & KEY_CONT)) {
+          /* entries fill in order: the first empty one ends them (most slots hold one or two) */
+          const uint32_t *ew = reinterpret_cast<const uint32_t *>(sm + q * 8 + 2);
           int ne = 0;
           uint32_t kf = 0;
-          #pragma unroll
-          for (int e = 0; e < 12; ++e) {
-            const uint32_t w = (uint32_t)(sm[q * 8 + 2 + e / 2] >> (32 * (e & 1)));
-            ne += w != 0;
-            kf += entry_count(w);
-          }
+          while (ne < 12 && ew[ne] != 0) kf += entry_count(ew[ne++]);
           kf = min(0xFFFFu, kf);
           listed = ne == 12 || kf >= ca.t[2];
           if (!listed) {
             const uint32_t kout = (kf < ca.t[0] || kf >= ca.t[1]) ? 2u : 0u;
-            #pragma unroll
-            for (int e = 0; e < 12; ++e) {
-              const uint32_t w = (uint32_t)(sm[q * 8 + 2 + e / 2] >> (32 * (e & 1)));
-              const uint32_t c16 = min(0xFFFFu, entry_count(w));
-              if (w) qh += 1ull << (16 * (kout | ((c16 < ca.t[4] || c16 >= ca.t[5]) ? 1u : 0u)));
+            for (int e = 0; e < ne; ++e) {
+              const uint32_t c16 = min(0xFFFFu, entry_count(ew[e]));
+              qh += 1ull << (16 * (kout | ((c16 < ca.t[4] || c16 >= ca.t[5]) ? 1u : 0u)));
             }
           }
         }
