@@ -1809,10 +1809,6 @@ __global__ void __launch_bounds__(XTPB, 2) k_split(const uint64_t *records, cons
   if (tid == 0 && S.overflow) atomicOr(&ctr->err, (unsigned long long)DERR_TABLE_FULL);
 }
 
-__device__ __forceinline__ void sm_ld_slot(uint32_t a, uint64_t *raw) {
-  asm volatile("ld.volatile.shared.v2.u64 {%0, %1}, [%2];" : "=l"(raw[0]), "=l"(raw[1]) : "r"(a) : "memory");
-  asm volatile("ld.volatile.shared.v2.u64 {%0, %1}, [%2];" : "=l"(raw[2]), "=l"(raw[3]) : "r"(a + 16) : "memory");
-}
 __device__ __forceinline__ uint64_t sm_cas128(uint32_t a, uint64_t cmp_lo, uint64_t cmp_hi, uint64_t new_lo,
                                               uint64_t new_hi, uint64_t &old_hi) {
   uint64_t olo, ohi;
@@ -1829,29 +1825,39 @@ __device__ __forceinline__ uint64_t sm_cas128(uint32_t a, uint64_t cmp_lo, uint6
   return olo;
 }
 
-/* count_in_entries on a slot in shared memory */
-template <int NE>
-__device__ __forceinline__ bool sm_count_entries(uint32_t *e, const uint32_t *seen, unsigned code,
-                                                 unsigned long long &claims) {
+
+/* one step of count_in_entries on entry word e (snapshot w): claim it if empty, count if it
+ * holds the code; true when the record is counted */
+__device__ __forceinline__ bool sm_entry_step(uint32_t *e, uint32_t w, unsigned code, unsigned long long &claims) {
+  if (w == 0) {
+    const uint32_t old = atomicCAS(e, 0u, (code << E_CODE_SHIFT) | (1u << E_COUNT_SHIFT));
+    if (old == 0) { ++claims; return true; }
+    w = old;
+  }
+  if (entry_code(w) == code) {
+    atomicAdd(e, 1u << E_COUNT_SHIFT);   /* a partition counted here holds fewer than 2^24 records */
+    return true;
+  }
+  return false;
+}
+
+/* count_in_entries over a slot's NE entry words in shared memory, reading them 16 bytes (four
+ * entries) at a time, and a group only when the entries before it did not settle the record
+ * (most k-mers hold one or two edges); `first` are the words already read */
+template <int NE, int FIRST>
+__device__ __forceinline__ bool sm_count_entries_lazy(uint32_t *e, uint32_t e_addr, const uint32_t *first,
+                                                      unsigned code, unsigned long long &claims) {
   #pragma unroll
-  for (int i = 0; i < NE; ++i) {
-    uint32_t w = seen[i];
-    if (w == 0) {
-      const uint32_t nw = (code << E_CODE_SHIFT) | (1u << E_COUNT_SHIFT);
-      const uint32_t old = atomicCAS(e + i, 0u, nw);
-      if (old == 0) { ++claims; return true; }
-      w = old;
-    }
-    if (entry_code(w) == code) {
-      if ((w >> E_COUNT_SHIFT) < (1u << 24) && !(w & E_BIG)) {
-        atomicAdd(e + i, 1u << E_COUNT_SHIFT);   /* result unused: a partition counted here holds
-                                                    fewer than 2^24 records, so this never reaches E_BIG */
-      } else {
-        const uint32_t old = atomicAdd(e + i, 1u << E_COUNT_SHIFT);
-        if (old >> 31) atomicOr(e + i, E_BIG);
-      }
-      return true;
-    }
+  for (int i = 0; i < FIRST; ++i)
+    if (sm_entry_step(e + i, first[i], code, claims)) return true;
+  #pragma unroll
+  for (int g = FIRST; g < NE; g += 4) {
+    uint64_t w0, w1;
+    asm volatile("ld.volatile.shared.v2.u64 {%0, %1}, [%2];" : "=l"(w0), "=l"(w1) : "r"(e_addr + 4u * g) : "memory");
+    const uint32_t s[4] = {(uint32_t)w0, (uint32_t)(w0 >> 32), (uint32_t)w1, (uint32_t)(w1 >> 32)};
+    #pragma unroll
+    for (int i = 0; i < 4; ++i)
+      if (g + i < NE && sm_entry_step(e + g + i, s[i], code, claims)) return true;
   }
   return false;
 }
@@ -1863,25 +1869,23 @@ __device__ __forceinline__ bool sm_count(uint64_t *sm, uint32_t sm_base, uint32_
   bool seen_primary = false;
   uint32_t j = home;
   for (uint32_t probe = 0; probe < region; ++probe) {
-    uint64_t raw[4];
-    sm_ld_slot(sm_base + j * 32u, raw);
-    uint64_t key = raw[0];
-    uint32_t seen[6];
-    #pragma unroll
-    for (int q = 0; q < 6; ++q) seen[q] = (uint32_t)(raw[1 + q / 2] >> (32 * (q & 1)));
+    const uint32_t a = sm_base + j * 32u;
+    uint64_t key, w01;   /* the key and entries 0-1; entries 2-5 only if these do not settle it */
+    asm volatile("ld.volatile.shared.v2.u64 {%0, %1}, [%2];" : "=l"(key), "=l"(w01) : "r"(a) : "memory");
     const uint64_t want = h | (seen_primary ? KEY_CONT : 0);
     if (key == KEY_EMPTY) {
       const uint64_t ne0 = (uint64_t)((code << E_CODE_SHIFT) | (1u << E_COUNT_SHIFT));
       uint64_t ohi;
-      const uint64_t olo = sm_cas128(sm_base + j * 32u, KEY_EMPTY, 0ull, want, ne0, ohi);
+      const uint64_t olo = sm_cas128(a, KEY_EMPTY, 0ull, want, ne0, ohi);
       if (olo == KEY_EMPTY && ohi == 0) { ++slot_claims; ++entry_claims; return true; }
       key = olo;
-      seen[0] = (uint32_t)ohi;
-      seen[1] = (uint32_t)(ohi >> 32);
+      w01 = ohi;
     }
     if (key == want) {
       seen_primary = true;
-      if (sm_count_entries<6>((uint32_t *)(sm + (uint64_t)j * 4 + 1), seen, code, entry_claims)) return true;
+      const uint32_t first[2] = {(uint32_t)w01, (uint32_t)(w01 >> 32)};
+      if (sm_count_entries_lazy<6, 2>((uint32_t *)(sm + (uint64_t)j * 4 + 1), a + 8u, first, code, entry_claims))
+        return true;
     }
     j = (j + 1 == region) ? 0u : j + 1;
   }
@@ -2168,30 +2172,16 @@ __device__ __forceinline__ bool sm_count2(uint64_t *sm, uint32_t sm_base, uint32
     uint64_t k0, k1;
     asm volatile("ld.volatile.shared.v2.u64 {%0, %1}, [%2];" : "=l"(k0), "=l"(k1) : "r"(a) : "memory");
     const uint64_t whi = hi | (seen_primary ? KEY_CONT : 0);
-    uint32_t seen[12];
-    bool fresh = false;
     if (k0 == KEY_EMPTY && k1 == KEY_EMPTY) {
       uint64_t ohi;
       const uint64_t olo = sm_cas128(a, KEY_EMPTY, KEY_EMPTY, lo, whi, ohi);
-      if (olo == KEY_EMPTY && ohi == KEY_EMPTY) { ++slot_claims; k0 = lo; k1 = whi; fresh = true; }
+      if (olo == KEY_EMPTY && ohi == KEY_EMPTY) { ++slot_claims; k0 = lo; k1 = whi; }
       else { k0 = olo; k1 = ohi; }
     }
-    if (k0 == lo && k1 == whi) {
+    if (k0 == lo && k1 == whi) {   /* the entries, four at a time as far as they are needed */
       seen_primary = true;
-      if (fresh) {   /* a slot just claimed has no entries yet */
-        #pragma unroll
-        for (int q = 0; q < 12; ++q) seen[q] = 0;
-      } else {
-        #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          uint64_t w0, w1;
-          asm volatile("ld.volatile.shared.v2.u64 {%0, %1}, [%2];" : "=l"(w0), "=l"(w1) : "r"(a + 16u + 16u * q)
-                       : "memory");
-          seen[4 * q] = (uint32_t)w0; seen[4 * q + 1] = (uint32_t)(w0 >> 32);
-          seen[4 * q + 2] = (uint32_t)w1; seen[4 * q + 3] = (uint32_t)(w1 >> 32);
-        }
-      }
-      if (sm_count_entries<12>((uint32_t *)(sm + (uint64_t)j * 8 + 2), seen, code, entry_claims)) return true;
+      if (sm_count_entries_lazy<12, 0>((uint32_t *)(sm + (uint64_t)j * 8 + 2), a + 16u, nullptr, code, entry_claims))
+        return true;
     }
     j = (j + 1 == region) ? 0u : j + 1;
   }
