@@ -75,8 +75,14 @@ __device__ __forceinline__ uint32_t block_exscan(uint32_t v, uint32_t &total) {
 
 /* ============================================================ FASTQ splitting */
 
-/* per 4 bytes: 0xFF in every byte equal to c (SIMD compare) */
-__device__ __forceinline__ uint32_t bytes_eq(uint32_t w, uint32_t c4) { return __vcmpeq4(w, c4); }
+/* per 4 bytes: 0x80 in every byte of w equal to that byte of c4, 0 elsewhere.  x = w ^ c4 is
+ * zero exactly in those bytes; (x & 0x7F) + 0x7F keeps a byte's top bit clear only when its low
+ * seven bits are zero and never carries into the next byte, and or-ing x itself in rules out
+ * 0x80. */
+__device__ __forceinline__ uint32_t bytes_eq(uint32_t w, uint32_t c4) {
+  const uint32_t x = w ^ c4;
+  return ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x | 0x7F7F7F7Fu);
+}
 
 /* 16 bytes at p (16-byte aligned if `aligned`, bounds-checked against n) as 4 words */
 __device__ __forceinline__ uint4 load16(const unsigned char *buf, uint64_t p, uint64_t n, bool aligned) {
@@ -88,43 +94,47 @@ __device__ __forceinline__ uint4 load16(const unsigned char *buf, uint64_t p, ui
 }
 
 /* newline count and last non-whitespace byte of each tile (16 bytes per thread-load) */
-__global__ void __launch_bounds__(TPB) k_tile_stats(const unsigned char *buf, uint64_t n, uint64_t *tile_cnt,
+__global__ void __launch_bounds__(TPB, 8) k_tile_stats(const unsigned char *buf, uint64_t n, uint64_t *tile_cnt,
                                                      DevCounters *ctr, bool aligned) {
   const uint64_t t0 = (uint64_t)blockIdx.x * TILE;
   const uint64_t t1 = (n < t0 + TILE ? n : t0 + TILE);
-  unsigned long long cnt = 0;
-  long long lastnw = -1;
+  const uint32_t tl = (uint32_t)(t1 - t0);   /* the tile's bytes; offsets below are in the tile */
+  uint32_t cnt = 0;
+  int last = -1;   /* offset of the thread's last non-whitespace byte */
   /* four 16-byte loads in flight per thread, then their bytes */
-  for (uint64_t p0 = t0 + 16ull * threadIdx.x; p0 < t1; p0 += 64ull * TPB) {
+  for (uint32_t o0 = 16u * threadIdx.x; o0 < tl; o0 += 64u * TPB) {
     uint4 v[4];
     #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const uint64_t p = p0 + 16ull * TPB * u;
-      v[u] = p < t1 ? load16(buf, p, t1, aligned) : make_uint4(0u, 0u, 0u, 0u);
+      const uint32_t o = o0 + 16u * TPB * u;
+      v[u] = o < tl ? load16(buf, t0 + o, t1, aligned) : make_uint4(0u, 0u, 0u, 0u);
     }
     #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const uint64_t p = p0 + 16ull * TPB * u;
-      if (p >= t1) continue;
+      const uint32_t o = o0 + 16u * TPB * u;
+      if (o >= tl) continue;
       const uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
       #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const uint32_t nl = bytes_eq(w[q], 0x0A0A0A0Au), cr = bytes_eq(w[q], 0x0D0D0D0Du);
-        cnt += __popc(nl) >> 3;
-        uint32_t keep = ~(nl | cr);
-        /* bytes beyond the tile end are zero padding, not data */
-        const uint64_t base = p + 4 * q;
-        if (base >= t1) keep = 0;
-        else if (base + 4 > t1) keep &= (1u << (8 * (t1 - base))) - 1u;
-        if (keep) lastnw = max(lastnw, (long long)(base + ((31 - __clz(keep)) >> 3)));
+        cnt += __popc(nl);
+        uint32_t keep = ~(nl | cr) & 0x80808080u;
+        const uint32_t base = o + 4u * q;
+        if (o + 16u > tl) {   /* the tile's ragged end: bytes past it are zero padding, not data */
+          if (base >= tl) keep = 0;
+          else if (base + 4u > tl) keep &= (1u << (8 * (tl - base))) - 1u;
+        }
+        /* a thread visits its bytes in increasing order, so the last hit is its largest */
+        if (keep) last = (int)(base + ((31 - __clz(keep)) >> 3));
       }
     }
   }
+  long long lastnw = last >= 0 ? (long long)(t0 + (uint32_t)last) : -1ll;
   __shared__ unsigned long long sc[TPB / 32];
   __shared__ long long sl[TPB / 32];
-  cnt = warp_sum(cnt);
+  const unsigned long long wcnt = warp_sum((unsigned long long)cnt);
   for (int o = 16; o > 0; o >>= 1) lastnw = max(lastnw, __shfl_down_sync(~0u, lastnw, o));
-  if ((threadIdx.x & 31) == 0) { sc[threadIdx.x >> 5] = cnt; sl[threadIdx.x >> 5] = lastnw; }
+  if ((threadIdx.x & 31) == 0) { sc[threadIdx.x >> 5] = wcnt; sl[threadIdx.x >> 5] = lastnw; }
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned long long c = 0; long long l = -1;
@@ -162,9 +172,10 @@ __global__ void __launch_bounds__(TPB) k_index_lines(const unsigned char *buf, u
       const uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
       #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const uint32_t nl = bytes_eq(w[q], 0x0A0A0A0Au);   /* 0xFF per newline byte */
-        #pragma unroll
-        for (int b = 0; b < 4; ++b) m |= (uint64_t)((nl >> (8 * b + 7)) & 1u) << (16 * u + 4 * q + b);
+        const uint32_t nl = bytes_eq(w[q], 0x0A0A0A0Au) >> 7;   /* bit 8b per newline byte b */
+        /* bits 0, 8, 16, 24 times 1 + 2^7 + 2^14 + 2^21 land on bits 21..24, and no two of the
+         * sixteen products share a bit, so nothing carries into them */
+        m |= (uint64_t)(((nl * 0x00204081u) >> 21) & 0xFu) << (16 * u + 4 * q);
       }
     }
     uint32_t total;
@@ -1731,14 +1742,16 @@ __global__ void __launch_bounds__(XTPB, 2) k_split(const uint64_t *records, cons
     const int sbits = G.g.pbits - NBUCKET_BITS, nq = 1 << sbits;
     const uint64_t *rb = records + X.rec_base + (uint64_t)b * X.cap;
     const int shift = 5 + LOW_BITS - sbits;
+    /* a round's records: every load of the round is in flight before the first use, and each
+     * round after the first is loaded while the round before it is written out */
+    uint64_t recs[SPLIT_ROUND];
+    #pragma unroll
+    for (int j = 0; j < SPLIT_ROUND; ++j) {
+      const uint64_t i = item.lo + (uint64_t)j * XTPB + tid;
+      recs[j] = i < item.hi ? __ldcs(rb + i) : 0ull;
+    }
     for (uint64_t r0 = item.lo; r0 < item.hi; r0 += SPLIT_REC) {
-      uint64_t recs[SPLIT_ROUND];   /* every load of the round is in flight before the first use */
       uint32_t pos[SPLIT_ROUND];    /* partition << 16 | rank in it; ~0 past the end */
-      #pragma unroll
-      for (int j = 0; j < SPLIT_ROUND; ++j) {
-        const uint64_t i = r0 + (uint64_t)j * XTPB + tid;
-        recs[j] = i < item.hi ? __ldcs(rb + i) : 0ull;
-      }
       #pragma unroll
       for (int j = 0; j < SPLIT_ROUND; ++j) {
         const uint64_t i = r0 + (uint64_t)j * XTPB + tid;
@@ -1795,6 +1808,13 @@ __global__ void __launch_bounds__(XTPB, 2) k_split(const uint64_t *records, cons
       for (int j = 0; j < SPLIT_ROUND; ++j)
         if (pos[j] != ~0u) S.buf[S.start[pos[j] >> 16] + (pos[j] & 0xFFFFu)] = recs[j];
       __syncthreads();
+      if (r0 + SPLIT_REC < item.hi) {
+        #pragma unroll
+        for (int j = 0; j < SPLIT_ROUND; ++j) {
+          const uint64_t i = r0 + SPLIT_REC + (uint64_t)j * XTPB + tid;
+          recs[j] = i < item.hi ? __ldcs(rb + i) : 0ull;
+        }
+      }
       const unsigned nr = S.wsum_total;   /* the round's records, holes left out */
       for (unsigned y = tid; y < nr; y += XTPB) {
         const uint64_t rec = S.buf[y];
