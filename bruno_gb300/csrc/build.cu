@@ -84,12 +84,13 @@ __device__ __forceinline__ uint32_t bytes_eq(uint32_t w, uint32_t c4) {
   return ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x | 0x7F7F7F7Fu);
 }
 
-/* 16 bytes at p (16-byte aligned if `aligned`, bounds-checked against n) as 4 words */
+/* 16 bytes at p (16-byte aligned if `aligned`, bounds-checked against n) as 4 words; a byte at
+ * or past n reads as a carriage return, which the line scans skip as whitespace */
 __device__ __forceinline__ uint4 load16(const unsigned char *buf, uint64_t p, uint64_t n, bool aligned) {
   if (aligned && p + 16 <= n) return *(const uint4 *)(buf + p);
   uint32_t w[4] = {0, 0, 0, 0};
   for (int i = 0; i < 16; ++i)
-    if (p + i < n) w[i >> 2] |= (uint32_t)buf[p + i] << (8 * (i & 3));
+    w[i >> 2] |= (uint32_t)(p + i < n ? buf[p + i] : (unsigned char)'\r') << (8 * (i & 3));
   return make_uint4(w[0], w[1], w[2], w[3]);
 }
 
@@ -99,8 +100,11 @@ __global__ void __launch_bounds__(TPB, 8) k_tile_stats(const unsigned char *buf,
   const uint64_t t0 = (uint64_t)blockIdx.x * TILE;
   const uint64_t t1 = (n < t0 + TILE ? n : t0 + TILE);
   const uint32_t tl = (uint32_t)(t1 - t0);   /* the tile's bytes; offsets below are in the tile */
-  uint32_t cnt = 0;
-  int last = -1;   /* offset of the thread's last non-whitespace byte */
+  /* newlines counted per byte lane of one word: a thread reads TILE / TPB bytes, so no lane
+   * passes 255 */
+  static_assert(TILE / TPB / 4 <= 255, "newline lane counts must fit a byte");
+  uint32_t lanes = 0;
+  uint32_t last_word = 0, last_keep = 0;   /* the thread's last word holding non-whitespace */
   /* four 16-byte loads in flight per thread, then their bytes */
   for (uint32_t o0 = 16u * threadIdx.x; o0 < tl; o0 += 64u * TPB) {
     uint4 v[4];
@@ -116,20 +120,17 @@ __global__ void __launch_bounds__(TPB, 8) k_tile_stats(const unsigned char *buf,
       const uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
       #pragma unroll
       for (int q = 0; q < 4; ++q) {
+        /* bytes past the tile's end read as carriage returns: neither counted nor kept */
         const uint32_t nl = bytes_eq(w[q], 0x0A0A0A0Au), cr = bytes_eq(w[q], 0x0D0D0D0Du);
-        cnt += __popc(nl);
-        uint32_t keep = ~(nl | cr) & 0x80808080u;
-        const uint32_t base = o + 4u * q;
-        if (o + 16u > tl) {   /* the tile's ragged end: bytes past it are zero padding, not data */
-          if (base >= tl) keep = 0;
-          else if (base + 4u > tl) keep &= (1u << (8 * (tl - base))) - 1u;
-        }
-        /* a thread visits its bytes in increasing order, so the last hit is its largest */
-        if (keep) last = (int)(base + ((31 - __clz(keep)) >> 3));
+        lanes += nl >> 7;
+        const uint32_t keep = ~(nl | cr) & 0x80808080u;
+        /* a thread visits its bytes in increasing order, so its last hit is its largest */
+        if (keep) { last_word = o + 4u * q; last_keep = keep; }
       }
     }
   }
-  long long lastnw = last >= 0 ? (long long)(t0 + (uint32_t)last) : -1ll;
+  const uint32_t cnt = (lanes & 0xFFu) + ((lanes >> 8) & 0xFFu) + ((lanes >> 16) & 0xFFu) + (lanes >> 24);
+  long long lastnw = last_keep ? (long long)(t0 + last_word + ((31 - __clz(last_keep)) >> 3)) : -1ll;
   __shared__ unsigned long long sc[TPB / 32];
   __shared__ long long sl[TPB / 32];
   const unsigned long long wcnt = warp_sum((unsigned long long)cnt);
