@@ -22,9 +22,10 @@
  * that still runs out of device memory is queued again, once, to run with no other build busy,
  * and no other request starts until it has finished.
  *
- * The batched mode (bruno_pool_create_batched) replaces the workers by one scheduler that runs
- * continuous batching over the fused form: every pass takes the queued requests that fit the
- * budget and builds them together in one pass of every kernel (bruno_build_samples).
+ * The batched mode (bruno_pool_create_batched) replaces the workers by two schedulers that run
+ * continuous batching over the fused form: every pass takes the queued requests that fit its
+ * scheduler's share of the budget and builds them together in one pass of every kernel
+ * (bruno_build_samples).
  */
 #include <cuda_runtime.h>
 
@@ -194,15 +195,13 @@ void take_sample(bruno_ctx *ctx, size_t i, int words, bruno_pool_result &r) {
   r.n_chars = nch;
 }
 
-/* Continuous batching: the scheduler takes every queued request that fits the memory budget
- * (at least one, at most max_samples), builds them in one fused pass (bruno_build_samples), and
- * hands out each request's results; requests that arrive during a pass wait for the next one.
+/* Continuous batching: a scheduler takes every queued request that fits its share of the memory
+ * budget (at least one, at most max_samples), builds them in one fused pass (bruno_build_samples),
+ * and hands out each request's results; requests that arrive during a pass wait for the next one.
  * Where the fused pass cannot run (a configuration the batched form refuses, or an error), each
  * request of the pass is built on its own with the plain path, so every result is always the
- * plain path's. */
-/* Scheduler w of the continuous-batching pool: its own context, passes of at most the budget's
- * share of one scheduler.  With two schedulers one pass's host work (the copies in, every
- * request's results out) runs beside the other pass's kernels. */
+ * plain path's.  Scheduler w has its own context; with two schedulers one pass's host work (the
+ * copies in, every request's results out) runs beside the other pass's kernels. */
 void batch_main(bruno_pool *p, int w) {
   bruno_ctx *ctx = nullptr;
   const int words = p->cfg.k <= 31 ? 1 : 2;
