@@ -196,7 +196,7 @@ def run_reference(args, w):
     value = statistics.mean(vals)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(secs), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded generator)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded generator, " + w.name + ")",
             "config": workload_config(w), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": b["sample"],
                              "phases_s": b["phases_s"]},
