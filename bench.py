@@ -166,17 +166,22 @@ class ClockSampler:
 
 
 def cpu_baseline(w, frac, threads):
-    """the oracle on the first `frac` of the workload's reads, all host threads"""
+    """the oracle on the first `frac` of the workload's reads, all host threads.  The time is
+    the sum of the oracle's six path phases (parse through compression, the steps the GPU step
+    runs); the exports the oracle adds for the parity tests (sorted node, chain-map and k2
+    copies, chain edges and summaries, the check_index tally) are left out of it."""
     from bruno_gb300 import synth, thresholds
     from oracle import oracle
     ws = w.scaled(frac)
     fq = synth.make_fastq(ws)
     t0 = time.perf_counter()
     r = oracle.run(fq, k=w.k, thresh=thresholds(w.lower), min_update=True, threads=threads)
-    dt = time.perf_counter() - t0
+    wall = time.perf_counter() - t0
+    dt = sum(r["seconds"].values())
     return {"value": r["n_instances"] / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"first {ws.n_reads} of {w.n_reads} reads ({frac * 100:g}%), {r['n_instances']} k-mers, "
-                      f"{dt:.2f} s", "seconds": dt, "instances": r["n_instances"],
+                      f"{dt:.2f} s in the six path phases ({wall:.2f} s with the oracle's test-only exports)",
+            "seconds": dt, "instances": r["n_instances"],
             "phases_s": {p: round(t, 4) for p, t in r["seconds"].items()}}
 
 
