@@ -64,3 +64,33 @@ def test_reference_arm_other_ranks_exit_without_work(monkeypatch, capsys):
         cpu_sample, warmup, steps, gpus = 0.01, 1, 1, 2
     bench.run_reference(Args(), synth.WORKLOADS["plain-small"])
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    """rank 0 prints one reference line on the arm's own config: the oracle's rate over its six
+    path phases, the same figure as its cpu_baseline and its e2e (no device copies)"""
+    import json
+    import bench
+    from bruno_gb300 import synth
+    monkeypatch.setenv("RANK", "0")
+    monkeypatch.setenv("WORLD_SIZE", "1")
+    w = synth.WORKLOADS["plain-small"]
+
+    class Args:
+        ref_sample, warmup, steps, gpus = 0.5, 0, 1, 1
+    bench.run_reference(Args(), w)
+    lines = capsys.readouterr().out.strip().splitlines()
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
+    assert line["config"] == bench.workload_config(w)
+    assert line["data"] == "synthetic (seeded generator, plain-small)"
+    assert line["higher_is_better"] is True and line["steps"] == 1 and line["warmup"] == 0
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    cb = line["cpu_baseline"]
+    assert cb["value"] == line["value"] and cb["kind"] == "port" and cb["cores"] >= 1
+    assert set(cb["phases_s"]) == {"parse", "count_k2mers", "filter_insert", "chainmap", "list_rank", "compress"}
+    # the step time is the six phases' sum (they are rounded to 0.1 ms in the line)
+    assert abs(line["ms_per_step"] - 1e3 * sum(cb["phases_s"].values())) < 1.0
+    assert "first 50000 of 100000 reads (50%)" in cb["sample"]
